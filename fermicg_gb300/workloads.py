@@ -1,0 +1,185 @@
+"""Seeded synthetic problems shaped like the benchmark configurations.
+
+A problem is: integrals -> consecutive clusters -> local eigenbases (M lowest
+per Fock sector) -> cluster operators (TDMs) -> clustered Hamiltonian ->
+a variational TPS space.
+
+The variational space stands in for a converged TPSCI selection: it is the
+set of the `n_cfg` lowest configurations by the sum of local energies
+(sum_c e_c(sector_c, state_c)) over all global Fock sectors with the right
+electron count (a deterministic, energy-ordered product space).  Sectors
+are inserted in order of their lowest configuration, configurations within a
+sector in increasing energy.
+"""
+from __future__ import annotations
+
+import heapq
+import itertools
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .integrals import InCoreInts, synthetic_integrals
+from .local_fci import compute_cluster_eigenbasis, compute_cluster_ops, add_cmf_operators
+from .state import TPSCIstate
+from .terms import extract_ClusteredTerms
+
+
+@dataclass
+class Problem:
+    ints: InCoreInts
+    clusters: list
+    init_fspace: list
+    bases: list
+    ops: list
+    ham: object
+    meta: dict = field(default_factory=dict)
+
+
+def consecutive_clusters(norb, sizes):
+    out, p = [], 0
+    for s in sizes:
+        out.append(list(range(p, p + s)))
+        p += s
+    assert p == norb
+    return out
+
+
+def build_problem(norb, cluster_sizes, init_fspace, n_chol, seed, max_roots, delta_elec=None,
+                  cmf=True):
+    """Integrals, bases, TDMs and clustered H for one synthetic system."""
+    ints = synthetic_integrals(norb, n_chol, seed)
+    clusters = consecutive_clusters(norb, cluster_sizes)
+    bases = compute_cluster_eigenbasis(ints, clusters, init_fspace=init_fspace,
+                                       delta_elec=delta_elec, max_roots=max_roots)
+    ops = compute_cluster_ops(bases, ints)
+    if cmf:
+        da, db = reference_density(bases, clusters, init_fspace, norb)
+        add_cmf_operators(ops, bases, ints, da, db)
+    ham = extract_ClusteredTerms(ints, clusters)
+    return Problem(ints, clusters, list(init_fspace), bases, ops, ham,
+                   dict(norb=norb, cluster_sizes=list(cluster_sizes), n_chol=n_chol, seed=seed,
+                        max_roots=max_roots, delta_elec=delta_elec))
+
+
+def reference_density(bases, clusters, init_fspace, norb):
+    """Block-diagonal alpha/beta 1-RDMs of the product of local ground states
+    in the reference sectors (the mean field a CMF embedding uses)."""
+    da = np.zeros((norb, norb))
+    db = np.zeros((norb, norb))
+    for cb, orbs, f in zip(bases, clusters, init_fspace):
+        sp = cb.space
+        v = cb.basis[tuple(f)][:, 0]
+        for spin, d in ((0, da), (1, db)):
+            r = sp.op_matrices("Aa" if spin == 0 else "Bb", *f)
+            if r is None:
+                continue
+            g = np.einsum("i,pqij,j->pq", v, r[1], v)
+            d[np.ix_(orbs, orbs)] = g
+    return da, db
+
+
+def _local_energy_tables(bases):
+    return [{sec: np.asarray(e) for sec, e in cb.energies.items()} for cb in bases]
+
+
+def energy_ordered_space(prob: Problem, n_cfg: int, R: int = 1, seed: int = 0):
+    """The n_cfg lowest configurations by summed local energy (see module doc).
+
+    Coefficients are seeded N(0,1), rows normalised per root."""
+    N = len(prob.clusters)
+    na_tot = sum(f[0] for f in prob.init_fspace)
+    nb_tot = sum(f[1] for f in prob.init_fspace)
+    et = _local_energy_tables(prob.bases)
+    # global sectors with the right electron count
+    secs = [sorted(b.basis.keys()) for b in prob.bases]
+    gsecs = []
+
+    def rec(c, cur, na, nb):
+        if c == N:
+            if na == na_tot and nb == nb_tot:
+                gsecs.append(tuple(cur))
+            return
+        for s in secs[c]:
+            cur.append(s)
+            rec(c + 1, cur, na + s[0], nb + s[1])
+            cur.pop()
+
+    rec(0, [], 0, 0)
+    # lazy k-best merge over sectors: per sector a best-first enumeration of state tuples
+    heap = []
+    gens = []
+    for gi, fs in enumerate(gsecs):
+        es = [et[c][fs[c]] for c in range(N)]
+        e0 = sum(float(e[0]) for e in es)
+        gens.append((fs, es))
+        heapq.heappush(heap, (e0, gi, (0,) * N))
+    seen = set((gi, (0,) * N) for gi in range(len(gsecs)))
+    chosen = []
+    while heap and len(chosen) < n_cfg:
+        e, gi, st = heapq.heappop(heap)
+        chosen.append((e, gi, st))
+        fs, es = gens[gi]
+        for c in range(N):
+            if st[c] + 1 < len(es[c]):
+                nst = st[:c] + (st[c] + 1,) + st[c + 1:]
+                if (gi, nst) in seen:
+                    continue
+                seen.add((gi, nst))
+                ne = e - float(es[c][st[c]]) + float(es[c][st[c] + 1])
+                heapq.heappush(heap, (ne, gi, nst))
+    # group by sector; sector order = order of first appearance
+    order = []
+    by = {}
+    for e, gi, st in chosen:
+        if gi not in by:
+            by[gi] = []
+            order.append(gi)
+        by[gi].append(st)
+    rng = np.random.default_rng(seed)
+    state = TPSCIstate(N, R)
+    coeffs = rng.standard_normal((len(chosen), R))
+    coeffs /= np.linalg.norm(coeffs, axis=0, keepdims=True)
+    i = 0
+    for gi in order:
+        fs = gsecs[gi]
+        state.add_fockconfig(fs)
+        for st in by[gi]:
+            state.data[fs][st] = coeffs[i].copy()
+            i += 1
+    return state
+
+
+def full_space(prob: Problem, R: int = 1, seed: int = 0):
+    """Every configuration of the right electron count (full TPS space)."""
+    N = len(prob.clusters)
+    na_tot = sum(f[0] for f in prob.init_fspace)
+    nb_tot = sum(f[1] for f in prob.init_fspace)
+    secs = [sorted(b.basis.keys()) for b in prob.bases]
+    state = TPSCIstate(N, R)
+    for fs in itertools.product(*secs):
+        if sum(f[0] for f in fs) != na_tot or sum(f[1] for f in fs) != nb_tot:
+            continue
+        dims = [prob.bases[c].basis[fs[c]].shape[1] for c in range(N)]
+        state.add_fockconfig(fs)
+        for st in itertools.product(*[range(d) for d in dims]):
+            state.data[fs][st] = np.zeros(R)
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((len(state), R))
+    v /= np.linalg.norm(v, axis=0, keepdims=True)
+    state.set_vector(v)
+    return state
+
+
+# ---- named workloads -------------------------------------------------------------
+
+def config0_problem(seed=0):
+    """12 orbitals, 6a/6b, 4 clusters x 3, K=36, full local FCI per sector."""
+    return build_problem(12, [3, 3, 3, 3], [(2, 1), (1, 2), (2, 1), (1, 2)], 36, seed,
+                         max_roots=1000)
+
+
+def config1_problem(seed=0):
+    """24 orbitals, 12a/12b, 6 clusters x 4, K=72, M=16 per sector within 2 electrons
+    of (2,2)."""
+    return build_problem(24, [4] * 6, [(2, 2)] * 6, 72, seed, max_roots=16, delta_elec=2)
