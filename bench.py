@@ -1,0 +1,276 @@
+"""Benchmark: TPSCI closed sigma builds/s (tps_ci_matvec) on one GB300, mixed vs FP64.
+
+Workload: 24 orbitals / 24 electrons, 6 clusters x 4 orbitals, K=72 seeded Cholesky
+integrals, M=16 lowest local states per Fock sector (sectors within 2 electrons of
+(2,2)), an energy-ordered variational space of 100,000 TPS configurations, 4 roots.
+A step is one sigma build sigma = H C over that space.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`value` is device-resident throughput (inputs in HBM, L2 flushed between steps);
+`e2e` goes through the C ABI with pinned host buffers (H2D of C and D2H of sigma
+inside the timed region).  The reference arm times the CPU oracle (a restatement
+of the reference's Julia loops) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TPSCI sigma builds/s (mixed FP32 vs FP64), config 24o/6 clusters/1e5 TPS configs/4 roots"
+WORKLOAD = "tpsci_closed_sigma_24o_6x4_M16_1e5cfg_R4"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n-cfg", type=int, default=100000)
+    ap.add_argument("--roots", type=int, default=4)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+def build_workload(n_cfg, R):
+    from fermicg_gb300 import pack, workloads
+    prob = workloads.config1_problem(seed=0)
+    st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=0)
+    po, pt = pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham)
+    f, c, v, _ = pack.pack_state(st)
+    return prob, st, po, pt, f, c, v
+
+
+def cpu_reference(po, pt, f, c, v, budget_s, threads):
+    """Time the oracle's tps_ci_matvec restatement on a growing bra-row sample; returns
+    (sigma builds/s extrapolated to the full space, sample description)."""
+    import oracle
+    O = oracle.Oracle(po, pt)
+    n = f.shape[0]
+    rows = 64
+    rng_rows = np.random.default_rng(1).permutation(n)
+    # contiguous blocks of rows are what the reference's per-bra jobs see; sample evenly spaced blocks
+    while True:
+        t0 = time.perf_counter()
+        done = 0
+        nblk = 8
+        for b in range(nblk):
+            s0 = int(rng_rows[b] // rows * rows) % max(n - rows, 1)
+            O.sigma_closed(f, c, v, rows=(s0, s0 + rows // nblk), n_threads=threads)
+            done += rows // nblk
+        dt = time.perf_counter() - t0
+        if dt > budget_s / 4 or rows >= n:
+            break
+        rows = min(n, rows * 4)
+    per_row = dt / done
+    return 1.0 / (per_row * n), f"{done} of {n} bra rows (8 blocks), {dt:.1f} s, extrapolated"
+
+
+def clocks_sampler():
+    out = []
+    stop = threading.Event()
+
+    def run():
+        try:
+            p = subprocess.Popen(["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                                  "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                                  "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                                  "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            return
+        while not stop.is_set():
+            line = p.stdout.readline()
+            if not line:
+                break
+            out.append(line.strip())
+        p.terminate()
+
+    th = threading.Thread(target=run, daemon=True)
+    th.start()
+
+    def finish():
+        stop.set()
+        th.join(timeout=2)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in out:
+            parts = [x.strip() for x in l.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower() in ("active", "1"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+    return finish
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        if rank != 0:
+            return
+        prob, st, po, pt, f, c, v = build_workload(a.n_cfg, a.roots)
+        threads = os.cpu_count() or 1
+        vals = []
+        for i in range(a.warmup + a.steps):
+            val, sample = cpu_reference(po, pt, f, c, v, a.cpu_seconds / max(a.steps, 1), threads)
+            if i >= a.warmup:
+                vals.append(val)
+        value = statistics.median(vals)
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": value, "unit": "sigma_builds/s", "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "n_cfg": int(f.shape[0]), "roots": a.roots},
+            "cpu_baseline": {"value": value, "unit": "sigma_builds/s", "cores": threads, "kind": "port",
+                             "sample": sample + "; restatement of tps_ci_matvec (Julia not available)"},
+            "e2e": {"value": value, "unit": "sigma_builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+    from fermicg_gb300 import build as fbuild
+    from fermicg_gb300.gpu import GpuSigma
+
+    fbuild.build()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    prob, st, po, pt, f, c, v = build_workload(a.n_cfg, a.roots)
+    n, R = v.shape
+    g = GpuSigma(local)
+    g.set_ops(po)
+    g.set_terms(pt)
+    g.state_set(f, c)
+    stream = torch.cuda.current_stream()
+    g.set_stream(stream.cuda_stream)
+    stats = g.stats()
+
+    d_c = torch.from_numpy(np.asfortranarray(v).T.copy()).cuda()  # (R, n) contiguous == column-major (n, R)
+    d_s = torch.empty_like(d_c)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, prec)
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        tot = 0.0
+        kern = []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, prec)
+            e1.record(stream)
+            e1.synchronize()
+            tot += e0.elapsed_time(e1)
+            kern.append(g.stats()["last_kernel_ms"])
+        torch.cuda.synchronize()
+        return tot / steps, statistics.median(kern)
+
+    finish = clocks_sampler()
+    ms32, k32 = timed("fp32", a.steps, a.warmup)
+    ms64, k64 = timed("fp64", max(3, a.steps // 4), a.warmup)
+    clocks = finish()
+    sig32 = d_s.clone()
+    g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp64")
+    torch.cuda.synchronize()
+    rel32 = float((sig32 - d_s).abs().max() / d_s.abs().max())
+
+    # end to end through the C ABI with pinned host buffers
+    h_c = torch.from_numpy(np.asfortranarray(v).T.copy()).pin_memory()
+    h_s = torch.empty_like(h_c).pin_memory()
+    import ctypes
+    L = g.L
+    for _ in range(a.warmup):
+        L.fcg_sigma_closed(g.h, R, ctypes.c_void_p(h_c.data_ptr()), ctypes.c_void_p(h_s.data_ptr()), 1)
+    # per-step wall time of the C-ABI call (H2D of C, sigma, D2H of sigma)
+    walls = []
+    for _ in range(a.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        L.fcg_sigma_closed(g.h, R, ctypes.c_void_p(h_c.data_ptr()), ctypes.c_void_p(h_s.data_ptr()), 1)
+        walls.append(time.perf_counter() - t1)
+    e2e_ms = 1e3 * statistics.mean(walls)
+
+    value = world * 1e3 / ms32
+    # algorithmic (compulsory) bytes of one FP32 sigma launch
+    N = prob.ham.n_clusters
+    op_bytes = po.data.size * 4 + pt.ints.size * 4
+    vec_bytes = 2 * n * R * 4
+    idx_bytes = n * (2 * N + 4 * N)
+    alg_bytes = op_bytes + vec_bytes + idx_bytes
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
+    achieved = alg_bytes / (k32 * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": value, "unit": "sigma_builds/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (mixed; fp64 line in fp64)", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n_cfg": n, "roots": R, "n_terms": prob.ham.n_terms(),
+                   "triples_per_sigma": stats["n_triples"], "work_items": stats["n_work_items"],
+                   "plan_seconds": stats["plan_seconds"], "l2": "flushed (256 MiB write) before every timed step",
+                   "parallelism": f"replicas{world}"},
+        "fp64": {"value": world * 1e3 / ms64, "ms_per_step": ms64, "kernel_ms": k64,
+                 "mixed_over_fp64": ms64 / ms32, "fp32_rel_err_vs_fp64": rel32},
+        "flops_reference_per_sigma": stats["flops_reference"],
+        "gflops_reference_count": {"fp32": stats["flops_reference"] / (k32 * 1e-3) / 1e9,
+                                   "fp64": stats["flops_reference"] / (k64 * 1e-3) / 1e9},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": achieved / hbm_peak, "traffic": None,
+                     "note": "compulsory bytes per launch / closed_sigma_kernel time (fp32); "
+                             "of measured HBM copy peak"},
+        "e2e": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": n * R * 8,
+                "d2h_bytes_per_step": n * R * 8},
+        "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
+        "clocks": clocks,
+    }
+    if rank == 0:
+        try:
+            thr = os.cpu_count() or 1
+            cv, sample = cpu_reference(po, pt, f, c, v, a.cpu_seconds, thr)
+            out["cpu_baseline"] = {"value": cv, "unit": "sigma_builds/s", "cores": thr, "kind": "port",
+                                   "sample": sample}
+        except Exception as ex:  # the baseline must not kill the GPU line
+            out["cpu_baseline"] = {"value": None, "error": str(ex)}
+        print(json.dumps(out))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

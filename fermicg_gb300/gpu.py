@@ -1,0 +1,178 @@
+"""ctypes binding of the in-tree CUDA library (include/fcg_gpu.h).
+
+This is the Python mirror of the reference's sigma entry points:
+  tps_ci_matvec(ci_vector, cluster_ops, clustered_ham)   src/tpsci_outer.jl:462
+  compute_diagonal(ci_vector, cluster_ops, H | "Hcmf")    src/tpsci_outer.jl:694/722
+all running on the GPU through libfcg_gpu.so.  There is no CPU fallback: if
+the library is missing or no GPU is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+from . import pack
+from .local_fci import N_OPS
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libfcg_gpu.so")
+
+FCG_FP64 = 0
+FCG_FP32 = 1
+PRECISION = {"fp64": FCG_FP64, "fp32": FCG_FP32, "mixed": FCG_FP32}
+
+# exported symbol -> (restype, argtypes); every name declared in include/fcg_gpu.h
+_P = ctypes.c_void_p
+_I = ctypes.c_int
+_L = ctypes.c_int64
+SIGNATURES = {
+    "fcg_version": (_I, []),
+    "fcg_ctx_create": (_I, [_I, ctypes.POINTER(_P)]),
+    "fcg_ctx_destroy": (_I, [_P]),
+    "fcg_last_error": (ctypes.c_char_p, [_P]),
+    "fcg_set_stream": (_I, [_P, _P]),
+    "fcg_set_ops": (_I, [_P, _I, _P, _L, _P, _L, _P]),
+    "fcg_set_terms": (_I, [_P, _I, _P, _L, _P, _I, _P]),
+    "fcg_state_set": (_I, [_P, _L, _P, _P]),
+    "fcg_sigma_closed": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_sigma_closed_device": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_diagonal": (_I, [_P, _I, _P]),
+    "fcg_get_stats": (_I, [_P, _P]),
+}
+
+
+class Stats(ctypes.Structure):
+    _fields_ = [("n_cfg", ctypes.c_int64), ("n_sectors", ctypes.c_int64), ("n_work_items", ctypes.c_int64),
+                ("n_triples", ctypes.c_int64), ("flops_reference", ctypes.c_int64),
+                ("plan_seconds", ctypes.c_double), ("last_kernel_ms", ctypes.c_double),
+                ("kernel_launches", ctypes.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libfcg_gpu.so (built by fermicg_gb300.build.build()); raises if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA library not built: {path} (run fermicg_gb300.build.build())")
+    L = ctypes.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class FcgError(RuntimeError):
+    pass
+
+
+class GpuSigma:
+    """One device context holding cluster ops, the clustered Hamiltonian and a state index."""
+
+    def __init__(self, device: int = 0):
+        self.L = load_library()
+        h = ctypes.c_void_p()
+        rc = self.L.fcg_ctx_create(device, ctypes.byref(h))
+        if rc != 0:
+            raise FcgError(f"fcg_ctx_create failed ({rc}): no usable CUDA device {device}")
+        self.h = h
+        self._keep = []
+        self.N = None
+        self.n_cfg = 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fcg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = self.L.fcg_last_error(self.h)
+            raise FcgError(f"{what} failed ({rc}): {msg.decode() if msg else ''}")
+
+    def set_stream(self, stream_ptr: int | None):
+        """Run later calls on an external cudaStream_t (e.g. torch's current stream)."""
+        self._check(self.L.fcg_set_stream(self.h, ctypes.c_void_p(stream_ptr or 0)), "fcg_set_stream")
+
+    # --- uploads ------------------------------------------------------------
+    def set_ops(self, packed_ops: "pack.PackedOps"):
+        tab = np.ascontiguousarray(packed_ops.table, dtype=np.int64)
+        dat = np.ascontiguousarray(packed_ops.data, dtype=np.float64)
+        norb = np.ascontiguousarray(packed_ops.cluster_norb, dtype=np.int32)
+        self.N = int(packed_ops.n_clusters)
+        self._check(self.L.fcg_set_ops(self.h, self.N, _ptr(norb), tab.shape[0], _ptr(tab), dat.size, _ptr(dat)),
+                    "fcg_set_ops")
+
+    def set_terms(self, packed_terms: "pack.PackedTerms"):
+        tab = np.ascontiguousarray(packed_terms.table, dtype=np.int32)
+        ints = np.ascontiguousarray(packed_terms.ints, dtype=np.float64)
+        tr = np.ascontiguousarray(packed_terms.transfers, dtype=np.int16)
+        self._check(self.L.fcg_set_terms(self.h, tab.shape[0], _ptr(tab), ints.size, _ptr(ints), tr.shape[0],
+                                         _ptr(tr)), "fcg_set_terms")
+
+    def set_problem(self, ops, bases, ham):
+        self.set_ops(pack.pack_ops(ops, bases))
+        self.set_terms(pack.pack_terms(ham))
+
+    def state_set(self, focks, cfgs):
+        f = np.ascontiguousarray(focks, dtype=np.int16)
+        c = np.ascontiguousarray(cfgs, dtype=np.int16)
+        self._check(self.L.fcg_state_set(self.h, f.shape[0], _ptr(f), _ptr(c)), "fcg_state_set")
+        self.n_cfg = f.shape[0]
+
+    # --- sigma --------------------------------------------------------------
+    def sigma_closed(self, coeffs, precision="fp64"):
+        """tps_ci_matvec: coeffs (n_cfg, R) host array -> sigma (n_cfg, R) float64."""
+        c = np.asfortranarray(coeffs, dtype=np.float64)
+        n, R = c.shape
+        if n != self.n_cfg:
+            raise ValueError("coefficient rows do not match the state")
+        sig = np.zeros((n, R), dtype=np.float64, order="F")
+        self._check(self.L.fcg_sigma_closed(self.h, R, _ptr(c), _ptr(sig), PRECISION[precision]),
+                    "fcg_sigma_closed")
+        return np.ascontiguousarray(sig)
+
+    def sigma_closed_device(self, d_c_ptr: int, d_sigma_ptr: int, R: int, precision="fp64"):
+        """Device-pointer variant (column-major n_cfg x R float64 buffers on this GPU)."""
+        self._check(self.L.fcg_sigma_closed_device(self.h, R, ctypes.c_void_p(d_c_ptr), ctypes.c_void_p(d_sigma_ptr),
+                                                   PRECISION[precision]), "fcg_sigma_closed_device")
+
+    def diagonal(self, op: str | None = None):
+        """compute_diagonal: op None = all zero-transfer terms; else an op string ("Hcmf", "H")."""
+        oid = -1 if op is None else pack.op_id_of(op)
+        hd = np.zeros(self.n_cfg)
+        self._check(self.L.fcg_diagonal(self.h, oid, _ptr(hd)), "fcg_diagonal")
+        return hd
+
+    def stats(self):
+        s = Stats()
+        self._check(self.L.fcg_get_stats(self.h, ctypes.byref(s)), "fcg_get_stats")
+        return s.as_dict()
+
+
+def tps_ci_matvec(state, gpu: GpuSigma, precision="fp64"):
+    """sigma = H c for a TPSCIstate already indexed on `gpu` (tpsci_outer.jl:462)."""
+    return gpu.sigma_closed(state.get_vector(), precision)
+
+
+assert N_OPS == 24

@@ -1,0 +1,106 @@
+/*
+ * fcg_gpu.h -- C ABI of the GB300 TPSCI sigma build (libfcg_gpu.so).
+ *
+ * The library replaces the hot path of FermiCG's tensor-product-state CI:
+ * the sigma build sigma = H c over a ClusteredOperator, for TPSCIstate vectors.
+ * Every entry point takes plain pointers and sizes, returns an int status
+ * (FCG_OK = 0, negative on error; fcg_last_error() gives the message) and
+ * never throws.  A context owns one GPU stream and all device memory; it is
+ * not thread-safe (one context per host thread, or serialise calls).
+ *
+ * Layouts (all integers little-endian, all indices 0-based):
+ *   op block table  int64 [n_blocks][10] = {cluster, op_id, fb_a, fb_b, fk_a, fk_b,
+ *                   n_idx, m_bra, m_ket, offset}; block element (p, I, J) is
+ *                   data[offset + p + n_idx*(I + m_bra*J)]  (Julia column-major
+ *                   (orbital-multi-index, I, J) of build_local_quantities.jl:176-188).
+ *                   op ids: 0..21 = A a B b AA aa BB bb Aa Bb Ab Ba AB ab AAa Aaa BBb Bbb
+ *                   ABa Aba ABb Bba, 22 = "H", 23 = "Hcmf".
+ *   term table      int32 [n_terms][28] = {nbody, transfer_id, cluster[4], op[4],
+ *                   delta_a[4], delta_b[4], parity[4], dim[4], ints_off_lo, ints_off_hi};
+ *                   a term's integrals are ints[off ...] flattened column-major.
+ *   transfers       int16 [n_transfers][n_clusters][2]  (TransferConfig).
+ *   state           fock int16 [n_cfg][n_clusters][2], cfg int16 [n_cfg][n_clusters]
+ *                   (ClusterConfig minus one); rows of one Fock sector contiguous,
+ *                   in TPSCIstate (get_vector) order.
+ *   coefficients    float64 column-major [R][n_cfg] (Julia Matrix{Float64}(n_cfg, R)).
+ * Limits: n_clusters <= 8, local states per sector <= 256, orbitals per cluster <= 15.
+ */
+#ifndef FCG_GPU_H
+#define FCG_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FCG_OK 0
+#define FCG_EINVAL -1
+#define FCG_ECUDA -2
+#define FCG_ENOMEM -3
+#define FCG_ESTATE -4
+#define FCG_ETIMEDOUT -5
+#define FCG_ELIMIT -6
+
+#define FCG_FP64 0  /* all arithmetic in float64 */
+#define FCG_FP32 1  /* contractions in float32 with float32 accumulation ("mixed") */
+
+typedef struct fcg_ctx fcg_ctx;
+
+typedef struct fcg_stats {
+  int64_t n_cfg;
+  int64_t n_sectors;
+  int64_t n_work_items;     /* (bra group, ket group, term list) blocks of the closed sigma */
+  int64_t n_triples;        /* (bra, ket, term) contractions of one closed sigma */
+  int64_t flops_reference;  /* sum over triples of 2*len(ints) (the reference's count) */
+  double plan_seconds;      /* host time of the last fcg_state_set */
+  double last_kernel_ms;    /* device time of the last sigma kernel (CUDA events) */
+  int64_t kernel_launches;  /* kernels launched by the last sigma call */
+} fcg_stats;
+
+int fcg_version(void);
+
+/* Create a context on CUDA device `device` (replaces nothing: setup). */
+int fcg_ctx_create(int device, fcg_ctx** out);
+int fcg_ctx_destroy(fcg_ctx* ctx);
+const char* fcg_last_error(const fcg_ctx* ctx);
+
+/* Run all later calls of this context on `stream` (a cudaStream_t of the
+ * context's device, owned by the caller); NULL returns to the context's own
+ * stream.  Calls still synchronise before returning. */
+int fcg_set_stream(fcg_ctx* ctx, void* stream);
+
+/* ClusterOps upload: Vector{ClusterOps} of compute_cluster_ops
+ * (src/build_local_quantities.jl:40-191, type src/type_ClusterOps.jl:1). */
+int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64_t n_blocks,
+                const int64_t* block_table, int64_t n_data, const double* data);
+
+/* ClusteredOperator upload: the Dict{TransferConfig, Vector{ClusteredTerm}} of
+ * extract_ClusteredTerms (src/type_ClusteredOperator.jl:5, 53-636). */
+int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t n_ints,
+                  const double* ints, int n_transfers, const int16_t* transfers);
+
+/* TPSCIstate structure (src/type_TPSCIstate.jl:11-14): uploads the rows and
+ * builds the device index used by every sigma call on this state. */
+int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg);
+
+/* tps_ci_matvec (src/tpsci_outer.jl:462-527): sigma = H c within the state's
+ * configurations.  Host buffers, column-major n_cfg x R; copies in and out
+ * inside the call.  precision: FCG_FP64 or FCG_FP32. */
+int fcg_sigma_closed(fcg_ctx* ctx, int R, const double* c, double* sigma, int precision);
+
+/* Same, on device buffers (column-major n_cfg x R float64) already resident
+ * on the context's device; runs on the context stream and synchronises. */
+int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
+
+/* compute_diagonal (src/tpsci_outer.jl:694-715) when op_id < 0 (all zero-transfer
+ * terms, bra == ket), else compute_diagonal! with that op string
+ * (src/tpsci_outer.jl:735-757, e.g. op_id 23 = "Hcmf").  hd: host, n_cfg. */
+int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd);
+
+int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FCG_GPU_H */
