@@ -288,13 +288,17 @@ __global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams
       for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r)
         if (r < R) val[r] = me * ck[r];
     }
-    // segmented suffix sums over runs of equal bra rows, then one atomic per run
+    // segmented suffix sums over runs of equal bra rows, then one atomic per run.
+    // The same bra can come back later in the warp (a new work item), so a lane
+    // only sums up to the next run head, never across another run.
     const int prev = __shfl_up_sync(0xffffffffu, key, 1);
     const bool head = (lane == 0) || (prev != key);
+    const unsigned heads = __ballot_sync(0xffffffffu, head);
+    const unsigned after = heads & ~((2u << lane) - 1u);
+    const int seg_end = after ? (__ffs(int(after)) - 1) : 32;
 #pragma unroll
     for (int off = 1; off < 32; off <<= 1) {
-      const int ko = __shfl_down_sync(0xffffffffu, key, off);
-      const bool take = (lane + off < 32) && (ko == key);
+      const bool take = (lane + off < seg_end);
 #pragma unroll
       for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r) {
         if (r < R) {
