@@ -58,28 +58,31 @@ def build_workload(n_cfg, R):
 
 
 def cpu_reference(po, pt, f, c, v, budget_s, threads):
-    """Time the oracle's tps_ci_matvec restatement on a growing bra-row sample; returns
-    (sigma builds/s extrapolated to the full space, sample description)."""
+    """Time the oracle's tps_ci_matvec restatement (all host threads): a 1/16 row sample
+    first; the full build when it fits the budget, else a larger evenly spaced sample.
+    Returns (sigma builds/s for the full space, description of what was timed)."""
     import oracle
     O = oracle.Oracle(po, pt)
     n = f.shape[0]
-    rows = 64
-    rng_rows = np.random.default_rng(1).permutation(n)
-    # contiguous blocks of rows are what the reference's per-bra jobs see; sample evenly spaced blocks
-    while True:
+
+    def run(nblk, frac):
+        rows = max(1, int(n * frac / nblk))
         t0 = time.perf_counter()
         done = 0
-        nblk = 8
         for b in range(nblk):
-            s0 = int(rng_rows[b] // rows * rows) % max(n - rows, 1)
-            O.sigma_closed(f, c, v, rows=(s0, s0 + rows // nblk), n_threads=threads)
-            done += rows // nblk
-        dt = time.perf_counter() - t0
-        if dt > budget_s / 4 or rows >= n:
-            break
-        rows = min(n, rows * 4)
-    per_row = dt / done
-    return 1.0 / (per_row * n), f"{done} of {n} bra rows (8 blocks), {dt:.1f} s, extrapolated"
+            s0 = (b * n) // nblk
+            O.sigma_closed(f, c, v, rows=(s0, min(n, s0 + rows)), n_threads=threads)
+            done += min(n, s0 + rows) - s0
+        return time.perf_counter() - t0, done
+
+    dt, done = run(16, 1.0 / 16)
+    est_full = dt * n / done
+    if est_full < budget_s:
+        dt, done = run(1, 1.0)
+        return 1.0 / dt, f"full build, all {n} bra rows, {dt:.2f} s"
+    frac = min(1.0, budget_s / est_full)
+    dt, done = run(16, frac)
+    return done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full build"
 
 
 def clocks_sampler():
@@ -201,6 +204,8 @@ def main():
     ms32, k32 = timed("fp32", a.steps, a.warmup)
     ms64, k64 = timed("fp64", max(3, a.steps // 4), a.warmup)
     clocks = finish()
+    g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp32")
+    torch.cuda.synchronize()
     sig32 = d_s.clone()
     g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp64")
     torch.cuda.synchronize()

@@ -40,15 +40,17 @@ def lib():
         L = ctypes.CDLL(_SO)
         P = ctypes.c_void_p
         i64 = ctypes.c_int64
+        L.oracle_set_problem.restype = ctypes.c_int
         L.oracle_set_problem.argtypes = [ctypes.c_int, P, ctypes.c_int, i64, P, P, ctypes.c_int, P, P,
                                          ctypes.c_int, P]
-        L.oracle_sigma_closed.argtypes = [i64, P, P, ctypes.c_int, P, P, i64, i64, ctypes.c_int]
-        L.oracle_diagonal_H.argtypes = [i64, P, P, P]
-        L.oracle_diagonal_op.argtypes = [i64, P, P, ctypes.c_int, P]
-        L.oracle_sigma_open.argtypes = [i64, P, P, ctypes.c_int, P, ctypes.c_double, ctypes.c_int, i64, i64,
+        L.oracle_sigma_closed.argtypes = [ctypes.c_int, i64, P, P, ctypes.c_int, P, P, i64, i64, ctypes.c_int]
+        L.oracle_diagonal_H.argtypes = [ctypes.c_int, i64, P, P, P]
+        L.oracle_build_H.argtypes = [ctypes.c_int, i64, P, P, P]
+        L.oracle_diagonal_op.argtypes = [ctypes.c_int, i64, P, P, ctypes.c_int, P]
+        L.oracle_sigma_open.argtypes = [ctypes.c_int, i64, P, P, ctypes.c_int, P, ctypes.c_double, ctypes.c_int, i64, i64,
                                         ctypes.c_int]
         L.oracle_sigma_open.restype = i64
-        L.oracle_open_fetch.argtypes = [P, P, P]
+        L.oracle_open_fetch.argtypes = [ctypes.c_int, P, P, P]
         _lib = L
     return _lib
 
@@ -74,8 +76,9 @@ class Oracle:
         self._keep = [opb, opd, trm, ints, trans, norb]
         rc = L.oracle_set_problem(self.N, _p(norb), N_OPS, opb.shape[0], _p(opb), _p(opd), trm.shape[0], _p(trm),
                                   _p(ints), trans.shape[0], _p(trans))
-        if rc != 0:
+        if rc < 0:
             raise RuntimeError("oracle_set_problem failed")
+        self.h = rc
 
     def sigma_closed(self, focks, cfgs, coeffs, rows=None, n_threads=0):
         """tps_ci_matvec; coeffs (n_cfg, R) -> sigma (n_cfg, R)."""
@@ -85,17 +88,27 @@ class Oracle:
         cf = np.asfortranarray(coeffs, dtype=np.float64)
         sig = np.zeros((n, R), dtype=np.float64, order="F")
         r0, r1 = (0, n) if rows is None else rows
-        rc = lib().oracle_sigma_closed(n, _p(f), _p(c), R, _p(cf), _p(sig), r0, r1, n_threads)
+        rc = lib().oracle_sigma_closed(self.h, n, _p(f), _p(c), R, _p(cf), _p(sig), r0, r1, n_threads)
         if rc != 0:
             raise RuntimeError("oracle_sigma_closed failed")
         return np.ascontiguousarray(sig)
+
+    def build_H(self, focks, cfgs):
+        """Dense H over the configurations (build_full_H)."""
+        n = focks.shape[0]
+        f = np.ascontiguousarray(focks, dtype=np.int16)
+        c = np.ascontiguousarray(cfgs, dtype=np.int16)
+        H = np.zeros((n, n))
+        if lib().oracle_build_H(self.h, n, _p(f), _p(c), _p(H)) != 0:
+            raise RuntimeError("oracle_build_H failed")
+        return H
 
     def diagonal_H(self, focks, cfgs):
         n = focks.shape[0]
         f = np.ascontiguousarray(focks, dtype=np.int16)
         c = np.ascontiguousarray(cfgs, dtype=np.int16)
         hd = np.zeros(n)
-        lib().oracle_diagonal_H(n, _p(f), _p(c), _p(hd))
+        lib().oracle_diagonal_H(self.h, n, _p(f), _p(c), _p(hd))
         return hd
 
     def diagonal_op(self, focks, cfgs, op_id):
@@ -103,7 +116,7 @@ class Oracle:
         f = np.ascontiguousarray(focks, dtype=np.int16)
         c = np.ascontiguousarray(cfgs, dtype=np.int16)
         hd = np.zeros(n)
-        rc = lib().oracle_diagonal_op(n, _p(f), _p(c), op_id, _p(hd))
+        rc = lib().oracle_diagonal_op(self.h, n, _p(f), _p(c), op_id, _p(hd))
         if rc != 0:
             raise RuntimeError("missing diagonal block")
         return hd
@@ -115,11 +128,11 @@ class Oracle:
         c = np.ascontiguousarray(cfgs, dtype=np.int16)
         cf = np.asfortranarray(coeffs, dtype=np.float64)
         r0, r1 = (0, n) if rows is None else rows
-        m = lib().oracle_sigma_open(n, _p(f), _p(c), R, _p(cf), float(thresh), nbody, r0, r1, n_threads)
+        m = lib().oracle_sigma_open(self.h, n, _p(f), _p(c), R, _p(cf), float(thresh), nbody, r0, r1, n_threads)
         if m < 0:
             raise RuntimeError("oracle_sigma_open failed")
         of = np.zeros((m, self.N, 2), dtype=np.int16)
         oc = np.zeros((m, self.N), dtype=np.int16)
         ov = np.zeros((m, R), dtype=np.float64)
-        lib().oracle_open_fetch(_p(of), _p(oc), _p(ov))
+        lib().oracle_open_fetch(self.h, _p(of), _p(oc), _p(ov))
         return of, oc, ov

@@ -76,7 +76,7 @@ struct State {
   std::map<std::vector<int16_t>, int> sec_of;  // fock key -> sector id
 };
 
-Problem* g_prob = nullptr;
+std::vector<Problem*> g_probs;  // one per oracle_set_problem call (handle = index)
 
 inline int32_t T(const Problem& P, int t, int col) { return P.trm[int64_t(t) * TRM_COLS + col]; }
 inline int64_t TOff(const Problem& P, int t) {
@@ -188,12 +188,12 @@ void build_sectors(const Problem& P, State& S) {
 
 extern "C" {
 
+// returns a problem handle (>= 0) used by every other call
 int oracle_set_problem(int n_clusters, const int32_t* cluster_norb, int n_ops, int64_t n_blocks,
                        const int64_t* opb, const double* opdata, int n_terms, const int32_t* trm,
                        const double* ints, int n_trans, const int16_t* trans) {
-  delete g_prob;
-  g_prob = new Problem();
-  Problem& P = *g_prob;
+  g_probs.push_back(new Problem());
+  Problem& P = *g_probs.back();
   P.N = n_clusters;
   P.norb.assign(cluster_norb, cluster_norb + n_clusters);
   P.nmax = *std::max_element(P.norb.begin(), P.norb.end());
@@ -213,15 +213,15 @@ int oracle_set_problem(int n_clusters, const int32_t* cluster_norb, int n_ops, i
   P.trans.assign(trans, trans + int64_t(n_trans) * n_clusters * 2);
   P.terms_of_trans.assign(n_trans, {});
   for (int t = 0; t < n_terms; ++t) P.terms_of_trans[T(P, t, 1)].push_back(t);
-  return 0;
+  return int(g_probs.size()) - 1;
 }
 
 // tps_ci_matvec (tpsci_outer.jl:462-527): sigma = H c restricted to the configs of c.
 // bra rows [row_begin, row_end) only (the full build is [0, n)); sigma rows outside are untouched.
-int oracle_sigma_closed(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int R, const double* c,
+int oracle_sigma_closed(int h, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int R, const double* c,
                         double* sigma, int64_t row_begin, int64_t row_end, int n_threads) {
-  if (!g_prob) return -1;
-  const Problem& P = *g_prob;
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const Problem& P = *g_probs[h];
   State S;
   S.n = n_cfg;
   S.fock = fock;
@@ -262,10 +262,50 @@ int oracle_sigma_closed(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, 
   return 0;
 }
 
+// build_full_H (tpsci_outer.jl:10-150): dense H[bra, ket] (row-major n x n) over the configs.
+int oracle_build_H(int h, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, double* H) {
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const Problem& P = *g_probs[h];
+  State S;
+  S.n = n_cfg;
+  S.fock = fock;
+  S.cfg = cfg;
+  build_sectors(P, S);
+  const int N = P.N;
+#pragma omp parallel
+  {
+    std::vector<int16_t> fk(2 * N);
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t ib = 0; ib < n_cfg; ++ib) {
+      const int16_t* fb = fock + ib * 2 * N;
+      const int16_t* b = cfg + ib * N;
+      double* row = H + ib * n_cfg;
+      for (int64_t j = 0; j < n_cfg; ++j) row[j] = 0.0;
+      for (int tr = 0; tr < P.n_trans; ++tr) {
+        const int16_t* tv = &P.trans[int64_t(tr) * N * 2];
+        for (int i = 0; i < 2 * N; ++i) fk[i] = int16_t(fb[i] - tv[i]);
+        auto it = S.sec_of.find(fk);
+        if (it == S.sec_of.end()) continue;
+        int64_t ks = S.sec_start[it->second], kn = S.sec_count[it->second];
+        for (int64_t ik = ks; ik < ks + kn; ++ik) {
+          const int16_t* k = cfg + ik * N;
+          for (int t : P.terms_of_trans[tr]) {
+            if (!check_term(P, t, fb, b, fk.data(), k)) continue;
+            double me;
+            if (!matrix_element(P, t, fb, b, fk.data(), k, &me)) continue;
+            row[ik] += me;
+          }
+        }
+      }
+    }
+  }
+  return 0;
+}
+
 // compute_diagonal (tpsci_outer.jl:694-715): sum of zero-transfer terms with bra == ket.
-int oracle_diagonal_H(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, double* hd) {
-  if (!g_prob) return -1;
-  const Problem& P = *g_prob;
+int oracle_diagonal_H(int h, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, double* hd) {
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const Problem& P = *g_probs[h];
   const int N = P.N;
   int zero = -1;
   for (int tr = 0; tr < P.n_trans; ++tr) {
@@ -287,9 +327,9 @@ int oracle_diagonal_H(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, do
 }
 
 // compute_diagonal! with an op string (tpsci_outer.jl:735-757): sum_c diag(op_c)[cfg_c].
-int oracle_diagonal_op(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int op, double* hd) {
-  if (!g_prob) return -1;
-  const Problem& P = *g_prob;
+int oracle_diagonal_op(int h, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int op, double* hd) {
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const Problem& P = *g_probs[h];
   const int N = P.N;
   for (int64_t i = 0; i < n_cfg; ++i) {
     double s = 0.0;
@@ -486,10 +526,10 @@ void open_contract(OpenCtx& X, int t, const int16_t* fbra, const int16_t* fket, 
 
 // open_matvec_thread: returns the number of output configurations (or < 0 on error).
 // ket rows [row_begin, row_end) only contribute (the full build is [0, n)).
-int64_t oracle_sigma_open(int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int R, const double* c,
+int64_t oracle_sigma_open(int h, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, int R, const double* c,
                           double thresh, int nbody, int64_t row_begin, int64_t row_end, int n_threads) {
-  if (!g_prob) return -1;
-  const Problem& P = *g_prob;
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const Problem& P = *g_probs[h];
   const int N = P.N;
   State S;
   S.n = n_cfg;
@@ -565,9 +605,9 @@ int64_t oracle_sigma_open(int64_t n_cfg, const int16_t* fock, const int16_t* cfg
 }
 
 // rows of the last open sigma: fock (n x N x 2), cfg (n x N), coeff (n x R row-major)
-int oracle_open_fetch(int16_t* fock, int16_t* cfg, double* coeff) {
-  if (!g_prob) return -1;
-  const int N = g_prob->N;
+int oracle_open_fetch(int h, int16_t* fock, int16_t* cfg, double* coeff) {
+  if (h < 0 || h >= int(g_probs.size())) return -1;
+  const int N = g_probs[h]->N;
   for (size_t i = 0; i < g_open_keys.size(); ++i) {
     std::memcpy(fock + i * 2 * N, g_open_keys[i].v.data(), sizeof(int16_t) * 2 * N);
     std::memcpy(cfg + i * N, g_open_keys[i].v.data() + 2 * N, sizeof(int16_t) * N);
