@@ -1,22 +1,27 @@
 // GB300 (sm_103a) TPSCI sigma build behind the C ABI of include/fcg_gpu.h.
 //
 // Device layout (one context, one stream):
-//   op data      the TDM blocks of every cluster in one blob, float64 and a float32 copy,
+//   op data      the TDM blocks of every cluster in one blob (float64 + float32 copy),
 //                block (p, I, J) at off + p + nidx*(I + mb*J)
+//   dressed ops  per term and per sector pair of its dressed cluster,
+//                W[(rest), b, k] = sum_i ints[..i..] G[i, b, k]  (float64 + float32 copy);
+//                1-body terms store their "H" block here
 //   block index  dense int32 table (cluster, op, fb_a, fb_b, fk_a, fk_b) -> block id
-//   terms        TermInfo per ClusteredTerm, integrals in a float64 blob (+ float32 copy)
-//   state        local states int16 [n_cfg][N]; sector fock int16 [n_sec][N][2]
-//   plan         work items (bra group x ket group x term list), their triple prefix sum,
-//                the grouping permutation pool and the term pool (plan.cpp)
+//   state        local states int16 [n_cfg][N]
+//   plan         work items (bra group x ket group x term-sector list), their triple
+//                prefix sum, the grouping permutation pool and the term-sector records
 //   vectors      coefficients / sigma row-major [n_cfg][R] in the compute precision
 //
 // Kernels:
-//   closed_sigma_kernel  one pass over the flattened (work item, bra, ket, term)
-//                        triple space; each CTA takes a fixed chunk (load balance is
-//                        exact), contracts term integrals with the TDM columns
-//                        (contract_matrix_element, src/tpsci_inner.jl:10-216) and
-//                        scatters sigma with warp-segmented sums + one atomic per run.
-//   diag_kernels         compute_diagonal (src/tpsci_outer.jl:694-757).
+//   dress_kernel         W blocks, once per problem (fcg_set_terms)
+//   closed_sigma_kernel  one pass over the flattened (work item, bra, ket, term) triple
+//                        space; each CTA takes a fixed chunk (exact load balance), each
+//                        warp 32 consecutive triples; a matrix element is the W column of
+//                        the dressed cluster contracted with the TDM columns of the other
+//                        active clusters (contract_matrix_element, src/tpsci_inner.jl:10-216,
+//                        re-associated); sigma is scattered with warp-segmented sums and
+//                        one atomic per run of equal bra rows.
+//   diag kernels         compute_diagonal (src/tpsci_outer.jl:694-757).
 //   pack / unpack        column-major float64 <-> row-major compute precision.
 #include <cuda_runtime.h>
 
@@ -71,8 +76,8 @@ struct DevBuf {
 
 struct fcg_ctx {
   int device = 0;
-  cudaStream_t stream = nullptr;       // stream every call runs on
-  cudaStream_t own_stream = nullptr;   // the context's own stream
+  cudaStream_t stream = nullptr;      // stream every call runs on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
   // problem
@@ -81,6 +86,8 @@ struct fcg_ctx {
   int nmax = 0;
   bool have_ops = false, have_terms = false, have_state = false;
   std::vector<int64_t> opb;
+  std::vector<BlockInfo> h_blocks;
+  std::vector<int32_t> h_blk_index;
   DevBuf<double> d_op64;
   DevBuf<float> d_op32;
   DevBuf<BlockInfo> d_blocks;
@@ -88,9 +95,14 @@ struct fcg_ctx {
   int n_terms = 0;
   std::vector<int32_t> trm;
   std::vector<TermInfo> terms;
+  std::vector<TermDress> dress;
+  std::vector<int64_t> w_index;
+  int64_t n_w = 0;
   DevBuf<TermInfo> d_terms;
   DevBuf<double> d_ints64;
   DevBuf<float> d_ints32;
+  DevBuf<double> d_w64;
+  DevBuf<float> d_w32;
   int n_trans = 0;
   std::vector<int16_t> trans;
   // state + plan
@@ -102,7 +114,7 @@ struct fcg_ctx {
   DevBuf<WorkItem> d_items;
   DevBuf<int64_t> d_prefix;
   DevBuf<int32_t> d_perm;
-  DevBuf<int32_t> d_term_pool;
+  DevBuf<TermSector> d_ts;
   DevBuf<int32_t> d_zero_terms;
   // vectors
   DevBuf<double> d_in64, d_out64;  // column-major staging for host calls
@@ -112,13 +124,13 @@ struct fcg_ctx {
   fcg_stats stats{};
 };
 
-#define FCG_CUDA(call)                                                                       \
-  do {                                                                                       \
-    cudaError_t e_ = (call);                                                                 \
-    if (e_ != cudaSuccess) {                                                                 \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                         \
-      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;                       \
-    }                                                                                        \
+#define FCG_CUDA(call)                                                               \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;               \
+    }                                                                                \
   } while (0)
 
 #define FCG_REQUIRE(cond, code, msg) \
@@ -133,99 +145,92 @@ struct fcg_ctx {
 // device code
 namespace {
 
+// ---- dressing ----------------------------------------------------------------------------
+__global__ void dress_kernel(const DressJob* __restrict__ jobs, const double* __restrict__ op,
+                             const double* __restrict__ ints, double* __restrict__ w) {
+  const DressJob J = jobs[blockIdx.x];
+  const int64_t n = int64_t(J.rest_len) * J.mb * J.mk;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int r = int(e % J.rest_len);
+    const int64_t bk = e / J.rest_len;
+    const int b = int(bk % J.mb);
+    const int k = int(bk / J.mb);
+    double acc;
+    if (J.one_body) {
+      acc = op[J.g_off + b + int64_t(J.mb) * k];
+    } else {
+      int64_t base = J.ints_off;
+      int rr = r;
+      for (int o = 0; o < J.nrem; ++o) {
+        base += int64_t(rr % J.rem_dim[o]) * J.rem_stride[o];
+        rr /= J.rem_dim[o];
+      }
+      const double* g = op + J.g_off + int64_t(J.nq) * (b + int64_t(J.mb) * k);
+      acc = 0.0;
+      for (int i = 0; i < J.nq; ++i) acc = fma(ints[base + int64_t(i) * J.stride_q], g[i], acc);
+    }
+    w[J.w_off + e] = acc;
+  }
+}
+
+__global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  for (; i < n; i += int64_t(gridDim.x) * blockDim.x) b[i] = float(a[i]);
+}
+
+// ---- closed sigma ------------------------------------------------------------------------
 struct SigmaParams {
   const WorkItem* items;
   const int64_t* prefix;
   int64_t n_items;
   int64_t n_triples;
   const int32_t* perm;
-  const int32_t* term_pool;
-  const TermInfo* terms;
-  const BlockInfo* blocks;
-  const int32_t* blk_index;
-  const int16_t* cfg;       // [n_cfg][N]
-  const int16_t* sec_fock;  // [n_sec][N][2]
+  const TermSector* ts;
+  const int16_t* cfg;  // [n_cfg][N]
   int N;
-  int nmax1;  // nmax + 1
   int R;
 };
 
-__device__ __forceinline__ int block_of(const SigmaParams& p, int c, int op, const int16_t* fb,
-                                        const int16_t* fk) {
-  int s = p.nmax1;
-  int64_t i = ((((int64_t(c) * kNumOps + op) * s + fb[2 * c]) * s + fb[2 * c + 1]) * s + fk[2 * c]) * s +
-              fk[2 * c + 1];
-  return p.blk_index[i];
-}
-
-// compute_terms_state_sign (src/type_ClusteredTerm.jl:181-196) from the ket sector
-__device__ __forceinline__ int term_sign(const TermInfo& tm, const int16_t* fk) {
-  int s = 0;
-  for (int o = 0; o < tm.nbody; ++o) {
-    if (tm.parity[o]) {
-      int ne = 0;
-      for (int ci = 0; ci < tm.c[o]; ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
-      s ^= ne & 1;
-    }
-  }
-  return s ? -1 : 1;
-}
-
-// One matrix element <bra|term|ket>: ints contracted with one TDM column per active
-// cluster, in the order of _contract (src/tpsci_inner.jl:270-329).
+// <bra| term |ket> from a term-sector record: the dressed cluster's W column contracted
+// with the other active clusters' TDM columns.
 template <typename T>
-__device__ T matrix_element(const SigmaParams& p, const TermInfo& tm, const T* __restrict__ op,
-                            const T* __restrict__ ints, const int16_t* fb, const int16_t* fk, int b, int k) {
-  const T* g[4];
-  int d[4];
-  for (int o = 0; o < tm.nbody; ++o) {
-    int c = tm.c[o];
-    int bl = block_of(p, c, tm.op[o], fb, fk);
-    if (bl < 0) return T(0);
-    BlockInfo bi = p.blocks[bl];
-    int sb = p.cfg[int64_t(b) * p.N + c];
-    int sk = p.cfg[int64_t(k) * p.N + c];
-    g[o] = op + bi.off + int64_t(bi.nidx) * (sb + int64_t(bi.mb) * sk);
-    d[o] = bi.nidx;
-  }
-  if (tm.nbody == 1) return g[0][0];
-  const T* v = ints + tm.ints_off;
+__device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __restrict__ w,
+                                             const T* __restrict__ op, const int16_t* __restrict__ cb,
+                                             const int16_t* __restrict__ ck) {
+  const T* wc = w + ts.w_off + int64_t(ts.rest_len) * (cb[ts.cw] + int64_t(ts.w_mb) * ck[ts.cw]);
+  if (ts.nrem == 0) return wc[0];
+  const T* g0 = op + ts.g_off[0] + int64_t(ts.g_dim[0]) * (cb[ts.cr[0]] + int64_t(ts.g_mb[0]) * ck[ts.cr[0]]);
+  const int d0 = ts.g_dim[0];
   T me = T(0);
-  if (tm.nbody == 2) {
-    for (int j = 0; j < d[1]; ++j) {
-      T acc = T(0);
-      const T* vj = v + d[0] * j;
-      for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], __ldg(vj + i), acc);
-      me = fma(acc, g[1][j], me);
-    }
-  } else if (tm.nbody == 3) {
-    for (int kk = 0; kk < d[2]; ++kk) {
-      T acck = T(0);
-      for (int j = 0; j < d[1]; ++j) {
-        T acc = T(0);
-        const T* vj = v + d[0] * (j + d[1] * kk);
-        for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], __ldg(vj + i), acc);
-        acck = fma(acc, g[1][j], acck);
-      }
-      me = fma(acck, g[2][kk], me);
-    }
+  if (ts.nrem == 1) {
+    for (int i = 0; i < d0; ++i) me = fma(wc[i], g0[i], me);
   } else {
-    for (int l = 0; l < d[3]; ++l) {
-      T accl = T(0);
-      for (int kk = 0; kk < d[2]; ++kk) {
-        T acck = T(0);
-        for (int j = 0; j < d[1]; ++j) {
-          T acc = T(0);
-          const T* vj = v + d[0] * (j + d[1] * (kk + d[2] * l));
-          for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], __ldg(vj + i), acc);
-          acck = fma(acc, g[1][j], acck);
-        }
-        accl = fma(acck, g[2][kk], accl);
+    const T* g1 = op + ts.g_off[1] + int64_t(ts.g_dim[1]) * (cb[ts.cr[1]] + int64_t(ts.g_mb[1]) * ck[ts.cr[1]]);
+    const int d1 = ts.g_dim[1];
+    if (ts.nrem == 2) {
+      for (int j = 0; j < d1; ++j) {
+        const T* wj = wc + d0 * j;
+        T acc = T(0);
+        for (int i = 0; i < d0; ++i) acc = fma(wj[i], g0[i], acc);
+        me = fma(acc, g1[j], me);
       }
-      me = fma(accl, g[3][l], me);
+    } else {
+      const T* g2 =
+          op + ts.g_off[2] + int64_t(ts.g_dim[2]) * (cb[ts.cr[2]] + int64_t(ts.g_mb[2]) * ck[ts.cr[2]]);
+      const int d2 = ts.g_dim[2];
+      for (int l = 0; l < d2; ++l) {
+        T accl = T(0);
+        for (int j = 0; j < d1; ++j) {
+          const T* wj = wc + d0 * (j + d1 * l);
+          T acc = T(0);
+          for (int i = 0; i < d0; ++i) acc = fma(wj[i], g0[i], acc);
+          accl = fma(acc, g1[j], accl);
+        }
+        me = fma(accl, g2[l], me);
+      }
     }
   }
-  return term_sign(tm, fk) * me;
+  return ts.sign < 0 ? -me : me;
 }
 
 constexpr int kSigmaThreads = 256;
@@ -246,46 +251,51 @@ __device__ __forceinline__ int64_t find_item(const int64_t* prefix, int64_t lo, 
 }
 
 template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams p, const T* __restrict__ op,
-                                                                      const T* __restrict__ ints,
+__global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
+                                                                      const T* __restrict__ op,
                                                                       const T* __restrict__ cin,
                                                                       T* __restrict__ sig) {
+  constexpr int RV = RR > 0 ? RR : kMaxR;
   const int64_t s0 = int64_t(blockIdx.x) * kSigmaChunk;
   const int64_t e0 = (s0 + kSigmaChunk < p.n_triples) ? s0 + kSigmaChunk : p.n_triples;
-  __shared__ int64_t w_lo, w_hi;
+  __shared__ int64_t w_lo_s, w_hi_s;
   if (threadIdx.x == 0) {
-    w_lo = find_item(p.prefix, 0, p.n_items - 1, s0);
-    w_hi = find_item(p.prefix, w_lo, p.n_items - 1, e0 - 1);
+    w_lo_s = find_item(p.prefix, 0, p.n_items - 1, s0);
+    w_hi_s = find_item(p.prefix, w_lo_s, p.n_items - 1, e0 - 1);
   }
   __syncthreads();
+  const int64_t w_hi = w_hi_s;
   const int lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int R = RR > 0 ? RR : p.R;
-  int64_t w = w_lo;
+  int64_t wcur = w_lo_s;  // warp-uniform: item of the warp's first triple
   for (int it = 0; it < kSigmaIters; ++it) {
-    const int64_t idx = s0 + int64_t(it) * kSigmaThreads + threadIdx.x;
+    const int64_t base = s0 + int64_t(it) * kSigmaThreads + int64_t(warp) * 32;
+    const int64_t idx = base + lane;
+    // the warp's first triple locates its item once; lanes step forward from it
+    if (base < e0) wcur = find_item(p.prefix, wcur, w_hi, base);
     int key = -1;
-    T val[RR > 0 ? RR : kMaxR];
+    T val[RV];
 #pragma unroll
-    for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r) val[r] = T(0);
+    for (int r = 0; r < RV; ++r) val[r] = T(0);
     if (idx < e0) {
-      w = find_item(p.prefix, w, w_hi, idx);
-      const WorkItem wi = p.items[w];
-      const int64_t local = idx - p.prefix[w];
+      int64_t wi_ = wcur;
+      while (wi_ < w_hi && __ldg(p.prefix + wi_ + 1) <= idx) ++wi_;
+      const WorkItem wi = p.items[wi_];
+      const int64_t local = idx - __ldg(p.prefix + wi_);
       // triple order inside an item: term fastest, then ket, then bra
       const int ti = int(local % wi.nt);
       const int64_t rest = local / wi.nt;
       const int kj = int(rest % wi.nk);
       const int bj = int(rest / wi.nk);
-      const int b = p.perm[wi.bra_off + bj];
-      const int k = p.perm[wi.ket_off + kj];
-      const TermInfo tm = p.terms[p.term_pool[wi.tl_off + ti]];
-      const int16_t* fb = p.sec_fock + int64_t(wi.sb) * 2 * p.N;
-      const int16_t* fk = p.sec_fock + int64_t(wi.sk) * 2 * p.N;
-      const T me = matrix_element<T>(p, tm, op, ints, fb, fk, b, k);
+      const int b = __ldg(p.perm + wi.bra_off + bj);
+      const int k = __ldg(p.perm + wi.ket_off + kj);
+      const TermSector ts = p.ts[wi.ts_off + ti];
+      const T me = dressed_element<T>(ts, w, op, p.cfg + int64_t(b) * p.N, p.cfg + int64_t(k) * p.N);
       key = b;
       const T* ck = cin + int64_t(k) * R;
 #pragma unroll
-      for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r)
+      for (int r = 0; r < RV; ++r)
         if (r < R) val[r] = me * ck[r];
     }
     // segmented suffix sums over runs of equal bra rows, then one atomic per run.
@@ -300,7 +310,7 @@ __global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams
     for (int off = 1; off < 32; off <<= 1) {
       const bool take = (lane + off < seg_end);
 #pragma unroll
-      for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r) {
+      for (int r = 0; r < RV; ++r) {
         if (r < R) {
           T vo = __shfl_down_sync(0xffffffffu, val[r], off);
           if (take) val[r] += vo;
@@ -309,7 +319,7 @@ __global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams
     }
     if (head && key >= 0) {
 #pragma unroll
-      for (int r = 0; r < (RR > 0 ? RR : kMaxR); ++r)
+      for (int r = 0; r < RV; ++r)
         if (r < R) atomicAdd(sig + int64_t(key) * R + r, val[r]);
     }
   }
@@ -333,29 +343,100 @@ __global__ void unpack_out_kernel(const T* __restrict__ s, double* __restrict__ 
   out[i] = double(s[row * R + r]);
 }
 
-__global__ void diag_terms_kernel(SigmaParams p, const double* __restrict__ op, const double* __restrict__ ints,
-                                  const int32_t* __restrict__ zero_terms, int n_zero,
-                                  const int32_t* __restrict__ row_sector, int64_t n, double* __restrict__ hd) {
+// ---- diagonal ------------------------------------------------------------------------------
+struct DiagParams {
+  const TermInfo* terms;
+  const BlockInfo* blocks;
+  const int32_t* blk_index;
+  const int16_t* cfg;
+  const int16_t* sec_fock;
+  const int32_t* row_sector;
+  int N;
+  int nmax1;
+};
+
+__device__ __forceinline__ int block_of(const DiagParams& p, int c, int op, const int16_t* f) {
+  return p.blk_index[dense_block_index(p.nmax1, c, op, f[2 * c], f[2 * c + 1], f[2 * c], f[2 * c + 1])];
+}
+
+// <cfg|term|cfg> in the order of _contract (src/tpsci_inner.jl:270-329)
+__device__ double diag_element(const DiagParams& p, const TermInfo& tm, const double* __restrict__ op,
+                               const double* __restrict__ ints, const int16_t* f, const int16_t* cf) {
+  const double* g[4];
+  int d[4];
+  for (int o = 0; o < tm.nbody; ++o) {
+    int c = tm.c[o];
+    int bl = block_of(p, c, tm.op[o], f);
+    if (bl < 0) return 0.0;
+    BlockInfo bi = p.blocks[bl];
+    g[o] = op + bi.off + int64_t(bi.nidx) * (cf[c] + int64_t(bi.mb) * cf[c]);
+    d[o] = bi.nidx;
+  }
+  if (tm.nbody == 1) return g[0][0];
+  const double* v = ints + tm.ints_off;
+  double me = 0.0;
+  if (tm.nbody == 2) {
+    for (int j = 0; j < d[1]; ++j) {
+      double acc = 0.0;
+      for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], v[i + d[0] * j], acc);
+      me = fma(acc, g[1][j], me);
+    }
+  } else if (tm.nbody == 3) {
+    for (int kk = 0; kk < d[2]; ++kk) {
+      double acck = 0.0;
+      for (int j = 0; j < d[1]; ++j) {
+        double acc = 0.0;
+        const double* vj = v + d[0] * (j + d[1] * kk);
+        for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], vj[i], acc);
+        acck = fma(acc, g[1][j], acck);
+      }
+      me = fma(acck, g[2][kk], me);
+    }
+  } else {
+    for (int l = 0; l < d[3]; ++l) {
+      double accl = 0.0;
+      for (int kk = 0; kk < d[2]; ++kk) {
+        double acck = 0.0;
+        for (int j = 0; j < d[1]; ++j) {
+          double acc = 0.0;
+          const double* vj = v + d[0] * (j + d[1] * (kk + d[2] * l));
+          for (int i = 0; i < d[0]; ++i) acc = fma(g[0][i], vj[i], acc);
+          acck = fma(acc, g[1][j], acck);
+        }
+        accl = fma(acck, g[2][kk], accl);
+      }
+      me = fma(accl, g[3][l], me);
+    }
+  }
+  int s = 0;
+  for (int o = 0; o < tm.nbody; ++o)
+    if (tm.parity[o]) {
+      int ne = 0;
+      for (int ci = 0; ci < tm.c[o]; ++ci) ne += f[2 * ci] + f[2 * ci + 1];
+      s ^= ne & 1;
+    }
+  return s ? -me : me;
+}
+
+__global__ void diag_terms_kernel(DiagParams p, const double* __restrict__ op, const double* __restrict__ ints,
+                                  const int32_t* __restrict__ zero_terms, int n_zero, int64_t n,
+                                  double* __restrict__ hd) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int16_t* f = p.sec_fock + int64_t(row_sector[i]) * 2 * p.N;
+  const int16_t* f = p.sec_fock + int64_t(p.row_sector[i]) * 2 * p.N;
   double s = 0.0;
-  for (int z = 0; z < n_zero; ++z) {
-    const TermInfo tm = p.terms[zero_terms[z]];
-    s += matrix_element<double>(p, tm, op, ints, f, f, int(i), int(i));
-  }
+  for (int z = 0; z < n_zero; ++z) s += diag_element(p, p.terms[zero_terms[z]], op, ints, f, p.cfg + i * p.N);
   hd[i] = s;
 }
 
-__global__ void diag_op_kernel(SigmaParams p, const double* __restrict__ op, int opid,
-                               const int32_t* __restrict__ row_sector, int64_t n, double* __restrict__ hd,
-                               int* __restrict__ missing) {
+__global__ void diag_op_kernel(DiagParams p, const double* __restrict__ op, int opid, int64_t n,
+                               double* __restrict__ hd, int* __restrict__ missing) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const int16_t* f = p.sec_fock + int64_t(row_sector[i]) * 2 * p.N;
+  const int16_t* f = p.sec_fock + int64_t(p.row_sector[i]) * 2 * p.N;
   double s = 0.0;
   for (int c = 0; c < p.N; ++c) {
-    int bl = block_of(p, c, opid, f, f);
+    int bl = block_of(p, c, opid, f);
     if (bl < 0) {
       atomicExch(missing, 1);
       continue;
@@ -372,28 +453,36 @@ __global__ void diag_op_kernel(SigmaParams p, const double* __restrict__ op, int
 // ---------------------------------------------------------------------------------------
 // host side
 
-static SigmaParams make_params(fcg_ctx* ctx, int R) {
+static SigmaParams make_sigma_params(fcg_ctx* ctx, int R) {
   SigmaParams p{};
   p.items = ctx->d_items.p;
   p.prefix = ctx->d_prefix.p;
   p.n_items = int64_t(ctx->plan.items.size());
   p.n_triples = ctx->plan.n_triples;
   p.perm = ctx->d_perm.p;
-  p.term_pool = ctx->d_term_pool.p;
+  p.ts = ctx->d_ts.p;
+  p.cfg = ctx->d_cfg.p;
+  p.N = ctx->N;
+  p.R = R;
+  return p;
+}
+
+static DiagParams make_diag_params(fcg_ctx* ctx) {
+  DiagParams p{};
   p.terms = ctx->d_terms.p;
   p.blocks = ctx->d_blocks.p;
   p.blk_index = ctx->d_blk_index.p;
   p.cfg = ctx->d_cfg.p;
   p.sec_fock = ctx->d_sec_fock.p;
+  p.row_sector = ctx->d_row_sector.p;
   p.N = ctx->N;
   p.nmax1 = ctx->nmax + 1;
-  p.R = R;
   return p;
 }
 
 extern "C" {
 
-int fcg_version(void) { return 1; }
+int fcg_version(void) { return 2; }
 
 int fcg_ctx_create(int device, fcg_ctx** out) {
   if (!out) return FCG_EINVAL;
@@ -438,7 +527,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
                 const int64_t* block_table, int64_t n_data, const double* data) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(n_clusters > 0 && n_clusters <= kMaxClusters, FCG_ELIMIT, "n_clusters must be in [1, 8]");
-  FCG_REQUIRE(cluster_norb && block_table && (data || n_data == 0), FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(cluster_norb && block_table && (data || n_data == 0) && n_blocks >= 0, FCG_EINVAL, "null pointer");
   FCG_CUDA(cudaSetDevice(ctx->device));
   ctx->N = n_clusters;
   ctx->norb.assign(cluster_norb, cluster_norb + n_clusters);
@@ -449,28 +538,29 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   }
   ctx->opb.assign(block_table, block_table + n_blocks * kOpbCols);
   const int s = ctx->nmax + 1;
-  std::vector<int32_t> index(size_t(n_clusters) * kNumOps * s * s * s * s, -1);
-  std::vector<BlockInfo> blocks(n_blocks);
+  ctx->h_blk_index.assign(size_t(n_clusters) * kNumOps * s * s * s * s, -1);
+  ctx->h_blocks.assign(n_blocks, BlockInfo{});
   for (int64_t b = 0; b < n_blocks; ++b) {
     const int64_t* r = &ctx->opb[b * kOpbCols];
     FCG_REQUIRE(r[0] >= 0 && r[0] < n_clusters && r[1] >= 0 && r[1] < kNumOps, FCG_EINVAL,
                 "block table: bad cluster or op id");
     for (int i = 2; i < 6; ++i)
       FCG_REQUIRE(r[i] >= 0 && r[i] <= ctx->norb[r[0]], FCG_EINVAL, "block table: bad Fock sector");
-    FCG_REQUIRE(r[6] > 0 && r[7] > 0 && r[8] > 0 && r[7] <= 256 && r[8] <= 256, FCG_ELIMIT,
-                "block table: block dims must be in [1, 256]");
+    FCG_REQUIRE(r[6] > 0 && r[7] > 0 && r[8] > 0 && r[6] <= 4096 && r[7] <= 256 && r[8] <= 256, FCG_ELIMIT,
+                "block table: block dims out of range");
     FCG_REQUIRE(r[9] >= 0 && r[9] + r[6] * r[7] * r[8] <= n_data, FCG_EINVAL, "block table: data out of range");
-    int64_t i = ((((r[0] * kNumOps + r[1]) * s + r[2]) * s + r[3]) * s + r[4]) * s + r[5];
-    index[i] = int32_t(b);
-    blocks[b] = BlockInfo{r[9], int32_t(r[6]), int32_t(r[7]), int32_t(r[8]), 0};
+    int64_t i = dense_block_index(s, int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5]));
+    ctx->h_blk_index[i] = int32_t(b);
+    ctx->h_blocks[b] = BlockInfo{r[9], int32_t(r[6]), int32_t(r[7]), int32_t(r[8]), 0};
   }
   std::vector<float> d32(data, data + n_data);
   FCG_CUDA(ctx->d_op64.upload(data, n_data, ctx->stream));
   FCG_CUDA(ctx->d_op32.upload(d32.data(), n_data, ctx->stream));
-  FCG_CUDA(ctx->d_blocks.upload(blocks.data(), blocks.size(), ctx->stream));
-  FCG_CUDA(ctx->d_blk_index.upload(index.data(), index.size(), ctx->stream));
+  FCG_CUDA(ctx->d_blocks.upload(ctx->h_blocks.data(), ctx->h_blocks.size(), ctx->stream));
+  FCG_CUDA(ctx->d_blk_index.upload(ctx->h_blk_index.data(), ctx->h_blk_index.size(), ctx->stream));
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_ops = true;
+  ctx->have_terms = false;
   ctx->have_state = false;
   return FCG_OK;
 }
@@ -482,6 +572,8 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   FCG_REQUIRE(term_table && transfers && (ints || n_ints == 0) && n_terms >= 0 && n_transfers > 0, FCG_EINVAL,
               "bad term arguments");
   FCG_CUDA(cudaSetDevice(ctx->device));
+  ctx->have_terms = false;
+  ctx->have_state = false;
   ctx->n_terms = n_terms;
   ctx->trm.assign(term_table, term_table + int64_t(n_terms) * kTrmCols);
   ctx->n_trans = n_transfers;
@@ -503,19 +595,38 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
         FCG_REQUIRE(r[2 + o] >= 0 && r[2 + o] < ctx->N, FCG_EINVAL, "term cluster out of range");
         FCG_REQUIRE(r[6 + o] >= 0 && r[6 + o] < kNumOps, FCG_EINVAL, "term op id out of range");
         FCG_REQUIRE(o == 0 || r[2 + o] > r[1 + o], FCG_EINVAL, "term clusters must increase");
+        FCG_REQUIRE(r[22 + o] >= 1 && r[22 + o] <= 4096, FCG_EINVAL, "term dims out of range");
       }
       len *= r[22 + o];
     }
     tm.ints_off = int64_t(uint32_t(r[26])) | (int64_t(r[27]) << 32);
     if (r[0] > 1) FCG_REQUIRE(tm.ints_off >= 0 && tm.ints_off + len <= n_ints, FCG_EINVAL, "term ints out of range");
   }
+  std::vector<DressJob> jobs;
+  int64_t w_total = 0;
+  {
+    std::string msg = build_dress(ctx->N, ctx->norb, ctx->nmax, ctx->trm, n_terms, ctx->h_blk_index, ctx->h_blocks,
+                                  ctx->terms, ctx->dress, ctx->w_index, jobs, w_total);
+    FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+  }
+  ctx->n_w = w_total;
   std::vector<float> i32(ints, ints + n_ints);
   FCG_CUDA(ctx->d_terms.upload(ctx->terms.data(), ctx->terms.size(), ctx->stream));
   FCG_CUDA(ctx->d_ints64.upload(ints, n_ints, ctx->stream));
   FCG_CUDA(ctx->d_ints32.upload(i32.data(), n_ints, ctx->stream));
+  DevBuf<DressJob> d_jobs;
+  FCG_CUDA(d_jobs.upload(jobs.data(), jobs.size(), ctx->stream));
+  FCG_CUDA(ctx->d_w64.alloc(std::max<int64_t>(w_total, 1)));
+  FCG_CUDA(ctx->d_w32.alloc(std::max<int64_t>(w_total, 1)));
+  if (!jobs.empty()) {
+    dress_kernel<<<unsigned(jobs.size()), 256, 0, ctx->stream>>>(d_jobs.p, ctx->d_op64.p, ctx->d_ints64.p,
+                                                                 ctx->d_w64.p);
+    FCG_CUDA(cudaGetLastError());
+    to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
+    FCG_CUDA(cudaGetLastError());
+  }
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_terms = true;
-  ctx->have_state = false;
   return FCG_OK;
 }
 
@@ -525,18 +636,25 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_REQUIRE(n_cfg > 0 && fock && cfg, FCG_EINVAL, "empty state");
   FCG_CUDA(cudaSetDevice(ctx->device));
   auto t0 = std::chrono::steady_clock::now();
-  std::string msg = build_plan(ctx->N, ctx->norb, ctx->trm, ctx->n_terms, ctx->trans, ctx->n_trans, n_cfg, fock,
-                               cfg, ctx->plan);
+  ProblemInfo pi;
+  pi.N = ctx->N;
+  pi.norb = ctx->norb;
+  pi.nmax = ctx->nmax;
+  pi.trm = &ctx->trm;
+  pi.n_terms = ctx->n_terms;
+  pi.trans = &ctx->trans;
+  pi.n_trans = ctx->n_trans;
+  pi.blk_index = &ctx->h_blk_index;
+  pi.blocks = &ctx->h_blocks;
+  pi.dress = &ctx->dress;
+  pi.w_index = &ctx->w_index;
+  ctx->have_state = false;
+  std::string msg = build_plan(pi, n_cfg, fock, cfg, ctx->plan);
   FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
-  for (int64_t i = 0; i < n_cfg; ++i)
-    for (int c = 0; c < ctx->N; ++c) {
-      int16_t fa = fock[(i * ctx->N + c) * 2], fbb = fock[(i * ctx->N + c) * 2 + 1];
-      FCG_REQUIRE(fa <= ctx->norb[c] && fbb <= ctx->norb[c], FCG_EINVAL, "Fock sector exceeds cluster size");
-    }
   const Plan& P = ctx->plan;
   std::vector<int32_t> row_sector(n_cfg);
-  for (size_t s = 0; s < P.sec_start.size(); ++s)
-    for (int64_t i = 0; i < P.sec_count[s]; ++i) row_sector[P.sec_start[s] + i] = int32_t(s);
+  for (size_t sct = 0; sct < P.sec_start.size(); ++sct)
+    for (int64_t i = 0; i < P.sec_count[sct]; ++i) row_sector[P.sec_start[sct] + i] = int32_t(sct);
   ctx->n_cfg = n_cfg;
   FCG_CUDA(ctx->d_cfg.upload(cfg, size_t(n_cfg) * ctx->N, ctx->stream));
   FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
@@ -544,7 +662,7 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));
   FCG_CUDA(ctx->d_prefix.upload(P.prefix.data(), P.prefix.size(), ctx->stream));
   FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
-  FCG_CUDA(ctx->d_term_pool.upload(P.term_pool.data(), P.term_pool.size(), ctx->stream));
+  FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   auto t1 = std::chrono::steady_clock::now();
@@ -553,6 +671,8 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   ctx->stats.n_work_items = int64_t(P.items.size());
   ctx->stats.n_triples = P.n_triples;
   ctx->stats.flops_reference = P.flops_ref;
+  ctx->stats.flops_executed = P.flops_dressed;
+  ctx->stats.dressed_elements = ctx->n_w;
   ctx->stats.plan_seconds = std::chrono::duration<double>(t1 - t0).count();
   ctx->have_state = true;
   return FCG_OK;
@@ -561,8 +681,8 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
 }  // extern "C"
 
 template <typename T>
-static int launch_closed(fcg_ctx* ctx, int R, const T* op, const T* ints, const T* cin, T* sig) {
-  SigmaParams p = make_params(ctx, R);
+static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig) {
+  SigmaParams p = make_sigma_params(ctx, R);
   FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
   int launches = 0;
   if (p.n_triples > 0) {
@@ -570,10 +690,10 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* op, const T* ints, const 
     FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many triples for one launch");
     FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     switch (R) {
-      case 1: closed_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, op, ints, cin, sig); break;
-      case 2: closed_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, op, ints, cin, sig); break;
-      case 4: closed_sigma_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, op, ints, cin, sig); break;
-      default: closed_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, op, ints, cin, sig); break;
+      case 1: closed_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      case 2: closed_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      case 4: closed_sigma_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      default: closed_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
     }
     FCG_CUDA(cudaGetLastError());
     FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
@@ -596,14 +716,14 @@ static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_s
     FCG_CUDA(ctx->d_c64.alloc(nR));
     FCG_CUDA(ctx->d_s64.alloc(nR));
     pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c64.p, n, R);
-    rc = launch_closed<double>(ctx, R, ctx->d_op64.p, ctx->d_ints64.p, ctx->d_c64.p, ctx->d_s64.p);
+    rc = launch_closed<double>(ctx, R, ctx->d_w64.p, ctx->d_op64.p, ctx->d_c64.p, ctx->d_s64.p);
     if (rc) return rc;
     unpack_out_kernel<double><<<g, 256, 0, ctx->stream>>>(ctx->d_s64.p, d_sigma, n, R);
   } else {
     FCG_CUDA(ctx->d_c32.alloc(nR));
     FCG_CUDA(ctx->d_s32.alloc(nR));
     pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c32.p, n, R);
-    rc = launch_closed<float>(ctx, R, ctx->d_op32.p, ctx->d_ints32.p, ctx->d_c32.p, ctx->d_s32.p);
+    rc = launch_closed<float>(ctx, R, ctx->d_w32.p, ctx->d_op32.p, ctx->d_c32.p, ctx->d_s32.p);
     if (rc) return rc;
     unpack_out_kernel<float><<<g, 256, 0, ctx->stream>>>(ctx->d_s32.p, d_sigma, n, R);
   }
@@ -652,19 +772,17 @@ int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd) {
   FCG_CUDA(cudaSetDevice(ctx->device));
   const int64_t n = ctx->n_cfg;
   FCG_CUDA(ctx->d_hd.alloc(n));
-  SigmaParams p = make_params(ctx, 1);
+  DiagParams p = make_diag_params(ctx);
   const unsigned g = unsigned((n + 127) / 128);
   if (op_id < 0) {
     diag_terms_kernel<<<g, 128, 0, ctx->stream>>>(p, ctx->d_op64.p, ctx->d_ints64.p, ctx->d_zero_terms.p,
-                                                  int(ctx->plan.zero_terms.size()), ctx->d_row_sector.p, n,
-                                                  ctx->d_hd.p);
+                                                  int(ctx->plan.zero_terms.size()), n, ctx->d_hd.p);
     FCG_CUDA(cudaGetLastError());
   } else {
     DevBuf<int> missing;
     FCG_CUDA(missing.alloc(1));
     FCG_CUDA(cudaMemsetAsync(missing.p, 0, sizeof(int), ctx->stream));
-    diag_op_kernel<<<g, 128, 0, ctx->stream>>>(p, ctx->d_op64.p, op_id, ctx->d_row_sector.p, n, ctx->d_hd.p,
-                                               missing.p);
+    diag_op_kernel<<<g, 128, 0, ctx->stream>>>(p, ctx->d_op64.p, op_id, n, ctx->d_hd.p, missing.p);
     FCG_CUDA(cudaGetLastError());
     int miss = 0;
     FCG_CUDA(cudaMemcpyAsync(&miss, missing.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));

@@ -33,41 +33,107 @@ struct TermInfo {
   int8_t pad[3];
 };
 
+// How a term is "dressed": its integrals are contracted once per problem with the TDM
+// of one active cluster (the one with the longest orbital multi-index), giving
+//   W[(rest), b, k] = sum_i ints[.. i ..] G_dressed[i, b, k]
+// for every (bra, ket) local-state pair of every sector pair of that cluster.  The
+// remaining clusters' TDM columns are contracted per matrix element.
+struct TermDress {
+  int pos;            // dressed position in the term (0..nbody-1); -1 for 1-body terms
+  int rest_len;       // product of the other dims
+  int nrem;           // nbody - 1
+  int rem_pos[3];     // the other positions, in order
+  int rem_dim[3];
+};
+
+// Per (sector pair, term): everything one matrix element needs besides the local states.
+struct TermSector {
+  int64_t w_off;      // W block base in the dressed array (1-body: the H block)
+  int64_t g_off[3];   // TDM block base of the remaining clusters
+  int32_t w_mb;       // bra states of the dressed cluster's block
+  int32_t g_mb[3];    // bra states of the remaining clusters' blocks
+  int16_t rest_len;   // W column length
+  int16_t g_dim[3];   // orbital multi-index length of the remaining clusters
+  int8_t cw;          // dressed cluster
+  int8_t cr[3];       // remaining clusters
+  int8_t nrem;        // number of remaining clusters (0..3)
+  int8_t sign;        // compute_terms_state_sign for the ket sector (+1 / -1)
+  int8_t pad[10];
+};
+static_assert(sizeof(TermSector) == 72, "TermSector layout");
+
 // A closed-sigma work item: every (bra in group, ket in group, term in list) triple.
 struct WorkItem {
   int32_t bra_off;  // offset of the bra group in the permutation pool
   int32_t ket_off;  // offset of the ket group in the permutation pool
   int32_t nb;       // bra group size
   int32_t nk;       // ket group size
-  int32_t tl_off;   // offset of the term list in the term pool
+  int32_t ts_off;   // offset of the term list in the TermSector pool
   int32_t nt;       // number of terms
-  int32_t sb;       // bra sector id
-  int32_t sk;       // ket sector id
+};
+
+// One W block to compute (fcg_set_terms): term t dressed with TDM block g of its dressed cluster.
+struct DressJob {
+  int64_t w_off;
+  int64_t g_off;
+  int64_t ints_off;
+  int32_t rest_len, mb, mk, nq;  // nq: dressed orbital multi-index length
+  int32_t stride_q;              // ints stride of the dressed index
+  int32_t nrem;
+  int32_t rem_dim[3];
+  int32_t rem_stride[3];
+  int32_t one_body;  // 1: copy the H block
+  int32_t pad;
+};
+
+// Problem description the planner needs (host copies).
+struct ProblemInfo {
+  int N = 0;
+  std::vector<int> norb;
+  int nmax = 0;
+  const std::vector<int32_t>* trm = nullptr;
+  int n_terms = 0;
+  const std::vector<int16_t>* trans = nullptr;
+  int n_trans = 0;
+  const std::vector<int32_t>* blk_index = nullptr;  // dense (c, op, fba, fbb, fka, fkb) -> block
+  const std::vector<BlockInfo>* blocks = nullptr;
+  const std::vector<TermDress>* dress = nullptr;
+  const std::vector<int64_t>* w_index = nullptr;    // [term][fb_a][fb_b] of the dressed cluster -> W offset
 };
 
 // Host-side plan of the closed sigma for one state.
 struct Plan {
   int N = 0;
   int64_t n_cfg = 0;
-  // sectors (contiguous runs of rows)
   std::vector<int64_t> sec_start, sec_count;
   std::vector<int16_t> sec_fock;  // n_sec x N x 2
-  // grouping pool: rows of every (sector, active set) sorted by spectator key
   std::vector<int32_t> perm_pool;
-  // term lists per (transfer, active set)
-  std::vector<int32_t> term_pool;
-  // work items and the triple prefix sum
+  std::vector<TermSector> ts_pool;
   std::vector<WorkItem> items;
   std::vector<int64_t> prefix;  // n_items + 1
   int64_t n_triples = 0;
-  int64_t flops_ref = 0;
-  // zero-transfer term list (diagonal)
+  int64_t flops_ref = 0;        // sum over triples of 2*len(ints) (the reference's count)
+  int64_t flops_dressed = 0;    // multiply-adds actually done per sigma (x2), excluding the R update
   std::vector<int32_t> zero_terms;
 };
 
-// Builds the plan; returns an empty string on success or an error message.
-std::string build_plan(int N, const std::vector<int>& norb, const std::vector<int32_t>& trm, int n_terms,
-                       const std::vector<int16_t>& trans, int n_trans, int64_t n_cfg, const int16_t* fock,
-                       const int16_t* cfg, Plan& plan);
+#ifdef __CUDACC__
+#define FCG_HD __host__ __device__
+#else
+#define FCG_HD
+#endif
+
+FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int fbb, int fka, int fkb) {
+  return ((((int64_t(c) * kNumOps + op) * nmax1 + fba) * nmax1 + fbb) * nmax1 + fka) * nmax1 + fkb;
+}
+
+std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& plan);
+
+// Dressing plan of every term (which cluster is dressed, the W block of each of its
+// TDM blocks); fills dress, w_index ([term][fb_a][fb_b] -> W offset or -1), jobs, w_total.
+std::string build_dress(int N, const std::vector<int>& norb, int nmax, const std::vector<int32_t>& trm, int n_terms,
+                        const std::vector<int32_t>& blk_index, const std::vector<BlockInfo>& blocks,
+                        const std::vector<TermInfo>& terms, std::vector<TermDress>& dress,
+                        std::vector<int64_t>& w_index, std::vector<DressJob>& jobs, int64_t& w_total);
 
 }  // namespace fcg

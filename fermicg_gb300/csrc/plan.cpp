@@ -43,10 +43,13 @@ struct Group {
 
 }  // namespace
 
-std::string build_plan(int N, const std::vector<int>& norb, const std::vector<int32_t>& trm, int n_terms,
-                       const std::vector<int16_t>& trans, int n_trans, int64_t n_cfg, const int16_t* fock,
-                       const int16_t* cfg, Plan& P) {
-  (void)norb;
+std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
+  const int N = pi.N;
+  const std::vector<int32_t>& trm = *pi.trm;
+  const int n_terms = pi.n_terms;
+  const std::vector<int16_t>& trans = *pi.trans;
+  const int n_trans = pi.n_trans;
+  const int nmax1 = pi.nmax + 1;
   P = Plan();
   P.N = N;
   P.n_cfg = n_cfg;
@@ -72,6 +75,14 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
   }
   for (int64_t i = 0; i < n_cfg * N; ++i)
     if (cfg[i] < 0 || cfg[i] > 255) return "local state index outside [0, 255]";
+  for (int64_t i = 0; i < n_cfg; ++i)
+    for (int c = 0; c < N; ++c) {
+      int fa = fock[(i * N + c) * 2], fbb = fock[(i * N + c) * 2 + 1];
+      if (fa > pi.norb[c] || fbb > pi.norb[c]) return "Fock sector exceeds cluster size";
+      int bl = (*pi.blk_index)[dense_block_index(nmax1, c, kOpH, fa, fbb, fa, fbb)];
+      if (bl < 0) return "a row uses a Fock sector with no local basis";
+      if (cfg[i * N + c] >= (*pi.blocks)[bl].mb) return "local state index beyond the sector's basis";
+    }
   const int64_t n_sec = int64_t(P.sec_start.size());
 
   // ---- active sets and term lists per (transfer, set) ----------------------
@@ -79,8 +90,7 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
   std::unordered_map<uint32_t, int> mask_id;
   struct TL {
     int s;
-    int32_t off, n;
-    int64_t flop;  // sum over the list of 2*len(ints)
+    std::vector<int32_t> terms;
   };
   std::vector<std::vector<TL>> tls(n_trans);
   {
@@ -106,15 +116,7 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
     for (int tr = 0; tr < n_trans; ++tr)
       for (int s = 0; s < int(by[tr].size()); ++s) {
         if (by[tr][s].empty()) continue;
-        TL tl{s, int32_t(P.term_pool.size()), int32_t(by[tr][s].size()), 0};
-        for (int t : by[tr][s]) {
-          P.term_pool.push_back(t);
-          int nb = TT(trm, t, 0);
-          int64_t len = 1;
-          for (int o = 0; o < 4; ++o) len *= TT(trm, t, 22 + o);
-          tl.flop += nb > 1 ? 2 * len : 0;
-        }
-        tls[tr].push_back(tl);
+        tls[tr].push_back(TL{s, by[tr][s]});
       }
     for (int tr = 0; tr < n_trans; ++tr) {
       bool zero = true;
@@ -165,13 +167,21 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
   }
 
   // ---- work items: merge-join per (bra sector, transfer, set) --------------
-  // items are collected per bra sector and concatenated in sector order, so the
-  // plan (and the kernel's summation order) does not depend on thread timing
+  // items and term-sector records are collected per bra sector and concatenated in
+  // sector order, so the plan (and the kernel's summation order) does not depend on
+  // thread timing
   std::vector<std::vector<WorkItem>> tItems(n_sec);
-  std::vector<int64_t> tFlop(n_sec, 0);
+  std::vector<std::vector<TermSector>> tTS(n_sec);
+  std::vector<int64_t> tFlop(n_sec, 0), tFlopD(n_sec, 0);
+  const std::vector<TermDress>& dress = *pi.dress;
+  const std::vector<int64_t>& w_index = *pi.w_index;
+  const std::vector<int32_t>& blk = *pi.blk_index;
+  const std::vector<BlockInfo>& blocks = *pi.blocks;
 #pragma omp parallel
   {
     std::vector<int16_t> fk(2 * N);
+    std::vector<TermSector> tsl;
+    std::vector<int64_t> tflop, tflopd;
 #pragma omp for schedule(dynamic, 1)
     for (int64_t sb = 0; sb < n_sec; ++sb) {
       const int16_t* fb = &P.sec_fock[sb * 2 * N];
@@ -184,6 +194,66 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
         if (it == sec_of.end()) continue;
         int64_t sk = it->second;
         for (const TL& tl : tls[tr]) {
+          // term-sector records of this (bra sector, ket sector, term list)
+          tsl.clear();
+          tflop.clear();
+          tflopd.clear();
+          for (int t : tl.terms) {
+            const TermDress& d = dress[t];
+            const int nbody = TT(trm, t, 0);
+            TermSector ts{};
+            int cw = TT(trm, t, 2 + (d.pos < 0 ? 0 : d.pos));
+            int opw = TT(trm, t, 6 + (d.pos < 0 ? 0 : d.pos));
+            int bw = blk[dense_block_index(nmax1, cw, opw, fb[2 * cw], fb[2 * cw + 1], fk[2 * cw], fk[2 * cw + 1])];
+            int64_t woff = w_index[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
+            if (bw < 0 || woff < 0) continue;  // a missing TDM block contributes nothing
+            ts.w_off = woff;
+            ts.w_mb = blocks[bw].mb;
+            ts.cw = int8_t(cw);
+            ts.rest_len = int16_t(nbody == 1 ? 1 : d.rest_len);
+            ts.nrem = int8_t(nbody == 1 ? 0 : d.nrem);
+            bool ok = true;
+            for (int r = 0; r < ts.nrem; ++r) {
+              int o = d.rem_pos[r];
+              int c = TT(trm, t, 2 + o), op = TT(trm, t, 6 + o);
+              int bl = blk[dense_block_index(nmax1, c, op, fb[2 * c], fb[2 * c + 1], fk[2 * c], fk[2 * c + 1])];
+              if (bl < 0) {
+                ok = false;
+                break;
+              }
+              ts.g_off[r] = blocks[bl].off;
+              ts.g_mb[r] = blocks[bl].mb;
+              ts.g_dim[r] = int16_t(blocks[bl].nidx);
+              ts.cr[r] = int8_t(c);
+            }
+            if (!ok) continue;
+            // compute_terms_state_sign (type_ClusteredTerm.jl:181-196) on the ket sector
+            int sgn = 0;
+            for (int o = 0; o < nbody; ++o)
+              if (TT(trm, t, 18 + o)) {
+                int ne = 0;
+                for (int ci = 0; ci < TT(trm, t, 2 + o); ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
+                sgn ^= ne & 1;
+              }
+            ts.sign = int8_t(nbody == 1 ? 1 : (sgn ? -1 : 1));
+            int64_t len = 1;
+            for (int o = 0; o < 4; ++o) len *= TT(trm, t, 22 + o);
+            tflop.push_back(nbody > 1 ? 2 * len : 0);
+            int64_t fma = 0;
+            if (ts.nrem == 1) fma = ts.rest_len;
+            if (ts.nrem == 2) fma = ts.rest_len + ts.g_dim[1];
+            if (ts.nrem == 3) fma = ts.rest_len + int64_t(ts.g_dim[1]) * ts.g_dim[2] + ts.g_dim[2];
+            tflopd.push_back(2 * fma);
+            tsl.push_back(ts);
+          }
+          if (tsl.empty()) continue;
+          int64_t flop = 0, flopd = 0;
+          for (size_t i = 0; i < tsl.size(); ++i) {
+            flop += tflop[i];
+            flopd += tflopd[i];
+          }
+          const int32_t ts_off = int32_t(tTS[sb].size());  // relative; rebased at concatenation
+          tTS[sb].insert(tTS[sb].end(), tsl.begin(), tsl.end());
           const auto& gb = groups[sb * n_sets + tl.s];
           const auto& gk = groups[sk * n_sets + tl.s];
           int64_t pb = fs_perm_off[sb * n_sets + tl.s], pk = fs_perm_off[sk * n_sets + tl.s];
@@ -199,12 +269,11 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
               w.ket_off = int32_t(pk + gk[b].start);
               w.nb = gb[a].count;
               w.nk = gk[b].count;
-              w.tl_off = tl.off;
-              w.nt = tl.n;
-              w.sb = int32_t(sb);
-              w.sk = int32_t(sk);
+              w.ts_off = ts_off;
+              w.nt = int32_t(tsl.size());
               tItems[sb].push_back(w);
-              tFlop[sb] += int64_t(w.nb) * w.nk * tl.flop;
+              tFlop[sb] += int64_t(w.nb) * w.nk * flop;
+              tFlopD[sb] += int64_t(w.nb) * w.nk * flopd;
               ++a;
               ++b;
             }
@@ -213,15 +282,98 @@ std::string build_plan(int N, const std::vector<int>& norb, const std::vector<in
       }
     }
   }
-  size_t tot = 0;
-  for (auto& v : tItems) tot += v.size();
+  size_t tot = 0, tots = 0;
+  for (int64_t sb = 0; sb < n_sec; ++sb) {
+    tot += tItems[sb].size();
+    tots += tTS[sb].size();
+  }
+  if (tots >= (size_t(1) << 31)) return "term-sector pool exceeds 2^31 records";
   P.items.reserve(tot);
-  for (auto& v : tItems) P.items.insert(P.items.end(), v.begin(), v.end());
-  for (int64_t f : tFlop) P.flops_ref += f;
+  P.ts_pool.reserve(tots);
+  for (int64_t sb = 0; sb < n_sec; ++sb) {
+    const int32_t base = int32_t(P.ts_pool.size());
+    for (WorkItem w : tItems[sb]) {
+      w.ts_off += base;
+      P.items.push_back(w);
+    }
+    P.ts_pool.insert(P.ts_pool.end(), tTS[sb].begin(), tTS[sb].end());
+    P.flops_ref += tFlop[sb];
+    P.flops_dressed += tFlopD[sb];
+  }
   P.prefix.assign(P.items.size() + 1, 0);
   for (size_t i = 0; i < P.items.size(); ++i)
     P.prefix[i + 1] = P.prefix[i] + int64_t(P.items[i].nb) * P.items[i].nk * P.items[i].nt;
   P.n_triples = P.prefix.back();
+  return "";
+}
+
+std::string build_dress(int N, const std::vector<int>& norb, int nmax, const std::vector<int32_t>& trm, int n_terms,
+                        const std::vector<int32_t>& blk_index, const std::vector<BlockInfo>& blocks,
+                        const std::vector<TermInfo>& terms, std::vector<TermDress>& dress,
+                        std::vector<int64_t>& w_index, std::vector<DressJob>& jobs, int64_t& w_total) {
+  (void)N;
+  const int s = nmax + 1;
+  dress.assign(n_terms, TermDress{});
+  w_index.assign(size_t(n_terms) * s * s, -1);
+  jobs.clear();
+  w_total = 0;
+  for (int t = 0; t < n_terms; ++t) {
+    const int32_t* r = &trm[int64_t(t) * kTrmCols];
+    TermDress& d = dress[t];
+    const int nb = r[0];
+    if (nb == 1) {
+      d.pos = -1;
+      d.rest_len = 1;
+      d.nrem = 0;
+    } else {
+      // contract the ints with the cluster of the longest orbital multi-index
+      d.pos = 0;
+      for (int o = 1; o < nb; ++o)
+        if (r[22 + o] > r[22 + d.pos]) d.pos = o;
+      d.nrem = nb - 1;
+      d.rest_len = 1;
+      for (int o = 0, q = 0; o < nb; ++o) {
+        if (o == d.pos) continue;
+        d.rem_pos[q] = o;
+        d.rem_dim[q] = r[22 + o];
+        d.rest_len *= r[22 + o];
+        ++q;
+      }
+      if (d.rest_len > 32767) return "dressed index too long";
+    }
+    const int pos = d.pos < 0 ? 0 : d.pos;
+    const int cw = r[2 + pos], opw = r[6 + pos];
+    int stride[4];
+    stride[0] = 1;
+    for (int o = 1; o < 4; ++o) stride[o] = stride[o - 1] * r[22 + o - 1];
+    for (int fba = 0; fba <= norb[cw]; ++fba)
+      for (int fbb = 0; fbb <= norb[cw]; ++fbb) {
+        int fka = fba - r[10 + pos], fkb = fbb - r[14 + pos];
+        if (fka < 0 || fkb < 0 || fka > norb[cw] || fkb > norb[cw]) continue;
+        int bl = blk_index[dense_block_index(s, cw, opw, fba, fbb, fka, fkb)];
+        if (bl < 0) continue;
+        const BlockInfo& B = blocks[bl];
+        if (nb > 1 && B.nidx != r[22 + pos]) return "term dims do not match the TDM block";
+        DressJob J{};
+        J.w_off = w_total;
+        J.g_off = B.off;
+        J.ints_off = terms[t].ints_off;
+        J.rest_len = d.rest_len;
+        J.mb = B.mb;
+        J.mk = B.mk;
+        J.nq = nb == 1 ? 1 : B.nidx;
+        J.stride_q = stride[pos];
+        J.nrem = d.nrem;
+        for (int q = 0; q < d.nrem; ++q) {
+          J.rem_dim[q] = d.rem_dim[q];
+          J.rem_stride[q] = stride[d.rem_pos[q]];
+        }
+        J.one_body = nb == 1;
+        jobs.push_back(J);
+        w_index[(int64_t(t) * s + fba) * s + fbb] = w_total;
+        w_total += int64_t(d.rest_len) * B.mb * B.mk;
+      }
+  }
   return "";
 }
 

@@ -46,6 +46,7 @@ SIGNATURES = {
 class Stats(ctypes.Structure):
     _fields_ = [("n_cfg", ctypes.c_int64), ("n_sectors", ctypes.c_int64), ("n_work_items", ctypes.c_int64),
                 ("n_triples", ctypes.c_int64), ("flops_reference", ctypes.c_int64),
+                ("flops_executed", ctypes.c_int64), ("dressed_elements", ctypes.c_int64),
                 ("plan_seconds", ctypes.c_double), ("last_kernel_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64)]
 

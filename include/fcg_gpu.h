@@ -53,6 +53,8 @@ typedef struct fcg_stats {
   int64_t n_work_items;     /* (bra group, ket group, term list) blocks of the closed sigma */
   int64_t n_triples;        /* (bra, ket, term) contractions of one closed sigma */
   int64_t flops_reference;  /* sum over triples of 2*len(ints) (the reference's count) */
+  int64_t flops_executed;   /* 2 x multiply-adds the dressed contraction does per sigma (R update excluded) */
+  int64_t dressed_elements; /* elements of the dressed operators W (one copy per precision) */
   double plan_seconds;      /* host time of the last fcg_state_set */
   double last_kernel_ms;    /* device time of the last sigma kernel (CUDA events) */
   int64_t kernel_launches;  /* kernels launched by the last sigma call */
