@@ -264,7 +264,7 @@ def main():
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
         "clocks": clocks,
     }
-    if rank == 0:
+    if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1
             cv, sample = cpu_reference(po, pt, f, c, v, a.cpu_seconds, thr)
@@ -272,6 +272,7 @@ def main():
                                    "sample": sample}
         except Exception as ex:  # the baseline must not kill the GPU line
             out["cpu_baseline"] = {"value": None, "error": str(ex)}
+    if rank == 0:
         print(json.dumps(out))
     if world > 1:
         torch.distributed.destroy_process_group()
