@@ -1,0 +1,141 @@
+// Context object and helpers shared by the CUDA translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "../../include/fcg_gpu.h"
+#include "fcg_internal.h"
+
+namespace fcg {
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    release();
+    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+  cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess) return e;
+    if (count == 0) return cudaSuccess;
+    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
+  }
+};
+
+}  // namespace fcg
+
+using namespace fcg;
+
+struct fcg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;      // stream every call runs on
+  cudaStream_t own_stream = nullptr;  // the context's own stream
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+  // problem
+  int N = 0;
+  std::vector<int> norb;
+  int nmax = 0;
+  bool have_ops = false, have_terms = false, have_state = false;
+  std::vector<int64_t> opb;
+  std::vector<BlockInfo> h_blocks;
+  std::vector<int32_t> h_blk_index;
+  DevBuf<double> d_op64;
+  DevBuf<float> d_op32;
+  DevBuf<BlockInfo> d_blocks;
+  DevBuf<int32_t> d_blk_index;
+  int n_terms = 0;
+  std::vector<int32_t> trm;
+  std::vector<TermInfo> terms;
+  std::vector<TermDress> dress;
+  std::vector<int64_t> w_index;
+  int64_t n_w = 0;
+  DevBuf<TermInfo> d_terms;
+  DevBuf<double> d_ints64;
+  DevBuf<float> d_ints32;
+  DevBuf<double> d_w64;
+  DevBuf<float> d_w32;
+  int n_trans = 0;
+  std::vector<int16_t> trans;
+  // state + plan
+  int64_t n_cfg = 0;
+  Plan plan;
+  DevBuf<int16_t> d_cfg;
+  DevBuf<int16_t> d_sec_fock;
+  DevBuf<int32_t> d_row_sector;
+  DevBuf<WorkItem> d_items;
+  DevBuf<int64_t> d_prefix;
+  DevBuf<int32_t> d_perm;
+  DevBuf<TermSector> d_ts;
+  DevBuf<int32_t> d_zero_terms;
+  // vectors
+  DevBuf<double> d_in64, d_out64;  // column-major staging for host calls
+  DevBuf<double> d_c64, d_s64;     // row-major fp64
+  DevBuf<float> d_c32, d_s32;      // row-major fp32
+  DevBuf<double> d_hd;
+  // screening maxima: Gmax[i, k] = max_b |G[i, b, k]| per TDM block, Wmax likewise per W block
+  std::vector<int64_t> gmax_off;   // per block
+  std::vector<int64_t> wmax_index; // parallel to w_index
+  DevBuf<double> d_gmax;
+  DevBuf<double> d_wmax;
+  // open sigma (FOIS) working set and last result
+  DevBuf<OpenTerm> d_oterms;
+  DevBuf<OpenItem> d_oitems;
+  DevBuf<int64_t> d_oprefix;
+  DevBuf<int64_t> d_ostrides;     // [n_bra_sectors][N]
+  DevBuf<int2> d_ojobs;           // kept (row, open term) pairs
+  DevBuf<int64_t> d_ojob_prefix;
+  DevBuf<unsigned long long> d_hkeys;
+  DevBuf<double> d_hvals;
+  DevBuf<unsigned long long> d_okeys;
+  DevBuf<double> d_ovals;
+  DevBuf<unsigned long long> d_counters;
+  DevBuf<unsigned char> d_scan_tmp;
+  std::vector<int16_t> open_bra_fock;   // [n_bra_sectors][N][2]
+  std::vector<int64_t> open_strides;    // [n_bra_sectors][N]
+  std::vector<int64_t> open_dims;       // [n_bra_sectors][N]
+  std::vector<unsigned long long> open_keys;
+  std::vector<double> open_vals;        // [n_out][R] row-major
+  int open_R = 0;
+  fcg_stats stats{};
+};
+
+#define FCG_CUDA(call)                                                               \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;               \
+    }                                                                                \
+  } while (0)
+
+#define FCG_REQUIRE(cond, code, msg) \
+  do {                               \
+    if (!(cond)) {                   \
+      ctx->err = (msg);              \
+      return (code);                 \
+    }                                \
+  } while (0)
+

@@ -37,109 +37,7 @@
 
 using namespace fcg;
 
-namespace {
-
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t n = 0;
-  DevBuf() = default;
-  DevBuf(const DevBuf&) = delete;
-  DevBuf& operator=(const DevBuf&) = delete;
-  ~DevBuf() { release(); }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    n = 0;
-  }
-  cudaError_t alloc(size_t count) {
-    if (count <= n && p) return cudaSuccess;
-    release();
-    size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
-    cudaError_t e = cudaMalloc(&p, bytes);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      return e;
-    }
-    n = count;
-    return cudaSuccess;
-  }
-  cudaError_t upload(const T* h, size_t count, cudaStream_t s) {
-    cudaError_t e = alloc(count);
-    if (e != cudaSuccess) return e;
-    if (count == 0) return cudaSuccess;
-    return cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s);
-  }
-};
-
-}  // namespace
-
-struct fcg_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;      // stream every call runs on
-  cudaStream_t own_stream = nullptr;  // the context's own stream
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  std::string err;
-  // problem
-  int N = 0;
-  std::vector<int> norb;
-  int nmax = 0;
-  bool have_ops = false, have_terms = false, have_state = false;
-  std::vector<int64_t> opb;
-  std::vector<BlockInfo> h_blocks;
-  std::vector<int32_t> h_blk_index;
-  DevBuf<double> d_op64;
-  DevBuf<float> d_op32;
-  DevBuf<BlockInfo> d_blocks;
-  DevBuf<int32_t> d_blk_index;
-  int n_terms = 0;
-  std::vector<int32_t> trm;
-  std::vector<TermInfo> terms;
-  std::vector<TermDress> dress;
-  std::vector<int64_t> w_index;
-  int64_t n_w = 0;
-  DevBuf<TermInfo> d_terms;
-  DevBuf<double> d_ints64;
-  DevBuf<float> d_ints32;
-  DevBuf<double> d_w64;
-  DevBuf<float> d_w32;
-  int n_trans = 0;
-  std::vector<int16_t> trans;
-  // state + plan
-  int64_t n_cfg = 0;
-  Plan plan;
-  DevBuf<int16_t> d_cfg;
-  DevBuf<int16_t> d_sec_fock;
-  DevBuf<int32_t> d_row_sector;
-  DevBuf<WorkItem> d_items;
-  DevBuf<int64_t> d_prefix;
-  DevBuf<int32_t> d_perm;
-  DevBuf<TermSector> d_ts;
-  DevBuf<int32_t> d_zero_terms;
-  // vectors
-  DevBuf<double> d_in64, d_out64;  // column-major staging for host calls
-  DevBuf<double> d_c64, d_s64;     // row-major fp64
-  DevBuf<float> d_c32, d_s32;      // row-major fp32
-  DevBuf<double> d_hd;
-  fcg_stats stats{};
-};
-
-#define FCG_CUDA(call)                                                               \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) {                                                         \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
-      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;               \
-    }                                                                                \
-  } while (0)
-
-#define FCG_REQUIRE(cond, code, msg) \
-  do {                               \
-    if (!(cond)) {                   \
-      ctx->err = (msg);              \
-      return (code);                 \
-    }                                \
-  } while (0)
+#include "fcg_ctx.cuh"
 
 // ---------------------------------------------------------------------------------------
 // device code
@@ -176,6 +74,26 @@ __global__ void dress_kernel(const DressJob* __restrict__ jobs, const double* __
 __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict__ b, int64_t n) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   for (; i < n; i += int64_t(gridDim.x) * blockDim.x) b[i] = float(a[i]);
+}
+
+// Column maxima over the bra index, used by the open-sigma screen:
+// out[i + len*k] = max_b |in[i + len*(b + mb*k)]| for every block of a list.
+struct MaxJob {
+  int64_t in_off, out_off;
+  int32_t len, mb, mk, pad;
+};
+
+__global__ void colmax_kernel(const MaxJob* __restrict__ jobs, const double* __restrict__ in,
+                              double* __restrict__ out) {
+  const MaxJob J = jobs[blockIdx.x];
+  const int64_t n = int64_t(J.len) * J.mk;
+  for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
+    const int i = int(e % J.len);
+    const int64_t k = e / J.len;
+    double m = 0.0;
+    for (int b = 0; b < J.mb; ++b) m = fmax(m, fabs(in[J.in_off + i + int64_t(J.len) * (b + int64_t(J.mb) * k)]));
+    out[J.out_off + e] = m;
+  }
 }
 
 // ---- closed sigma ------------------------------------------------------------------------
@@ -558,7 +476,25 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   FCG_CUDA(ctx->d_op32.upload(d32.data(), n_data, ctx->stream));
   FCG_CUDA(ctx->d_blocks.upload(ctx->h_blocks.data(), ctx->h_blocks.size(), ctx->stream));
   FCG_CUDA(ctx->d_blk_index.upload(ctx->h_blk_index.data(), ctx->h_blk_index.size(), ctx->stream));
-  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  {
+    std::vector<MaxJob> mj(n_blocks);
+    ctx->gmax_off.assign(n_blocks, 0);
+    int64_t tot = 0;
+    for (int64_t b = 0; b < n_blocks; ++b) {
+      const BlockInfo& B = ctx->h_blocks[b];
+      mj[b] = MaxJob{B.off, tot, B.nidx, B.mb, B.mk, 0};
+      ctx->gmax_off[b] = tot;
+      tot += int64_t(B.nidx) * B.mk;
+    }
+    DevBuf<MaxJob> d_mj;
+    FCG_CUDA(d_mj.upload(mj.data(), mj.size(), ctx->stream));
+    FCG_CUDA(ctx->d_gmax.alloc(std::max<int64_t>(tot, 1)));
+    if (n_blocks > 0) {
+      colmax_kernel<<<unsigned(n_blocks), 128, 0, ctx->stream>>>(d_mj.p, ctx->d_op64.p, ctx->d_gmax.p);
+      FCG_CUDA(cudaGetLastError());
+    }
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
   ctx->have_ops = true;
   ctx->have_terms = false;
   ctx->have_state = false;
@@ -625,7 +561,32 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
     to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
     FCG_CUDA(cudaGetLastError());
   }
-  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  {
+    // Wmax[rest, k] per W block, indexed like w_index
+    std::vector<MaxJob> mj(jobs.size());
+    ctx->wmax_index.assign(ctx->w_index.size(), -1);
+    int64_t tot = 0;
+    for (size_t j = 0; j < jobs.size(); ++j) {
+      const DressJob& J = jobs[j];
+      mj[j] = MaxJob{J.w_off, tot, J.rest_len, J.mb, J.mk, 0};
+      tot += int64_t(J.rest_len) * J.mk;
+    }
+    for (size_t i = 0; i < ctx->w_index.size(); ++i) {
+      if (ctx->w_index[i] < 0) continue;
+      // jobs are in w_off order; find the job of this W block
+      auto it = std::lower_bound(jobs.begin(), jobs.end(), ctx->w_index[i],
+                                 [](const DressJob& J, int64_t v) { return J.w_off < v; });
+      ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
+    }
+    DevBuf<MaxJob> d_mj;
+    FCG_CUDA(d_mj.upload(mj.data(), mj.size(), ctx->stream));
+    FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
+    if (!jobs.empty()) {
+      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj.p, ctx->d_w64.p, ctx->d_wmax.p);
+      FCG_CUDA(cudaGetLastError());
+    }
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // before d_mj / d_jobs are freed
+  }
   ctx->have_terms = true;
   return FCG_OK;
 }

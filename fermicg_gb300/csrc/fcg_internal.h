@@ -62,6 +62,26 @@ struct TermSector {
 };
 static_assert(sizeof(TermSector) == 72, "TermSector layout");
 
+// Open (FOIS) sigma: one term acting from one ket sector into one bra sector
+// (open_matvec_thread, src/tpsci_matvec_thread.jl:11-263).
+struct OpenTerm {
+  TermSector ts;        // dressed W / remaining TDM columns, ket-sector sign
+  int64_t wmax_off;     // Wmax[rest, k] at wmax_off + rest + rest_len*k
+  int64_t gmax_off[3];  // Gmax[i, k] of the remaining clusters at off + i + g_dim*k
+  int32_t bsec;         // bra sector id
+  int32_t out_count;    // product of the bra dims of the active clusters
+  int16_t mb_act[4];    // bra dims of the active clusters, order [dressed, remaining...]
+  int8_t c_act[4];      // cluster ids in the same order
+  int8_t n_act;
+  int8_t pad[3];
+};
+static_assert(sizeof(OpenTerm) == 128, "OpenTerm layout");
+
+// Open sigma work item: every (ket row in [row0, row0+nrow), term in [ot_off, ot_off+nt)) job.
+struct OpenItem {
+  int32_t row0, nrow, ot_off, nt;
+};
+
 // A closed-sigma work item: every (bra in group, ket in group, term in list) triple.
 struct WorkItem {
   int32_t bra_off;  // offset of the bra group in the permutation pool
@@ -128,6 +148,10 @@ FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int f
 }
 
 std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& plan);
+
+// The term-sector record of term t between bra sector fb and ket sector fk (N x 2 each);
+// false when a TDM block the term needs does not exist there.
+bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int16_t* fk, TermSector& ts);
 
 // Dressing plan of every term (which cluster is dressed, the W block of each of its
 // TDM blocks); fills dress, w_index ([term][fb_a][fb_b] -> W offset or -1), jobs, w_total.

@@ -1,0 +1,508 @@
+// Open (first-order interacting space) sigma on the GPU: open_matvec_thread
+// (src/tpsci_matvec_thread.jl:11-885) behind fcg_sigma_open / fcg_sigma_open_fetch.
+//
+// For every ket row of the state and every term whose target sector passes the job
+// filter (:26-56), every bra local-state tuple of the term's active clusters gets
+//     x = sign * sum W[(rest), b_w, k_w] prod_c G_c[i_c, b_c, k_c]
+// and contributes x * c_ket to sigma[bra config] when |x| > thresh / max_r |c_ket[r]|,
+// the per-contribution test of _collect_significant_thread! (:830-885).
+//
+// Pipeline (one stream):
+//   screen_kernel   one thread per (ket row, term) job: a rigorous max-norm bound
+//                   sum_rest Wmax * prod Gmax skips jobs whose every contribution would
+//                   fail the threshold (the role of upper_bound_thread, :897-1023; skipping
+//                   changes no result), the survivors are compacted;
+//   CUB scan        output-tuple prefix over the surviving jobs;
+//   expand_kernel   one thread per (job, bra tuple): contraction, threshold, then an
+//                   insert into an open-addressed table keyed by (bra sector, mixed-radix
+//                   local-state index) with atomic accumulation of the R values;
+//   compact_kernel  occupied slots -> (key, values).
+// A table that overflows its probe limit sets a flag and the call is repeated with a
+// table twice as large.
+#include <cub/cub.cuh>
+
+#include <cmath>
+#include <unordered_map>
+
+#include "fcg_ctx.cuh"
+
+using namespace fcg;
+
+namespace {
+
+constexpr unsigned long long kEmpty = ~0ull;
+constexpr int kMaxProbe = 1 << 16;
+constexpr int kKeyIdxBits = 40;
+
+// counters: [0] kept jobs, [1] elements of kept jobs, [2] table overflow, [3] output rows
+struct OpenParams {
+  const OpenTerm* ot;
+  const OpenItem* items;
+  const int64_t* prefix;  // job prefix over items
+  int64_t n_items;
+  int64_t n_jobs;
+  const int16_t* cfg;
+  const double* c;  // row-major [n_cfg][R]
+  const int64_t* strides;  // [n_bra_sectors][N]
+  int N;
+  int R;
+  double thresh;
+};
+
+__device__ __forceinline__ int64_t find_item(const int64_t* prefix, int64_t lo, int64_t hi, int64_t x) {
+  while (lo < hi) {
+    int64_t mid = (lo + hi + 1) >> 1;
+    if (__ldg(prefix + mid) <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ double row_maxabs(const double* c, int R) {
+  double m = 0.0;
+  for (int r = 0; r < R; ++r) m = fmax(m, fabs(c[r]));
+  return m;
+}
+
+// rigorous bound on max over bra tuples of |x| for one (ket, term) job
+__device__ double job_bound(const OpenTerm& o, const double* __restrict__ wmax, const double* __restrict__ gmax,
+                            const int16_t* ck) {
+  const TermSector& ts = o.ts;
+  const double* wm = wmax + o.wmax_off + int64_t(ts.rest_len) * ck[ts.cw];
+  if (ts.nrem == 0) return wm[0];
+  const double* g0 = gmax + o.gmax_off[0] + int64_t(ts.g_dim[0]) * ck[ts.cr[0]];
+  const int d0 = ts.g_dim[0];
+  double bnd = 0.0;
+  if (ts.nrem == 1) {
+    for (int i = 0; i < d0; ++i) bnd += wm[i] * g0[i];
+    return bnd;
+  }
+  const double* g1 = gmax + o.gmax_off[1] + int64_t(ts.g_dim[1]) * ck[ts.cr[1]];
+  const int d1 = ts.g_dim[1];
+  if (ts.nrem == 2) {
+    for (int j = 0; j < d1; ++j) {
+      double a = 0.0;
+      for (int i = 0; i < d0; ++i) a += wm[i + d0 * j] * g0[i];
+      bnd += a * g1[j];
+    }
+    return bnd;
+  }
+  const double* g2 = gmax + o.gmax_off[2] + int64_t(ts.g_dim[2]) * ck[ts.cr[2]];
+  const int d2 = ts.g_dim[2];
+  for (int l = 0; l < d2; ++l) {
+    double al = 0.0;
+    for (int j = 0; j < d1; ++j) {
+      double a = 0.0;
+      for (int i = 0; i < d0; ++i) a += wm[i + d0 * (j + d1 * l)] * g0[i];
+      al += a * g1[j];
+    }
+    bnd += al * g2[l];
+  }
+  return bnd;
+}
+
+__global__ void screen_kernel(OpenParams p, const double* __restrict__ wmax, const double* __restrict__ gmax,
+                              int2* __restrict__ kept, unsigned long long* __restrict__ counters) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= p.n_jobs) return;
+  const int64_t it = find_item(p.prefix, 0, p.n_items - 1, j);
+  const OpenItem I = p.items[it];
+  const int64_t local = j - p.prefix[it];
+  const int ti = int(local % I.nt);
+  const int row = I.row0 + int(local / I.nt);
+  const OpenTerm& o = p.ot[I.ot_off + ti];
+  const double maxc = row_maxabs(p.c + int64_t(row) * p.R, p.R);
+  if (!(maxc > 0.0)) return;
+  const double bnd = job_bound(o, wmax, gmax, p.cfg + int64_t(row) * p.N);
+  // keep unless every |x| <= bnd < thresh / maxc (a 1e-9 margin covers the bound's rounding)
+  if (!(bnd * (1.0 + 1e-9) > p.thresh / maxc)) return;
+  const unsigned long long pos = atomicAdd(counters + 0, 1ull);
+  kept[pos] = make_int2(row, I.ot_off + ti);
+  atomicAdd(counters + 1, (unsigned long long)o.out_count);
+}
+
+__global__ void job_counts_kernel(const int2* __restrict__ kept, int64_t n, const OpenTerm* __restrict__ ot,
+                                  int64_t* __restrict__ counts) {
+  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  counts[j] = ot[kept[j].y].out_count;
+}
+
+__device__ __forceinline__ void table_add(unsigned long long* keys, double* vals, unsigned long long cap_mask,
+                                          unsigned long long key, const double* add, int R,
+                                          unsigned long long* overflow) {
+  unsigned long long h = key * 0x9E3779B97F4A7C15ull;
+  h ^= h >> 29;
+  unsigned long long slot = h & cap_mask;
+  for (int probe = 0; probe < kMaxProbe; ++probe) {
+    unsigned long long cur = keys[slot];
+    if (cur == kEmpty) {
+      unsigned long long prev = atomicCAS(keys + slot, kEmpty, key);
+      if (prev == kEmpty || prev == key) cur = key;
+      else cur = prev;
+    }
+    if (cur == key) {
+      for (int r = 0; r < R; ++r) atomicAdd(vals + slot * R + r, add[r]);
+      return;
+    }
+    slot = (slot + 1) & cap_mask;
+  }
+  atomicExch(overflow, 1ull);
+}
+
+__global__ void expand_kernel(OpenParams p, const int2* __restrict__ kept, const int64_t* __restrict__ jprefix,
+                              int64_t n_kept, int64_t n_elem, const double* __restrict__ w,
+                              const double* __restrict__ op, unsigned long long* __restrict__ keys,
+                              double* __restrict__ vals, unsigned long long cap_mask,
+                              unsigned long long* __restrict__ counters) {
+  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (e >= n_elem) return;
+  const int64_t j = find_item(jprefix, 0, n_kept - 1, e);
+  const int2 job = kept[j];
+  const OpenTerm& o = p.ot[job.y];
+  const TermSector& ts = o.ts;
+  int64_t loc = e - jprefix[j];
+  int b[4];
+  for (int a = 0; a < o.n_act; ++a) {
+    b[a] = int(loc % o.mb_act[a]);
+    loc /= o.mb_act[a];
+  }
+  const int16_t* ck = p.cfg + int64_t(job.x) * p.N;
+  const double* wc = w + ts.w_off + int64_t(ts.rest_len) * (b[0] + int64_t(ts.w_mb) * ck[ts.cw]);
+  double x;
+  if (ts.nrem == 0) {
+    x = wc[0];
+  } else {
+    const double* g0 = op + ts.g_off[0] + int64_t(ts.g_dim[0]) * (b[1] + int64_t(ts.g_mb[0]) * ck[ts.cr[0]]);
+    const int d0 = ts.g_dim[0];
+    x = 0.0;
+    if (ts.nrem == 1) {
+      for (int i = 0; i < d0; ++i) x = fma(wc[i], g0[i], x);
+    } else {
+      const double* g1 = op + ts.g_off[1] + int64_t(ts.g_dim[1]) * (b[2] + int64_t(ts.g_mb[1]) * ck[ts.cr[1]]);
+      const int d1 = ts.g_dim[1];
+      if (ts.nrem == 2) {
+        for (int jj = 0; jj < d1; ++jj) {
+          double acc = 0.0;
+          for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * jj], g0[i], acc);
+          x = fma(acc, g1[jj], x);
+        }
+      } else {
+        const double* g2 =
+            op + ts.g_off[2] + int64_t(ts.g_dim[2]) * (b[3] + int64_t(ts.g_mb[2]) * ck[ts.cr[2]]);
+        const int d2 = ts.g_dim[2];
+        for (int l = 0; l < d2; ++l) {
+          double al = 0.0;
+          for (int jj = 0; jj < d1; ++jj) {
+            double acc = 0.0;
+            for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * (jj + d1 * l)], g0[i], acc);
+            al = fma(acc, g1[jj], al);
+          }
+          x = fma(al, g2[l], x);
+        }
+      }
+    }
+    if (ts.sign < 0) x = -x;
+  }
+  const double* crow = p.c + int64_t(job.x) * p.R;
+  const double maxc = row_maxabs(crow, p.R);
+  const double tc = p.thresh / maxc;
+  if (!(fabs(x) > tc)) return;
+  // bra configuration: the ket's states with the active clusters replaced
+  const int64_t* st = p.strides + int64_t(o.bsec) * p.N;
+  int64_t idx = 0;
+  for (int c = 0; c < p.N; ++c) idx += int64_t(ck[c]) * st[c];
+  for (int a = 0; a < o.n_act; ++a) idx += int64_t(b[a] - ck[o.c_act[a]]) * st[o.c_act[a]];
+  const unsigned long long key = (unsigned long long)(o.bsec) << kKeyIdxBits | (unsigned long long)idx;
+  double add[16];
+  for (int r = 0; r < p.R; ++r) add[r] = x * crow[r];
+  table_add(keys, vals, cap_mask, key, add, p.R, counters + 2);
+}
+
+__global__ void compact_kernel(const unsigned long long* __restrict__ keys, const double* __restrict__ vals,
+                               unsigned long long cap, int R, unsigned long long* __restrict__ okeys,
+                               double* __restrict__ ovals, unsigned long long* __restrict__ counters) {
+  const unsigned long long s = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= cap) return;
+  const unsigned long long k = keys[s];
+  if (k == kEmpty) return;
+  const unsigned long long pos = atomicAdd(counters + 3, 1ull);
+  okeys[pos] = k;
+  for (int r = 0; r < R; ++r) ovals[pos * R + r] = vals[s * R + r];
+}
+
+__global__ void pack_rows_kernel(const double* __restrict__ c, double* __restrict__ out, int64_t n, int R) {
+  int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n * R) return;
+  int64_t row = i / R;
+  int r = int(i - row * R);
+  out[i] = c[row + n * r];
+}
+
+inline bool fock_key(const int16_t* f, int N, uint64_t* key) {
+  uint64_t k = 0;
+  for (int i = 0; i < 2 * N; ++i) {
+    if (f[i] < 0 || f[i] > 15) return false;
+    k |= uint64_t(f[i]) << (4 * i);
+  }
+  *key = k;
+  return true;
+}
+
+}  // namespace
+
+#define FCG_CUDA(call)                                                               \
+  do {                                                                               \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess) {                                                         \
+      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
+      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;               \
+    }                                                                                \
+  } while (0)
+
+#define FCG_REQUIRE(cond, code, msg) \
+  do {                               \
+    if (!(cond)) {                   \
+      ctx->err = (msg);              \
+      return (code);                 \
+    }                                \
+  } while (0)
+
+extern "C" {
+
+int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbody, int64_t* n_out) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  FCG_REQUIRE(c && n_out, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(R >= 1 && R <= 16, FCG_ELIMIT, "R must be in [1, 16]");
+  FCG_REQUIRE(thresh >= 0.0, FCG_EINVAL, "thresh must be >= 0");
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  *n_out = 0;
+  const int N = ctx->N;
+  const int nmax1 = ctx->nmax + 1;
+  const Plan& P = ctx->plan;
+  // ---- host plan: bra sectors and open term records per (ket sector, transfer) -------
+  ProblemInfo pi;
+  pi.N = N;
+  pi.norb = ctx->norb;
+  pi.nmax = ctx->nmax;
+  pi.trm = &ctx->trm;
+  pi.n_terms = ctx->n_terms;
+  pi.trans = &ctx->trans;
+  pi.n_trans = ctx->n_trans;
+  pi.blk_index = &ctx->h_blk_index;
+  pi.blocks = &ctx->h_blocks;
+  pi.dress = &ctx->dress;
+  pi.w_index = &ctx->w_index;
+  std::vector<std::vector<int>> terms_of(ctx->n_trans);
+  for (int t = 0; t < ctx->n_terms; ++t) terms_of[ctx->trm[int64_t(t) * kTrmCols + 1]].push_back(t);
+  std::unordered_map<uint64_t, int32_t> bsec_of;
+  ctx->open_bra_fock.clear();
+  ctx->open_strides.clear();
+  ctx->open_dims.clear();
+  std::vector<OpenTerm> ots;
+  std::vector<OpenItem> items;
+  std::vector<int16_t> fb(2 * N);
+  for (size_t sk = 0; sk < P.sec_start.size(); ++sk) {
+    const int16_t* fk = &P.sec_fock[sk * 2 * N];
+    for (int tr = 0; tr < ctx->n_trans; ++tr) {
+      if (terms_of[tr].empty()) continue;
+      bool ok = true;
+      for (int i = 0; i < 2 * N; ++i) {
+        fb[i] = int16_t(fk[i] + ctx->trans[size_t(tr) * 2 * N + i]);
+        if (fb[i] < 0 || fb[i] > ctx->norb[i / 2]) ok = false;
+      }
+      if (!ok) continue;
+      // every cluster must have a local basis in its bra sector (:39-46)
+      int64_t dims[kMaxClusters];
+      for (int ci = 0; ci < N && ok; ++ci) {
+        int bl = ctx->h_blk_index[dense_block_index(nmax1, ci, kOpH, fb[2 * ci], fb[2 * ci + 1], fb[2 * ci],
+                                                    fb[2 * ci + 1])];
+        if (bl < 0)
+          ok = false;
+        else
+          dims[ci] = ctx->h_blocks[bl].mb;
+      }
+      if (!ok) continue;
+      uint64_t key;
+      fock_key(fb.data(), N, &key);
+      int32_t bs;
+      auto it = bsec_of.find(key);
+      if (it == bsec_of.end()) {
+        bs = int32_t(ctx->open_bra_fock.size() / (2 * N));
+        FCG_REQUIRE(bs < (1 << 23), FCG_ELIMIT, "too many bra sectors for the open sigma key");
+        bsec_of[key] = bs;
+        ctx->open_bra_fock.insert(ctx->open_bra_fock.end(), fb.begin(), fb.end());
+        int64_t stride = 1;
+        for (int ci = 0; ci < N; ++ci) {
+          ctx->open_strides.push_back(stride);
+          ctx->open_dims.push_back(dims[ci]);
+          stride *= dims[ci];
+        }
+        FCG_REQUIRE(stride < (int64_t(1) << kKeyIdxBits), FCG_ELIMIT, "bra sector product space exceeds 2^40");
+      } else {
+        bs = it->second;
+      }
+      const int32_t ot_off = int32_t(ots.size());
+      for (int t : terms_of[tr]) {
+        const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+        if (r[0] > nbody) continue;
+        OpenTerm o{};
+        if (!make_term_sector(pi, t, fb.data(), fk, o.ts)) continue;
+        const int pos = ctx->dress[t].pos < 0 ? 0 : ctx->dress[t].pos;
+        const int cw = r[2 + pos];
+        o.wmax_off = ctx->wmax_index[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
+        o.bsec = bs;
+        o.n_act = int8_t(1 + o.ts.nrem);
+        o.c_act[0] = int8_t(cw);
+        o.mb_act[0] = int16_t(o.ts.w_mb);
+        int64_t cnt = o.ts.w_mb;
+        for (int q = 0; q < o.ts.nrem; ++q) {
+          const int cq = o.ts.cr[q];
+          const int op = r[6 + ctx->dress[t].rem_pos[q]];
+          const int bl = ctx->h_blk_index[dense_block_index(nmax1, cq, op, fb[2 * cq], fb[2 * cq + 1], fk[2 * cq],
+                                                            fk[2 * cq + 1])];
+          o.gmax_off[q] = ctx->gmax_off[bl];
+          o.c_act[1 + q] = int8_t(cq);
+          o.mb_act[1 + q] = int16_t(o.ts.g_mb[q]);
+          cnt *= o.ts.g_mb[q];
+        }
+        FCG_REQUIRE(cnt < (int64_t(1) << 31), FCG_ELIMIT, "bra tuples of one term exceed 2^31");
+        o.out_count = int32_t(cnt);
+        ots.push_back(o);
+      }
+      const int32_t nt = int32_t(ots.size()) - ot_off;
+      if (nt > 0) items.push_back(OpenItem{int32_t(P.sec_start[sk]), int32_t(P.sec_count[sk]), ot_off, nt});
+    }
+  }
+  ctx->open_R = R;
+  ctx->open_keys.clear();
+  ctx->open_vals.clear();
+  if (items.empty()) return FCG_OK;
+  std::vector<int64_t> prefix(items.size() + 1, 0);
+  for (size_t i = 0; i < items.size(); ++i) prefix[i + 1] = prefix[i] + int64_t(items[i].nrow) * items[i].nt;
+  const int64_t n_jobs = prefix.back();
+  // ---- device ---------------------------------------------------------------------------
+  cudaStream_t s = ctx->stream;
+  const int64_t n = ctx->n_cfg;
+  FCG_CUDA(ctx->d_oterms.upload(ots.data(), ots.size(), s));
+  FCG_CUDA(ctx->d_oitems.upload(items.data(), items.size(), s));
+  FCG_CUDA(ctx->d_oprefix.upload(prefix.data(), prefix.size(), s));
+  FCG_CUDA(ctx->d_ostrides.upload(ctx->open_strides.data(), ctx->open_strides.size(), s));
+  FCG_CUDA(ctx->d_in64.alloc(size_t(n) * R));
+  FCG_CUDA(ctx->d_c64.alloc(size_t(n) * R));
+  FCG_CUDA(cudaMemcpyAsync(ctx->d_in64.p, c, sizeof(double) * n * R, cudaMemcpyHostToDevice, s));
+  pack_rows_kernel<<<unsigned((n * R + 255) / 256), 256, 0, s>>>(ctx->d_in64.p, ctx->d_c64.p, n, R);
+  FCG_CUDA(cudaGetLastError());
+  FCG_CUDA(ctx->d_counters.alloc(4));
+  FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, 4 * sizeof(unsigned long long), s));
+  FCG_CUDA(ctx->d_ojobs.alloc(size_t(n_jobs)));
+  OpenParams p{};
+  p.ot = ctx->d_oterms.p;
+  p.items = ctx->d_oitems.p;
+  p.prefix = ctx->d_oprefix.p;
+  p.n_items = int64_t(items.size());
+  p.n_jobs = n_jobs;
+  p.cfg = ctx->d_cfg.p;
+  p.c = ctx->d_c64.p;
+  p.strides = ctx->d_ostrides.p;
+  p.N = N;
+  p.R = R;
+  p.thresh = thresh;
+  FCG_CUDA(cudaEventRecord(ctx->ev0, s));
+  screen_kernel<<<unsigned((n_jobs + 255) / 256), 256, 0, s>>>(p, ctx->d_wmax.p, ctx->d_gmax.p, ctx->d_ojobs.p,
+                                                              ctx->d_counters.p);
+  FCG_CUDA(cudaGetLastError());
+  unsigned long long cnt[4];
+  FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  FCG_CUDA(cudaStreamSynchronize(s));
+  const int64_t n_kept = int64_t(cnt[0]);
+  const int64_t n_elem = int64_t(cnt[1]);
+  int launches = 2;
+  if (n_kept > 0) {
+    FCG_CUDA(ctx->d_ojob_prefix.alloc(size_t(n_kept) + 1));
+    DevBuf<int64_t> counts;
+    FCG_CUDA(counts.alloc(size_t(n_kept) + 1));
+    job_counts_kernel<<<unsigned((n_kept + 255) / 256), 256, 0, s>>>(ctx->d_ojobs.p, n_kept, ctx->d_oterms.p,
+                                                                     counts.p);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaMemsetAsync(counts.p + n_kept, 0, sizeof(int64_t), s));
+    size_t tmp_bytes = 0;
+    FCG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, counts.p, ctx->d_ojob_prefix.p, n_kept + 1, s));
+    FCG_CUDA(ctx->d_scan_tmp.alloc(tmp_bytes));
+    FCG_CUDA(cub::DeviceScan::ExclusiveSum(ctx->d_scan_tmp.p, tmp_bytes, counts.p, ctx->d_ojob_prefix.p, n_kept + 1,
+                                           s));
+    // table: twice the contributions, power of two, at least 4096 slots; doubled on overflow
+    unsigned long long cap = 4096;
+    while (cap < 2ull * (unsigned long long)n_elem && cap < (1ull << 28)) cap <<= 1;
+    for (int attempt = 0;; ++attempt) {
+      FCG_CUDA(ctx->d_hkeys.alloc(cap));
+      FCG_CUDA(ctx->d_hvals.alloc(cap * R));
+      FCG_CUDA(cudaMemsetAsync(ctx->d_hkeys.p, 0xFF, cap * sizeof(unsigned long long), s));
+      FCG_CUDA(cudaMemsetAsync(ctx->d_hvals.p, 0, cap * R * sizeof(double), s));
+      FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p + 2, 0, 2 * sizeof(unsigned long long), s));
+      expand_kernel<<<unsigned((n_elem + 255) / 256), 256, 0, s>>>(p, ctx->d_ojobs.p, ctx->d_ojob_prefix.p, n_kept,
+                                                                  n_elem, ctx->d_w64.p, ctx->d_op64.p,
+                                                                  ctx->d_hkeys.p, ctx->d_hvals.p, cap - 1,
+                                                                  ctx->d_counters.p);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+      FCG_CUDA(cudaStreamSynchronize(s));
+      launches += 2;
+      if (cnt[2] == 0) break;
+      FCG_REQUIRE(attempt < 3 && cap < (1ull << 31), FCG_ENOMEM, "open sigma hash table overflow");
+      cap <<= 1;
+    }
+    FCG_CUDA(ctx->d_okeys.alloc(cap));
+    FCG_CUDA(ctx->d_ovals.alloc(cap * R));
+    compact_kernel<<<unsigned((cap + 255) / 256), 256, 0, s>>>(ctx->d_hkeys.p, ctx->d_hvals.p, cap, R,
+                                                               ctx->d_okeys.p, ctx->d_ovals.p, ctx->d_counters.p);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaEventRecord(ctx->ev1, s));
+    FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+    FCG_CUDA(cudaStreamSynchronize(s));
+    launches += 1;
+    const int64_t n_rows = int64_t(cnt[3]);
+    ctx->open_keys.resize(n_rows);
+    ctx->open_vals.resize(size_t(n_rows) * R);
+    FCG_CUDA(cudaMemcpyAsync(ctx->open_keys.data(), ctx->d_okeys.p, n_rows * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, s));
+    FCG_CUDA(cudaMemcpyAsync(ctx->open_vals.data(), ctx->d_ovals.p, n_rows * R * sizeof(double),
+                             cudaMemcpyDeviceToHost, s));
+    FCG_CUDA(cudaStreamSynchronize(s));
+    float ms = 0.f;
+    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.last_kernel_ms = ms;
+  }
+  ctx->stats.kernel_launches = launches;
+  ctx->stats.open_jobs = n_jobs;
+  ctx->stats.open_jobs_kept = n_kept;
+  ctx->stats.open_contractions = n_elem;
+  *n_out = int64_t(ctx->open_keys.size());
+  return FCG_OK;
+}
+
+int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coeff) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(fock && cfg && coeff, FCG_EINVAL, "null pointer");
+  const int N = ctx->N;
+  const int R = ctx->open_R;
+  const int64_t m = int64_t(ctx->open_keys.size());
+  for (int64_t i = 0; i < m; ++i) {
+    const unsigned long long key = ctx->open_keys[i];
+    const int64_t bs = int64_t(key >> kKeyIdxBits);
+    int64_t idx = int64_t(key & ((1ull << kKeyIdxBits) - 1));
+    std::memcpy(fock + i * 2 * N, &ctx->open_bra_fock[bs * 2 * N], sizeof(int16_t) * 2 * N);
+    for (int c = 0; c < N; ++c) {
+      const int64_t d = ctx->open_dims[bs * N + c];
+      cfg[i * N + c] = int16_t(idx % d);
+      idx /= d;
+    }
+    for (int r = 0; r < R; ++r) coeff[i + m * r] = ctx->open_vals[size_t(i) * R + r];
+  }
+  return FCG_OK;
+}
+
+}  // extern "C"

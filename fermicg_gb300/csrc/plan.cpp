@@ -43,6 +43,46 @@ struct Group {
 
 }  // namespace
 
+bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int16_t* fk, TermSector& ts) {
+  const std::vector<int32_t>& trm = *pi.trm;
+  const TermDress& d = (*pi.dress)[t];
+  const std::vector<int32_t>& blk = *pi.blk_index;
+  const std::vector<BlockInfo>& blocks = *pi.blocks;
+  const int nmax1 = pi.nmax + 1;
+  const int nbody = TT(trm, t, 0);
+  ts = TermSector{};
+  const int pos = d.pos < 0 ? 0 : d.pos;
+  const int cw = TT(trm, t, 2 + pos), opw = TT(trm, t, 6 + pos);
+  const int bw = blk[dense_block_index(nmax1, cw, opw, fb[2 * cw], fb[2 * cw + 1], fk[2 * cw], fk[2 * cw + 1])];
+  const int64_t woff = (*pi.w_index)[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
+  if (bw < 0 || woff < 0) return false;
+  ts.w_off = woff;
+  ts.w_mb = blocks[bw].mb;
+  ts.cw = int8_t(cw);
+  ts.rest_len = int16_t(nbody == 1 ? 1 : d.rest_len);
+  ts.nrem = int8_t(nbody == 1 ? 0 : d.nrem);
+  for (int r = 0; r < ts.nrem; ++r) {
+    const int o = d.rem_pos[r];
+    const int c = TT(trm, t, 2 + o), op = TT(trm, t, 6 + o);
+    const int bl = blk[dense_block_index(nmax1, c, op, fb[2 * c], fb[2 * c + 1], fk[2 * c], fk[2 * c + 1])];
+    if (bl < 0) return false;
+    ts.g_off[r] = blocks[bl].off;
+    ts.g_mb[r] = blocks[bl].mb;
+    ts.g_dim[r] = int16_t(blocks[bl].nidx);
+    ts.cr[r] = int8_t(c);
+  }
+  // compute_terms_state_sign (type_ClusteredTerm.jl:181-196) on the ket sector
+  int sgn = 0;
+  for (int o = 0; o < nbody; ++o)
+    if (TT(trm, t, 18 + o)) {
+      int ne = 0;
+      for (int ci = 0; ci < TT(trm, t, 2 + o); ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
+      sgn ^= ne & 1;
+    }
+  ts.sign = int8_t(nbody == 1 ? 1 : (sgn ? -1 : 1));
+  return true;
+}
+
 std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
   const int N = pi.N;
   const std::vector<int32_t>& trm = *pi.trm;
@@ -173,10 +213,6 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
   std::vector<std::vector<WorkItem>> tItems(n_sec);
   std::vector<std::vector<TermSector>> tTS(n_sec);
   std::vector<int64_t> tFlop(n_sec, 0), tFlopD(n_sec, 0);
-  const std::vector<TermDress>& dress = *pi.dress;
-  const std::vector<int64_t>& w_index = *pi.w_index;
-  const std::vector<int32_t>& blk = *pi.blk_index;
-  const std::vector<BlockInfo>& blocks = *pi.blocks;
 #pragma omp parallel
   {
     std::vector<int16_t> fk(2 * N);
@@ -199,43 +235,9 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
           tflop.clear();
           tflopd.clear();
           for (int t : tl.terms) {
-            const TermDress& d = dress[t];
+            TermSector ts;
+            if (!make_term_sector(pi, t, fb, fk.data(), ts)) continue;  // a missing TDM block contributes nothing
             const int nbody = TT(trm, t, 0);
-            TermSector ts{};
-            int cw = TT(trm, t, 2 + (d.pos < 0 ? 0 : d.pos));
-            int opw = TT(trm, t, 6 + (d.pos < 0 ? 0 : d.pos));
-            int bw = blk[dense_block_index(nmax1, cw, opw, fb[2 * cw], fb[2 * cw + 1], fk[2 * cw], fk[2 * cw + 1])];
-            int64_t woff = w_index[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
-            if (bw < 0 || woff < 0) continue;  // a missing TDM block contributes nothing
-            ts.w_off = woff;
-            ts.w_mb = blocks[bw].mb;
-            ts.cw = int8_t(cw);
-            ts.rest_len = int16_t(nbody == 1 ? 1 : d.rest_len);
-            ts.nrem = int8_t(nbody == 1 ? 0 : d.nrem);
-            bool ok = true;
-            for (int r = 0; r < ts.nrem; ++r) {
-              int o = d.rem_pos[r];
-              int c = TT(trm, t, 2 + o), op = TT(trm, t, 6 + o);
-              int bl = blk[dense_block_index(nmax1, c, op, fb[2 * c], fb[2 * c + 1], fk[2 * c], fk[2 * c + 1])];
-              if (bl < 0) {
-                ok = false;
-                break;
-              }
-              ts.g_off[r] = blocks[bl].off;
-              ts.g_mb[r] = blocks[bl].mb;
-              ts.g_dim[r] = int16_t(blocks[bl].nidx);
-              ts.cr[r] = int8_t(c);
-            }
-            if (!ok) continue;
-            // compute_terms_state_sign (type_ClusteredTerm.jl:181-196) on the ket sector
-            int sgn = 0;
-            for (int o = 0; o < nbody; ++o)
-              if (TT(trm, t, 18 + o)) {
-                int ne = 0;
-                for (int ci = 0; ci < TT(trm, t, 2 + o); ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
-                sgn ^= ne & 1;
-              }
-            ts.sign = int8_t(nbody == 1 ? 1 : (sgn ? -1 : 1));
             int64_t len = 1;
             for (int o = 0; o < 4; ++o) len *= TT(trm, t, 22 + o);
             tflop.push_back(nbody > 1 ? 2 * len : 0);

@@ -39,6 +39,10 @@ SIGNATURES = {
     "fcg_sigma_closed": (_I, [_P, _I, _P, _P, _I]),
     "fcg_sigma_closed_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_diagonal": (_I, [_P, _I, _P]),
+    "fcg_sigma_open": (_I, [_P, _I, _P, ctypes.c_double, _I, ctypes.POINTER(_L)]),
+    "fcg_sigma_open_fetch": (_I, [_P, _P, _P, _P]),
+    "fcg_davidson": (_I, [_P, _I, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P,
+                          ctypes.POINTER(_I)]),
     "fcg_get_stats": (_I, [_P, _P]),
 }
 
@@ -48,7 +52,9 @@ class Stats(ctypes.Structure):
                 ("n_triples", ctypes.c_int64), ("flops_reference", ctypes.c_int64),
                 ("flops_executed", ctypes.c_int64), ("dressed_elements", ctypes.c_int64),
                 ("plan_seconds", ctypes.c_double), ("last_kernel_ms", ctypes.c_double),
-                ("kernel_launches", ctypes.c_int64)]
+                ("kernel_launches", ctypes.c_int64), ("open_jobs", ctypes.c_int64),
+                ("open_jobs_kept", ctypes.c_int64), ("open_contractions", ctypes.c_int64),
+                ("davidson_sigma_calls", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -164,6 +170,38 @@ class GpuSigma:
         hd = np.zeros(self.n_cfg)
         self._check(self.L.fcg_diagonal(self.h, oid, _ptr(hd)), "fcg_diagonal")
         return hd
+
+    def sigma_open(self, coeffs, thresh, nbody=4):
+        """open_matvec_thread: (fock (m,N,2) int16, cfg (m,N) int16, coeff (m,R)) of the FOIS sigma."""
+        c = np.asfortranarray(coeffs, dtype=np.float64)
+        n, R = c.shape
+        if n != self.n_cfg:
+            raise ValueError("coefficient rows do not match the state")
+        m = ctypes.c_int64(0)
+        self._check(self.L.fcg_sigma_open(self.h, R, _ptr(c), float(thresh), int(nbody), ctypes.byref(m)),
+                    "fcg_sigma_open")
+        m = m.value
+        of = np.zeros((m, self.N, 2), dtype=np.int16)
+        oc = np.zeros((m, self.N), dtype=np.int16)
+        ov = np.zeros((m, R), dtype=np.float64, order="F")
+        self._check(self.L.fcg_sigma_open_fetch(self.h, _ptr(of), _ptr(oc), _ptr(ov)), "fcg_sigma_open_fetch")
+        return of, oc, np.ascontiguousarray(ov)
+
+    def davidson(self, v0, max_iter=100, max_ss_vecs=12, tol=1e-8, lindep=1e-12, precision="fp64",
+                 precond=True):
+        """Block Davidson on the device (tps_ci_davidson): returns (energies, vectors, residuals, iters)."""
+        v = np.asfortranarray(v0, dtype=np.float64)
+        n, R = v.shape
+        if n != self.n_cfg:
+            raise ValueError("guess rows do not match the state")
+        e = np.zeros(R)
+        res = np.zeros(R)
+        out = np.zeros((n, R), order="F")
+        it = ctypes.c_int(0)
+        self._check(self.L.fcg_davidson(self.h, R, _ptr(v), int(max_iter), int(max_ss_vecs), float(tol),
+                                        float(lindep), PRECISION[precision], int(bool(precond)), _ptr(e),
+                                        _ptr(out), _ptr(res), ctypes.byref(it)), "fcg_davidson")
+        return e, np.ascontiguousarray(out), res, it.value
 
     def stats(self):
         s = Stats()

@@ -104,3 +104,96 @@ class TPSCIstate:
 
     def as_dict(self):
         return {(f, c): v for f, cs in self.data.items() for c, v in cs.items()}
+
+
+# ---- host-side TPSCIstate algebra (src/type_TPSCIstate.jl, src/tpsci_outer.jl) ------------
+
+def copy_state(s: TPSCIstate) -> TPSCIstate:
+    """deepcopy (type_TPSCIstate.jl:491): empty sectors are dropped."""
+    out = TPSCIstate(s.n_clusters, s.R, s.dtype)
+    for f, cs in s.data.items():
+        if cs:
+            out.data[f] = {c: v.copy() for c, v in cs.items()}
+    return out
+
+
+def add_state(s1: TPSCIstate, s2: TPSCIstate):
+    """add! (type_TPSCIstate.jl:617): s1 += s2, new configurations appended."""
+    for f, cs in s2.data.items():
+        d = s1.data.setdefault(f, {})
+        for c, v in cs.items():
+            if c in d:
+                d[c] = d[c] + v
+            else:
+                d[c] = v.copy()
+
+
+def scale_state(s: TPSCIstate, a: float):
+    for cs in s.data.values():
+        for c in cs:
+            cs[c] = cs[c] * a
+
+
+def times_matrix(s: TPSCIstate, C) -> TPSCIstate:
+    """A * C (type_TPSCIstate.jl:456)."""
+    out = copy_state(s)
+    if len(out):
+        out.set_vector(s.get_vector() @ C)
+    return out
+
+
+def minus_state(A: TPSCIstate, B: TPSCIstate) -> TPSCIstate:
+    """A - B (type_TPSCIstate.jl:478)."""
+    C = copy_state(B)
+    scale_state(C, -1.0)
+    add_state(C, A)
+    return C
+
+
+def overlap(v1: TPSCIstate, v2: TPSCIstate):
+    """R x R overlap over the shared configurations (type_TPSCIstate.jl:416)."""
+    S = np.zeros((v2.R, v2.R))
+    for f, cs in v2.data.items():
+        d1 = v1.data.get(f)
+        if not d1:
+            continue
+        for c, v in cs.items():
+            if c in d1:
+                S += np.outer(d1[c], v)
+    return S
+
+
+def project_out(v: TPSCIstate, w: TPSCIstate):
+    """project_out! (tpsci_outer.jl:869): drop w's configurations from v."""
+    for f, cs in w.data.items():
+        if f in v.data:
+            d = v.data[f]
+            for c in cs:
+                d.pop(c, None)
+            if not d:
+                del v.data[f]
+
+
+def clip(s: TPSCIstate, thresh: float):
+    """clip! (type_TPSCIstate.jl:589): drop configurations with every |c| < thresh."""
+    for f in list(s.data):
+        cs = s.data[f]
+        for c in list(cs):
+            if np.all(np.abs(cs[c]) < thresh):
+                del cs[c]
+        if not cs:
+            del s.data[f]
+
+
+def zero_state(s: TPSCIstate):
+    for cs in s.data.values():
+        for c in cs:
+            cs[c] = np.zeros(s.R, dtype=s.dtype)
+
+
+def state_from_rows(n_clusters, R, focks, cfgs, coeffs) -> TPSCIstate:
+    out = TPSCIstate(n_clusters, R)
+    for i in range(len(cfgs)):
+        f = tuple((int(a), int(b)) for a, b in focks[i])
+        out.data.setdefault(f, {})[tuple(int(x) for x in cfgs[i])] = np.array(coeffs[i], dtype=np.float64)
+    return out

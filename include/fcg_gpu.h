@@ -56,8 +56,12 @@ typedef struct fcg_stats {
   int64_t flops_executed;   /* 2 x multiply-adds the dressed contraction does per sigma (R update excluded) */
   int64_t dressed_elements; /* elements of the dressed operators W (one copy per precision) */
   double plan_seconds;      /* host time of the last fcg_state_set */
-  double last_kernel_ms;    /* device time of the last sigma kernel (CUDA events) */
+  double last_kernel_ms;    /* device time of the last sigma kernel(s) (CUDA events) */
   int64_t kernel_launches;  /* kernels launched by the last sigma call */
+  int64_t open_jobs;        /* (ket, term) pairs of the last open sigma */
+  int64_t open_jobs_kept;   /* of those, the ones the screen kept */
+  int64_t open_contractions;/* (ket, term, bra tuple) elements evaluated */
+  int64_t davidson_sigma_calls; /* sigma builds of the last fcg_davidson */
 } fcg_stats;
 
 int fcg_version(void);
@@ -99,6 +103,28 @@ int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_si
  * terms, bra == ket), else compute_diagonal! with that op string
  * (src/tpsci_outer.jl:735-757, e.g. op_id 23 = "Hcmf").  hd: host, n_cfg. */
 int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd);
+
+/* open_matvec_thread (src/tpsci_matvec_thread.jl:11-129): sigma over the first-order
+ * interacting space of the state's configurations, keeping each (ket, term, bra)
+ * contribution x with |x| > thresh / max_r |c_ket[r]| (_collect_significant_thread!,
+ * :830-885), terms of at most `nbody` clusters.  c: host, column-major n_cfg x R.
+ * Returns the number of output configurations in *n_out; fetch them with
+ * fcg_sigma_open_fetch.  Output order is unspecified (as in the reference). */
+int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbody, int64_t* n_out);
+
+/* Rows of the last fcg_sigma_open: fock int16 [n_out][N][2], cfg int16 [n_out][N],
+ * coeff float64 column-major n_out x R. */
+int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coeff);
+
+/* The Davidson solve of tps_ci_davidson (src/tpsci_outer.jl:364-454; BlockDavidson
+ * Davidson(Hmap; v0, max_iter, max_ss_vecs, nroots=R, tol, lindep_thresh) + eigs with
+ * Adiag = compute_diagonal): lowest R eigenpairs of H within the state's configurations.
+ * v0, vectors: host column-major n_cfg x R; energies, residuals: R; tol is the residual
+ * norm.  precision FCG_FP64, or FCG_FP32 = float32 sigma builds until the residuals
+ * reach max(tol, 1e-5), then float64 sigma builds to tol.  precond: 1 = diagonal
+ * preconditioner.  Subspace holds at most max_ss_vecs * R vectors. */
+int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol, double lindep,
+                 int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 

@@ -83,3 +83,39 @@ def test_empty_and_single_row_states():
     O = oracle.Oracle(po, pt)
     x = np.array([[0.7]])
     np.testing.assert_allclose(g.sigma_closed(x), O.sigma_closed(f[:1], c[:1], x), rtol=1e-12)
+
+
+def _open_dict(of, oc, ov):
+    return {(of[i].tobytes(), oc[i].tobytes()): ov[i] for i in range(len(of))}
+
+
+@pytest.mark.parametrize("thresh", [0.0, 1e-4])
+def test_open_sigma_full_space_matches_oracle(thresh):
+    """open_matvec_thread: FOIS sigma key set and values vs the oracle (prescreen off)."""
+    prob, st = small_full()
+    g, po, pt, f, c = _gpu_for(prob, st)
+    O = oracle.Oracle(po, pt)
+    x = np.random.default_rng(11).standard_normal((len(st), 2))
+    ref = _open_dict(*O.sigma_open(f, c, x, thresh))
+    out = _open_dict(*g.sigma_open(x, thresh))
+    assert set(out) == set(ref)
+    scale = max(np.abs(v).max() for v in ref.values())
+    for k, v in ref.items():
+        np.testing.assert_allclose(out[k], v, rtol=0, atol=1e-10 * scale)
+
+
+@pytest.mark.parametrize("thresh,nbody", [(1e-5, 4), (1e-3, 4), (1e-4, 2)])
+def test_open_sigma_config1_subspace_matches_oracle(thresh, nbody):
+    prob, st = config1_subspace(400, 2)
+    g, po, pt, f, c = _gpu_for(prob, st)
+    O = oracle.Oracle(po, pt)
+    x = st.get_vector()
+    ref = _open_dict(*O.sigma_open(f, c, x, thresh, nbody=nbody))
+    out = _open_dict(*g.sigma_open(x, thresh, nbody=nbody))
+    assert len(ref) > len(st)
+    assert set(out) == set(ref)
+    scale = max(np.abs(v).max() for v in ref.values())
+    for k, v in ref.items():
+        np.testing.assert_allclose(out[k], v, rtol=0, atol=1e-10 * scale)
+    s = g.stats()
+    assert s["open_jobs_kept"] <= s["open_jobs"]

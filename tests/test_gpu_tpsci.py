@@ -1,0 +1,69 @@
+"""Device Davidson and the GPU TPSCI driver vs the oracle and the reference's goldens."""
+import numpy as np
+import pytest
+
+import oracle
+from fermicg_gb300 import pack
+from fermicg_gb300.gpu import GpuSigma
+from fermicg_gb300.state import TPSCIstate
+from helpers import config1_subspace, packed
+
+pytestmark = pytest.mark.gpu
+
+
+def _dense_lowest(prob, st, R):
+    po, pt = packed(prob)
+    f, c, v, _ = pack.pack_state(st)
+    H = oracle.Oracle(po, pt).build_H(f, c)
+    return np.linalg.eigvalsh(0.5 * (H + H.T))[:R]
+
+
+@pytest.mark.parametrize("precision,tol_e", [("fp64", 1e-9), ("fp32", 1e-6)])
+def test_davidson_matches_dense_eigenvalues(precision, tol_e):
+    """Energies within 1e-9 (FP64) / 1 uEh (mixed: FP32 sigma + FP64 refinement) of a dense solve."""
+    prob, st = config1_subspace(1500, 4)
+    ref = _dense_lowest(prob, st, 4)
+    g = GpuSigma(0)
+    po, pt = packed(prob)
+    g.set_ops(po)
+    g.set_terms(pt)
+    f, c, v, _ = pack.pack_state(st)
+    g.state_set(f, c)
+    guess = np.zeros_like(v)
+    hd = g.diagonal()
+    for r, i in enumerate(np.argsort(hd)[:4]):
+        guess[i, r] = 1.0
+    e, X, res, it = g.davidson(guess, tol=1e-7, max_iter=300, precision=precision)
+    assert np.abs(e - ref).max() < tol_e, (e, ref)
+    assert res.max() < 1e-7
+    # Ritz vectors are orthonormal eigenvectors
+    np.testing.assert_allclose(X.T @ X, np.eye(4), atol=1e-10)
+
+
+def _h12():
+    from test_golden import _h12_problem
+    return _h12_problem()
+
+
+def test_gpu_tpsci_h12_matches_reference_energies():
+    """test/test_tpsci.jl "tpsci h12 64bit": e0 and e0+e2 of 7 roots within 1e-8, on the GPU."""
+    from fermicg_gb300.tpsci import GpuTPSCI
+    ints, z, m, b, ops, H = _h12()
+    R, N = m["nroots"], len(m["clusters"])
+    st = TPSCIstate(N, R)
+    ref = tuple(map(tuple, m["init_fspace"]))
+    row = np.zeros(R)
+    row[0] = 1.0
+    st[(ref, (0,) * N)] = row
+    for i, ex in enumerate(m["excitons"]):
+        row = np.zeros(R)
+        row[i + 1] = 1.0
+        st[(ref, tuple(ex))] = row
+    kw = m["tpsci_kwargs"]
+    T = GpuTPSCI(ops, b, H)
+    e0, v0 = T.tpsci_ci(st, thresh_cipsi=kw["thresh_cipsi"], thresh_foi=kw["thresh_foi"],
+                        thresh_asci=kw.get("thresh_asci"), conv_thresh=kw["conv_thresh"], ci_conv=1e-9)
+    np.testing.assert_allclose(np.abs(e0), np.abs(np.array(m["e0"])), atol=1e-8, rtol=0)
+    e2 = T.pt2_energy(v0, thresh_foi=m["pt2_thresh_foi"])
+    np.testing.assert_allclose(np.abs(e0 + e2), np.abs(np.array(m["e0_plus_e2"])), atol=1e-8, rtol=0)
+    T.close()
