@@ -283,8 +283,9 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
   W.kmax = std::max(W.kmax, std::min<int>(2 * R, int(n)));
   const int kmax = W.kmax;
   W.gram_grid = int(std::min<int64_t>(304, (n + 255) / 256));
-  FCG_CUDA(W.V.alloc(size_t(n) * kmax));
-  FCG_CUDA(W.AV.alloc(size_t(n) * kmax));
+  // room for a full subspace plus one block of new directions (restart keeps nv <= kmax)
+  FCG_CUDA(W.V.alloc(size_t(n) * (kmax + R)));
+  FCG_CUDA(W.AV.alloc(size_t(n) * (kmax + R)));
   FCG_CUDA(W.X.alloc(size_t(n) * R));
   FCG_CUDA(W.HX.alloc(size_t(n) * R));
   FCG_CUDA(W.T.alloc(size_t(n) * R));
@@ -305,7 +306,24 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
   FCG_CUDA(cudaMemcpyAsync(W.V.p, v0, sizeof(double) * n * R, cudaMemcpyHostToDevice, ctx->stream));
   int nv = 0, m = 0, rc;
   if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, lindep, &m))) return rc;
-  FCG_REQUIRE(m == R, FCG_EINVAL, "initial vectors are linearly dependent");
+  if (m != R) {
+    double nrm_min = 1e300, nrm_max = 0.0;
+    int nonfinite = 0;
+    for (int j = 0; j < R; ++j) {
+      double s2 = 0.0;
+      for (int64_t i = 0; i < n; ++i) {
+        const double x = v0[i + n * j];
+        if (!std::isfinite(x)) ++nonfinite;
+        s2 += x * x;
+      }
+      nrm_min = std::min(nrm_min, s2);
+      nrm_max = std::max(nrm_max, s2);
+    }
+    ctx->err = "initial vectors are linearly dependent (kept " + std::to_string(m) + " of " + std::to_string(R) +
+               ", n " + std::to_string(n) + ", squared norms " + std::to_string(nrm_min) + ".." +
+               std::to_string(nrm_max) + ", non-finite entries " + std::to_string(nonfinite) + ")";
+    return FCG_EINVAL;
+  }
   if ((rc = fcg_sigma_closed_device(ctx, R, W.V.p, W.AV.p, prec))) return rc;
   nv = R;
   std::vector<double> Hs, w, Y, th(R), rn(R);
@@ -319,6 +337,12 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
       for (int i = 0; i < j; ++i) {
         double a = 0.5 * (Hs[i + nv * j] + Hs[j + nv * i]);
         Hs[i + nv * j] = Hs[j + nv * i] = a;
+      }
+    for (double x : Hs)
+      if (!std::isfinite(x)) {
+        ctx->err = "Davidson: non-finite subspace matrix at iteration " + std::to_string(it) + " (subspace " +
+                   std::to_string(nv) + ")";
+        return FCG_ECUDA;
       }
     jacobi_eigh(nv, Hs, w, Y);
     Y.resize(size_t(nv) * R);
@@ -336,6 +360,10 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
     for (int j = 0; j < R; ++j) {
       rn[j] = std::sqrt(rn[j]);
       rmax = std::max(rmax, rn[j]);
+      if (!std::isfinite(rn[j]) || !std::isfinite(th[j])) {
+        ctx->err = "Davidson: non-finite residual or Ritz value at iteration " + std::to_string(it);
+        return FCG_ECUDA;
+      }
     }
     const bool switching = (prec == FCG_FP32) && rmax < switch_tol;
     if (rmax < tol && prec == FCG_FP64) {

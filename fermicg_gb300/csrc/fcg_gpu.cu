@@ -109,42 +109,118 @@ struct SigmaParams {
   int R;
 };
 
+// ---- vector loads ---------------------------------------------------------------------------
+template <typename T>
+struct Vec4;
+template <>
+struct Vec4<float> {
+  float v[4];
+  __device__ __forceinline__ void load(const float* p) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+  }
+};
+template <>
+struct Vec4<double> {
+  double v[4];
+  __device__ __forceinline__ void load(const double* p) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+  }
+};
+
+// one local state out of a 16-byte row of 8 int16 (no dynamic register indexing)
+__device__ __forceinline__ int state_of(const uint4& r, int c) {
+  const unsigned w = c < 4 ? (c < 2 ? r.x : r.y) : (c < 6 ? r.z : r.w);
+  return int((w >> (16 * (c & 1))) & 0xFFFFu);
+}
+
 // <bra| term |ket> from a term-sector record: the dressed cluster's W column contracted
-// with the other active clusters' TDM columns.
+// with the other active clusters' TDM columns (contract_matrix_element re-associated).
+// Columns whose length is a multiple of 4 are read with 16-byte loads (blocks are aligned
+// on the device); the common n=4 shapes are fully unrolled.
 template <typename T>
 __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __restrict__ w,
-                                             const T* __restrict__ op, const int16_t* __restrict__ cb,
-                                             const int16_t* __restrict__ ck) {
-  const T* wc = w + ts.w_off + int64_t(ts.rest_len) * (cb[ts.cw] + int64_t(ts.w_mb) * ck[ts.cw]);
-  if (ts.nrem == 0) return wc[0];
-  const T* g0 = op + ts.g_off[0] + int64_t(ts.g_dim[0]) * (cb[ts.cr[0]] + int64_t(ts.g_mb[0]) * ck[ts.cr[0]]);
+                                             const T* __restrict__ op, const uint4& rb, const uint4& rk) {
+  const T* wc = w + ts.w_off + int64_t(ts.rest_len) * (state_of(rb, ts.cw) + int64_t(ts.w_mb) * state_of(rk, ts.cw));
+  if (ts.nrem == 0) return __ldg(wc);
   const int d0 = ts.g_dim[0];
+  const T* g0 =
+      op + ts.g_off[0] + int64_t(d0) * (state_of(rb, ts.cr[0]) + int64_t(ts.g_mb[0]) * state_of(rk, ts.cr[0]));
   T me = T(0);
   if (ts.nrem == 1) {
-    for (int i = 0; i < d0; ++i) me = fma(wc[i], g0[i], me);
-  } else {
-    const T* g1 = op + ts.g_off[1] + int64_t(ts.g_dim[1]) * (cb[ts.cr[1]] + int64_t(ts.g_mb[1]) * ck[ts.cr[1]]);
-    const int d1 = ts.g_dim[1];
-    if (ts.nrem == 2) {
-      for (int j = 0; j < d1; ++j) {
-        const T* wj = wc + d0 * j;
-        T acc = T(0);
-        for (int i = 0; i < d0; ++i) acc = fma(wj[i], g0[i], acc);
-        me = fma(acc, g1[j], me);
+    if ((d0 & 3) == 0) {
+      for (int i = 0; i < d0; i += 4) {
+        Vec4<T> a, g;
+        a.load(wc + i);
+        g.load(g0 + i);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) me = fma(a.v[q], g.v[q], me);
       }
     } else {
-      const T* g2 =
-          op + ts.g_off[2] + int64_t(ts.g_dim[2]) * (cb[ts.cr[2]] + int64_t(ts.g_mb[2]) * ck[ts.cr[2]]);
-      const int d2 = ts.g_dim[2];
-      for (int l = 0; l < d2; ++l) {
-        T accl = T(0);
-        for (int j = 0; j < d1; ++j) {
-          const T* wj = wc + d0 * (j + d1 * l);
-          T acc = T(0);
-          for (int i = 0; i < d0; ++i) acc = fma(wj[i], g0[i], acc);
-          accl = fma(acc, g1[j], accl);
+      for (int i = 0; i < d0; ++i) me = fma(__ldg(wc + i), __ldg(g0 + i), me);
+    }
+  } else {
+    const int d1 = ts.g_dim[1];
+    const T* g1 =
+        op + ts.g_off[1] + int64_t(d1) * (state_of(rb, ts.cr[1]) + int64_t(ts.g_mb[1]) * state_of(rk, ts.cr[1]));
+    if (ts.nrem == 2) {
+      if (d0 == 4 && d1 == 4) {
+        Vec4<T> a0, a1;
+        a0.load(g0);
+        a1.load(g1);
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          Vec4<T> wv;
+          wv.load(wc + 4 * j);
+          T acc = wv.v[0] * a0.v[0];
+#pragma unroll
+          for (int i = 1; i < 4; ++i) acc = fma(wv.v[i], a0.v[i], acc);
+          me = fma(acc, a1.v[j], me);
         }
-        me = fma(accl, g2[l], me);
+      } else {
+        for (int j = 0; j < d1; ++j) {
+          const T* wj = wc + d0 * j;
+          T acc = T(0);
+          for (int i = 0; i < d0; ++i) acc = fma(__ldg(wj + i), __ldg(g0 + i), acc);
+          me = fma(acc, __ldg(g1 + j), me);
+        }
+      }
+    } else {
+      const int d2 = ts.g_dim[2];
+      const T* g2 =
+          op + ts.g_off[2] + int64_t(d2) * (state_of(rb, ts.cr[2]) + int64_t(ts.g_mb[2]) * state_of(rk, ts.cr[2]));
+      if (d0 == 4 && d1 == 4 && d2 == 4) {
+        Vec4<T> a0, a1, a2;
+        a0.load(g0);
+        a1.load(g1);
+        a2.load(g2);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+          T accl = T(0);
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            Vec4<T> wv;
+            wv.load(wc + 4 * (j + 4 * l));
+            T acc = wv.v[0] * a0.v[0];
+#pragma unroll
+            for (int i = 1; i < 4; ++i) acc = fma(wv.v[i], a0.v[i], acc);
+            accl = fma(acc, a1.v[j], accl);
+          }
+          me = fma(accl, a2.v[l], me);
+        }
+      } else {
+        for (int l = 0; l < d2; ++l) {
+          T accl = T(0);
+          for (int j = 0; j < d1; ++j) {
+            const T* wj = wc + d0 * (j + d1 * l);
+            T acc = T(0);
+            for (int i = 0; i < d0; ++i) acc = fma(__ldg(wj + i), __ldg(g0 + i), acc);
+            accl = fma(acc, __ldg(g1 + j), accl);
+          }
+          me = fma(accl, __ldg(g2 + l), me);
+        }
       }
     }
   }
@@ -152,8 +228,8 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
 }
 
 constexpr int kSigmaThreads = 256;
-constexpr int kSigmaIters = 8;
-constexpr int64_t kSigmaChunk = int64_t(kSigmaThreads) * kSigmaIters;
+constexpr int kSigmaRun = 16;  // consecutive triples per thread
+constexpr int64_t kSigmaChunk = int64_t(kSigmaThreads) * kSigmaRun;
 constexpr int kMaxR = 16;
 
 // largest w in [lo, hi] with prefix[w] <= x
@@ -169,7 +245,19 @@ __device__ __forceinline__ int64_t find_item(const int64_t* prefix, int64_t lo, 
 }
 
 template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
+__device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* acc, int R) {
+  constexpr int RV = RR > 0 ? RR : kMaxR;
+#pragma unroll
+  for (int r = 0; r < RV; ++r)
+    if (r < R) atomicAdd(sig + int64_t(b) * R + r, acc[r]);
+}
+
+// Each CTA owns a fixed chunk of the flattened triple space (exact load balance) and each
+// thread a run of kSigmaRun consecutive triples (term fastest, then ket, then bra inside a
+// work item), decoded incrementally; contributions to one bra row are summed in registers
+// and flushed with one atomic per root when the bra changes.
+template <typename T, int RR>
+__global__ void __launch_bounds__(kSigmaThreads, 3) closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
                                                                       const T* __restrict__ op,
                                                                       const T* __restrict__ cin,
                                                                       T* __restrict__ sig) {
@@ -182,65 +270,57 @@ __global__ void __launch_bounds__(kSigmaThreads) closed_sigma_kernel(SigmaParams
     w_hi_s = find_item(p.prefix, w_lo_s, p.n_items - 1, e0 - 1);
   }
   __syncthreads();
-  const int64_t w_hi = w_hi_s;
-  const int lane = threadIdx.x & 31;
-  const int warp = threadIdx.x >> 5;
   const int R = RR > 0 ? RR : p.R;
-  int64_t wcur = w_lo_s;  // warp-uniform: item of the warp's first triple
-  for (int it = 0; it < kSigmaIters; ++it) {
-    const int64_t base = s0 + int64_t(it) * kSigmaThreads + int64_t(warp) * 32;
-    const int64_t idx = base + lane;
-    // the warp's first triple locates its item once; lanes step forward from it
-    if (base < e0) wcur = find_item(p.prefix, wcur, w_hi, base);
-    int key = -1;
-    T val[RV];
+  const int64_t t0 = s0 + int64_t(threadIdx.x) * kSigmaRun;
+  if (t0 >= e0) return;
+  const int64_t t1 = (t0 + kSigmaRun < e0) ? t0 + kSigmaRun : e0;
+  const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
+  int64_t wi = find_item(p.prefix, w_lo_s, w_hi_s, t0);
+  WorkItem it = p.items[wi];
+  int64_t local = t0 - __ldg(p.prefix + wi);
+  int ti = int(local % it.nt);
+  int64_t rest = local / it.nt;
+  int kj = int(rest % it.nk);
+  int bj = int(rest / it.nk);
+  int b = __ldg(p.perm + it.bra_off + bj);
+  int k = __ldg(p.perm + it.ket_off + kj);
+  uint4 rb = __ldg(cfg + b);
+  uint4 rk = __ldg(cfg + k);
+  T acc[RV];
 #pragma unroll
-    for (int r = 0; r < RV; ++r) val[r] = T(0);
-    if (idx < e0) {
-      int64_t wi_ = wcur;
-      while (wi_ < w_hi && __ldg(p.prefix + wi_ + 1) <= idx) ++wi_;
-      const WorkItem wi = p.items[wi_];
-      const int64_t local = idx - __ldg(p.prefix + wi_);
-      // triple order inside an item: term fastest, then ket, then bra
-      const int ti = int(local % wi.nt);
-      const int64_t rest = local / wi.nt;
-      const int kj = int(rest % wi.nk);
-      const int bj = int(rest / wi.nk);
-      const int b = __ldg(p.perm + wi.bra_off + bj);
-      const int k = __ldg(p.perm + wi.ket_off + kj);
-      const TermSector ts = p.ts[wi.ts_off + ti];
-      const T me = dressed_element<T>(ts, w, op, p.cfg + int64_t(b) * p.N, p.cfg + int64_t(k) * p.N);
-      key = b;
-      const T* ck = cin + int64_t(k) * R;
+  for (int r = 0; r < RV; ++r) acc[r] = T(0);
+  for (int64_t idx = t0; idx < t1; ++idx) {
+    const TermSector ts = p.ts[it.ts_off + ti];
+    const T me = dressed_element<T>(ts, w, op, rb, rk);
+    const T* ck = cin + int64_t(k) * R;
 #pragma unroll
-      for (int r = 0; r < RV; ++r)
-        if (r < R) val[r] = me * ck[r];
-    }
-    // segmented suffix sums over runs of equal bra rows, then one atomic per run.
-    // The same bra can come back later in the warp (a new work item), so a lane
-    // only sums up to the next run head, never across another run.
-    const int prev = __shfl_up_sync(0xffffffffu, key, 1);
-    const bool head = (lane == 0) || (prev != key);
-    const unsigned heads = __ballot_sync(0xffffffffu, head);
-    const unsigned after = heads & ~((2u << lane) - 1u);
-    const int seg_end = after ? (__ffs(int(after)) - 1) : 32;
+    for (int r = 0; r < RV; ++r)
+      if (r < R) acc[r] = fma(me, __ldg(ck + r), acc[r]);
+    if (idx + 1 == t1) break;
+    // advance to the next triple
+    if (++ti == it.nt) {
+      ti = 0;
+      if (++kj == it.nk) {
+        kj = 0;
+        if (++bj == it.nb) {  // next work item
+          bj = 0;
+          ++wi;
+          it = p.items[wi];
+        }
+        const int nb_row = __ldg(p.perm + it.bra_off + bj);
+        if (nb_row != b) {
+          flush_row<T, RR>(sig, b, acc, R);
 #pragma unroll
-    for (int off = 1; off < 32; off <<= 1) {
-      const bool take = (lane + off < seg_end);
-#pragma unroll
-      for (int r = 0; r < RV; ++r) {
-        if (r < R) {
-          T vo = __shfl_down_sync(0xffffffffu, val[r], off);
-          if (take) val[r] += vo;
+          for (int r = 0; r < RV; ++r) acc[r] = T(0);
+          b = nb_row;
+          rb = __ldg(cfg + b);
         }
       }
-    }
-    if (head && key >= 0) {
-#pragma unroll
-      for (int r = 0; r < RV; ++r)
-        if (r < R) atomicAdd(sig + int64_t(key) * R + r, val[r]);
+      k = __ldg(p.perm + it.ket_off + kj);
+      rk = __ldg(cfg + k);
     }
   }
+  flush_row<T, RR>(sig, b, acc, R);
 }
 
 template <typename T>
@@ -343,7 +423,7 @@ __global__ void diag_terms_kernel(DiagParams p, const double* __restrict__ op, c
   if (i >= n) return;
   const int16_t* f = p.sec_fock + int64_t(p.row_sector[i]) * 2 * p.N;
   double s = 0.0;
-  for (int z = 0; z < n_zero; ++z) s += diag_element(p, p.terms[zero_terms[z]], op, ints, f, p.cfg + i * p.N);
+  for (int z = 0; z < n_zero; ++z) s += diag_element(p, p.terms[zero_terms[z]], op, ints, f, p.cfg + i * kCfgStride);
   hd[i] = s;
 }
 
@@ -360,7 +440,7 @@ __global__ void diag_op_kernel(DiagParams p, const double* __restrict__ op, int 
       continue;
     }
     BlockInfo bi = p.blocks[bl];
-    int st = p.cfg[i * p.N + c];
+    int st = p.cfg[i * kCfgStride + c];
     s += op[bi.off + st + int64_t(bi.mb) * st];
   }
   hd[i] = s;
@@ -469,11 +549,24 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
     FCG_REQUIRE(r[9] >= 0 && r[9] + r[6] * r[7] * r[8] <= n_data, FCG_EINVAL, "block table: data out of range");
     int64_t i = dense_block_index(s, int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5]));
     ctx->h_blk_index[i] = int32_t(b);
-    ctx->h_blocks[b] = BlockInfo{r[9], int32_t(r[6]), int32_t(r[7]), int32_t(r[8]), 0};
   }
-  std::vector<float> d32(data, data + n_data);
-  FCG_CUDA(ctx->d_op64.upload(data, n_data, ctx->stream));
-  FCG_CUDA(ctx->d_op32.upload(d32.data(), n_data, ctx->stream));
+  // device copy: every block starts on a multiple of kAlign elements (16-byte vector loads
+  // of TDM columns whose length is a multiple of 4)
+  int64_t cursor = 0;
+  for (int64_t b = 0; b < n_blocks; ++b) {
+    const int64_t* r = &ctx->opb[b * kOpbCols];
+    cursor = (cursor + kAlign - 1) / kAlign * kAlign;
+    ctx->h_blocks[b] = BlockInfo{cursor, int32_t(r[6]), int32_t(r[7]), int32_t(r[8]), 0};
+    cursor += r[6] * r[7] * r[8];
+  }
+  std::vector<double> d64(size_t(std::max<int64_t>(cursor, 1)), 0.0);
+  for (int64_t b = 0; b < n_blocks; ++b) {
+    const int64_t* r = &ctx->opb[b * kOpbCols];
+    std::memcpy(&d64[ctx->h_blocks[b].off], data + r[9], sizeof(double) * r[6] * r[7] * r[8]);
+  }
+  std::vector<float> d32(d64.begin(), d64.end());
+  FCG_CUDA(ctx->d_op64.upload(d64.data(), d64.size(), ctx->stream));
+  FCG_CUDA(ctx->d_op32.upload(d32.data(), d32.size(), ctx->stream));
   FCG_CUDA(ctx->d_blocks.upload(ctx->h_blocks.data(), ctx->h_blocks.size(), ctx->stream));
   FCG_CUDA(ctx->d_blk_index.upload(ctx->h_blk_index.data(), ctx->h_blk_index.size(), ctx->stream));
   {
@@ -617,7 +710,12 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   for (size_t sct = 0; sct < P.sec_start.size(); ++sct)
     for (int64_t i = 0; i < P.sec_count[sct]; ++i) row_sector[P.sec_start[sct] + i] = int32_t(sct);
   ctx->n_cfg = n_cfg;
-  FCG_CUDA(ctx->d_cfg.upload(cfg, size_t(n_cfg) * ctx->N, ctx->stream));
+  {
+    std::vector<int16_t> cfg8(size_t(n_cfg) * kCfgStride, 0);
+    for (int64_t i = 0; i < n_cfg; ++i)
+      for (int c = 0; c < ctx->N; ++c) cfg8[i * kCfgStride + c] = cfg[i * ctx->N + c];
+    FCG_CUDA(ctx->d_cfg.upload(cfg8.data(), cfg8.size(), ctx->stream));
+  }
   FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
   FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
   FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));

@@ -115,7 +115,7 @@ __global__ void screen_kernel(OpenParams p, const double* __restrict__ wmax, con
   const OpenTerm& o = p.ot[I.ot_off + ti];
   const double maxc = row_maxabs(p.c + int64_t(row) * p.R, p.R);
   if (!(maxc > 0.0)) return;
-  const double bnd = job_bound(o, wmax, gmax, p.cfg + int64_t(row) * p.N);
+  const double bnd = job_bound(o, wmax, gmax, p.cfg + int64_t(row) * kCfgStride);
   // keep unless every |x| <= bnd < thresh / maxc (a 1e-9 margin covers the bound's rounding)
   if (!(bnd * (1.0 + 1e-9) > p.thresh / maxc)) return;
   const unsigned long long pos = atomicAdd(counters + 0, 1ull);
@@ -169,7 +169,7 @@ __global__ void expand_kernel(OpenParams p, const int2* __restrict__ kept, const
     b[a] = int(loc % o.mb_act[a]);
     loc /= o.mb_act[a];
   }
-  const int16_t* ck = p.cfg + int64_t(job.x) * p.N;
+  const int16_t* ck = p.cfg + int64_t(job.x) * kCfgStride;
   const double* wc = w + ts.w_off + int64_t(ts.rest_len) * (b[0] + int64_t(ts.w_mb) * ck[ts.cw]);
   double x;
   if (ts.nrem == 0) {

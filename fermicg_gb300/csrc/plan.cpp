@@ -356,6 +356,7 @@ std::string build_dress(int N, const std::vector<int>& norb, int nmax, const std
         if (bl < 0) continue;
         const BlockInfo& B = blocks[bl];
         if (nb > 1 && B.nidx != r[22 + pos]) return "term dims do not match the TDM block";
+        w_total = (w_total + kAlign - 1) / kAlign * kAlign;  // vector-load alignment of W blocks
         DressJob J{};
         J.w_off = w_total;
         J.g_off = B.off;

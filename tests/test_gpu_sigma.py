@@ -85,8 +85,27 @@ def test_empty_and_single_row_states():
     np.testing.assert_allclose(g.sigma_closed(x), O.sigma_closed(f[:1], c[:1], x), rtol=1e-12)
 
 
-def _open_dict(of, oc, ov):
-    return {(of[i].tobytes(), oc[i].tobytes()): ov[i] for i in range(len(of))}
+def _canon(of, oc, ov):
+    """Rows of an open sigma as (sorted uint64 keys, values in key order)."""
+    f = of.reshape(len(of), -1).astype(np.uint64)
+    c = oc.astype(np.uint64)
+    k1 = np.zeros(len(of), dtype=np.uint64)
+    for j in range(f.shape[1]):
+        k1 = (k1 << np.uint64(4)) | f[:, j]
+    k2 = np.zeros(len(of), dtype=np.uint64)
+    for j in range(c.shape[1]):
+        k2 = (k2 << np.uint64(8)) | c[:, j]
+    order = np.lexsort((k2, k1))
+    return np.stack([k1[order], k2[order]], axis=1), ov[order]
+
+
+def _assert_open_equal(out, ref):
+    ko, vo = _canon(*out)
+    kr, vr = _canon(*ref)
+    assert ko.shape == kr.shape, (ko.shape, kr.shape)
+    assert np.array_equal(ko, kr)
+    scale = np.abs(vr).max()
+    assert np.abs(vo - vr).max() <= 1e-10 * scale
 
 
 @pytest.mark.parametrize("thresh", [0.0, 1e-4])
@@ -96,26 +115,31 @@ def test_open_sigma_full_space_matches_oracle(thresh):
     g, po, pt, f, c = _gpu_for(prob, st)
     O = oracle.Oracle(po, pt)
     x = np.random.default_rng(11).standard_normal((len(st), 2))
-    ref = _open_dict(*O.sigma_open(f, c, x, thresh))
-    out = _open_dict(*g.sigma_open(x, thresh))
-    assert set(out) == set(ref)
-    scale = max(np.abs(v).max() for v in ref.values())
-    for k, v in ref.items():
-        np.testing.assert_allclose(out[k], v, rtol=0, atol=1e-10 * scale)
+    _assert_open_equal(g.sigma_open(x, thresh), O.sigma_open(f, c, x, thresh))
 
 
-@pytest.mark.parametrize("thresh,nbody", [(1e-5, 4), (1e-3, 4), (1e-4, 2)])
-def test_open_sigma_config1_subspace_matches_oracle(thresh, nbody):
-    prob, st = config1_subspace(400, 2)
+@pytest.mark.parametrize("n_cfg,thresh,nbody", [(120, 1e-5, 4), (400, 1e-3, 4), (400, 1e-4, 2)])
+def test_open_sigma_config1_subspace_matches_oracle(n_cfg, thresh, nbody):
+    prob, st = config1_subspace(n_cfg, 2)
     g, po, pt, f, c = _gpu_for(prob, st)
     O = oracle.Oracle(po, pt)
     x = st.get_vector()
-    ref = _open_dict(*O.sigma_open(f, c, x, thresh, nbody=nbody))
-    out = _open_dict(*g.sigma_open(x, thresh, nbody=nbody))
-    assert len(ref) > len(st)
-    assert set(out) == set(ref)
-    scale = max(np.abs(v).max() for v in ref.values())
-    for k, v in ref.items():
-        np.testing.assert_allclose(out[k], v, rtol=0, atol=1e-10 * scale)
+    ref = O.sigma_open(f, c, x, thresh, nbody=nbody)
+    assert len(ref[0]) > len(st)
+    _assert_open_equal(g.sigma_open(x, thresh, nbody=nbody), ref)
     s = g.stats()
     assert s["open_jobs_kept"] <= s["open_jobs"]
+
+
+@pytest.mark.parametrize("R", [5, 7])
+def test_closed_sigma_many_roots(R):
+    """Root counts outside the specialised kernels (generic path) on uneven cluster sizes."""
+    prob = workloads.build_problem(10, [2, 2, 4, 2], [(1, 1), (1, 1), (2, 2), (1, 0)], 8, 4, max_roots=1000)
+    st = workloads.energy_ordered_space(prob, 600, R=R, seed=2)
+    g, po, pt, f, c = _gpu_for(prob, st)
+    O = oracle.Oracle(po, pt)
+    x = st.get_vector()
+    ref = O.sigma_closed(f, c, x)
+    assert rel_err(g.sigma_closed(x, "fp64"), ref) < FP64_TOL
+    assert rel_err(g.sigma_closed(x, "fp32"), ref) < FP32_TOL
+    np.testing.assert_allclose(g.diagonal(), O.diagonal_H(f, c), rtol=1e-12, atol=1e-12)

@@ -67,3 +67,39 @@ def test_gpu_tpsci_h12_matches_reference_energies():
     e2 = T.pt2_energy(v0, thresh_foi=m["pt2_thresh_foi"])
     np.testing.assert_allclose(np.abs(e0 + e2), np.abs(np.array(m["e0_plus_e2"])), atol=1e-8, rtol=0)
     T.close()
+
+
+def test_davidson_seven_roots_from_padded_guess():
+    """The solve of the second H12 TPSCI iteration: 7 roots, previous eigenvectors padded with
+    zeros for the new configurations (the oracle driver produces the space)."""
+    from oracle.tpsci import OracleTPSCI, _add, _copy, _zero
+    from fermicg_gb300.state import TPSCIstate as TS
+    ints, z, m, b, ops, H = _h12()
+    R, N = m["nroots"], len(m["clusters"])
+    st = TS(N, R)
+    ref = tuple(map(tuple, m["init_fspace"]))
+    row = np.zeros(R)
+    row[0] = 1.0
+    st[(ref, (0,) * N)] = row
+    for i, ex in enumerate(m["excitons"]):
+        row = np.zeros(R)
+        row[i + 1] = 1.0
+        st[(ref, tuple(ex))] = row
+    kw = m["tpsci_kwargs"]
+    T = OracleTPSCI(ops, b, H)
+    e1, v1 = T.tpsci_ci(st, thresh_cipsi=kw["thresh_cipsi"], thresh_foi=kw["thresh_foi"], max_iter=2,
+                        conv_thresh=0.0)
+    # v1 is the 2nd-iteration variational vector; rebuild its padded guess
+    f, c, v, _ = pack.pack_state(v1)
+    po, pt = pack.pack_ops(ops, b), pack.pack_terms(H)
+    Hd = oracle.Oracle(po, pt).build_H(f, c)
+    ref_e = np.linalg.eigvalsh(0.5 * (Hd + Hd.T))[:R]
+    g = GpuSigma(0)
+    g.set_ops(po)
+    g.set_terms(pt)
+    g.state_set(f, c)
+    guess = np.zeros_like(v)
+    guess[:R] = np.eye(R)
+    e, X, res, it = g.davidson(guess, tol=1e-9, max_iter=300)
+    assert np.all(np.isfinite(X))
+    assert np.abs(e - ref_e).max() < 1e-9, (e, ref_e)
