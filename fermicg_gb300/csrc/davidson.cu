@@ -196,62 +196,87 @@ struct DavidsonWork {
   }
 };
 
-// Orthonormalise columns [0, b) of T against V[:, 0..nv) (classical GS, twice) and among
-// themselves (Cholesky of the Gram matrix, dropping directions below lindep); the kept
-// columns are packed to the front.  Returns the kept count in *kept.
-int orthonormalize_block(DavidsonWork& W, double* Tp, int b, const double* Vp, int nv, double lindep, int* kept) {
+// Orthonormalise columns [0, b) of T against V[:, 0..nv) and among themselves; the kept
+// columns are packed to the front and their count returned in *kept.  Every column is
+// first scaled to unit norm, then projected out of V (classical Gram-Schmidt, twice); a
+// direction is dropped when less than `drop` of it survives the projection (it lies in
+// the subspace already, up to rounding).  The survivors are orthonormalised by Cholesky
+// QR, twice.
+int orthonormalize_block(DavidsonWork& W, double* Tp, int b, const double* Vp, int nv, double drop, int* kept) {
   fcg_ctx* ctx = W.ctx;
   std::vector<double> S;
   int rc;
-  for (int pass = 0; pass < 2 && nv > 0; ++pass) {
-    if ((rc = W.gram(Vp, nv, Tp, b, S))) return rc;
-    if ((rc = W.update(Vp, nv, S, b, Tp, 2))) return rc;
-  }
-  // normalise each column first, drop tiny ones
-  if ((rc = W.gram(Tp, b, Tp, b, S))) return rc;
+  auto scale_to_unit = [&](int m, std::vector<int>& keep, double floor2) -> int {
+    if ((rc = W.gram(Tp, m, Tp, m, S))) return rc;
+    keep.clear();
+    std::vector<double> D(size_t(m) * m, 0.0);
+    for (int j = 0; j < m; ++j) {
+      const double n2 = S[j + m * j];
+      if (std::isfinite(n2) && n2 > floor2) {
+        D[j + m * j] = 1.0 / std::sqrt(n2);
+        keep.push_back(j);
+      }
+    }
+    FCG_CUDA(cudaMemcpyAsync(W.small.p, D.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
+    scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return FCG_OK;
+  };
+  auto pack = [&](const std::vector<int>& keep) -> int {
+    for (size_t q = 0; q < keep.size(); ++q)
+      if (int(q) != keep[q])
+        FCG_CUDA(cudaMemcpyAsync(Tp + W.n * q, Tp + W.n * keep[q], sizeof(double) * W.n, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+    return FCG_OK;
+  };
   std::vector<int> keep;
-  for (int j = 0; j < b; ++j)
-    if (S[j + b * j] > lindep * lindep) keep.push_back(j);
-  // pack kept columns
-  for (size_t q = 0; q < keep.size(); ++q)
-    if (int(q) != keep[q])
-      FCG_CUDA(cudaMemcpyAsync(Tp + W.n * q, Tp + W.n * keep[q], sizeof(double) * W.n, cudaMemcpyDeviceToDevice,
-                               ctx->stream));
+  if ((rc = scale_to_unit(b, keep, 1e-300))) return rc;
+  if ((rc = pack(keep))) return rc;
   int m = int(keep.size());
+  if (m > 0 && nv > 0) {
+    for (int pass = 0; pass < 2; ++pass) {
+      if ((rc = W.gram(Vp, nv, Tp, m, S))) return rc;
+      if ((rc = W.update(Vp, nv, S, m, Tp, 2))) return rc;
+    }
+    // what survived the projection, relative to the unit input
+    if ((rc = scale_to_unit(m, keep, drop * drop))) return rc;
+    if ((rc = pack(keep))) return rc;
+    m = int(keep.size());
+  }
   for (int it = 0; it < 2 && m > 0; ++it) {
     if ((rc = W.gram(Tp, m, Tp, m, S))) return rc;
-    // modified Cholesky: drop columns whose remaining norm falls below lindep
-    std::vector<double> Lc(size_t(m) * m, 0.0);  // upper triangular R with S = R^T R
-    std::vector<int> good;
+    // Cholesky S = R^T R, stopping at the first column that is dependent on the previous ones
+    std::vector<double> Lc(size_t(m) * m, 0.0);
+    int good = 0;
     for (int j = 0; j < m; ++j) {
       double d = S[j + m * j];
       for (int p = 0; p < j; ++p) d -= Lc[p + m * j] * Lc[p + m * j];
-      if (d <= lindep * lindep) break;  // stop at the first dependent column
+      if (!(d > drop * drop * S[j + m * j])) break;
       Lc[j + m * j] = std::sqrt(d);
       for (int q = j + 1; q < m; ++q) {
         double v = S[j + m * q];
         for (int p = 0; p < j; ++p) v -= Lc[p + m * j] * Lc[p + m * q];
         Lc[j + m * q] = v / Lc[j + m * j];
       }
-      good.push_back(j);
+      ++good;
     }
-    m = int(good.size());
+    m = good;
     if (m == 0) break;
-    // inverse of the leading m x m block of R (upper triangular), column-major
-    std::vector<double> Ri(size_t(m) * m, 0.0);
+    std::vector<double> Ri(size_t(m) * m, 0.0);  // inverse of the leading m x m block of R
     for (int j = 0; j < m; ++j) {
       Ri[j + m * j] = 1.0 / Lc[j + m * j];
       for (int i = j - 1; i >= 0; --i) {
-        double s = 0.0;
-        for (int p = i + 1; p <= j; ++p) s += Lc[i + m * p] * Ri[p + m * j];
-        Ri[i + m * j] = -s / Lc[i + m * i];
+        double s2 = 0.0;
+        for (int p = i + 1; p <= j; ++p) s2 += Lc[i + m * p] * Ri[p + m * j];
+        Ri[i + m * j] = -s2 / Lc[i + m * i];
       }
     }
     FCG_CUDA(cudaMemcpyAsync(W.small.p, Ri.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
     scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
     FCG_CUDA(cudaGetLastError());
     FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (nv > 0) {  // one more projection pass for safety after the rescaling
+    if (nv > 0) {  // restore orthogonality to V lost in the rescaling
       if ((rc = W.gram(Vp, nv, Tp, m, S))) return rc;
       if ((rc = W.update(Vp, nv, S, m, Tp, 2))) return rc;
     }
@@ -301,11 +326,13 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
     FCG_CUDA(cudaMemcpyAsync(W.hd.p, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
   }
   int prec = precision;  // current sigma precision
+  // a new direction must keep at least this fraction of its norm after projection
+  const double drop = std::max(lindep, 1e-8);
   const double switch_tol = std::max(tol, 1e-5);
   // initial block
   FCG_CUDA(cudaMemcpyAsync(W.V.p, v0, sizeof(double) * n * R, cudaMemcpyHostToDevice, ctx->stream));
   int nv = 0, m = 0, rc;
-  if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, lindep, &m))) return rc;
+  if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, drop, &m))) return rc;
   if (m != R) {
     double nrm_min = 1e300, nrm_max = 0.0;
     int nonfinite = 0;
@@ -375,7 +402,7 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
       FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
       if (switching) {
         prec = FCG_FP64;
-        if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, lindep, &m))) return rc;
+        if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, drop, &m))) return rc;
         if ((rc = fcg_sigma_closed_device(ctx, R, W.V.p, W.AV.p, prec))) return rc;
         ++sigma_calls;
         nv = R;
@@ -384,9 +411,16 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
       FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.HX.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
       nv = R;
     }
-    // new directions: preconditioned residuals, orthonormalised against the subspace
-    FCG_CUDA(cudaMemcpyAsync(W.V.p + n * nv, W.T.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
-    if ((rc = orthonormalize_block(W, W.V.p + n * nv, R, W.V.p, nv, lindep, &m))) return rc;
+    // new directions: preconditioned residuals of the roots not yet converged,
+    // orthonormalised against the subspace
+    int nt = 0;
+    for (int j = 0; j < R; ++j)
+      if (rn[j] >= tol || prec == FCG_FP32) {
+        FCG_CUDA(cudaMemcpyAsync(W.V.p + n * (nv + nt), W.T.p + n * j, sizeof(double) * n,
+                                 cudaMemcpyDeviceToDevice, ctx->stream));
+        ++nt;
+      }
+    if ((rc = orthonormalize_block(W, W.V.p + n * nv, nt, W.V.p, nv, drop, &m))) return rc;
     if (m == 0) {  // the subspace cannot grow: converged as far as lindep allows
       converged = rmax < tol;
       break;
