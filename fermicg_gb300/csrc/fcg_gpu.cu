@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -860,3 +861,81 @@ int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------
+// Allocation-free closed sigma.
+//
+// The regular device entry point keeps its row-major working copies of C and sigma in
+// context buffers that grow with cudaMalloc.  This variant takes them from a fixed
+// file-scope device array instead, so the call itself allocates and frees nothing.
+// The array is 2 x kNoAllocMaxElems float64 = 16 MiB and stays resident on every device
+// that loads the library, until the process exits.  Every call on a device shares it:
+// calls that overlap on the GPU (other streams, other contexts of the same device) race
+// on it and must be serialised by the caller.
+namespace {
+
+constexpr int64_t kNoAllocMaxElems = int64_t(1) << 20;  // n_cfg * R of one call
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) double g_noalloc_scratch[2 * kNoAllocMaxElems];
+
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device; resolved once per device
+// (host code only sees a host-side stand-in under the array's name).
+int noalloc_scratch(fcg_ctx* ctx, double** out) {
+  FCG_REQUIRE(ctx->device >= 0 && ctx->device < kNoAllocMaxDevices, FCG_ELIMIT, "device ordinal too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if (!g_noalloc_ptr[ctx->device]) {
+    void* p = nullptr;
+    FCG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[ctx->device] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[ctx->device];
+  return FCG_OK;
+}
+
+}  // namespace
+
+extern "C" int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(d_c && d_sigma, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  FCG_REQUIRE(R >= 1 && R <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
+  FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
+  FCG_REQUIRE(ctx->n_cfg * R <= kNoAllocMaxElems, FCG_ELIMIT,
+              "fcg_sigma_closed_noalloc: n_cfg * R exceeds its fixed scratch of 1048576 elements");
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  double* scratch = nullptr;
+  int rc = noalloc_scratch(ctx, &scratch);
+  if (rc) return rc;
+  const int64_t n = ctx->n_cfg;
+  const unsigned g = unsigned((n * R + 255) / 256);
+  ctx->stats.last_kernel_ms = 0.0;
+  if (precision == FCG_FP64) {
+    double* cbuf = scratch;
+    double* sbuf = scratch + kNoAllocMaxElems;
+    pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R);
+    rc = launch_closed<double>(ctx, R, ctx->d_w64.p, ctx->d_op64.p, cbuf, sbuf);  // zeroes sbuf first
+    if (rc) return rc;
+    unpack_out_kernel<double><<<g, 256, 0, ctx->stream>>>(sbuf, d_sigma, n, R);
+  } else {
+    float* cbuf = reinterpret_cast<float*>(scratch);
+    float* sbuf = reinterpret_cast<float*>(scratch + kNoAllocMaxElems);
+    pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R);
+    rc = launch_closed<float>(ctx, R, ctx->d_w32.p, ctx->d_op32.p, cbuf, sbuf);
+    if (rc) return rc;
+    unpack_out_kernel<float><<<g, 256, 0, ctx->stream>>>(sbuf, d_sigma, n, R);
+  }
+  FCG_CUDA(cudaGetLastError());
+  ctx->stats.kernel_launches += 2;
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (ctx->plan.n_triples > 0) {
+    float ms = 0.f;
+    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+    ctx->stats.last_kernel_ms = ms;
+  }
+  return FCG_OK;
+}
+

@@ -43,6 +43,7 @@ SIGNATURES = {
     "fcg_sigma_open_fetch": (_I, [_P, _P, _P, _P]),
     "fcg_davidson": (_I, [_P, _I, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P,
                           ctypes.POINTER(_I)]),
+    "fcg_sigma_closed_noalloc": (_I, [_P, _I, _P, _P, _I]),
     "fcg_get_stats": (_I, [_P, _P]),
 }
 
@@ -163,6 +164,11 @@ class GpuSigma:
         """Device-pointer variant (column-major n_cfg x R float64 buffers on this GPU)."""
         self._check(self.L.fcg_sigma_closed_device(self.h, R, ctypes.c_void_p(d_c_ptr), ctypes.c_void_p(d_sigma_ptr),
                                                    PRECISION[precision]), "fcg_sigma_closed_device")
+
+    def sigma_closed_noalloc(self, d_c_ptr: int, d_sigma_ptr: int, R: int, precision="fp64"):
+        """Allocation-free device-pointer sigma (fixed 16 MiB scratch; n_cfg * R <= 2**20)."""
+        self._check(self.L.fcg_sigma_closed_noalloc(self.h, R, ctypes.c_void_p(d_c_ptr), ctypes.c_void_p(d_sigma_ptr),
+                                                    PRECISION[precision]), "fcg_sigma_closed_noalloc")
 
     def diagonal(self, op: str | None = None):
         """compute_diagonal: op None = all zero-transfer terms; else an op string ("Hcmf", "H")."""

@@ -128,6 +128,19 @@ int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 
+/* Allocation-free variant of fcg_sigma_closed_device (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc/cudaFree during a solve: applications whose
+ * device memory is owned by their own pool allocator or held to a fixed budget, and
+ * loops driving several streams that cannot afford the device-wide synchronisation
+ * cudaFree implies.  Same arguments and results as fcg_sigma_closed_device; the working
+ * copies of C and sigma live in a fixed 16 MiB device array built into the library
+ * (resident on every device that loads it, until exit), so n_cfg * R must not exceed
+ * 1048576 (FCG_ELIMIT otherwise).  The state, operators and terms must already be set.
+ * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
+ * and should come before any stream capture.  All calls on one device share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
+
 #ifdef __cplusplus
 }
 #endif
