@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--n-cfg", type=int, default=100000)
     ap.add_argument("--roots", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the solve-latency stream")
     return ap.parse_args()
 
 
@@ -83,6 +84,56 @@ def cpu_reference(po, pt, f, c, v, budget_s, threads):
     frac = min(1.0, budget_s / est_full)
     dt, done = run(16, frac)
     return done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full build"
+
+
+def serving_benchmark(n_req=60, rate=200.0, seed=7):
+    """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
+    per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
+    stream.  Returns p50/p99 latency and solves/s per precision."""
+    from fermicg_gb300 import pack, workloads
+    from fermicg_gb300.serving import Request, SolveServer, latency_summary
+    shapes = [  # (name, builder, n_cfg, roots, share)
+        ("12o_4x3_full", lambda sd: workloads.build_problem(12, [3] * 4, [(2, 1), (1, 2), (2, 1), (1, 2)], 36, sd,
+                                                             max_roots=1000), 2000, 1, 0.6),
+        ("24o_6x4_M16", lambda sd: workloads.build_problem(24, [4] * 6, [(2, 2)] * 6, 72, sd, max_roots=16,
+                                                            delta_elec=2), 10000, 4, 0.3),
+        ("32o_8x4_M8", lambda sd: workloads.build_problem(32, [4] * 8, [(2, 2)] * 8, 96, sd, max_roots=8,
+                                                           delta_elec=2), 5000, 2, 0.1),
+    ]
+    pools = []
+    for k, (name, build, n_cfg, R, share) in enumerate(shapes):
+        pool = []
+        for j in range(2 if k < 2 else 1):
+            prob = build(1000 * (k + 1) + j)
+            st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=j)
+            f, c, v, _ = pack.pack_state(st)
+            guess = np.zeros_like(v)
+            guess[:R] = np.eye(R)
+            pool.append((pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, guess))
+        pools.append(pool)
+    rng = np.random.default_rng(seed)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    kinds = rng.choice(len(shapes), size=n_req, p=[sh[4] for sh in shapes])
+    picks = [int(rng.integers(len(pools[k]))) for k in kinds]
+    out = {}
+    for prec in ("fp32", "fp64"):
+        reqs = []
+        for i in range(n_req):
+            po, pt, f, c, guess = pools[kinds[i]][picks[i]]
+            reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
+                                shape=shapes[kinds[i]][0]))
+        srv = SolveServer(slots=4)
+        res = srv.run(reqs)
+        srv.close()
+        summ = latency_summary(res)
+        summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
+                                  for sh in shapes}
+        out["mixed" if prec == "fp32" else "fp64"] = summ
+    # same stream, same results: energies of mixed vs fp64 per request
+    out["requests"] = n_req
+    out["arrival_rate_per_s"] = rate
+    out["mix"] = {sh[0]: sh[4] for sh in shapes}
+    return out
 
 
 def clocks_sampler():
@@ -264,6 +315,11 @@ def main():
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
         "clocks": clocks,
     }
+    if rank == 0 and a.serving:
+        try:
+            out["serving"] = serving_benchmark()
+        except Exception as ex:
+            out["serving"] = {"error": str(ex)}
     if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1

@@ -1,0 +1,150 @@
+"""A request loop serving Davidson solves on one GPU (continuous batching).
+
+Requests (a problem = cluster operators + clustered Hamiltonian, a variational space,
+a starting guess, a root count and a tolerance) arrive over time.  A request is admitted
+as soon as a slot is free and its estimated HBM footprint fits the budget; admitted
+requests run concurrently, each on its own device context and CUDA stream, so their
+sigma builds and Davidson steps overlap on the GPU.  Operators, subspace vectors and the
+sigma plan of a request stay resident on the device for the whole solve.  Each request's
+latency runs from its arrival to its result.
+
+The per-request work is exactly the standalone solve (fcg_set_ops, fcg_set_terms,
+fcg_state_set, fcg_davidson), so a result does not depend on what else is in flight.
+"""
+from __future__ import annotations
+
+import heapq
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .gpu import GpuSigma
+
+
+@dataclass(order=True)
+class Request:
+    arrival: float
+    rid: int = field(compare=False)
+    packed_ops: object = field(compare=False, default=None)
+    packed_terms: object = field(compare=False, default=None)
+    focks: np.ndarray = field(compare=False, default=None)
+    cfgs: np.ndarray = field(compare=False, default=None)
+    guess: np.ndarray = field(compare=False, default=None)
+    tol: float = field(compare=False, default=1e-6)
+    precision: str = field(compare=False, default="fp64")
+    max_iter: int = field(compare=False, default=200)
+    shape: str = field(compare=False, default="")
+
+
+@dataclass
+class Result:
+    rid: int
+    shape: str
+    energies: np.ndarray
+    residuals: np.ndarray
+    iters: int
+    arrival: float
+    start: float
+    end: float
+
+    @property
+    def latency(self):
+        return self.end - self.arrival
+
+
+def footprint_bytes(req: Request) -> int:
+    """HBM a solve holds while admitted: operators (float64 + float32 copies), dressed
+    operators (estimated as 8x the TDM blob, both precisions), the state index, and the
+    Davidson subspace (2 x 12R vectors) plus sigma working copies."""
+    n = req.focks.shape[0]
+    R = req.guess.shape[1]
+    ops = req.packed_ops.data.size * 12
+    dressed = req.packed_ops.data.size * 8 * 12
+    ints = req.packed_terms.ints.size * 12
+    index = n * (16 + 8 * 60)
+    dav = n * 8 * (2 * (12 * R + R) + 6 * R)
+    return int(ops + dressed + ints + index + dav)
+
+
+class SolveServer:
+    def __init__(self, slots: int = 4, hbm_budget: float = 64e9, device: int = 0):
+        self.slots = slots
+        self.budget = hbm_budget
+        self.device = device
+        self._lock = threading.Condition()
+        self._in_use = 0
+        self._active = 0
+        self.results: list[Result] = []
+        self._ctx_pool = [None] * slots
+
+    def _run_one(self, slot: int, req: Request, fp: int):
+        start = time.perf_counter()
+        g = self._ctx_pool[slot]
+        if g is None:
+            g = GpuSigma(self.device)
+            self._ctx_pool[slot] = g
+        try:
+            g.set_ops(req.packed_ops)
+            g.set_terms(req.packed_terms)
+            g.state_set(req.focks, req.cfgs)
+            e, X, res, it = g.davidson(req.guess, tol=req.tol, max_iter=req.max_iter, precision=req.precision)
+            end = time.perf_counter()
+            with self._lock:
+                self.results.append(Result(req.rid, req.shape, e, res, it, req.arrival, start, end))
+        finally:
+            with self._lock:
+                self._in_use -= fp
+                self._active -= 1
+                self._free_slots.append(slot)
+                self._lock.notify_all()
+
+    def run(self, requests: list[Request], t0: float | None = None):
+        """Serve `requests` (arrival times relative to t0 = now); returns the results."""
+        pending = sorted(requests)
+        t0 = time.perf_counter() if t0 is None else t0
+        for r in pending:
+            r.arrival = t0 + r.arrival
+        self._free_slots = list(range(self.slots))
+        threads = []
+        queue: list = []
+        i = 0
+        while i < len(pending) or queue:
+            now = time.perf_counter()
+            while i < len(pending) and pending[i].arrival <= now:
+                heapq.heappush(queue, pending[i])
+                i += 1
+            admitted = False
+            with self._lock:
+                if queue and self._free_slots:
+                    fp = footprint_bytes(queue[0])
+                    if self._in_use + fp <= self.budget or self._active == 0:
+                        req = heapq.heappop(queue)
+                        slot = self._free_slots.pop()
+                        self._in_use += fp
+                        self._active += 1
+                        th = threading.Thread(target=self._run_one, args=(slot, req, fp), daemon=True)
+                        th.start()
+                        threads.append(th)
+                        admitted = True
+                if not admitted:
+                    wait = 0.01
+                    if i < len(pending):
+                        wait = max(0.0, min(wait, pending[i].arrival - time.perf_counter()))
+                    self._lock.wait(timeout=wait if wait > 0 else 0.0005)
+        for th in threads:
+            th.join()
+        return sorted(self.results, key=lambda r: r.rid)
+
+    def close(self):
+        for g in self._ctx_pool:
+            if g is not None:
+                g.close()
+
+
+def latency_summary(results: list[Result]):
+    lat = np.array([r.latency for r in results])
+    span = max(r.end for r in results) - min(r.arrival for r in results)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "solves_per_s": len(results) / span, "n": len(results)}

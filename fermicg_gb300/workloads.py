@@ -91,43 +91,78 @@ def energy_ordered_space(prob: Problem, n_cfg: int, R: int = 1, seed: int = 0):
     na_tot = sum(f[0] for f in prob.init_fspace)
     nb_tot = sum(f[1] for f in prob.init_fspace)
     et = _local_energy_tables(prob.bases)
-    # global sectors with the right electron count
+    # global sectors with the right electron count, enumerated by branch and bound on their
+    # lowest configuration energy: only sectors below a cutoff are visited, and the cutoff
+    # grows until n_cfg configurations lie below it (then no excluded sector can hold one
+    # of the n_cfg lowest configurations)
     secs = [sorted(b.basis.keys()) for b in prob.bases]
-    gsecs = []
+    lo_a = [0] * (N + 1)
+    hi_a = [0] * (N + 1)
+    lo_b = [0] * (N + 1)
+    hi_b = [0] * (N + 1)
+    emin = [0.0] * (N + 1)
+    for c in range(N - 1, -1, -1):
+        lo_a[c] = lo_a[c + 1] + min(s[0] for s in secs[c])
+        hi_a[c] = hi_a[c + 1] + max(s[0] for s in secs[c])
+        lo_b[c] = lo_b[c + 1] + min(s[1] for s in secs[c])
+        hi_b[c] = hi_b[c + 1] + max(s[1] for s in secs[c])
+        emin[c] = emin[c + 1] + min(float(et[c][s][0]) for s in secs[c])
 
-    def rec(c, cur, na, nb):
-        if c == N:
-            if na == na_tot and nb == nb_tot:
-                gsecs.append(tuple(cur))
-            return
-        for s in secs[c]:
-            cur.append(s)
-            rec(c + 1, cur, na + s[0], nb + s[1])
-            cur.pop()
+    def sectors_below(ecut):
+        out = []
 
-    rec(0, [], 0, 0)
-    # lazy k-best merge over sectors: per sector a best-first enumeration of state tuples
-    heap = []
-    gens = []
-    for gi, fs in enumerate(gsecs):
-        es = [et[c][fs[c]] for c in range(N)]
-        e0 = sum(float(e[0]) for e in es)
-        gens.append((fs, es))
-        heapq.heappush(heap, (e0, gi, (0,) * N))
-    seen = set((gi, (0,) * N) for gi in range(len(gsecs)))
-    chosen = []
-    while heap and len(chosen) < n_cfg:
-        e, gi, st = heapq.heappop(heap)
-        chosen.append((e, gi, st))
-        fs, es = gens[gi]
-        for c in range(N):
-            if st[c] + 1 < len(es[c]):
-                nst = st[:c] + (st[c] + 1,) + st[c + 1:]
-                if (gi, nst) in seen:
-                    continue
-                seen.add((gi, nst))
-                ne = e - float(es[c][st[c]]) + float(es[c][st[c] + 1])
-                heapq.heappush(heap, (ne, gi, nst))
+        def rec(c, cur, na, nb, e):
+            if e + emin[c] > ecut:
+                return
+            if c == N:
+                if na == na_tot and nb == nb_tot:
+                    out.append(tuple(cur))
+                return
+            if not (lo_a[c] <= na_tot - na <= hi_a[c] and lo_b[c] <= nb_tot - nb <= hi_b[c]):
+                return
+            for s in secs[c]:
+                cur.append(s)
+                rec(c + 1, cur, na + s[0], nb + s[1], e + float(et[c][s][0]))
+                cur.pop()
+
+        rec(0, [], 0, 0, 0.0)
+        return out
+
+    def k_best(gsecs, ecut):
+        heap = []
+        gens = []
+        for gi, fs in enumerate(gsecs):
+            es = [et[c][fs[c]] for c in range(N)]
+            gens.append((fs, es))
+            heap.append((sum(float(e[0]) for e in es), gi, (0,) * N))
+        heapq.heapify(heap)
+        seen = set((gi, (0,) * N) for gi in range(len(gsecs)))
+        chosen = []
+        while heap and len(chosen) < n_cfg:
+            e, gi, st = heapq.heappop(heap)
+            if e > ecut:
+                break
+            chosen.append((e, gi, st))
+            fs, es = gens[gi]
+            for c in range(N):
+                if st[c] + 1 < len(es[c]):
+                    nst = st[:c] + (st[c] + 1,) + st[c + 1:]
+                    if (gi, nst) in seen:
+                        continue
+                    seen.add((gi, nst))
+                    ne = e - float(es[c][st[c]]) + float(es[c][st[c] + 1])
+                    heapq.heappush(heap, (ne, gi, nst))
+        return chosen
+
+    e_floor = emin[0]
+    width = 1.0
+    while True:
+        ecut = e_floor + width
+        gsecs = sectors_below(ecut)
+        chosen = k_best(gsecs, ecut)
+        if len(chosen) >= n_cfg or width > 1e6:
+            break
+        width *= 2.0
     # group by sector; sector order = order of first appearance
     order = []
     by = {}
