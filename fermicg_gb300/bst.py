@@ -104,10 +104,12 @@ class PackedBST:
         return out
 
 
-def plan_triples(pb: PackedBST, ham, ops_lookup=None, nbody=4):
+def plan_triples(pb: PackedBST, ham, ops=None, nbody=4):
     """(bra block, ket block, term) triples of build_sigma! that pass check_term on
     TuckerConfigs, with the state sign of each (compute_terms_state_sign on the ket
-    sector).  Returns int32 [n][4] = {bra, ket, term index in pack_terms order, sign}."""
+    sector).  With `ops` (ClusterOps list), terms whose TDM block of an active cluster is
+    absent for the sector pair are left out (build_dense_H_term has nothing to contract).
+    Returns int32 [n][4] = {bra, ket, term index in pack_terms order, sign}."""
     N = pb.N
     term_index = {}
     ti = 0
@@ -139,6 +141,9 @@ def plan_triples(pb: PackedBST, ham, ops_lookup=None, nbody=4):
                 continue
             for t in terms:
                 if t.nbody > nbody:
+                    continue
+                if ops is not None and any((fb[c], fk[c]) not in ops[c].data.get(op, {})
+                                           for c, op in zip(t.clusters, t.ops)):
                     continue
                 act = frozenset(t.clusters)
                 g = group(fk, act)

@@ -10,7 +10,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfcg_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fcg_gpu.cu", "open_sigma.cu", "davidson.cu", "plan.cpp"]
+SOURCES = ["fcg_gpu.cu", "open_sigma.cu", "davidson.cu", "bst.cu", "plan.cpp"]
 
 
 def _nvcc():

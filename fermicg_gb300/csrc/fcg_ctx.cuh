@@ -119,6 +119,24 @@ struct fcg_ctx {
   std::vector<unsigned long long> open_keys;
   std::vector<double> open_vals;        // [n_out][R] row-major
   int open_R = 0;
+  // block-sparse Tucker vector structure and its operator cache (bst.cu)
+  bool have_bst = false;
+  int64_t bst_core_total = 0;
+  std::vector<BstBlock> bst_blocks;
+  std::vector<BstGroup> bst_groups;
+  std::vector<int32_t> bst_triples;     // [n][4] = {bra, ket, term, sign}
+  std::vector<int32_t> bst_small, bst_large;  // groups whose workspace fits shared memory / does not
+  int32_t bst_ws_large = 0;
+  int bst_list_R = 0;          // R and element size the two lists were made for
+  size_t bst_list_elem = 0;
+  DevBuf<BstBlock> d_bst_blocks;
+  DevBuf<BstGroup> d_bst_groups;
+  DevBuf<int32_t> d_bst_small, d_bst_large;
+  DevBuf<double> d_bst_factors;
+  DevBuf<double> d_bst_op64, d_bst_s64;
+  DevBuf<float> d_bst_op32, d_bst_s32;
+  DevBuf<double> d_bst_in64, d_bst_out64, d_bst_ws64;
+  DevBuf<float> d_bst_in32, d_bst_out32, d_bst_ws32;
   fcg_stats stats{};
 };
 

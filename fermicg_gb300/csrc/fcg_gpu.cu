@@ -592,6 +592,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   ctx->have_ops = true;
   ctx->have_terms = false;
   ctx->have_state = false;
+  ctx->have_bst = false;
   return FCG_OK;
 }
 
@@ -604,6 +605,7 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   FCG_CUDA(cudaSetDevice(ctx->device));
   ctx->have_terms = false;
   ctx->have_state = false;
+  ctx->have_bst = false;
   ctx->n_terms = n_terms;
   ctx->trm.assign(term_table, term_table + int64_t(n_terms) * kTrmCols);
   ctx->n_trans = n_transfers;

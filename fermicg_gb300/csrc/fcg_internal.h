@@ -108,6 +108,52 @@ struct DressJob {
   int32_t pad;
 };
 
+// ---- block-sparse Tucker (BST) vectors ---------------------------------------------------
+
+// One Tucker block (fock sector, TuckerConfig) of a BST vector on the device.
+struct BstBlock {
+  int64_t core_off;                    // core of root r at cores[r * core_total + core_off], column-major
+  int64_t factor_off[kMaxClusters];    // factor of cluster c: (len[c] x rank[c]) column-major
+  int32_t rank[kMaxClusters];
+  int32_t start[kMaxClusters];         // first local state of the range (0-based)
+  int32_t len[kMaxClusters];           // range length
+  int32_t core_len;
+  int32_t pad;
+};
+
+// Dressed TDM of one active cluster between a bra and a ket block:
+//   g[p, kb, kk] = sum_{I,J} U_bra[I, kb] G[p, start_bra + I, start_ket + J] U_ket[J, kk]
+struct BstGamma {
+  int64_t g_off;
+  int64_t tdm_off;   // TDM block in the device op blob
+  int32_t bra, ket, c;
+  int32_t np;        // orbital multi-index length of the TDM
+  int32_t tdm_mb;    // bra dimension of the TDM block
+  int32_t pad;
+};
+
+// One term's share of a group operator.
+struct BstGroupTerm {
+  int64_t g_off[4];  // dressed TDMs of the active clusters, in term order
+  int64_t ints_off;  // -1: 1-body term (coefficient 1)
+  int32_t np[4];
+  int32_t nact;
+  int32_t sign;      // compute_terms_state_sign on the ket sector (1 for 1-body terms)
+};
+
+// All terms that couple one bra block to one ket block through the same active clusters:
+//   OP[kk + k*kb] = (prod of scalar spectator overlaps) * sum_t sign_t sum_p ints_t[p] prod_a g_{t,a}[p_a, kb_a, kk_a]
+// (kk / kb: mixed-radix over the active clusters in increasing cluster order, ket / bra ranks).
+struct BstGroup {
+  int64_t op_off;
+  int64_t s_off[kMaxClusters];  // spectator overlap U_bra^T U_ket (rank_bra x rank_ket); -1 when both ranks are 1
+  int32_t bra, ket;
+  int32_t m, k;                 // products of the active bra / ket ranks
+  int32_t act_mask;
+  int32_t t_off, nt;            // terms in the group-term pool
+  int32_t ws;                   // largest intermediate tensor of the sigma step (elements per root)
+};
+
 // Problem description the planner needs (host copies).
 struct ProblemInfo {
   int N = 0;

@@ -45,6 +45,10 @@ SIGNATURES = {
                           ctypes.POINTER(_I)]),
     "fcg_sigma_closed_noalloc": (_I, [_P, _I, _P, _P, _I]),
     "fcg_get_stats": (_I, [_P, _P]),
+    "fcg_bst_set": (_I, [_P, _I, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
+    "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_bst_sigma_device": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_bst_triples": (_I, [_P, _P]),
 }
 
 
@@ -55,7 +59,10 @@ class Stats(ctypes.Structure):
                 ("plan_seconds", ctypes.c_double), ("last_kernel_ms", ctypes.c_double),
                 ("kernel_launches", ctypes.c_int64), ("open_jobs", ctypes.c_int64),
                 ("open_jobs_kept", ctypes.c_int64), ("open_contractions", ctypes.c_int64),
-                ("davidson_sigma_calls", ctypes.c_int64)]
+                ("davidson_sigma_calls", ctypes.c_int64), ("bst_blocks", ctypes.c_int64),
+                ("bst_triples", ctypes.c_int64), ("bst_groups", ctypes.c_int64),
+                ("bst_cache_elements", ctypes.c_int64), ("bst_flops_reference", ctypes.c_int64),
+                ("bst_flops_executed", ctypes.c_int64), ("bst_cache_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -208,6 +215,42 @@ class GpuSigma:
                                         float(lindep), PRECISION[precision], int(bool(precond)), _ptr(e),
                                         _ptr(out), _ptr(res), ctypes.byref(it)), "fcg_davidson")
         return e, np.ascontiguousarray(out), res, it.value
+
+    # --- block-sparse Tucker ---------------------------------------------------
+    def bst_set(self, packed_bst, nbody=4):
+        """cache_hamiltonian for a BST structure (fermicg_gb300.bst.PackedBST); returns core_total."""
+        pb = packed_bst
+        N = pb.N
+        fock = np.ascontiguousarray(np.array([[list(f) for f in k[0]] for k in pb.keys], dtype=np.int16)
+                                    .reshape(-1, N, 2))
+        blocks = np.ascontiguousarray(pb.blocks[:, 5:5 + 3 * N], dtype=np.int64)
+        foff = np.ascontiguousarray(pb.factor_off, dtype=np.int64)
+        fac = np.ascontiguousarray(pb.factors, dtype=np.float64)
+        ct = ctypes.c_int64(0)
+        self._check(self.L.fcg_bst_set(self.h, int(nbody), blocks.shape[0], _ptr(fock), _ptr(blocks), _ptr(foff),
+                                       fac.size, _ptr(fac), ctypes.byref(ct)), "fcg_bst_set")
+        self.bst_core_total = ct.value
+        return ct.value
+
+    def bst_sigma(self, cores, precision="fp64"):
+        """build_sigma!: cores (R, core_total) -> sigma cores (R, core_total) float64."""
+        c = np.ascontiguousarray(cores, dtype=np.float64)
+        R = c.shape[0]
+        if c.shape[1] != self.bst_core_total:
+            raise ValueError("core length does not match the BST structure")
+        out = np.zeros_like(c)
+        self._check(self.L.fcg_bst_sigma(self.h, R, _ptr(c), _ptr(out), PRECISION[precision]), "fcg_bst_sigma")
+        return out
+
+    def bst_sigma_device(self, d_cores_ptr: int, d_sigma_ptr: int, R: int, precision="fp64"):
+        self._check(self.L.fcg_bst_sigma_device(self.h, R, ctypes.c_void_p(d_cores_ptr), ctypes.c_void_p(d_sigma_ptr),
+                                                PRECISION[precision]), "fcg_bst_sigma_device")
+
+    def bst_triples(self):
+        n = self.stats()["bst_triples"]
+        out = np.zeros((n, 4), dtype=np.int32)
+        self._check(self.L.fcg_bst_triples(self.h, _ptr(out)), "fcg_bst_triples")
+        return out
 
     def stats(self):
         s = Stats()

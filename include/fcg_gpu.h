@@ -62,6 +62,13 @@ typedef struct fcg_stats {
   int64_t open_jobs_kept;   /* of those, the ones the screen kept */
   int64_t open_contractions;/* (ket, term, bra tuple) elements evaluated */
   int64_t davidson_sigma_calls; /* sigma builds of the last fcg_davidson */
+  int64_t bst_blocks;       /* Tucker blocks of the last fcg_bst_set */
+  int64_t bst_triples;      /* (bra block, ket block, term) triples passing check_term */
+  int64_t bst_groups;       /* (bra block, ket block, active clusters) groups = cached operators */
+  int64_t bst_cache_elements; /* elements of the cached group operators */
+  int64_t bst_flops_reference; /* per root: sum over triples of 2*m*k*n + spectator transforms (reference count) */
+  int64_t bst_flops_executed;  /* per root: the same sums over groups (what one fcg_bst_sigma root does) */
+  double bst_cache_seconds; /* wall time of the last fcg_bst_set (planning + operator cache) */
 } fcg_stats;
 
 int fcg_version(void);
@@ -127,6 +134,42 @@ int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss
                  int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
+
+/* ---- block-sparse Tucker (BST) vectors ----------------------------------------------
+ * A BSTstate (src/type_BSTstate.jl:13-18) is flattened to blocks, one per (FockConfig,
+ * TuckerConfig) in iteration order:
+ *   fock     int16 [n_blocks][N][2]
+ *   blocks   int64 [n_blocks][3N] = {rank[N], range_start[N] (0-based), range_len[N]}
+ *            (the TuckerConfig UnitRanges and the Tucker ranks)
+ *   factor_off int64 [n_blocks][N]: offset in `factors` of each (range_len x rank) factor,
+ *            column-major (Tucker.factors)
+ *   cores    float64 [R][core_total]: each block's core (rank_1 x ... x rank_N, column-major,
+ *            cluster 0 fastest) at the block's core offset; blocks are concatenated in order,
+ *            so block b starts at sum_{b' < b} prod(rank of b').
+ * fcg_bst_set plans the (bra block, ket block, term) triples of build_sigma!
+ * (src/tucker_inner.jl:165-245: check_term on TuckerConfigs, terms of at most `nbody`
+ * clusters) and builds every dense term operator in the Tucker bases once, as
+ * cache_hamiltonian does (src/tucker_inner.jl:90-159, build_dense_H_term
+ * src/tucker_build_dense_H_term.jl:5-175).  Terms that couple the same two blocks
+ * through the same active clusters share one cached operator (their sign-weighted sum).
+ * The operators, terms and op blocks of this context must be set.  *core_total receives
+ * the core length of one root. */
+int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
+                const int64_t* factor_off, int64_t n_factors, const double* factors, int64_t* core_total);
+
+/* build_sigma! with the cache (src/tucker_inner.jl:165-245, form_sigma_block! :253-304,
+ * contract_dense_H_with_state src/tucker_contract_dense_H_with_state.jl:4-330):
+ * sigma = H * cores over the blocks of the last fcg_bst_set (sigma is overwritten; the
+ * reference adds into a zeroed sigma).  Host buffers [R][core_total].  precision:
+ * FCG_FP64, or FCG_FP32 (float32 operators, cores and accumulation). */
+int fcg_bst_sigma(fcg_ctx* ctx, int R, const double* cores, double* sigma, int precision);
+
+/* Same on device buffers [R][core_total] float64 of the context's device. */
+int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision);
+
+/* The triples of the last fcg_bst_set: int32 [bst_triples][4] = {bra block, ket block,
+ * term index (term-table row), state sign}. */
+int fcg_bst_triples(fcg_ctx* ctx, int32_t* out);
 
 /* Allocation-free variant of fcg_sigma_closed_device (no counterpart in the reference).
  * For callers that cannot call cudaMalloc/cudaFree during a solve: applications whose

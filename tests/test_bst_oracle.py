@@ -9,7 +9,7 @@ import oracle
 from oracle import bst
 from fermicg_gb300 import pack, workloads
 from fermicg_gb300.state import TPSCIstate
-from helpers import packed
+from helpers import packed, random_bst
 
 
 def _problem():
@@ -32,35 +32,6 @@ def _expand(prob, vec, N, R):
                     st[key] = np.zeros(R)
                 st.data[fock][cfg][r] += full[idx]
     return st
-
-
-
-
-def _random_vec(prob, N, R, rank_cut, seed, split):
-    rng = np.random.default_rng(seed)
-    na = sum(f[0] for f in prob.init_fspace)
-    nb = sum(f[1] for f in prob.init_fspace)
-    secs = [sorted(b.basis) for b in prob.bases]
-    vec = {}
-    for fs in itertools.product(*secs):
-        if sum(f[0] for f in fs) != na or sum(f[1] for f in fs) != nb:
-            continue
-        Ms = [prob.bases[c].basis[fs[c]].shape[1] for c in range(N)]
-        ranges_per_c = []
-        for M in Ms:
-            rs = [(0, M)] if (not split or M < 2) else [(0, 1), (1, M)]
-            ranges_per_c.append(rs)
-        for tcfg in itertools.product(*ranges_per_c):
-            factors, shape = [], []
-            for c in range(N):
-                L = tcfg[c][1] - tcfg[c][0]
-                rk = max(1, min(L, L - rank_cut)) if L > 1 else 1
-                Q, _ = np.linalg.qr(rng.standard_normal((L, L)))
-                factors.append(Q[:, :rk].copy())
-                shape.append(rk)
-            core = [rng.standard_normal(shape) for _ in range(R)]
-            vec[(fs, tcfg)] = {"core": core, "factors": factors}
-    return vec
 
 
 def _check(prob, vec, N, R):
@@ -89,7 +60,7 @@ def _check(prob, vec, N, R):
 
 def test_bst_sigma_full_rank_equals_tps_sigma():
     prob = _problem()
-    vec = _random_vec(prob, 3, 2, rank_cut=0, seed=1, split=False)
+    vec = random_bst(prob, 3, 2, rank_cut=0, seed=1, split=False)
     err, scale = _check(prob, vec, 3, 2)
     assert err < 1e-11 * scale
 
@@ -99,7 +70,7 @@ def test_bst_sigma_split_truncated_blocks_equals_projected_tps_sigma():
     of H on the expanded vector when the block spaces do not overlap (they don't: ranges
     partition each sector)."""
     prob = _problem()
-    vec = _random_vec(prob, 3, 2, rank_cut=1, seed=2, split=True)
+    vec = random_bst(prob, 3, 2, rank_cut=1, seed=2, split=True)
     err, scale = _check(prob, vec, 3, 2)
     assert err < 1e-11 * scale
 
@@ -108,6 +79,37 @@ def test_bst_sigma_four_clusters_with_4body_terms():
     prob = workloads.build_problem(6, [2, 1, 2, 1], [(1, 1), (1, 0), (1, 1), (0, 1)], 6, 7, max_roots=1000,
                                    cmf=False)
     assert any(t.nbody == 4 for tr, ts in prob.ham for t in ts)
-    vec = _random_vec(prob, 4, 1, rank_cut=1, seed=3, split=True)
+    vec = random_bst(prob, 4, 1, rank_cut=1, seed=3, split=True)
     err, scale = _check(prob, vec, 4, 1)
     assert err < 1e-11 * scale
+
+
+def test_bst_planner_matches_check_term_enumeration():
+    """plan_triples enumerates exactly the (bra, ket, term) triples that build_sigma!'s loops
+    accept through check_term on TuckerConfigs and then contract (TDM blocks present)."""
+    from fermicg_gb300.bst import PackedBST, plan_triples
+    from fermicg_gb300.terms import compute_terms_state_sign
+    prob = workloads.build_problem(6, [2, 1, 2, 1], [(1, 1), (1, 0), (1, 1), (0, 1)], 6, 7, max_roots=1000,
+                                   cmf=False)
+    N = 4
+    vec = random_bst(prob, N, 1, rank_cut=1, seed=3, split=True)
+    pb = PackedBST(vec, N, 1)
+    got = {tuple(int(x) for x in r) for r in plan_triples(pb, prob.ham, ops=prob.ops)}
+    tindex = {}
+    for tr, terms in prob.ham:
+        for t in terms:
+            tindex[id(t)] = len(tindex)
+    want = set()
+    for b, (fb, tb) in enumerate(pb.keys):
+        for k, (fk, tk) in enumerate(pb.keys):
+            tr = tuple((fb[c][0] - fk[c][0], fb[c][1] - fk[c][1]) for c in range(N))
+            for t in prob.ham.trans.get(tr, []):
+                if not bst.check_term_tucker(t, fb, tb, fk, tk):
+                    continue
+                # the oracle's build_dense_H_term skips a term whose TDM block is absent
+                if any((fb[c], fk[c]) not in prob.ops[c].data.get(op, {}) for c, op in zip(t.clusters, t.ops)):
+                    continue
+                sgn = 1 if t.nbody == 1 else compute_terms_state_sign(t, fk)
+                want.add((b, k, tindex[id(t)], sgn))
+    assert len(want) > 1000
+    assert got == want
