@@ -42,6 +42,9 @@ def parse():
     ap.add_argument("--roots", type=int, default=4)
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the solve-latency stream")
+    ap.add_argument("--no-bst", dest="bst", action="store_false", help="skip the block-sparse Tucker sigma leg")
+    ap.add_argument("--bst-only", action="store_true", help="run only the block-sparse Tucker sigma leg")
+    ap.add_argument("--bst-sectors", type=int, default=0, help="first K Fock sectors of the BST vector (0 = all)")
     return ap.parse_args()
 
 
@@ -136,6 +139,109 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7):
     return out
 
 
+def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
+    """build_sigma! with the operator cache on the 32-orbital / 8-cluster BST vector: the
+    reference sector and its 112 single-charge-transfer sectors, TuckerConfigs with at most
+    two clusters in their excited range, Tucker ranks 4-12, 2 roots.  FP64 and FP32 device
+    timings (L2 flushed before each step), the HBM roofline of reading the operator cache,
+    the host-buffer path, and a CPU sample of the oracle's build_sigma!."""
+    import torch
+    from fermicg_gb300 import pack, workloads
+    from fermicg_gb300.bst import PackedBST, synthetic_bst
+    from fermicg_gb300.gpu import GpuSigma
+    prob = workloads.config2_problem(0)
+    secs = workloads.single_transfer_sectors(prob)
+    if n_sectors > 0:
+        secs = secs[:n_sectors]
+    R = 2
+    vec = synthetic_bst(prob, secs, max_q=2, rank_range=(4, 12), R=R, seed=0)
+    pb = PackedBST(vec, len(prob.clusters), R)
+    g = GpuSigma(torch.cuda.current_device())
+    g.set_ops(pack.pack_ops(prob.ops, prob.bases))
+    g.set_terms(pack.pack_terms(prob.ham))
+    t0 = time.perf_counter()
+    g.bst_set(pb)
+    t_set = time.perf_counter() - t0
+    st = g.stats()
+    stream = torch.cuda.current_stream()
+    g.set_stream(stream.cuda_stream)
+    host = pb.cores_of(vec)
+    x = torch.from_numpy(host).cuda()
+    y = torch.empty_like(x)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+
+    def timed(prec):
+        for _ in range(warmup):
+            g.bst_sigma_device(x.data_ptr(), y.data_ptr(), R, prec)
+        torch.cuda.synchronize()
+        ms, kern = [], []
+        for _ in range(steps):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            g.bst_sigma_device(x.data_ptr(), y.data_ptr(), R, prec)
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+            kern.append(g.stats()["last_kernel_ms"])
+        return statistics.mean(ms), statistics.median(kern)
+
+    ms64, k64 = timed("fp64")
+    y64 = y.clone()
+    ms32, k32 = timed("fp32")
+    rel32 = float((y - y64).abs().max() / y64.abs().max())
+    walls = []
+    for _ in range(max(3, steps // 2)):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g.bst_sigma(host, "fp32")
+        walls.append(time.perf_counter() - t1)
+    e2e_ms = 1e3 * statistics.mean(walls)
+    cache = st["bst_cache_elements"]
+    core_bytes = 2 * pb.core_total * R
+
+    def roof(kms, elem):
+        alg = cache * elem + core_bytes * elem
+        ach = alg / (kms * 1e-3) / 1e9
+        return {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
+                "bytes_per_sigma": alg, "note": "operator cache + cores read/written per sigma, of measured HBM copy peak"}
+
+    out = {
+        "workload": "bst_sigma_32o_8x4_M16_113sectors_q2_ranks4-12_R2", "blocks": len(pb.keys),
+        "core_total": pb.core_total, "roots": R, "triples": st["bst_triples"], "groups": st["bst_groups"],
+        "cache_elements": cache, "cache_seconds": st["bst_cache_seconds"], "plan_seconds": st["bst_plan_seconds"],
+        "set_wall_s": t_set,
+        "flops_reference_per_sigma": st["bst_flops_reference"] * R,
+        "fp64": {"value": 1e3 / ms64, "unit": "sigma_builds/s", "ms_per_step": ms64, "kernel_ms": k64,
+                 "roofline": roof(k64, 8)},
+        "fp32": {"value": 1e3 / ms32, "unit": "sigma_builds/s", "ms_per_step": ms32, "kernel_ms": k32,
+                 "roofline": roof(k32, 4), "rel_err_vs_fp64": rel32},
+        "e2e_fp32": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": host.nbytes,
+                     "d2h_bytes_per_step": host.nbytes},
+    }
+    if cpu_seconds > 0:
+        from oracle import bst as obst
+        tri = g.bst_triples()
+        keys = list(vec.keys())
+        for stride in (400, 100, 25):
+            sample = keys[::stride]
+            idx = {pb.index[k] for k in sample}
+            frac = float(np.isin(tri[:, 0], list(idx)).sum()) / max(len(tri), 1)
+            t1 = time.perf_counter()
+            obst.build_sigma({k: obst.zero_like({k: vec[k]}, R)[k] for k in sample}, vec, prob.ops, prob.ham,
+                             len(prob.clusters), R)
+            dt = time.perf_counter() - t1
+            if dt > cpu_seconds / 4 or stride == 25:
+                break
+        out["cpu_baseline"] = {"value": frac / dt if frac > 0 else None, "unit": "sigma_builds/s", "cores": 1,
+                               "kind": "port", "sample": f"{len(sample)} of {len(keys)} bra blocks "
+                               f"({100 * frac:.2f} % of the triples) in {dt:.1f} s, oracle build_sigma!, numpy"}
+    g.close()
+    return out
+
+
 def clocks_sampler():
     out = []
     stop = threading.Event()
@@ -213,6 +319,16 @@ def main():
 
     fbuild.build()
     torch.cuda.set_device(local)
+    if a.bst_only:
+        peaks = {}
+        try:
+            peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        except Exception:
+            pass
+        if rank == 0:
+            print(json.dumps({"bst": bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds,
+                                                   peaks.get("hbm_gbs", 6800.0), a.bst_sectors)}))
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -320,6 +436,11 @@ def main():
             out["serving"] = serving_benchmark()
         except Exception as ex:
             out["serving"] = {"error": str(ex)}
+    if rank == 0 and a.bst:
+        try:
+            out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, hbm_peak, a.bst_sectors)
+        except Exception as ex:
+            out["bst"] = {"error": str(ex)}
     if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1

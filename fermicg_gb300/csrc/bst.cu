@@ -29,8 +29,12 @@ using namespace fcg;
 namespace {
 
 constexpr int kBstThreads = 256;
+constexpr int kOpThreads = 64;            // threads per group of the operator-cache build
 constexpr int kGammaSmem = 6144;          // doubles of the per-p staging tile of the gamma kernel
-constexpr int kSigmaSmemBytes = 96 * 1024;  // shared-memory workspace of the sigma kernel
+constexpr int kSigmaSmemBytes = 96 * 1024;  // shared-memory workspace of a CTA-per-group sigma launch
+constexpr int kWarpSmemBytes = 8 * 1024;    // shared memory of one warp of bst_sigma_bra_kernel (description + workspace)
+constexpr int kAccBytes = 32 * 1024;        // shared-memory bra-core accumulator of bst_sigma_bra_kernel
+constexpr int64_t kChunkWork = int64_t(1) << 18;  // multiply-adds per bst_sigma_bra_kernel CTA, about
 
 // ---- operator cache ----------------------------------------------------------------------
 
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(kBstThreads) bst_gamma_kernel(const BstGamma* 
 }
 
 // One CTA per group: the group operator, scaled by the product of the rank-1 spectator overlaps.
-__global__ void __launch_bounds__(kBstThreads) bst_op_kernel(const BstGroup* __restrict__ groups,
+__global__ void __launch_bounds__(kOpThreads) bst_op_kernel(const BstGroup* __restrict__ groups,
                                                              const BstGroupTerm* __restrict__ gterms,
                                                              const BstBlock* __restrict__ blocks, int N,
                                                              const double* __restrict__ ints,
@@ -196,121 +200,238 @@ __global__ void bst_widen_kernel(const float* __restrict__ a, double* __restrict
 
 // ---- sigma ---------------------------------------------------------------------------------
 
-// One group, all R roots, by the CTA.  ws holds two buffers of `stride` elements per root.
-template <typename T>
-__device__ void bst_group_apply(const BstGroup& Gp, const BstBlock& B, const BstBlock& K, int N, int R,
-                                const T* __restrict__ op, const T* __restrict__ S, const T* __restrict__ cin,
-                                T* __restrict__ cout, int64_t core_total, T* ws, int stride) {
-  int d[kMaxClusters];
-  for (int c = 0; c < N; ++c) d[c] = K.rank[c];
-  // 1. ket cores
-  {
-    const int n = K.core_len;
-    for (int idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
-      const int r = idx / n, e = idx - r * n;
-      ws[int64_t(2 * r) * stride + e] = cin[int64_t(r) * core_total + K.core_off + e];
-    }
-  }
-  __syncthreads();
-  // 2. spectator modes to the bra bases (mode products with S_c = U_bra^T U_ket)
-  int cur = 0;
-  for (int c = 0; c < N; ++c) {
-    if (Gp.s_off[c] < 0) continue;
-    int inner = 1, outer = 1;
-    for (int c2 = 0; c2 < c; ++c2) inner *= d[c2];
-    for (int c2 = c + 1; c2 < N; ++c2) outer *= d[c2];
-    const int rb = B.rank[c], rk = d[c];
-    const int n = inner * rb * outer;
-    const T* Sc = S + Gp.s_off[c];
-    for (int idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
-      const int r = idx / n, e = idx - r * n;
-      const int a = e % inner, j = (e / inner) % rb, o = e / (inner * rb);
-      const T* src = ws + int64_t(2 * r + cur) * stride + a + int64_t(inner) * rk * o;
-      T s = T(0);
-      for (int l = 0; l < rk; ++l) s = fma(Sc[j + rb * l], src[int64_t(inner) * l], s);
-      ws[int64_t(2 * r + (cur ^ 1)) * stride + e] = s;
-    }
+template <int TEAM>
+__device__ __forceinline__ void team_sync() {
+  if (TEAM == 32)
+    __syncwarp();
+  else
     __syncthreads();
-    cur ^= 1;
-    d[c] = rb;
-  }
-  // 3. bra core += OP^T X over the active clusters
-  int act[4], na = 0;
-  int64_t sx[kMaxClusters];
-  {
-    int64_t s = 1;
-    for (int c = 0; c < N; ++c) {
-      sx[c] = s;
-      s *= d[c];
-      if ((Gp.act_mask >> c) & 1) act[na++] = c;
-    }
-  }
-  int kr[4] = {1, 1, 1, 1};
-  int64_t ks[4] = {0, 0, 0, 0};
-  for (int a = 0; a < na; ++a) {
-    kr[a] = K.rank[act[a]];
-    ks[a] = sx[act[a]];
-  }
-  const int n = B.core_len;
-  const T* opg = op + Gp.op_off;
-  for (int idx = threadIdx.x; idx < R * n; idx += blockDim.x) {
-    const int r = idx / n, e = idx - r * n;
-    int rem = e;
-    int64_t base = 0, kb = 0, kbm = 1;
-    for (int c = 0; c < N; ++c) {
-      const int v = rem % B.rank[c];
-      rem /= B.rank[c];
-      if ((Gp.act_mask >> c) & 1) {
-        kb += v * kbm;
-        kbm *= B.rank[c];
-      } else {
-        base += v * sx[c];
-      }
-    }
-    const T* X = ws + int64_t(2 * r + cur) * stride + base;
-    const T* o = opg + int64_t(Gp.k) * kb;
-    T acc = T(0);
-    for (int i3 = 0; i3 < kr[3]; ++i3)
-      for (int i2 = 0; i2 < kr[2]; ++i2)
-        for (int i1 = 0; i1 < kr[1]; ++i1) {
-          const T* xp = X + i1 * ks[1] + i2 * ks[2] + i3 * ks[3];
-          for (int i0 = 0; i0 < kr[0]; ++i0) acc = fma(o[i0], xp[i0 * ks[0]], acc);
-          o += kr[0];
-        }
-    atomicAdd(cout + int64_t(r) * core_total + B.core_off + e, acc);
+}
+
+// Copy a group description into shared memory (16-byte units) by a team.
+template <int TEAM>
+__device__ __forceinline__ void load_group(const BstGroup* __restrict__ src, BstGroup* dst, int tid) {
+  const int4* s4 = reinterpret_cast<const int4*>(src);
+  int4* d4 = reinterpret_cast<int4*>(dst);
+  for (int i = tid; i < int(sizeof(BstGroup) / 16); i += TEAM) d4[i] = s4[i];
+  team_sync<TEAM>();
+}
+
+// Prefetch [p, p + bytes) into L2 (or L1), one 128-byte line per request, by a team.
+template <int TEAM, bool L1>
+__device__ __forceinline__ void prefetch_range(const void* p, int64_t bytes, int tid) {
+  const char* c = static_cast<const char*>(p);
+  for (int64_t off = int64_t(tid) * 128; off < bytes; off += int64_t(TEAM) * 128) {
+    if (L1)
+      asm volatile("prefetch.global.L1 [%0];" ::"l"(c + off));
+    else
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(c + off));
   }
 }
 
-// Groups whose two workspace buffers fit shared memory: one CTA per group.
+// One group, all R roots, by a team of TEAM threads (a warp or the CTA); G is the group's
+// description in shared memory, ws two buffers of `stride` elements per root.
+// The ket core is gathered with the active clusters merged into one leading mode of length
+// k (mixed radix in cluster order) followed by the spectator modes in cluster order, so that
+//   X[kk + k*s]
+// is the GEMM operand of contract_dense_H_with_state (actives permuted to the front).  The
+// spectator modes then go to the bra bases (mode products with S_j = U_bra^T U_ket), and
+// every (bra active column kb, spectator index s, root) is one dot product of length k of
+// two contiguous vectors, OP[:, kb] and X[:, s], taken by a sub-warp of `lanes` threads
+// (power of two, <= 32) and added to out[r * out_stride + bra core index].
+template <typename T, int TEAM, bool ATOMIC>
+__device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ op, const T* __restrict__ S,
+                                const T* __restrict__ cin, int64_t core_total, T* ws, int stride, T* out,
+                                int64_t out_stride) {
+  const int tid = TEAM == 32 ? int(threadIdx.x & 31) : int(threadIdx.x);
+  const int k = G.k, m = G.m, na = G.na, nsp = G.nsp;
+  prefetch_range<TEAM, true>(op + G.op_off, int64_t(m) * k * int64_t(sizeof(T)), tid);
+  // 1. gather the ket cores in X order
+  {
+    const int n = G.kcore;
+    for (int idx = tid; idx < R * n; idx += TEAM) {
+      const int r = idx / n, e = idx - r * n;
+      int rem = e, src = 0;
+      for (int a = 0; a < na; ++a) {
+        const int d = rem % G.a_kr[a];
+        rem /= G.a_kr[a];
+        src += d * G.a_ks[a];
+      }
+      for (int j = 0; j < nsp; ++j) {
+        const int d = rem % G.s_kr[j];
+        rem /= G.s_kr[j];
+        src += d * G.s_ks[j];
+      }
+      ws[int64_t(2 * r) * stride + e] = cin[int64_t(r) * core_total + G.k_off + src];
+    }
+  }
+  team_sync<TEAM>();
+  // 2. spectator modes to the bra bases
+  int cur = 0;
+  {
+    int inner = k;
+    for (int j = 0; j < nsp; ++j) {
+      int outer = 1;
+      for (int i = j + 1; i < nsp; ++i) outer *= G.s_kr[i];
+      const int rb = G.s_br[j], rk = G.s_kr[j];
+      const int n = inner * rb * outer;
+      const T* Sj = S + G.s_off[j];
+      for (int idx = tid; idx < R * n; idx += TEAM) {
+        const int r = idx / n, e = idx - r * n;
+        const int a = e % inner, q = (e / inner) % rb, o = e / (inner * rb);
+        const T* src = ws + int64_t(2 * r + cur) * stride + a + inner * rk * o;
+        T acc = T(0);
+        for (int l = 0; l < rk; ++l) acc = fma(Sj[q + rb * l], src[inner * l], acc);
+        ws[int64_t(2 * r + (cur ^ 1)) * stride + e] = acc;
+      }
+      team_sync<TEAM>();
+      cur ^= 1;
+      inner *= rb;
+    }
+  }
+  // 3. bra core[kb, s] += OP[:, kb] . X[:, s]
+  int ns = 1;
+  for (int j = 0; j < nsp; ++j) ns *= G.s_br[j];
+  const int items = m * ns * R;
+  const T* opg = op + G.op_off;
+  auto bra_index = [&](int col, int s) {
+    int off = 0, rem = col;
+    for (int a = 0; a < na; ++a) {
+      off += (rem % G.a_br[a]) * G.a_bs[a];
+      rem /= G.a_br[a];
+    }
+    rem = s;
+    for (int j = 0; j < nsp; ++j) {
+      off += (rem % G.s_br[j]) * G.s_bs[j];
+      rem /= G.s_br[j];
+    }
+    return off;
+  };
+  if (k < 32) {
+    // short columns: one thread per (kb, s, root); items of one group never share an output
+    for (int it = tid; it < items; it += TEAM) {
+      const int col = it % m;
+      const int s = (it / m) % ns;
+      const int r = it / (m * ns);
+      const T* o = opg + int64_t(k) * col;
+      const T* X = ws + int64_t(2 * r + cur) * stride + int64_t(k) * s;
+      T acc = T(0), acc2 = T(0);
+      int kk = 0;
+      for (; kk + 1 < k; kk += 2) {
+        acc = fma(o[kk], X[kk], acc);
+        acc2 = fma(o[kk + 1], X[kk + 1], acc2);
+      }
+      if (kk < k) acc = fma(o[kk], X[kk], acc);
+      acc += acc2;
+      T* dst = out + int64_t(r) * out_stride + bra_index(col, s);
+      if (ATOMIC)
+        atomicAdd(dst, acc);
+      else
+        *dst += acc;
+    }
+    return;
+  }
+  // long columns: a warp per (kb, s, root), lanes along the column (coalesced reads of OP)
+  const int wid = tid >> 5, lane = tid & 31;
+  constexpr int nw = TEAM >> 5;
+  for (int it = wid; it < items; it += nw) {
+    const int col = it % m;
+    const int s = (it / m) % ns;
+    const int r = it / (m * ns);
+    const T* o = opg + int64_t(k) * col;
+    const T* X = ws + int64_t(2 * r + cur) * stride + int64_t(k) * s;
+    T acc = T(0);
+    for (int kk = lane; kk < k; kk += 32) acc = fma(o[kk], X[kk], acc);
+    for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
+    if (lane == 0) {
+      T* dst = out + int64_t(r) * out_stride + bra_index(col, s);
+      if (ATOMIC)
+        atomicAdd(dst, acc);
+      else
+        *dst += acc;
+    }
+  }
+}
+
+// Chunks of the groups of one bra block whose R cores fit shared memory: one CTA per
+// chunk.  Its warps take the chunk's groups in turn (one group per warp, each warp with a
+// slice of `slice` bytes: the group description, then its workspace) and add into
+// shared-memory copies of the bra cores -- one private copy per warp when `priv` (plain
+// adds), else one shared copy (shared-memory atomics) -- and the CTA adds the sum to sigma.
+template <typename T>
+__global__ void __launch_bounds__(kBstThreads) bst_sigma_bra_kernel(const int32_t* __restrict__ chunk_bra,
+                                                                    const int64_t* __restrict__ chunk_ptr,
+                                                                    const int32_t* __restrict__ glist,
+                                                                    const BstGroup* __restrict__ groups,
+                                                                    const BstBlock* __restrict__ blocks, int R,
+                                                                    const T* __restrict__ op,
+                                                                    const T* __restrict__ S,
+                                                                    const T* __restrict__ cin, T* __restrict__ cout,
+                                                                    int64_t core_total, int slice, int priv) {
+  extern __shared__ __align__(16) unsigned char bst_smem[];
+  constexpr int kWarps = kBstThreads / 32;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  BstGroup* G = reinterpret_cast<BstGroup*>(bst_smem + size_t(w) * slice);
+  T* ws = reinterpret_cast<T*>(bst_smem + size_t(w) * slice + sizeof(BstGroup));
+  T* acc = reinterpret_cast<T*>(bst_smem + size_t(kWarps) * slice);
+  const BstBlock& B = blocks[chunk_bra[blockIdx.x]];
+  const int n = B.core_len;
+  const int copies = priv ? kWarps : 1;
+  for (int i = threadIdx.x; i < copies * R * n; i += kBstThreads) acc[i] = T(0);
+  __syncthreads();
+  const int64_t j1 = chunk_ptr[blockIdx.x + 1];
+  T* mine = acc + (priv ? size_t(w) * R * n : 0);
+  for (int64_t j = chunk_ptr[blockIdx.x] + w; j < j1; j += kWarps) {
+    if (j + kWarps < j1) {  // the operator of this warp's next group, to L2
+      const BstGroup* nx = groups + glist[j + kWarps];
+      prefetch_range<32, false>(op + nx->op_off, int64_t(nx->m) * nx->k * int64_t(sizeof(T)), lane);
+    }
+    load_group<32>(groups + glist[j], G, lane);
+    if (priv)
+      bst_group_apply<T, 32, false>(*G, R, op, S, cin, core_total, ws, G->ws, mine, n);
+    else
+      bst_group_apply<T, 32, true>(*G, R, op, S, cin, core_total, ws, G->ws, mine, n);
+    __syncwarp();  // the next description overwrites this one
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < R * n; i += kBstThreads) {
+    T v = T(0);
+    for (int c = 0; c < copies; ++c) v += acc[size_t(c) * R * n + i];
+    const int r = i / n, e = i - r * n;
+    if (v != T(0)) atomicAdd(cout + int64_t(r) * core_total + B.core_off + e, v);
+  }
+}
+
+// Medium groups: one CTA per group, description and workspace in shared memory.
 template <typename T>
 __global__ void __launch_bounds__(kBstThreads) bst_sigma_smem_kernel(const int32_t* __restrict__ list,
-                                                                     const BstGroup* __restrict__ groups,
-                                                                     const BstBlock* __restrict__ blocks, int N,
-                                                                     int R, const T* __restrict__ op,
+                                                                     const BstGroup* __restrict__ groups, int R,
+                                                                     const T* __restrict__ op,
                                                                      const T* __restrict__ S,
                                                                      const T* __restrict__ cin, T* __restrict__ cout,
                                                                      int64_t core_total) {
   extern __shared__ __align__(16) unsigned char bst_smem[];
-  T* ws = reinterpret_cast<T*>(bst_smem);
-  const BstGroup Gp = groups[list[blockIdx.x]];
-  bst_group_apply<T>(Gp, blocks[Gp.bra], blocks[Gp.ket], N, R, op, S, cin, cout, core_total, ws, Gp.ws);
+  BstGroup* G = reinterpret_cast<BstGroup*>(bst_smem);
+  T* ws = reinterpret_cast<T*>(bst_smem + sizeof(BstGroup));
+  load_group<kBstThreads>(groups + list[blockIdx.x], G, threadIdx.x);
+  bst_group_apply<T, kBstThreads, true>(*G, R, op, S, cin, core_total, ws, G->ws, cout + G->b_off, core_total);
 }
 
-// The other groups: a grid of CTAs, each with its own global-memory workspace slice,
-// walking the list with a stride of the grid size.
+// Large groups: a grid of CTAs, each with its own global-memory workspace slice, walking
+// the list with a stride of the grid size.
 template <typename T>
 __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int32_t* __restrict__ list, int n_list,
-                                                                       const BstGroup* __restrict__ groups,
-                                                                       const BstBlock* __restrict__ blocks, int N,
-                                                                       int R, const T* __restrict__ op,
+                                                                       const BstGroup* __restrict__ groups, int R,
+                                                                       const T* __restrict__ op,
                                                                        const T* __restrict__ S,
                                                                        const T* __restrict__ cin,
                                                                        T* __restrict__ cout, int64_t core_total,
                                                                        T* __restrict__ ws_all, int stride) {
+  __shared__ __align__(16) BstGroup G;
   T* ws = ws_all + int64_t(blockIdx.x) * 2 * R * stride;
   for (int i = blockIdx.x; i < n_list; i += gridDim.x) {
-    const BstGroup Gp = groups[list[i]];
-    bst_group_apply<T>(Gp, blocks[Gp.bra], blocks[Gp.ket], N, R, op, S, cin, cout, core_total, ws, stride);
+    load_group<kBstThreads>(groups + list[i], &G, threadIdx.x);
+    bst_group_apply<T, kBstThreads, true>(G, R, op, S, cin, core_total, ws, stride, cout + G.b_off, core_total);
     __syncthreads();
   }
 }
@@ -356,33 +477,46 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
     if (r[0] <= nbody) by_trans[r[1]].push_back(t);
   }
-  // ket lookup per active-cluster mask: (fock, spectator ranges) -> blocks
-  std::map<int, std::map<std::vector<int32_t>, std::vector<int32_t>>> lookup;
-  auto key_of = [&](int64_t b, const int16_t* f, int mask) {
-    std::vector<int32_t> k(4 * N);
-    for (int c = 0; c < N; ++c) {
-      k[4 * c] = f[2 * c];
-      k[4 * c + 1] = f[2 * c + 1];
-      const bool a = (mask >> c) & 1;
-      k[4 * c + 2] = a ? -1 : blk[b].start[c];
-      k[4 * c + 3] = a ? -1 : blk[b].len[c];
-    }
-    return k;
+  // ket lookup per active-cluster mask: hash of (fock, spectator ranges) -> blocks; the
+  // candidates of a hash are compared in full before use
+  auto mix = [](uint64_t h, uint64_t v) {
+    h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+    return h;
   };
-  auto kets_of = [&](int mask) -> std::map<std::vector<int32_t>, std::vector<int32_t>>& {
+  auto hash_of = [&](int64_t b, const int16_t* f, int mask) {
+    uint64_t h = uint64_t(mask) * 0x100000001b3ULL;
+    for (int c = 0; c < N; ++c) {
+      h = mix(h, uint64_t(uint16_t(f[2 * c])) | (uint64_t(uint16_t(f[2 * c + 1])) << 16));
+      if (!((mask >> c) & 1)) h = mix(h, uint64_t(uint32_t(blk[b].start[c])) | (uint64_t(uint32_t(blk[b].len[c])) << 32));
+    }
+    return h;
+  };
+  std::unordered_map<int, std::unordered_map<uint64_t, std::vector<int32_t>>> lookup;
+  auto kets_of = [&](int mask) -> std::unordered_map<uint64_t, std::vector<int32_t>>& {
     auto it = lookup.find(mask);
     if (it != lookup.end()) return it->second;
     auto& m = lookup[mask];
-    for (int64_t k = 0; k < nb; ++k) m[key_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
+    for (int64_t k = 0; k < nb; ++k) m[hash_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
     return m;
   };
+  auto matches = [&](int64_t b, const int16_t* fk, int64_t k, int mask) {
+    const int16_t* f = fock + 2 * N * k;
+    for (int c = 0; c < N; ++c) {
+      if (f[2 * c] != fk[2 * c] || f[2 * c + 1] != fk[2 * c + 1]) return false;
+      if (!((mask >> c) & 1) && (blk[k].start[c] != blk[b].start[c] || blk[k].len[c] != blk[b].len[c])) return false;
+    }
+    return true;
+  };
+  // Fock sectors present (a transfer into any other sector has no ket)
+  std::unordered_map<uint64_t, int> sectors;
+  for (int64_t k = 0; k < nb; ++k) sectors[hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
   std::unordered_map<uint64_t, int64_t> gamma_at;   // (bra, ket, c, op) -> g offset
   std::unordered_map<uint64_t, int64_t> overlap_at; // (bra, ket, c) -> S offset
   std::vector<std::vector<BstGroupTerm>> gt;        // terms per group
   std::vector<int16_t> fk(2 * N);
   for (int64_t b = 0; b < nb; ++b) {
     const int16_t* fb = fock + 2 * N * b;
-    std::map<std::pair<int32_t, int>, int32_t> grp;  // (ket, mask) -> group
+    std::unordered_map<uint64_t, int32_t> grp;  // (ket, mask) -> group
     for (int tr = 0; tr < ctx->n_trans; ++tr) {
       if (by_trans[tr].empty()) continue;
       bool ok = true;
@@ -393,6 +527,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
           fk[2 * c + s] = int16_t(v);
         }
       if (!ok) continue;
+      if (!sectors.count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
       for (int t : by_trans[tr]) {
         const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
         int mask = 0;
@@ -408,16 +543,18 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
         }
         if (!have) continue;
         auto& m = kets_of(mask);
-        auto it = m.find(key_of(b, fk.data(), mask));
+        auto it = m.find(hash_of(b, fk.data(), mask));
         if (it == m.end()) continue;
         const int sign = term_state_sign(r, fk.data());
         for (int32_t k : it->second) {
+          if (!matches(b, fk.data(), k, mask)) continue;
           P.triples.insert(P.triples.end(), {int32_t(b), k, int32_t(t), int32_t(sign)});
-          auto gi = grp.find({k, mask});
+          const uint64_t gk = (uint64_t(uint32_t(k)) << 8) | uint64_t(mask);
+          auto gi = grp.find(gk);
           int32_t g;
           if (gi == grp.end()) {
             g = int32_t(P.groups.size());
-            grp[{k, mask}] = g;
+            grp[gk] = g;
             BstGroup G{};
             G.bra = int32_t(b);
             G.ket = k;
@@ -482,9 +619,41 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     G.t_off = int32_t(P.gterms.size());
     G.nt = int32_t(gt[g].size());
     P.gterms.insert(P.gterms.end(), gt[g].begin(), gt[g].end());
-    int64_t size = K.core_len, ws = size, tf = 0;
+    // core strides and the index description of the rank > 1 clusters
+    int64_t kst[kMaxClusters], bst[kMaxClusters];
+    {
+      int64_t a = 1, b2 = 1;
+      for (int c = 0; c < N; ++c) {
+        kst[c] = a;
+        bst[c] = b2;
+        a *= K.rank[c];
+        b2 *= B.rank[c];
+      }
+    }
+    G.k_off = K.core_off;
+    G.b_off = B.core_off;
+    G.kcore = K.core_len;
+    G.bcore = B.core_len;
+    G.na = 0;
+    G.nsp = 0;
     for (int c = 0; c < N; ++c) {
-      G.s_off[c] = -1;
+      if (B.rank[c] == 1 && K.rank[c] == 1) continue;
+      if ((G.act_mask >> c) & 1) {
+        const int a = G.na++;
+        G.a_kr[a] = K.rank[c];
+        G.a_br[a] = B.rank[c];
+        G.a_ks[a] = int32_t(kst[c]);
+        G.a_bs[a] = int32_t(bst[c]);
+      } else {
+        const int j = G.nsp++;
+        G.s_kr[j] = K.rank[c];
+        G.s_br[j] = B.rank[c];
+        G.s_ks[j] = int32_t(kst[c]);
+        G.s_bs[j] = int32_t(bst[c]);
+      }
+    }
+    int64_t size = K.core_len, ws = size, tf = 0;
+    for (int c = 0, j = 0; c < N; ++c) {
       if ((G.act_mask >> c) & 1) continue;
       if (B.rank[c] == 1 && K.rank[c] == 1) continue;
       const uint64_t key = (uint64_t(G.bra) * uint64_t(nb) + uint64_t(G.ket)) * 8 + uint64_t(c);
@@ -494,11 +663,12 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
         it = overlap_at.emplace(key, P.s_total).first;
         P.s_total += align_up(int64_t(B.rank[c]) * K.rank[c]);
       }
-      G.s_off[c] = it->second;
+      G.s_off[j++] = it->second;
       size = size / K.rank[c] * B.rank[c];
       tf += 2 * size * K.rank[c];
       ws = std::max(ws, size);
     }
+    for (int j = G.nsp; j < kMaxClusters; ++j) G.s_off[j] = 0;
     if (ws > (int64_t(1) << 30)) return "BST: a core exceeds 2^30 elements";
     G.ws = int32_t(align_up(ws));
     const int64_t f = 2 * m * k * n + tf;
@@ -508,19 +678,96 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
   return "";
 }
 
-// Lists of groups that run from shared memory (two buffers per root fit) and from global memory.
+// Every index the sigma kernels form from a group description, checked against the buffers
+// it addresses (ket / bra cores, operator cache, overlaps, workspace).
+std::string check_groups(const std::vector<BstGroup>& groups, const std::vector<BstBlock>& blk, int64_t core_total,
+                         int64_t op_total, int64_t s_total) {
+  for (const BstGroup& G : groups) {
+    if (G.bra < 0 || G.ket < 0 || size_t(G.bra) >= blk.size() || size_t(G.ket) >= blk.size()) return "BST check: block id";
+    const BstBlock& B = blk[G.bra];
+    const BstBlock& K = blk[G.ket];
+    if (G.kcore != K.core_len || G.bcore != B.core_len || G.k_off != K.core_off || G.b_off != B.core_off)
+      return "BST check: core extents";
+    if (G.k_off + G.kcore > core_total || G.b_off + G.bcore > core_total) return "BST check: core offsets";
+    if (G.na < 0 || G.na > 4 || G.nsp < 0 || G.nsp > kMaxClusters) return "BST check: mode counts";
+    int64_t kprod = 1, bprod = 1, ka = 1, ba = 1, kmax = 0, bmax = 0;
+    for (int a = 0; a < G.na; ++a) {
+      if (G.a_kr[a] < 1 || G.a_br[a] < 1) return "BST check: active ranks";
+      ka *= G.a_kr[a];
+      ba *= G.a_br[a];
+      kmax += int64_t(G.a_kr[a] - 1) * G.a_ks[a];
+      bmax += int64_t(G.a_br[a] - 1) * G.a_bs[a];
+    }
+    kprod = ka;
+    bprod = ba;
+    int64_t size = G.kcore, ws_need = size;
+    for (int j = 0; j < G.nsp; ++j) {
+      if (G.s_kr[j] < 1 || G.s_br[j] < 1) return "BST check: spectator ranks";
+      kprod *= G.s_kr[j];
+      bprod *= G.s_br[j];
+      kmax += int64_t(G.s_kr[j] - 1) * G.s_ks[j];
+      bmax += int64_t(G.s_br[j] - 1) * G.s_bs[j];
+      if (G.s_off[j] < 0 || G.s_off[j] + int64_t(G.s_br[j]) * G.s_kr[j] > s_total) return "BST check: overlap extent";
+      size = size / G.s_kr[j] * G.s_br[j];
+      ws_need = std::max(ws_need, size);
+    }
+    if (ka != G.k || ba != G.m) return "BST check: active products";
+    if (kprod != G.kcore || bprod != G.bcore) return "BST check: mode products";
+    if (kmax >= G.kcore || bmax >= G.bcore) return "BST check: core strides";
+    if (int64_t(G.ws) < ws_need || int64_t(G.k) * (G.bcore / std::max(G.m, 1)) > G.ws) return "BST check: workspace";
+    if (G.op_off < 0 || G.op_off + int64_t(G.m) * G.k > op_total) return "BST check: operator extent";
+  }
+  return "";
+}
+
+// Groups by where they run.  Groups whose workspace fits a warp slice and whose bra block's
+// R cores fit kAccBytes go to bst_sigma_bra_kernel, cut per bra block into chunks of about
+// kChunkWork multiply-adds; the others run one CTA per group from shared memory, or from
+// global memory.
 void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
+  ctx->bst_bra_ids.clear();
+  ctx->bst_bra_ptr.assign(1, 0);
+  ctx->bst_bra_glist.clear();
   ctx->bst_small.clear();
   ctx->bst_large.clear();
   ctx->bst_ws_large = 0;
-  for (size_t g = 0; g < ctx->bst_groups.size(); ++g) {
-    const BstGroup& G = ctx->bst_groups[g];
-    if (size_t(2) * R * G.ws * elem <= size_t(kSigmaSmemBytes)) {
-      ctx->bst_small.push_back(int32_t(g));
-    } else {
-      ctx->bst_large.push_back(int32_t(g));
-      ctx->bst_ws_large = std::max(ctx->bst_ws_large, G.ws);
+  ctx->bst_bra_slice = 0;
+  ctx->bst_bra_acc = 0;
+  const size_t ng = ctx->bst_groups.size();
+  size_t g = 0;
+  while (g < ng) {
+    const int32_t b = ctx->bst_groups[g].bra;
+    size_t g1 = g;
+    while (g1 < ng && ctx->bst_groups[g1].bra == b) ++g1;  // groups of one bra are contiguous
+    const size_t acc = size_t(R) * ctx->bst_blocks[b].core_len * elem;
+    const bool own = acc <= size_t(kAccBytes);
+    int64_t work = 0;
+    bool open = false;
+    for (size_t q = g; q < g1; ++q) {
+      const BstGroup& G = ctx->bst_groups[q];
+      const size_t need = sizeof(BstGroup) + size_t(2) * R * G.ws * elem;
+      if (own && need <= size_t(kWarpSmemBytes)) {
+        if (!open || work > kChunkWork) {
+          if (open) ctx->bst_bra_ptr.push_back(int64_t(ctx->bst_bra_glist.size()));
+          ctx->bst_bra_ids.push_back(b);
+          open = true;
+          work = 0;
+        }
+        ctx->bst_bra_glist.push_back(int32_t(q));
+        ctx->bst_bra_slice = std::max(ctx->bst_bra_slice, int((need + 15) / 16 * 16));
+        work += int64_t(R) * (int64_t(G.m) * G.k * (G.bcore / std::max(G.m, 1)) + 2 * G.kcore + 64);
+      } else if (need <= size_t(kSigmaSmemBytes)) {
+        ctx->bst_small.push_back(int32_t(q));
+      } else {
+        ctx->bst_large.push_back(int32_t(q));
+        ctx->bst_ws_large = std::max(ctx->bst_ws_large, G.ws);
+      }
     }
+    if (open) {
+      ctx->bst_bra_ptr.push_back(int64_t(ctx->bst_bra_glist.size()));
+      ctx->bst_bra_acc = std::max(ctx->bst_bra_acc, int((acc + 15) / 16 * 16));
+    }
+    g = g1;
   }
 }
 
@@ -529,23 +776,37 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
   const size_t elem = sizeof(T);
   if (ctx->bst_list_R != R || ctx->bst_list_elem != elem) {
     bst_lists(ctx, R, elem);
+    FCG_CUDA(ctx->d_bst_bra_ids.upload(ctx->bst_bra_ids.data(), ctx->bst_bra_ids.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_bra_ptr.upload(ctx->bst_bra_ptr.data(), ctx->bst_bra_ptr.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_bra_glist.upload(ctx->bst_bra_glist.data(), ctx->bst_bra_glist.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_small.upload(ctx->bst_small.data(), ctx->bst_small.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_large.upload(ctx->bst_large.data(), ctx->bst_large.size(), ctx->stream));
     ctx->bst_list_R = R;
     ctx->bst_list_elem = elem;
   }
-  const int N = ctx->N;
   const int64_t ct = ctx->bst_core_total;
   FCG_CUDA(cudaMemsetAsync(cout, 0, elem * size_t(ct) * R, ctx->stream));
   int launches = 1;
+  if (!ctx->bst_bra_ids.empty()) {
+    constexpr int kWarps = kBstThreads / 32;
+    const int priv = size_t(kWarps) * ctx->bst_bra_acc <= size_t(kAccBytes) ? 1 : 0;
+    const size_t smem = size_t(kWarps) * ctx->bst_bra_slice + size_t(priv ? kWarps : 1) * ctx->bst_bra_acc;
+    FCG_CUDA(cudaFuncSetAttribute(bst_sigma_bra_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  int(kWarps * kWarpSmemBytes + kAccBytes)));
+    bst_sigma_bra_kernel<T><<<unsigned(ctx->bst_bra_ids.size()), kBstThreads, smem, ctx->stream>>>(
+        ctx->d_bst_bra_ids.p, ctx->d_bst_bra_ptr.p, ctx->d_bst_bra_glist.p, ctx->d_bst_groups.p, ctx->d_bst_blocks.p,
+        R, op, S, cin, cout, ct, ctx->bst_bra_slice, priv);
+    FCG_CUDA(cudaGetLastError());
+    ++launches;
+  }
   if (!ctx->bst_small.empty()) {
     int ws_max = 0;
     for (int32_t g : ctx->bst_small) ws_max = std::max(ws_max, ctx->bst_groups[g].ws);
-    const size_t smem = size_t(2) * R * ws_max * elem;
+    const size_t smem = sizeof(BstGroup) + size_t(2) * R * ws_max * elem;
     FCG_CUDA(cudaFuncSetAttribute(bst_sigma_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(kSigmaSmemBytes)));
     bst_sigma_smem_kernel<T><<<unsigned(ctx->bst_small.size()), kBstThreads, smem, ctx->stream>>>(
-        ctx->d_bst_small.p, ctx->d_bst_groups.p, ctx->d_bst_blocks.p, N, R, op, S, cin, cout, ct);
+        ctx->d_bst_small.p, ctx->d_bst_groups.p, R, op, S, cin, cout, ct);
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -554,8 +815,8 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     const int64_t stride = ctx->bst_ws_large;
     FCG_CUDA(ws.alloc(size_t(grid) * 2 * R * stride));
     bst_sigma_global_kernel<T><<<unsigned(grid), kBstThreads, 0, ctx->stream>>>(
-        ctx->d_bst_large.p, int(ctx->bst_large.size()), ctx->d_bst_groups.p, ctx->d_bst_blocks.p, N, R, op, S, cin,
-        cout, ct, ws.p, int(stride));
+        ctx->d_bst_large.p, int(ctx->bst_large.size()), ctx->d_bst_groups.p, R, op, S, cin, cout, ct, ws.p,
+        int(stride));
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -610,7 +871,12 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
     std::string msg = plan_bst(ctx, nbody, blk, fock, P);
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
+  const double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   FCG_REQUIRE(P.groups.size() < (size_t(1) << 31), FCG_ELIMIT, "BST: too many groups");
+  {
+    std::string msg = check_groups(P.groups, blk, off, P.op_total, P.s_total);
+    FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+  }
   // device structures and the operator cache
   FCG_CUDA(ctx->d_bst_factors.upload(factors, size_t(n_factors), ctx->stream));
   FCG_CUDA(ctx->d_bst_blocks.upload(blk.data(), blk.size(), ctx->stream));
@@ -635,7 +901,7 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
     FCG_CUDA(cudaGetLastError());
   }
   if (!P.groups.empty()) {
-    bst_op_kernel<<<unsigned(P.groups.size()), kBstThreads, 0, ctx->stream>>>(
+    bst_op_kernel<<<unsigned(P.groups.size()), kOpThreads, 0, ctx->stream>>>(
         ctx->d_bst_groups.p, d_gt.p, ctx->d_bst_blocks.p, N, ctx->d_ints64.p, d_g.p, ctx->d_bst_factors.p,
         ctx->d_bst_op64.p);
     FCG_CUDA(cudaGetLastError());
@@ -665,6 +931,7 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
   ctx->stats.bst_flops_executed = P.flops_exec;
   ctx->stats.bst_cache_seconds =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx->stats.bst_plan_seconds = plan_s;
   ctx->have_bst = true;
   return FCG_OK;
 }
@@ -675,6 +942,9 @@ int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_s
   FCG_REQUIRE(R >= 1 && R <= 64, FCG_ELIMIT, "R must be in [1, 64]");
   FCG_REQUIRE(d_cores && d_sigma, FCG_EINVAL, "null pointer");
   FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
+  int64_t max_core = 0;
+  for (const BstBlock& B : ctx->bst_blocks) max_core = std::max<int64_t>(max_core, B.core_len);
+  FCG_REQUIRE(max_core * R < (int64_t(1) << 31), FCG_ELIMIT, "R times the largest core must stay below 2^31");
   FCG_CUDA(cudaSetDevice(ctx->device));
   const int64_t n = ctx->bst_core_total * R;
   ctx->stats.last_kernel_ms = 0.0;

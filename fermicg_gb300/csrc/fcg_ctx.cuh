@@ -125,13 +125,17 @@ struct fcg_ctx {
   std::vector<BstBlock> bst_blocks;
   std::vector<BstGroup> bst_groups;
   std::vector<int32_t> bst_triples;     // [n][4] = {bra, ket, term, sign}
-  std::vector<int32_t> bst_small, bst_large;  // groups whose workspace fits shared memory / does not
+  std::vector<int32_t> bst_small, bst_large;  // groups run one CTA per group from shared / global memory
   int32_t bst_ws_large = 0;
-  int bst_list_R = 0;          // R and element size the two lists were made for
+  std::vector<int32_t> bst_bra_ids, bst_bra_glist;  // bra block of each chunk, and the chunks' groups
+  std::vector<int64_t> bst_bra_ptr;                 // chunk c holds bst_bra_glist[ptr[c], ptr[c+1])
+  int bst_bra_slice = 0, bst_bra_acc = 0;           // shared-memory bytes per warp slice / accumulator
+  int bst_list_R = 0;          // R and element size the lists were made for
   size_t bst_list_elem = 0;
   DevBuf<BstBlock> d_bst_blocks;
   DevBuf<BstGroup> d_bst_groups;
-  DevBuf<int32_t> d_bst_small, d_bst_large;
+  DevBuf<int32_t> d_bst_small, d_bst_large, d_bst_bra_ids, d_bst_bra_glist;
+  DevBuf<int64_t> d_bst_bra_ptr;
   DevBuf<double> d_bst_factors;
   DevBuf<double> d_bst_op64, d_bst_s64;
   DevBuf<float> d_bst_op32, d_bst_s32;

@@ -143,16 +143,27 @@ struct BstGroupTerm {
 
 // All terms that couple one bra block to one ket block through the same active clusters:
 //   OP[kk + k*kb] = (prod of scalar spectator overlaps) * sum_t sign_t sum_p ints_t[p] prod_a g_{t,a}[p_a, kb_a, kk_a]
-// (kk / kb: mixed-radix over the active clusters in increasing cluster order, ket / bra ranks).
+// (kk / kb: mixed-radix over the active clusters in increasing cluster order, ket / bra ranks),
+// with the index description the sigma kernels use: only clusters of rank > 1 on the bra or
+// the ket side appear (a rank-1 cluster has a single index value on both sides).
 struct BstGroup {
   int64_t op_off;
-  int64_t s_off[kMaxClusters];  // spectator overlap U_bra^T U_ket (rank_bra x rank_ket); -1 when both ranks are 1
+  int64_t k_off, b_off;          // ket / bra core offsets
+  int64_t s_off[kMaxClusters];   // overlap U_bra^T U_ket (rank_bra x rank_ket) of spectator mode j
   int32_t bra, ket;
-  int32_t m, k;                 // products of the active bra / ket ranks
+  int32_t m, k;                  // products of the active bra / ket ranks
   int32_t act_mask;
-  int32_t t_off, nt;            // terms in the group-term pool
-  int32_t ws;                   // largest intermediate tensor of the sigma step (elements per root)
+  int32_t t_off, nt;             // terms in the group-term pool
+  int32_t ws;                    // largest intermediate tensor of the sigma step (elements per root)
+  int32_t kcore, bcore;          // ket / bra core lengths
+  int32_t na, nsp;               // active clusters / spectator modes with rank > 1 on either side
+  int32_t a_kr[4], a_br[4];      // their ket / bra ranks
+  int32_t a_ks[4], a_bs[4];      // their strides in the ket / bra core
+  int32_t s_kr[kMaxClusters], s_br[kMaxClusters];
+  int32_t s_ks[kMaxClusters], s_bs[kMaxClusters];
+  int32_t pad[2];
 };
+static_assert(sizeof(BstGroup) % 16 == 0, "BstGroup is copied to shared memory in 16-byte units");
 
 // Problem description the planner needs (host copies).
 struct ProblemInfo {

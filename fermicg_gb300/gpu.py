@@ -62,7 +62,8 @@ class Stats(ctypes.Structure):
                 ("davidson_sigma_calls", ctypes.c_int64), ("bst_blocks", ctypes.c_int64),
                 ("bst_triples", ctypes.c_int64), ("bst_groups", ctypes.c_int64),
                 ("bst_cache_elements", ctypes.c_int64), ("bst_flops_reference", ctypes.c_int64),
-                ("bst_flops_executed", ctypes.c_int64), ("bst_cache_seconds", ctypes.c_double)]
+                ("bst_flops_executed", ctypes.c_int64), ("bst_cache_seconds", ctypes.c_double),
+                ("bst_plan_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

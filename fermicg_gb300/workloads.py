@@ -218,3 +218,31 @@ def config1_problem(seed=0):
     """24 orbitals, 12a/12b, 6 clusters x 4, K=72, M=16 per sector within 2 electrons
     of (2,2)."""
     return build_problem(24, [4] * 6, [(2, 2)] * 6, 72, seed, max_roots=16, delta_elec=2)
+
+
+def config2_problem(seed=0):
+    """32 orbitals, 16a/16b, 8 clusters x 4, K=96, M=16 per sector within 1 electron of
+    (2,2) (the BST / Tucker configuration)."""
+    return build_problem(32, [4] * 8, [(2, 2)] * 8, 96, seed, max_roots=16, delta_elec=1)
+
+
+def single_transfer_sectors(prob):
+    """The reference Fock sector and every sector reached from it by moving one alpha or
+    one beta electron between two clusters (the charge-transfer blocks of a BST vector)."""
+    ref = tuple(tuple(f) for f in prob.init_fspace)
+    N = len(ref)
+    out = [ref]
+    for i in range(N):
+        for j in range(N):
+            if i == j:
+                continue
+            for s in (0, 1):
+                fs = [list(f) for f in ref]
+                fs[i][s] -= 1
+                fs[j][s] += 1
+                if fs[i][s] < 0 or fs[j][s] > len(prob.clusters[j]):
+                    continue
+                key = tuple(tuple(f) for f in fs)
+                if all(key[c] in prob.bases[c].basis for c in range(N)):
+                    out.append(key)
+    return out

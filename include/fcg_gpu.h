@@ -69,6 +69,7 @@ typedef struct fcg_stats {
   int64_t bst_flops_reference; /* per root: sum over triples of 2*m*k*n + spectator transforms (reference count) */
   int64_t bst_flops_executed;  /* per root: the same sums over groups (what one fcg_bst_sigma root does) */
   double bst_cache_seconds; /* wall time of the last fcg_bst_set (planning + operator cache) */
+  double bst_plan_seconds;  /* of which host planning (triples, groups, cache layout) */
 } fcg_stats;
 
 int fcg_version(void);
