@@ -87,6 +87,7 @@ struct fcg_ctx {
   DevBuf<int32_t> d_row_sector;
   DevBuf<WorkItem> d_items;
   DevBuf<int64_t> d_prefix;
+  DevBuf<int64_t> d_cta32, d_cta64;  // first work item of each closed-sigma CTA (float / double chunks)
   DevBuf<int32_t> d_perm;
   DevBuf<TermSector> d_ts;
   DevBuf<int32_t> d_zero_terms;

@@ -101,6 +101,7 @@ __global__ void colmax_kernel(const MaxJob* __restrict__ jobs, const double* __r
 struct SigmaParams {
   const WorkItem* items;
   const int64_t* prefix;
+  const int64_t* cta_lo;  // work item holding each CTA's first triple; [n_cta] = last item
   int64_t n_items;
   int64_t n_triples;
   const int32_t* perm;
@@ -111,6 +112,10 @@ struct SigmaParams {
 };
 
 // ---- vector loads ---------------------------------------------------------------------------
+// Vec4: 4 consecutive elements (16 bytes float, 32 bytes double); Chunk: 32 bytes (8 float
+// or 4 double) in one 256-bit load.  Callers guarantee the alignment: device TDM and W
+// blocks start on multiples of kAlign = 8 elements and the columns read this way have
+// lengths that are multiples of the vector length.
 template <typename T>
 struct Vec4;
 template <>
@@ -125,9 +130,28 @@ template <>
 struct Vec4<double> {
   double v[4];
   __device__ __forceinline__ void load(const double* p) {
-    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
-    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
-    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
+  }
+};
+
+template <typename T>
+struct Chunk;
+template <>
+struct Chunk<float> {
+  static constexpr int n = 8;
+  float v[8];
+  __device__ __forceinline__ void load(const float* p) {
+    asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+        : "l"(p));
+  }
+};
+template <>
+struct Chunk<double> {
+  static constexpr int n = 4;
+  double v[4];
+  __device__ __forceinline__ void load(const double* p) {
+    asm("ld.global.nc.v4.f64 {%0, %1, %2, %3}, [%4];" : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
   }
 };
 
@@ -150,8 +174,17 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
   const T* g0 =
       op + ts.g_off[0] + int64_t(d0) * (state_of(rb, ts.cr[0]) + int64_t(ts.g_mb[0]) * state_of(rk, ts.cr[0]));
   T me = T(0);
+  constexpr int C = Chunk<T>::n;
   if (ts.nrem == 1) {
-    if ((d0 & 3) == 0) {
+    if (d0 % C == 0) {
+      for (int i = 0; i < d0; i += C) {
+        Chunk<T> a, g;
+        a.load(wc + i);
+        g.load(g0 + i);
+#pragma unroll
+        for (int q = 0; q < C; ++q) me = fma(a.v[q], g.v[q], me);
+      }
+    } else if ((d0 & 3) == 0) {
       for (int i = 0; i < d0; i += 4) {
         Vec4<T> a, g;
         a.load(wc + i);
@@ -172,13 +205,16 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
         a0.load(g0);
         a1.load(g1);
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
-          Vec4<T> wv;
-          wv.load(wc + 4 * j);
-          T acc = wv.v[0] * a0.v[0];
+        for (int c = 0; c < 16 / C; ++c) {
+          Chunk<T> wv;
+          wv.load(wc + C * c);
 #pragma unroll
-          for (int i = 1; i < 4; ++i) acc = fma(wv.v[i], a0.v[i], acc);
-          me = fma(acc, a1.v[j], me);
+          for (int h = 0; h < C / 4; ++h) {
+            T acc = wv.v[4 * h] * a0.v[0];
+#pragma unroll
+            for (int i = 1; i < 4; ++i) acc = fma(wv.v[4 * h + i], a0.v[i], acc);
+            me = fma(acc, a1.v[c * (C / 4) + h], me);
+          }
         }
       } else {
         for (int j = 0; j < d1; ++j) {
@@ -201,13 +237,16 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
         for (int l = 0; l < 4; ++l) {
           T accl = T(0);
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            Vec4<T> wv;
-            wv.load(wc + 4 * (j + 4 * l));
-            T acc = wv.v[0] * a0.v[0];
+          for (int c = 0; c < 16 / C; ++c) {
+            Chunk<T> wv;
+            wv.load(wc + 16 * l + C * c);
 #pragma unroll
-            for (int i = 1; i < 4; ++i) acc = fma(wv.v[i], a0.v[i], acc);
-            accl = fma(acc, a1.v[j], accl);
+            for (int h = 0; h < C / 4; ++h) {
+              T acc = wv.v[4 * h] * a0.v[0];
+#pragma unroll
+              for (int i = 1; i < 4; ++i) acc = fma(wv.v[4 * h + i], a0.v[i], acc);
+              accl = fma(acc, a1.v[c * (C / 4) + h], accl);
+            }
           }
           me = fma(accl, a2.v[l], me);
         }
@@ -228,9 +267,28 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
   return ts.sign < 0 ? -me : me;
 }
 
+#ifndef FCG_SIGMA_RUN32
+#define FCG_SIGMA_RUN32 16
+#endif
+#ifndef FCG_SIGMA_RUN64
+#define FCG_SIGMA_RUN64 16
+#endif
+#ifndef FCG_SIGMA_MINB32
+#define FCG_SIGMA_MINB32 4
+#endif
+#ifndef FCG_SIGMA_MINB64
+#define FCG_SIGMA_MINB64 3
+#endif
 constexpr int kSigmaThreads = 256;
-constexpr int kSigmaRun = 16;  // consecutive triples per thread
-constexpr int64_t kSigmaChunk = int64_t(kSigmaThreads) * kSigmaRun;
+// consecutive triples per thread, and per CTA
+template <typename T>
+__host__ __device__ constexpr int sigma_run() {
+  return sizeof(T) == 4 ? FCG_SIGMA_RUN32 : FCG_SIGMA_RUN64;
+}
+template <typename T>
+__host__ __device__ constexpr int64_t sigma_chunk() {
+  return int64_t(kSigmaThreads) * sigma_run<T>();
+}
 constexpr int kMaxR = 16;
 
 // largest w in [lo, hi] with prefix[w] <= x
@@ -245,6 +303,20 @@ __device__ __forceinline__ int64_t find_item(const int64_t* prefix, int64_t lo, 
   return lo;
 }
 
+// the same over a shared-memory copy of prefix[base ..]
+__device__ __forceinline__ int find_item_shared(const int64_t* s_pre, int lo, int hi, int64_t x) {
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (s_pre[mid] <= x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+constexpr int kPrefixShared = 1024;  // prefix entries a CTA stages in shared memory
+
 template <typename T, int RR>
 __device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* acc, int R) {
   constexpr int RV = RR > 0 ? RR : kMaxR;
@@ -254,31 +326,43 @@ __device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* a
 }
 
 // Each CTA owns a fixed chunk of the flattened triple space (exact load balance) and each
-// thread a run of kSigmaRun consecutive triples (term fastest, then ket, then bra inside a
+// thread a run of sigma_run<T>() consecutive triples (term fastest, then ket, then bra inside a
 // work item), decoded incrementally; contributions to one bra row are summed in registers
 // and flushed with one atomic per root when the bra changes.
 template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads, 3) closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
+    closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
                                                                       const T* __restrict__ op,
                                                                       const T* __restrict__ cin,
                                                                       T* __restrict__ sig) {
   constexpr int RV = RR > 0 ? RR : kMaxR;
-  const int64_t s0 = int64_t(blockIdx.x) * kSigmaChunk;
-  const int64_t e0 = (s0 + kSigmaChunk < p.n_triples) ? s0 + kSigmaChunk : p.n_triples;
-  __shared__ int64_t w_lo_s, w_hi_s;
-  if (threadIdx.x == 0) {
-    w_lo_s = find_item(p.prefix, 0, p.n_items - 1, s0);
-    w_hi_s = find_item(p.prefix, w_lo_s, p.n_items - 1, e0 - 1);
-  }
+  constexpr int64_t kChunk = sigma_chunk<T>();
+  constexpr int kRun = sigma_run<T>();
+  const int64_t s0 = int64_t(blockIdx.x) * kChunk;
+  const int64_t e0 = (s0 + kChunk < p.n_triples) ? s0 + kChunk : p.n_triples;
+  // the CTA's work items [w_lo, w_hi] come from the plan; their prefix goes to shared memory
+  __shared__ int64_t s_pre[kPrefixShared];
+  const int64_t w_lo = __ldg(p.cta_lo + blockIdx.x), w_hi = __ldg(p.cta_lo + blockIdx.x + 1);
+  const int span = int(w_hi - w_lo + 1 < kPrefixShared + 1 ? w_hi - w_lo + 1 : kPrefixShared + 1);
+  const bool staged = span <= kPrefixShared;
+  if (staged)
+    for (int i = threadIdx.x; i < span; i += kSigmaThreads) s_pre[i] = __ldg(p.prefix + w_lo + i);
   __syncthreads();
   const int R = RR > 0 ? RR : p.R;
-  const int64_t t0 = s0 + int64_t(threadIdx.x) * kSigmaRun;
+  const int64_t t0 = s0 + int64_t(threadIdx.x) * kRun;
   if (t0 >= e0) return;
-  const int64_t t1 = (t0 + kSigmaRun < e0) ? t0 + kSigmaRun : e0;
+  const int64_t t1 = (t0 + kRun < e0) ? t0 + kRun : e0;
   const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
-  int64_t wi = find_item(p.prefix, w_lo_s, w_hi_s, t0);
+  int64_t wi, local;
+  if (staged) {
+    const int q = find_item_shared(s_pre, 0, span - 1, t0);
+    wi = w_lo + q;
+    local = t0 - s_pre[q];
+  } else {
+    wi = find_item(p.prefix, w_lo, w_hi, t0);
+    local = t0 - __ldg(p.prefix + wi);
+  }
   WorkItem it = p.items[wi];
-  int64_t local = t0 - __ldg(p.prefix + wi);
   int ti = int(local % it.nt);
   int64_t rest = local / it.nt;
   int kj = int(rest % it.nk);
@@ -291,7 +375,7 @@ __global__ void __launch_bounds__(kSigmaThreads, 3) closed_sigma_kernel(SigmaPar
 #pragma unroll
   for (int r = 0; r < RV; ++r) acc[r] = T(0);
   for (int64_t idx = t0; idx < t1; ++idx) {
-    const TermSector ts = p.ts[it.ts_off + ti];
+    const TermSector& ts = p.ts[it.ts_off + ti];  // fields read where used: fewer live registers
     const T me = dressed_element<T>(ts, w, op, rb, rk);
     const T* ck = cin + int64_t(k) * R;
 #pragma unroll
@@ -551,7 +635,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
     int64_t i = dense_block_index(s, int(r[0]), int(r[1]), int(r[2]), int(r[3]), int(r[4]), int(r[5]));
     ctx->h_blk_index[i] = int32_t(b);
   }
-  // device copy: every block starts on a multiple of kAlign elements (16-byte vector loads
+  // device copy: every block starts on a multiple of kAlign elements (32-byte vector loads
   // of TDM columns whose length is a multiple of 4)
   int64_t cursor = 0;
   for (int64_t b = 0; b < n_blocks; ++b) {
@@ -723,6 +807,23 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
   FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));
   FCG_CUDA(ctx->d_prefix.upload(P.prefix.data(), P.prefix.size(), ctx->stream));
+  {
+    // work item holding the first triple of every closed-sigma CTA, per precision's chunk
+    std::vector<int64_t> lo32, lo64;
+    const int64_t n_items = int64_t(P.items.size());
+    auto cta_items = [&](int64_t chunk, std::vector<int64_t>& out) {
+      const int64_t n_cta = P.n_triples > 0 ? (P.n_triples + chunk - 1) / chunk : 0;
+      out.assign(size_t(n_cta) + 1, std::max<int64_t>(n_items - 1, 0));
+      for (int64_t c = 0; c < n_cta; ++c) {
+        const int64_t x = c * chunk;
+        out[c] = int64_t(std::upper_bound(P.prefix.begin(), P.prefix.begin() + n_items, x) - P.prefix.begin()) - 1;
+      }
+    };
+    cta_items(sigma_chunk<float>(), lo32);
+    cta_items(sigma_chunk<double>(), lo64);
+    FCG_CUDA(ctx->d_cta32.upload(lo32.data(), lo32.size(), ctx->stream));
+    FCG_CUDA(ctx->d_cta64.upload(lo64.data(), lo64.size(), ctx->stream));
+  }
   FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
@@ -745,10 +846,11 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
 template <typename T>
 static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig) {
   SigmaParams p = make_sigma_params(ctx, R);
+  p.cta_lo = sizeof(T) == 4 ? ctx->d_cta32.p : ctx->d_cta64.p;
   FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
   int launches = 0;
   if (p.n_triples > 0) {
-    int64_t grid = (p.n_triples + kSigmaChunk - 1) / kSigmaChunk;
+    int64_t grid = (p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
     FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many triples for one launch");
     FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     switch (R) {

@@ -13,7 +13,7 @@ constexpr int kNumOps = 24;  // 22 op strings + "H" + "Hcmf"
 constexpr int kOpH = 22;
 constexpr int kOpHcmf = 23;
 constexpr int kCfgStride = 8;  // device rows of local states are padded to 8 int16 (16 bytes)
-constexpr int kAlign = 4;      // device TDM / W blocks start on multiples of 4 elements
+constexpr int kAlign = 8;      // device TDM / W blocks start on multiples of 8 elements (32-byte loads)
 
 // One TDM block on the device.
 struct BlockInfo {
