@@ -423,9 +423,14 @@ def main():
         "gflops_reference_count": {"fp32": stats["flops_reference"] / (k32 * 1e-3) / 1e9,
                                    "fp64": stats["flops_reference"] / (k64 * 1e-3) / 1e9},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": None,
-                     "note": "compulsory bytes per launch / closed_sigma_kernel time (fp32); "
-                             "of measured HBM copy peak"},
+                     "frac": achieved / hbm_peak,
+                     # dram__bytes_read.sum + dram__bytes_write.sum of one float launch on this
+                     # exact workload, from the ncu capture summarised in
+                     # profiles/closed_sigma_kernel_v4_24o6c.md
+                     "traffic": (190.4e6 + 3.2e6) if (n == 100000 and R == 4) else None,
+                     "note": "compulsory bytes per launch / closed_sigma_kernel time (fp32), of measured HBM "
+                             "copy peak; the kernel is bound by the L1 data pipe (80.6 % of peak wavefronts) "
+                             "and the double build by the FP64 pipe (87 %), not by HBM"},
         "e2e": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": n * R * 8,
                 "d2h_bytes_per_step": n * R * 8},
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
