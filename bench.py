@@ -45,6 +45,9 @@ def parse():
     ap.add_argument("--no-bst", dest="bst", action="store_false", help="skip the block-sparse Tucker sigma leg")
     ap.add_argument("--bst-only", action="store_true", help="run only the block-sparse Tucker sigma leg")
     ap.add_argument("--bst-sectors", type=int, default=0, help="first K Fock sectors of the BST vector (0 = all)")
+    ap.add_argument("--no-batched", dest="batched", action="store_false",
+                    help="skip the grouped launch of 256 uneven problems")
+    ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
     return ap.parse_args()
 
 
@@ -242,6 +245,61 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
     return out
 
 
+def batched_benchmark(steps, warmup, n_inst=256):
+    """Batched uneven instances: n_inst independent problems (orbitals in {8,12,16,20},
+    clusters of 2-4 orbitals, half filling, M=8-16, 1-3 roots, seeds 3000+i), each problem's
+    closed sigma in one grouped launch (fcg_sigma_closed_grouped) against the same sigmas
+    launched one context after another.  Returns problem-sigmas/s for both, mixed and FP64."""
+    import torch
+    from fermicg_gb300 import pack, workloads
+    from fermicg_gb300.gpu import GpuSigma, sigma_closed_grouped
+    t0 = time.perf_counter()
+    items = []
+    for i in range(n_inst):
+        prob, st = workloads.config3_instance(i, max_cluster=4)
+        f, c, v, _ = pack.pack_state(st)
+        g = GpuSigma(torch.cuda.current_device())
+        g.set_problem(prob.ops, prob.bases, prob.ham)
+        g.state_set(f, c)
+        dc = torch.from_numpy(np.asfortranarray(v).T.copy()).cuda()
+        items.append((g, dc, torch.empty_like(dc), v.shape[1], f.shape[0]))
+    t_build = time.perf_counter() - t0
+    gs = [it[0] for it in items]
+    cps, sps, rs = [it[1].data_ptr() for it in items], [it[2].data_ptr() for it in items], [it[3] for it in items]
+    out = {"workload": f"{n_inst}_uneven_tpsci_problems_8-20o_clusters2-4_M8-16_R1-3",
+           "instances": n_inst, "total_configs": int(sum(it[4] for it in items)),
+           "total_triples": int(sum(it[0].stats()["n_triples"] for it in items)), "setup_s": t_build}
+    for prec in ("fp32", "fp64"):
+        for _ in range(warmup):
+            sigma_closed_grouped(gs, cps, sps, rs, prec)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            sigma_closed_grouped(gs, cps, sps, rs, prec)
+        e1.record()
+        torch.cuda.synchronize()
+        grouped_ms = e0.elapsed_time(e1) / steps
+        for g, dc, ds, R, _ in items[:4]:
+            g.sigma_closed_device(dc.data_ptr(), ds.data_ptr(), R, prec)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(steps):
+            for g, dc, ds, R, _ in items:
+                g.sigma_closed_device(dc.data_ptr(), ds.data_ptr(), R, prec)
+        e1.record()
+        torch.cuda.synchronize()
+        seq_ms = e0.elapsed_time(e1) / steps
+        out["mixed" if prec == "fp32" else "fp64"] = {
+            "grouped_ms": grouped_ms, "sequential_ms": seq_ms,
+            "problem_sigmas_per_s_grouped": n_inst * 1e3 / grouped_ms,
+            "problem_sigmas_per_s_sequential": n_inst * 1e3 / seq_ms, "grouped_over_sequential": seq_ms / grouped_ms}
+    for g in gs:
+        g.close()
+    return out
+
+
 def clocks_sampler():
     out = []
     stop = threading.Event()
@@ -319,6 +377,10 @@ def main():
 
     fbuild.build()
     torch.cuda.set_device(local)
+    if a.batched_only:
+        if rank == 0:
+            print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup)}))
+        return
     if a.bst_only:
         peaks = {}
         try:
@@ -441,6 +503,11 @@ def main():
             out["serving"] = serving_benchmark()
         except Exception as ex:
             out["serving"] = {"error": str(ex)}
+    if rank == 0 and a.batched:
+        try:
+            out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup)
+        except Exception as ex:
+            out["batched"] = {"error": str(ex)}
     if rank == 0 and a.bst:
         try:
             out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, hbm_peak, a.bst_sectors)

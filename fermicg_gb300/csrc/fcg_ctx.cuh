@@ -90,6 +90,8 @@ struct fcg_ctx {
   DevBuf<int64_t> d_cta32, d_cta64;  // first work item of each closed-sigma CTA (float / double chunks)
   DevBuf<int32_t> d_perm;
   DevBuf<TermSector> d_ts;
+  DevBuf<unsigned char> d_group;    // entries of the last grouped closed sigma led by this context
+  DevBuf<int32_t> d_group_cta;      // problem of every CTA of that launch
   DevBuf<int32_t> d_zero_terms;
   // vectors
   DevBuf<double> d_in64, d_out64;  // column-major staging for host calls

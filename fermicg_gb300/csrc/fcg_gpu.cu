@@ -317,9 +317,8 @@ __device__ __forceinline__ int find_item_shared(const int64_t* s_pre, int lo, in
 
 constexpr int kPrefixShared = 1024;  // prefix entries a CTA stages in shared memory
 
-template <typename T, int RR>
+template <typename T, int RV>
 __device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* acc, int R) {
-  constexpr int RV = RR > 0 ? RR : kMaxR;
 #pragma unroll
   for (int r = 0; r < RV; ++r)
     if (r < R) atomicAdd(sig + int64_t(b) * R + r, acc[r]);
@@ -329,20 +328,19 @@ __device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* a
 // thread a run of sigma_run<T>() consecutive triples (term fastest, then ket, then bra inside a
 // work item), decoded incrementally; contributions to one bra row are summed in registers
 // and flushed with one atomic per root when the bra changes.
-template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
-    closed_sigma_kernel(SigmaParams p, const T* __restrict__ w,
-                                                                      const T* __restrict__ op,
-                                                                      const T* __restrict__ cin,
-                                                                      T* __restrict__ sig) {
-  constexpr int RV = RR > 0 ? RR : kMaxR;
+// RR > 0: exactly RR roots; RR == 0: p.R roots, at most RMAX
+template <typename T, int RR, int RMAX = kMaxR>
+__device__ __forceinline__ void closed_sigma_cta(const SigmaParams& p, const T* __restrict__ w,
+                                                 const T* __restrict__ op, const T* __restrict__ cin,
+                                                 T* __restrict__ sig, int64_t cta) {
+  constexpr int RV = RR > 0 ? RR : RMAX;
   constexpr int64_t kChunk = sigma_chunk<T>();
   constexpr int kRun = sigma_run<T>();
-  const int64_t s0 = int64_t(blockIdx.x) * kChunk;
+  const int64_t s0 = int64_t(cta) * kChunk;
   const int64_t e0 = (s0 + kChunk < p.n_triples) ? s0 + kChunk : p.n_triples;
   // the CTA's work items [w_lo, w_hi] come from the plan; their prefix goes to shared memory
   __shared__ int64_t s_pre[kPrefixShared];
-  const int64_t w_lo = __ldg(p.cta_lo + blockIdx.x), w_hi = __ldg(p.cta_lo + blockIdx.x + 1);
+  const int64_t w_lo = __ldg(p.cta_lo + cta), w_hi = __ldg(p.cta_lo + cta + 1);
   const int span = int(w_hi - w_lo + 1 < kPrefixShared + 1 ? w_hi - w_lo + 1 : kPrefixShared + 1);
   const bool staged = span <= kPrefixShared;
   if (staged)
@@ -394,7 +392,7 @@ __global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB
         }
         const int nb_row = __ldg(p.perm + it.bra_off + bj);
         if (nb_row != b) {
-          flush_row<T, RR>(sig, b, acc, R);
+          flush_row<T, RV>(sig, b, acc, R);
 #pragma unroll
           for (int r = 0; r < RV; ++r) acc[r] = T(0);
           b = nb_row;
@@ -405,7 +403,63 @@ __global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB
       rk = __ldg(cfg + k);
     }
   }
-  flush_row<T, RR>(sig, b, acc, R);
+  flush_row<T, RV>(sig, b, acc, R);
+}
+
+template <typename T, int RR>
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
+    closed_sigma_kernel(SigmaParams p, const T* __restrict__ w, const T* __restrict__ op,
+                        const T* __restrict__ cin, T* __restrict__ sig) {
+  closed_sigma_cta<T, RR>(p, w, op, cin, sig, blockIdx.x);
+}
+
+// Many independent problems in one launch: problem q owns CTAs [cta0, cta0 + its CTA count)
+// of the grid; cta_problem maps every CTA to its problem.
+template <typename T>
+struct GroupEntry {
+  SigmaParams p;
+  const T* w;
+  const T* op;
+  T* cin;            // row-major [n_cfg][R] working copy of C
+  T* sig;            // row-major [n_cfg][R] sigma
+  const double* src; // caller's column-major C
+  double* dst;       // caller's column-major sigma
+  int64_t cta0;
+  int64_t n_cfg;
+};
+
+template <typename T, int RMAX>
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
+    closed_sigma_grouped_kernel(const GroupEntry<T>* __restrict__ g, const int32_t* __restrict__ cta_problem) {
+  const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
+  const SigmaParams p = e.p;
+  closed_sigma_cta<T, 0, RMAX>(p, e.w, e.op, e.cin, e.sig, int64_t(blockIdx.x) - e.cta0);
+}
+
+// problem blockIdx.y: C to the row-major working copy, sigma zeroed
+template <typename T>
+__global__ void grouped_pack_kernel(const GroupEntry<T>* __restrict__ g) {
+  const GroupEntry<T>& e = g[blockIdx.y];
+  const int64_t n = e.n_cfg;
+  const int R = e.p.R;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n * R; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = i / R;
+    const int r = int(i - row * R);
+    e.cin[i] = T(e.src[row + n * r]);
+    e.sig[i] = T(0);
+  }
+}
+
+template <typename T>
+__global__ void grouped_unpack_kernel(const GroupEntry<T>* __restrict__ g) {
+  const GroupEntry<T>& e = g[blockIdx.y];
+  const int64_t n = e.n_cfg;
+  const int R = e.p.R;
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n * R; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t row = i % n;
+    const int r = int(i / n);
+    e.dst[i] = double(e.sig[row * R + r]);
+  }
 }
 
 template <typename T>
@@ -909,6 +963,98 @@ int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_si
   FCG_REQUIRE(d_c && d_sigma, FCG_EINVAL, "null pointer");
   FCG_CUDA(cudaSetDevice(ctx->device));
   return sigma_device_impl(ctx, R, d_c, d_sigma, precision);
+}
+
+}  // extern "C"
+
+// One grouped launch (plus one pack and one unpack launch) over the closed sigmas of several
+// contexts on one device, on the first context's stream.
+template <typename T>
+static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double* const* d_c,
+                        double* const* d_sigma) {
+  fcg_ctx* ctx = ctxs[0];
+  std::vector<GroupEntry<T>> entries(n);
+  std::vector<int32_t> cta_problem;
+  int64_t cta = 0, max_nr = 0;
+  for (int q = 0; q < n; ++q) {
+    fcg_ctx* c = ctxs[q];
+    const int64_t nr = c->n_cfg * R[q];
+    GroupEntry<T>& e = entries[q];
+    e.p = make_sigma_params(c, R[q]);
+    e.p.cta_lo = sizeof(T) == 4 ? c->d_cta32.p : c->d_cta64.p;
+    if (sizeof(T) == 4) {
+      FCG_CUDA(c->d_c32.alloc(size_t(nr)));
+      FCG_CUDA(c->d_s32.alloc(size_t(nr)));
+      e.w = reinterpret_cast<const T*>(c->d_w32.p);
+      e.op = reinterpret_cast<const T*>(c->d_op32.p);
+      e.cin = reinterpret_cast<T*>(c->d_c32.p);
+      e.sig = reinterpret_cast<T*>(c->d_s32.p);
+    } else {
+      FCG_CUDA(c->d_c64.alloc(size_t(nr)));
+      FCG_CUDA(c->d_s64.alloc(size_t(nr)));
+      e.w = reinterpret_cast<const T*>(c->d_w64.p);
+      e.op = reinterpret_cast<const T*>(c->d_op64.p);
+      e.cin = reinterpret_cast<T*>(c->d_c64.p);
+      e.sig = reinterpret_cast<T*>(c->d_s64.p);
+    }
+    e.src = d_c[q];
+    e.dst = d_sigma[q];
+    e.cta0 = cta;
+    e.n_cfg = c->n_cfg;
+    const int64_t n_cta = (e.p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
+    FCG_REQUIRE(cta + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
+    cta_problem.insert(cta_problem.end(), size_t(n_cta), int32_t(q));
+    cta += n_cta;
+    max_nr = std::max(max_nr, nr);
+  }
+  FCG_CUDA(ctx->d_group.upload(reinterpret_cast<const unsigned char*>(entries.data()),
+                               entries.size() * sizeof(GroupEntry<T>), ctx->stream));
+  FCG_CUDA(ctx->d_group_cta.upload(cta_problem.data(), cta_problem.size(), ctx->stream));
+  const GroupEntry<T>* dg = reinterpret_cast<const GroupEntry<T>*>(ctx->d_group.p);
+  const dim3 pgrid = dim3(unsigned(std::min<int64_t>((max_nr + 255) / 256, 1024)), unsigned(n));
+  grouped_pack_kernel<T><<<pgrid, 256, 0, ctx->stream>>>(dg);
+  FCG_CUDA(cudaGetLastError());
+  FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (cta > 0) {
+    int rmax = 0;
+    for (int q = 0; q < n; ++q) rmax = std::max(rmax, R[q]);
+    if (rmax <= 4)
+      closed_sigma_grouped_kernel<T, 4><<<unsigned(cta), kSigmaThreads, 0, ctx->stream>>>(dg, ctx->d_group_cta.p);
+    else
+      closed_sigma_grouped_kernel<T, kMaxR><<<unsigned(cta), kSigmaThreads, 0, ctx->stream>>>(dg, ctx->d_group_cta.p);
+    FCG_CUDA(cudaGetLastError());
+  }
+  FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+  grouped_unpack_kernel<T><<<pgrid, 256, 0, ctx->stream>>>(dg);
+  FCG_CUDA(cudaGetLastError());
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  float ms = 0.f;
+  FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->stats.last_kernel_ms = ms;
+  ctx->stats.kernel_launches = cta > 0 ? 3 : 2;
+  return FCG_OK;
+}
+
+extern "C" {
+
+int fcg_sigma_closed_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* d_c,
+                             double* const* d_sigma, int precision) {
+  if (n < 1 || !ctxs || !ctxs[0]) return FCG_EINVAL;
+  fcg_ctx* ctx = ctxs[0];
+  FCG_REQUIRE(R && d_c && d_sigma, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(n <= 65535, FCG_ELIMIT, "at most 65535 problems per grouped launch");
+  FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
+  for (int q = 0; q < n; ++q) {
+    FCG_REQUIRE(ctxs[q] && d_c[q] && d_sigma[q], FCG_EINVAL, "null context or buffer in the group");
+    FCG_REQUIRE(ctxs[q]->device == ctx->device, FCG_EINVAL, "all contexts of a group must share a device");
+    FCG_REQUIRE(ctxs[q]->have_state, FCG_ESTATE, "every context of the group needs fcg_state_set");
+    FCG_REQUIRE(R[q] >= 1 && R[q] <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
+    for (int q2 = 0; q2 < q; ++q2)
+      FCG_REQUIRE(ctxs[q2] != ctxs[q], FCG_EINVAL, "a context appears twice in the group");
+  }
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  return precision == FCG_FP64 ? grouped_impl<double>(n, ctxs, R, d_c, d_sigma)
+                               : grouped_impl<float>(n, ctxs, R, d_c, d_sigma);
 }
 
 int fcg_sigma_closed(fcg_ctx* ctx, int R, const double* c, double* sigma, int precision) {

@@ -49,6 +49,7 @@ SIGNATURES = {
     "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_sigma_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_triples": (_I, [_P, _P]),
+    "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
 }
 
 
@@ -257,6 +258,22 @@ class GpuSigma:
         s = Stats()
         self._check(self.L.fcg_get_stats(self.h, ctypes.byref(s)), "fcg_get_stats")
         return s.as_dict()
+
+
+def sigma_closed_grouped(gpus, d_c_ptrs, d_sigma_ptrs, roots, precision="fp64"):
+    """Closed sigmas of independent problems (one GpuSigma each, state set) in one grouped
+    launch; device buffers column-major (n_cfg, R) float64.  Returns the leading context's
+    stats (kernel time of the grouped launch)."""
+    n = len(gpus)
+    if not (len(d_c_ptrs) == len(d_sigma_ptrs) == len(roots) == n) or n == 0:
+        raise ValueError("one buffer pair and root count per context")
+    L = gpus[0].L
+    hs = (ctypes.c_void_p * n)(*[g.h.value for g in gpus])
+    rs = (ctypes.c_int * n)(*[int(r) for r in roots])
+    cs = (ctypes.c_void_p * n)(*[int(p) for p in d_c_ptrs])
+    ss = (ctypes.c_void_p * n)(*[int(p) for p in d_sigma_ptrs])
+    gpus[0]._check(L.fcg_sigma_closed_grouped(n, hs, rs, cs, ss, PRECISION[precision]), "fcg_sigma_closed_grouped")
+    return gpus[0].stats()
 
 
 def tps_ci_matvec(state, gpu: GpuSigma, precision="fp64"):

@@ -246,3 +246,32 @@ def single_transfer_sectors(prob):
                 if all(key[c] in prob.bases[c].basis for c in range(N)):
                     out.append(key)
     return out
+
+
+def config3_instance(i, base_seed=3000, max_cluster=5, n_cfg_range=(1000, 4000)):
+    """Instance i of the batched-uneven workload: seed base_seed + i; orbitals drawn from
+    {8, 12, 16, 20}, 2-5 clusters of 2..max_cluster consecutive orbitals, half filling
+    spread over the clusters, M = 8-16 local states per sector (sectors within one electron
+    of the reference), 1-3 roots, an energy-ordered space of n_cfg_range configurations.
+    Returns (problem, state)."""
+    rng = np.random.default_rng(base_seed + i)
+    while True:
+        norb = int(rng.choice([8, 12, 16, 20]))
+        nc = int(rng.integers(2, 6))
+        sizes = [int(x) for x in rng.integers(2, max_cluster + 1, size=nc)]
+        if sum(sizes) == norb:
+            break
+    na = norb // 2
+    alpha = [s // 2 for s in sizes]
+    c = 0
+    while sum(alpha) < na:
+        if alpha[c % nc] < sizes[c % nc]:
+            alpha[c % nc] += 1
+        c += 1
+    fspace = [(a, a) for a in alpha]
+    M = int(rng.integers(8, 17))
+    R = int(rng.integers(1, 4))
+    prob = build_problem(norb, sizes, fspace, 2 * norb, base_seed + i, max_roots=M, delta_elec=1)
+    n_cfg = int(rng.integers(n_cfg_range[0], n_cfg_range[1] + 1))
+    st = energy_ordered_space(prob, n_cfg, R=R, seed=base_seed + i)
+    return prob, st

@@ -136,6 +136,16 @@ int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 
+/* The closed sigma (tps_ci_matvec, src/tpsci_outer.jl:462-527) of n independent problems in
+ * one grouped launch: problem q lives in ctxs[q] (ops, terms and state set), with R[q] roots
+ * and device buffers d_c[q] / d_sigma[q] (column-major n_cfg_q x R[q] float64).  The
+ * reference runs independent problems one after another; here every problem's triples are
+ * CTAs of one grid (plus one pack and one unpack launch), on ctxs[0]'s stream.  All
+ * contexts must be on one device and distinct; the call synchronises.  Timing and launch
+ * counts go to ctxs[0]'s stats. */
+int fcg_sigma_closed_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* d_c,
+                             double* const* d_sigma, int precision);
+
 /* ---- block-sparse Tucker (BST) vectors ----------------------------------------------
  * A BSTstate (src/type_BSTstate.jl:13-18) is flattened to blocks, one per (FockConfig,
  * TuckerConfig) in iteration order:
