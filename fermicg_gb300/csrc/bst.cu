@@ -241,28 +241,19 @@ __device__ __forceinline__ void prefetch_range(const void* p, int64_t bytes, int
 // (power of two, <= 32) and added to out[r * out_stride + bra core index].
 template <typename T, int TEAM, bool ATOMIC>
 __device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ op, const T* __restrict__ S,
-                                const T* __restrict__ cin, int64_t core_total, T* ws, int stride, T* out,
-                                int64_t out_stride) {
+                                const int32_t* __restrict__ perm, const T* __restrict__ cin, int64_t core_total,
+                                T* ws, int stride, T* out, int64_t out_stride) {
   const int tid = TEAM == 32 ? int(threadIdx.x & 31) : int(threadIdx.x);
   const int k = G.k, m = G.m, na = G.na, nsp = G.nsp;
   prefetch_range<TEAM, true>(op + G.op_off, int64_t(m) * k * int64_t(sizeof(T)), tid);
-  // 1. gather the ket cores in X order
+  // 1. gather the ket cores in X order (the ket's actives-first index table)
   {
     const int n = G.kcore;
-    for (int idx = tid; idx < R * n; idx += TEAM) {
-      const int r = idx / n, e = idx - r * n;
-      int rem = e, src = 0;
-      for (int a = 0; a < na; ++a) {
-        const int d = rem % G.a_kr[a];
-        rem /= G.a_kr[a];
-        src += d * G.a_ks[a];
-      }
-      for (int j = 0; j < nsp; ++j) {
-        const int d = rem % G.s_kr[j];
-        rem /= G.s_kr[j];
-        src += d * G.s_ks[j];
-      }
-      ws[int64_t(2 * r) * stride + e] = cin[int64_t(r) * core_total + G.k_off + src];
+    const int32_t* kp = perm + G.kperm_off;
+    for (int r = 0; r < R; ++r) {
+      const T* src = cin + int64_t(r) * core_total + G.k_off;
+      T* dst = ws + int64_t(2 * r) * stride;
+      for (int e = tid; e < n; e += TEAM) dst[e] = src[__ldg(kp + e)];
     }
   }
   team_sync<TEAM>();
@@ -289,62 +280,53 @@ __device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ 
       inner *= rb;
     }
   }
-  // 3. bra core[kb, s] += OP[:, kb] . X[:, s]
+  // 3. bra core[kb, s] += OP[:, kb] . X[:, s]; position col + m*s of the bra's actives-first
+  // layout is bra core index bp[col + m*s]
   int ns = 1;
   for (int j = 0; j < nsp; ++j) ns *= G.s_br[j];
-  const int items = m * ns * R;
+  const int mn = m * ns;
   const T* opg = op + G.op_off;
-  auto bra_index = [&](int col, int s) {
-    int off = 0, rem = col;
-    for (int a = 0; a < na; ++a) {
-      off += (rem % G.a_br[a]) * G.a_bs[a];
-      rem /= G.a_br[a];
-    }
-    rem = s;
-    for (int j = 0; j < nsp; ++j) {
-      off += (rem % G.s_br[j]) * G.s_bs[j];
-      rem /= G.s_br[j];
-    }
-    return off;
-  };
+  const int32_t* bp = perm + G.bperm_off;
   if (k < 32) {
-    // short columns: one thread per (kb, s, root); items of one group never share an output
-    for (int it = tid; it < items; it += TEAM) {
-      const int col = it % m;
-      const int s = (it / m) % ns;
-      const int r = it / (m * ns);
-      const T* o = opg + int64_t(k) * col;
-      const T* X = ws + int64_t(2 * r + cur) * stride + int64_t(k) * s;
-      T acc = T(0), acc2 = T(0);
-      int kk = 0;
-      for (; kk + 1 < k; kk += 2) {
-        acc = fma(o[kk], X[kk], acc);
-        acc2 = fma(o[kk + 1], X[kk + 1], acc2);
+    // short columns: one thread per (kb, s) and root; items of one group never share an output
+    for (int r = 0; r < R; ++r) {
+      const T* Xr = ws + int64_t(2 * r + cur) * stride;
+      T* outr = out + int64_t(r) * out_stride;
+      for (int it = tid; it < mn; it += TEAM) {
+        const int s = it / m, col = it - s * m;
+        const T* o = opg + int64_t(k) * col;
+        const T* X = Xr + int64_t(k) * s;
+        T acc = T(0), acc2 = T(0);
+        int kk = 0;
+        for (; kk + 1 < k; kk += 2) {
+          acc = fma(o[kk], X[kk], acc);
+          acc2 = fma(o[kk + 1], X[kk + 1], acc2);
+        }
+        if (kk < k) acc = fma(o[kk], X[kk], acc);
+        acc += acc2;
+        T* dst = outr + __ldg(bp + it);
+        if (ATOMIC)
+          atomicAdd(dst, acc);
+        else
+          *dst += acc;
       }
-      if (kk < k) acc = fma(o[kk], X[kk], acc);
-      acc += acc2;
-      T* dst = out + int64_t(r) * out_stride + bra_index(col, s);
-      if (ATOMIC)
-        atomicAdd(dst, acc);
-      else
-        *dst += acc;
     }
     return;
   }
   // long columns: a warp per (kb, s, root), lanes along the column (coalesced reads of OP)
   const int wid = tid >> 5, lane = tid & 31;
   constexpr int nw = TEAM >> 5;
+  const int items = mn * R;
   for (int it = wid; it < items; it += nw) {
-    const int col = it % m;
-    const int s = (it / m) % ns;
-    const int r = it / (m * ns);
+    const int r = it / mn, rem = it - r * mn;
+    const int s = rem / m, col = rem - s * m;
     const T* o = opg + int64_t(k) * col;
     const T* X = ws + int64_t(2 * r + cur) * stride + int64_t(k) * s;
     T acc = T(0);
     for (int kk = lane; kk < k; kk += 32) acc = fma(o[kk], X[kk], acc);
     for (int w = 16; w > 0; w >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, w);
     if (lane == 0) {
-      T* dst = out + int64_t(r) * out_stride + bra_index(col, s);
+      T* dst = out + int64_t(r) * out_stride + __ldg(bp + rem);
       if (ATOMIC)
         atomicAdd(dst, acc);
       else
@@ -366,6 +348,7 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_bra_kernel(const int32_
                                                                     const BstBlock* __restrict__ blocks, int R,
                                                                     const T* __restrict__ op,
                                                                     const T* __restrict__ S,
+                                                                    const int32_t* __restrict__ perm,
                                                                     const T* __restrict__ cin, T* __restrict__ cout,
                                                                     int64_t core_total, int slice, int priv) {
   extern __shared__ __align__(16) unsigned char bst_smem[];
@@ -388,9 +371,9 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_bra_kernel(const int32_
     }
     load_group<32>(groups + glist[j], G, lane);
     if (priv)
-      bst_group_apply<T, 32, false>(*G, R, op, S, cin, core_total, ws, G->ws, mine, n);
+      bst_group_apply<T, 32, false>(*G, R, op, S, perm, cin, core_total, ws, G->ws, mine, n);
     else
-      bst_group_apply<T, 32, true>(*G, R, op, S, cin, core_total, ws, G->ws, mine, n);
+      bst_group_apply<T, 32, true>(*G, R, op, S, perm, cin, core_total, ws, G->ws, mine, n);
     __syncwarp();  // the next description overwrites this one
   }
   __syncthreads();
@@ -408,13 +391,15 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_smem_kernel(const int32
                                                                      const BstGroup* __restrict__ groups, int R,
                                                                      const T* __restrict__ op,
                                                                      const T* __restrict__ S,
+                                                                     const int32_t* __restrict__ perm,
                                                                      const T* __restrict__ cin, T* __restrict__ cout,
                                                                      int64_t core_total) {
   extern __shared__ __align__(16) unsigned char bst_smem[];
   BstGroup* G = reinterpret_cast<BstGroup*>(bst_smem);
   T* ws = reinterpret_cast<T*>(bst_smem + sizeof(BstGroup));
   load_group<kBstThreads>(groups + list[blockIdx.x], G, threadIdx.x);
-  bst_group_apply<T, kBstThreads, true>(*G, R, op, S, cin, core_total, ws, G->ws, cout + G->b_off, core_total);
+  bst_group_apply<T, kBstThreads, true>(*G, R, op, S, perm, cin, core_total, ws, G->ws, cout + G->b_off,
+                                        core_total);
 }
 
 // Large groups: a grid of CTAs, each with its own global-memory workspace slice, walking
@@ -424,6 +409,7 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int
                                                                        const BstGroup* __restrict__ groups, int R,
                                                                        const T* __restrict__ op,
                                                                        const T* __restrict__ S,
+                                                                       const int32_t* __restrict__ perm,
                                                                        const T* __restrict__ cin,
                                                                        T* __restrict__ cout, int64_t core_total,
                                                                        T* __restrict__ ws_all, int stride) {
@@ -431,7 +417,8 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int
   T* ws = ws_all + int64_t(blockIdx.x) * 2 * R * stride;
   for (int i = blockIdx.x; i < n_list; i += gridDim.x) {
     load_group<kBstThreads>(groups + list[i], &G, threadIdx.x);
-    bst_group_apply<T, kBstThreads, true>(G, R, op, S, cin, core_total, ws, stride, cout + G.b_off, core_total);
+    bst_group_apply<T, kBstThreads, true>(G, R, op, S, perm, cin, core_total, ws, stride, cout + G.b_off,
+                                          core_total);
     __syncthreads();
   }
 }
@@ -459,9 +446,36 @@ struct BstPlan {
   std::vector<BstGroup> groups;
   std::vector<BstOverlapJob> overlaps;
   std::vector<int32_t> triples;
+  std::vector<int32_t> perm;  // actives-first index tables
   int64_t g_total = 0, op_total = 0, s_total = 0;
   int64_t flops_ref = 0, flops_exec = 0;
 };
+
+// perm[x] = core offset of position x of block B's actives-first layout for the active
+// clusters `mask`: x = (mixed radix over the active clusters) + (their rank product) *
+// (mixed radix over the other clusters), both in increasing cluster order.
+void append_perm(const BstBlock& B, int N, int mask, std::vector<int32_t>& perm) {
+  const size_t base = perm.size();
+  perm.resize(base + size_t(B.core_len));
+  int ka_len = 1;
+  for (int c = 0; c < N; ++c)
+    if ((mask >> c) & 1) ka_len *= B.rank[c];
+  for (int e = 0; e < B.core_len; ++e) {
+    int rem = e, ka = 0, kam = 1, sp = 0, spm = 1;
+    for (int c = 0; c < N; ++c) {
+      const int v = rem % B.rank[c];
+      rem /= B.rank[c];
+      if ((mask >> c) & 1) {
+        ka += v * kam;
+        kam *= B.rank[c];
+      } else {
+        sp += v * spm;
+        spm *= B.rank[c];
+      }
+    }
+    perm[base + size_t(ka) + size_t(ka_len) * size_t(sp)] = e;
+  }
+}
 
 // The triples of build_sigma! (every bra block against every ket block whose Fock sector
 // differs by a TransferConfig of H, every term of that transfer with at most nbody clusters
@@ -512,6 +526,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
   for (int64_t k = 0; k < nb; ++k) sectors[hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
   std::unordered_map<uint64_t, int64_t> gamma_at;   // (bra, ket, c, op) -> g offset
   std::unordered_map<uint64_t, int64_t> overlap_at; // (bra, ket, c) -> S offset
+  std::unordered_map<uint64_t, int64_t> perm_at;    // (block, active mask) -> index table offset
   std::vector<std::vector<BstGroupTerm>> gt;        // terms per group
   std::vector<int16_t> fk(2 * N);
   for (int64_t b = 0; b < nb; ++b) {
@@ -671,6 +686,16 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     for (int j = G.nsp; j < kMaxClusters; ++j) G.s_off[j] = 0;
     if (ws > (int64_t(1) << 30)) return "BST: a core exceeds 2^30 elements";
     G.ws = int32_t(align_up(ws));
+    for (int side = 0; side < 2; ++side) {
+      const int32_t b = side == 0 ? G.ket : G.bra;
+      const uint64_t key = uint64_t(b) * 256 + uint64_t(G.act_mask);
+      auto it = perm_at.find(key);
+      if (it == perm_at.end()) {
+        it = perm_at.emplace(key, int64_t(P.perm.size())).first;
+        append_perm(blk[b], N, G.act_mask, P.perm);
+      }
+      (side == 0 ? G.kperm_off : G.bperm_off) = it->second;
+    }
     const int64_t f = 2 * m * k * n + tf;
     P.flops_exec += f;
     P.flops_ref += f * G.nt;
@@ -681,7 +706,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
 // Every index the sigma kernels form from a group description, checked against the buffers
 // it addresses (ket / bra cores, operator cache, overlaps, workspace).
 std::string check_groups(const std::vector<BstGroup>& groups, const std::vector<BstBlock>& blk, int64_t core_total,
-                         int64_t op_total, int64_t s_total) {
+                         int64_t op_total, int64_t s_total, int64_t perm_total) {
   for (const BstGroup& G : groups) {
     if (G.bra < 0 || G.ket < 0 || size_t(G.bra) >= blk.size() || size_t(G.ket) >= blk.size()) return "BST check: block id";
     const BstBlock& B = blk[G.bra];
@@ -716,6 +741,9 @@ std::string check_groups(const std::vector<BstGroup>& groups, const std::vector<
     if (kmax >= G.kcore || bmax >= G.bcore) return "BST check: core strides";
     if (int64_t(G.ws) < ws_need || int64_t(G.k) * (G.bcore / std::max(G.m, 1)) > G.ws) return "BST check: workspace";
     if (G.op_off < 0 || G.op_off + int64_t(G.m) * G.k > op_total) return "BST check: operator extent";
+    if (G.kperm_off < 0 || G.kperm_off + G.kcore > perm_total || G.bperm_off < 0 || G.bperm_off + G.bcore > perm_total)
+      return "BST check: index-table extent";
+    if (int64_t(G.m) * (G.bcore / std::max(G.m, 1)) != G.bcore) return "BST check: bra layout";
   }
   return "";
 }
@@ -795,7 +823,7 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
                                   int(kWarps * kWarpSmemBytes + kAccBytes)));
     bst_sigma_bra_kernel<T><<<unsigned(ctx->bst_bra_ids.size()), kBstThreads, smem, ctx->stream>>>(
         ctx->d_bst_bra_ids.p, ctx->d_bst_bra_ptr.p, ctx->d_bst_bra_glist.p, ctx->d_bst_groups.p, ctx->d_bst_blocks.p,
-        R, op, S, cin, cout, ct, ctx->bst_bra_slice, priv);
+        R, op, S, ctx->d_bst_perm.p, cin, cout, ct, ctx->bst_bra_slice, priv);
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -806,7 +834,7 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     FCG_CUDA(cudaFuncSetAttribute(bst_sigma_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(kSigmaSmemBytes)));
     bst_sigma_smem_kernel<T><<<unsigned(ctx->bst_small.size()), kBstThreads, smem, ctx->stream>>>(
-        ctx->d_bst_small.p, ctx->d_bst_groups.p, R, op, S, cin, cout, ct);
+        ctx->d_bst_small.p, ctx->d_bst_groups.p, R, op, S, ctx->d_bst_perm.p, cin, cout, ct);
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -815,8 +843,8 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     const int64_t stride = ctx->bst_ws_large;
     FCG_CUDA(ws.alloc(size_t(grid) * 2 * R * stride));
     bst_sigma_global_kernel<T><<<unsigned(grid), kBstThreads, 0, ctx->stream>>>(
-        ctx->d_bst_large.p, int(ctx->bst_large.size()), ctx->d_bst_groups.p, R, op, S, cin, cout, ct, ws.p,
-        int(stride));
+        ctx->d_bst_large.p, int(ctx->bst_large.size()), ctx->d_bst_groups.p, R, op, S, ctx->d_bst_perm.p, cin, cout,
+        ct, ws.p, int(stride));
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
@@ -874,11 +902,12 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
   const double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   FCG_REQUIRE(P.groups.size() < (size_t(1) << 31), FCG_ELIMIT, "BST: too many groups");
   {
-    std::string msg = check_groups(P.groups, blk, off, P.op_total, P.s_total);
+    std::string msg = check_groups(P.groups, blk, off, P.op_total, P.s_total, int64_t(P.perm.size()));
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
   // device structures and the operator cache
   FCG_CUDA(ctx->d_bst_factors.upload(factors, size_t(n_factors), ctx->stream));
+  FCG_CUDA(ctx->d_bst_perm.upload(P.perm.data(), P.perm.size(), ctx->stream));
   FCG_CUDA(ctx->d_bst_blocks.upload(blk.data(), blk.size(), ctx->stream));
   FCG_CUDA(ctx->d_bst_groups.upload(P.groups.data(), P.groups.size(), ctx->stream));
   DevBuf<BstGamma> d_gam;

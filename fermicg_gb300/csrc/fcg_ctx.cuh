@@ -140,6 +140,7 @@ struct fcg_ctx {
   DevBuf<int32_t> d_bst_small, d_bst_large, d_bst_bra_ids, d_bst_bra_glist;
   DevBuf<int64_t> d_bst_bra_ptr;
   DevBuf<double> d_bst_factors;
+  DevBuf<int32_t> d_bst_perm;      // actives-first index tables per (block, active clusters)
   DevBuf<double> d_bst_op64, d_bst_s64;
   DevBuf<float> d_bst_op32, d_bst_s32;
   DevBuf<double> d_bst_in64, d_bst_out64, d_bst_ws64;

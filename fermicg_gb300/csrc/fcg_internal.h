@@ -162,6 +162,9 @@ struct BstGroup {
   int32_t s_kr[kMaxClusters], s_br[kMaxClusters];
   int32_t s_ks[kMaxClusters], s_bs[kMaxClusters];
   int32_t pad[2];
+  // index tables (core offset of every position of the actives-first layout) of the ket and
+  // the bra block for this group's active clusters
+  int64_t kperm_off, bperm_off;
 };
 static_assert(sizeof(BstGroup) % 16 == 0, "BstGroup is copied to shared memory in 16-byte units");
 
