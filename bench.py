@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the grouped launch of 256 uneven problems")
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
+    ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
+    ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
     return ap.parse_args()
 
 
@@ -300,6 +302,60 @@ def batched_benchmark(steps, warmup, n_inst=256):
     return out
 
 
+def open_benchmark(steps, warmup, cpu_seconds, n_cfg=10000, R=4, thresh=1e-4):
+    """open_matvec_thread (the FOIS sigma of TPSCI's selection step) on the bench problem:
+    the n_cfg lowest configurations, R roots, contributions kept when |x| > thresh/max|c|.
+    Device time of fcg_sigma_open (screen, expand, hash, compact) and the whole call with
+    the outputs fetched to the host; the oracle's restatement on a sample of ket rows."""
+    from fermicg_gb300 import pack, workloads
+    from fermicg_gb300.gpu import GpuSigma
+    prob = workloads.config1_problem(0)
+    st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=0)
+    f, c, v, _ = pack.pack_state(st)
+    po, pt = pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham)
+    g = GpuSigma(0)
+    g.set_ops(po)
+    g.set_terms(pt)
+    g.state_set(f, c)
+    for _ in range(warmup):
+        of, oc, ov = g.sigma_open(v, thresh)
+    walls, kms = [], []
+    for _ in range(steps):
+        t1 = time.perf_counter()
+        of, oc, ov = g.sigma_open(v, thresh)
+        walls.append(time.perf_counter() - t1)
+        kms.append(g.stats()["last_kernel_ms"])
+    st_ = g.stats()
+    wall = statistics.median(walls)
+    out = {"workload": f"open_sigma_24o_6x4_M16_{n_cfg}cfg_R{R}_thresh{thresh:g}", "n_cfg": int(f.shape[0]),
+           "roots": R, "thresh": thresh, "n_out": int(of.shape[0]), "jobs": st_["open_jobs"],
+           "jobs_kept_by_screen": st_["open_jobs_kept"], "contractions": st_["open_contractions"],
+           "value": 1.0 / wall, "unit": "open_sigma_builds/s", "wall_ms": 1e3 * wall,
+           "device_ms": statistics.median(kms),
+           "contractions_per_s": st_["open_contractions"] / wall}
+    g.close()
+    if cpu_seconds > 0:
+        import oracle
+        O = oracle.Oracle(po, pt)
+        threads = os.cpu_count() or 1
+        n = f.shape[0]
+        nblk = 8
+        for frac in (0.0025, 0.01):
+            rows = max(1, int(n * frac / nblk))
+            t1 = time.perf_counter()
+            for b in range(nblk):
+                s0 = (b * n) // nblk
+                O.sigma_open(f, c, v, thresh, rows=(s0, min(n, s0 + rows)), n_threads=threads)
+            dt = time.perf_counter() - t1
+            if dt > cpu_seconds / 4:
+                break
+        done = nblk * rows
+        out["cpu_baseline"] = {"value": done / (dt * n), "unit": "open_sigma_builds/s", "cores": threads,
+                               "kind": "port", "sample": f"{done} of {n} ket rows in {nblk} evenly spaced blocks, "
+                               f"{dt:.1f} s, scaled to the full build (oracle open_matvec_thread restatement)"}
+    return out
+
+
 def clocks_sampler():
     out = []
     stop = threading.Event()
@@ -377,6 +433,10 @@ def main():
 
     fbuild.build()
     torch.cuda.set_device(local)
+    if a.open_only:
+        if rank == 0:
+            print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)}))
+        return
     if a.batched_only:
         if rank == 0:
             print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup)}))
@@ -503,6 +563,11 @@ def main():
             out["serving"] = serving_benchmark()
         except Exception as ex:
             out["serving"] = {"error": str(ex)}
+    if rank == 0 and a.open:
+        try:
+            out["open_sigma"] = open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)
+        except Exception as ex:
+            out["open_sigma"] = {"error": str(ex)}
     if rank == 0 and a.batched:
         try:
             out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup)
