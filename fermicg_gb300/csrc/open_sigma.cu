@@ -12,16 +12,17 @@
 //                   sum_rest Wmax * prod Gmax skips jobs whose every contribution would
 //                   fail the threshold (the role of upper_bound_thread, :897-1023; skipping
 //                   changes no result), the survivors are compacted;
-//   CUB scan        output-tuple prefix over the surviving jobs;
-//   expand_kernel   one thread per (job, bra tuple): contraction, threshold, then an
-//                   insert into an open-addressed table keyed by (bra sector, mixed-radix
-//                   local-state index) with atomic accumulation of the R values;
+//   expand_jobs_kernel  persistent CTAs take the surviving (ket, term) jobs from a counter,
+//                   stage the job's W block and TDM columns in shared memory, contract
+//                   W with the first TDM once per job and evaluate every bra tuple from
+//                   there (threshold per contribution, as the reference), then insert into
+//                   an open-addressed table keyed by (bra sector, mixed-radix local-state
+//                   index) with atomic accumulation of the R values;
 //   compact_kernel  occupied slots -> (key, values).
 // A table that overflows its probe limit sets a flag and the call is repeated with a
 // table twice as large.
-#include <cub/cub.cuh>
-
 #include <cmath>
+#include <cstring>
 #include <unordered_map>
 
 #include "fcg_ctx.cuh"
@@ -34,7 +35,8 @@ constexpr unsigned long long kEmpty = ~0ull;
 constexpr int kMaxProbe = 1 << 16;
 constexpr int kKeyIdxBits = 40;
 
-// counters: [0] kept jobs, [1] elements of kept jobs, [2] table overflow, [3] output rows
+// counters: [0] kept jobs, [1] elements of kept jobs, [2] table overflow, [3] output rows,
+// [4] next job of the expand CTAs
 struct OpenParams {
   const OpenTerm* ot;
   const OpenItem* items;
@@ -123,13 +125,6 @@ __global__ void screen_kernel(OpenParams p, const double* __restrict__ wmax, con
   atomicAdd(counters + 1, (unsigned long long)o.out_count);
 }
 
-__global__ void job_counts_kernel(const int2* __restrict__ kept, int64_t n, const OpenTerm* __restrict__ ot,
-                                  int64_t* __restrict__ counts) {
-  const int64_t j = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (j >= n) return;
-  counts[j] = ot[kept[j].y].out_count;
-}
-
 __device__ __forceinline__ void table_add(unsigned long long* keys, double* vals, unsigned long long cap_mask,
                                           unsigned long long key, const double* add, int R,
                                           unsigned long long* overflow) {
@@ -152,73 +147,211 @@ __device__ __forceinline__ void table_add(unsigned long long* keys, double* vals
   atomicExch(overflow, 1ull);
 }
 
-__global__ void expand_kernel(OpenParams p, const int2* __restrict__ kept, const int64_t* __restrict__ jprefix,
-                              int64_t n_kept, int64_t n_elem, const double* __restrict__ w,
-                              const double* __restrict__ op, unsigned long long* __restrict__ keys,
-                              double* __restrict__ vals, unsigned long long cap_mask,
-                              unsigned long long* __restrict__ counters) {
-  const int64_t e = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (e >= n_elem) return;
-  const int64_t j = find_item(jprefix, 0, n_kept - 1, e);
-  const int2 job = kept[j];
-  const OpenTerm& o = p.ot[job.y];
+constexpr int kExpThreads = 256;
+constexpr int kExpSmemBytes = 96 * 1024;  // shared-memory budget of one expand CTA
+
+// Shared-memory layout of one job's tiles (in doubles): W block of the ket's dressed-cluster
+// state for every bra state of that cluster [rest][mb0], TDM columns of the remaining
+// clusters [d_a][mb_a], and T1[pair + P*jl] = sum_i W[i + d0*jl, b0] G0[i, b1] with
+// pair = b0 + mb0*b1, P = mb0*mb1, jl < rest/d0.
+struct ExpandTiles {
+  int w, g0, g1, g2, t1, total;
+};
+
+__device__ __forceinline__ ExpandTiles expand_tiles(const OpenTerm& o) {
   const TermSector& ts = o.ts;
-  int64_t loc = e - jprefix[j];
-  int b[4];
-  for (int a = 0; a < o.n_act; ++a) {
-    b[a] = int(loc % o.mb_act[a]);
-    loc /= o.mb_act[a];
-  }
-  const int16_t* ck = p.cfg + int64_t(job.x) * kCfgStride;
-  const double* wc = w + ts.w_off + int64_t(ts.rest_len) * (b[0] + int64_t(ts.w_mb) * ck[ts.cw]);
-  double x;
-  if (ts.nrem == 0) {
-    x = wc[0];
-  } else {
-    const double* g0 = op + ts.g_off[0] + int64_t(ts.g_dim[0]) * (b[1] + int64_t(ts.g_mb[0]) * ck[ts.cr[0]]);
-    const int d0 = ts.g_dim[0];
-    x = 0.0;
-    if (ts.nrem == 1) {
-      for (int i = 0; i < d0; ++i) x = fma(wc[i], g0[i], x);
-    } else {
-      const double* g1 = op + ts.g_off[1] + int64_t(ts.g_dim[1]) * (b[2] + int64_t(ts.g_mb[1]) * ck[ts.cr[1]]);
-      const int d1 = ts.g_dim[1];
-      if (ts.nrem == 2) {
-        for (int jj = 0; jj < d1; ++jj) {
-          double acc = 0.0;
-          for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * jj], g0[i], acc);
-          x = fma(acc, g1[jj], x);
-        }
-      } else {
-        const double* g2 =
-            op + ts.g_off[2] + int64_t(ts.g_dim[2]) * (b[3] + int64_t(ts.g_mb[2]) * ck[ts.cr[2]]);
-        const int d2 = ts.g_dim[2];
-        for (int l = 0; l < d2; ++l) {
-          double al = 0.0;
-          for (int jj = 0; jj < d1; ++jj) {
-            double acc = 0.0;
-            for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * (jj + d1 * l)], g0[i], acc);
-            al = fma(acc, g1[jj], al);
-          }
-          x = fma(al, g2[l], x);
-        }
-      }
-    }
-    if (ts.sign < 0) x = -x;
-  }
-  const double* crow = p.c + int64_t(job.x) * p.R;
-  const double maxc = row_maxabs(crow, p.R);
-  const double tc = p.thresh / maxc;
+  ExpandTiles t{};
+  const int rest = ts.rest_len, mb0 = o.mb_act[0];
+  t.w = 0;
+  int cur = rest * mb0;
+  t.g0 = cur;
+  if (ts.nrem >= 1) cur += ts.g_dim[0] * o.mb_act[1];
+  t.g1 = cur;
+  if (ts.nrem >= 2) cur += ts.g_dim[1] * o.mb_act[2];
+  t.g2 = cur;
+  if (ts.nrem >= 3) cur += ts.g_dim[2] * o.mb_act[3];
+  t.t1 = cur;
+  if (ts.nrem >= 2) cur += (rest / ts.g_dim[0]) * mb0 * o.mb_act[1];
+  t.total = cur;
+  return t;
+}
+
+// one kept contribution: threshold, bra key, accumulation of x * c_ket
+__device__ __forceinline__ void expand_emit(const OpenParams& p, double x, double tc, const double* crow,
+                                            unsigned long long keybase, int64_t idx, unsigned long long* keys,
+                                            double* vals, unsigned long long cap_mask,
+                                            unsigned long long* counters) {
   if (!(fabs(x) > tc)) return;
-  // bra configuration: the ket's states with the active clusters replaced
-  const int64_t* st = p.strides + int64_t(o.bsec) * p.N;
-  int64_t idx = 0;
-  for (int c = 0; c < p.N; ++c) idx += int64_t(ck[c]) * st[c];
-  for (int a = 0; a < o.n_act; ++a) idx += int64_t(b[a] - ck[o.c_act[a]]) * st[o.c_act[a]];
-  const unsigned long long key = (unsigned long long)(o.bsec) << kKeyIdxBits | (unsigned long long)idx;
   double add[16];
   for (int r = 0; r < p.R; ++r) add[r] = x * crow[r];
-  table_add(keys, vals, cap_mask, key, add, p.R, counters + 2);
+  table_add(keys, vals, cap_mask, keybase | (unsigned long long)idx, add, p.R, counters + 2);
+}
+
+// Persistent CTAs take kept (ket, term) jobs from a counter.  Per job the W block and the
+// TDM columns for all bra states are staged in shared memory and W is contracted with the
+// first remaining cluster's TDM once (T1); every thread then owns (b0, b1, b2) units and
+// runs the remaining sums -- the same sums, in the same order and with the same fused
+// multiply-adds, as the per-element formula, so every x is bit-identical to it.  Jobs whose
+// tiles exceed the shared-memory budget are evaluated per element from global memory.
+__global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
+    OpenParams p, const int2* __restrict__ kept, int64_t n_kept, const double* __restrict__ w,
+    const double* __restrict__ op, unsigned long long* __restrict__ keys, double* __restrict__ vals,
+    unsigned long long cap_mask, unsigned long long* __restrict__ counters, int smem_doubles) {
+  extern __shared__ __align__(16) double xs[];
+  __shared__ unsigned long long s_job;
+  for (;;) {
+    if (threadIdx.x == 0) s_job = atomicAdd(counters + 4, 1ull);
+    __syncthreads();
+    const int64_t jn = int64_t(s_job);
+    if (jn >= n_kept) break;  // uniform over the CTA
+    const int2 job = kept[jn];
+    const OpenTerm& o = p.ot[job.y];
+    const TermSector& ts = o.ts;
+    const int16_t* ck = p.cfg + int64_t(job.x) * kCfgStride;
+    const double* crow = p.c + int64_t(job.x) * p.R;
+    const double tc = p.thresh / row_maxabs(crow, p.R);
+    const int nrem = ts.nrem, rest = ts.rest_len;
+    int mb[4] = {1, 1, 1, 1}, ca[4] = {0, 0, 0, 0};
+    for (int a = 0; a < o.n_act; ++a) {
+      mb[a] = o.mb_act[a];
+      ca[a] = o.c_act[a];
+    }
+    // bra key of (b0, .., b3) = keybase | (base + sum_a b_a * st[c_a])
+    const int64_t* st = p.strides + int64_t(o.bsec) * p.N;
+    int64_t base = 0;
+    for (int c = 0; c < p.N; ++c) base += int64_t(ck[c]) * st[c];
+    int64_t sa[4] = {0, 0, 0, 0};
+    for (int a = 0; a < o.n_act; ++a) {
+      base -= int64_t(ck[ca[a]]) * st[ca[a]];
+      sa[a] = st[ca[a]];
+    }
+    const unsigned long long keybase = (unsigned long long)(o.bsec) << kKeyIdxBits;
+    const double sg = ts.sign < 0 ? -1.0 : 1.0;
+    const double* wblk = w + ts.w_off + int64_t(rest) * ts.w_mb * ck[ts.cw];  // [rest][mb0] for the ket state
+    const double* gblk[3] = {nullptr, nullptr, nullptr};
+    for (int r = 0; r < nrem; ++r) gblk[r] = op + ts.g_off[r] + int64_t(ts.g_dim[r]) * ts.g_mb[r] * ck[ts.cr[r]];
+    const ExpandTiles t = expand_tiles(o);
+    if (t.total <= smem_doubles && (nrem < 3 || ts.g_dim[2] <= 16)) {
+      // stage the tiles
+      for (int i = threadIdx.x; i < rest * mb[0]; i += kExpThreads) xs[t.w + i] = wblk[i];
+      for (int r = 0; r < nrem; ++r) {
+        const int n = ts.g_dim[r] * mb[r + 1];
+        double* dst = xs + (r == 0 ? t.g0 : r == 1 ? t.g1 : t.g2);
+        for (int i = threadIdx.x; i < n; i += kExpThreads) dst[i] = gblk[r][i];
+      }
+      __syncthreads();
+      const double* W = xs + t.w;
+      const double* G0 = xs + t.g0;
+      if (nrem == 0) {
+        for (int b0 = threadIdx.x; b0 < mb[0]; b0 += kExpThreads)
+          expand_emit(p, W[b0], tc, crow, keybase, base + b0 * sa[0], keys, vals, cap_mask, counters);
+      } else if (nrem == 1) {
+        const int d0 = ts.g_dim[0];
+        const int P = mb[0] * mb[1];
+        for (int pr = threadIdx.x; pr < P; pr += kExpThreads) {
+          const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
+          double x = 0.0;
+          for (int i = 0; i < d0; ++i) x = fma(W[i + rest * b0], G0[i + d0 * b1], x);
+          expand_emit(p, sg * x, tc, crow, keybase, base + b0 * sa[0] + b1 * sa[1], keys, vals, cap_mask, counters);
+        }
+      } else {
+        const int d0 = ts.g_dim[0], d1 = ts.g_dim[1];
+        const int JL = rest / d0, P = mb[0] * mb[1];
+        double* T1 = xs + t.t1;
+        for (int e = threadIdx.x; e < JL * P; e += kExpThreads) {
+          const int jl = e / P, pr = e - jl * P;
+          const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
+          const double* wc = W + d0 * jl + rest * b0;
+          const double* g0 = G0 + d0 * b1;
+          double acc = 0.0;
+          for (int i = 0; i < d0; ++i) acc = fma(wc[i], g0[i], acc);
+          T1[pr + P * jl] = acc;
+        }
+        __syncthreads();
+        const double* G1 = xs + t.g1;
+        const int units = P * mb[2];
+        for (int u = threadIdx.x; u < units; u += kExpThreads) {
+          const int b2 = u / P, pr = u - b2 * P;
+          const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
+          const int64_t idx3 = base + b0 * sa[0] + b1 * sa[1] + b2 * sa[2];
+          const double* g1 = G1 + d1 * b2;
+          if (nrem == 2) {
+            double x = 0.0;
+            for (int j = 0; j < d1; ++j) x = fma(T1[pr + P * j], g1[j], x);
+            expand_emit(p, sg * x, tc, crow, keybase, idx3, keys, vals, cap_mask, counters);
+          } else {
+            const int d2 = ts.g_dim[2];
+            const double* G2 = xs + t.g2;
+            double ul[16];
+#pragma unroll
+            for (int l = 0; l < 16; ++l) {
+              ul[l] = 0.0;
+              if (l < d2)
+                for (int j = 0; j < d1; ++j) ul[l] = fma(T1[pr + P * (j + d1 * l)], g1[j], ul[l]);
+            }
+            for (int b3 = 0; b3 < mb[3]; ++b3) {
+              const double* g2 = G2 + d2 * b3;
+              double x = 0.0;
+#pragma unroll
+              for (int l = 0; l < 16; ++l)
+                if (l < d2) x = fma(ul[l], g2[l], x);
+              expand_emit(p, sg * x, tc, crow, keybase, idx3 + b3 * sa[3], keys, vals, cap_mask, counters);
+            }
+          }
+        }
+      }
+    } else {
+      // tiles too large: every element from global memory
+      const int64_t n_el = o.out_count;
+      for (int64_t e = threadIdx.x; e < n_el; e += kExpThreads) {
+        int64_t loc = e;
+        int b[4] = {0, 0, 0, 0};
+        for (int a = 0; a < o.n_act; ++a) {
+          b[a] = int(loc % mb[a]);
+          loc /= mb[a];
+        }
+        const double* wc = wblk + int64_t(rest) * b[0];
+        double x;
+        if (nrem == 0) {
+          x = wc[0];
+        } else {
+          const int d0 = ts.g_dim[0];
+          const double* g0 = gblk[0] + int64_t(d0) * b[1];
+          x = 0.0;
+          if (nrem == 1) {
+            for (int i = 0; i < d0; ++i) x = fma(wc[i], g0[i], x);
+          } else {
+            const int d1 = ts.g_dim[1];
+            const double* g1 = gblk[1] + int64_t(d1) * b[2];
+            if (nrem == 2) {
+              for (int jj = 0; jj < d1; ++jj) {
+                double acc = 0.0;
+                for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * jj], g0[i], acc);
+                x = fma(acc, g1[jj], x);
+              }
+            } else {
+              const int d2 = ts.g_dim[2];
+              const double* g2 = gblk[2] + int64_t(d2) * b[3];
+              for (int l = 0; l < d2; ++l) {
+                double al = 0.0;
+                for (int jj = 0; jj < d1; ++jj) {
+                  double acc = 0.0;
+                  for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * (jj + d1 * l)], g0[i], acc);
+                  al = fma(acc, g1[jj], al);
+                }
+                x = fma(al, g2[l], x);
+              }
+            }
+          }
+          x *= sg;
+        }
+        int64_t idx = base;
+        for (int a = 0; a < o.n_act; ++a) idx += b[a] * sa[a];
+        expand_emit(p, x, tc, crow, keybase, idx, keys, vals, cap_mask, counters);
+      }
+    }
+    __syncthreads();  // tiles and s_job are rewritten for the next job
+  }
 }
 
 __global__ void compact_kernel(const unsigned long long* __restrict__ keys, const double* __restrict__ vals,
@@ -396,7 +529,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   FCG_CUDA(cudaMemcpyAsync(ctx->d_in64.p, c, sizeof(double) * n * R, cudaMemcpyHostToDevice, s));
   pack_rows_kernel<<<unsigned((n * R + 255) / 256), 256, 0, s>>>(ctx->d_in64.p, ctx->d_c64.p, n, R);
   FCG_CUDA(cudaGetLastError());
-  FCG_CUDA(ctx->d_counters.alloc(4));
+  FCG_CUDA(ctx->d_counters.alloc(5));
   FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, 4 * sizeof(unsigned long long), s));
   FCG_CUDA(ctx->d_ojobs.alloc(size_t(n_jobs)));
   OpenParams p{};
@@ -422,18 +555,22 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   const int64_t n_elem = int64_t(cnt[1]);
   int launches = 2;
   if (n_kept > 0) {
-    FCG_CUDA(ctx->d_ojob_prefix.alloc(size_t(n_kept) + 1));
-    DevBuf<int64_t> counts;
-    FCG_CUDA(counts.alloc(size_t(n_kept) + 1));
-    job_counts_kernel<<<unsigned((n_kept + 255) / 256), 256, 0, s>>>(ctx->d_ojobs.p, n_kept, ctx->d_oterms.p,
-                                                                     counts.p);
-    FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaMemsetAsync(counts.p + n_kept, 0, sizeof(int64_t), s));
-    size_t tmp_bytes = 0;
-    FCG_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, counts.p, ctx->d_ojob_prefix.p, n_kept + 1, s));
-    FCG_CUDA(ctx->d_scan_tmp.alloc(tmp_bytes));
-    FCG_CUDA(cub::DeviceScan::ExclusiveSum(ctx->d_scan_tmp.p, tmp_bytes, counts.p, ctx->d_ojob_prefix.p, n_kept + 1,
-                                           s));
+    // shared memory of the expand CTAs: the largest job tiles, up to the budget
+    int smem_doubles = 0;
+    for (const OpenTerm& o : ots) {
+      const TermSector& ts = o.ts;
+      int tot = ts.rest_len * o.mb_act[0];
+      for (int r = 0; r < ts.nrem; ++r) tot += ts.g_dim[r] * o.mb_act[r + 1];
+      if (ts.nrem >= 2) tot += (ts.rest_len / ts.g_dim[0]) * o.mb_act[0] * o.mb_act[1];
+      smem_doubles = std::max(smem_doubles, tot);
+    }
+    smem_doubles = std::min(smem_doubles, int(kExpSmemBytes / sizeof(double)));
+    const size_t smem = size_t(smem_doubles) * sizeof(double);
+    FCG_CUDA(cudaFuncSetAttribute(expand_jobs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kExpSmemBytes));
+    int per_sm = 0, n_sm = 0;
+    FCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, expand_jobs_kernel, kExpThreads, smem));
+    FCG_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>(int64_t(std::max(per_sm, 1)) * n_sm, n_kept));
     // table: twice the contributions, power of two, at least 4096 slots; doubled on overflow
     unsigned long long cap = 4096;
     while (cap < 2ull * (unsigned long long)n_elem && cap < (1ull << 28)) cap <<= 1;
@@ -442,11 +579,10 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
       FCG_CUDA(ctx->d_hvals.alloc(cap * R));
       FCG_CUDA(cudaMemsetAsync(ctx->d_hkeys.p, 0xFF, cap * sizeof(unsigned long long), s));
       FCG_CUDA(cudaMemsetAsync(ctx->d_hvals.p, 0, cap * R * sizeof(double), s));
-      FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p + 2, 0, 2 * sizeof(unsigned long long), s));
-      expand_kernel<<<unsigned((n_elem + 255) / 256), 256, 0, s>>>(p, ctx->d_ojobs.p, ctx->d_ojob_prefix.p, n_kept,
-                                                                  n_elem, ctx->d_w64.p, ctx->d_op64.p,
-                                                                  ctx->d_hkeys.p, ctx->d_hvals.p, cap - 1,
-                                                                  ctx->d_counters.p);
+      FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p + 2, 0, 3 * sizeof(unsigned long long), s));
+      expand_jobs_kernel<<<unsigned(grid), kExpThreads, smem, s>>>(p, ctx->d_ojobs.p, n_kept, ctx->d_w64.p,
+                                                                   ctx->d_op64.p, ctx->d_hkeys.p, ctx->d_hvals.p,
+                                                                   cap - 1, ctx->d_counters.p, smem_doubles);
       FCG_CUDA(cudaGetLastError());
       FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
       FCG_CUDA(cudaStreamSynchronize(s));
