@@ -50,6 +50,7 @@ def parse():
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
     ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
+    ap.add_argument("--open-cfg", type=int, default=10000, help="variational configurations of the open sigma leg")
     return ap.parse_args()
 
 
@@ -435,7 +436,8 @@ def main():
     torch.cuda.set_device(local)
     if a.open_only:
         if rank == 0:
-            print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)}))
+            print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds,
+                                                           n_cfg=a.open_cfg)}))
         return
     if a.batched_only:
         if rank == 0:
@@ -565,7 +567,7 @@ def main():
             out["serving"] = {"error": str(ex)}
     if rank == 0 and a.open:
         try:
-            out["open_sigma"] = open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)
+            out["open_sigma"] = open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds, n_cfg=a.open_cfg)
         except Exception as ex:
             out["open_sigma"] = {"error": str(ex)}
     if rank == 0 and a.batched:
