@@ -149,34 +149,79 @@ __device__ __forceinline__ void table_add(unsigned long long* keys, double* vals
 
 constexpr int kExpThreads = 256;
 constexpr int kExpSmemBytes = 96 * 1024;  // shared-memory budget of one expand CTA
+// The float pre-filter keeps a contribution for the exact double evaluation unless
+// |x32| + kFilterMargin * s32 <= thresh / max|c|, where s32 = sum of |products| of the same
+// sum.  The float evaluation differs from the exact value by at most about
+// (number of factors + summed terms) * 2^-24 * s (below 1e-5 s for every shape here), so
+// the margin of 1e-4 s never drops a contribution the double evaluation would keep.
+constexpr float kFilterMargin = 1e-4f;
 
-// Shared-memory layout of one job's tiles (in doubles): W block of the ket's dressed-cluster
-// state for every bra state of that cluster [rest][mb0], TDM columns of the remaining
-// clusters [d_a][mb_a], and T1[pair + P*jl] = sum_i W[i + d0*jl, b0] G0[i, b1] with
-// pair = b0 + mb0*b1, P = mb0*mb1, jl < rest/d0.
+// Shared-memory tiles of one job.  Doubles: the W block of the ket's dressed-cluster state
+// for every bra state of that cluster [rest][mb0] and the TDM columns of the remaining
+// clusters [d_r][mb_{r+1}] (for the exact evaluations).  Floats: the same tiles, and
+// T1[pair + P*jl] = sum_i W[i + d0*jl, b0] G0[i, b1] with its absolute-value twin T1a
+// (pair = b0 + mb0*b1, P = mb0*mb1, jl < rest/d0).
 struct ExpandTiles {
-  int w, g0, g1, g2, t1, total;
+  int w64, g64[3];           // offsets in doubles
+  int w32, g32[3], t1, t1a;  // offsets in floats, after the doubles
+  int bytes;
 };
 
-__device__ __forceinline__ ExpandTiles expand_tiles(const OpenTerm& o) {
-  const TermSector& ts = o.ts;
+__host__ __device__ inline ExpandTiles expand_tiles(int nrem, int rest, const int16_t* g_dim, const int16_t* mb) {
   ExpandTiles t{};
-  const int rest = ts.rest_len, mb0 = o.mb_act[0];
-  t.w = 0;
-  int cur = rest * mb0;
-  t.g0 = cur;
-  if (ts.nrem >= 1) cur += ts.g_dim[0] * o.mb_act[1];
-  t.g1 = cur;
-  if (ts.nrem >= 2) cur += ts.g_dim[1] * o.mb_act[2];
-  t.g2 = cur;
-  if (ts.nrem >= 3) cur += ts.g_dim[2] * o.mb_act[3];
-  t.t1 = cur;
-  if (ts.nrem >= 2) cur += (rest / ts.g_dim[0]) * mb0 * o.mb_act[1];
-  t.total = cur;
+  int d = 0;
+  t.w64 = d;
+  d += rest * mb[0];
+  for (int r = 0; r < 3; ++r) {
+    t.g64[r] = d;
+    if (r < nrem) d += g_dim[r] * mb[r + 1];
+  }
+  d += d & 1;  // float part starts on an even double
+  int f = 2 * d;
+  t.w32 = f;
+  f += rest * mb[0];
+  for (int r = 0; r < 3; ++r) {
+    t.g32[r] = f;
+    if (r < nrem) f += g_dim[r] * mb[r + 1];
+  }
+  const int jlp = nrem >= 2 ? (rest / g_dim[0]) * mb[0] * mb[1] : 0;
+  t.t1 = f;
+  f += jlp;
+  t.t1a = f;
+  f += jlp;
+  t.bytes = 4 * f;
   return t;
 }
 
-// one kept contribution: threshold, bra key, accumulation of x * c_ket
+// The exact contribution of one bra tuple (columns already selected): the sums of the
+// per-element formula, in its order, with its fused multiply-adds.
+__device__ __forceinline__ double exact_x(int nrem, int d0, int d1, int d2, const double* wc, const double* g0,
+                                          const double* g1, const double* g2) {
+  if (nrem == 0) return wc[0];
+  double x = 0.0;
+  if (nrem == 1) {
+    for (int i = 0; i < d0; ++i) x = fma(wc[i], g0[i], x);
+  } else if (nrem == 2) {
+    for (int jj = 0; jj < d1; ++jj) {
+      double acc = 0.0;
+      for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * jj], g0[i], acc);
+      x = fma(acc, g1[jj], x);
+    }
+  } else {
+    for (int l = 0; l < d2; ++l) {
+      double al = 0.0;
+      for (int jj = 0; jj < d1; ++jj) {
+        double acc = 0.0;
+        for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * (jj + d1 * l)], g0[i], acc);
+        al = fma(acc, g1[jj], al);
+      }
+      x = fma(al, g2[l], x);
+    }
+  }
+  return x;
+}
+
+// one contribution: threshold, bra key, accumulation of x * c_ket
 __device__ __forceinline__ void expand_emit(const OpenParams& p, double x, double tc, const double* crow,
                                             unsigned long long keybase, int64_t idx, unsigned long long* keys,
                                             double* vals, unsigned long long cap_mask,
@@ -188,16 +233,19 @@ __device__ __forceinline__ void expand_emit(const OpenParams& p, double x, doubl
 }
 
 // Persistent CTAs take kept (ket, term) jobs from a counter.  Per job the W block and the
-// TDM columns for all bra states are staged in shared memory and W is contracted with the
-// first remaining cluster's TDM once (T1); every thread then owns (b0, b1, b2) units and
-// runs the remaining sums -- the same sums, in the same order and with the same fused
-// multiply-adds, as the per-element formula, so every x is bit-identical to it.  Jobs whose
-// tiles exceed the shared-memory budget are evaluated per element from global memory.
+// TDM columns for all bra states are staged in shared memory (double and float copies) and,
+// for three- and four-cluster terms, W is contracted with the first remaining cluster's
+// TDM once in float (T1, with its absolute-value twin).  Every bra tuple is then screened
+// in float (value and the sum of |products|); the tuples that can pass the threshold are
+// evaluated exactly with the per-element double formula (exact_x) and thresholded as the
+// reference does.  Jobs whose tiles exceed the shared-memory budget are evaluated per
+// element, exactly, from global memory.
 __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
     OpenParams p, const int2* __restrict__ kept, int64_t n_kept, const double* __restrict__ w,
     const double* __restrict__ op, unsigned long long* __restrict__ keys, double* __restrict__ vals,
-    unsigned long long cap_mask, unsigned long long* __restrict__ counters, int smem_doubles) {
+    unsigned long long cap_mask, unsigned long long* __restrict__ counters, int smem_bytes) {
   extern __shared__ __align__(16) double xs[];
+  float* xf = reinterpret_cast<float*>(xs);
   __shared__ unsigned long long s_job;
   for (;;) {
     if (threadIdx.x == 0) s_job = atomicAdd(counters + 4, 1ull);
@@ -210,98 +258,133 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
     const int16_t* ck = p.cfg + int64_t(job.x) * kCfgStride;
     const double* crow = p.c + int64_t(job.x) * p.R;
     const double tc = p.thresh / row_maxabs(crow, p.R);
+    const float tcf = float(tc * (1.0 - 1e-6));
     const int nrem = ts.nrem, rest = ts.rest_len;
-    int mb[4] = {1, 1, 1, 1}, ca[4] = {0, 0, 0, 0};
-    for (int a = 0; a < o.n_act; ++a) {
-      mb[a] = o.mb_act[a];
-      ca[a] = o.c_act[a];
-    }
+    const int d0 = nrem >= 1 ? ts.g_dim[0] : 1, d1 = nrem >= 2 ? ts.g_dim[1] : 1, d2 = nrem >= 3 ? ts.g_dim[2] : 1;
+    int mb[4] = {1, 1, 1, 1};
+    int64_t sa[4] = {0, 0, 0, 0};
     // bra key of (b0, .., b3) = keybase | (base + sum_a b_a * st[c_a])
     const int64_t* st = p.strides + int64_t(o.bsec) * p.N;
     int64_t base = 0;
     for (int c = 0; c < p.N; ++c) base += int64_t(ck[c]) * st[c];
-    int64_t sa[4] = {0, 0, 0, 0};
     for (int a = 0; a < o.n_act; ++a) {
-      base -= int64_t(ck[ca[a]]) * st[ca[a]];
-      sa[a] = st[ca[a]];
+      mb[a] = o.mb_act[a];
+      sa[a] = st[o.c_act[a]];
+      base -= int64_t(ck[o.c_act[a]]) * sa[a];
     }
     const unsigned long long keybase = (unsigned long long)(o.bsec) << kKeyIdxBits;
     const double sg = ts.sign < 0 ? -1.0 : 1.0;
     const double* wblk = w + ts.w_off + int64_t(rest) * ts.w_mb * ck[ts.cw];  // [rest][mb0] for the ket state
     const double* gblk[3] = {nullptr, nullptr, nullptr};
     for (int r = 0; r < nrem; ++r) gblk[r] = op + ts.g_off[r] + int64_t(ts.g_dim[r]) * ts.g_mb[r] * ck[ts.cr[r]];
-    const ExpandTiles t = expand_tiles(o);
-    if (t.total <= smem_doubles && (nrem < 3 || ts.g_dim[2] <= 16)) {
-      // stage the tiles
-      for (int i = threadIdx.x; i < rest * mb[0]; i += kExpThreads) xs[t.w + i] = wblk[i];
+    const ExpandTiles t = expand_tiles(nrem, rest, ts.g_dim, o.mb_act);
+    if (t.bytes <= smem_bytes && d2 <= 16) {
+      for (int i = threadIdx.x; i < rest * mb[0]; i += kExpThreads) {
+        const double v = wblk[i];
+        xs[t.w64 + i] = v;
+        xf[t.w32 + i] = float(v);
+      }
       for (int r = 0; r < nrem; ++r) {
         const int n = ts.g_dim[r] * mb[r + 1];
-        double* dst = xs + (r == 0 ? t.g0 : r == 1 ? t.g1 : t.g2);
-        for (int i = threadIdx.x; i < n; i += kExpThreads) dst[i] = gblk[r][i];
+        for (int i = threadIdx.x; i < n; i += kExpThreads) {
+          const double v = gblk[r][i];
+          xs[t.g64[r] + i] = v;
+          xf[t.g32[r] + i] = float(v);
+        }
       }
       __syncthreads();
-      const double* W = xs + t.w;
-      const double* G0 = xs + t.g0;
+      const double* W = xs + t.w64;
+      const float* Wf = xf + t.w32;
+      const float* G0f = xf + t.g32[0];
+      const int P = mb[0] * mb[1];
       if (nrem == 0) {
         for (int b0 = threadIdx.x; b0 < mb[0]; b0 += kExpThreads)
           expand_emit(p, W[b0], tc, crow, keybase, base + b0 * sa[0], keys, vals, cap_mask, counters);
       } else if (nrem == 1) {
-        const int d0 = ts.g_dim[0];
-        const int P = mb[0] * mb[1];
         for (int pr = threadIdx.x; pr < P; pr += kExpThreads) {
           const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
-          double x = 0.0;
-          for (int i = 0; i < d0; ++i) x = fma(W[i + rest * b0], G0[i + d0 * b1], x);
-          expand_emit(p, sg * x, tc, crow, keybase, base + b0 * sa[0] + b1 * sa[1], keys, vals, cap_mask, counters);
+          const float* wc = Wf + rest * b0;
+          const float* g0 = G0f + d0 * b1;
+          float x32 = 0.f, s32 = 0.f;
+          for (int i = 0; i < d0; ++i) {
+            x32 = fmaf(wc[i], g0[i], x32);
+            s32 = fmaf(fabsf(wc[i]), fabsf(g0[i]), s32);
+          }
+          if (fabsf(x32) + kFilterMargin * s32 > tcf) {
+            const double x = sg * exact_x(1, d0, 1, 1, W + rest * b0, xs + t.g64[0] + d0 * b1, nullptr, nullptr);
+            expand_emit(p, x, tc, crow, keybase, base + b0 * sa[0] + b1 * sa[1], keys, vals, cap_mask, counters);
+          }
         }
       } else {
-        const int d0 = ts.g_dim[0], d1 = ts.g_dim[1];
-        const int JL = rest / d0, P = mb[0] * mb[1];
-        double* T1 = xs + t.t1;
+        const int JL = rest / d0;
+        float* T1 = xf + t.t1;
+        float* T1a = xf + t.t1a;
         for (int e = threadIdx.x; e < JL * P; e += kExpThreads) {
           const int jl = e / P, pr = e - jl * P;
           const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
-          const double* wc = W + d0 * jl + rest * b0;
-          const double* g0 = G0 + d0 * b1;
-          double acc = 0.0;
-          for (int i = 0; i < d0; ++i) acc = fma(wc[i], g0[i], acc);
+          const float* wc = Wf + d0 * jl + rest * b0;
+          const float* g0 = G0f + d0 * b1;
+          float acc = 0.f, aa = 0.f;
+          for (int i = 0; i < d0; ++i) {
+            acc = fmaf(wc[i], g0[i], acc);
+            aa = fmaf(fabsf(wc[i]), fabsf(g0[i]), aa);
+          }
           T1[pr + P * jl] = acc;
+          T1a[pr + P * jl] = aa;
         }
         __syncthreads();
-        const double* G1 = xs + t.g1;
+        const float* G1f = xf + t.g32[1];
         const int units = P * mb[2];
         for (int u = threadIdx.x; u < units; u += kExpThreads) {
           const int b2 = u / P, pr = u - b2 * P;
           const int b1 = pr / mb[0], b0 = pr - b1 * mb[0];
           const int64_t idx3 = base + b0 * sa[0] + b1 * sa[1] + b2 * sa[2];
-          const double* g1 = G1 + d1 * b2;
+          const float* g1 = G1f + d1 * b2;
+          const double* wc = W + rest * b0;
+          const double* g0d = xs + t.g64[0] + d0 * b1;
+          const double* g1d = xs + t.g64[1] + d1 * b2;
           if (nrem == 2) {
-            double x = 0.0;
-            for (int j = 0; j < d1; ++j) x = fma(T1[pr + P * j], g1[j], x);
-            expand_emit(p, sg * x, tc, crow, keybase, idx3, keys, vals, cap_mask, counters);
+            float x32 = 0.f, s32 = 0.f;
+            for (int j = 0; j < d1; ++j) {
+              x32 = fmaf(T1[pr + P * j], g1[j], x32);
+              s32 = fmaf(T1a[pr + P * j], fabsf(g1[j]), s32);
+            }
+            if (fabsf(x32) + kFilterMargin * s32 > tcf) {
+              const double x = sg * exact_x(2, d0, d1, 1, wc, g0d, g1d, nullptr);
+              expand_emit(p, x, tc, crow, keybase, idx3, keys, vals, cap_mask, counters);
+            }
           } else {
-            const int d2 = ts.g_dim[2];
-            const double* G2 = xs + t.g2;
-            double ul[16];
+            const float* G2f = xf + t.g32[2];
+            float ul[16], ua[16];
 #pragma unroll
             for (int l = 0; l < 16; ++l) {
-              ul[l] = 0.0;
+              ul[l] = 0.f;
+              ua[l] = 0.f;
               if (l < d2)
-                for (int j = 0; j < d1; ++j) ul[l] = fma(T1[pr + P * (j + d1 * l)], g1[j], ul[l]);
+                for (int j = 0; j < d1; ++j) {
+                  ul[l] = fmaf(T1[pr + P * (j + d1 * l)], g1[j], ul[l]);
+                  ua[l] = fmaf(T1a[pr + P * (j + d1 * l)], fabsf(g1[j]), ua[l]);
+                }
             }
             for (int b3 = 0; b3 < mb[3]; ++b3) {
-              const double* g2 = G2 + d2 * b3;
-              double x = 0.0;
+              const float* g2 = G2f + d2 * b3;
+              float x32 = 0.f, s32 = 0.f;
 #pragma unroll
               for (int l = 0; l < 16; ++l)
-                if (l < d2) x = fma(ul[l], g2[l], x);
-              expand_emit(p, sg * x, tc, crow, keybase, idx3 + b3 * sa[3], keys, vals, cap_mask, counters);
+                if (l < d2) {
+                  x32 = fmaf(ul[l], g2[l], x32);
+                  s32 = fmaf(ua[l], fabsf(g2[l]), s32);
+                }
+              if (fabsf(x32) + kFilterMargin * s32 > tcf) {
+                const double x = sg * exact_x(3, d0, d1, d2, wc, g0d, g1d, xs + t.g64[2] + d2 * b3);
+                expand_emit(p, x, tc, crow, keybase, idx3 + b3 * sa[3], keys, vals, cap_mask, counters);
+              }
             }
           }
         }
       }
     } else {
-      // tiles too large: every element from global memory
+      // tiles too large: every element exactly, from global memory
       const int64_t n_el = o.out_count;
       for (int64_t e = threadIdx.x; e < n_el; e += kExpThreads) {
         int64_t loc = e;
@@ -310,41 +393,11 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
           b[a] = int(loc % mb[a]);
           loc /= mb[a];
         }
-        const double* wc = wblk + int64_t(rest) * b[0];
-        double x;
-        if (nrem == 0) {
-          x = wc[0];
-        } else {
-          const int d0 = ts.g_dim[0];
-          const double* g0 = gblk[0] + int64_t(d0) * b[1];
-          x = 0.0;
-          if (nrem == 1) {
-            for (int i = 0; i < d0; ++i) x = fma(wc[i], g0[i], x);
-          } else {
-            const int d1 = ts.g_dim[1];
-            const double* g1 = gblk[1] + int64_t(d1) * b[2];
-            if (nrem == 2) {
-              for (int jj = 0; jj < d1; ++jj) {
-                double acc = 0.0;
-                for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * jj], g0[i], acc);
-                x = fma(acc, g1[jj], x);
-              }
-            } else {
-              const int d2 = ts.g_dim[2];
-              const double* g2 = gblk[2] + int64_t(d2) * b[3];
-              for (int l = 0; l < d2; ++l) {
-                double al = 0.0;
-                for (int jj = 0; jj < d1; ++jj) {
-                  double acc = 0.0;
-                  for (int i = 0; i < d0; ++i) acc = fma(wc[i + d0 * (jj + d1 * l)], g0[i], acc);
-                  al = fma(acc, g1[jj], al);
-                }
-                x = fma(al, g2[l], x);
-              }
-            }
-          }
-          x *= sg;
-        }
+        const double xr = exact_x(nrem, d0, d1, d2, wblk + int64_t(rest) * b[0],
+                                  nrem >= 1 ? gblk[0] + int64_t(d0) * b[1] : nullptr,
+                                  nrem >= 2 ? gblk[1] + int64_t(d1) * b[2] : nullptr,
+                                  nrem >= 3 ? gblk[2] + int64_t(d2) * b[3] : nullptr);
+        const double x = nrem == 0 ? xr : sg * xr;
         int64_t idx = base;
         for (int a = 0; a < o.n_act; ++a) idx += b[a] * sa[a];
         expand_emit(p, x, tc, crow, keybase, idx, keys, vals, cap_mask, counters);
@@ -556,16 +609,11 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   int launches = 2;
   if (n_kept > 0) {
     // shared memory of the expand CTAs: the largest job tiles, up to the budget
-    int smem_doubles = 0;
-    for (const OpenTerm& o : ots) {
-      const TermSector& ts = o.ts;
-      int tot = ts.rest_len * o.mb_act[0];
-      for (int r = 0; r < ts.nrem; ++r) tot += ts.g_dim[r] * o.mb_act[r + 1];
-      if (ts.nrem >= 2) tot += (ts.rest_len / ts.g_dim[0]) * o.mb_act[0] * o.mb_act[1];
-      smem_doubles = std::max(smem_doubles, tot);
-    }
-    smem_doubles = std::min(smem_doubles, int(kExpSmemBytes / sizeof(double)));
-    const size_t smem = size_t(smem_doubles) * sizeof(double);
+    int smem_bytes = 0;
+    for (const OpenTerm& o : ots)
+      smem_bytes = std::max(smem_bytes, expand_tiles(o.ts.nrem, o.ts.rest_len, o.ts.g_dim, o.mb_act).bytes);
+    smem_bytes = std::min(smem_bytes, kExpSmemBytes);
+    const size_t smem = size_t(smem_bytes);
     FCG_CUDA(cudaFuncSetAttribute(expand_jobs_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kExpSmemBytes));
     int per_sm = 0, n_sm = 0;
     FCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, expand_jobs_kernel, kExpThreads, smem));
@@ -582,7 +630,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
       FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p + 2, 0, 3 * sizeof(unsigned long long), s));
       expand_jobs_kernel<<<unsigned(grid), kExpThreads, smem, s>>>(p, ctx->d_ojobs.p, n_kept, ctx->d_w64.p,
                                                                    ctx->d_op64.p, ctx->d_hkeys.p, ctx->d_hvals.p,
-                                                                   cap - 1, ctx->d_counters.p, smem_doubles);
+                                                                   cap - 1, ctx->d_counters.p, smem_bytes);
       FCG_CUDA(cudaGetLastError());
       FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
       FCG_CUDA(cudaStreamSynchronize(s));
