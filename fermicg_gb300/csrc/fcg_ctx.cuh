@@ -44,6 +44,32 @@ struct DevBuf {
   }
 };
 
+// Grow-only page-locked host buffer (fast device-to-host copies of large results).
+template <typename T>
+struct PinnedBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  PinnedBuf() = default;
+  PinnedBuf(const PinnedBuf&) = delete;
+  PinnedBuf& operator=(const PinnedBuf&) = delete;
+  ~PinnedBuf() {
+    if (p) cudaFreeHost(p);
+  }
+  cudaError_t alloc(size_t count) {
+    if (count <= n && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    n = 0;
+    cudaError_t e = cudaMallocHost(reinterpret_cast<void**>(&p), std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return e;
+    }
+    n = count;
+    return cudaSuccess;
+  }
+};
+
 }  // namespace fcg
 
 using namespace fcg;
@@ -119,8 +145,9 @@ struct fcg_ctx {
   std::vector<int16_t> open_bra_fock;   // [n_bra_sectors][N][2]
   std::vector<int64_t> open_strides;    // [n_bra_sectors][N]
   std::vector<int64_t> open_dims;       // [n_bra_sectors][N]
-  std::vector<unsigned long long> open_keys;
-  std::vector<double> open_vals;        // [n_out][R] row-major
+  PinnedBuf<unsigned long long> open_keys;  // keys of the last open sigma, open_rows of them
+  PinnedBuf<double> open_vals;              // [open_rows][R] row-major
+  int64_t open_rows = 0;
   int open_R = 0;
   // block-sparse Tucker vector structure and its operator cache (bst.cu)
   bool have_bst = false;

@@ -564,8 +564,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
     }
   }
   ctx->open_R = R;
-  ctx->open_keys.clear();
-  ctx->open_vals.clear();
+  ctx->open_rows = 0;
   if (items.empty()) return FCG_OK;
   std::vector<int64_t> prefix(items.size() + 1, 0);
   for (size_t i = 0; i < items.size(); ++i) prefix[i + 1] = prefix[i] + int64_t(items[i].nrow) * items[i].nt;
@@ -649,11 +648,12 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
     FCG_CUDA(cudaStreamSynchronize(s));
     launches += 1;
     const int64_t n_rows = int64_t(cnt[3]);
-    ctx->open_keys.resize(n_rows);
-    ctx->open_vals.resize(size_t(n_rows) * R);
-    FCG_CUDA(cudaMemcpyAsync(ctx->open_keys.data(), ctx->d_okeys.p, n_rows * sizeof(unsigned long long),
+    FCG_CUDA(ctx->open_keys.alloc(size_t(n_rows)));
+    FCG_CUDA(ctx->open_vals.alloc(size_t(n_rows) * R));
+    ctx->open_rows = n_rows;
+    FCG_CUDA(cudaMemcpyAsync(ctx->open_keys.p, ctx->d_okeys.p, n_rows * sizeof(unsigned long long),
                              cudaMemcpyDeviceToHost, s));
-    FCG_CUDA(cudaMemcpyAsync(ctx->open_vals.data(), ctx->d_ovals.p, n_rows * R * sizeof(double),
+    FCG_CUDA(cudaMemcpyAsync(ctx->open_vals.p, ctx->d_ovals.p, n_rows * R * sizeof(double),
                              cudaMemcpyDeviceToHost, s));
     FCG_CUDA(cudaStreamSynchronize(s));
     float ms = 0.f;
@@ -664,7 +664,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   ctx->stats.open_jobs = n_jobs;
   ctx->stats.open_jobs_kept = n_kept;
   ctx->stats.open_contractions = n_elem;
-  *n_out = int64_t(ctx->open_keys.size());
+  *n_out = ctx->open_rows;
   return FCG_OK;
 }
 
@@ -673,9 +673,10 @@ int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coef
   FCG_REQUIRE(fock && cfg && coeff, FCG_EINVAL, "null pointer");
   const int N = ctx->N;
   const int R = ctx->open_R;
-  const int64_t m = int64_t(ctx->open_keys.size());
+  const int64_t m = ctx->open_rows;
+#pragma omp parallel for schedule(static)
   for (int64_t i = 0; i < m; ++i) {
-    const unsigned long long key = ctx->open_keys[i];
+    const unsigned long long key = ctx->open_keys.p[i];
     const int64_t bs = int64_t(key >> kKeyIdxBits);
     int64_t idx = int64_t(key & ((1ull << kKeyIdxBits) - 1));
     std::memcpy(fock + i * 2 * N, &ctx->open_bra_fock[bs * 2 * N], sizeof(int16_t) * 2 * N);
@@ -684,7 +685,7 @@ int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coef
       cfg[i * N + c] = int16_t(idx % d);
       idx /= d;
     }
-    for (int r = 0; r < R; ++r) coeff[i + m * r] = ctx->open_vals[size_t(i) * R + r];
+    for (int r = 0; r < R; ++r) coeff[i + m * r] = ctx->open_vals.p[size_t(i) * R + r];
   }
   return FCG_OK;
 }

@@ -196,9 +196,9 @@ class GpuSigma:
         self._check(self.L.fcg_sigma_open(self.h, R, _ptr(c), float(thresh), int(nbody), ctypes.byref(m)),
                     "fcg_sigma_open")
         m = m.value
-        of = np.zeros((m, self.N, 2), dtype=np.int16)
-        oc = np.zeros((m, self.N), dtype=np.int16)
-        ov = np.zeros((m, R), dtype=np.float64, order="F")
+        of = np.empty((m, self.N, 2), dtype=np.int16)
+        oc = np.empty((m, self.N), dtype=np.int16)
+        ov = np.empty((m, R), dtype=np.float64, order="F")
         self._check(self.L.fcg_sigma_open_fetch(self.h, _ptr(of), _ptr(oc), _ptr(ov)), "fcg_sigma_open_fetch")
         return of, oc, np.ascontiguousarray(ov)
 
