@@ -232,6 +232,43 @@ __device__ __forceinline__ void expand_emit(const OpenParams& p, double x, doubl
   table_add(keys, vals, cap_mask, keybase | (unsigned long long)idx, add, p.R, counters + 2);
 }
 
+// One (b0, b1, b2) unit of a four-cluster job: float sums over the third remaining cluster's
+// index l < D2 for every b3, screened; survivors evaluated exactly.  D2 = 16 serves any
+// d2 <= 16 with the run-time length `d2`.
+template <int D2>
+__device__ __forceinline__ void unit4(const OpenParams& p, const float* T1, const float* T1a, int P, int pr, int d1,
+                                      const float* g1, const float* G2f, int mb3, float tcf, double tc, double sg,
+                                      int d0, const double* wc, const double* g0d, const double* g1d,
+                                      const double* G2d, const double* crow, unsigned long long keybase,
+                                      int64_t idx3, int64_t sa3, unsigned long long* keys, double* vals,
+                                      unsigned long long cap_mask, unsigned long long* counters, int d2 = D2) {
+  float ul[D2], ua[D2];
+#pragma unroll
+  for (int l = 0; l < D2; ++l) {
+    ul[l] = 0.f;
+    ua[l] = 0.f;
+    if (D2 != 16 || l < d2)
+      for (int j = 0; j < d1; ++j) {
+        ul[l] = fmaf(T1[pr + P * (j + d1 * l)], g1[j], ul[l]);
+        ua[l] = fmaf(T1a[pr + P * (j + d1 * l)], fabsf(g1[j]), ua[l]);
+      }
+  }
+  for (int b3 = 0; b3 < mb3; ++b3) {
+    const float* g2 = G2f + d2 * b3;
+    float x32 = 0.f, s32 = 0.f;
+#pragma unroll
+    for (int l = 0; l < D2; ++l)
+      if (D2 != 16 || l < d2) {
+        x32 = fmaf(ul[l], g2[l], x32);
+        s32 = fmaf(ua[l], fabsf(g2[l]), s32);
+      }
+    if (fabsf(x32) + kFilterMargin * s32 > tcf) {
+      const double x = sg * exact_x(3, d0, d1, d2, wc, g0d, g1d, G2d + d2 * b3);
+      expand_emit(p, x, tc, crow, keybase, idx3 + b3 * sa3, keys, vals, cap_mask, counters);
+    }
+  }
+}
+
 // Persistent CTAs take kept (ket, term) jobs from a counter.  Per job the W block and the
 // TDM columns for all bra states are staged in shared memory (double and float copies) and,
 // for three- and four-cluster terms, W is contracted with the first remaining cluster's
@@ -354,31 +391,23 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
               expand_emit(p, x, tc, crow, keybase, idx3, keys, vals, cap_mask, counters);
             }
           } else {
-            const float* G2f = xf + t.g32[2];
-            float ul[16], ua[16];
-#pragma unroll
-            for (int l = 0; l < 16; ++l) {
-              ul[l] = 0.f;
-              ua[l] = 0.f;
-              if (l < d2)
-                for (int j = 0; j < d1; ++j) {
-                  ul[l] = fmaf(T1[pr + P * (j + d1 * l)], g1[j], ul[l]);
-                  ua[l] = fmaf(T1a[pr + P * (j + d1 * l)], fabsf(g1[j]), ua[l]);
-                }
-            }
-            for (int b3 = 0; b3 < mb[3]; ++b3) {
-              const float* g2 = G2f + d2 * b3;
-              float x32 = 0.f, s32 = 0.f;
-#pragma unroll
-              for (int l = 0; l < 16; ++l)
-                if (l < d2) {
-                  x32 = fmaf(ul[l], g2[l], x32);
-                  s32 = fmaf(ua[l], fabsf(g2[l]), s32);
-                }
-              if (fabsf(x32) + kFilterMargin * s32 > tcf) {
-                const double x = sg * exact_x(3, d0, d1, d2, wc, g0d, g1d, xs + t.g64[2] + d2 * b3);
-                expand_emit(p, x, tc, crow, keybase, idx3 + b3 * sa[3], keys, vals, cap_mask, counters);
-              }
+            switch (d2) {
+              case 1: unit4<1>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 2: unit4<2>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 3: unit4<3>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 4: unit4<4>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 5: unit4<5>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 6: unit4<6>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              case 8: unit4<8>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                               xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
+              default: unit4<16>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+                                 xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters, d2); break;
             }
           }
         }
