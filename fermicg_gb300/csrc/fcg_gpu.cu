@@ -1074,6 +1074,50 @@ int fcg_sigma_closed(fcg_ctx* ctx, int R, const double* c, double* sigma, int pr
   return FCG_OK;
 }
 
+int fcg_expectation(fcg_ctx* ctx, int R, const double* c, double* e, int precision) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(c && e, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  FCG_REQUIRE(R >= 1 && R <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
+  const int64_t n = ctx->n_cfg;
+  std::vector<double> sig(size_t(n) * R);
+  const int rc = fcg_sigma_closed(ctx, R, c, sig.data(), precision);
+  if (rc) return rc;
+  for (int r = 0; r < R; ++r) {
+    double acc = 0.0;
+    for (int64_t i = 0; i < n; ++i) acc += c[i + n * r] * sig[size_t(i) + size_t(n) * r];
+    e[r] = acc;
+  }
+  return FCG_OK;
+}
+
+int fcg_build_full_h(fcg_ctx* ctx, double* H) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(H, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  const int64_t n = ctx->n_cfg;
+  FCG_REQUIRE(n <= 65536, FCG_ELIMIT, "fcg_build_full_h is for spaces of at most 65536 configurations");
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  constexpr int kCols = 16;
+  FCG_CUDA(ctx->d_in64.alloc(size_t(n) * kCols));
+  FCG_CUDA(ctx->d_out64.alloc(size_t(n) * kCols));
+  for (int64_t j0 = 0; j0 < n; j0 += kCols) {
+    const int R = int(std::min<int64_t>(kCols, n - j0));
+    // identity columns j0 .. j0+R-1 (column-major n x R)
+    FCG_CUDA(cudaMemsetAsync(ctx->d_in64.p, 0, sizeof(double) * size_t(n) * R, ctx->stream));
+    const double one = 1.0;
+    for (int r = 0; r < R; ++r)
+      FCG_CUDA(cudaMemcpyAsync(ctx->d_in64.p + (j0 + r) + n * r, &one, sizeof(double), cudaMemcpyHostToDevice,
+                               ctx->stream));
+    const int rc = sigma_device_impl(ctx, R, ctx->d_in64.p, ctx->d_out64.p, FCG_FP64);
+    if (rc) return rc;
+    FCG_CUDA(cudaMemcpyAsync(H + n * j0, ctx->d_out64.p, sizeof(double) * size_t(n) * R, cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  }
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return FCG_OK;
+}
+
 int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");

@@ -50,6 +50,8 @@ SIGNATURES = {
     "fcg_bst_sigma_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_triples": (_I, [_P, _P]),
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
+    "fcg_expectation": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_build_full_h": (_I, [_P, _P]),
 }
 
 
@@ -178,6 +180,22 @@ class GpuSigma:
         """Allocation-free device-pointer sigma (fixed 16 MiB scratch; n_cfg * R <= 2**20)."""
         self._check(self.L.fcg_sigma_closed_noalloc(self.h, R, ctypes.c_void_p(d_c_ptr), ctypes.c_void_p(d_sigma_ptr),
                                                     PRECISION[precision]), "fcg_sigma_closed_noalloc")
+
+    def expectation(self, coeffs, precision="fp64"):
+        """compute_expectation_value_parallel: c_r^T H c_r per root (coeffs (n_cfg, R))."""
+        c = np.asfortranarray(coeffs, dtype=np.float64)
+        n, R = c.shape
+        if n != self.n_cfg:
+            raise ValueError("coefficient rows do not match the state")
+        e = np.zeros(R)
+        self._check(self.L.fcg_expectation(self.h, R, _ptr(c), _ptr(e), PRECISION[precision]), "fcg_expectation")
+        return e
+
+    def build_full_h(self):
+        """build_full_H_parallel on the state: dense (n_cfg, n_cfg) float64."""
+        H = np.zeros((self.n_cfg, self.n_cfg), order="F")
+        self._check(self.L.fcg_build_full_h(self.h, _ptr(H)), "fcg_build_full_h")
+        return H
 
     def diagonal(self, op: str | None = None):
         """compute_diagonal: op None = all zero-transfer terms; else an op string ("Hcmf", "H")."""

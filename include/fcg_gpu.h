@@ -107,6 +107,16 @@ int fcg_sigma_closed(fcg_ctx* ctx, int R, const double* c, double* sigma, int pr
  * on the context's device; runs on the context stream and synchronises. */
 int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
 
+/* compute_expectation_value_parallel (src/tpsci_outer.jl:601-687): e[r] = c_r^T H c_r for
+ * the state's configurations (c: host, column-major n_cfg x R; not normalised, as in the
+ * reference). */
+int fcg_expectation(fcg_ctx* ctx, int R, const double* c, double* e, int precision);
+
+/* build_full_H_parallel (src/tpsci_outer.jl:59-150) with the same state on both sides:
+ * the dense n_cfg x n_cfg H (host, column-major), built from closed sigmas of identity
+ * blocks in float64; n_cfg <= 65536. */
+int fcg_build_full_h(fcg_ctx* ctx, double* H);
+
 /* compute_diagonal (src/tpsci_outer.jl:694-715) when op_id < 0 (all zero-transfer
  * terms, bra == ket), else compute_diagonal! with that op string
  * (src/tpsci_outer.jl:735-757, e.g. op_id 23 = "Hcmf").  hd: host, n_cfg. */
