@@ -191,7 +191,8 @@ struct DavidsonWork {
     FCG_CUDA(cudaMemcpyAsync(small.p, Y.data(), sizeof(double) * a * b, cudaMemcpyHostToDevice, ctx->stream));
     update_kernel<<<unsigned((n + 255) / 256), 256, 0, ctx->stream>>>(A, n, a, small.p, b, C, n, n, mode);
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    // no wait: a pageable host-to-device copy has staged Y when it returns, and every later
+    // use of C runs behind this kernel on the same stream
     return FCG_OK;
   }
 };
@@ -220,7 +221,6 @@ int orthonormalize_block(DavidsonWork& W, double* Tp, int b, const double* Vp, i
     FCG_CUDA(cudaMemcpyAsync(W.small.p, D.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
     scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
     return FCG_OK;
   };
   auto pack = [&](const std::vector<int>& keep) -> int {
@@ -275,7 +275,6 @@ int orthonormalize_block(DavidsonWork& W, double* Tp, int b, const double* Vp, i
     FCG_CUDA(cudaMemcpyAsync(W.small.p, Ri.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
     scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (nv > 0) {  // restore orthogonality to V lost in the rescaling
       if ((rc = W.gram(Vp, nv, Tp, m, S))) return rc;
       if ((rc = W.update(Vp, nv, S, m, Tp, 2))) return rc;
