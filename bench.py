@@ -95,7 +95,7 @@ def cpu_reference(po, pt, f, c, v, budget_s, threads):
     return done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full build"
 
 
-def serving_benchmark(n_req=60, rate=200.0, seed=7):
+def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16):
     """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
     per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
     stream.  Returns p50/p99 latency and solves/s per precision."""
@@ -131,7 +131,7 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7):
             po, pt, f, c, guess = pools[kinds[i]][picks[i]]
             reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
                                 shape=shapes[kinds[i]][0]))
-        srv = SolveServer(slots=4)
+        srv = SolveServer(slots=slots)
         res = srv.run(reqs)
         srv.close()
         summ = latency_summary(res)
@@ -140,6 +140,7 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7):
         out["mixed" if prec == "fp32" else "fp64"] = summ
     # same stream, same results: energies of mixed vs fp64 per request
     out["requests"] = n_req
+    out["slots"] = slots
     out["arrival_rate_per_s"] = rate
     out["mix"] = {sh[0]: sh[4] for sh in shapes}
     return out
