@@ -6,288 +6,494 @@
 // the reference tree; this is a standard block Davidson written from its call sites.
 //
 // Everything of size n stays on the GPU in float64: the subspace V and H V (column-major,
-// one column per vector), Gram matrices V^T W, Ritz vectors X = V Y and H X = (HV) Y,
-// residuals r = HX - X theta, the diagonal preconditioner t = r / (theta - H_dd), and
-// classical Gram-Schmidt applied twice.  Only the k x k Rayleigh-Ritz problem (k <=
-// max_ss_vecs * R) goes to the host (cyclic Jacobi).
+// one column per vector), the Ritz vectors X = V Y, the residuals r = (HV) Y - X theta and
+// the preconditioned corrections t = r / (theta - H_dd), written straight behind V.  The
+// host keeps the projected matrix V^T H V (extended by one block of columns per
+// iteration) and solves the small problems: the Rayleigh-Ritz eigenproblem and the Cholesky
+// factors of the new directions' Gram matrices (small_dense.h).
+//
+// One iteration waits for the device at most three times: for the new columns of V^T H V,
+// for the residual norms together with [V T]^T T, and for the Gram matrix after the first
+// projection of T.  The projections (classical Gram-Schmidt, twice) are fused with the
+// unit scaling and the Cholesky QR of the new block into one kernel each; a second Cholesky
+// QR pass runs only when the block's Gram matrix is ill-conditioned.  All partial sums are
+// reduced in a fixed order, so a solve gives the same bits whatever runs beside it.
+//
+// Restarts keep the current and the previous Ritz vectors (GD+k, "locally optimal"
+// restart; Stathopoulos & Saad, "Restarting techniques for the (Jacobi-)Davidson symmetric
+// eigenvalue methods", ETNA 7, 1998): the kept basis V Q and H V Q are formed on the
+// device from an orthonormal Q of the two coefficient blocks, the projected matrix as
+// Q^T (V^T H V) Q on the host, so a restart costs no sigma build.
 //
 // Precision: FCG_FP64 runs every sigma in float64.  FCG_FP32 ("mixed") runs the sigma
 // builds in float32 until the residual norms reach max(tol, 1e-5), then restarts from
 // the Ritz vectors with float64 sigma builds (the refinement) until tol.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "fcg_ctx.cuh"
+#include "small_dense.h"
 
 using namespace fcg;
 
 namespace {
 
-// out[i + a*j] = sum_rows A[row + lda*i] * B[row + ldb*j]  (out zeroed by the caller)
-__global__ void gram_kernel(const double* __restrict__ A, int64_t lda, int a, const double* __restrict__ B,
-                            int64_t ldb, int b, int64_t n, double* __restrict__ out) {
-  extern __shared__ double red[];
-  const int64_t rows_per = (n + gridDim.x - 1) / gridDim.x;
-  const int64_t r0 = int64_t(blockIdx.x) * rows_per;
-  const int64_t r1 = (r0 + rows_per < n) ? r0 + rows_per : n;
-  for (int p = 0; p < a * b; ++p) {
-    const int i = p % a, j = p / a;
-    double s = 0.0;
-    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) s = fma(A[r + lda * i], B[r + ldb * j], s);
-    // block reduction
-    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      double t = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.0;
-      for (int off = 16; off > 0; off >>= 1) t += __shfl_down_sync(0xffffffffu, t, off);
-      if (threadIdx.x == 0) atomicAdd(out + p, t);
+constexpr int kDavThreads = 256;
+constexpr int kGramWarps = 8;
+constexpr int kMaxB = 16;         // columns of the right-hand block of a Gram product (<= R)
+constexpr int kMaxRowBlocks = 128;  // row blocks of a Gram product (partial sums per output)
+constexpr int kGramRows = 64;       // rows per row block while the block count allows
+
+// out[i + a*j] = sum_r A[r + lda*i] * B[r + ldb*j] for i < a, j < b <= BM.  The kernels of
+// this file are compiled for block widths BM = 1, 2, 4, 8, 16 and launched with the smallest
+// that fits: unrolled loops over unused columns would still issue their FP64 instructions.
+// Grid: x = row blocks, y = groups of 32 columns of A; a lane owns one column of A, each warp
+// a contiguous slice of the block's rows.  Each block writes its partial sums to
+// part[blk][i + a*j]; the last block of a column group to finish (counted in
+// counters[blockIdx.y], which it resets) adds the group's partials in row-block order, so
+// the result does not depend on the order in which blocks run.
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) gram_kernel(const double* __restrict__ A, int64_t lda, int a,
+                                                           const double* __restrict__ B, int64_t ldb, int b, int64_t n,
+                                                           int64_t rows_per_block, double* __restrict__ part,
+                                                           double* __restrict__ out, unsigned* __restrict__ counters) {
+  __shared__ double red[kGramWarps][BM][32];
+  __shared__ unsigned ticket;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int i = blockIdx.y * 32 + lane;
+  const int64_t r0 = int64_t(blockIdx.x) * rows_per_block;
+  const int64_t r1 = r0 + rows_per_block < n ? r0 + rows_per_block : n;
+  const int64_t slice = (rows_per_block + kGramWarps - 1) / kGramWarps;
+  const int64_t s0 = r0 + warp * slice;
+  const int64_t s1 = s0 + slice < r1 ? s0 + slice : r1;
+  double acc[BM];
+#pragma unroll
+  for (int j = 0; j < BM; ++j) acc[j] = 0.0;
+  if (i < a) {
+    const double* Ai = A + lda * i;
+    int64_t r = s0;
+    for (; r + 8 <= s1; r += 8) {  // eight rows per step: independent loads in flight
+      double x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = Ai[r + u];
+#pragma unroll
+      for (int j = 0; j < BM; ++j)
+        if (j < b) {
+          const double* Bj = B + ldb * j + r;
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[j] = fma(x[u], Bj[u], acc[j]);
+        }
     }
-    __syncthreads();
+    for (; r < s1; ++r) {
+      const double x = Ai[r];
+#pragma unroll
+      for (int j = 0; j < BM; ++j)
+        if (j < b) acc[j] = fma(x, B[r + ldb * j], acc[j]);
+    }
   }
+#pragma unroll
+  for (int j = 0; j < BM; ++j)
+    if (j < b) red[warp][j][lane] = acc[j];
+  __syncthreads();
+  const int64_t P = int64_t(a) * b;
+  for (int t = threadIdx.x; t < b * 32; t += blockDim.x) {
+    const int j = t >> 5, l = t & 31;
+    const int col = blockIdx.y * 32 + l;
+    double s = 0.0;
+    for (int w = 0; w < kGramWarps; ++w) s += red[w][j][l];
+    if (col < a) part[int64_t(blockIdx.x) * P + col + int64_t(a) * j] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(counters + blockIdx.y, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  for (int t = threadIdx.x; t < b * 32; t += blockDim.x) {
+    const int j = t >> 5, l = t & 31;
+    const int col = blockIdx.y * 32 + l;
+    if (col >= a) continue;
+    const int64_t p = col + int64_t(a) * j;
+    double s = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) s += __ldcg(part + int64_t(k) * P + p);
+    out[p] = s;
+  }
+  if (threadIdx.x == 0) counters[blockIdx.y] = 0u;
 }
 
-// C[:, j] (+)= sum_i A[:, i] * Y[i + a*j]   (ldc columns); beta = 0 overwrites, 1 accumulates, -1 subtracts
+// C[:, j] = sum_i A[:, i] * Y[i + a*j] for j < b (C and A must not overlap)
 __global__ void update_kernel(const double* __restrict__ A, int64_t lda, int a, const double* __restrict__ Y, int b,
-                              double* __restrict__ C, int64_t ldc, int64_t n, int mode) {
+                              double* __restrict__ C, int64_t ldc, int64_t n) {
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= n) return;
   for (int j = 0; j < b; ++j) {
     double s = 0.0;
-    for (int i = 0; i < a; ++i) s = fma(A[r + lda * i], Y[i + a * j], s);
-    double* c = C + r + ldc * j;
-    if (mode == 0)
-      *c = s;
-    else if (mode == 1)
-      *c += s;
-    else
-      *c -= s;
+    for (int i = 0; i < a; ++i) s = fma(A[r + lda * i], Y[i + int64_t(a) * j], s);
+    C[r + ldc * j] = s;
   }
 }
 
-// residual r_j = HX_j - theta_j X_j, its squared norm, and the preconditioned
-// correction t_j = r_j / (theta_j - Hd) (denominator kept away from zero)
-__global__ void residual_kernel(const double* __restrict__ X, const double* __restrict__ HX,
-                                const double* __restrict__ theta, const double* __restrict__ hd, int R, int64_t n,
-                                double* __restrict__ T, double* __restrict__ rnorm2, int precond) {
+// Ritz vectors and corrections for R roots: per row r,
+//   x_j = sum_i V[r, i] Y[i, j],  hx_j = sum_i AV[r, i] Y[i, j],  res_j = hx_j - theta_j x_j,
+//   X[r, j] = x_j,  T[r, j] = res_j / (theta_j - hd[r])  (res_j when !precond; the denominator
+//   is kept at least 1e-6 away from zero), and rn_out[j] = sum_r res_j^2 (per-block partial
+//   sums in rn_part, added in block order by the last block to finish).
+// Y (nv x R, column-major) and theta are staged in shared memory.
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double* __restrict__ V,
+                                                                    const double* __restrict__ AV, int64_t ld, int nv,
+                                                                    const double* __restrict__ Y,
+                                                                    const double* __restrict__ theta,
+                                                                    const double* __restrict__ hd, int R, int64_t n,
+                                                                    double* __restrict__ X, double* __restrict__ T,
+                                                                    int precond, double* __restrict__ rn_part,
+                                                                    double* __restrict__ rn_out,
+                                                                    unsigned* __restrict__ counter) {
+  extern __shared__ double sm[];
+  double* sY = sm;              // nv * R
+  double* sth = sm + nv * R;    // R
+  __shared__ double red[kDavThreads / 32][BM];
+  for (int t = threadIdx.x; t < nv * R; t += blockDim.x) sY[t] = Y[t];
+  for (int t = threadIdx.x; t < R; t += blockDim.x) sth[t] = theta[t];
+  __syncthreads();
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  for (int j = 0; j < R; ++j) {
+  double x[BM], hx[BM];
+#pragma unroll
+  for (int j = 0; j < BM; ++j) x[j] = hx[j] = 0.0;
+  if (r < n) {
+    for (int i0 = 0; i0 < nv; i0 += 8) {  // eight columns' loads in flight before their use
+      double v[8], av[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const bool in = i0 + u < nv;
+        v[u] = in ? V[r + ld * (i0 + u)] : 0.0;
+        av[u] = in ? AV[r + ld * (i0 + u)] : 0.0;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (i0 + u >= nv) break;
+        const double* y = sY + i0 + u;
+#pragma unroll
+        for (int j = 0; j < BM; ++j)
+          if (j < R) {
+            x[j] = fma(v[u], y[nv * j], x[j]);
+            hx[j] = fma(av[u], y[nv * j], hx[j]);
+          }
+      }
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int j = 0; j < BM; ++j) {
+    if (j >= R) break;
     double res = 0.0;
     if (r < n) {
-      res = HX[r + n * j] - theta[j] * X[r + n * j];
-      double d = precond ? theta[j] - hd[r] : 1.0;
+      res = hx[j] - sth[j] * x[j];
+      double d = precond ? sth[j] - hd[r] : 1.0;
       if (fabs(d) < 1e-6) d = d < 0 ? -1e-6 : 1e-6;
-      T[r + n * j] = res / d;
+      X[r + n * j] = x[j];
+      T[r + ld * j] = res / d;
     }
     double s = res * res;
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    if ((threadIdx.x & 31) == 0) atomicAdd(rnorm2 + j, s);
+    if (lane == 0) red[warp][j] = s;
   }
+  __syncthreads();
+  if (threadIdx.x < R) {
+    double s = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
+    rn_part[int64_t(blockIdx.x) * R + threadIdx.x] = s;
+  }
+  // the last block to finish adds the blocks' partial sums in block order
+  __shared__ unsigned ticket;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  if (threadIdx.x < R) {
+    double s = 0.0;
+    for (unsigned k = 0; k < gridDim.x; ++k) s += __ldcg(rn_part + int64_t(k) * R + threadIdx.x);
+    rn_out[threadIdx.x] = s;
+  }
+  if (threadIdx.x == 0) *counter = 0u;
 }
 
-__global__ void scale_cols_kernel(double* __restrict__ A, int64_t lda, const double* __restrict__ L, int b,
-                                  int64_t n, double* __restrict__ tmp) {
-  // A[:, 0..b) <- A[:, 0..b) * L  (L upper-triangular b x b, column-major); tmp: n x b scratch
+// In place on the new block T = V[:, nv : nv + kt] (leading dimension ld):
+//   T[:, j] <- sum_{i < kt} T[:, i] M[i + kt*j] - sum_{i < nv} V[:, i] P[i + nv*j],  j < mo.
+// A thread owns a row: it reads the row's T entries before writing any (kt, mo <= BM).
+// M (kt x mo) and P (nv x mo) are staged in shared memory; P may be null (no projection).
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) combine_kernel(double* __restrict__ V, int64_t ld, int nv, int kt,
+                                                              const double* __restrict__ M,
+                                                              const double* __restrict__ P, int mo, int64_t n) {
+  extern __shared__ double sm[];
+  double* sM = sm;            // kt * mo
+  double* sP = sm + kt * mo;  // nv * mo
+  for (int t = threadIdx.x; t < kt * mo; t += blockDim.x) sM[t] = M[t];
+  if (P)
+    for (int t = threadIdx.x; t < nv * mo; t += blockDim.x) sP[t] = P[t];
+  __syncthreads();
   const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  for (int j = 0; j < b; ++j) {
+  double* T = V + ld * nv;
+  double t_in[BM], out[BM];
+#pragma unroll
+  for (int i = 0; i < BM; ++i) t_in[i] = i < kt ? T[r + ld * i] : 0.0;
+#pragma unroll
+  for (int j = 0; j < BM; ++j) {
     double s = 0.0;
-    for (int i = 0; i <= j; ++i) s = fma(A[r + lda * i], L[i + b * j], s);
-    tmp[r + n * j] = s;
+    if (j < mo) {
+#pragma unroll
+      for (int i = 0; i < BM; ++i)
+        if (i < kt) s = fma(t_in[i], sM[i + kt * j], s);
+    }
+    out[j] = s;
   }
-  for (int j = 0; j < b; ++j) A[r + lda * j] = tmp[r + n * j];
+  if (P) {
+    for (int i0 = 0; i0 < nv; i0 += 8) {  // eight columns' loads in flight before their use
+      double v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = i0 + u < nv ? V[r + ld * (i0 + u)] : 0.0;
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        if (i0 + u >= nv) break;
+        const double* pp = sP + i0 + u;
+#pragma unroll
+        for (int j = 0; j < BM; ++j)
+          if (j < mo) out[j] = fma(-v[u], pp[nv * j], out[j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < BM; ++j)
+    if (j < mo) T[r + ld * j] = out[j];
 }
 
-// cyclic Jacobi eigen-decomposition of a symmetric k x k matrix (column-major, in place);
-// eigenvalues ascending in w, eigenvectors in the columns of Vv
-void jacobi_eigh(int k, std::vector<double>& A, std::vector<double>& w, std::vector<double>& Vv) {
-  Vv.assign(size_t(k) * k, 0.0);
-  for (int i = 0; i < k; ++i) Vv[i + k * i] = 1.0;
-  for (int sweep = 0; sweep < 100; ++sweep) {
-    double off = 0.0, tot = 0.0;
-    for (int j = 0; j < k; ++j)
-      for (int i = 0; i < k; ++i) {
-        tot += A[i + k * j] * A[i + k * j];
-        if (i != j) off += A[i + k * j] * A[i + k * j];
-      }
-    if (off <= 1e-30 * std::max(tot, 1e-300)) break;
-    for (int p = 0; p < k - 1; ++p)
-      for (int q = p + 1; q < k; ++q) {
-        const double apq = A[p + k * q];
-        if (std::fabs(apq) < 1e-300) continue;
-        const double app = A[p + k * p], aqq = A[q + k * q];
-        const double tau = (aqq - app) / (2.0 * apq);
-        const double t = (tau >= 0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
-        const double c = 1.0 / std::sqrt(1.0 + t * t), s = t * c;
-        for (int r = 0; r < k; ++r) {  // columns p, q
-          const double arp = A[r + k * p], arq = A[r + k * q];
-          A[r + k * p] = c * arp - s * arq;
-          A[r + k * q] = s * arp + c * arq;
-        }
-        for (int r = 0; r < k; ++r) {  // rows p, q
-          const double apr = A[p + k * r], aqr = A[q + k * r];
-          A[p + k * r] = c * apr - s * aqr;
-          A[q + k * r] = s * apr + c * aqr;
-        }
-        for (int r = 0; r < k; ++r) {
-          const double vrp = Vv[r + k * p], vrq = Vv[r + k * q];
-          Vv[r + k * p] = c * vrp - s * vrq;
-          Vv[r + k * q] = s * vrp + c * vrq;
-        }
-      }
+// the smallest compiled block width (1, 2, 4, 8, 16) that holds w columns
+inline int width_class(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : w <= 8 ? 8 : 16; }
+
+#define FCG_WIDTH_SWITCH(w, KERNEL, LAUNCH, ...)       \
+  switch (width_class(w)) {                            \
+    case 1: KERNEL<1><<<LAUNCH>>>(__VA_ARGS__); break; \
+    case 2: KERNEL<2><<<LAUNCH>>>(__VA_ARGS__); break; \
+    case 4: KERNEL<4><<<LAUNCH>>>(__VA_ARGS__); break; \
+    case 8: KERNEL<8><<<LAUNCH>>>(__VA_ARGS__); break; \
+    default: KERNEL<16><<<LAUNCH>>>(__VA_ARGS__); break; \
   }
-  std::vector<int> idx(k);
-  for (int i = 0; i < k; ++i) idx[i] = i;
-  std::sort(idx.begin(), idx.end(), [&](int a, int b) { return A[a + k * a] < A[b + k * b]; });
-  std::vector<double> Vs(size_t(k) * k);
-  w.assign(k, 0.0);
-  for (int j = 0; j < k; ++j) {
-    w[j] = A[idx[j] + k * idx[j]];
-    for (int i = 0; i < k; ++i) Vs[i + k * j] = Vv[i + k * idx[j]];
-  }
-  Vv.swap(Vs);
-}
 
 }  // namespace
 
-#define FCG_CUDA(call)                                                               \
-  do {                                                                               \
-    cudaError_t e_ = (call);                                                         \
-    if (e_ != cudaSuccess) {                                                         \
-      ctx->err = std::string(#call) + ": " + cudaGetErrorString(e_);                 \
-      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;               \
-    }                                                                                \
-  } while (0)
-
-#define FCG_REQUIRE(cond, code, msg) \
-  do {                               \
-    if (!(cond)) {                   \
-      ctx->err = (msg);              \
-      return (code);                 \
-    }                                \
-  } while (0)
+extern "C" int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd);
 
 namespace {
 
 struct DavidsonWork {
-  fcg_ctx* ctx;
-  int64_t n;
-  int kmax;
-  DevBuf<double> V, AV, X, HX, T, tmp, small, theta, hd, rn;
-  int gram_grid;
+  fcg_ctx* ctx = nullptr;
+  int64_t n = 0;
+  int R = 0, kmax = 0, kcap = 0;  // kcap = kmax + R columns of V and AV
+  int row_blocks = 1;             // Gram products: row blocks, rows per block
+  int64_t rows_per_block = 1;
+  int res_blocks = 1;             // residual kernel blocks
+  DevBuf<double> V, AV, X, tmp, hd, part, rn_part, d_out, d_up;
+  DevBuf<unsigned> counters;  // last-block tickets: [0, ngroups) Gram column groups, [ngroups] residual
+  int ngroups = 1;
+  PinnedBuf<double> h_out, h_up;
+  size_t up_used = 0, up_sent = 0;
 
-  int gram(const double* A, int a, const double* B, int b, std::vector<double>& out) {
+  // Stage `count` doubles in the pinned upload area and return where they will be on the
+  // device once flush() has queued the copy.  The area is reused only after the next fetch().
+  int upload(const double* src, size_t count, const double** dptr) {
     fcg_ctx* ctx = this->ctx;
-    FCG_CUDA(cudaMemsetAsync(small.p, 0, sizeof(double) * a * b, ctx->stream));
-    gram_kernel<<<gram_grid, 256, 8 * sizeof(double), ctx->stream>>>(A, n, a, B, n, b, n, small.p);
+    const size_t off = (up_used + 3) & ~size_t(3);
+    FCG_REQUIRE(off + count <= h_up.n, FCG_ELIMIT, "Davidson: staging area exhausted");
+    if (count) std::memcpy(h_up.p + off, src, count * sizeof(double));
+    up_used = off + count;
+    *dptr = d_up.p + off;
+    return FCG_OK;
+  }
+  // one host-to-device copy of everything staged since the last flush
+  int flush() {
+    fcg_ctx* ctx = this->ctx;
+    if (up_used > up_sent)
+      FCG_CUDA(cudaMemcpyAsync(d_up.p + up_sent, h_up.p + up_sent, (up_used - up_sent) * sizeof(double),
+                               cudaMemcpyHostToDevice, ctx->stream));
+    up_sent = up_used;
+    return FCG_OK;
+  }
+  // out[0 : a*b) = A^T B on the device (A: a columns, B: b columns, leading dimension n)
+  int gram(const double* A, int a, const double* B, int b, double* out) {
+    fcg_ctx* ctx = this->ctx;
+    FCG_REQUIRE(a >= 1 && a <= kcap && b >= 1 && b <= R, FCG_ELIMIT, "Davidson: Gram block out of range");
+    const dim3 grid(unsigned(row_blocks), unsigned((a + 31) / 32));
+#define FCG_GRAM_LAUNCH grid, kDavThreads, 0, ctx->stream
+    FCG_WIDTH_SWITCH(b, gram_kernel, FCG_GRAM_LAUNCH, A, n, a, B, n, b, n, rows_per_block, part.p, out, counters.p)
+#undef FCG_GRAM_LAUNCH
     FCG_CUDA(cudaGetLastError());
-    out.resize(size_t(a) * b);
-    FCG_CUDA(cudaMemcpyAsync(out.data(), small.p, sizeof(double) * a * b, cudaMemcpyDeviceToHost, ctx->stream));
+    return FCG_OK;
+  }
+  // wait for the stream; h_out[0 : count) = d_out[0 : count)
+  int fetch(size_t count) {
+    fcg_ctx* ctx = this->ctx;
+    FCG_CUDA(cudaMemcpyAsync(h_out.p, d_out.p, count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    up_used = up_sent = 0;
     return FCG_OK;
   }
-  // C (+/-)= A * Y with Y a host a x b matrix
-  int update(const double* A, int a, const std::vector<double>& Y, int b, double* C, int mode) {
+  // T = V[:, nv : nv + kt] <- T M - V[:, :nv] P  (M: kt x mo, P: nv x mo or null)
+  int combine(int nv, int kt, const std::vector<double>& M, const std::vector<double>* P, int mo) {
     fcg_ctx* ctx = this->ctx;
-    FCG_CUDA(cudaMemcpyAsync(small.p, Y.data(), sizeof(double) * a * b, cudaMemcpyHostToDevice, ctx->stream));
-    update_kernel<<<unsigned((n + 255) / 256), 256, 0, ctx->stream>>>(A, n, a, small.p, b, C, n, n, mode);
+    FCG_REQUIRE(kt >= 1 && kt <= kMaxB && mo >= 1 && mo <= kMaxB, FCG_ELIMIT, "Davidson: block out of range");
+    const double *dM = nullptr, *dP = nullptr;
+    int rc;
+    if ((rc = upload(M.data(), size_t(kt) * mo, &dM))) return rc;
+    const bool proj = P && nv > 0;
+    if (proj && (rc = upload(P->data(), size_t(nv) * mo, &dP))) return rc;
+    if ((rc = flush())) return rc;
+    const size_t smem = sizeof(double) * (size_t(kt) * mo + (proj ? size_t(nv) * mo : 0));
+    const unsigned blocks = unsigned((n + kDavThreads - 1) / kDavThreads);
+#define FCG_COMBINE_LAUNCH blocks, kDavThreads, smem, ctx->stream
+    FCG_WIDTH_SWITCH(std::max(kt, mo), combine_kernel, FCG_COMBINE_LAUNCH, V.p, n, nv, kt, dM, dP, mo, n)
+#undef FCG_COMBINE_LAUNCH
     FCG_CUDA(cudaGetLastError());
-    // no wait: a pageable host-to-device copy has staged Y when it returns, and every later
-    // use of C runs behind this kernel on the same stream
     return FCG_OK;
   }
+  int orthonormalize(int nv, int nt, std::vector<double> G0, double drop, int* kept);
+  int start_block(int nt, double drop, int* kept);
 };
 
-// Orthonormalise columns [0, b) of T against V[:, 0..nv) and among themselves; the kept
-// columns are packed to the front and their count returned in *kept.  Every column is
-// first scaled to unit norm, then projected out of V (classical Gram-Schmidt, twice); a
-// direction is dropped when less than `drop` of it survives the projection (it lies in
-// the subspace already, up to rounding).  The survivors are orthonormalised by Cholesky
-// QR, twice.
-int orthonormalize_block(DavidsonWork& W, double* Tp, int b, const double* Vp, int nv, double drop, int* kept) {
-  fcg_ctx* ctx = W.ctx;
-  std::vector<double> S;
+// Orthonormalise the new directions T = V[:, nv : nv + nt] against V[:, :nv] and among
+// themselves, given G0 = [V T]^T T ((nv + nt) x nt, column-major).  Every direction is first
+// scaled to unit norm and projected out of V (classical Gram-Schmidt, twice); a direction is
+// dropped when less than `drop` of it survives (it lies in the subspace already, up to
+// rounding).  The survivors are orthonormalised by Cholesky QR (stopping at the first
+// dependent column), twice when their Gram matrix has a condition number above 1e4.  The
+// kept directions end up in V[:, nv : nv + *kept].
+int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double drop, int* kept) {
+  *kept = 0;
+  const int ld0 = nv + nt;
   int rc;
-  auto scale_to_unit = [&](int m, std::vector<int>& keep, double floor2) -> int {
-    if ((rc = W.gram(Tp, m, Tp, m, S))) return rc;
-    keep.clear();
-    std::vector<double> D(size_t(m) * m, 0.0);
-    for (int j = 0; j < m; ++j) {
-      const double n2 = S[j + m * j];
-      if (std::isfinite(n2) && n2 > floor2) {
-        D[j + m * j] = 1.0 / std::sqrt(n2);
-        keep.push_back(j);
-      }
-    }
-    FCG_CUDA(cudaMemcpyAsync(W.small.p, D.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
-    scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
-    FCG_CUDA(cudaGetLastError());
-    return FCG_OK;
-  };
-  auto pack = [&](const std::vector<int>& keep) -> int {
-    for (size_t q = 0; q < keep.size(); ++q)
-      if (int(q) != keep[q])
-        FCG_CUDA(cudaMemcpyAsync(Tp + W.n * q, Tp + W.n * keep[q], sizeof(double) * W.n, cudaMemcpyDeviceToDevice,
-                                 ctx->stream));
-    return FCG_OK;
-  };
+  // 1. unit scaling (and the first projection)
   std::vector<int> keep;
-  if ((rc = scale_to_unit(b, keep, 1e-300))) return rc;
-  if ((rc = pack(keep))) return rc;
-  int m = int(keep.size());
-  if (m > 0 && nv > 0) {
-    for (int pass = 0; pass < 2; ++pass) {
-      if ((rc = W.gram(Vp, nv, Tp, m, S))) return rc;
-      if ((rc = W.update(Vp, nv, S, m, Tp, 2))) return rc;
-    }
-    // what survived the projection, relative to the unit input
-    if ((rc = scale_to_unit(m, keep, drop * drop))) return rc;
-    if ((rc = pack(keep))) return rc;
-    m = int(keep.size());
+  for (int j = 0; j < nt; ++j) {
+    const double g = G0[nv + j + size_t(ld0) * j];
+    if (std::isfinite(g) && g > 1e-300) keep.push_back(j);
   }
-  for (int it = 0; it < 2 && m > 0; ++it) {
-    if ((rc = W.gram(Tp, m, Tp, m, S))) return rc;
-    // Cholesky S = R^T R, stopping at the first column that is dependent on the previous ones
-    std::vector<double> Lc(size_t(m) * m, 0.0);
-    int good = 0;
-    for (int j = 0; j < m; ++j) {
-      double d = S[j + m * j];
-      for (int p = 0; p < j; ++p) d -= Lc[p + m * j] * Lc[p + m * j];
-      if (!(d > drop * drop * S[j + m * j])) break;
-      Lc[j + m * j] = std::sqrt(d);
-      for (int q = j + 1; q < m; ++q) {
-        double v = S[j + m * q];
-        for (int p = 0; p < j; ++p) v -= Lc[p + m * j] * Lc[p + m * q];
-        Lc[j + m * q] = v / Lc[j + m * j];
-      }
-      ++good;
-    }
-    m = good;
-    if (m == 0) break;
-    std::vector<double> Ri(size_t(m) * m, 0.0);  // inverse of the leading m x m block of R
-    for (int j = 0; j < m; ++j) {
-      Ri[j + m * j] = 1.0 / Lc[j + m * j];
-      for (int i = j - 1; i >= 0; --i) {
-        double s2 = 0.0;
-        for (int p = i + 1; p <= j; ++p) s2 += Lc[i + m * p] * Ri[p + m * j];
-        Ri[i + m * j] = -s2 / Lc[i + m * i];
-      }
-    }
-    FCG_CUDA(cudaMemcpyAsync(W.small.p, Ri.data(), sizeof(double) * m * m, cudaMemcpyHostToDevice, ctx->stream));
-    scale_cols_kernel<<<unsigned((W.n + 255) / 256), 256, 0, ctx->stream>>>(Tp, W.n, W.small.p, m, W.n, W.tmp.p);
-    FCG_CUDA(cudaGetLastError());
-    if (nv > 0) {  // restore orthogonality to V lost in the rescaling
-      if ((rc = W.gram(Vp, nv, Tp, m, S))) return rc;
-      if ((rc = W.update(Vp, nv, S, m, Tp, 2))) return rc;
-    }
+  const int k1 = int(keep.size());
+  if (k1 == 0) return FCG_OK;
+  std::vector<double> M1(size_t(nt) * k1, 0.0), dsc(k1);
+  for (int q = 0; q < k1; ++q) {
+    dsc[q] = 1.0 / std::sqrt(G0[nv + keep[q] + size_t(ld0) * keep[q]]);
+    M1[keep[q] + size_t(nt) * q] = dsc[q];
   }
-  *kept = m;
+  std::vector<double> S2, G2(size_t(k1) * k1);
+  if (nv == 0) {
+    if ((rc = combine(0, nt, M1, nullptr, k1))) return rc;
+    for (int q = 0; q < k1; ++q)
+      for (int p = 0; p < k1; ++p) G2[p + size_t(k1) * q] = dsc[p] * dsc[q] * G0[keep[p] + size_t(ld0) * keep[q]];
+  } else {
+    std::vector<double> P1(size_t(nv) * k1);
+    for (int q = 0; q < k1; ++q)
+      for (int i = 0; i < nv; ++i) P1[i + size_t(nv) * q] = G0[i + size_t(ld0) * keep[q]] * dsc[q];
+    if ((rc = combine(nv, nt, M1, &P1, k1))) return rc;
+    // 2. second projection, from the Gram matrix of the projected block
+    if ((rc = gram(V.p, nv + k1, V.p + n * nv, k1, d_out.p))) return rc;
+    if ((rc = fetch(size_t(nv + k1) * k1))) return rc;
+    const int ld1 = nv + k1;
+    const double* G1 = h_out.p;
+    S2.assign(size_t(nv) * k1, 0.0);
+    for (int q = 0; q < k1; ++q)
+      for (int i = 0; i < nv; ++i) S2[i + size_t(nv) * q] = G1[i + size_t(ld1) * q];
+    // Gram matrix after the second projection: T1^T T1 - S2^T S2 (V orthonormal)
+    for (int q = 0; q < k1; ++q)
+      for (int p = 0; p < k1; ++p) {
+        double s = G1[nv + p + size_t(ld1) * q];
+        for (int i = 0; i < nv; ++i) s -= S2[i + size_t(nv) * p] * S2[i + size_t(nv) * q];
+        G2[p + size_t(k1) * q] = s;
+      }
+    for (int q = 0; q < k1; ++q)
+      for (int p = 0; p < q; ++p) {
+        const double a = 0.5 * (G2[p + size_t(k1) * q] + G2[q + size_t(k1) * p]);
+        G2[p + size_t(k1) * q] = G2[q + size_t(k1) * p] = a;
+      }
+  }
+  // 3. survivors, Cholesky QR fused with the second projection
+  std::vector<int> keep2;
+  for (int p = 0; p < k1; ++p) {
+    const double g = G2[p + size_t(k1) * p];
+    if (std::isfinite(g) && g >= drop * drop) keep2.push_back(p);
+  }
+  const int k2 = int(keep2.size());
+  if (k2 == 0) return FCG_OK;
+  std::vector<double> G2k(size_t(k2) * k2);
+  for (int q = 0; q < k2; ++q)
+    for (int p = 0; p < k2; ++p) G2k[p + size_t(k2) * q] = G2[keep2[p] + size_t(k1) * keep2[q]];
+  std::vector<double> Ri;
+  int good = fcg_small::chol_inverse(k2, G2k.data(), k2, drop, Ri);
+  if (good == 0) return FCG_OK;
+  std::vector<double> M2(size_t(k1) * good, 0.0);
+  for (int c = 0; c < good; ++c)
+    for (int q = 0; q < good; ++q) M2[keep2[q] + size_t(k1) * c] = Ri[q + size_t(good) * c];
+  if (nv == 0) {
+    if ((rc = combine(0, k1, M2, nullptr, good))) return rc;
+  } else {
+    std::vector<double> P2(size_t(nv) * good, 0.0);
+    for (int c = 0; c < good; ++c)
+      for (int p = 0; p < k1; ++p) {
+        const double m = M2[p + size_t(k1) * c];
+        if (m == 0.0) continue;
+        for (int i = 0; i < nv; ++i) P2[i + size_t(nv) * c] += S2[i + size_t(nv) * p] * m;
+      }
+    if ((rc = combine(nv, k1, M2, &P2, good))) return rc;
+  }
+  // 4. second Cholesky QR (and projection) for an ill-conditioned block only
+  if (fcg_small::spd_condition(good, G2k.data(), k2) > 1e4) {
+    if ((rc = gram(V.p, nv + good, V.p + n * nv, good, d_out.p))) return rc;
+    if ((rc = fetch(size_t(nv + good) * good))) return rc;
+    const int ld3 = nv + good;
+    const double* G3 = h_out.p;
+    std::vector<double> S3(size_t(nv) * good), G3t(size_t(good) * good);
+    for (int q = 0; q < good; ++q)
+      for (int i = 0; i < nv; ++i) S3[i + size_t(nv) * q] = G3[i + size_t(ld3) * q];
+    for (int q = 0; q < good; ++q)
+      for (int p = 0; p < good; ++p) {
+        double s = 0.5 * (G3[nv + p + size_t(ld3) * q] + G3[nv + q + size_t(ld3) * p]);
+        for (int i = 0; i < nv; ++i) s -= S3[i + size_t(nv) * p] * S3[i + size_t(nv) * q];
+        G3t[p + size_t(good) * q] = s;
+      }
+    std::vector<double> Ri3;
+    const int good3 = fcg_small::chol_inverse(good, G3t.data(), good, drop, Ri3);
+    if (good3 == 0) return FCG_OK;
+    std::vector<double> M3(size_t(good) * good3, 0.0);
+    for (int c = 0; c < good3; ++c)
+      for (int i = 0; i < good3; ++i) M3[i + size_t(good) * c] = Ri3[i + size_t(good3) * c];
+    std::vector<double> P3;
+    if (nv > 0) {
+      P3.assign(size_t(nv) * good3, 0.0);
+      for (int c = 0; c < good3; ++c)
+        for (int p = 0; p < good3; ++p) {
+          const double m = M3[p + size_t(good) * c];
+          for (int i = 0; i < nv; ++i) P3[i + size_t(nv) * c] += S3[i + size_t(nv) * p] * m;
+        }
+    }
+    if ((rc = combine(nv, good, M3, nv > 0 ? &P3 : nullptr, good3))) return rc;
+    good = good3;
+  }
+  *kept = good;
   return FCG_OK;
 }
 
-}  // namespace
+// orthonormalise the block V[:, 0 : nt] on its own (the first block of a (re)start)
+int DavidsonWork::start_block(int nt, double drop, int* kept) {
+  int rc;
+  if ((rc = gram(V.p, nt, V.p, nt, d_out.p))) return rc;
+  if ((rc = fetch(size_t(nt) * nt))) return rc;
+  std::vector<double> G0(h_out.p, h_out.p + size_t(nt) * nt);
+  return orthonormalize(0, nt, std::move(G0), drop, kept);
+}
 
-extern "C" int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
-extern "C" int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd);
+}  // namespace
 
 extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
                             double lindep, int precision, int precond, double* energies, double* vectors,
@@ -295,7 +501,7 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
   FCG_REQUIRE(v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
-  FCG_REQUIRE(R >= 1 && R <= 16 && R <= ctx->n_cfg, FCG_ELIMIT, "R must be in [1, min(16, n_cfg)]");
+  FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= ctx->n_cfg, FCG_ELIMIT, "R must be in [1, min(16, n_cfg)]");
   FCG_REQUIRE(max_ss_vecs >= 2 && max_iter >= 1 && tol > 0, FCG_EINVAL, "bad Davidson settings");
   FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
   FCG_CUDA(cudaSetDevice(ctx->device));
@@ -303,35 +509,64 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
   DavidsonWork W;
   W.ctx = ctx;
   W.n = n;
+  W.R = R;
   W.kmax = int(std::min<int64_t>(int64_t(max_ss_vecs) * R, n));
   W.kmax = std::max(W.kmax, std::min<int>(2 * R, int(n)));
-  const int kmax = W.kmax;
-  W.gram_grid = int(std::min<int64_t>(304, (n + 255) / 256));
-  // room for a full subspace plus one block of new directions (restart keeps nv <= kmax)
-  FCG_CUDA(W.V.alloc(size_t(n) * (kmax + R)));
-  FCG_CUDA(W.AV.alloc(size_t(n) * (kmax + R)));
+  W.kcap = W.kmax + R;
+  const int kmax = W.kmax, kcap = W.kcap;
+  // shared memory of the residual and combine kernels: (kcap x R) + R doubles at most
+  const size_t smem_max = sizeof(double) * (size_t(kcap) * R + size_t(R) * R + R);
+  FCG_REQUIRE(smem_max <= 200 * 1024, FCG_ELIMIT, "max_ss_vecs * R too large for the subspace kernels");
+  if (smem_max > 48 * 1024) {
+    const int sm = int(smem_max);
+    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<1>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<2>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<4>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<8>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<16>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<1>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<2>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<4>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<8>, attr, sm));
+    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<16>, attr, sm));
+  }
+  W.row_blocks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxRowBlocks, (n + kGramRows - 1) / kGramRows)));
+  W.rows_per_block = (n + W.row_blocks - 1) / W.row_blocks;
+  W.res_blocks = int((n + kDavThreads - 1) / kDavThreads);
+  FCG_CUDA(W.V.alloc(size_t(n) * kcap));
+  FCG_CUDA(W.AV.alloc(size_t(n) * kcap));
   FCG_CUDA(W.X.alloc(size_t(n) * R));
-  FCG_CUDA(W.HX.alloc(size_t(n) * R));
-  FCG_CUDA(W.T.alloc(size_t(n) * R));
-  FCG_CUDA(W.tmp.alloc(size_t(n) * std::max(R, kmax)));
-  FCG_CUDA(W.small.alloc(size_t(kmax) * kmax + 16));
-  FCG_CUDA(W.theta.alloc(16));
-  FCG_CUDA(W.rn.alloc(16));
+  FCG_CUDA(W.tmp.alloc(size_t(n) * std::min(kmax, 2 * R)));
   FCG_CUDA(W.hd.alloc(n));
+  FCG_CUDA(W.part.alloc(size_t(W.row_blocks) * kcap * R));
+  FCG_CUDA(W.rn_part.alloc(size_t(W.res_blocks) * R));
+  W.ngroups = (kcap + 31) / 32;
+  FCG_CUDA(W.counters.alloc(size_t(W.ngroups) + 1));
+  FCG_CUDA(cudaMemsetAsync(W.counters.p, 0, sizeof(unsigned) * (W.ngroups + 1), ctx->stream));
+  const size_t out_cap = size_t(R) + size_t(kcap) * R + 16;
+  const size_t up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
+  FCG_CUDA(W.d_out.alloc(out_cap));
+  FCG_CUDA(W.h_out.alloc(out_cap));
+  FCG_CUDA(W.d_up.alloc(up_cap));
+  FCG_CUDA(W.h_up.alloc(up_cap));
   if (precond) {
     std::vector<double> hd(n);
     int rc = fcg_diagonal(ctx, -1, hd.data());
     if (rc) return rc;
     FCG_CUDA(cudaMemcpyAsync(W.hd.p, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // hd is a local vector
   }
   int prec = precision;  // current sigma precision
   // a new direction must keep at least this fraction of its norm after projection
   const double drop = std::max(lindep, 1e-8);
   const double switch_tol = std::max(tol, 1e-5);
+  // GD+k restarts keep 2R vectors when the subspace has room for them and a new block
+  const bool gdk = kmax >= 3 * R;
   // initial block
   FCG_CUDA(cudaMemcpyAsync(W.V.p, v0, sizeof(double) * n * R, cudaMemcpyHostToDevice, ctx->stream));
   int nv = 0, m = 0, rc;
-  if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, drop, &m))) return rc;
+  if ((rc = W.start_block(R, drop, &m))) return rc;
   if (m != R) {
     double nrm_min = 1e300, nrm_max = 0.0;
     int nonfinite = 0;
@@ -350,82 +585,187 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
                std::to_string(nrm_max) + ", non-finite entries " + std::to_string(nonfinite) + ")";
     return FCG_EINVAL;
   }
-  if ((rc = fcg_sigma_closed_device(ctx, R, W.V.p, W.AV.p, prec))) return rc;
+  if ((rc = sigma_closed_device_async(ctx, R, W.V.p, W.AV.p, prec))) return rc;
   nv = R;
-  std::vector<double> Hs, w, Y, th(R), rn(R);
+  int newlo = 0;  // first column of AV whose projections are not in Hs yet
+  std::vector<double> Hs(size_t(kcap) * kcap, 0.0), A, w, Y, th(R), rn(R);
+  std::vector<double> Yprev;  // previous Ritz coefficients in the current basis (yprev_rows x R)
+  int yprev_rows = 0;
   int it = 0;
   int64_t sigma_calls = 1;
-  bool converged = false;
   for (it = 1; it <= max_iter; ++it) {
-    // Rayleigh-Ritz
-    if ((rc = W.gram(W.V.p, nv, W.AV.p, nv, Hs))) return rc;
+    // Rayleigh-Ritz: the new columns of V^T H V, then the projected eigenproblem
+    const int nb = nv - newlo;
+    if ((rc = W.gram(W.V.p, nv, W.AV.p + n * newlo, nb, W.d_out.p))) return rc;
+    if ((rc = W.fetch(size_t(nv) * nb))) return rc;
+    {
+      const double* C = W.h_out.p;
+      for (int c = 0; c < nb; ++c) {
+        const int col = newlo + c;
+        for (int i = 0; i < nv; ++i) {
+          double h = C[i + size_t(nv) * c];
+          if (i >= newlo) h = 0.5 * (h + C[col + size_t(nv) * (i - newlo)]);
+          if (!std::isfinite(h)) {
+            ctx->err = "Davidson: non-finite subspace matrix at iteration " + std::to_string(it) + " (subspace " +
+                       std::to_string(nv) + ")";
+            return FCG_ECUDA;
+          }
+          Hs[i + size_t(kcap) * col] = Hs[col + size_t(kcap) * i] = h;
+        }
+      }
+    }
+    A.resize(size_t(nv) * nv);
     for (int j = 0; j < nv; ++j)
-      for (int i = 0; i < j; ++i) {
-        double a = 0.5 * (Hs[i + nv * j] + Hs[j + nv * i]);
-        Hs[i + nv * j] = Hs[j + nv * i] = a;
-      }
-    for (double x : Hs)
-      if (!std::isfinite(x)) {
-        ctx->err = "Davidson: non-finite subspace matrix at iteration " + std::to_string(it) + " (subspace " +
-                   std::to_string(nv) + ")";
-        return FCG_ECUDA;
-      }
-    jacobi_eigh(nv, Hs, w, Y);
-    Y.resize(size_t(nv) * R);
+      for (int i = 0; i < nv; ++i) A[i + size_t(nv) * j] = Hs[i + size_t(kcap) * j];
+    if (fcg_small::symeig(nv, A.data(), w, Y, R)) {
+      ctx->err = "Davidson: subspace eigensolver did not converge at iteration " + std::to_string(it);
+      return FCG_ECUDA;
+    }
     for (int j = 0; j < R; ++j) th[j] = w[j];
-    if ((rc = W.update(W.V.p, nv, Y, R, W.X.p, 0))) return rc;
-    if ((rc = W.update(W.AV.p, nv, Y, R, W.HX.p, 0))) return rc;
-    FCG_CUDA(cudaMemcpyAsync(W.theta.p, th.data(), sizeof(double) * R, cudaMemcpyHostToDevice, ctx->stream));
-    FCG_CUDA(cudaMemsetAsync(W.rn.p, 0, sizeof(double) * R, ctx->stream));
-    residual_kernel<<<unsigned((n + 255) / 256), 256, 0, ctx->stream>>>(W.X.p, W.HX.p, W.theta.p, W.hd.p, R, n,
-                                                                        W.T.p, W.rn.p, precond);
+    // Ritz vectors, residual norms, corrections behind V, and [V T]^T T
+    const double *dY = nullptr, *dth = nullptr;
+    if ((rc = W.upload(Y.data(), size_t(nv) * R, &dY))) return rc;
+    if ((rc = W.upload(th.data(), size_t(R), &dth))) return rc;
+    if ((rc = W.flush())) return rc;
+    const size_t ritz_smem = sizeof(double) * (size_t(nv) * R + R);
+#define FCG_RITZ_LAUNCH unsigned(W.res_blocks), kDavThreads, ritz_smem, ctx->stream
+    FCG_WIDTH_SWITCH(R, ritz_residual_kernel, FCG_RITZ_LAUNCH, W.V.p, W.AV.p, n, nv, dY, dth, W.hd.p, R, n, W.X.p,
+                     W.V.p + n * nv, precond, W.rn_part.p, W.d_out.p, W.counters.p + W.ngroups)
+#undef FCG_RITZ_LAUNCH
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaMemcpyAsync(rn.data(), W.rn.p, sizeof(double) * R, cudaMemcpyDeviceToHost, ctx->stream));
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if ((rc = W.gram(W.V.p, nv + R, W.V.p + n * nv, R, W.d_out.p + R))) return rc;
+    if ((rc = W.fetch(size_t(R) + size_t(nv + R) * R))) return rc;
     double rmax = 0.0;
     for (int j = 0; j < R; ++j) {
-      rn[j] = std::sqrt(rn[j]);
+      rn[j] = std::sqrt(W.h_out.p[j]);
       rmax = std::max(rmax, rn[j]);
       if (!std::isfinite(rn[j]) || !std::isfinite(th[j])) {
         ctx->err = "Davidson: non-finite residual or Ritz value at iteration " + std::to_string(it);
         return FCG_ECUDA;
       }
     }
-    const bool switching = (prec == FCG_FP32) && rmax < switch_tol;
-    if (rmax < tol && prec == FCG_FP64) {
-      converged = true;
-      break;
-    }
-    if (switching || nv + R > kmax) {
-      // restart from the Ritz vectors (and, when switching precision, rebuild H X in float64)
+    if (rmax < tol && prec == FCG_FP64) break;
+    if (prec == FCG_FP32 && rmax < switch_tol) {
+      // refinement: restart from the Ritz vectors with float64 sigma builds
+      prec = FCG_FP64;
       FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
-      if (switching) {
-        prec = FCG_FP64;
-        if ((rc = orthonormalize_block(W, W.V.p, R, nullptr, 0, drop, &m))) return rc;
-        if ((rc = fcg_sigma_closed_device(ctx, R, W.V.p, W.AV.p, prec))) return rc;
-        ++sigma_calls;
-        nv = R;
-        continue;
-      }
-      FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.HX.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
-      nv = R;
+      if ((rc = W.start_block(R, drop, &m))) return rc;
+      if (m < R) break;  // Ritz vectors numerically dependent: keep the float32 result
+      if ((rc = sigma_closed_device_async(ctx, m, W.V.p, W.AV.p, prec))) return rc;
+      ++sigma_calls;
+      nv = m;
+      newlo = 0;
+      yprev_rows = 0;
+      continue;
     }
-    // new directions: preconditioned residuals of the roots not yet converged,
-    // orthonormalised against the subspace
-    int nt = 0;
+    // new directions: corrections of the roots not yet converged (all roots in float32)
+    std::vector<int> sel;
     for (int j = 0; j < R; ++j)
-      if (rn[j] >= tol || prec == FCG_FP32) {
-        FCG_CUDA(cudaMemcpyAsync(W.V.p + n * (nv + nt), W.T.p + n * j, sizeof(double) * n,
-                                 cudaMemcpyDeviceToDevice, ctx->stream));
-        ++nt;
-      }
-    if ((rc = orthonormalize_block(W, W.V.p + n * nv, nt, W.V.p, nv, drop, &m))) return rc;
-    if (m == 0) {  // the subspace cannot grow: converged as far as lindep allows
-      converged = rmax < tol;
-      break;
+      if (rn[j] >= tol || prec == FCG_FP32) sel.push_back(j);
+    const int nt = int(sel.size());
+    const int ldg = nv + R;
+    const double* Gall = W.h_out.p + R;  // [V T]^T T, (nv + R) x R
+    std::vector<double> S(size_t(nv) * nt), Gtt(size_t(nt) * nt);
+    for (int q = 0; q < nt; ++q) {
+      for (int i = 0; i < nv; ++i) S[i + size_t(nv) * q] = Gall[i + size_t(ldg) * sel[q]];
+      for (int p = 0; p < nt; ++p) Gtt[p + size_t(nt) * q] = Gall[nv + sel[p] + size_t(ldg) * sel[q]];
     }
-    if ((rc = fcg_sigma_closed_device(ctx, m, W.V.p + n * nv, W.AV.p + n * nv, prec))) return rc;
+    const int nv_old = nv;
+    if (nv + nt > kmax) {
+      // restart on span{Y, Yprev}: Q orthonormal (nv x q), V <- V Q, AV <- AV Q, Hs <- Q^T Hs Q
+      const int zc = R + ((gdk && yprev_rows > 0) ? R : 0);
+      std::vector<double> Q;
+      int q = 0;
+      for (int c = 0; c < zc; ++c) {
+        std::vector<double> z(nv, 0.0);
+        if (c < R)
+          for (int i = 0; i < nv; ++i) z[i] = Y[i + size_t(nv) * c];
+        else
+          for (int i = 0; i < yprev_rows; ++i) z[i] = Yprev[i + size_t(yprev_rows) * (c - R)];
+        double n0 = 0.0;
+        for (double x : z) n0 += x * x;
+        n0 = std::sqrt(n0);
+        for (int pass = 0; pass < 2; ++pass)
+          for (int k = 0; k < q; ++k) {
+            double d = 0.0;
+            for (int i = 0; i < nv; ++i) d += Q[i + size_t(nv) * k] * z[i];
+            for (int i = 0; i < nv; ++i) z[i] -= d * Q[i + size_t(nv) * k];
+          }
+        double nz = 0.0;
+        for (double x : z) nz += x * x;
+        nz = std::sqrt(nz);
+        if (!(nz > 1e-8 * n0)) continue;
+        for (double& x : z) x /= nz;
+        Q.insert(Q.end(), z.begin(), z.end());
+        ++q;
+      }
+      const double* dQ = nullptr;
+      if ((rc = W.upload(Q.data(), size_t(nv) * q, &dQ))) return rc;
+      if ((rc = W.flush())) return rc;
+      const unsigned g = unsigned((n + 255) / 256);
+      update_kernel<<<g, 256, 0, ctx->stream>>>(W.V.p, n, nv, dQ, q, W.tmp.p, n, n);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaMemcpyAsync(W.V.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
+      update_kernel<<<g, 256, 0, ctx->stream>>>(W.AV.p, n, nv, dQ, q, W.tmp.p, n, n);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
+      std::vector<double> HQ(size_t(nv) * q, 0.0), Hn(size_t(q) * q, 0.0), Sn(size_t(q) * nt, 0.0),
+          Yp(size_t(q) * R, 0.0);
+      for (int c = 0; c < q; ++c)
+        for (int k = 0; k < nv; ++k) {
+          const double qk = Q[k + size_t(nv) * c];
+          for (int i = 0; i < nv; ++i) HQ[i + size_t(nv) * c] += Hs[i + size_t(kcap) * k] * qk;
+        }
+      for (int c = 0; c < q; ++c)
+        for (int r2 = 0; r2 < q; ++r2) {
+          double s = 0.0;
+          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * HQ[i + size_t(nv) * c];
+          Hn[r2 + size_t(q) * c] = s;
+        }
+      for (int c = 0; c < q; ++c)
+        for (int r2 = 0; r2 < c; ++r2) {
+          const double a = 0.5 * (Hn[r2 + size_t(q) * c] + Hn[c + size_t(q) * r2]);
+          Hn[r2 + size_t(q) * c] = Hn[c + size_t(q) * r2] = a;
+        }
+      for (int c = 0; c < nt; ++c)
+        for (int r2 = 0; r2 < q; ++r2) {
+          double s = 0.0;
+          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * S[i + size_t(nv) * c];
+          Sn[r2 + size_t(q) * c] = s;
+        }
+      for (int c = 0; c < R; ++c)
+        for (int r2 = 0; r2 < q; ++r2) {
+          double s = 0.0;
+          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * Y[i + size_t(nv) * c];
+          Yp[r2 + size_t(q) * c] = s;
+        }
+      for (int c = 0; c < q; ++c)
+        for (int r2 = 0; r2 < q; ++r2) Hs[r2 + size_t(kcap) * c] = Hn[r2 + size_t(q) * c];
+      S.swap(Sn);
+      Yprev.swap(Yp);
+      yprev_rows = q;
+      nv = q;
+    } else {
+      Yprev = Y;
+      yprev_rows = nv;
+    }
+    // the selected corrections move to V[:, nv : nv + nt] (never onto a later source column)
+    for (int q = 0; q < nt; ++q) {
+      const int src = nv_old + sel[q], dst = nv + q;
+      if (src != dst)
+        FCG_CUDA(cudaMemcpyAsync(W.V.p + n * dst, W.V.p + n * src, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                                 ctx->stream));
+    }
+    std::vector<double> G0(size_t(nv + nt) * nt);
+    for (int c = 0; c < nt; ++c) {
+      for (int i = 0; i < nv; ++i) G0[i + size_t(nv + nt) * c] = S[i + size_t(nv) * c];
+      for (int p = 0; p < nt; ++p) G0[nv + p + size_t(nv + nt) * c] = Gtt[p + size_t(nt) * c];
+    }
+    if ((rc = W.orthonormalize(nv, nt, std::move(G0), drop, &m))) return rc;
+    if (m == 0) break;  // the subspace cannot grow: converged as far as lindep allows
+    if ((rc = sigma_closed_device_async(ctx, m, W.V.p + n * nv, W.AV.p + n * nv, prec))) return rc;
     ++sigma_calls;
+    newlo = nv;
     nv += m;
   }
   for (int j = 0; j < R; ++j) {
@@ -436,6 +776,5 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   *iters = std::min(it, max_iter);
   ctx->stats.davidson_sigma_calls = sigma_calls;
-  (void)converged;
   return FCG_OK;
 }

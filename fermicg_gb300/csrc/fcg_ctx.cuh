@@ -175,6 +175,11 @@ struct fcg_ctx {
   fcg_stats stats{};
 };
 
+// closed sigma on device vectors (column-major n_cfg x R) queued on ctx->stream, without the
+// host wait of fcg_sigma_closed_device; for drivers that keep working on the same stream
+// (fcg_gpu.cu)
+int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
+
 #define FCG_CUDA(call)                                                               \
   do {                                                                               \
     cudaError_t e_ = (call);                                                         \

@@ -463,12 +463,14 @@ __global__ void grouped_unpack_kernel(const GroupEntry<T>* __restrict__ g) {
 }
 
 template <typename T>
-__global__ void pack_in_kernel(const double* __restrict__ c, T* __restrict__ out, int64_t n, int R) {
+__global__ void pack_in_kernel(const double* __restrict__ c, T* __restrict__ out, int64_t n, int R,
+                               T* __restrict__ zero) {
   int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (i >= n * R) return;
   int64_t row = i / R;
   int r = int(i - row * R);
   out[i] = T(c[row + n * r]);
+  if (zero) zero[i] = T(0);  // the sigma accumulator of the same shape, when given
 }
 
 template <typename T>
@@ -898,15 +900,16 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
 }  // extern "C"
 
 template <typename T>
-static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig) {
+static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig, bool zero_sig = true,
+                         bool timed = true) {
   SigmaParams p = make_sigma_params(ctx, R);
   p.cta_lo = sizeof(T) == 4 ? ctx->d_cta32.p : ctx->d_cta64.p;
-  FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
+  if (zero_sig) FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
   int launches = 0;
   if (p.n_triples > 0) {
     int64_t grid = (p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
     FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many triples for one launch");
-    FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     switch (R) {
       case 1: closed_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
       case 2: closed_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
@@ -914,14 +917,15 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* 
       default: closed_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
     }
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     launches = 1;
   }
   ctx->stats.kernel_launches = launches;
   return FCG_OK;
 }
 
-static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision) {
+static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision,
+                             bool wait = true) {
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
   FCG_REQUIRE(R >= 1 && R <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
   FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
@@ -933,20 +937,21 @@ static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_s
   if (precision == FCG_FP64) {
     FCG_CUDA(ctx->d_c64.alloc(nR));
     FCG_CUDA(ctx->d_s64.alloc(nR));
-    pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c64.p, n, R);
-    rc = launch_closed<double>(ctx, R, ctx->d_w64.p, ctx->d_op64.p, ctx->d_c64.p, ctx->d_s64.p);
+    pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c64.p, n, R, ctx->d_s64.p);
+    rc = launch_closed<double>(ctx, R, ctx->d_w64.p, ctx->d_op64.p, ctx->d_c64.p, ctx->d_s64.p, false, wait);
     if (rc) return rc;
     unpack_out_kernel<double><<<g, 256, 0, ctx->stream>>>(ctx->d_s64.p, d_sigma, n, R);
   } else {
     FCG_CUDA(ctx->d_c32.alloc(nR));
     FCG_CUDA(ctx->d_s32.alloc(nR));
-    pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c32.p, n, R);
-    rc = launch_closed<float>(ctx, R, ctx->d_w32.p, ctx->d_op32.p, ctx->d_c32.p, ctx->d_s32.p);
+    pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, ctx->d_c32.p, n, R, ctx->d_s32.p);
+    rc = launch_closed<float>(ctx, R, ctx->d_w32.p, ctx->d_op32.p, ctx->d_c32.p, ctx->d_s32.p, false, wait);
     if (rc) return rc;
     unpack_out_kernel<float><<<g, 256, 0, ctx->stream>>>(ctx->d_s32.p, d_sigma, n, R);
   }
   FCG_CUDA(cudaGetLastError());
   ctx->stats.kernel_launches += 2;
+  if (!wait) return FCG_OK;  // untimed: no events were recorded
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   if (ctx->plan.n_triples > 0) {
     float ms = 0.f;
@@ -954,6 +959,10 @@ static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_s
     ctx->stats.last_kernel_ms = ms;
   }
   return FCG_OK;
+}
+
+int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision) {
+  return sigma_device_impl(ctx, R, d_c, d_sigma, precision, false);
 }
 
 extern "C" {
@@ -1210,14 +1219,14 @@ extern "C" int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, 
   if (precision == FCG_FP64) {
     double* cbuf = scratch;
     double* sbuf = scratch + kNoAllocMaxElems;
-    pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R);
+    pack_in_kernel<double><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R, nullptr);
     rc = launch_closed<double>(ctx, R, ctx->d_w64.p, ctx->d_op64.p, cbuf, sbuf);  // zeroes sbuf first
     if (rc) return rc;
     unpack_out_kernel<double><<<g, 256, 0, ctx->stream>>>(sbuf, d_sigma, n, R);
   } else {
     float* cbuf = reinterpret_cast<float*>(scratch);
     float* sbuf = reinterpret_cast<float*>(scratch + kNoAllocMaxElems);
-    pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R);
+    pack_in_kernel<float><<<g, 256, 0, ctx->stream>>>(d_c, cbuf, n, R, nullptr);
     rc = launch_closed<float>(ctx, R, ctx->d_w32.p, ctx->d_op32.p, cbuf, sbuf);
     if (rc) return rc;
     unpack_out_kernel<float><<<g, 256, 0, ctx->stream>>>(sbuf, d_sigma, n, R);

@@ -1,0 +1,24 @@
+// C entry points over fermicg_gb300/csrc/small_dense.h so that the host-side linear algebra
+// of the Davidson driver can be checked against numpy on a machine without a GPU.
+#include "../fermicg_gb300/csrc/small_dense.h"
+
+#include <cstring>
+
+extern "C" int sd_symeig(int k, double* A, double* w, double* Z, int nvec) {
+  std::vector<double> wv, Zv;
+  const int rc = fcg_small::symeig(k, A, wv, Zv, nvec);
+  if (k > 0) {
+    std::memcpy(w, wv.data(), sizeof(double) * k);
+    std::memcpy(Z, Zv.data(), sizeof(double) * Zv.size());
+  }
+  return rc;
+}
+
+extern "C" int sd_chol_inverse(int m, const double* G, int ldg, double drop, double* Ri) {
+  std::vector<double> R;
+  const int good = fcg_small::chol_inverse(m, G, ldg, drop, R);
+  if (good > 0) std::memcpy(Ri, R.data(), sizeof(double) * size_t(good) * good);
+  return good;
+}
+
+extern "C" double sd_spd_condition(int m, const double* G, int ldg) { return fcg_small::spd_condition(m, G, ldg); }
