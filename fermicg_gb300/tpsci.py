@@ -1,7 +1,8 @@
 """TPSCI driver on the GPU sigma build.
 
-tpsci_ci (src/tpsci.jl:39-363, incremental-sigma branch) and compute_pt2_energy
-(src/tpsci_pt2_energy.jl:10-233), with every sigma-sized operation on the device:
+tpsci_ci (src/tpsci.jl:39-363, incremental-sigma branch), compute_pt2_energy
+(src/tpsci_pt2_energy.jl:10-233) and compute_pt1_wavefunction
+(src/tpsci_pt1_wavefunction.jl:11-83), with every sigma-sized operation on the device:
 the variational solve is the device Davidson (fcg_davidson, the tps_ci_davidson
 solve), the FOIS sigma is fcg_sigma_open, the PT denominators are fcg_diagonal("Hcmf"),
 <0|H0|0> is a closed sigma of the 1-body "Hcmf" operator.  The TPSCIstate bookkeeping
@@ -127,3 +128,25 @@ class GpuTPSCI:
         hd = self.diagonal_cmf(sig)
         sv = sig.get_vector()
         return np.array([np.sum(sv[:, r] ** 2 / (e0[r] - hd)) for r in range(v.R)])
+
+    def pt1_wavefunction(self, ci_vector: TPSCIstate, thresh_foi=1e-8, nbody=4, E0=None):
+        """compute_pt1_wavefunction with H0 = Hcmf: the FOIS sigma with the variational
+        configurations removed, divided by (E0_r / |v_r|^2 - Hd); returns (e2, PT1 state).
+        E0 = <v_r|H0|v_r> unless given (src/tpsci_pt1_wavefunction.jl:11-83)."""
+        R = ci_vector.R
+        norms = np.linalg.norm(ci_vector.get_vector(), axis=0)
+        sig = self.open_sigma(ci_vector, thresh_foi, nbody)
+        project_out(sig, ci_vector)
+        hd = self.diagonal_cmf(sig)
+        if E0 is None:
+            E0 = self.expectation0(ci_vector)
+        sig_v = sig.get_vector() if len(sig) else np.zeros((0, R))
+        v_pt = np.zeros_like(sig_v)
+        e2 = np.zeros(R)
+        for r in range(R):
+            denom = 1.0 / (E0[r] / (norms[r] * norms[r]) - hd)
+            v_pt[:, r] = denom * sig_v[:, r]
+            e2[r] = float(np.sum(sig_v[:, r] * v_pt[:, r]))
+        if len(sig):
+            sig.set_vector(v_pt)
+        return e2, sig

@@ -211,3 +211,25 @@ class OracleTPSCI:
         f, c, sv = self._flat(sig)
         hd = self.O.diagonal_op(f, c, self.hcmf)
         return np.array([np.sum(sv[:, r] ** 2 / (e0[r] - hd)) for r in range(v.R)])
+
+    def pt1_wavefunction(self, ci_vector, thresh_foi=1e-8, nbody=4, E0=None):
+        """compute_pt1_wavefunction (tpsci_pt1_wavefunction.jl:11-83) with H0 = Hcmf:
+        v_pt = sigma / (E0_r / |v_r|^2 - Hd) on the FOIS minus the variational configurations,
+        e2_r = sum sigma_r * v_pt_r; returns (e2, PT1 state)."""
+        R = ci_vector.R
+        norms = np.linalg.norm(ci_vector.get_vector(), axis=0)
+        sig = self.open_sigma(ci_vector, thresh_foi, nbody)
+        _project_out(sig, ci_vector)
+        f, c, sig_v = self._flat(sig)
+        hd = self.O.diagonal_op(f, c, self.hcmf) if len(sig) else np.zeros(0)
+        if E0 is None:
+            E0 = self.expectation(ci_vector, zeroth=True)
+        v_pt = np.zeros_like(sig_v)
+        e2 = np.zeros(R)
+        for r in range(R):
+            denom = 1.0 / (E0[r] / (norms[r] * norms[r]) - hd)
+            v_pt[:, r] = denom * sig_v[:, r]
+            e2[r] = float(np.sum(sig_v[:, r] * v_pt[:, r]))
+        if len(sig):
+            sig.set_vector(v_pt)
+        return e2, sig

@@ -102,3 +102,10 @@ def test_h12_tpsci_energies_match_reference():
     # compute_pt2_energy(v0, thresh_foi=1e-10): e0 + e2 (reference asserts 1e-8)
     e2 = T.pt2_energy(v0, thresh_foi=m["pt2_thresh_foi"])
     np.testing.assert_allclose(np.abs(e0 + e2), np.abs(np.array(m["e0_plus_e2"])), atol=1e-8, rtol=0)
+    # compute_pt1_wavefunction on the same orthonormal vectors gives the same e2, and its
+    # PT1 amplitudes reproduce it: e2_r = sum_x sigma_x,r * v_pt_x,r
+    e2_pt1, v_pt = T.pt1_wavefunction(v0, thresh_foi=m["pt2_thresh_foi"])
+    np.testing.assert_allclose(e2_pt1, e2, atol=1e-12, rtol=0)
+    assert len(v_pt) > len(v0)
+    d0 = v0.as_dict()
+    assert not any(k in d0 for k in v_pt.keys())

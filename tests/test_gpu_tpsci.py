@@ -66,6 +66,16 @@ def test_gpu_tpsci_h12_matches_reference_energies():
     np.testing.assert_allclose(np.abs(e0), np.abs(np.array(m["e0"])), atol=1e-8, rtol=0)
     e2 = T.pt2_energy(v0, thresh_foi=m["pt2_thresh_foi"])
     np.testing.assert_allclose(np.abs(e0 + e2), np.abs(np.array(m["e0_plus_e2"])), atol=1e-8, rtol=0)
+    # compute_pt1_wavefunction on the GPU vs the oracle, same input vectors: same FOIS keys,
+    # amplitudes and e2 within 1e-10
+    from oracle.tpsci import OracleTPSCI
+    e2g, vg = T.pt1_wavefunction(v0, thresh_foi=m["pt2_thresh_foi"])
+    e2o, vo = OracleTPSCI(ops, b, H).pt1_wavefunction(v0, thresh_foi=m["pt2_thresh_foi"])
+    np.testing.assert_allclose(e2g, e2o, atol=1e-10, rtol=0)
+    dg, do = vg.as_dict(), vo.as_dict()
+    assert set(dg) == set(do)
+    for k, x in do.items():
+        np.testing.assert_allclose(dg[k], x, atol=1e-10, rtol=1e-10)
     T.close()
 
 
