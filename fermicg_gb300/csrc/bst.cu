@@ -482,7 +482,7 @@ void append_perm(const BstBlock& B, int N, int mask, std::vector<int32_t>& perm)
 // for which check_term holds on the TuckerConfigs: equal Fock sectors and equal ranges on
 // the spectators), grouped by (bra, ket, active clusters).
 std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>& blk, const int16_t* fock,
-                     BstPlan& P) {
+                     BstPlan& P, const int32_t* given = nullptr, int64_t n_given = 0) {
   const int N = ctx->N;
   const int nmax1 = ctx->nmax + 1;
   const int64_t nb = int64_t(blk.size());
@@ -528,6 +528,99 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
   std::unordered_map<uint64_t, int64_t> overlap_at; // (bra, ket, c) -> S offset
   std::unordered_map<uint64_t, int64_t> perm_at;    // (block, active mask) -> index table offset
   std::vector<std::vector<BstGroupTerm>> gt;        // terms per group
+  // one (bra, ket, term) triple into its (bra, ket, active clusters) group, with the
+  // dressed TDMs it needs; grp maps (ket, mask) to the bra block's groups
+  auto add_triple = [&](int64_t b, int32_t k, int t, const int32_t* r, int mask, const int* tdm, int sign,
+                        std::unordered_map<uint64_t, int32_t>& grp) -> std::string {
+    P.triples.insert(P.triples.end(), {int32_t(b), k, int32_t(t), int32_t(sign)});
+    const uint64_t gk = (uint64_t(uint32_t(k)) << 8) | uint64_t(mask);
+    auto gi = grp.find(gk);
+    int32_t g;
+    if (gi == grp.end()) {
+      g = int32_t(P.groups.size());
+      grp[gk] = g;
+      BstGroup G{};
+      G.bra = int32_t(b);
+      G.ket = k;
+      G.act_mask = mask;
+      P.groups.push_back(G);
+      gt.emplace_back();
+    } else {
+      g = gi->second;
+    }
+    BstGroupTerm T{};
+    T.nact = r[0];
+    T.sign = sign;
+    T.ints_off = r[0] == 1 ? -1 : ctx->terms[t].ints_off;
+    for (int o = 0; o < r[0]; ++o) {
+      const int c = r[2 + o];
+      const BlockInfo& BI = ctx->h_blocks[tdm[o]];
+      if (r[0] > 1 && BI.nidx != r[22 + o]) return "BST: TDM multi-index length differs from the term's ints";
+      const uint64_t key = ((uint64_t(b) * uint64_t(nb) + uint64_t(k)) * 8 + uint64_t(c)) * 32 + uint64_t(r[6 + o]);
+      auto ga = gamma_at.find(key);
+      if (ga == gamma_at.end()) {
+        BstGamma Q{};
+        Q.g_off = P.g_total;
+        Q.tdm_off = BI.off;
+        Q.bra = int32_t(b);
+        Q.ket = k;
+        Q.c = c;
+        Q.np = BI.nidx;
+        Q.tdm_mb = BI.mb;
+        if (blk[b].start[c] + blk[b].len[c] > BI.mb || blk[k].start[c] + blk[k].len[c] > BI.mk)
+          return "BST: a Tucker range exceeds the local basis of its Fock sector";
+        P.gammas.push_back(Q);
+        ga = gamma_at.emplace(key, P.g_total).first;
+        P.g_total += align_up(int64_t(BI.nidx) * blk[b].rank[c] * blk[k].rank[c]);
+      }
+      T.g_off[o] = ga->second;
+      T.np[o] = BI.nidx;
+    }
+    gt[g].push_back(T);
+    return std::string();
+  };
+  if (given) {
+    // the caller's triples {bra, ket, term}, taken in bra order (the groups of one bra block
+    // must be contiguous); each is checked as check_term would
+    std::vector<int64_t> order(static_cast<size_t>(n_given));
+    for (int64_t q = 0; q < n_given; ++q) order[size_t(q)] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return given[3 * x] < given[3 * y]; });
+    std::unordered_map<uint64_t, int32_t> grp;
+    int64_t cur_bra = -1;
+    for (int64_t q : order) {
+      const int32_t* tq = given + 3 * q;
+      const int64_t b = tq[0];
+      const int32_t k = tq[1];
+      const int t = tq[2];
+      if (b < 0 || b >= nb || k < 0 || k >= nb || t < 0 || t >= ctx->n_terms) return "BST: a given triple is out of range";
+      if (b != cur_bra) {
+        grp.clear();
+        cur_bra = b;
+      }
+      const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+      if (r[0] > nbody) return "BST: a given triple's term has more than nbody clusters";
+      const int16_t* fb = fock + 2 * N * b;
+      const int16_t* fkk = fock + 2 * N * k;
+      int mask = 0;
+      for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
+      for (int c = 0; c < N; ++c) {
+        for (int s2 = 0; s2 < 2; ++s2)
+          if (fb[2 * c + s2] - fkk[2 * c + s2] != ctx->trans[(int64_t(r[1]) * N + c) * 2 + s2])
+            return "BST: a given triple's Fock sectors do not differ by its term's transfer";
+        if (!((mask >> c) & 1) && (blk[b].start[c] != blk[k].start[c] || blk[b].len[c] != blk[k].len[c]))
+          return "BST: a given triple fails check_term on the spectator ranges";
+      }
+      int tdm[4];
+      for (int o = 0; o < r[0]; ++o) {
+        const int c = r[2 + o];
+        tdm[o] = ctx->h_blk_index[dense_block_index(nmax1, c, r[6 + o], fb[2 * c], fb[2 * c + 1], fkk[2 * c],
+                                                    fkk[2 * c + 1])];
+        if (tdm[o] < 0) return "BST: a given triple needs a TDM block that does not exist";
+      }
+      std::string msg = add_triple(b, k, t, r, mask, tdm, term_state_sign(r, fkk), grp);
+      if (!msg.empty()) return msg;
+    }
+  } else {
   std::vector<int16_t> fk(2 * N);
   for (int64_t b = 0; b < nb; ++b) {
     const int16_t* fb = fock + 2 * N * b;
@@ -563,55 +656,15 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
         const int sign = term_state_sign(r, fk.data());
         for (int32_t k : it->second) {
           if (!matches(b, fk.data(), k, mask)) continue;
-          P.triples.insert(P.triples.end(), {int32_t(b), k, int32_t(t), int32_t(sign)});
-          const uint64_t gk = (uint64_t(uint32_t(k)) << 8) | uint64_t(mask);
-          auto gi = grp.find(gk);
-          int32_t g;
-          if (gi == grp.end()) {
-            g = int32_t(P.groups.size());
-            grp[gk] = g;
-            BstGroup G{};
-            G.bra = int32_t(b);
-            G.ket = k;
-            G.act_mask = mask;
-            P.groups.push_back(G);
-            gt.emplace_back();
-          } else {
-            g = gi->second;
+          {
+            std::string msg = add_triple(b, k, t, r, mask, tdm, sign, grp);
+            if (!msg.empty()) return msg;
           }
-          BstGroupTerm T{};
-          T.nact = r[0];
-          T.sign = sign;
-          T.ints_off = r[0] == 1 ? -1 : ctx->terms[t].ints_off;
-          for (int o = 0; o < r[0]; ++o) {
-            const int c = r[2 + o];
-            const BlockInfo& BI = ctx->h_blocks[tdm[o]];
-            if (r[0] > 1 && BI.nidx != r[22 + o]) return "BST: TDM multi-index length differs from the term's ints";
-            const uint64_t key = ((uint64_t(b) * uint64_t(nb) + uint64_t(k)) * 8 + uint64_t(c)) * 32 + uint64_t(r[6 + o]);
-            auto ga = gamma_at.find(key);
-            if (ga == gamma_at.end()) {
-              BstGamma Q{};
-              Q.g_off = P.g_total;
-              Q.tdm_off = BI.off;
-              Q.bra = int32_t(b);
-              Q.ket = k;
-              Q.c = c;
-              Q.np = BI.nidx;
-              Q.tdm_mb = BI.mb;
-              if (blk[b].start[c] + blk[b].len[c] > BI.mb || blk[k].start[c] + blk[k].len[c] > BI.mk)
-                return "BST: a Tucker range exceeds the local basis of its Fock sector";
-              P.gammas.push_back(Q);
-              ga = gamma_at.emplace(key, P.g_total).first;
-              P.g_total += align_up(int64_t(BI.nidx) * blk[b].rank[c] * blk[k].rank[c]);
-            }
-            T.g_off[o] = ga->second;
-            T.np[o] = BI.nidx;
-          }
-          gt[g].push_back(T);
         }
       }
     }
   }
+  }  // enumeration
   // group operators, spectator overlaps, workspace sizes and flop counts
   for (size_t g = 0; g < P.groups.size(); ++g) {
     BstGroup& G = P.groups[g];
@@ -854,10 +907,9 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
 
 }  // namespace
 
-extern "C" {
-
-int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
-                const int64_t* factor_off, int64_t n_factors, const double* factors, int64_t* core_total) {
+int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
+                 const int64_t* factor_off, int64_t n_factors, const double* factors, const int32_t* triples,
+                 int64_t n_triples, int64_t* core_total) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_ops && ctx->have_terms, FCG_ESTATE, "upload ops and terms first");
   FCG_REQUIRE(n_blocks > 0 && fock && blocks && factor_off && factors && core_total && n_factors > 0, FCG_EINVAL,
@@ -896,7 +948,7 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
   }
   BstPlan P;
   {
-    std::string msg = plan_bst(ctx, nbody, blk, fock, P);
+    std::string msg = plan_bst(ctx, nbody, blk, fock, P, triples, n_triples);
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
   const double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -963,6 +1015,13 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
   ctx->stats.bst_plan_seconds = plan_s;
   ctx->have_bst = true;
   return FCG_OK;
+}
+
+extern "C" {
+
+int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
+                const int64_t* factor_off, int64_t n_factors, const double* factors, int64_t* core_total) {
+  return bst_set_impl(ctx, nbody, n_blocks, fock, blocks, factor_off, n_factors, factors, nullptr, 0, core_total);
 }
 
 int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision) {

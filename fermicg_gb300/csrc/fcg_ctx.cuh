@@ -95,6 +95,7 @@ struct fcg_ctx {
   int n_terms = 0;
   std::vector<int32_t> trm;
   std::vector<TermInfo> terms;
+  std::vector<double> term_ints_norm;  // Frobenius norm of each term's integrals (0 for 1-body terms)
   std::vector<TermDress> dress;
   std::vector<int64_t> w_index;
   int64_t n_w = 0;
@@ -172,6 +173,14 @@ struct fcg_ctx {
   DevBuf<float> d_bst_op32, d_bst_s32;
   DevBuf<double> d_bst_in64, d_bst_out64, d_bst_ws64;
   DevBuf<float> d_bst_in32, d_bst_out32, d_bst_ws32;
+  // the last compressed first-order space (bst_fois.cu), in the fcg_bst_set layout
+  struct {
+    int R = 0;
+    int64_t n_blocks = 0, core_total = 0;
+    std::vector<int16_t> fock;
+    std::vector<int64_t> blocks, factor_off;
+    std::vector<double> factors, cores;
+  } fois;
   fcg_stats stats{};
 };
 
@@ -179,6 +188,12 @@ struct fcg_ctx {
 // host wait of fcg_sigma_closed_device; for drivers that keep working on the same stream
 // (fcg_gpu.cu)
 int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
+
+// fcg_bst_set with an optional caller-given triple list {bra, ket, term} (n_triples of them)
+// in place of the check_term enumeration (bst.cu)
+int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
+                 const int64_t* factor_off, int64_t n_factors, const double* factors, const int32_t* triples,
+                 int64_t n_triples, int64_t* core_total);
 
 #define FCG_CUDA(call)                                                               \
   do {                                                                               \

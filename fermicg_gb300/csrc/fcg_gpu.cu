@@ -774,6 +774,16 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
     tm.ints_off = int64_t(uint32_t(r[26])) | (int64_t(r[27]) << 32);
     if (r[0] > 1) FCG_REQUIRE(tm.ints_off >= 0 && tm.ints_off + len <= n_ints, FCG_EINVAL, "term ints out of range");
   }
+  ctx->term_ints_norm.assign(size_t(n_terms), 0.0);
+  for (int t = 0; t < n_terms; ++t) {
+    const int32_t* r = term_table + int64_t(t) * kTrmCols;
+    if (r[0] < 2) continue;
+    int64_t len = 1;
+    for (int o = 0; o < r[0]; ++o) len *= r[22 + o];
+    double s2 = 0.0;
+    for (int64_t i = 0; i < len; ++i) s2 += ints[ctx->terms[t].ints_off + i] * ints[ctx->terms[t].ints_off + i];
+    ctx->term_ints_norm[size_t(t)] = std::sqrt(s2);
+  }
   std::vector<DressJob> jobs;
   int64_t w_total = 0;
   {

@@ -52,6 +52,9 @@ SIGNATURES = {
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
     "fcg_expectation": (_I, [_P, _I, _P, _P, _I]),
     "fcg_build_full_h": (_I, [_P, _P]),
+    "fcg_bst_fois": (_I, [_P, _I, _I, ctypes.c_double, _I, _L, _P, _P, _P, _L, _P, _P, _P, ctypes.POINTER(_L),
+                          ctypes.POINTER(_L), ctypes.POINTER(_L)]),
+    "fcg_bst_fois_get": (_I, [_P, _P, _P, _P, _P, _P]),
 }
 
 
@@ -66,7 +69,8 @@ class Stats(ctypes.Structure):
                 ("bst_triples", ctypes.c_int64), ("bst_groups", ctypes.c_int64),
                 ("bst_cache_elements", ctypes.c_int64), ("bst_flops_reference", ctypes.c_int64),
                 ("bst_flops_executed", ctypes.c_int64), ("bst_cache_seconds", ctypes.c_double),
-                ("bst_plan_seconds", ctypes.c_double)]
+                ("bst_plan_seconds", ctypes.c_double), ("bst_fois_items", ctypes.c_int64),
+                ("bst_fois_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -252,6 +256,18 @@ class GpuSigma:
         self.bst_core_total = ct.value
         return ct.value
 
+    def bst_set_raw(self, fock, blocks, factor_off, factors, nbody=4):
+        """fcg_bst_set on arrays in its own layout (blocks [n][3N] = {rank, start, len})."""
+        f = np.ascontiguousarray(fock, dtype=np.int16)
+        bl = np.ascontiguousarray(blocks, dtype=np.int64)
+        fo = np.ascontiguousarray(factor_off, dtype=np.int64)
+        fa = np.ascontiguousarray(factors, dtype=np.float64)
+        ct = ctypes.c_int64(0)
+        self._check(self.L.fcg_bst_set(self.h, int(nbody), bl.shape[0], _ptr(f), _ptr(bl), _ptr(fo), fa.size, _ptr(fa),
+                                       ctypes.byref(ct)), "fcg_bst_set")
+        self.bst_core_total = ct.value
+        return ct.value
+
     def bst_sigma(self, cores, precision="fp64"):
         """build_sigma!: cores (R, core_total) -> sigma cores (R, core_total) float64."""
         c = np.ascontiguousarray(cores, dtype=np.float64)
@@ -271,6 +287,31 @@ class GpuSigma:
         out = np.zeros((n, 4), dtype=np.int32)
         self._check(self.L.fcg_bst_triples(self.h, _ptr(out)), "fcg_bst_triples")
         return out
+
+    def bst_fois(self, fock, blocks, factor_off, factors, cores, spaces, thresh, nbody=4, compress_twice=True):
+        """build_compressed_1st_order_state on the device (fcg_bst_fois).  Inputs in the
+        fcg_bst_set layout (blocks [n][3N] = {rank, start, len}), cores (R, core_total), spaces
+        int32 [N][nmax+1][nmax+1][4].  Returns (fock, blocks, factor_off, factors, cores)."""
+        f = np.ascontiguousarray(fock, dtype=np.int16)
+        bl = np.ascontiguousarray(blocks, dtype=np.int64)
+        fo = np.ascontiguousarray(factor_off, dtype=np.int64)
+        fa = np.ascontiguousarray(factors, dtype=np.float64)
+        co = np.ascontiguousarray(cores, dtype=np.float64)
+        sp = np.ascontiguousarray(spaces, dtype=np.int32)
+        R = co.shape[0]
+        nb, ct, nf = ctypes.c_int64(0), ctypes.c_int64(0), ctypes.c_int64(0)
+        self._check(self.L.fcg_bst_fois(self.h, R, int(nbody), float(thresh), int(bool(compress_twice)), bl.shape[0],
+                                        _ptr(f), _ptr(bl), _ptr(fo), fa.size, _ptr(fa), _ptr(co), _ptr(sp),
+                                        ctypes.byref(nb), ctypes.byref(ct), ctypes.byref(nf)), "fcg_bst_fois")
+        N = self.N
+        of = np.zeros((nb.value, N, 2), dtype=np.int16)
+        ob = np.zeros((nb.value, 3 * N), dtype=np.int64)
+        oo = np.zeros((nb.value, N), dtype=np.int64)
+        ofa = np.zeros(max(nf.value, 1))
+        oc = np.zeros((R, max(ct.value, 1)))
+        self._check(self.L.fcg_bst_fois_get(self.h, _ptr(of), _ptr(ob), _ptr(oo), _ptr(ofa), _ptr(oc)),
+                    "fcg_bst_fois_get")
+        return of, ob, oo, ofa[:nf.value], oc[:, :ct.value]
 
     def stats(self):
         s = Stats()

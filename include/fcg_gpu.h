@@ -70,6 +70,8 @@ typedef struct fcg_stats {
   int64_t bst_flops_executed;  /* per root: the same sums over groups (what one fcg_bst_sigma root does) */
   double bst_cache_seconds; /* wall time of the last fcg_bst_set (planning + operator cache) */
   double bst_plan_seconds;  /* of which host planning (triples, groups, cache layout) */
+  int64_t bst_fois_items;   /* (term, ket block, target TuckerConfig) contributions of the last fcg_bst_fois */
+  double bst_fois_seconds;  /* wall time of the last fcg_bst_fois */
 } fcg_stats;
 
 int fcg_version(void);
@@ -191,6 +193,28 @@ int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_s
 /* The triples of the last fcg_bst_set: int32 [bst_triples][4] = {bra block, ket block,
  * term index (term-table row), state sign}. */
 int fcg_bst_triples(fcg_ctx* ctx, int32_t* out);
+
+/* The compressed first-order interacting space of a BST state: build_compressed_1st_order_state
+ * (src/tucker_outer.jl:717-910) with form_sigma_block_expand (src/tucker_form_sigma_block_expand.jl
+ * :7-722; 3- and 4-body local operators truncated by SVD, precontract = true), the HOSVD
+ * compressions (compress, src/hosvd.jl:337-349) and nonorth_add (src/hosvd.jl:83-156), and a
+ * final compress_iteratively (src/type_BSTstate.jl:283-296).  The state is given in the
+ * fcg_bst_set layout with R roots of cores [R][core_total]; `spaces` holds each cluster's P and Q
+ * ranges per local Fock sector, int32 [N][nmax+1][nmax+1][4] = {p_start, p_len, q_start, q_len}
+ * (0-based, length 0: absent), as BSTstate.p_spaces / q_spaces.  thresh is the reference's
+ * `thresh` (HOSVD threshold and prescreen), compress_twice its flag.  The result stays in the
+ * context; its sizes go to *out_n_blocks, *out_core_total (per root) and *out_n_factors, and
+ * fcg_bst_fois_get copies it out.  The context's BST structure (fcg_bst_set) is replaced by the
+ * expansion's. */
+int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twice, int64_t n_blocks,
+                 const int16_t* fock, const int64_t* blocks, const int64_t* factor_off, int64_t n_factors,
+                 const double* factors, const double* cores, const int32_t* spaces, int64_t* out_n_blocks,
+                 int64_t* out_core_total, int64_t* out_n_factors);
+
+/* The last fcg_bst_fois result in the fcg_bst_set layout: fock [n][N][2], blocks [n][3N]
+ * {rank, start, len}, factor_off [n][N], factors [n_factors], cores [R][core_total]. */
+int fcg_bst_fois_get(fcg_ctx* ctx, int16_t* fock, int64_t* blocks, int64_t* factor_off, double* factors,
+                     double* cores);
 
 /* Allocation-free variant of fcg_sigma_closed_device (no counterpart in the reference).
  * For callers that cannot call cudaMalloc/cudaFree during a solve: applications whose
