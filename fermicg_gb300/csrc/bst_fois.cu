@@ -38,7 +38,7 @@ using namespace fcg_tucker;
 
 namespace {
 
-constexpr int kFoisThreads = 64;
+constexpr int kCtaThreads = 128;  // threads of the CTA that works on one small problem
 
 // One Tucker tensor of a batch: the core of root r starts at core_off + r * stride (stride is
 // the batch's), column-major with dims rank[0..N); factor m is (dim[m] x rank[m]) column-major.
@@ -60,75 +60,113 @@ struct PrecJob {
   double scale1;     // max(1, max_r |ket core_r|) * |ints|
 };
 
-__global__ void fois_precontract_kernel(int n, const PrecJob* __restrict__ jobs, const double* __restrict__ tdm,
-                                        const double* __restrict__ fac, double prescreen, double* __restrict__ out,
-                                        int32_t* __restrict__ nkeep, double* __restrict__ work) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const PrecJob J = jobs[i];
-  const int bl = J.bra_len, PL = J.np * J.L;
-  double* D = work + J.work_off;           // bl x PL
-  double* G = D + int64_t(bl) * PL;        // bl x bl
-  double* V = G + bl * bl;                 // bl x bl
-  double* w = V + bl * bl;                 // bl
-  const double* Gm = tdm + J.tdm_off;
-  const double* U = fac + J.kfac_off;
-  for (int l = 0; l < J.L; ++l)
-    for (int p = 0; p < J.np; ++p)
-      for (int I = 0; I < bl; ++I) {
-        double s = 0.0;
-        for (int q = 0; q < J.ket_len; ++q)
-          s += Gm[p + int64_t(J.np) * ((J.bra_start + I) + int64_t(J.mb) * (J.ket_start + q))] *
-               U[q + int64_t(J.ket_len) * l];
-        D[I + int64_t(bl) * (p + int64_t(J.np) * l)] = s;
-      }
-  for (int b = 0; b < bl; ++b)
-    for (int a = 0; a <= b; ++a) {
-      double s = 0.0;
-      for (int64_t e = 0; e < PL; ++e) s += D[a + bl * e] * D[b + bl * e];
-      G[a + bl * b] = s;
-      G[b + bl * a] = s;
-    }
-  jacobi_eigh_desc(bl, G, w, V);
-  int k = 0;
-  for (int a = 0; a < bl; ++a)
-    if (sqrt(fabs(w[a])) * J.scale1 > prescreen) ++k;
-  for (int j = 0; j < k; ++j)
-    for (int a = 0; a < bl; ++a) out[J.out_off + a + int64_t(bl) * j] = V[a + bl * j];
-  nkeep[i] = k;
+// Shared memory of one CTA working on one small problem: the d x d matrix and eigenvectors,
+// eigenvalues, rotation pairs, two flags, a reduction row and the eigenvalue order.
+struct CtaSmem {
+  double *A, *V, *w, *cs, *red, *row;
+  int* perm;
+};
+
+__device__ inline CtaSmem carve(double* sm, int dmax) {
+  CtaSmem S;
+  S.A = sm;
+  S.V = S.A + dmax * dmax;
+  S.w = S.V + dmax * dmax;
+  S.cs = S.w + dmax;
+  S.red = S.cs + dmax + 2;
+  S.row = S.red + 4;
+  S.perm = reinterpret_cast<int*>(S.row + kCtaThreads);
+  return S;
 }
 
-// HOSVD truncation (tucker_decompose + compress, src/hosvd.jl:337-545): per mode the
-// eigenvectors of the summed Gram matrix of the R cores with sqrt|eigenvalue| > thresh; the
-// cores projected onto them, the factors multiplied by them.  out_rank[t][m] receives the
-// new ranks (a 0 anywhere: the tensor vanished).  Scratch per tensor: Gram, eigenvectors and
-// eigenvalues (max rank^2, max rank^2, max rank), the kept vectors of every mode
-// (sum rank_m^2) and two core buffers of the input core length.
-__global__ void tucker_compress_kernel(int n, int N, int R, double thresh, const TuckDesc* __restrict__ in,
-                                       int64_t in_stride, const double* __restrict__ in_core,
-                                       const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank,
-                                       const TuckDesc* __restrict__ out, int64_t out_stride,
-                                       double* __restrict__ out_core, double* __restrict__ out_fac,
-                                       int32_t* __restrict__ out_rank, double* __restrict__ work) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+size_t cta_smem_bytes(int dmax) {
+  return sizeof(double) * (2 * size_t(dmax) * dmax + 2 * size_t(dmax) + 6 + kCtaThreads) + sizeof(int) * size_t(dmax);
+}
+
+// One CTA per job: g[I, (p, l)] = sum_J G[p, start_b + I, start_k + J] U_ket[J, l] in the job's
+// scratch, its Gram matrix over I, the eigenvectors with sqrt|eigenvalue| * scale1 > prescreen
+// (the left singular vectors of the reference's SVD, largest first) to out.
+__global__ void __launch_bounds__(kCtaThreads) fois_precontract_kernel(int n, const PrecJob* __restrict__ jobs,
+                                                                      const double* __restrict__ tdm,
+                                                                      const double* __restrict__ fac, double prescreen,
+                                                                      double* __restrict__ out,
+                                                                      int32_t* __restrict__ nkeep,
+                                                                      double* __restrict__ work, int dmax) {
+  extern __shared__ double sm[];
+  const int i = blockIdx.x;
+  if (i >= n) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const CtaSmem S = carve(sm, dmax);
+  const PrecJob J = jobs[i];
+  const int bl = J.bra_len;
+  const int64_t PL = int64_t(J.np) * J.L;
+  double* D = work + J.work_off;
+  const double* Gm = tdm + J.tdm_off;
+  const double* U = fac + J.kfac_off;
+  for (int64_t e = tid; e < int64_t(bl) * PL; e += nt) {
+    const int I = int(e % bl);
+    const int64_t pl = e / bl;
+    const int p = int(pl % J.np), l = int(pl / J.np);
+    double s = 0.0;
+    for (int q = 0; q < J.ket_len; ++q)
+      s += Gm[p + int64_t(J.np) * ((J.bra_start + I) + int64_t(J.mb) * (J.ket_start + q))] *
+           U[q + int64_t(J.ket_len) * l];
+    D[e] = s;
+  }
+  __syncthreads();
+  for (int pp = tid; pp < bl * (bl + 1) / 2; pp += nt) {
+    int b = int((sqrt(8.0 * pp + 1.0) - 1.0) * 0.5);
+    while (b * (b + 1) / 2 > pp) --b;
+    while ((b + 1) * (b + 2) / 2 <= pp) ++b;
+    const int a = pp - b * (b + 1) / 2;
+    double s = 0.0;
+    for (int64_t e = 0; e < PL; ++e) s += D[a + bl * e] * D[b + bl * e];
+    S.A[a + bl * b] = s;
+    S.A[b + bl * a] = s;
+  }
+  __syncthreads();
+  coop_jacobi_eigh(bl, S.A, S.w, S.V, S.perm, S.cs, S.red, tid, nt);
+  if (tid == 0) {
+    int k = 0;
+    for (int a = 0; a < bl; ++a)
+      if (sqrt(fabs(S.w[a])) * J.scale1 > prescreen) ++k;
+    S.red[1] = k;
+    nkeep[i] = k;
+  }
+  __syncthreads();
+  const int k = int(S.red[1]);
+  for (int e = tid; e < bl * k; e += nt) {
+    const int a = e % bl, j = e / bl;
+    out[J.out_off + e] = S.V[a + bl * S.perm[j]];
+  }
+}
+
+// HOSVD truncation (tucker_decompose + compress, src/hosvd.jl:337-545), one CTA per tensor: per
+// mode the eigenvectors of the summed Gram matrix of the R cores with sqrt|eigenvalue| > thresh;
+// the cores projected onto them, the factors multiplied by them.  out_rank[t][m] receives the
+// new ranks (a 0 anywhere: the tensor vanished).  Global scratch per tensor: the kept vectors
+// of every mode (sum rank_m^2) and two core buffers of the input core length.
+__global__ void __launch_bounds__(kCtaThreads) tucker_compress_kernel(
+    int n, int N, int R, double thresh, const TuckDesc* __restrict__ in, int64_t in_stride,
+    const double* __restrict__ in_core, const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank,
+    const TuckDesc* __restrict__ out, int64_t out_stride, double* __restrict__ out_core, double* __restrict__ out_fac,
+    int32_t* __restrict__ out_rank, double* __restrict__ work, int dmax) {
+  extern __shared__ double sm[];
+  const int t = blockIdx.x;
   if (t >= n) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const CtaSmem S = carve(sm, dmax);
   const TuckDesc A = in[t];
   const TuckDesc O = out[t];
   int32_t dims[kTuckMaxModes], k[kTuckMaxModes];
-  int dmax = 1;
-  for (int m = 0; m < N; ++m) {
-    dims[m] = in_rank ? in_rank[int64_t(t) * N + m] : A.rank[m];
-    dmax = max(dmax, int(dims[m]));
-  }
+  for (int m = 0; m < N; ++m) dims[m] = in_rank ? in_rank[int64_t(t) * N + m] : A.rank[m];
   const int64_t len = tensor_len(dims, N);
   if (len == 0) {
-    for (int m = 0; m < N; ++m) out_rank[int64_t(t) * N + m] = 0;
+    if (tid == 0)
+      for (int m = 0; m < N; ++m) out_rank[int64_t(t) * N + m] = 0;
     return;
   }
-  double* G = work + A.work_off;
-  double* V = G + dmax * dmax;
-  double* w = V + dmax * dmax;
-  double* W = w + dmax;  // kept vectors of mode m at W + wo[m]
+  double* W = work + A.work_off;
   int64_t wo[kTuckMaxModes];
   int64_t acc = 0;
   for (int m = 0; m < N; ++m) {
@@ -140,17 +178,26 @@ __global__ void tucker_compress_kernel(int n, int N, int R, double thresh, const
   bool empty = false;
   for (int m = 0; m < N; ++m) {
     const int d = dims[m];
-    for (int r = 0; r < R; ++r) mode_gram(in_core + A.core_off + r * in_stride, dims, N, m, G, r > 0);
-    jacobi_eigh_desc(d, G, w, V);
-    int nk = 0;
-    for (int a = 0; a < d; ++a)
-      if (sqrt(fabs(w[a])) > thresh) ++nk;
-    for (int j = 0; j < nk; ++j)
-      for (int a = 0; a < d; ++a) W[wo[m] + a + int64_t(d) * j] = V[a + d * j];
+    for (int r = 0; r < R; ++r) coop_mode_gram(in_core + A.core_off + r * in_stride, dims, N, m, S.A, r > 0, tid, nt);
+    coop_jacobi_eigh(d, S.A, S.w, S.V, S.perm, S.cs, S.red, tid, nt);
+    if (tid == 0) {
+      int nk = 0;
+      for (int a = 0; a < d; ++a)
+        if (sqrt(fabs(S.w[a])) > thresh) ++nk;
+      S.red[1] = nk;
+    }
+    __syncthreads();
+    const int nk = int(S.red[1]);
+    for (int e = tid; e < d * nk; e += nt) {
+      const int a = e % d, j = e / d;
+      W[wo[m] + e] = S.V[a + d * S.perm[j]];
+    }
+    __syncthreads();
     k[m] = nk;
     if (nk == 0) empty = true;
   }
-  for (int m = 0; m < N; ++m) out_rank[int64_t(t) * N + m] = k[m];
+  if (tid == 0)
+    for (int m = 0; m < N; ++m) out_rank[int64_t(t) * N + m] = k[m];
   if (empty) return;
   const int64_t nlen = tensor_len(k, N);
   for (int r = 0; r < R; ++r) {
@@ -159,50 +206,66 @@ __global__ void tucker_compress_kernel(int n, int N, int R, double thresh, const
     const double* src = in_core + A.core_off + r * in_stride;
     double* dst = buf0;
     for (int m = 0; m < N; ++m) {
-      mode_product_t(src, cur, N, m, W + wo[m], dims[m], k[m], dst);
+      coop_mode_product_t(src, cur, N, m, W + wo[m], dims[m], k[m], dst, tid, nt);
       cur[m] = k[m];
       src = dst;
       dst = (dst == buf0) ? buf1 : buf0;
     }
     double* o = out_core + O.core_off + r * out_stride;
-    for (int64_t e = 0; e < nlen; ++e) o[e] = src[e];
+    for (int64_t e = tid; e < nlen; e += nt) o[e] = src[e];
+    __syncthreads();
   }
-  for (int m = 0; m < N; ++m)
-    matmul(in_fac + A.fac_off[m], W + wo[m], A.dim[m], dims[m], k[m], out_fac + O.fac_off[m]);
+  for (int m = 0; m < N; ++m) {
+    const int rows = A.dim[m], d = dims[m];
+    const double* F = in_fac + A.fac_off[m];
+    for (int e = tid; e < rows * k[m]; e += nt) {
+      const int i = e % rows, j = e / rows;
+      double s = 0.0;
+      for (int q = 0; q < d; ++q) s += F[i + int64_t(rows) * q] * W[wo[m] + q + int64_t(d) * j];
+      out_fac[O.fac_off[m] + e] = s;
+    }
+  }
 }
 
 // nonorth_add (src/hosvd.jl:83-156) of the tensors members[ptr[g] .. ptr[g+1]) that are not
-// empty: taken by decreasing norm; per mode the left singular vectors of the stacked factors
-// with singular value > thresh (from the eigen-decomposition of their Gram matrix, ignoring
-// eigenvalues at rounding level); the sum of the members' cores transformed into those
-// bases.  A single member is copied.  Scratch per block (host-sized): member order, Gram,
-// eigenvectors, eigenvalues, the new factors, one transform and two core buffers.
-__global__ void tucker_add_kernel(int ng, int N, int R, double thresh, const int64_t* __restrict__ ptr,
-                                  const int32_t* __restrict__ members, const TuckDesc* __restrict__ in,
-                                  int64_t in_stride, const double* __restrict__ in_core,
-                                  const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank,
-                                  const TuckDesc* __restrict__ out, int64_t out_stride,
-                                  double* __restrict__ out_core, double* __restrict__ out_fac,
-                                  int32_t* __restrict__ out_rank, double* __restrict__ work,
-                                  const int64_t* __restrict__ work_off, const int64_t* __restrict__ buf_len) {
-  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+// empty, one CTA per target block: taken by decreasing norm; per mode the left singular vectors
+// of the stacked factors with singular value > thresh (from the eigen-decomposition of their
+// Gram matrix, ignoring eigenvalues at rounding level); the sum of the members' cores
+// transformed into those bases.  A single member is copied.  Global scratch per block
+// (host-sized): member order and norms, one transform and two core buffers.
+__global__ void __launch_bounds__(kCtaThreads) tucker_add_kernel(
+    int ng, int N, int R, double thresh, const int64_t* __restrict__ ptr, const int32_t* __restrict__ members,
+    const TuckDesc* __restrict__ in, int64_t in_stride, const double* __restrict__ in_core,
+    const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank, const TuckDesc* __restrict__ out,
+    int64_t out_stride, double* __restrict__ out_core, double* __restrict__ out_fac, int32_t* __restrict__ out_rank,
+    double* __restrict__ work, const int64_t* __restrict__ work_off, const int64_t* __restrict__ buf_len, int dmax) {
+  extern __shared__ double sm[];
+  const int g = blockIdx.x;
   if (g >= ng) return;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const CtaSmem S = carve(sm, dmax);
   const TuckDesc O = out[g];
+  const int64_t nmem = ptr[g + 1] - ptr[g];
   double* ord = work + work_off[g];  // member ids (exact in a double) in the order of addition
-  int nval = 0;
-  for (int64_t q = ptr[g]; q < ptr[g + 1]; ++q) {
-    const int32_t t = members[q];
-    int64_t l = 1;
-    for (int m = 0; m < N; ++m) l *= in_rank[int64_t(t) * N + m];
-    if (l > 0) ord[nval++] = double(t);
+  double* nrm = ord + nmem;
+  if (tid == 0) {
+    int nv = 0;
+    for (int64_t q = ptr[g]; q < ptr[g + 1]; ++q) {
+      const int32_t t = members[q];
+      int64_t l = 1;
+      for (int m = 0; m < N; ++m) l *= in_rank[int64_t(t) * N + m];
+      if (l > 0) ord[nv++] = double(t);
+    }
+    S.red[1] = nv;
   }
+  __syncthreads();
+  const int nval = int(S.red[1]);
   if (nval == 0) {
-    for (int m = 0; m < N; ++m) out_rank[int64_t(g) * N + m] = 0;
+    if (tid == 0)
+      for (int m = 0; m < N; ++m) out_rank[int64_t(g) * N + m] = 0;
     return;
   }
-  // norms, then a stable insertion sort by decreasing norm
-  double* nrm = ord + nval;
-  for (int a = 0; a < nval; ++a) {
+  for (int a = 0; a < nval; ++a) {  // norms over all roots
     const int32_t t = int32_t(ord[a]);
     int32_t dims[kTuckMaxModes];
     for (int m = 0; m < N; ++m) dims[m] = in_rank[int64_t(t) * N + m];
@@ -210,105 +273,124 @@ __global__ void tucker_add_kernel(int ng, int N, int R, double thresh, const int
     double s = 0.0;
     for (int r = 0; r < R; ++r) {
       const double* c = in_core + in[t].core_off + r * in_stride;
-      for (int64_t e = 0; e < l; ++e) s += c[e] * c[e];
+      for (int64_t e = tid; e < l; e += nt) s += c[e] * c[e];
     }
-    nrm[a] = sqrt(s);
-  }
-  for (int a = 1; a < nval; ++a) {
-    const double kn = nrm[a], kt = ord[a];
-    int b = a - 1;
-    while (b >= 0 && nrm[b] < kn) {
-      nrm[b + 1] = nrm[b];
-      ord[b + 1] = ord[b];
-      --b;
+    S.row[tid] = s;
+    __syncthreads();
+    if (tid == 0) {
+      double tot = 0.0;
+      for (int q = 0; q < nt; ++q) tot += S.row[q];
+      nrm[a] = sqrt(tot);
     }
-    nrm[b + 1] = kn;
-    ord[b + 1] = kt;
+    __syncthreads();
   }
-  const int32_t t0 = int32_t(ord[0]);
+  if (tid == 0)  // stable insertion sort by decreasing norm
+    for (int a = 1; a < nval; ++a) {
+      const double kn = nrm[a], kt = ord[a];
+      int b = a - 1;
+      while (b >= 0 && nrm[b] < kn) {
+        nrm[b + 1] = nrm[b];
+        ord[b + 1] = ord[b];
+        --b;
+      }
+      nrm[b + 1] = kn;
+      ord[b + 1] = kt;
+    }
+  __syncthreads();
   if (nval == 1) {
+    const int32_t t0 = int32_t(ord[0]);
     int32_t dims[kTuckMaxModes];
     for (int m = 0; m < N; ++m) dims[m] = in_rank[int64_t(t0) * N + m];
     const int64_t l = tensor_len(dims, N);
     for (int r = 0; r < R; ++r)
-      for (int64_t e = 0; e < l; ++e)
+      for (int64_t e = tid; e < l; e += nt)
         out_core[O.core_off + r * out_stride + e] = in_core[in[t0].core_off + r * in_stride + e];
     for (int m = 0; m < N; ++m) {
       const int64_t fl = int64_t(in[t0].dim[m]) * dims[m];
-      for (int64_t e = 0; e < fl; ++e) out_fac[O.fac_off[m] + e] = in_fac[in[t0].fac_off[m] + e];
-      out_rank[int64_t(g) * N + m] = dims[m];
+      for (int64_t e = tid; e < fl; e += nt) out_fac[O.fac_off[m] + e] = in_fac[in[t0].fac_off[m] + e];
     }
+    if (tid == 0)
+      for (int m = 0; m < N; ++m) out_rank[int64_t(g) * N + m] = dims[m];
     return;
   }
-  int dmax = 1;
-  for (int m = 0; m < N; ++m) dmax = max(dmax, int(O.dim[m]));
-  double* G = nrm + nval;
-  double* V = G + dmax * dmax;
-  double* w = V + dmax * dmax;
-  double* M = w + dmax;            // transform (r x k), at most dmax x dmax
+  double* M = nrm + nmem;  // transform (r x k), at most dmax x dmax
   double* buf0 = M + dmax * dmax;
   double* buf1 = buf0 + buf_len[g];
   int32_t k[kTuckMaxModes];
   bool empty = false;
   for (int m = 0; m < N; ++m) {
     const int d = O.dim[m];
-    for (int e = 0; e < d * d; ++e) G[e] = 0.0;
-    for (int a = 0; a < nval; ++a) {
-      const int32_t t = int32_t(ord[a]);
-      const int rt = in_rank[int64_t(t) * N + m];
-      const double* F = in_fac + in[t].fac_off[m];
-      for (int j = 0; j < d; ++j)
-        for (int i = 0; i <= j; ++i) {
-          double s = 0.0;
-          for (int c = 0; c < rt; ++c) s += F[i + int64_t(d) * c] * F[j + int64_t(d) * c];
-          G[i + d * j] += s;
-          if (i != j) G[j + d * i] += s;
-        }
+    for (int pp = tid; pp < d * (d + 1) / 2; pp += nt) {
+      int j = int((sqrt(8.0 * pp + 1.0) - 1.0) * 0.5);
+      while (j * (j + 1) / 2 > pp) --j;
+      while ((j + 1) * (j + 2) / 2 <= pp) ++j;
+      const int i = pp - j * (j + 1) / 2;
+      double s = 0.0;
+      for (int a = 0; a < nval; ++a) {
+        const int32_t t = int32_t(ord[a]);
+        const int rt = in_rank[int64_t(t) * N + m];
+        const double* F = in_fac + in[t].fac_off[m];
+        for (int c = 0; c < rt; ++c) s += F[i + int64_t(d) * c] * F[j + int64_t(d) * c];
+      }
+      S.A[i + d * j] = s;
+      S.A[j + d * i] = s;
     }
-    jacobi_eigh_desc(d, G, w, V);
-    const double floor2 = fmax(thresh * thresh, 64.0 * 2.220446049250313e-16 * fmax(w[0], 0.0));
-    int nk = 0;
-    for (int a = 0; a < d; ++a)
-      if (w[a] > floor2) ++nk;
-    nk = min(nk, int(O.rank[m]));  // the host's capacity (never binding: nk <= both bounds)
-    for (int j = 0; j < nk; ++j)
-      for (int a = 0; a < d; ++a) out_fac[O.fac_off[m] + a + int64_t(d) * j] = V[a + d * j];
+    __syncthreads();
+    coop_jacobi_eigh(d, S.A, S.w, S.V, S.perm, S.cs, S.red, tid, nt);
+    if (tid == 0) {
+      const double floor2 = fmax(thresh * thresh, 64.0 * 2.220446049250313e-16 * fmax(S.w[S.perm[0]], 0.0));
+      int nk = 0;
+      for (int a = 0; a < d; ++a)
+        if (S.w[a] > floor2) ++nk;
+      S.red[1] = min(nk, int(O.rank[m]));  // the host's capacity (never binding)
+    }
+    __syncthreads();
+    const int nk = int(S.red[1]);
+    for (int e = tid; e < d * nk; e += nt) {
+      const int a = e % d, j = e / d;
+      out_fac[O.fac_off[m] + e] = S.V[a + d * S.perm[j]];
+    }
+    __syncthreads();
     k[m] = nk;
     if (nk == 0) empty = true;
   }
-  for (int m = 0; m < N; ++m) out_rank[int64_t(g) * N + m] = k[m];
+  if (tid == 0)
+    for (int m = 0; m < N; ++m) out_rank[int64_t(g) * N + m] = k[m];
   if (empty) return;
   const int64_t nlen = tensor_len(k, N);
   for (int r = 0; r < R; ++r)
-    for (int64_t e = 0; e < nlen; ++e) out_core[O.core_off + r * out_stride + e] = 0.0;
+    for (int64_t e = tid; e < nlen; e += nt) out_core[O.core_off + r * out_stride + e] = 0.0;
+  __syncthreads();
   for (int a = 0; a < nval; ++a) {
     const int32_t t = int32_t(ord[a]);
-    const TuckDesc& A = in[t];
+    const TuckDesc& Ad = in[t];
     int32_t dims[kTuckMaxModes];
     for (int m = 0; m < N; ++m) dims[m] = in_rank[int64_t(t) * N + m];
     for (int r = 0; r < R; ++r) {
       int32_t cur[kTuckMaxModes];
       for (int m = 0; m < N; ++m) cur[m] = dims[m];
-      const double* src = in_core + A.core_off + r * in_stride;
+      const double* src = in_core + Ad.core_off + r * in_stride;
       double* dst = buf0;
       for (int m = 0; m < N; ++m) {
         // M[c + rt * j] = sum_i F_t[i, c] Unew[i, j]  (the transform Unew^T F_t, transposed)
         const int d = O.dim[m], rt = dims[m];
-        const double* F = in_fac + A.fac_off[m];
+        const double* F = in_fac + Ad.fac_off[m];
         const double* Un = out_fac + O.fac_off[m];
-        for (int j = 0; j < k[m]; ++j)
-          for (int c = 0; c < rt; ++c) {
-            double s = 0.0;
-            for (int i = 0; i < d; ++i) s += F[i + int64_t(d) * c] * Un[i + int64_t(d) * j];
-            M[c + rt * j] = s;
-          }
-        mode_product_t(src, cur, N, m, M, rt, k[m], dst);
+        for (int e = tid; e < rt * k[m]; e += nt) {
+          const int c = e % rt, j = e / rt;
+          double s = 0.0;
+          for (int i = 0; i < d; ++i) s += F[i + int64_t(d) * c] * Un[i + int64_t(d) * j];
+          M[e] = s;
+        }
+        __syncthreads();
+        coop_mode_product_t(src, cur, N, m, M, rt, k[m], dst, tid, nt);
         cur[m] = k[m];
         src = dst;
         dst = (dst == buf0) ? buf1 : buf0;
       }
       double* o = out_core + O.core_off + r * out_stride;
-      for (int64_t e = 0; e < nlen; ++e) o[e] += src[e];
+      for (int64_t e = tid; e < nlen; e += nt) o[e] += src[e];
+      __syncthreads();
     }
   }
 }
@@ -346,13 +428,22 @@ void lay_out(TuckBatch& b, int N) {
 
 // scratch of tucker_compress_kernel for a tensor of capacity ranks rk
 int64_t compress_work(const TuckDesc& d, int N) {
-  int64_t dmax = 1, sq = 0, len = 1;
+  int64_t sq = 0, len = 1;
   for (int m = 0; m < N; ++m) {
-    dmax = std::max<int64_t>(dmax, d.rank[m]);
     sq += int64_t(d.rank[m]) * d.rank[m];
     len *= d.rank[m];
   }
-  return 2 * dmax * dmax + dmax + sq + 2 * len;
+  return sq + 2 * len;
+}
+
+// dynamic shared memory of a CTA-per-problem launch with matrices up to dmax x dmax
+template <typename K>
+int cta_smem(K kernel, int dmax, size_t* bytes) {
+  *bytes = cta_smem_bytes(std::max(dmax, 1));
+  if (*bytes > 48 * 1024)
+    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(*bytes)) == cudaSuccess ? 0
+                                                                                                                  : 1;
+  return 0;
 }
 
 int run_compress(fcg_ctx* ctx, int N, int R, double thresh, TuckBatch& in, const int32_t* d_in_rank, TuckBatch& out,
@@ -361,10 +452,14 @@ int run_compress(fcg_ctx* ctx, int N, int R, double thresh, TuckBatch& in, const
   out.desc = in.desc;
   lay_out(out, N);
   int64_t wo = 0;
+  int dmax = 1;
   for (size_t t = 0; t < in.desc.size(); ++t) {
     in.desc[t].work_off = wo;
     wo += compress_work(in.desc[t], N);
+    for (int m = 0; m < N; ++m) dmax = std::max(dmax, int(in.desc[t].rank[m]));
   }
+  size_t smem = 0;
+  FCG_REQUIRE(!cta_smem(tucker_compress_kernel, dmax, &smem), FCG_ECUDA, "FOIS: shared memory attribute");
   FCG_CUDA(in.d_desc.upload(in.desc.data(), in.desc.size(), ctx->stream));
   FCG_CUDA(out.d_desc.upload(out.desc.data(), out.desc.size(), ctx->stream));
   FCG_CUDA(out.core.alloc(size_t(out.stride) * R));
@@ -372,9 +467,9 @@ int run_compress(fcg_ctx* ctx, int N, int R, double thresh, TuckBatch& in, const
   FCG_CUDA(out.rank.alloc(size_t(std::max(n, 1)) * N));
   FCG_CUDA(work.alloc(size_t(std::max<int64_t>(wo, 1))));
   if (n > 0) {
-    tucker_compress_kernel<<<unsigned((n + kFoisThreads - 1) / kFoisThreads), kFoisThreads, 0, ctx->stream>>>(
+    tucker_compress_kernel<<<unsigned(n), kCtaThreads, smem, ctx->stream>>>(
         n, N, R, thresh, in.d_desc.p, in.stride, in.core.p, in.fac.p, d_in_rank, out.d_desc.p, out.stride,
-        out.core.p, out.fac.p, out.rank.p, work.p);
+        out.core.p, out.fac.p, out.rank.p, work.p, dmax);
     FCG_CUDA(cudaGetLastError());
   }
   return FCG_OK;
@@ -613,7 +708,7 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
       J.out_off = pout;
       pout += int64_t(J.bra_len) * J.bra_len;
       J.work_off = pwork;
-      pwork += int64_t(J.bra_len) * J.np * J.L + 2 * int64_t(J.bra_len) * J.bra_len + J.bra_len;
+      pwork += int64_t(J.bra_len) * J.np * J.L;
       pj.push_back(J);
     }
   }
@@ -628,8 +723,12 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     FCG_CUDA(d_pwork.alloc(size_t(std::max<int64_t>(pwork, 1))));
     FCG_CUDA(d_nk.alloc(pj.size()));
     const int n = int(pj.size());
-    fois_precontract_kernel<<<unsigned((n + kFoisThreads - 1) / kFoisThreads), kFoisThreads, 0, ctx->stream>>>(
-        n, d_pj.p, ctx->d_op64.p, d_kfac.p, thresh, d_pfac.p, d_nk.p, d_pwork.p);
+    int dmax = 1;
+    for (const PrecJob& J : pj) dmax = std::max(dmax, J.bra_len);
+    size_t smem = 0;
+    FCG_REQUIRE(!cta_smem(fois_precontract_kernel, dmax, &smem), FCG_ECUDA, "FOIS: shared memory attribute");
+    fois_precontract_kernel<<<unsigned(n), kCtaThreads, smem, ctx->stream>>>(n, d_pj.p, ctx->d_op64.p, d_kfac.p, thresh,
+                                                                              d_pfac.p, d_nk.p, d_pwork.p, dmax);
     FCG_CUDA(cudaGetLastError());
     std::vector<int32_t> nk(pj.size());
     pfac.resize(size_t(std::max<int64_t>(pout, 1)));
@@ -754,7 +853,7 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
   TuckBatch T2;
   T2.desc.resize(size_t(ng));
   std::vector<int64_t> gwork(static_cast<size_t>(ng)), gbuf(static_cast<size_t>(ng));
-  int64_t wtot = 0;
+  int64_t wtot = 0, gdmax = 1;
   for (int64_t g = 0; g < ng; ++g) {
     TuckDesc& d = T2.desc[size_t(g)];
     d = TuckDesc{};
@@ -774,7 +873,8 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     const int64_t nm = gptr[size_t(g) + 1] - gptr[size_t(g)];
     gbuf[size_t(g)] = buf;
     gwork[size_t(g)] = wtot;
-    wtot += 2 * nm + 3 * dmax * dmax + dmax + 2 * buf;
+    wtot += 2 * nm + dmax * dmax + 2 * buf;
+    gdmax = std::max<int64_t>(gdmax, dmax);
   }
   lay_out(T2, N);
   FCG_CUDA(T2.d_desc.upload(T2.desc.data(), T2.desc.size(), ctx->stream));
@@ -790,9 +890,11 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     FCG_CUDA(d_gwork.upload(gwork.data(), gwork.size(), ctx->stream));
     FCG_CUDA(d_gbuf.upload(gbuf.data(), gbuf.size(), ctx->stream));
     FCG_CUDA(d_work.alloc(size_t(std::max<int64_t>(wtot, 1))));
-    tucker_add_kernel<<<unsigned((ng + kFoisThreads - 1) / kFoisThreads), kFoisThreads, 0, ctx->stream>>>(
+    size_t smem = 0;
+    FCG_REQUIRE(!cta_smem(tucker_add_kernel, int(gdmax), &smem), FCG_ECUDA, "FOIS: shared memory attribute");
+    tucker_add_kernel<<<unsigned(ng), kCtaThreads, smem, ctx->stream>>>(
         int(ng), N, R, 1e-10, d_gptr.p, d_gmem.p, T1.d_desc.p, T1.stride, T1.core.p, T1.fac.p, T1.rank.p,
-        T2.d_desc.p, T2.stride, T2.core.p, T2.fac.p, T2.rank.p, d_work.p, d_gwork.p, d_gbuf.p);
+        T2.d_desc.p, T2.stride, T2.core.p, T2.fac.p, T2.rank.p, d_work.p, d_gwork.p, d_gbuf.p, int(gdmax));
     FCG_CUDA(cudaGetLastError());
     FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // before the launch's buffers are freed
   }

@@ -22,3 +22,19 @@ extern "C" int sd_chol_inverse(int m, const double* G, int ldg, double drop, dou
 }
 
 extern "C" double sd_spd_condition(int m, const double* G, int ldg) { return fcg_small::spd_condition(m, G, ldg); }
+
+#include "../fermicg_gb300/csrc/tucker_small.cuh"
+
+extern "C" void sd_coop_jacobi(int n, double* A, double* w, double* V, int* perm) {
+  std::vector<double> cs(size_t(n) + 2), red(4);
+  fcg_tucker::coop_jacobi_eigh(n, A, w, V, perm, cs.data(), red.data(), 0, 1);
+}
+
+extern "C" void sd_coop_mode_gram(const double* A, const int32_t* dims, int n, int m, double* G) {
+  fcg_tucker::coop_mode_gram(A, dims, n, m, G, 0, 0, 1);
+}
+
+extern "C" void sd_coop_mode_product_t(const double* A, const int32_t* dims, int n, int m, const double* M, int ld,
+                                       int knew, double* B) {
+  fcg_tucker::coop_mode_product_t(A, dims, n, m, M, ld, knew, B, 0, 1);
+}

@@ -129,3 +129,59 @@ def test_spd_condition(lib):
     assert abs(lib.sd_spd_condition(3, _p(G), 3) - 100.0) < 1e-9
     G2 = np.asfortranarray(np.diag([1.0, 0.0]))
     assert lib.sd_spd_condition(2, _p(G2), 2) == float("inf")
+
+
+# ---- the cooperative Tucker routines of csrc/tucker_small.cuh, run with one thread ----------
+def _coop(lib):
+    dp, ip = ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int32)
+    lib.sd_coop_jacobi.argtypes = [ctypes.c_int, dp, dp, dp, ip]
+    lib.sd_coop_mode_gram.argtypes = [dp, ip, ctypes.c_int, ctypes.c_int, dp]
+    lib.sd_coop_mode_product_t.argtypes = [dp, ip, ctypes.c_int, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int, dp]
+    return lib
+
+
+@pytest.mark.parametrize("n,case", [(1, "rand"), (2, "rand"), (7, "rand"), (36, "rand"), (64, "rand"),
+                                    (20, "degenerate"), (12, "zero")])
+def test_coop_jacobi(lib, n, case):
+    L = _coop(lib)
+    rng = np.random.default_rng(n)
+    if case == "rand":
+        B = rng.standard_normal((n, n))
+        A = B @ B.T
+    elif case == "degenerate":
+        Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        A = Q @ np.diag([2.0] * (n // 2) + [0.5] * (n - n // 2)) @ Q.T
+    else:
+        A = np.zeros((n, n))
+    a = np.asfortranarray(A.copy())
+    w = np.zeros(n)
+    V = np.zeros((n, n), order="F")
+    perm = np.zeros(n, dtype=np.int32)
+    L.sd_coop_jacobi(n, _p(a), _p(w), _p(V), perm.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)))
+    ws = w[perm]
+    assert np.all(np.diff(ws) <= 1e-12 * max(1.0, abs(ws).max()))
+    np.testing.assert_allclose(np.sort(ws), np.linalg.eigvalsh(A), atol=1e-11 * max(1.0, np.abs(A).max()))
+    Vs = V[:, perm]
+    np.testing.assert_allclose(Vs.T @ Vs, np.eye(n), atol=1e-12)
+    np.testing.assert_allclose(A @ Vs, Vs * ws, atol=1e-10 * max(1.0, np.abs(A).max()))
+
+
+def test_coop_mode_gram_and_product(lib):
+    L = _coop(lib)
+    rng = np.random.default_rng(2)
+    dims = np.array([3, 4, 5], dtype=np.int32)
+    T = rng.standard_normal(tuple(dims))
+    a = np.asfortranarray(T).reshape(-1, order="F").copy()
+    for m in range(3):
+        d = dims[m]
+        G = np.zeros((d, d), order="F")
+        L.sd_coop_mode_gram(_p(a), dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 3, m, _p(G))
+        Mm = np.moveaxis(T, m, 0).reshape(d, -1)
+        np.testing.assert_allclose(G, Mm @ Mm.T, atol=1e-12)
+        k = 2
+        M = np.asfortranarray(rng.standard_normal((d, k)))
+        out = np.zeros(int(np.prod(dims)) // d * k)
+        L.sd_coop_mode_product_t(_p(a), dims.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)), 3, m, _p(M), d, k,
+                                 _p(out))
+        ref = np.moveaxis(np.tensordot(T, M, axes=([m], [0])), -1, m)
+        np.testing.assert_allclose(out.reshape(ref.shape, order="F"), ref, atol=1e-12)
