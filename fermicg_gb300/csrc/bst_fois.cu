@@ -91,7 +91,8 @@ __global__ void __launch_bounds__(kCtaThreads) fois_precontract_kernel(int n, co
                                                                       const double* __restrict__ fac, double prescreen,
                                                                       double* __restrict__ out,
                                                                       int32_t* __restrict__ nkeep,
-                                                                      double* __restrict__ work, int dmax) {
+                                                                      double* __restrict__ work, int64_t work_total,
+                                                                      int dmax, int* __restrict__ err) {
   extern __shared__ double sm[];
   const int i = blockIdx.x;
   if (i >= n) return;
@@ -100,6 +101,10 @@ __global__ void __launch_bounds__(kCtaThreads) fois_precontract_kernel(int n, co
   const PrecJob J = jobs[i];
   const int bl = J.bra_len;
   const int64_t PL = int64_t(J.np) * J.L;
+  if (bl > dmax || J.work_off < 0 || J.work_off + int64_t(bl) * PL > work_total) {  // extents the host sized
+    if (tid == 0) atomicExch(err, 1);
+    return;
+  }
   double* D = work + J.work_off;
   const double* Gm = tdm + J.tdm_off;
   const double* U = fac + J.kfac_off;
@@ -150,7 +155,7 @@ __global__ void __launch_bounds__(kCtaThreads) tucker_compress_kernel(
     int n, int N, int R, double thresh, const TuckDesc* __restrict__ in, int64_t in_stride,
     const double* __restrict__ in_core, const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank,
     const TuckDesc* __restrict__ out, int64_t out_stride, double* __restrict__ out_core, double* __restrict__ out_fac,
-    int32_t* __restrict__ out_rank, double* __restrict__ work, int dmax) {
+    int32_t* __restrict__ out_rank, double* __restrict__ work, int64_t work_total, int dmax, int* __restrict__ err) {
   extern __shared__ double sm[];
   const int t = blockIdx.x;
   if (t >= n) return;
@@ -169,9 +174,15 @@ __global__ void __launch_bounds__(kCtaThreads) tucker_compress_kernel(
   double* W = work + A.work_off;
   int64_t wo[kTuckMaxModes];
   int64_t acc = 0;
+  int dm = 0;
   for (int m = 0; m < N; ++m) {
     wo[m] = acc;
     acc += int64_t(dims[m]) * dims[m];
+    dm = max(dm, int(dims[m]));
+  }
+  if (dm > dmax || A.work_off < 0 || A.work_off + acc + 2 * len > work_total) {  // extents the host sized
+    if (tid == 0) atomicExch(err, 1);
+    return;
   }
   double* buf0 = W + acc;
   double* buf1 = buf0 + len;
@@ -238,7 +249,8 @@ __global__ void __launch_bounds__(kCtaThreads) tucker_add_kernel(
     const TuckDesc* __restrict__ in, int64_t in_stride, const double* __restrict__ in_core,
     const double* __restrict__ in_fac, const int32_t* __restrict__ in_rank, const TuckDesc* __restrict__ out,
     int64_t out_stride, double* __restrict__ out_core, double* __restrict__ out_fac, int32_t* __restrict__ out_rank,
-    double* __restrict__ work, const int64_t* __restrict__ work_off, const int64_t* __restrict__ buf_len, int dmax) {
+    double* __restrict__ work, const int64_t* __restrict__ work_off, const int64_t* __restrict__ buf_len,
+    int64_t work_total, int dmax, int* __restrict__ err) {
   extern __shared__ double sm[];
   const int g = blockIdx.x;
   if (g >= ng) return;
@@ -246,6 +258,14 @@ __global__ void __launch_bounds__(kCtaThreads) tucker_add_kernel(
   const CtaSmem S = carve(sm, dmax);
   const TuckDesc O = out[g];
   const int64_t nmem = ptr[g + 1] - ptr[g];
+  {
+    int dm = 0;
+    for (int m = 0; m < N; ++m) dm = max(dm, int(O.dim[m]));
+    if (dm > dmax || work_off[g] < 0 || work_off[g] + 2 * nmem + int64_t(dmax) * dmax + 2 * buf_len[g] > work_total) {
+      if (tid == 0) atomicExch(err, 1);  // extents the host sized
+      return;
+    }
+  }
   double* ord = work + work_off[g];  // member ids (exact in a double) in the order of addition
   double* nrm = ord + nmem;
   if (tid == 0) {
@@ -447,7 +467,7 @@ int cta_smem(K kernel, int dmax, size_t* bytes) {
 }
 
 int run_compress(fcg_ctx* ctx, int N, int R, double thresh, TuckBatch& in, const int32_t* d_in_rank, TuckBatch& out,
-                 DevBuf<double>& work) {
+                 DevBuf<double>& work, int* d_err) {
   const int n = int(in.desc.size());
   out.desc = in.desc;
   lay_out(out, N);
@@ -469,7 +489,7 @@ int run_compress(fcg_ctx* ctx, int N, int R, double thresh, TuckBatch& in, const
   if (n > 0) {
     tucker_compress_kernel<<<unsigned(n), kCtaThreads, smem, ctx->stream>>>(
         n, N, R, thresh, in.d_desc.p, in.stride, in.core.p, in.fac.p, d_in_rank, out.d_desc.p, out.stride,
-        out.core.p, out.fac.p, out.rank.p, work.p, dmax);
+        out.core.p, out.fac.p, out.rank.p, work.p, int64_t(work.n), dmax, d_err);
     FCG_CUDA(cudaGetLastError());
   }
   return FCG_OK;
@@ -674,6 +694,18 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
   }
   const int64_t n_items = int64_t(items.size());
   FCG_REQUIRE(n_items < (int64_t(1) << 24), FCG_ELIMIT, "FOIS: more than 2^24 contributions");
+  // every kernel checks the scratch extents it was given and raises this flag instead of
+  // touching memory outside them
+  DevBuf<int> d_err;
+  FCG_CUDA(d_err.alloc(1));
+  FCG_CUDA(cudaMemsetAsync(d_err.p, 0, sizeof(int), ctx->stream));
+  auto check_err = [&]() -> int {
+    int e = 0;
+    FCG_CUDA(cudaMemcpyAsync(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    FCG_REQUIRE(e == 0, FCG_ECUDA, "FOIS: a kernel found its scratch smaller than it needs");
+    return FCG_OK;
+  };
   // 1. the truncated bra factors of 3- and 4-body contributions
   std::vector<int32_t> item_nk(size_t(n_items) * 4, 0);  // per active cluster: kept vectors
   std::vector<int64_t> prec_of(size_t(n_items), -1);     // first job of the item
@@ -727,8 +759,8 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     for (const PrecJob& J : pj) dmax = std::max(dmax, J.bra_len);
     size_t smem = 0;
     FCG_REQUIRE(!cta_smem(fois_precontract_kernel, dmax, &smem), FCG_ECUDA, "FOIS: shared memory attribute");
-    fois_precontract_kernel<<<unsigned(n), kCtaThreads, smem, ctx->stream>>>(n, d_pj.p, ctx->d_op64.p, d_kfac.p, thresh,
-                                                                              d_pfac.p, d_nk.p, d_pwork.p, dmax);
+    fois_precontract_kernel<<<unsigned(n), kCtaThreads, smem, ctx->stream>>>(
+        n, d_pj.p, ctx->d_op64.p, d_kfac.p, thresh, d_pfac.p, d_nk.p, d_pwork.p, int64_t(d_pwork.n), dmax, d_err.p);
     FCG_CUDA(cudaGetLastError());
     std::vector<int32_t> nk(pj.size());
     pfac.resize(size_t(std::max<int64_t>(pout, 1)));
@@ -736,6 +768,10 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     FCG_CUDA(cudaMemcpyAsync(pfac.data(), d_pfac.p, sizeof(double) * pfac.size(), cudaMemcpyDeviceToHost,
                              ctx->stream));
     FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    {
+      const int rc = check_err();
+      if (rc) return rc;
+    }
     for (int64_t i = 0; i < n_items; ++i) {
       if (prec_of[size_t(i)] < 0) continue;
       const int32_t* r = &ctx->trm[int64_t(items[size_t(i)].term) * kTrmCols];
@@ -835,7 +871,7 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
   {
     TuckBatch& in = T0;
     in.fac.p = const_cast<double*>(d_sfac);  // borrowed, released below before T0 goes out of scope
-    int rc = run_compress(ctx, N, R, thresh, in, nullptr, T1, work);
+    int rc = run_compress(ctx, N, R, thresh, in, nullptr, T1, work, d_err.p);
     in.fac.p = nullptr;
     if (rc) return rc;
   }
@@ -851,8 +887,8 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     for (int64_t q = 0; q < n_kept; ++q) gmem[size_t(pos[size_t(items[size_t(kept[size_t(q)])].group)]++)] = int32_t(q);
   }
   TuckBatch T2;
-  T2.desc.resize(size_t(ng));
-  std::vector<int64_t> gwork(static_cast<size_t>(ng)), gbuf(static_cast<size_t>(ng));
+  T2.desc.resize(static_cast<size_t>(ng));
+  std::vector<int64_t> gwork(static_cast<size_t>(ng)), gbuf(static_cast<size_t>(ng)), gnm(static_cast<size_t>(ng));
   int64_t wtot = 0, gdmax = 1;
   for (int64_t g = 0; g < ng; ++g) {
     TuckDesc& d = T2.desc[size_t(g)];
@@ -870,11 +906,15 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
       buf *= std::max<int64_t>(d.rank[c], std::max<int64_t>(rmax, 1));
       dmax = std::max<int64_t>(dmax, dim);
     }
-    const int64_t nm = gptr[size_t(g) + 1] - gptr[size_t(g)];
     gbuf[size_t(g)] = buf;
-    gwork[size_t(g)] = wtot;
-    wtot += 2 * nm + dmax * dmax + 2 * buf;
+    gnm[size_t(g)] = gptr[size_t(g) + 1] - gptr[size_t(g)];
     gdmax = std::max<int64_t>(gdmax, dmax);
+  }
+  // the kernel places each block's transform (gdmax x gdmax, the launch's largest dimension)
+  // between the member lists and the core buffers
+  for (int64_t g = 0; g < ng; ++g) {
+    gwork[size_t(g)] = wtot;
+    wtot += 2 * gnm[size_t(g)] + gdmax * gdmax + 2 * gbuf[size_t(g)];
   }
   lay_out(T2, N);
   FCG_CUDA(T2.d_desc.upload(T2.desc.data(), T2.desc.size(), ctx->stream));
@@ -894,16 +934,18 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
     FCG_REQUIRE(!cta_smem(tucker_add_kernel, int(gdmax), &smem), FCG_ECUDA, "FOIS: shared memory attribute");
     tucker_add_kernel<<<unsigned(ng), kCtaThreads, smem, ctx->stream>>>(
         int(ng), N, R, 1e-10, d_gptr.p, d_gmem.p, T1.d_desc.p, T1.stride, T1.core.p, T1.fac.p, T1.rank.p,
-        T2.d_desc.p, T2.stride, T2.core.p, T2.fac.p, T2.rank.p, d_work.p, d_gwork.p, d_gbuf.p, int(gdmax));
+        T2.d_desc.p, T2.stride, T2.core.p, T2.fac.p, T2.rank.p, d_work.p, d_gwork.p, d_gbuf.p, int64_t(d_work.n),
+        int(gdmax), d_err.p);
     FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // before the launch's buffers are freed
+    const int rc = check_err();  // waits for the launch before its buffers are freed
+    if (rc) return rc;
   }
   // 6. compress each target block (compress_twice), then the whole space until its length
   //    stops falling (compress_iteratively: at least one pass)
   TuckBatch A, B;
   TuckBatch* cur = &T2;
   if (compress_twice) {
-    const int rc = run_compress(ctx, N, R, thresh, T2, T2.rank.p, A, work);
+    const int rc = run_compress(ctx, N, R, thresh, T2, T2.rank.p, A, work, d_err.p);
     if (rc) return rc;
     cur = &A;
   }
@@ -925,13 +967,17 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
   FCG_REQUIRE(len0 >= 0, FCG_ECUDA, "FOIS: rank read-back failed");
   for (int pass = 0; pass < 20; ++pass) {
     TuckBatch* next = (cur == &A) ? &B : &A;
-    const int rc = run_compress(ctx, N, R, thresh, *cur, cur->rank.p, *next, work);
+    const int rc = run_compress(ctx, N, R, thresh, *cur, cur->rank.p, *next, work, d_err.p);
     if (rc) return rc;
     const int64_t len1 = length_of(next);
     FCG_REQUIRE(len1 >= 0, FCG_ECUDA, "FOIS: rank read-back failed");
     cur = next;
     if (!(len1 < len0)) break;
     len0 = len1;
+  }
+  {
+    const int rc = check_err();
+    if (rc) return rc;
   }
   // 7. the result in the fcg_bst_set layout, empty blocks dropped
   std::vector<double> hcore(size_t(cur->stride) * R), hfac(size_t(cur->n_fac));
