@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
     ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
+    ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
+    ap.add_argument("--fois-only", action="store_true", help="run only the BST first-order space leg")
     ap.add_argument("--open-cfg", type=int, default=10000, help="variational configurations of the open sigma leg")
     return ap.parse_args()
 
@@ -304,6 +306,46 @@ def batched_benchmark(steps, warmup, n_inst=256):
     return out
 
 
+def fois_benchmark(steps, warmup, cpu_seconds, thresh=1e-3):
+    """build_compressed_1st_order_state of the CMF state of the 32-orbital / 8-cluster x 4 problem
+    (local bases of 16 states per sector) at thresh 1e-3: wall time of fcg_bst_fois (planning,
+    SVD precontraction, expansion through the BST sigma, HOSVD compressions, nonorth_add, results
+    fetched), one do_fois_pt2 on top of it, and the oracle's restatement of the same build on the
+    host (one run, when the CPU budget allows)."""
+    from fermicg_gb300 import bst_fois as G
+    from fermicg_gb300 import workloads
+    prob = workloads.config2_problem(0)
+    g = G.GpuBSTFois(prob.ops, prob.bases, prob.ham)
+    vec, P, Q = G.cmf_state(prob.bases, prob.init_fspace, R=1)
+    for _ in range(warmup):
+        fg = g.fois(vec, P, Q, thresh=thresh)
+    walls = []
+    for _ in range(steps):
+        t1 = time.perf_counter()
+        fg = g.fois(vec, P, Q, thresh=thresh)
+        walls.append(time.perf_counter() - t1)
+    st = g.H.stats()
+    t1 = time.perf_counter()
+    e, _ = g.do_fois_pt2(vec, P, Q, thresh_foi=thresh)
+    pt2_s = time.perf_counter() - t1
+    g.close()
+    out = {"workload": "CMF state of the 32-orbital / 8-cluster x 4 problem, thresh 1e-3",
+           "contributions": st["bst_fois_items"], "fois_blocks": len(fg),
+           "fois_length": int(sum(G._len(t) for t in fg.values())), "fois_ms": 1e3 * float(np.median(walls)),
+           "contributions_per_s": st["bst_fois_items"] / float(np.median(walls)),
+           "fois_pt2_s": pt2_s, "e_pt2": float(e[0])}
+    if cpu_seconds > 0:
+        from oracle import bst_fois as F
+        t1 = time.perf_counter()
+        fo = F.build_compressed_1st_order_state(vec, P, Q, prob.ops, prob.ham, len(prob.clusters), 1, thresh=thresh,
+                                               norb=[len(c) for c in prob.clusters])
+        cpu_s = time.perf_counter() - t1
+        out["cpu_baseline"] = {"value": cpu_s, "unit": "s per build", "cores": 1, "kind": "port",
+                               "sample": "the whole build (oracle restatement, numpy)", "blocks": len(fo)}
+        out["gpu_over_cpu"] = cpu_s / (out["fois_ms"] * 1e-3)
+    return out
+
+
 def open_benchmark(steps, warmup, cpu_seconds, n_cfg=10000, R=4, thresh=1e-4):
     """open_matvec_thread (the FOIS sigma of TPSCI's selection step) on the bench problem:
     the n_cfg lowest configurations, R roots, contributions kept when |x| > thresh/max|c|.
@@ -439,6 +481,10 @@ def main():
         if rank == 0:
             print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds,
                                                            n_cfg=a.open_cfg)}))
+        return
+    if a.fois_only:
+        if rank == 0:
+            print(json.dumps({"bst_fois": fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)}))
         return
     if a.batched_only:
         if rank == 0:
@@ -581,6 +627,11 @@ def main():
             out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, hbm_peak, a.bst_sectors)
         except Exception as ex:
             out["bst"] = {"error": str(ex)}
+    if rank == 0 and a.fois:
+        try:
+            out["bst_fois"] = fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)
+        except Exception as ex:
+            out["bst_fois"] = {"error": str(ex)}
     if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1

@@ -81,3 +81,23 @@ def test_fois_everything_below_threshold_is_empty(h12):
     m, b, ops, H, g = h12
     gv, gP, gQ = G.cmf_state(b, m["init_fspace"], R=1)
     assert g.fois(gv, gP, gQ, thresh=1e6) == {}
+
+
+def test_fois_cmf_32_orbitals_matches_oracle():
+    """The 32-orbital, 8-cluster x 4 problem (local bases of 16 states per sector, all eight
+    Tucker modes): the CMF state's FOIS at thresh 1e-3, block by block against the oracle."""
+    from fermicg_gb300 import bst_fois as G
+    from fermicg_gb300 import workloads
+    prob = workloads.config2_problem(0)
+    N = len(prob.clusters)
+    vec, P, Q = F.cmf_bst(prob.bases, prob.init_fspace, R=1)
+    fo = F.build_compressed_1st_order_state(vec, P, Q, prob.ops, prob.ham, N, 1, thresh=1e-3,
+                                           norb=[len(c) for c in prob.clusters])
+    g = G.GpuBSTFois(prob.ops, prob.bases, prob.ham)
+    try:
+        fg = g.fois(vec, P, Q, thresh=1e-3)
+        assert g.H.stats()["bst_fois_items"] > 5000
+    finally:
+        g.close()
+    assert len(fg) > 1000
+    _compare(fo, fg, 1, 1e-9)
