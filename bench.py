@@ -52,6 +52,9 @@ def parse():
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
     ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
     ap.add_argument("--fois-only", action="store_true", help="run only the BST first-order space leg")
+    ap.add_argument("--no-davidson", dest="davidson", action="store_false", help="skip the per-shape solve timings")
+    ap.add_argument("--davidson-only", action="store_true",
+                    help="run only the per-shape Davidson solve timings of the serving shapes")
     ap.add_argument("--open-cfg", type=int, default=10000, help="variational configurations of the open sigma leg")
     return ap.parse_args()
 
@@ -97,20 +100,71 @@ def cpu_reference(po, pt, f, c, v, budget_s, threads):
     return done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full build"
 
 
+def _shape_12o(seed):
+    from fermicg_gb300 import workloads
+    return workloads.build_problem(12, [3] * 4, [(2, 1), (1, 2), (2, 1), (1, 2)], 36, seed, max_roots=1000)
+
+
+def _shape_24o(seed):
+    from fermicg_gb300 import workloads
+    return workloads.build_problem(24, [4] * 6, [(2, 2)] * 6, 72, seed, max_roots=16, delta_elec=2)
+
+
+def _shape_32o(seed):
+    from fermicg_gb300 import workloads
+    return workloads.build_problem(32, [4] * 8, [(2, 2)] * 8, 96, seed, max_roots=8, delta_elec=2)
+
+
+SERVING_SHAPES = [  # (name, builder(seed), n_cfg, roots, share of the serving stream)
+    ("12o_4x3_full", _shape_12o, 2000, 1, 0.6),
+    ("24o_6x4_M16", _shape_24o, 10000, 4, 0.3),
+    ("32o_8x4_M8", _shape_32o, 5000, 2, 0.1),
+]
+
+
+def davidson_benchmark(reps=2):
+    """One solve per serving shape, alone on the GPU (tol 1e-6, mixed and FP64): the host time
+    of each stage of a request (fcg_set_ops, fcg_set_terms, fcg_state_set, fcg_davidson), the
+    iteration count and the time per iteration."""
+    from fermicg_gb300 import pack, workloads
+    from fermicg_gb300.gpu import GpuSigma
+    g = GpuSigma(0)
+    out = {}
+    for name, build, n_cfg, R, _ in SERVING_SHAPES:
+        prob = build(1001)
+        st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=0)
+        f, c, v, _ = pack.pack_state(st)
+        guess = np.zeros_like(v)
+        guess[:R] = np.eye(R)
+        po, pt = pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham)
+        for prec in ("fp32", "fp64"):
+            best = None
+            for _ in range(reps):
+                t = [time.perf_counter()]
+                g.set_ops(po)
+                t.append(time.perf_counter())
+                g.set_terms(pt)
+                t.append(time.perf_counter())
+                g.state_set(f, c)
+                t.append(time.perf_counter())
+                e, X, res, it = g.davidson(guess, tol=1e-6, max_iter=200, precision=prec)
+                t.append(time.perf_counter())
+                d = np.diff(t) * 1e3
+                if best is None or d[3] < best["davidson_ms"]:
+                    best = {"set_ops_ms": d[0], "set_terms_ms": d[1], "state_set_ms": d[2], "davidson_ms": d[3],
+                            "iterations": it, "ms_per_iteration": d[3] / max(it, 1)}
+            out[f"{name}/{'mixed' if prec == 'fp32' else 'fp64'}"] = best
+    g.close()
+    return out
+
+
 def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16):
     """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
     per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
     stream.  Returns p50/p99 latency and solves/s per precision."""
     from fermicg_gb300 import pack, workloads
     from fermicg_gb300.serving import Request, SolveServer, latency_summary
-    shapes = [  # (name, builder, n_cfg, roots, share)
-        ("12o_4x3_full", lambda sd: workloads.build_problem(12, [3] * 4, [(2, 1), (1, 2), (2, 1), (1, 2)], 36, sd,
-                                                             max_roots=1000), 2000, 1, 0.6),
-        ("24o_6x4_M16", lambda sd: workloads.build_problem(24, [4] * 6, [(2, 2)] * 6, 72, sd, max_roots=16,
-                                                            delta_elec=2), 10000, 4, 0.3),
-        ("32o_8x4_M8", lambda sd: workloads.build_problem(32, [4] * 8, [(2, 2)] * 8, 96, sd, max_roots=8,
-                                                           delta_elec=2), 5000, 2, 0.1),
-    ]
+    shapes = SERVING_SHAPES
     pools = []
     for k, (name, build, n_cfg, R, share) in enumerate(shapes):
         pool = []
@@ -482,6 +536,10 @@ def main():
             print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds,
                                                            n_cfg=a.open_cfg)}))
         return
+    if a.davidson_only:
+        if rank == 0:
+            print(json.dumps({"davidson": davidson_benchmark()}))
+        return
     if a.fois_only:
         if rank == 0:
             print(json.dumps({"bst_fois": fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)}))
@@ -627,6 +685,11 @@ def main():
             out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, hbm_peak, a.bst_sectors)
         except Exception as ex:
             out["bst"] = {"error": str(ex)}
+    if rank == 0 and a.davidson:
+        try:
+            out["davidson"] = davidson_benchmark()
+        except Exception as ex:
+            out["davidson"] = {"error": str(ex)}
     if rank == 0 and a.fois:
         try:
             out["bst_fois"] = fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)
