@@ -382,12 +382,17 @@ def fois_benchmark(steps, warmup, cpu_seconds, thresh=1e-3):
     t1 = time.perf_counter()
     e, _ = g.do_fois_pt2(vec, P, Q, thresh_foi=thresh)
     pt2_s = time.perf_counter() - t1
+    cg = g.cg_info[0]
     g.close()
     out = {"workload": "CMF state of the 32-orbital / 8-cluster x 4 problem, thresh 1e-3",
            "contributions": st["bst_fois_items"], "fois_blocks": len(fg),
            "fois_length": int(sum(G._len(t) for t in fg.values())), "fois_ms": 1e3 * float(np.median(walls)),
            "contributions_per_s": st["bst_fois_items"] / float(np.median(walls)),
-           "fois_pt2_s": pt2_s, "e_pt2": float(e[0])}
+           "fois_pt2_s": pt2_s, "e_pt2": float(e[0]),
+           "hylleraas_cg": {"products": cg[0], "converged": cg[1], "residual": cg[2],
+                            "note": "" if cg[1] else "the reference's CG (abstol 1e-6, at most 100 products) "
+                                    "does not converge here: H0 - E0 is not positive definite on this synthetic "
+                                    "problem, so E(PT2) is the last iterate's, as in the reference"}}
     if cpu_seconds > 0:
         from oracle import bst_fois as F
         t1 = time.perf_counter()

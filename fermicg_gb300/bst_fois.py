@@ -168,11 +168,14 @@ def project_out(v, w):
     return v
 
 
-def compress_state(vec, thresh):
-    """compress(ts::BSTstate) (src/type_BSTstate.jl:260-281): empty blocks dropped."""
+def compress_state(vec, thresh, only=None):
+    """compress(ts::BSTstate) (src/type_BSTstate.jl:260-281): empty blocks dropped.  With `only`,
+    the other blocks are kept as they are: for a state that is already a fixed point of compress
+    (the output of compress_iteratively) compressing them again changes nothing but a rotation
+    of their factors."""
     out = {}
     for k, t in vec.items():
-        tt = compress_block(t, thresh)
+        tt = compress_block(t, thresh) if only is None or k in only else t
         if _len(tt) > 0:
             out[k] = tt
     return out
@@ -201,7 +204,7 @@ class JointSigma:
     """H applied on the device to vectors over [reference blocks; FOIS blocks]: one
     fcg_bst_set of the joined structure, then fcg_bst_sigma per product."""
 
-    def __init__(self, g: GpuSigma, ref, fois, R, nbody=4):
+    def __init__(self, g: GpuSigma, ref, fois, R, nbody=4, between=False):
         self.g = g
         self.N = g.N
         self.R = R
@@ -209,8 +212,11 @@ class JointSigma:
         self.fois_keys = list(fois.keys())
         entries = [(k, ref[k]) for k in self.ref_keys] + [(k, fois[k]) for k in self.fois_keys]
         self.fock, self.blocks, self.foff, self.fac, _, offs = pack_blocks(entries, self.N, 1)
-        g.bst_set_raw(self.fock, self.blocks, self.foff, self.fac, nbody)
         self.n_ref = len(self.ref_keys)
+        if between and fois:  # only <FOIS|H|ref> and <ref|H|FOIS>
+            g.bst_set_between_raw(self.n_ref, self.fock, self.blocks, self.foff, self.fac, nbody)
+        else:
+            g.bst_set_raw(self.fock, self.blocks, self.foff, self.fac, nbody)
         self.offs = offs
         self.lens = [int(np.prod(self.blocks[i, :self.N])) for i in range(len(entries))]
         self.total = sum(self.lens)
@@ -274,10 +280,11 @@ class GpuBSTFois:
 
     def hylleraas(self, fois, ref, R, tol=1e-6, max_iter=100):
         """hylleraas_compressed_mp2 (src/tucker_pt.jl:358-532) with H0 = Hcmf: (psi1, e_pt2)."""
-        JH = JointSigma(self.H, ref, fois, R)
-        JF = JointSigma(self.H0, ref, fois, R)
         c0 = _vector(ref, R)
-        href, hx0 = JH.apply(c0, None)
+        href = JointSigma(self.H, ref, {}, R).apply(c0, None)[0]
+        JH = JointSigma(self.H, ref, fois, R, between=True)
+        JF = JointSigma(self.H0, ref, fois, R)
+        _, hx0 = JH.apply(c0, None)
         fref, fx0 = JF.apply(c0, None)
         e_ref = np.einsum("ir,ir->r", href, c0)
         e0 = np.einsum("ir,ir->r", fref, c0)
@@ -295,8 +302,10 @@ class GpuBSTFois:
             return JF.apply(None, x[:, None])[1][:, 0] - e0[0] * x
 
         X = np.zeros_like(b)
+        self.cg_info = []  # per root: (products, converged, final residual norm)
         for r in range(R):
-            X[:, r] = _cg(matvec, b[:, r] + sxv[:, r] * (e_ref[r] - e0[r]), abstol=tol, maxiter=max_iter)
+            X[:, r], info = _cg(matvec, b[:, r] + sxv[:, r] * (e_ref[r] - e0[r]), abstol=tol, maxiter=max_iter)
+            self.cg_info.append(info)
         psi1 = _zero(fois, R)
         for r in range(R):
             _set_vector(psi1, X[:, r], r)
@@ -312,14 +321,15 @@ class GpuBSTFois:
         _, ref_vec = self.ci_solve(ref, R)
         pt1 = self.fois(ref_vec, P, Q, thresh=thresh_foi, nbody=nbody)
         project_out(pt1, ref)
-        pt1 = compress_state(pt1, thresh_foi)
+        pt1 = compress_state(pt1, thresh_foi, only=set(ref))
         psi1, e = self.hylleraas(pt1, ref_vec, R, tol=tol, max_iter=max_iter)
         return e, psi1
 
 
 def _cg(matvec, b, abstol=1e-6, maxiter=100):
     """IterativeSolvers.cg! from x = 0: stop when |r| <= max(sqrt(eps) |b|, abstol) or after
-    maxiter products."""
+    maxiter products.  Returns (x, (products, converged, residual norm)); like the reference it
+    returns the last iterate when maxiter is reached (H0 - E0 need not be positive definite)."""
     x = np.zeros_like(b)
     r = b.copy()
     u = np.zeros_like(b)
@@ -337,4 +347,4 @@ def _cg(matvec, b, abstol=1e-6, maxiter=100):
         prev = res
         res = float(np.linalg.norm(r))
         it += 1
-    return x
+    return x, (it, bool(res <= tol), res)

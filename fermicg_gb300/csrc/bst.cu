@@ -482,7 +482,7 @@ void append_perm(const BstBlock& B, int N, int mask, std::vector<int32_t>& perm)
 // for which check_term holds on the TuckerConfigs: equal Fock sectors and equal ranges on
 // the spectators), grouped by (bra, ket, active clusters).
 std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>& blk, const int16_t* fock,
-                     BstPlan& P, const int32_t* given = nullptr, int64_t n_given = 0) {
+                     BstPlan& P, const int32_t* given = nullptr, int64_t n_given = 0, int64_t split = 0) {
   const int N = ctx->N;
   const int nmax1 = ctx->nmax + 1;
   const int64_t nb = int64_t(blk.size());
@@ -505,12 +505,16 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     }
     return h;
   };
+  // ket sides: 0 = blocks [0, split), 1 = blocks [split, nb), 2 = all blocks (no split)
+  auto in_side = [&](int64_t k, int side) { return side == 2 || ((k < split) == (side == 0)); };
   std::unordered_map<int, std::unordered_map<uint64_t, std::vector<int32_t>>> lookup;
-  auto kets_of = [&](int mask) -> std::unordered_map<uint64_t, std::vector<int32_t>>& {
-    auto it = lookup.find(mask);
+  auto kets_of = [&](int mask, int side) -> std::unordered_map<uint64_t, std::vector<int32_t>>& {
+    const int key = mask * 4 + side;
+    auto it = lookup.find(key);
     if (it != lookup.end()) return it->second;
-    auto& m = lookup[mask];
-    for (int64_t k = 0; k < nb; ++k) m[hash_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
+    auto& m = lookup[key];
+    for (int64_t k = 0; k < nb; ++k)
+      if (in_side(k, side)) m[hash_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
     return m;
   };
   auto matches = [&](int64_t b, const int16_t* fk, int64_t k, int mask) {
@@ -522,8 +526,10 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     return true;
   };
   // Fock sectors present (a transfer into any other sector has no ket)
-  std::unordered_map<uint64_t, int> sectors;
-  for (int64_t k = 0; k < nb; ++k) sectors[hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
+  std::unordered_map<uint64_t, int> sectors[3];
+  for (int64_t k = 0; k < nb; ++k)
+    for (int side = 0; side < 3; ++side)
+      if (in_side(k, side)) sectors[side][hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
   std::unordered_map<uint64_t, int64_t> gamma_at;   // (bra, ket, c, op) -> g offset
   std::unordered_map<uint64_t, int64_t> overlap_at; // (bra, ket, c) -> S offset
   std::unordered_map<uint64_t, int64_t> perm_at;    // (block, active mask) -> index table offset
@@ -624,6 +630,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
   std::vector<int16_t> fk(2 * N);
   for (int64_t b = 0; b < nb; ++b) {
     const int16_t* fb = fock + 2 * N * b;
+    const int kside = split > 0 ? (b < split ? 1 : 0) : 2;  // the other state's blocks only
     std::unordered_map<uint64_t, int32_t> grp;  // (ket, mask) -> group
     for (int tr = 0; tr < ctx->n_trans; ++tr) {
       if (by_trans[tr].empty()) continue;
@@ -635,7 +642,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
           fk[2 * c + s] = int16_t(v);
         }
       if (!ok) continue;
-      if (!sectors.count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
+      if (!sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
       for (int t : by_trans[tr]) {
         const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
         int mask = 0;
@@ -650,7 +657,7 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
           have = tdm[o] >= 0;
         }
         if (!have) continue;
-        auto& m = kets_of(mask);
+        auto& m = kets_of(mask, kside);
         auto it = m.find(hash_of(b, fk.data(), mask));
         if (it == m.end()) continue;
         const int sign = term_state_sign(r, fk.data());
@@ -909,7 +916,7 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
 
 int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
                  const int64_t* factor_off, int64_t n_factors, const double* factors, const int32_t* triples,
-                 int64_t n_triples, int64_t* core_total) {
+                 int64_t n_triples, int64_t* core_total, int64_t split) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_ops && ctx->have_terms, FCG_ESTATE, "upload ops and terms first");
   FCG_REQUIRE(n_blocks > 0 && fock && blocks && factor_off && factors && core_total && n_factors > 0, FCG_EINVAL,
@@ -948,7 +955,7 @@ int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock,
   }
   BstPlan P;
   {
-    std::string msg = plan_bst(ctx, nbody, blk, fock, P, triples, n_triples);
+    std::string msg = plan_bst(ctx, nbody, blk, fock, P, triples, n_triples, split);
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
   const double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -1021,7 +1028,16 @@ extern "C" {
 
 int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
                 const int64_t* factor_off, int64_t n_factors, const double* factors, int64_t* core_total) {
-  return bst_set_impl(ctx, nbody, n_blocks, fock, blocks, factor_off, n_factors, factors, nullptr, 0, core_total);
+  return bst_set_impl(ctx, nbody, n_blocks, fock, blocks, factor_off, n_factors, factors, nullptr, 0, core_total, 0);
+}
+
+int fcg_bst_set_between(fcg_ctx* ctx, int nbody, int64_t n_first, int64_t n_blocks, const int16_t* fock,
+                        const int64_t* blocks, const int64_t* factor_off, int64_t n_factors, const double* factors,
+                        int64_t* core_total) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(n_first >= 1 && n_first < n_blocks, FCG_EINVAL, "n_first must split the blocks into two states");
+  return bst_set_impl(ctx, nbody, n_blocks, fock, blocks, factor_off, n_factors, factors, nullptr, 0, core_total,
+                      n_first);
 }
 
 int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision) {

@@ -190,10 +190,11 @@ struct fcg_ctx {
 int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
 
 // fcg_bst_set with an optional caller-given triple list {bra, ket, term} (n_triples of them)
-// in place of the check_term enumeration (bst.cu)
+// in place of the check_term enumeration, or (split > 0) with only the triples that couple a
+// block of [0, split) with a block of [split, n_blocks) (bst.cu)
 int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
                  const int64_t* factor_off, int64_t n_factors, const double* factors, const int32_t* triples,
-                 int64_t n_triples, int64_t* core_total);
+                 int64_t n_triples, int64_t* core_total, int64_t split = 0);
 
 #define FCG_CUDA(call)                                                               \
   do {                                                                               \

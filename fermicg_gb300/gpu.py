@@ -47,6 +47,7 @@ SIGNATURES = {
     "fcg_get_stats": (_I, [_P, _P]),
     "fcg_bst_set": (_I, [_P, _I, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
     "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_bst_set_between": (_I, [_P, _I, _L, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
     "fcg_bst_sigma_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_triples": (_I, [_P, _P]),
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
@@ -265,6 +266,18 @@ class GpuSigma:
         ct = ctypes.c_int64(0)
         self._check(self.L.fcg_bst_set(self.h, int(nbody), bl.shape[0], _ptr(f), _ptr(bl), _ptr(fo), fa.size, _ptr(fa),
                                        ctypes.byref(ct)), "fcg_bst_set")
+        self.bst_core_total = ct.value
+        return ct.value
+
+    def bst_set_between_raw(self, n_first, fock, blocks, factor_off, factors, nbody=4):
+        """fcg_bst_set_between: only couplings between blocks [0, n_first) and the rest."""
+        f = np.ascontiguousarray(fock, dtype=np.int16)
+        bl = np.ascontiguousarray(blocks, dtype=np.int64)
+        fo = np.ascontiguousarray(factor_off, dtype=np.int64)
+        fa = np.ascontiguousarray(factors, dtype=np.float64)
+        ct = ctypes.c_int64(0)
+        self._check(self.L.fcg_bst_set_between(self.h, int(nbody), int(n_first), bl.shape[0], _ptr(f), _ptr(bl),
+                                               _ptr(fo), fa.size, _ptr(fa), ctypes.byref(ct)), "fcg_bst_set_between")
         self.bst_core_total = ct.value
         return ct.value
 

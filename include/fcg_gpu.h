@@ -190,6 +190,15 @@ int fcg_bst_sigma(fcg_ctx* ctx, int R, const double* cores, double* sigma, int p
 /* Same on device buffers [R][core_total] float64 of the context's device. */
 int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision);
 
+/* fcg_bst_set for build_sigma! between two different BST states (src/tucker_inner.jl:165-245
+ * with sigma_vector and ci_vector distinct): blocks [0, n_first) are one state, blocks
+ * [n_first, n_blocks) the other, and only the triples that couple a block of one state with a
+ * block of the other are planned (both directions), so one fcg_bst_sigma gives <A|H|B> and
+ * <B|H|A> without the couplings inside either state. */
+int fcg_bst_set_between(fcg_ctx* ctx, int nbody, int64_t n_first, int64_t n_blocks, const int16_t* fock,
+                        const int64_t* blocks, const int64_t* factor_off, int64_t n_factors, const double* factors,
+                        int64_t* core_total);
+
 /* The triples of the last fcg_bst_set: int32 [bst_triples][4] = {bra block, ket block,
  * term index (term-table row), state sign}. */
 int fcg_bst_triples(fcg_ctx* ctx, int32_t* out);

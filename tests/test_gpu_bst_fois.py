@@ -55,6 +55,7 @@ def test_fois_pt2_h12_matches_reference(h12):
     e, psi1 = g.do_fois_pt2(gv, gP, gQ, thresh_foi=1e-3)
     assert abs(e[0] - (-18.326971095822113)) < 1e-8, e
     assert len(psi1) > 0
+    assert g.cg_info[0][1]  # the Hylleraas conjugate gradient converged
 
 
 def test_fois_two_roots_multiblock_matches_oracle(h12):
@@ -101,3 +102,26 @@ def test_fois_cmf_32_orbitals_matches_oracle():
         g.close()
     assert len(fg) > 1000
     _compare(fo, fg, 1, 1e-9)
+
+
+def test_bst_sigma_between_two_states_matches_oracle(h12):
+    """fcg_bst_set_between: build_sigma! between two different BST states (the CMF block and a
+    FOIS with two roots), both directions, against the oracle's build_sigma!."""
+    from fermicg_gb300 import bst_fois as G
+    from oracle import bst as OB
+    m, b, ops, H, g = h12
+    N = len(m["clusters"])
+    vec, P, Q = F.cmf_bst(b, m["init_fspace"], R=1)
+    fo = F.build_compressed_1st_order_state(vec, P, Q, ops, H, N, 1, thresh=1e-3, norb=[len(c) for c in m["clusters"]])
+    rng = np.random.default_rng(11)
+    ref = {k: {"core": [t["core"][0], 0.5 * t["core"][0]], "factors": t["factors"]} for k, t in vec.items()}
+    fois = {k: {"core": [t["core"][0], rng.standard_normal(t["core"][0].shape)], "factors": t["factors"]}
+            for k, t in fo.items()}
+    J = G.JointSigma(g.H, ref, fois, 2, between=True)
+    hx_ref, hx_fois = J.apply(G._vector(ref, 2), None)          # <X|H|0>
+    h0_ref, _ = J.apply(None, G._vector(fois, 2))                # <0|H|X>
+    assert np.abs(hx_ref).max() == 0.0                           # no reference-reference couplings
+    sx = OB.build_sigma(OB.zero_like(fois, 2), ref, ops, H, N, 2)
+    s0 = OB.build_sigma(OB.zero_like(ref, 2), fois, ops, H, N, 2)
+    np.testing.assert_allclose(hx_fois, G._vector(sx, 2), atol=1e-11)
+    np.testing.assert_allclose(h0_ref, G._vector(s0, 2), atol=1e-11)
