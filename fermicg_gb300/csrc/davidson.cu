@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
 #include <vector>
 
 #include "fcg_ctx.cuh"
@@ -333,14 +334,14 @@ struct DavidsonWork {
     FCG_CUDA(cudaGetLastError());
     return FCG_OK;
   }
-  // wait for the stream; h_out[0 : count) = d_out[0 : count)
-  int fetch(size_t count) {
+  // queue h_out[0 : count) = d_out[0 : count); the values are there after the next wait for
+  // the stream, after which after_wait() frees the staging area
+  int enqueue_fetch(size_t count) {
     fcg_ctx* ctx = this->ctx;
     FCG_CUDA(cudaMemcpyAsync(h_out.p, d_out.p, count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-    up_used = up_sent = 0;
     return FCG_OK;
   }
+  void after_wait() { up_used = up_sent = 0; }
   // T = V[:, nv : nv + kt] <- T M - V[:, :nv] P  (M: kt x mo, P: nv x mo or null)
   int combine(int nv, int kt, const std::vector<double>& M, const std::vector<double>* P, int mo) {
     fcg_ctx* ctx = this->ctx;
@@ -359,8 +360,16 @@ struct DavidsonWork {
     FCG_CUDA(cudaGetLastError());
     return FCG_OK;
   }
-  int orthonormalize(int nv, int nt, std::vector<double> G0, double drop, int* kept);
-  int start_block(int nt, double drop, int* kept);
+  // Resumable orthonormalisation of the new directions V[:, nv : nv + nt] (see ortho_start):
+  // each call either finishes (*wait = false; the kept count in o_kept) or has queued a Gram
+  // product and its fetch (*wait = true) and continues in ortho_resume after the wait.
+  int ortho_start(int nv, int nt, std::vector<double> G0, double drop, bool* wait);
+  int ortho_resume(bool* wait);
+  int ortho_solve(std::vector<double> G2, int k1, bool* wait);
+  int o_state = 0;  // 0 idle, 1 waiting for the Gram matrix after the first projection, 2 for the second QR
+  int o_nv = 0, o_nt = 0, o_k1 = 0, o_good = 0, o_kept = 0;
+  double o_drop = 0.0;
+  std::vector<double> o_S2;
 };
 
 // Orthonormalise the new directions T = V[:, nv : nv + nt] against V[:, :nv] and among
@@ -369,9 +378,15 @@ struct DavidsonWork {
 // dropped when less than `drop` of it survives (it lies in the subspace already, up to
 // rounding).  The survivors are orthonormalised by Cholesky QR (stopping at the first
 // dependent column), twice when their Gram matrix has a condition number above 1e4.  The
-// kept directions end up in V[:, nv : nv + *kept].
-int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double drop, int* kept) {
-  *kept = 0;
+// kept directions end up in V[:, nv : nv + o_kept].  The work pauses (*wait) where it needs a
+// Gram matrix from the device: after the first projection, and before the second QR.
+int DavidsonWork::ortho_start(int nv, int nt, std::vector<double> G0, double drop, bool* wait) {
+  *wait = false;
+  o_state = 0;
+  o_kept = 0;
+  o_nv = nv;
+  o_nt = nt;
+  o_drop = drop;
   const int ld0 = nv + nt;
   int rc;
   // 1. unit scaling (and the first projection)
@@ -381,35 +396,49 @@ int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double 
     if (std::isfinite(g) && g > 1e-300) keep.push_back(j);
   }
   const int k1 = int(keep.size());
+  o_k1 = k1;
   if (k1 == 0) return FCG_OK;
   std::vector<double> M1(size_t(nt) * k1, 0.0), dsc(k1);
   for (int q = 0; q < k1; ++q) {
     dsc[q] = 1.0 / std::sqrt(G0[nv + keep[q] + size_t(ld0) * keep[q]]);
     M1[keep[q] + size_t(nt) * q] = dsc[q];
   }
-  std::vector<double> S2, G2(size_t(k1) * k1);
   if (nv == 0) {
     if ((rc = combine(0, nt, M1, nullptr, k1))) return rc;
+    std::vector<double> G2(size_t(k1) * k1);
     for (int q = 0; q < k1; ++q)
       for (int p = 0; p < k1; ++p) G2[p + size_t(k1) * q] = dsc[p] * dsc[q] * G0[keep[p] + size_t(ld0) * keep[q]];
-  } else {
-    std::vector<double> P1(size_t(nv) * k1);
-    for (int q = 0; q < k1; ++q)
-      for (int i = 0; i < nv; ++i) P1[i + size_t(nv) * q] = G0[i + size_t(ld0) * keep[q]] * dsc[q];
-    if ((rc = combine(nv, nt, M1, &P1, k1))) return rc;
-    // 2. second projection, from the Gram matrix of the projected block
-    if ((rc = gram(V.p, nv + k1, V.p + n * nv, k1, d_out.p))) return rc;
-    if ((rc = fetch(size_t(nv + k1) * k1))) return rc;
-    const int ld1 = nv + k1;
+    o_S2.clear();
+    return ortho_solve(std::move(G2), k1, wait);
+  }
+  std::vector<double> P1(size_t(nv) * k1);
+  for (int q = 0; q < k1; ++q)
+    for (int i = 0; i < nv; ++i) P1[i + size_t(nv) * q] = G0[i + size_t(ld0) * keep[q]] * dsc[q];
+  if ((rc = combine(nv, nt, M1, &P1, k1))) return rc;
+  // 2. second projection, from the Gram matrix of the projected block
+  if ((rc = gram(V.p, nv + k1, V.p + n * nv, k1, d_out.p))) return rc;
+  if ((rc = enqueue_fetch(size_t(nv + k1) * k1))) return rc;
+  o_state = 1;
+  *wait = true;
+  return FCG_OK;
+}
+
+int DavidsonWork::ortho_resume(bool* wait) {
+  *wait = false;
+  const int nv = o_nv;
+  if (o_state == 1) {
+    o_state = 0;
+    const int k1 = o_k1, ld1 = nv + k1;
     const double* G1 = h_out.p;
-    S2.assign(size_t(nv) * k1, 0.0);
+    o_S2.assign(size_t(nv) * k1, 0.0);
     for (int q = 0; q < k1; ++q)
-      for (int i = 0; i < nv; ++i) S2[i + size_t(nv) * q] = G1[i + size_t(ld1) * q];
+      for (int i = 0; i < nv; ++i) o_S2[i + size_t(nv) * q] = G1[i + size_t(ld1) * q];
     // Gram matrix after the second projection: T1^T T1 - S2^T S2 (V orthonormal)
+    std::vector<double> G2(size_t(k1) * k1);
     for (int q = 0; q < k1; ++q)
       for (int p = 0; p < k1; ++p) {
         double s = G1[nv + p + size_t(ld1) * q];
-        for (int i = 0; i < nv; ++i) s -= S2[i + size_t(nv) * p] * S2[i + size_t(nv) * q];
+        for (int i = 0; i < nv; ++i) s -= o_S2[i + size_t(nv) * p] * o_S2[i + size_t(nv) * q];
         G2[p + size_t(k1) * q] = s;
       }
     for (int q = 0; q < k1; ++q)
@@ -417,41 +446,11 @@ int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double 
         const double a = 0.5 * (G2[p + size_t(k1) * q] + G2[q + size_t(k1) * p]);
         G2[p + size_t(k1) * q] = G2[q + size_t(k1) * p] = a;
       }
+    return ortho_solve(std::move(G2), k1, wait);
   }
-  // 3. survivors, Cholesky QR fused with the second projection
-  std::vector<int> keep2;
-  for (int p = 0; p < k1; ++p) {
-    const double g = G2[p + size_t(k1) * p];
-    if (std::isfinite(g) && g >= drop * drop) keep2.push_back(p);
-  }
-  const int k2 = int(keep2.size());
-  if (k2 == 0) return FCG_OK;
-  std::vector<double> G2k(size_t(k2) * k2);
-  for (int q = 0; q < k2; ++q)
-    for (int p = 0; p < k2; ++p) G2k[p + size_t(k2) * q] = G2[keep2[p] + size_t(k1) * keep2[q]];
-  std::vector<double> Ri;
-  int good = fcg_small::chol_inverse(k2, G2k.data(), k2, drop, Ri);
-  if (good == 0) return FCG_OK;
-  std::vector<double> M2(size_t(k1) * good, 0.0);
-  for (int c = 0; c < good; ++c)
-    for (int q = 0; q < good; ++q) M2[keep2[q] + size_t(k1) * c] = Ri[q + size_t(good) * c];
-  if (nv == 0) {
-    if ((rc = combine(0, k1, M2, nullptr, good))) return rc;
-  } else {
-    std::vector<double> P2(size_t(nv) * good, 0.0);
-    for (int c = 0; c < good; ++c)
-      for (int p = 0; p < k1; ++p) {
-        const double m = M2[p + size_t(k1) * c];
-        if (m == 0.0) continue;
-        for (int i = 0; i < nv; ++i) P2[i + size_t(nv) * c] += S2[i + size_t(nv) * p] * m;
-      }
-    if ((rc = combine(nv, k1, M2, &P2, good))) return rc;
-  }
-  // 4. second Cholesky QR (and projection) for an ill-conditioned block only
-  if (fcg_small::spd_condition(good, G2k.data(), k2) > 1e4) {
-    if ((rc = gram(V.p, nv + good, V.p + n * nv, good, d_out.p))) return rc;
-    if ((rc = fetch(size_t(nv + good) * good))) return rc;
-    const int ld3 = nv + good;
+  if (o_state == 2) {  // the second Cholesky QR (and projection)
+    o_state = 0;
+    const int good = o_good, ld3 = nv + good;
     const double* G3 = h_out.p;
     std::vector<double> S3(size_t(nv) * good), G3t(size_t(good) * good);
     for (int q = 0; q < good; ++q)
@@ -463,8 +462,11 @@ int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double 
         G3t[p + size_t(good) * q] = s;
       }
     std::vector<double> Ri3;
-    const int good3 = fcg_small::chol_inverse(good, G3t.data(), good, drop, Ri3);
-    if (good3 == 0) return FCG_OK;
+    const int good3 = fcg_small::chol_inverse(good, G3t.data(), good, o_drop, Ri3);
+    if (good3 == 0) {
+      o_kept = 0;
+      return FCG_OK;
+    }
     std::vector<double> M3(size_t(good) * good3, 0.0);
     for (int c = 0; c < good3; ++c)
       for (int i = 0; i < good3; ++i) M3[i + size_t(good) * c] = Ri3[i + size_t(good3) * c];
@@ -477,20 +479,590 @@ int DavidsonWork::orthonormalize(int nv, int nt, std::vector<double> G0, double 
           for (int i = 0; i < nv; ++i) P3[i + size_t(nv) * c] += S3[i + size_t(nv) * p] * m;
         }
     }
-    if ((rc = combine(nv, good, M3, nv > 0 ? &P3 : nullptr, good3))) return rc;
-    good = good3;
+    const int rc = combine(nv, good, M3, nv > 0 ? &P3 : nullptr, good3);
+    if (rc) return rc;
+    o_kept = good3;
   }
-  *kept = good;
   return FCG_OK;
 }
 
-// orthonormalise the block V[:, 0 : nt] on its own (the first block of a (re)start)
-int DavidsonWork::start_block(int nt, double drop, int* kept) {
+// 3. survivors, Cholesky QR fused with the second projection; then the second QR when the
+// block's Gram matrix is ill-conditioned (it needs one more Gram matrix: *wait)
+int DavidsonWork::ortho_solve(std::vector<double> G2, int k1, bool* wait) {
+  *wait = false;
+  const int nv = o_nv;
+  const double drop = o_drop;
   int rc;
-  if ((rc = gram(V.p, nt, V.p, nt, d_out.p))) return rc;
-  if ((rc = fetch(size_t(nt) * nt))) return rc;
-  std::vector<double> G0(h_out.p, h_out.p + size_t(nt) * nt);
-  return orthonormalize(0, nt, std::move(G0), drop, kept);
+  std::vector<int> keep2;
+  for (int p = 0; p < k1; ++p) {
+    const double g = G2[p + size_t(k1) * p];
+    if (std::isfinite(g) && g >= drop * drop) keep2.push_back(p);
+  }
+  const int k2 = int(keep2.size());
+  if (k2 == 0) return FCG_OK;
+  std::vector<double> G2k(size_t(k2) * k2);
+  for (int q = 0; q < k2; ++q)
+    for (int p = 0; p < k2; ++p) G2k[p + size_t(k2) * q] = G2[keep2[p] + size_t(k1) * keep2[q]];
+  std::vector<double> Ri;
+  const int good = fcg_small::chol_inverse(k2, G2k.data(), k2, drop, Ri);
+  if (good == 0) return FCG_OK;
+  std::vector<double> M2(size_t(k1) * good, 0.0);
+  for (int c = 0; c < good; ++c)
+    for (int q = 0; q < good; ++q) M2[keep2[q] + size_t(k1) * c] = Ri[q + size_t(good) * c];
+  if (nv == 0) {
+    if ((rc = combine(0, k1, M2, nullptr, good))) return rc;
+  } else {
+    std::vector<double> P2(size_t(nv) * good, 0.0);
+    for (int c = 0; c < good; ++c)
+      for (int p = 0; p < k1; ++p) {
+        const double m = M2[p + size_t(k1) * c];
+        if (m == 0.0) continue;
+        for (int i = 0; i < nv; ++i) P2[i + size_t(nv) * c] += o_S2[i + size_t(nv) * p] * m;
+      }
+    if ((rc = combine(nv, k1, M2, &P2, good))) return rc;
+  }
+  o_kept = good;
+  if (fcg_small::spd_condition(good, G2k.data(), k2) > 1e4) {
+    o_good = good;
+    if ((rc = gram(V.p, nv + good, V.p + n * nv, good, d_out.p))) return rc;
+    if ((rc = enqueue_fetch(size_t(nv + good) * good))) return rc;
+    o_state = 2;
+    *wait = true;
+  }
+  return FCG_OK;
+}
+
+
+// One problem's block Davidson as a resumable state machine: step() runs until the problem
+// needs the device (WAIT: work and a fetch are queued on its stream), needs the sigma of its
+// new block (SIGMA: columns [sig_col, sig_col + sig_m) of V into the same columns of AV, in
+// precision sig_prec), or is done.  A driver waits for the stream and runs the sigma builds,
+// for one problem (fcg_davidson) or for many at once (fcg_davidson_grouped).
+enum class Act { kWait, kSigma, kDone };
+
+struct DavidsonRun {
+  DavidsonWork W;
+  fcg_ctx* ctx = nullptr;
+  int R = 0, max_iter = 0, precond = 0, prec = 0;
+  double tol = 0, drop = 0, switch_tol = 0;
+  bool gdk = false;
+  const double* v0 = nullptr;
+  double *energies = nullptr, *vectors = nullptr, *residuals = nullptr;
+  int* iters = nullptr;
+  // iteration state
+  enum St { kInit, kInitG0, kInitOrtho, kInitDone, kAfterInitSigma, kIter, kRRWait, kResWait, kOrtho, kOrthoDone,
+            kAfterSigma, kSwG0, kSwOrtho, kSwDone, kAfterSwSigma, kFinish, kFinished };
+  St st = kInit;
+  int nv = 0, newlo = 0, m = 0, it = 0;
+  int64_t sigma_calls = 0;
+  std::vector<double> Hs, A, w, Y, th, rn, Yprev;
+  int yprev_rows = 0;
+  int sig_col = 0, sig_m = 0, sig_prec = 0;
+
+  int init(fcg_ctx* c, int R_, const double* v0_, int max_iter_, int max_ss_vecs, double tol_, double lindep,
+           int precision, int precond_, double* e, double* vecs, double* res, int* its) {
+    ctx = c;
+    R = R_;
+    v0 = v0_;
+    max_iter = max_iter_;
+    tol = tol_;
+    precond = precond_;
+    prec = precision;
+    energies = e;
+    vectors = vecs;
+    residuals = res;
+    iters = its;
+    FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+    FCG_REQUIRE(v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
+    FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= ctx->n_cfg, FCG_ELIMIT, "R must be in [1, min(16, n_cfg)]");
+    FCG_REQUIRE(max_ss_vecs >= 2 && max_iter >= 1 && tol > 0, FCG_EINVAL, "bad Davidson settings");
+    FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
+    const int64_t n = ctx->n_cfg;
+    W.ctx = ctx;
+    W.n = n;
+    W.R = R;
+    W.kmax = int(std::min<int64_t>(int64_t(max_ss_vecs) * R, n));
+    W.kmax = std::max(W.kmax, std::min<int>(2 * R, int(n)));
+    W.kcap = W.kmax + R;
+    const int kmax = W.kmax, kcap = W.kcap;
+    // shared memory of the residual and combine kernels: (kcap x R) + R doubles at most
+    const size_t smem_max = sizeof(double) * (size_t(kcap) * R + size_t(R) * R + R);
+    FCG_REQUIRE(smem_max <= 200 * 1024, FCG_ELIMIT, "max_ss_vecs * R too large for the subspace kernels");
+    if (smem_max > 48 * 1024) {
+      const int sm = int(smem_max);
+      const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+      FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<1>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<2>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<4>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<8>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<16>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_kernel<1>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_kernel<2>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_kernel<4>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_kernel<8>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_kernel<16>, attr, sm));
+    }
+    W.row_blocks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxRowBlocks, (n + kGramRows - 1) / kGramRows)));
+    W.rows_per_block = (n + W.row_blocks - 1) / W.row_blocks;
+    W.res_blocks = int((n + kDavThreads - 1) / kDavThreads);
+    FCG_CUDA(W.V.alloc(size_t(n) * kcap));
+    FCG_CUDA(W.AV.alloc(size_t(n) * kcap));
+    FCG_CUDA(W.X.alloc(size_t(n) * R));
+    FCG_CUDA(W.tmp.alloc(size_t(n) * std::min(kmax, 2 * R)));
+    FCG_CUDA(W.hd.alloc(n));
+    FCG_CUDA(W.part.alloc(size_t(W.row_blocks) * kcap * R));
+    FCG_CUDA(W.rn_part.alloc(size_t(W.res_blocks) * R));
+    W.ngroups = (kcap + 31) / 32;
+    FCG_CUDA(W.counters.alloc(size_t(W.ngroups) + 1));
+    FCG_CUDA(cudaMemsetAsync(W.counters.p, 0, sizeof(unsigned) * (W.ngroups + 1), ctx->stream));
+    const size_t out_cap = size_t(R) + size_t(kcap) * R + 16;
+    const size_t up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
+    FCG_CUDA(W.d_out.alloc(out_cap));
+    FCG_CUDA(W.h_out.alloc(out_cap));
+    FCG_CUDA(W.d_up.alloc(up_cap));
+    FCG_CUDA(W.h_up.alloc(up_cap));
+    if (precond) {
+      std::vector<double> hd(n);
+      int rc = fcg_diagonal(ctx, -1, hd.data());
+      if (rc) return rc;
+      FCG_CUDA(cudaMemcpyAsync(W.hd.p, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+      FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // hd is a local vector
+    }
+    // a new direction must keep at least this fraction of its norm after projection
+    drop = std::max(lindep, 1e-8);
+    switch_tol = std::max(tol, 1e-5);
+    // GD+k restarts keep 2R vectors when the subspace has room for them and a new block
+    gdk = kmax >= 3 * R;
+    Hs.assign(size_t(kcap) * kcap, 0.0);
+    th.assign(R, 0.0);
+    rn.assign(R, 0.0);
+    FCG_CUDA(cudaMemcpyAsync(W.V.p, v0, sizeof(double) * n * R, cudaMemcpyHostToDevice, ctx->stream));
+    st = kInit;
+    return FCG_OK;
+  }
+
+  // request the sigma of columns [col, col + cols) in precision p
+  Act sigma(int col, int cols, int p, St next) {
+    sig_col = col;
+    sig_m = cols;
+    sig_prec = p;
+    st = next;
+    return Act::kSigma;
+  }
+
+  int step(Act* act);
+  int new_directions(bool* wait);
+};
+
+int DavidsonRun::step(Act* act) {
+  const int64_t n = W.n;
+  const int kcap = W.kcap;
+  int rc;
+  bool wait = false;
+  for (;;) {
+    switch (st) {
+      case kInit:  // the initial block on its own
+        if ((rc = W.gram(W.V.p, R, W.V.p, R, W.d_out.p))) return rc;
+        if ((rc = W.enqueue_fetch(size_t(R) * R))) return rc;
+        st = kInitG0;
+        *act = Act::kWait;
+        return FCG_OK;
+      case kInitG0: {
+        std::vector<double> G0(W.h_out.p, W.h_out.p + size_t(R) * R);
+        if ((rc = W.ortho_start(0, R, std::move(G0), drop, &wait))) return rc;
+        st = wait ? kInitOrtho : kInitDone;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        break;
+      }
+      case kInitOrtho:
+        if ((rc = W.ortho_resume(&wait))) return rc;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        st = kInitDone;
+        break;
+      case kInitDone: {
+        m = W.o_kept;
+        if (m != R) {
+          double nrm_min = 1e300, nrm_max = 0.0;
+          int nonfinite = 0;
+          for (int j = 0; j < R; ++j) {
+            double s2 = 0.0;
+            for (int64_t i = 0; i < n; ++i) {
+              const double x = v0[i + n * j];
+              if (!std::isfinite(x)) ++nonfinite;
+              s2 += x * x;
+            }
+            nrm_min = std::min(nrm_min, s2);
+            nrm_max = std::max(nrm_max, s2);
+          }
+          ctx->err = "initial vectors are linearly dependent (kept " + std::to_string(m) + " of " +
+                     std::to_string(R) + ", n " + std::to_string(n) + ", squared norms " + std::to_string(nrm_min) +
+                     ".." + std::to_string(nrm_max) + ", non-finite entries " + std::to_string(nonfinite) + ")";
+          return FCG_EINVAL;
+        }
+        *act = sigma(0, R, prec, kAfterInitSigma);
+        return FCG_OK;
+      }
+      case kAfterInitSigma:
+        nv = R;
+        newlo = 0;
+        it = 0;
+        sigma_calls = 1;
+        st = kIter;
+        break;
+      case kIter: {  // Rayleigh-Ritz: the new columns of V^T H V
+        if (++it > max_iter) {
+          st = kFinish;
+          break;
+        }
+        const int nb = nv - newlo;
+        if ((rc = W.gram(W.V.p, nv, W.AV.p + n * newlo, nb, W.d_out.p))) return rc;
+        if ((rc = W.enqueue_fetch(size_t(nv) * nb))) return rc;
+        st = kRRWait;
+        *act = Act::kWait;
+        return FCG_OK;
+      }
+      case kRRWait: {  // the projected eigenproblem; Ritz vectors, residuals, corrections, [V T]^T T
+        const int nb = nv - newlo;
+        const double* C = W.h_out.p;
+        for (int c = 0; c < nb; ++c) {
+          const int col = newlo + c;
+          for (int i = 0; i < nv; ++i) {
+            double h = C[i + size_t(nv) * c];
+            if (i >= newlo) h = 0.5 * (h + C[col + size_t(nv) * (i - newlo)]);
+            if (!std::isfinite(h)) {
+              ctx->err = "Davidson: non-finite subspace matrix at iteration " + std::to_string(it) + " (subspace " +
+                         std::to_string(nv) + ")";
+              return FCG_ECUDA;
+            }
+            Hs[i + size_t(kcap) * col] = Hs[col + size_t(kcap) * i] = h;
+          }
+        }
+        A.resize(size_t(nv) * nv);
+        for (int j = 0; j < nv; ++j)
+          for (int i = 0; i < nv; ++i) A[i + size_t(nv) * j] = Hs[i + size_t(kcap) * j];
+        if (fcg_small::symeig(nv, A.data(), w, Y, R)) {
+          ctx->err = "Davidson: subspace eigensolver did not converge at iteration " + std::to_string(it);
+          return FCG_ECUDA;
+        }
+        for (int j = 0; j < R; ++j) th[j] = w[j];
+        const double *dY = nullptr, *dth = nullptr;
+        if ((rc = W.upload(Y.data(), size_t(nv) * R, &dY))) return rc;
+        if ((rc = W.upload(th.data(), size_t(R), &dth))) return rc;
+        if ((rc = W.flush())) return rc;
+        const size_t ritz_smem = sizeof(double) * (size_t(nv) * R + R);
+#define FCG_RITZ_LAUNCH unsigned(W.res_blocks), kDavThreads, ritz_smem, ctx->stream
+        FCG_WIDTH_SWITCH(R, ritz_residual_kernel, FCG_RITZ_LAUNCH, W.V.p, W.AV.p, n, nv, dY, dth, W.hd.p, R, n, W.X.p,
+                         W.V.p + n * nv, precond, W.rn_part.p, W.d_out.p, W.counters.p + W.ngroups)
+#undef FCG_RITZ_LAUNCH
+        FCG_CUDA(cudaGetLastError());
+        if ((rc = W.gram(W.V.p, nv + R, W.V.p + n * nv, R, W.d_out.p + R))) return rc;
+        if ((rc = W.enqueue_fetch(size_t(R) + size_t(nv + R) * R))) return rc;
+        st = kResWait;
+        *act = Act::kWait;
+        return FCG_OK;
+      }
+      case kResWait: {
+        double rmax = 0.0;
+        for (int j = 0; j < R; ++j) {
+          rn[j] = std::sqrt(W.h_out.p[j]);
+          rmax = std::max(rmax, rn[j]);
+          if (!std::isfinite(rn[j]) || !std::isfinite(th[j])) {
+            ctx->err = "Davidson: non-finite residual or Ritz value at iteration " + std::to_string(it);
+            return FCG_ECUDA;
+          }
+        }
+        if (rmax < tol && prec == FCG_FP64) {
+          st = kFinish;
+          break;
+        }
+        if (prec == FCG_FP32 && rmax < switch_tol) {
+          // refinement: restart from the Ritz vectors with float64 sigma builds
+          prec = FCG_FP64;
+          FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
+          if ((rc = W.gram(W.V.p, R, W.V.p, R, W.d_out.p))) return rc;
+          if ((rc = W.enqueue_fetch(size_t(R) * R))) return rc;
+          st = kSwG0;
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        if ((rc = new_directions(&wait))) return rc;
+        st = wait ? kOrtho : kOrthoDone;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        break;
+      }
+      case kOrtho:
+        if ((rc = W.ortho_resume(&wait))) return rc;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        st = kOrthoDone;
+        break;
+      case kOrthoDone:
+        m = W.o_kept;
+        if (m == 0) {  // the subspace cannot grow: converged as far as lindep allows
+          st = kFinish;
+          break;
+        }
+        *act = sigma(nv, m, prec, kAfterSigma);
+        return FCG_OK;
+      case kAfterSigma:
+        ++sigma_calls;
+        newlo = nv;
+        nv += m;
+        st = kIter;
+        break;
+      case kSwG0: {
+        std::vector<double> G0(W.h_out.p, W.h_out.p + size_t(R) * R);
+        if ((rc = W.ortho_start(0, R, std::move(G0), drop, &wait))) return rc;
+        st = wait ? kSwOrtho : kSwDone;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        break;
+      }
+      case kSwOrtho:
+        if ((rc = W.ortho_resume(&wait))) return rc;
+        if (wait) {
+          *act = Act::kWait;
+          return FCG_OK;
+        }
+        st = kSwDone;
+        break;
+      case kSwDone:
+        m = W.o_kept;
+        if (m < R) {  // Ritz vectors numerically dependent: keep the float32 result
+          st = kFinish;
+          break;
+        }
+        *act = sigma(0, m, prec, kAfterSwSigma);
+        return FCG_OK;
+      case kAfterSwSigma:
+        ++sigma_calls;
+        nv = m;
+        newlo = 0;
+        yprev_rows = 0;
+        st = kIter;
+        break;
+      case kFinish:
+        for (int j = 0; j < R; ++j) {
+          energies[j] = th[j];
+          residuals[j] = rn[j];
+        }
+        FCG_CUDA(cudaMemcpyAsync(vectors, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToHost, ctx->stream));
+        *iters = std::min(it, max_iter);
+        ctx->stats.davidson_sigma_calls = sigma_calls;
+        st = kFinished;
+        *act = Act::kWait;  // the vectors are the caller's once the stream has been waited for
+        return FCG_OK;
+      case kFinished:
+        *act = Act::kDone;
+        return FCG_OK;
+    }
+  }
+}
+
+// New directions: corrections of the roots not yet converged (all roots in float32), with a
+// restart on span{Y, Yprev} when the subspace is full (Q orthonormal, V <- V Q, AV <- AV Q,
+// Hs <- Q^T Hs Q), then the orthonormalisation of the corrections against V (may wait).
+int DavidsonRun::new_directions(bool* wait) {
+  const int64_t n = W.n;
+  const int kcap = W.kcap, kmax = W.kmax;
+  int rc;
+  std::vector<int> sel;
+  for (int j = 0; j < R; ++j)
+    if (rn[j] >= tol || prec == FCG_FP32) sel.push_back(j);
+  const int nt = int(sel.size());
+  const int ldg = nv + R;
+  const double* Gall = W.h_out.p + R;  // [V T]^T T, (nv + R) x R
+  std::vector<double> S(size_t(nv) * nt), Gtt(size_t(nt) * nt);
+  for (int q = 0; q < nt; ++q) {
+    for (int i = 0; i < nv; ++i) S[i + size_t(nv) * q] = Gall[i + size_t(ldg) * sel[q]];
+    for (int p = 0; p < nt; ++p) Gtt[p + size_t(nt) * q] = Gall[nv + sel[p] + size_t(ldg) * sel[q]];
+  }
+  const int nv_old = nv;
+  if (nv + nt > kmax) {
+    const int zc = R + ((gdk && yprev_rows > 0) ? R : 0);
+    std::vector<double> Q;
+    int q = 0;
+    for (int c = 0; c < zc; ++c) {
+      std::vector<double> z(nv, 0.0);
+      if (c < R)
+        for (int i = 0; i < nv; ++i) z[i] = Y[i + size_t(nv) * c];
+      else
+        for (int i = 0; i < yprev_rows; ++i) z[i] = Yprev[i + size_t(yprev_rows) * (c - R)];
+      double n0 = 0.0;
+      for (double x : z) n0 += x * x;
+      n0 = std::sqrt(n0);
+      for (int pass = 0; pass < 2; ++pass)
+        for (int k = 0; k < q; ++k) {
+          double d = 0.0;
+          for (int i = 0; i < nv; ++i) d += Q[i + size_t(nv) * k] * z[i];
+          for (int i = 0; i < nv; ++i) z[i] -= d * Q[i + size_t(nv) * k];
+        }
+      double nz = 0.0;
+      for (double x : z) nz += x * x;
+      nz = std::sqrt(nz);
+      if (!(nz > 1e-8 * n0)) continue;
+      for (double& x : z) x /= nz;
+      Q.insert(Q.end(), z.begin(), z.end());
+      ++q;
+    }
+    const double* dQ = nullptr;
+    if ((rc = W.upload(Q.data(), size_t(nv) * q, &dQ))) return rc;
+    if ((rc = W.flush())) return rc;
+    const unsigned g = unsigned((n + 255) / 256);
+    update_kernel<<<g, 256, 0, ctx->stream>>>(W.V.p, n, nv, dQ, q, W.tmp.p, n, n);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaMemcpyAsync(W.V.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
+    update_kernel<<<g, 256, 0, ctx->stream>>>(W.AV.p, n, nv, dQ, q, W.tmp.p, n, n);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
+    std::vector<double> HQ(size_t(nv) * q, 0.0), Hn(size_t(q) * q, 0.0), Sn(size_t(q) * nt, 0.0),
+        Yp(size_t(q) * R, 0.0);
+    for (int c = 0; c < q; ++c)
+      for (int k = 0; k < nv; ++k) {
+        const double qk = Q[k + size_t(nv) * c];
+        for (int i = 0; i < nv; ++i) HQ[i + size_t(nv) * c] += Hs[i + size_t(kcap) * k] * qk;
+      }
+    for (int c = 0; c < q; ++c)
+      for (int r2 = 0; r2 < q; ++r2) {
+        double s = 0.0;
+        for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * HQ[i + size_t(nv) * c];
+        Hn[r2 + size_t(q) * c] = s;
+      }
+    for (int c = 0; c < q; ++c)
+      for (int r2 = 0; r2 < c; ++r2) {
+        const double a = 0.5 * (Hn[r2 + size_t(q) * c] + Hn[c + size_t(q) * r2]);
+        Hn[r2 + size_t(q) * c] = Hn[c + size_t(q) * r2] = a;
+      }
+    for (int c = 0; c < nt; ++c)
+      for (int r2 = 0; r2 < q; ++r2) {
+        double s = 0.0;
+        for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * S[i + size_t(nv) * c];
+        Sn[r2 + size_t(q) * c] = s;
+      }
+    for (int c = 0; c < R; ++c)
+      for (int r2 = 0; r2 < q; ++r2) {
+        double s = 0.0;
+        for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * Y[i + size_t(nv) * c];
+        Yp[r2 + size_t(q) * c] = s;
+      }
+    for (int c = 0; c < q; ++c)
+      for (int r2 = 0; r2 < q; ++r2) Hs[r2 + size_t(kcap) * c] = Hn[r2 + size_t(q) * c];
+    S.swap(Sn);
+    Yprev.swap(Yp);
+    yprev_rows = q;
+    nv = q;
+  } else {
+    Yprev = Y;
+    yprev_rows = nv;
+  }
+  // the selected corrections move to V[:, nv : nv + nt] (never onto a later source column)
+  for (int q = 0; q < nt; ++q) {
+    const int src = nv_old + sel[q], dst = nv + q;
+    if (src != dst)
+      FCG_CUDA(cudaMemcpyAsync(W.V.p + n * dst, W.V.p + n * src, sizeof(double) * n, cudaMemcpyDeviceToDevice,
+                               ctx->stream));
+  }
+  std::vector<double> G0(size_t(nv + nt) * nt);
+  for (int c = 0; c < nt; ++c) {
+    for (int i = 0; i < nv; ++i) G0[i + size_t(nv + nt) * c] = S[i + size_t(nv) * c];
+    for (int p = 0; p < nt; ++p) G0[nv + p + size_t(nv + nt) * c] = Gtt[p + size_t(nt) * c];
+  }
+  return W.ortho_start(nv, nt, std::move(G0), drop, wait);
+}
+
+}  // namespace
+
+extern "C" int fcg_sigma_closed_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* d_c,
+                                        double* const* d_sigma, int precision);
+
+namespace {
+
+// Drive the problems to completion on the leader's stream: every round runs each ready
+// problem until it needs the device; then either one wait for the stream serves all problems
+// that queued work, or -- when every unfinished problem asks for its sigma -- the sigma builds
+// run (one asynchronous launch for a single problem, one grouped launch per precision for
+// several), and the round repeats.
+int run_lockstep(std::vector<std::unique_ptr<DavidsonRun>>& runs, fcg_ctx* leader) {
+  fcg_ctx* ctx = leader;
+  enum { kReady, kWaiting, kSigma, kDone };
+  const int P = int(runs.size());
+  std::vector<int> state(P, kReady);
+  int active = P;
+  while (active > 0) {
+    for (int q = 0; q < P; ++q) {
+      if (state[q] != kReady) continue;
+      Act a = Act::kDone;
+      const int rc = runs[q]->step(&a);
+      if (rc) {
+        if (runs[q]->ctx != leader) leader->err = runs[q]->ctx->err + " (problem " + std::to_string(q) + ")";
+        return rc;
+      }
+      state[q] = a == Act::kWait ? kWaiting : a == Act::kSigma ? kSigma : kDone;
+      if (a == Act::kDone) --active;
+    }
+    bool waiting = false;
+    for (int q = 0; q < P; ++q) waiting = waiting || state[q] == kWaiting;
+    if (waiting) {
+      FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+      for (int q = 0; q < P; ++q)
+        if (state[q] == kWaiting) {
+          runs[q]->W.after_wait();
+          state[q] = kReady;
+        }
+      continue;
+    }
+    if (P == 1) {
+      if (state[0] == kSigma) {
+        DavidsonRun& r = *runs[0];
+        const int64_t n = r.W.n;
+        const int rc = sigma_closed_device_async(r.ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col,
+                                                 r.sig_prec);
+        if (rc) return rc;
+        state[0] = kReady;
+      }
+      continue;
+    }
+    for (int p : {FCG_FP32, FCG_FP64}) {
+      std::vector<fcg_ctx*> cs;
+      std::vector<int> Rs, who;
+      std::vector<const double*> dc;
+      std::vector<double*> ds;
+      for (int q = 0; q < P; ++q) {
+        DavidsonRun& r = *runs[q];
+        if (state[q] != kSigma || r.sig_prec != p) continue;
+        const int64_t n = r.W.n;
+        cs.push_back(r.ctx);
+        Rs.push_back(r.sig_m);
+        dc.push_back(r.W.V.p + n * r.sig_col);
+        ds.push_back(r.W.AV.p + n * r.sig_col);
+        who.push_back(q);
+      }
+      if (cs.empty()) continue;
+      const int rc = fcg_sigma_closed_grouped(int(cs.size()), cs.data(), Rs.data(), dc.data(), ds.data(), p);
+      if (rc) {
+        if (cs[0] != leader) leader->err = cs[0]->err;
+        return rc;
+      }
+      for (int q : who) {
+        runs[q]->W.after_wait();
+        state[q] = kReady;
+      }
+    }
+  }
+  return FCG_OK;
 }
 
 }  // namespace
@@ -499,282 +1071,45 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
                             double lindep, int precision, int precond, double* energies, double* vectors,
                             double* residuals, int* iters) {
   if (!ctx) return FCG_EINVAL;
-  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
-  FCG_REQUIRE(v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
-  FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= ctx->n_cfg, FCG_ELIMIT, "R must be in [1, min(16, n_cfg)]");
-  FCG_REQUIRE(max_ss_vecs >= 2 && max_iter >= 1 && tol > 0, FCG_EINVAL, "bad Davidson settings");
-  FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
   FCG_CUDA(cudaSetDevice(ctx->device));
-  const int64_t n = ctx->n_cfg;
-  DavidsonWork W;
-  W.ctx = ctx;
-  W.n = n;
-  W.R = R;
-  W.kmax = int(std::min<int64_t>(int64_t(max_ss_vecs) * R, n));
-  W.kmax = std::max(W.kmax, std::min<int>(2 * R, int(n)));
-  W.kcap = W.kmax + R;
-  const int kmax = W.kmax, kcap = W.kcap;
-  // shared memory of the residual and combine kernels: (kcap x R) + R doubles at most
-  const size_t smem_max = sizeof(double) * (size_t(kcap) * R + size_t(R) * R + R);
-  FCG_REQUIRE(smem_max <= 200 * 1024, FCG_ELIMIT, "max_ss_vecs * R too large for the subspace kernels");
-  if (smem_max > 48 * 1024) {
-    const int sm = int(smem_max);
-    const auto attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<1>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<2>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<4>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<8>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(ritz_residual_kernel<16>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<1>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<2>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<4>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<8>, attr, sm));
-    FCG_CUDA(cudaFuncSetAttribute(combine_kernel<16>, attr, sm));
+  std::vector<std::unique_ptr<DavidsonRun>> runs;
+  runs.emplace_back(new DavidsonRun());
+  const int rc = runs[0]->init(ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, precond, energies, vectors,
+                               residuals, iters);
+  if (rc) return rc;
+  return run_lockstep(runs, ctx);
+}
+
+extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* v0, int max_iter,
+                                    int max_ss_vecs, double tol, double lindep, int precision, int precond,
+                                    double* const* energies, double* const* vectors, double* const* residuals,
+                                    int* iters) {
+  if (n < 1 || !ctxs || !ctxs[0]) return FCG_EINVAL;
+  fcg_ctx* ctx = ctxs[0];
+  FCG_REQUIRE(R && v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(n <= 65535, FCG_ELIMIT, "at most 65535 problems per group");
+  for (int q = 0; q < n; ++q) {
+    FCG_REQUIRE(ctxs[q], FCG_EINVAL, "null context in the group");
+    FCG_REQUIRE(ctxs[q]->device == ctx->device, FCG_EINVAL, "all contexts of a group must share a device");
+    for (int q2 = 0; q2 < q; ++q2) FCG_REQUIRE(ctxs[q2] != ctxs[q], FCG_EINVAL, "a context appears twice in the group");
   }
-  W.row_blocks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxRowBlocks, (n + kGramRows - 1) / kGramRows)));
-  W.rows_per_block = (n + W.row_blocks - 1) / W.row_blocks;
-  W.res_blocks = int((n + kDavThreads - 1) / kDavThreads);
-  FCG_CUDA(W.V.alloc(size_t(n) * kcap));
-  FCG_CUDA(W.AV.alloc(size_t(n) * kcap));
-  FCG_CUDA(W.X.alloc(size_t(n) * R));
-  FCG_CUDA(W.tmp.alloc(size_t(n) * std::min(kmax, 2 * R)));
-  FCG_CUDA(W.hd.alloc(n));
-  FCG_CUDA(W.part.alloc(size_t(W.row_blocks) * kcap * R));
-  FCG_CUDA(W.rn_part.alloc(size_t(W.res_blocks) * R));
-  W.ngroups = (kcap + 31) / 32;
-  FCG_CUDA(W.counters.alloc(size_t(W.ngroups) + 1));
-  FCG_CUDA(cudaMemsetAsync(W.counters.p, 0, sizeof(unsigned) * (W.ngroups + 1), ctx->stream));
-  const size_t out_cap = size_t(R) + size_t(kcap) * R + 16;
-  const size_t up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
-  FCG_CUDA(W.d_out.alloc(out_cap));
-  FCG_CUDA(W.h_out.alloc(out_cap));
-  FCG_CUDA(W.d_up.alloc(up_cap));
-  FCG_CUDA(W.h_up.alloc(up_cap));
-  if (precond) {
-    std::vector<double> hd(n);
-    int rc = fcg_diagonal(ctx, -1, hd.data());
-    if (rc) return rc;
-    FCG_CUDA(cudaMemcpyAsync(W.hd.p, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // hd is a local vector
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  // every problem's work goes to the leader's stream while the group is solved
+  std::vector<cudaStream_t> saved(n);
+  for (int q = 0; q < n; ++q) {
+    saved[q] = ctxs[q]->stream;
+    ctxs[q]->stream = ctx->stream;
   }
-  int prec = precision;  // current sigma precision
-  // a new direction must keep at least this fraction of its norm after projection
-  const double drop = std::max(lindep, 1e-8);
-  const double switch_tol = std::max(tol, 1e-5);
-  // GD+k restarts keep 2R vectors when the subspace has room for them and a new block
-  const bool gdk = kmax >= 3 * R;
-  // initial block
-  FCG_CUDA(cudaMemcpyAsync(W.V.p, v0, sizeof(double) * n * R, cudaMemcpyHostToDevice, ctx->stream));
-  int nv = 0, m = 0, rc;
-  if ((rc = W.start_block(R, drop, &m))) return rc;
-  if (m != R) {
-    double nrm_min = 1e300, nrm_max = 0.0;
-    int nonfinite = 0;
-    for (int j = 0; j < R; ++j) {
-      double s2 = 0.0;
-      for (int64_t i = 0; i < n; ++i) {
-        const double x = v0[i + n * j];
-        if (!std::isfinite(x)) ++nonfinite;
-        s2 += x * x;
-      }
-      nrm_min = std::min(nrm_min, s2);
-      nrm_max = std::max(nrm_max, s2);
-    }
-    ctx->err = "initial vectors are linearly dependent (kept " + std::to_string(m) + " of " + std::to_string(R) +
-               ", n " + std::to_string(n) + ", squared norms " + std::to_string(nrm_min) + ".." +
-               std::to_string(nrm_max) + ", non-finite entries " + std::to_string(nonfinite) + ")";
-    return FCG_EINVAL;
+  std::vector<std::unique_ptr<DavidsonRun>> runs;
+  int rc = FCG_OK;
+  for (int q = 0; q < n && rc == FCG_OK; ++q) {
+    runs.emplace_back(new DavidsonRun());
+    rc = runs[q]->init(ctxs[q], R[q], v0[q], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[q],
+                       vectors[q], residuals[q], &iters[q]);
+    if (rc && q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
   }
-  if ((rc = sigma_closed_device_async(ctx, R, W.V.p, W.AV.p, prec))) return rc;
-  nv = R;
-  int newlo = 0;  // first column of AV whose projections are not in Hs yet
-  std::vector<double> Hs(size_t(kcap) * kcap, 0.0), A, w, Y, th(R), rn(R);
-  std::vector<double> Yprev;  // previous Ritz coefficients in the current basis (yprev_rows x R)
-  int yprev_rows = 0;
-  int it = 0;
-  int64_t sigma_calls = 1;
-  for (it = 1; it <= max_iter; ++it) {
-    // Rayleigh-Ritz: the new columns of V^T H V, then the projected eigenproblem
-    const int nb = nv - newlo;
-    if ((rc = W.gram(W.V.p, nv, W.AV.p + n * newlo, nb, W.d_out.p))) return rc;
-    if ((rc = W.fetch(size_t(nv) * nb))) return rc;
-    {
-      const double* C = W.h_out.p;
-      for (int c = 0; c < nb; ++c) {
-        const int col = newlo + c;
-        for (int i = 0; i < nv; ++i) {
-          double h = C[i + size_t(nv) * c];
-          if (i >= newlo) h = 0.5 * (h + C[col + size_t(nv) * (i - newlo)]);
-          if (!std::isfinite(h)) {
-            ctx->err = "Davidson: non-finite subspace matrix at iteration " + std::to_string(it) + " (subspace " +
-                       std::to_string(nv) + ")";
-            return FCG_ECUDA;
-          }
-          Hs[i + size_t(kcap) * col] = Hs[col + size_t(kcap) * i] = h;
-        }
-      }
-    }
-    A.resize(size_t(nv) * nv);
-    for (int j = 0; j < nv; ++j)
-      for (int i = 0; i < nv; ++i) A[i + size_t(nv) * j] = Hs[i + size_t(kcap) * j];
-    if (fcg_small::symeig(nv, A.data(), w, Y, R)) {
-      ctx->err = "Davidson: subspace eigensolver did not converge at iteration " + std::to_string(it);
-      return FCG_ECUDA;
-    }
-    for (int j = 0; j < R; ++j) th[j] = w[j];
-    // Ritz vectors, residual norms, corrections behind V, and [V T]^T T
-    const double *dY = nullptr, *dth = nullptr;
-    if ((rc = W.upload(Y.data(), size_t(nv) * R, &dY))) return rc;
-    if ((rc = W.upload(th.data(), size_t(R), &dth))) return rc;
-    if ((rc = W.flush())) return rc;
-    const size_t ritz_smem = sizeof(double) * (size_t(nv) * R + R);
-#define FCG_RITZ_LAUNCH unsigned(W.res_blocks), kDavThreads, ritz_smem, ctx->stream
-    FCG_WIDTH_SWITCH(R, ritz_residual_kernel, FCG_RITZ_LAUNCH, W.V.p, W.AV.p, n, nv, dY, dth, W.hd.p, R, n, W.X.p,
-                     W.V.p + n * nv, precond, W.rn_part.p, W.d_out.p, W.counters.p + W.ngroups)
-#undef FCG_RITZ_LAUNCH
-    FCG_CUDA(cudaGetLastError());
-    if ((rc = W.gram(W.V.p, nv + R, W.V.p + n * nv, R, W.d_out.p + R))) return rc;
-    if ((rc = W.fetch(size_t(R) + size_t(nv + R) * R))) return rc;
-    double rmax = 0.0;
-    for (int j = 0; j < R; ++j) {
-      rn[j] = std::sqrt(W.h_out.p[j]);
-      rmax = std::max(rmax, rn[j]);
-      if (!std::isfinite(rn[j]) || !std::isfinite(th[j])) {
-        ctx->err = "Davidson: non-finite residual or Ritz value at iteration " + std::to_string(it);
-        return FCG_ECUDA;
-      }
-    }
-    if (rmax < tol && prec == FCG_FP64) break;
-    if (prec == FCG_FP32 && rmax < switch_tol) {
-      // refinement: restart from the Ritz vectors with float64 sigma builds
-      prec = FCG_FP64;
-      FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
-      if ((rc = W.start_block(R, drop, &m))) return rc;
-      if (m < R) break;  // Ritz vectors numerically dependent: keep the float32 result
-      if ((rc = sigma_closed_device_async(ctx, m, W.V.p, W.AV.p, prec))) return rc;
-      ++sigma_calls;
-      nv = m;
-      newlo = 0;
-      yprev_rows = 0;
-      continue;
-    }
-    // new directions: corrections of the roots not yet converged (all roots in float32)
-    std::vector<int> sel;
-    for (int j = 0; j < R; ++j)
-      if (rn[j] >= tol || prec == FCG_FP32) sel.push_back(j);
-    const int nt = int(sel.size());
-    const int ldg = nv + R;
-    const double* Gall = W.h_out.p + R;  // [V T]^T T, (nv + R) x R
-    std::vector<double> S(size_t(nv) * nt), Gtt(size_t(nt) * nt);
-    for (int q = 0; q < nt; ++q) {
-      for (int i = 0; i < nv; ++i) S[i + size_t(nv) * q] = Gall[i + size_t(ldg) * sel[q]];
-      for (int p = 0; p < nt; ++p) Gtt[p + size_t(nt) * q] = Gall[nv + sel[p] + size_t(ldg) * sel[q]];
-    }
-    const int nv_old = nv;
-    if (nv + nt > kmax) {
-      // restart on span{Y, Yprev}: Q orthonormal (nv x q), V <- V Q, AV <- AV Q, Hs <- Q^T Hs Q
-      const int zc = R + ((gdk && yprev_rows > 0) ? R : 0);
-      std::vector<double> Q;
-      int q = 0;
-      for (int c = 0; c < zc; ++c) {
-        std::vector<double> z(nv, 0.0);
-        if (c < R)
-          for (int i = 0; i < nv; ++i) z[i] = Y[i + size_t(nv) * c];
-        else
-          for (int i = 0; i < yprev_rows; ++i) z[i] = Yprev[i + size_t(yprev_rows) * (c - R)];
-        double n0 = 0.0;
-        for (double x : z) n0 += x * x;
-        n0 = std::sqrt(n0);
-        for (int pass = 0; pass < 2; ++pass)
-          for (int k = 0; k < q; ++k) {
-            double d = 0.0;
-            for (int i = 0; i < nv; ++i) d += Q[i + size_t(nv) * k] * z[i];
-            for (int i = 0; i < nv; ++i) z[i] -= d * Q[i + size_t(nv) * k];
-          }
-        double nz = 0.0;
-        for (double x : z) nz += x * x;
-        nz = std::sqrt(nz);
-        if (!(nz > 1e-8 * n0)) continue;
-        for (double& x : z) x /= nz;
-        Q.insert(Q.end(), z.begin(), z.end());
-        ++q;
-      }
-      const double* dQ = nullptr;
-      if ((rc = W.upload(Q.data(), size_t(nv) * q, &dQ))) return rc;
-      if ((rc = W.flush())) return rc;
-      const unsigned g = unsigned((n + 255) / 256);
-      update_kernel<<<g, 256, 0, ctx->stream>>>(W.V.p, n, nv, dQ, q, W.tmp.p, n, n);
-      FCG_CUDA(cudaGetLastError());
-      FCG_CUDA(cudaMemcpyAsync(W.V.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
-      update_kernel<<<g, 256, 0, ctx->stream>>>(W.AV.p, n, nv, dQ, q, W.tmp.p, n, n);
-      FCG_CUDA(cudaGetLastError());
-      FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
-      std::vector<double> HQ(size_t(nv) * q, 0.0), Hn(size_t(q) * q, 0.0), Sn(size_t(q) * nt, 0.0),
-          Yp(size_t(q) * R, 0.0);
-      for (int c = 0; c < q; ++c)
-        for (int k = 0; k < nv; ++k) {
-          const double qk = Q[k + size_t(nv) * c];
-          for (int i = 0; i < nv; ++i) HQ[i + size_t(nv) * c] += Hs[i + size_t(kcap) * k] * qk;
-        }
-      for (int c = 0; c < q; ++c)
-        for (int r2 = 0; r2 < q; ++r2) {
-          double s = 0.0;
-          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * HQ[i + size_t(nv) * c];
-          Hn[r2 + size_t(q) * c] = s;
-        }
-      for (int c = 0; c < q; ++c)
-        for (int r2 = 0; r2 < c; ++r2) {
-          const double a = 0.5 * (Hn[r2 + size_t(q) * c] + Hn[c + size_t(q) * r2]);
-          Hn[r2 + size_t(q) * c] = Hn[c + size_t(q) * r2] = a;
-        }
-      for (int c = 0; c < nt; ++c)
-        for (int r2 = 0; r2 < q; ++r2) {
-          double s = 0.0;
-          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * S[i + size_t(nv) * c];
-          Sn[r2 + size_t(q) * c] = s;
-        }
-      for (int c = 0; c < R; ++c)
-        for (int r2 = 0; r2 < q; ++r2) {
-          double s = 0.0;
-          for (int i = 0; i < nv; ++i) s += Q[i + size_t(nv) * r2] * Y[i + size_t(nv) * c];
-          Yp[r2 + size_t(q) * c] = s;
-        }
-      for (int c = 0; c < q; ++c)
-        for (int r2 = 0; r2 < q; ++r2) Hs[r2 + size_t(kcap) * c] = Hn[r2 + size_t(q) * c];
-      S.swap(Sn);
-      Yprev.swap(Yp);
-      yprev_rows = q;
-      nv = q;
-    } else {
-      Yprev = Y;
-      yprev_rows = nv;
-    }
-    // the selected corrections move to V[:, nv : nv + nt] (never onto a later source column)
-    for (int q = 0; q < nt; ++q) {
-      const int src = nv_old + sel[q], dst = nv + q;
-      if (src != dst)
-        FCG_CUDA(cudaMemcpyAsync(W.V.p + n * dst, W.V.p + n * src, sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                                 ctx->stream));
-    }
-    std::vector<double> G0(size_t(nv + nt) * nt);
-    for (int c = 0; c < nt; ++c) {
-      for (int i = 0; i < nv; ++i) G0[i + size_t(nv + nt) * c] = S[i + size_t(nv) * c];
-      for (int p = 0; p < nt; ++p) G0[nv + p + size_t(nv + nt) * c] = Gtt[p + size_t(nt) * c];
-    }
-    if ((rc = W.orthonormalize(nv, nt, std::move(G0), drop, &m))) return rc;
-    if (m == 0) break;  // the subspace cannot grow: converged as far as lindep allows
-    if ((rc = sigma_closed_device_async(ctx, m, W.V.p + n * nv, W.AV.p + n * nv, prec))) return rc;
-    ++sigma_calls;
-    newlo = nv;
-    nv += m;
-  }
-  for (int j = 0; j < R; ++j) {
-    energies[j] = th[j];
-    residuals[j] = rn[j];
-  }
-  FCG_CUDA(cudaMemcpyAsync(vectors, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToHost, ctx->stream));
-  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  *iters = std::min(it, max_iter);
-  ctx->stats.davidson_sigma_calls = sigma_calls;
-  return FCG_OK;
+  if (rc == FCG_OK) rc = run_lockstep(runs, ctx);
+  cudaStreamSynchronize(ctx->stream);  // nothing of the group in flight when the streams change back
+  for (int q = 0; q < n; ++q) ctxs[q]->stream = saved[q];
+  return rc;
 }

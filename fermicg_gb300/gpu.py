@@ -51,6 +51,8 @@ SIGNATURES = {
     "fcg_bst_sigma_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_triples": (_I, [_P, _P]),
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
+    "fcg_davidson_grouped": (_I, [_I, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P,
+                                  _P]),
     "fcg_expectation": (_I, [_P, _I, _P, _P, _I]),
     "fcg_build_full_h": (_I, [_P, _P]),
     "fcg_bst_fois": (_I, [_P, _I, _I, ctypes.c_double, _I, _L, _P, _P, _P, _L, _P, _P, _P, ctypes.POINTER(_L),
@@ -346,6 +348,32 @@ def sigma_closed_grouped(gpus, d_c_ptrs, d_sigma_ptrs, roots, precision="fp64"):
     ss = (ctypes.c_void_p * n)(*[int(p) for p in d_sigma_ptrs])
     gpus[0]._check(L.fcg_sigma_closed_grouped(n, hs, rs, cs, ss, PRECISION[precision]), "fcg_sigma_closed_grouped")
     return gpus[0].stats()
+
+
+def davidson_grouped(gpus, guesses, max_iter=100, max_ss_vecs=12, tol=1e-8, lindep=1e-12, precision="fp64",
+                     precond=True):
+    """Davidson solves of independent problems (one GpuSigma each, state set) in lockstep, their
+    sigma builds grouped per iteration (fcg_davidson_grouped).  guesses: one (n_cfg, R) array
+    per problem.  Returns a list of (energies, vectors, residuals, iterations)."""
+    n = len(gpus)
+    if len(guesses) != n or n == 0:
+        raise ValueError("one guess per context")
+    L = gpus[0].L
+    vs = [np.asfortranarray(v, dtype=np.float64) for v in guesses]
+    for g, v in zip(gpus, vs):
+        if v.shape[0] != g.n_cfg:
+            raise ValueError("guess rows do not match the state")
+    es = [np.zeros(v.shape[1]) for v in vs]
+    rs = [np.zeros(v.shape[1]) for v in vs]
+    xs = [np.zeros(v.shape, order="F") for v in vs]
+    its = (ctypes.c_int * n)()
+    P = ctypes.c_void_p
+    gpus[0]._check(L.fcg_davidson_grouped(
+        n, (P * n)(*[g.h.value for g in gpus]), (ctypes.c_int * n)(*[v.shape[1] for v in vs]),
+        (P * n)(*[v.ctypes.data for v in vs]), int(max_iter), int(max_ss_vecs), float(tol), float(lindep),
+        PRECISION[precision], int(bool(precond)), (P * n)(*[e.ctypes.data for e in es]),
+        (P * n)(*[x.ctypes.data for x in xs]), (P * n)(*[r.ctypes.data for r in rs]), its), "fcg_davidson_grouped")
+    return [(es[q], np.ascontiguousarray(xs[q]), rs[q], its[q]) for q in range(n)]
 
 
 def tps_ci_matvec(state, gpu: GpuSigma, precision="fp64"):

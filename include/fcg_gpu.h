@@ -146,6 +146,18 @@ int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coef
 int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol, double lindep,
                  int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
+/* The Davidson solves of n independent problems (one context each, state set) in lockstep:
+ * every problem runs fcg_davidson's algorithm; their device work shares the first context's
+ * stream and each wait for it, and the sigma builds of their new blocks run as one grouped
+ * launch (fcg_sigma_closed_grouped) per precision.  The reference solves independent
+ * problems one after another (tps_ci_davidson, src/tpsci_outer.jl:364-454, per problem).
+ * Per problem q: R[q] roots, v0[q] / vectors[q] host column-major n_cfg_q x R[q],
+ * energies[q], residuals[q], iters[q]; the settings are shared.  All contexts on one device
+ * and distinct; errors name the problem. */
+int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* v0, int max_iter,
+                         int max_ss_vecs, double tol, double lindep, int precision, int precond,
+                         double* const* energies, double* const* vectors, double* const* residuals, int* iters);
+
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 
 /* The closed sigma (tps_ci_matvec, src/tpsci_outer.jl:462-527) of n independent problems in

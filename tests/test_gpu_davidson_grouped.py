@@ -1,0 +1,62 @@
+"""fcg_davidson_grouped: independent Davidson solves in lockstep with grouped sigma builds give
+each problem the same eigenpairs as its solve alone (and as a dense diagonalisation)."""
+import numpy as np
+import pytest
+
+import oracle
+from fermicg_gb300 import pack, workloads
+from fermicg_gb300.gpu import GpuSigma, davidson_grouped
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems(n, max_cluster=4):
+    out = []
+    for i in range(n):
+        prob, st = workloads.config3_instance(i, max_cluster=max_cluster, n_cfg_range=(300, 1500))
+        f, c, v, _ = pack.pack_state(st)
+        po, pt = pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham)
+        g = GpuSigma(0)
+        g.set_ops(po)
+        g.set_terms(pt)
+        g.state_set(f, c)
+        R = v.shape[1]
+        guess = np.zeros_like(v)
+        for r, k in enumerate(np.argsort(g.diagonal())[:R]):
+            guess[k, r] = 1.0
+        H = oracle.Oracle(po, pt).build_H(f, c)
+        out.append((g, guess, np.linalg.eigvalsh(0.5 * (H + H.T))[:R]))
+    return out
+
+
+@pytest.mark.parametrize("precision,tol_e", [("fp64", 1e-9), ("fp32", 1e-6)])
+def test_grouped_solves_equal_solo_solves(precision, tol_e):
+    probs = _problems(6)
+    gpus = [p[0] for p in probs]
+    res = davidson_grouped(gpus, [p[1] for p in probs], tol=1e-7, max_iter=300, precision=precision)
+    for (g, guess, ref), (e, X, r, it) in zip(probs, res):
+        assert np.abs(e - ref).max() < tol_e, (e, ref)
+        assert r.max() < 1e-7 and it > 0
+        np.testing.assert_allclose(X.T @ X, np.eye(len(e)), atol=1e-10)
+        e1, X1, r1, it1 = g.davidson(guess, tol=1e-7, max_iter=300, precision=precision)
+        assert np.abs(e - e1).max() < 1e-10
+        # same eigenvectors up to sign (the spectra here are not degenerate)
+        np.testing.assert_allclose(np.abs(np.sum(X * X1, axis=0)), 1.0, atol=1e-8)
+    for g in gpus:
+        g.close()
+
+
+def test_grouped_single_problem_is_fcg_davidson():
+    (g, guess, ref), = _problems(1)
+    e, X, r, it = davidson_grouped([g], [guess], tol=1e-8, max_iter=300)[0]
+    e1, X1, r1, it1 = g.davidson(guess, tol=1e-8, max_iter=300)
+    assert np.abs(e - ref).max() < 1e-9
+    assert np.abs(e - e1).max() < 1e-11 and it == it1
+    g.close()
+
+
+def test_grouped_rejects_a_context_twice():
+    (g, guess, ref), = _problems(1)
+    with pytest.raises(Exception):
+        davidson_grouped([g, g], [guess, guess])
+    g.close()
