@@ -29,9 +29,15 @@
 // builds in float32 until the residual norms reach max(tol, 1e-5), then restarts from
 // the Ritz vectors with float64 sigma builds (the refinement) until tol.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
+#include <condition_variable>
 #include <cstring>
+#include <deque>
+#include <map>
 #include <memory>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 #include "fcg_ctx.cuh"
@@ -1113,3 +1119,279 @@ extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, c
   for (int q = 0; q < n; ++q) ctxs[q]->stream = saved[q];
   return rc;
 }
+
+// ---- serving: continuous batching of Davidson solves ---------------------------------------
+//
+// A server owns one stream and a scheduler thread.  Callers prepare a context per request
+// (fcg_set_ops, fcg_set_terms, fcg_state_set -- in their own threads) and submit it with a
+// guess; the scheduler admits requests while slots and the memory budget allow, and runs all
+// admitted solves in lockstep rounds as fcg_davidson_grouped does: every round advances each
+// solve to its next need of the device, then serves all of them with one wait for the stream
+// or one grouped sigma launch per precision.  Solves that finish leave after the round,
+// queued requests join at the next, so a request's work overlaps with whatever is in flight.
+// A solve's result is the same as fcg_davidson's on its own (the grouped sigma adds each
+// problem's sums in another order).
+
+struct fcg_server {
+  int device = 0;
+  int max_active = 1;
+  double budget = 0;
+  cudaStream_t stream = nullptr;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done;
+  bool stop = false;
+  std::thread worker;
+  struct Ticket {
+    int64_t id = 0;
+    fcg_ctx* ctx = nullptr;
+    int R = 0, max_iter = 0, max_ss_vecs = 0, precision = 0, precond = 0;
+    double tol = 0, lindep = 0;
+    std::vector<double> v0, energies, vectors, residuals;
+    int iters = 0;
+    int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
+    int rc = 0;
+    std::string err;
+    double footprint = 0;
+  };
+  std::map<int64_t, std::shared_ptr<Ticket>> tickets;
+  std::deque<std::shared_ptr<Ticket>> queue;
+  int64_t next_id = 1;
+  double in_use = 0;
+
+  void loop();
+};
+
+namespace {
+
+struct Slot {
+  std::shared_ptr<fcg_server::Ticket> t;
+  std::unique_ptr<DavidsonRun> run;
+  cudaStream_t saved = nullptr;
+  int state = 0;  // 0 ready, 1 waiting, 2 sigma, 3 failed, 4 done
+  int rc = 0;
+};
+
+}  // namespace
+
+void fcg_server::loop() {
+  cudaSetDevice(device);
+  std::vector<Slot> active;
+  auto finish = [&](Slot& sl, int rc) {  // under the lock
+    sl.t->ctx->stream = sl.saved;
+    sl.t->rc = rc;
+    sl.t->state = rc == FCG_OK ? 2 : 3;
+    if (rc != FCG_OK) sl.t->err = sl.t->ctx->err;
+    in_use -= sl.t->footprint;
+    cv_done.notify_all();
+  };
+  for (;;) {
+    {
+      std::unique_lock<std::mutex> lk(mu);
+      while (!queue.empty() && int(active.size()) < max_active &&
+             (active.empty() || in_use + queue.front()->footprint <= budget)) {
+        auto t = queue.front();
+        queue.pop_front();
+        Slot sl;
+        sl.t = t;
+        sl.saved = t->ctx->stream;
+        t->ctx->stream = stream;
+        t->state = 1;
+        in_use += t->footprint;
+        sl.run.reset(new DavidsonRun());
+        lk.unlock();
+        const int rc = sl.run->init(t->ctx, t->R, t->v0.data(), t->max_iter, t->max_ss_vecs, t->tol, t->lindep,
+                                    t->precision, t->precond, t->energies.data(), t->vectors.data(),
+                                    t->residuals.data(), &t->iters);
+        lk.lock();
+        if (rc) {
+          cudaStreamSynchronize(stream);
+          finish(sl, rc);
+        } else {
+          active.push_back(std::move(sl));
+        }
+      }
+      if (active.empty()) {
+        if (stop && queue.empty()) return;
+        cv_work.wait_for(lk, std::chrono::milliseconds(20));
+        continue;
+      }
+    }
+    // one round over the admitted solves
+    for (size_t q = 0; q < active.size(); ++q) {
+      Slot& sl = active[q];
+      while (sl.state == 0) {
+        Act a = Act::kDone;
+        const int rc = sl.run->step(&a);
+        if (rc) {
+          sl.rc = rc;
+          sl.state = 3;
+          break;
+        }
+        sl.state = a == Act::kWait ? 1 : a == Act::kSigma ? 2 : 4;
+      }
+    }
+    bool waiting = false;
+    for (auto& sl : active) waiting = waiting || sl.state == 1;
+    int rc_round = FCG_OK;
+    if (waiting) {
+      rc_round = cudaStreamSynchronize(stream) == cudaSuccess ? FCG_OK : FCG_ECUDA;
+      for (auto& sl : active)
+        if (sl.state == 1) {
+          sl.run->W.after_wait();
+          sl.state = 0;
+        }
+    } else {
+      for (int p : {FCG_FP32, FCG_FP64}) {
+        std::vector<fcg_ctx*> cs;
+        std::vector<int> Rs;
+        std::vector<const double*> dc;
+        std::vector<double*> ds;
+        std::vector<Slot*> who;
+        for (auto& sl : active) {
+          DavidsonRun& r = *sl.run;
+          if (sl.state != 2 || r.sig_prec != p) continue;
+          const int64_t n = r.W.n;
+          cs.push_back(r.ctx);
+          Rs.push_back(r.sig_m);
+          dc.push_back(r.W.V.p + n * r.sig_col);
+          ds.push_back(r.W.AV.p + n * r.sig_col);
+          who.push_back(&sl);
+        }
+        if (cs.empty()) continue;
+        const int rc = fcg_sigma_closed_grouped(int(cs.size()), cs.data(), Rs.data(), dc.data(), ds.data(), p);
+        for (Slot* sl : who) {
+          if (rc) {
+            sl->state = 3;
+            sl->rc = rc;
+            sl->t->ctx->err = cs[0]->err;
+          } else {
+            sl->run->W.after_wait();
+            sl->state = 0;
+          }
+        }
+      }
+    }
+    // retire finished and failed solves
+    std::unique_lock<std::mutex> lk(mu);
+    std::vector<Slot> keep;
+    for (size_t q = 0; q < active.size(); ++q) {
+      Slot& sl = active[q];
+      if (sl.state == 4) {
+        finish(sl, FCG_OK);
+      } else if (sl.state == 3 || rc_round != FCG_OK) {
+        cudaStreamSynchronize(stream);
+        if (sl.state != 3) sl.t->ctx->err = "serving: the shared stream failed";
+        finish(sl, sl.state == 3 ? sl.rc : rc_round);
+      } else {
+        keep.push_back(std::move(sl));
+      }
+    }
+    active.swap(keep);
+  }
+}
+
+extern "C" {
+
+int fcg_server_create(int device, int max_active, double memory_budget, fcg_server** out) {
+  if (!out || max_active < 1 || !(memory_budget > 0)) return FCG_EINVAL;
+  *out = nullptr;
+  if (cudaSetDevice(device) != cudaSuccess) return FCG_ECUDA;
+  std::unique_ptr<fcg_server> s(new fcg_server());
+  s->device = device;
+  s->max_active = max_active;
+  s->budget = memory_budget;
+  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return FCG_ECUDA;
+  fcg_server* raw = s.get();
+  s->worker = std::thread([raw] { raw->loop(); });
+  *out = s.release();
+  return FCG_OK;
+}
+
+int fcg_server_destroy(fcg_server* s) {
+  if (!s) return FCG_EINVAL;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->stop = true;
+    for (auto& t : s->queue) {  // never admitted: failed, their contexts untouched
+      t->state = 3;
+      t->rc = FCG_ESTATE;
+      t->err = "serving: the server was destroyed before the request ran";
+    }
+    s->queue.clear();
+    s->cv_done.notify_all();
+  }
+  s->cv_work.notify_all();
+  s->worker.join();  // the admitted solves finish first (each is bounded by its max_iter)
+  cudaStreamDestroy(s->stream);
+  delete s;
+  return FCG_OK;
+}
+
+int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
+               double lindep, int precision, int precond, int64_t* ticket) {
+  if (!s || !ctx || !v0 || !ticket || R < 1 || R > kMaxB) return FCG_EINVAL;
+  if (!ctx->have_state || ctx->n_cfg < R) return FCG_ESTATE;
+  if (ctx->device != s->device) return FCG_EINVAL;
+  auto t = std::make_shared<fcg_server::Ticket>();
+  const int64_t n = ctx->n_cfg;
+  t->ctx = ctx;
+  t->R = R;
+  t->max_iter = max_iter;
+  t->max_ss_vecs = max_ss_vecs;
+  t->tol = tol;
+  t->lindep = lindep;
+  t->precision = precision;
+  t->precond = precond;
+  t->v0.assign(v0, v0 + n * R);
+  t->energies.assign(R, 0.0);
+  t->residuals.assign(R, 0.0);
+  t->vectors.assign(size_t(n) * R, 0.0);
+  // device memory the solve holds: V and H V (max_ss_vecs R + R columns), X, the restart
+  // scratch, the Gram partial sums and the float64 / float32 sigma copies
+  const double kcap = double(std::min<int64_t>(int64_t(std::max(max_ss_vecs, 2)) * R, n) + R);
+  t->footprint = 8.0 * double(n) * (2.0 * kcap + 6.0 * R) + 8.0 * 128.0 * kcap * R;
+  std::lock_guard<std::mutex> lk(s->mu);
+  for (auto& kv : s->tickets)
+    if (kv.second->ctx == ctx && kv.second->state < 2) return FCG_EINVAL;  // the context is busy
+  t->id = s->next_id++;
+  s->tickets[t->id] = t;
+  s->queue.push_back(t);
+  *ticket = t->id;
+  s->cv_work.notify_all();
+  return FCG_OK;
+}
+
+int fcg_poll(fcg_server* s, int64_t ticket, int* state) {
+  if (!s || !state) return FCG_EINVAL;
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FCG_EINVAL;
+  *state = it->second->state;
+  return FCG_OK;
+}
+
+int fcg_wait(fcg_server* s, int64_t ticket, int timeout_ms, double* energies, double* vectors, double* residuals,
+             int* iters) {
+  if (!s) return FCG_EINVAL;
+  std::unique_lock<std::mutex> lk(s->mu);
+  auto it = s->tickets.find(ticket);
+  if (it == s->tickets.end()) return FCG_EINVAL;
+  std::shared_ptr<fcg_server::Ticket> t = it->second;
+  const bool ended = s->cv_done.wait_for(lk, std::chrono::milliseconds(std::max(timeout_ms, 0)),
+                                         [&] { return t->state >= 2; });
+  if (!ended) return FCG_ETIMEDOUT;
+  if (t->state == 3) {
+    t->ctx->err = t->err;
+    const int rc = t->rc ? t->rc : FCG_ECUDA;
+    s->tickets.erase(it);
+    return rc;
+  }
+  if (energies) std::copy(t->energies.begin(), t->energies.end(), energies);
+  if (residuals) std::copy(t->residuals.begin(), t->residuals.end(), residuals);
+  if (vectors) std::copy(t->vectors.begin(), t->vectors.end(), vectors);
+  if (iters) *iters = t->iters;
+  s->tickets.erase(it);
+  return FCG_OK;
+}
+
+}  // extern "C"

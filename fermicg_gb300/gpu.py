@@ -53,6 +53,11 @@ SIGNATURES = {
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
     "fcg_davidson_grouped": (_I, [_I, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P,
                                   _P]),
+    "fcg_server_create": (_I, [_I, _I, ctypes.c_double, ctypes.POINTER(_P)]),
+    "fcg_server_destroy": (_I, [_P]),
+    "fcg_submit": (_I, [_P, _P, _I, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, ctypes.POINTER(_L)]),
+    "fcg_poll": (_I, [_P, _L, ctypes.POINTER(_I)]),
+    "fcg_wait": (_I, [_P, _L, _I, _P, _P, _P, ctypes.POINTER(_I)]),
     "fcg_expectation": (_I, [_P, _I, _P, _P, _I]),
     "fcg_build_full_h": (_I, [_P, _P]),
     "fcg_bst_fois": (_I, [_P, _I, _I, ctypes.c_double, _I, _L, _P, _P, _P, _L, _P, _P, _P, ctypes.POINTER(_L),

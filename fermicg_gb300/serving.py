@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .gpu import GpuSigma
+from .gpu import PRECISION, GpuSigma, _ptr
 
 
 @dataclass(order=True)
@@ -148,3 +148,97 @@ def latency_summary(results: list[Result]):
     span = max(r.end for r in results) - min(r.arrival for r in results)
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
             "mean_s": float(lat.mean()), "solves_per_s": len(results) / span, "n": len(results)}
+
+
+class NativeSolveServer:
+    """The library's continuous-batching server (fcg_server_create / fcg_submit / fcg_wait).
+
+    Each request is set up in a host thread of its own (a pooled context: fcg_set_ops,
+    fcg_set_terms, fcg_state_set) and submitted when ready; the library's scheduler thread
+    admits requests while fewer than `slots` run and the memory budget allows, and advances all
+    admitted solves together: one wait for its stream, or one grouped sigma launch per precision,
+    per round for all of them, with finished solves leaving and new ones joining between
+    rounds.  Latency runs from a request's arrival to its result, set-up included."""
+
+    def __init__(self, slots: int = 16, hbm_budget: float = 64e9, device: int = 0):
+        import ctypes
+        from .gpu import load_library
+        self._ct = ctypes
+        self.L = load_library()
+        h = ctypes.c_void_p()
+        rc = self.L.fcg_server_create(device, int(slots), float(hbm_budget), ctypes.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"fcg_server_create failed ({rc})")
+        self.h = h
+        self.device = device
+        self._free = []
+        self._lock = threading.Lock()
+        self.results: list[Result] = []
+
+    def _context(self):
+        with self._lock:
+            if self._free:
+                return self._free.pop()
+        return GpuSigma(self.device)
+
+    def _serve(self, req: Request, t0: float):
+        ct = self._ct
+        wait = req.arrival - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        start = time.perf_counter()
+        g = self._context()
+        try:
+            g.set_ops(req.packed_ops)
+            g.set_terms(req.packed_terms)
+            g.state_set(req.focks, req.cfgs)
+            v = np.asfortranarray(req.guess, dtype=np.float64)
+            n, R = v.shape
+            ticket = ct.c_int64(0)
+            g._check(self.L.fcg_submit(self.h, g.h, R, _ptr(v), int(req.max_iter), 12, float(req.tol), 1e-12,
+                                       PRECISION[req.precision], 1, ct.byref(ticket)), "fcg_submit")
+            e, res = np.zeros(R), np.zeros(R)
+            X = np.zeros((n, R), order="F")
+            it = ct.c_int(0)
+            while True:
+                rc = self.L.fcg_wait(self.h, ticket.value, 1000, _ptr(e), _ptr(X), _ptr(res), ct.byref(it))
+                if rc != -5:  # FCG_ETIMEDOUT: keep waiting
+                    break
+            g._check(rc, "fcg_wait")
+            end = time.perf_counter()
+            with self._lock:
+                self.results.append(Result(req.rid, req.shape, e, res, it.value, req.arrival, start, end))
+        finally:
+            with self._lock:
+                self._free.append(g)
+
+    def run(self, requests: list[Request], t0: float | None = None):
+        """Serve `requests` (arrival times relative to t0 = now); returns the results by id."""
+        t0 = time.perf_counter() if t0 is None else t0
+        reqs = sorted(requests)
+        for r in reqs:
+            r.arrival = t0 + r.arrival
+        errors = []
+
+        def work(r):
+            try:
+                self._serve(r, t0)
+            except Exception as ex:  # reported after all threads end
+                errors.append(ex)
+
+        threads = [threading.Thread(target=work, args=(r,), daemon=True) for r in reqs]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        if errors:
+            raise errors[0]
+        return sorted(self.results, key=lambda r: r.rid)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fcg_server_destroy(self.h)
+            self.h = None
+        for g in self._free:
+            g.close()
+        self._free = []

@@ -158,6 +158,30 @@ int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double
                          int max_ss_vecs, double tol, double lindep, int precision, int precond,
                          double* const* energies, double* const* vectors, double* const* residuals, int* iters);
 
+/* ---- serving: continuous batching of Davidson solves ---------------------------------
+ * A server owns a stream and a scheduler thread on `device`.  The caller prepares one
+ * context per request (fcg_set_ops, fcg_set_terms, fcg_state_set, in any thread) and submits
+ * it with a guess; the server admits requests while fewer than max_active run and their
+ * device memory (Davidson subspace and sigma copies) fits memory_budget bytes, and runs the
+ * admitted solves in lockstep rounds as fcg_davidson_grouped does: finished solves leave and
+ * queued ones join between rounds, so their sigma builds are grouped per iteration.  A
+ * submitted context belongs to the server until its ticket is waited for.  fcg_poll: state
+ * 0 queued, 1 running, 2 done, 3 failed.  fcg_wait returns FCG_ETIMEDOUT after timeout_ms
+ * (0: just look) and never blocks longer; on success it copies the results (energies R,
+ * vectors column-major n_cfg x R, residuals R, iterations; any may be null) and retires the
+ * ticket; a failed solve returns its error code with the message in fcg_last_error(ctx).
+ * fcg_server_destroy fails the queued requests, lets the running ones finish (each is
+ * bounded by its max_iter) and must come after the last wait.  The reference has no
+ * serving loop: each request is the tps_ci_davidson solve of fcg_davidson. */
+typedef struct fcg_server fcg_server;
+int fcg_server_create(int device, int max_active, double memory_budget, fcg_server** out);
+int fcg_server_destroy(fcg_server* s);
+int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
+               double lindep, int precision, int precond, int64_t* ticket);
+int fcg_poll(fcg_server* s, int64_t ticket, int* state);
+int fcg_wait(fcg_server* s, int64_t ticket, int timeout_ms, double* energies, double* vectors, double* residuals,
+             int* iters);
+
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 
 /* The closed sigma (tps_ci_matvec, src/tpsci_outer.jl:462-527) of n independent problems in
