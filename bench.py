@@ -53,6 +53,7 @@ def parse():
     ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
     ap.add_argument("--fois-only", action="store_true", help="run only the BST first-order space leg")
     ap.add_argument("--no-davidson", dest="davidson", action="store_false", help="skip the per-shape solve timings")
+    ap.add_argument("--serving-only", action="store_true", help="run only the solve-stream leg (both servers)")
     ap.add_argument("--davidson-only", action="store_true",
                     help="run only the per-shape Davidson solve timings of the serving shapes")
     ap.add_argument("--open-cfg", type=int, default=10000, help="variational configurations of the open sigma leg")
@@ -134,8 +135,7 @@ def davidson_benchmark(reps=2):
         prob = build(1001)
         st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=0)
         f, c, v, _ = pack.pack_state(st)
-        guess = np.zeros_like(v)
-        guess[:R] = np.eye(R)
+        guess = workloads.davidson_guess(f.shape[0], R, seed=0)
         po, pt = pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham)
         for prec in ("fp32", "fp64"):
             best = None
@@ -158,12 +158,12 @@ def davidson_benchmark(reps=2):
     return out
 
 
-def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16):
+def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4):
     """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
     per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
     stream.  Returns p50/p99 latency and solves/s per precision."""
     from fermicg_gb300 import pack, workloads
-    from fermicg_gb300.serving import Request, SolveServer, latency_summary
+    from fermicg_gb300.serving import NativeSolveServer, Request, SolveServer, latency_summary
     shapes = SERVING_SHAPES
     pools = []
     for k, (name, build, n_cfg, R, share) in enumerate(shapes):
@@ -172,8 +172,7 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16):
             prob = build(1000 * (k + 1) + j)
             st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=j)
             f, c, v, _ = pack.pack_state(st)
-            guess = np.zeros_like(v)
-            guess[:R] = np.eye(R)
+            guess = workloads.davidson_guess(f.shape[0], R, seed=j)
             pool.append((pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, guess))
         pools.append(pool)
     rng = np.random.default_rng(seed)
@@ -181,19 +180,28 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16):
     kinds = rng.choice(len(shapes), size=n_req, p=[sh[4] for sh in shapes])
     picks = [int(rng.integers(len(pools[k]))) for k in kinds]
     out = {}
-    for prec in ("fp32", "fp64"):
-        reqs = []
-        for i in range(n_req):
-            po, pt, f, c, guess = pools[kinds[i]][picks[i]]
-            reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
-                                shape=shapes[kinds[i]][0]))
-        srv = SolveServer(slots=slots)
-        res = srv.run(reqs)
-        srv.close()
-        summ = latency_summary(res)
-        summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
-                                  for sh in shapes}
-        out["mixed" if prec == "fp32" else "fp64"] = summ
+    for server in ("threads", "native"):
+        for prec in ("fp32", "fp64"):
+            reqs = []
+            for i in range(n_req):
+                po, pt, f, c, guess = pools[kinds[i]][picks[i]]
+                reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
+                                    shape=shapes[kinds[i]][0]))
+            srv = SolveServer(slots=slots) if server == "threads" else NativeSolveServer(slots=slots, lanes=lanes)
+            res = srv.run(reqs)
+            srv.close()
+            summ = latency_summary(res)
+            summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
+                                      for sh in shapes}
+            key = "mixed" if prec == "fp32" else "fp64"
+            if server == "threads":
+                out[key] = summ
+            else:
+                out.setdefault("native", {})[key] = summ
+    out["servers"] = {"threads": "one context, stream and host thread per slot; solves overlap on the GPU",
+                      "native": f"fcg_server: continuous batching in {lanes} lanes (a scheduler thread and a "
+                                "stream each); a lane's solves run in lockstep rounds, one grouped sigma launch "
+                                "per precision per round"}
     # same stream, same results: energies of mixed vs fp64 per request
     out["requests"] = n_req
     out["slots"] = slots
@@ -355,6 +363,32 @@ def batched_benchmark(steps, warmup, n_inst=256):
             "grouped_ms": grouped_ms, "sequential_ms": seq_ms,
             "problem_sigmas_per_s_grouped": n_inst * 1e3 / grouped_ms,
             "problem_sigmas_per_s_sequential": n_inst * 1e3 / seq_ms, "grouped_over_sequential": seq_ms / grouped_ms}
+    # whole Davidson solves of all instances (tol 1e-6): one after another, and in lockstep
+    # with their sigma builds grouped per iteration (fcg_davidson_grouped); the guesses have a
+    # seeded dense part, so every arm looks for the same (lowest) roots
+    from fermicg_gb300.gpu import davidson_grouped
+    guesses = [workloads.davidson_guess(n, R, seed=5000 + q, lowest=np.argsort(g.diagonal())[:R])
+               for q, (g, dc, ds, R, n) in enumerate(items)]
+    tol = 1e-6
+    solved = {}
+    for prec in ("fp32", "fp64"):
+        davidson_grouped(gs[:8], guesses[:8], tol=tol, max_iter=200, precision=prec)  # warm-up
+        t1 = time.perf_counter()
+        res = davidson_grouped(gs, guesses, tol=tol, max_iter=200, precision=prec)
+        grouped_s = time.perf_counter() - t1
+        t1 = time.perf_counter()
+        seq = [g.davidson(gu, tol=tol, max_iter=200, precision=prec) for g, gu in zip(gs, guesses)]
+        seq_s = time.perf_counter() - t1
+        solved[prec] = (res, seq)
+        dmax = max(float(np.abs(r[0] - q[0]).max()) for r, q in zip(res, seq))
+        out["solves_mixed" if prec == "fp32" else "solves_fp64"] = {
+            "grouped_s": grouped_s, "sequential_s": seq_s, "solves_per_s_grouped": n_inst / grouped_s,
+            "solves_per_s_sequential": n_inst / seq_s, "grouped_over_sequential": seq_s / grouped_s,
+            "max_energy_difference": dmax, "iterations_total": int(sum(r[3] for r in res)),
+            "not_converged_grouped": int(sum(r[2].max() >= tol for r in res)),
+            "not_converged_sequential": int(sum(q[2].max() >= tol for q in seq))}
+    out["solves_mixed"]["max_energy_difference_vs_fp64"] = max(
+        float(np.abs(a[0] - b[0]).max()) for a, b in zip(solved["fp32"][0], solved["fp64"][1]))
     for g in gs:
         g.close()
     return out
@@ -540,6 +574,10 @@ def main():
         if rank == 0:
             print(json.dumps({"open_sigma": open_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds,
                                                            n_cfg=a.open_cfg)}))
+        return
+    if a.serving_only:
+        if rank == 0:
+            print(json.dumps({"serving": serving_benchmark()}))
         return
     if a.davidson_only:
         if rank == 0:

@@ -551,6 +551,9 @@ struct DavidsonRun {
   fcg_ctx* ctx = nullptr;
   int R = 0, max_iter = 0, precond = 0, prec = 0;
   double tol = 0, drop = 0, switch_tol = 0;
+  // float32 phase: best largest residual so far and the iterations since it last fell by 10%
+  double best32 = 0;
+  int stall32 = 0;
   bool gdk = false;
   const double* v0 = nullptr;
   double *energies = nullptr, *vectors = nullptr, *residuals = nullptr;
@@ -787,7 +790,23 @@ int DavidsonRun::step(Act* act) {
           st = kFinish;
           break;
         }
-        if (prec == FCG_FP32 && rmax < switch_tol) {
+        bool to_fp64 = false;
+        if (prec == FCG_FP32) {
+          // The float32 sigma leaves a residual floor from its rounding of |H| |x| (measured
+          // 3-5e-7 * |theta| on 50-65 Eh problems); the solve moves to float64 below the larger
+          // of switch_tol and 5e-7 * |theta|, or once the residual has stopped falling
+          // (5 iterations without a 10% gain while below 1e-3).
+          double tmax = 0.0;
+          for (int j = 0; j < R; ++j) tmax = std::max(tmax, std::fabs(th[j]));
+          if (best32 == 0.0 || rmax < 0.9 * best32) {
+            best32 = rmax;
+            stall32 = 0;
+          } else {
+            ++stall32;
+          }
+          to_fp64 = rmax < std::max(switch_tol, 5e-7 * tmax) || (stall32 >= 5 && rmax < 1e-3);
+        }
+        if (to_fp64) {
           // refinement: restart from the Ritz vectors with float64 sigma builds
           prec = FCG_FP64;
           FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1134,13 +1153,14 @@ extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, c
 
 struct fcg_server {
   int device = 0;
-  int max_active = 1;
+  int max_active = 1;  // admitted solves over all lanes
+  int lanes = 1;       // scheduler threads, each with its own stream and lockstep group
   double budget = 0;
-  cudaStream_t stream = nullptr;
+  std::vector<cudaStream_t> streams;  // one per lane
   std::mutex mu;
   std::condition_variable cv_work, cv_done;
   bool stop = false;
-  std::thread worker;
+  std::vector<std::thread> workers;
   struct Ticket {
     int64_t id = 0;
     fcg_ctx* ctx = nullptr;
@@ -1157,8 +1177,9 @@ struct fcg_server {
   std::deque<std::shared_ptr<Ticket>> queue;
   int64_t next_id = 1;
   double in_use = 0;
+  int running = 0;  // admitted solves over all lanes
 
-  void loop();
+  void lane_loop(int lane);
 };
 
 namespace {
@@ -1173,8 +1194,14 @@ struct Slot {
 
 }  // namespace
 
-void fcg_server::loop() {
+// One lane: admits queued requests while it runs fewer than its share of max_active, the
+// server runs fewer than max_active and the memory budget allows (a request larger than the
+// budget runs when nothing else does), and advances its admitted solves in lockstep rounds on
+// its own stream.  Lanes overlap one another's kernels and host work.
+void fcg_server::lane_loop(int lane) {
   cudaSetDevice(device);
+  cudaStream_t stream = streams[lane];
+  const int share = (max_active + lanes - 1) / lanes;
   std::vector<Slot> active;
   auto finish = [&](Slot& sl, int rc) {  // under the lock
     sl.t->ctx->stream = sl.saved;
@@ -1182,13 +1209,15 @@ void fcg_server::loop() {
     sl.t->state = rc == FCG_OK ? 2 : 3;
     if (rc != FCG_OK) sl.t->err = sl.t->ctx->err;
     in_use -= sl.t->footprint;
+    --running;
     cv_done.notify_all();
+    cv_work.notify_all();  // memory and a slot are free for the other lanes
   };
   for (;;) {
     {
       std::unique_lock<std::mutex> lk(mu);
-      while (!queue.empty() && int(active.size()) < max_active &&
-             (active.empty() || in_use + queue.front()->footprint <= budget)) {
+      while (!queue.empty() && int(active.size()) < share && running < max_active &&
+             (running == 0 || in_use + queue.front()->footprint <= budget)) {
         auto t = queue.front();
         queue.pop_front();
         Slot sl;
@@ -1197,6 +1226,7 @@ void fcg_server::loop() {
         t->ctx->stream = stream;
         t->state = 1;
         in_use += t->footprint;
+        ++running;
         sl.run.reset(new DavidsonRun());
         lk.unlock();
         const int rc = sl.run->init(t->ctx, t->R, t->v0.data(), t->max_iter, t->max_ss_vecs, t->tol, t->lindep,
@@ -1292,17 +1322,25 @@ void fcg_server::loop() {
 
 extern "C" {
 
-int fcg_server_create(int device, int max_active, double memory_budget, fcg_server** out) {
-  if (!out || max_active < 1 || !(memory_budget > 0)) return FCG_EINVAL;
+int fcg_server_create(int device, int max_active, int lanes, double memory_budget, fcg_server** out) {
+  if (!out || max_active < 1 || lanes < 1 || lanes > 64 || !(memory_budget > 0)) return FCG_EINVAL;
   *out = nullptr;
   if (cudaSetDevice(device) != cudaSuccess) return FCG_ECUDA;
   std::unique_ptr<fcg_server> s(new fcg_server());
   s->device = device;
   s->max_active = max_active;
+  s->lanes = std::min(lanes, max_active);
   s->budget = memory_budget;
-  if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) return FCG_ECUDA;
+  for (int l = 0; l < s->lanes; ++l) {
+    cudaStream_t st = nullptr;
+    if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess) {
+      for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
+      return FCG_ECUDA;
+    }
+    s->streams.push_back(st);
+  }
   fcg_server* raw = s.get();
-  s->worker = std::thread([raw] { raw->loop(); });
+  for (int l = 0; l < s->lanes; ++l) s->workers.emplace_back([raw, l] { raw->lane_loop(l); });
   *out = s.release();
   return FCG_OK;
 }
@@ -1321,8 +1359,8 @@ int fcg_server_destroy(fcg_server* s) {
     s->cv_done.notify_all();
   }
   s->cv_work.notify_all();
-  s->worker.join();  // the admitted solves finish first (each is bounded by its max_iter)
-  cudaStreamDestroy(s->stream);
+  for (auto& w : s->workers) w.join();  // the admitted solves finish first (each is bounded by its max_iter)
+  for (cudaStream_t x : s->streams) cudaStreamDestroy(x);
   delete s;
   return FCG_OK;
 }

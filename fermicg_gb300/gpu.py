@@ -53,7 +53,7 @@ SIGNATURES = {
     "fcg_sigma_closed_grouped": (_I, [_I, _P, _P, _P, _P, _I]),
     "fcg_davidson_grouped": (_I, [_I, _P, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, _P, _P, _P,
                                   _P]),
-    "fcg_server_create": (_I, [_I, _I, ctypes.c_double, ctypes.POINTER(_P)]),
+    "fcg_server_create": (_I, [_I, _I, _I, ctypes.c_double, ctypes.POINTER(_P)]),
     "fcg_server_destroy": (_I, [_P]),
     "fcg_submit": (_I, [_P, _P, _I, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _I, ctypes.POINTER(_L)]),
     "fcg_poll": (_I, [_P, _L, ctypes.POINTER(_I)]),

@@ -154,19 +154,20 @@ class NativeSolveServer:
     """The library's continuous-batching server (fcg_server_create / fcg_submit / fcg_wait).
 
     Each request is set up in a host thread of its own (a pooled context: fcg_set_ops,
-    fcg_set_terms, fcg_state_set) and submitted when ready; the library's scheduler thread
-    admits requests while fewer than `slots` run and the memory budget allows, and advances all
-    admitted solves together: one wait for its stream, or one grouped sigma launch per precision,
-    per round for all of them, with finished solves leaving and new ones joining between
-    rounds.  Latency runs from a request's arrival to its result, set-up included."""
+    fcg_set_terms, fcg_state_set) and submitted when ready; the library's `lanes` scheduler
+    threads (a stream each) admit requests while fewer than `slots` run and the memory budget
+    allows, and each advances its admitted solves together: one wait for its stream, or one
+    grouped sigma launch per precision, per round for all of them, with finished solves
+    leaving and new ones joining between rounds.  Latency runs from a request's arrival to its
+    result, set-up included."""
 
-    def __init__(self, slots: int = 16, hbm_budget: float = 64e9, device: int = 0):
+    def __init__(self, slots: int = 16, hbm_budget: float = 64e9, device: int = 0, lanes: int = 4):
         import ctypes
         from .gpu import load_library
         self._ct = ctypes
         self.L = load_library()
         h = ctypes.c_void_p()
-        rc = self.L.fcg_server_create(device, int(slots), float(hbm_budget), ctypes.byref(h))
+        rc = self.L.fcg_server_create(device, int(slots), int(lanes), float(hbm_budget), ctypes.byref(h))
         if rc != 0:
             raise RuntimeError(f"fcg_server_create failed ({rc})")
         self.h = h

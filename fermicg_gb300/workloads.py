@@ -275,3 +275,18 @@ def config3_instance(i, base_seed=3000, max_cluster=5, n_cfg_range=(1000, 4000))
     n_cfg = int(rng.integers(n_cfg_range[0], n_cfg_range[1] + 1))
     st = energy_ordered_space(prob, n_cfg, R=R, seed=base_seed + i)
     return prob, st
+
+
+def davidson_guess(n, R, seed=0, lowest=None, spread=0.05):
+    """Starting block for R roots of an n-configuration problem: unit vectors on the
+    configurations `lowest` (default the first R, the lowest in an energy-ordered space; pass
+    the indices of the R smallest diagonal elements of H otherwise), plus a seeded dense part
+    of norm about `spread` per column.  The dense part gives the block a component in every
+    symmetry sector of H: unit vectors alone leave Davidson in the sectors they start in, and
+    floating-point rounding then decides whether the lowest root of another sector is found."""
+    rng = np.random.default_rng(seed)
+    g = (spread / np.sqrt(n)) * rng.standard_normal((n, R))
+    idx = range(R) if lowest is None else lowest
+    for r, k in enumerate(idx):
+        g[int(k), r] += 1.0
+    return g

@@ -159,12 +159,15 @@ int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double
                          double* const* energies, double* const* vectors, double* const* residuals, int* iters);
 
 /* ---- serving: continuous batching of Davidson solves ---------------------------------
- * A server owns a stream and a scheduler thread on `device`.  The caller prepares one
- * context per request (fcg_set_ops, fcg_set_terms, fcg_state_set, in any thread) and submits
- * it with a guess; the server admits requests while fewer than max_active run and their
- * device memory (Davidson subspace and sigma copies) fits memory_budget bytes, and runs the
- * admitted solves in lockstep rounds as fcg_davidson_grouped does: finished solves leave and
- * queued ones join between rounds, so their sigma builds are grouped per iteration.  A
+ * A server owns `lanes` scheduler threads on `device`, each with a stream of its own (lanes
+ * is clipped to max_active).  The caller prepares one context per request (fcg_set_ops,
+ * fcg_set_terms, fcg_state_set, in any thread) and submits it with a guess; a lane admits
+ * requests while it runs fewer than ceil(max_active / lanes), the server fewer than
+ * max_active, and their device memory (Davidson subspace and sigma copies) fits
+ * memory_budget bytes (a larger request runs when nothing else does).  Each lane runs its
+ * solves in lockstep rounds as fcg_davidson_grouped does: finished solves leave and queued
+ * ones join between rounds, so their sigma builds are grouped per iteration, while the lanes
+ * overlap one another's kernels and host work.  A
  * submitted context belongs to the server until its ticket is waited for.  fcg_poll: state
  * 0 queued, 1 running, 2 done, 3 failed.  fcg_wait returns FCG_ETIMEDOUT after timeout_ms
  * (0: just look) and never blocks longer; on success it copies the results (energies R,
@@ -174,7 +177,7 @@ int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double
  * bounded by its max_iter) and must come after the last wait.  The reference has no
  * serving loop: each request is the tps_ci_davidson solve of fcg_davidson. */
 typedef struct fcg_server fcg_server;
-int fcg_server_create(int device, int max_active, double memory_budget, fcg_server** out);
+int fcg_server_create(int device, int max_active, int lanes, double memory_budget, fcg_server** out);
 int fcg_server_destroy(fcg_server* s);
 int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
                double lindep, int precision, int precond, int64_t* ticket);

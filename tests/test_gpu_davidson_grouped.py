@@ -21,9 +21,7 @@ def _problems(n, max_cluster=4):
         g.set_terms(pt)
         g.state_set(f, c)
         R = v.shape[1]
-        guess = np.zeros_like(v)
-        for r, k in enumerate(np.argsort(g.diagonal())[:R]):
-            guess[k, r] = 1.0
+        guess = workloads.davidson_guess(f.shape[0], R, seed=i, lowest=np.argsort(g.diagonal())[:R])
         H = oracle.Oracle(po, pt).build_H(f, c)
         out.append((g, guess, np.linalg.eigvalsh(0.5 * (H + H.T))[:R]))
     return out

@@ -11,8 +11,7 @@ pytestmark = pytest.mark.gpu
 def _request(rid, prob, n_cfg, R, seed, arrival, precision="fp64"):
     st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=seed)
     f, c, v, _ = pack.pack_state(st)
-    guess = np.zeros_like(v)
-    guess[:R] = np.eye(R)  # lowest configurations first (energy-ordered space)
+    guess = workloads.davidson_guess(f.shape[0], R, seed=seed)  # lowest configurations first
     return Request(arrival, rid, pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, guess,
                    tol=1e-7, precision=precision, shape=f"{prob.meta['norb']}o")
 
@@ -40,9 +39,10 @@ def test_results_alone_equal_results_in_the_mix():
     assert s["p99_s"] >= s["p50_s"] > 0
 
 
-def test_native_server_results_equal_results_alone():
-    """fcg_server (continuous batching, grouped sigma builds): each request's energies equal its
-    solve alone."""
+@pytest.mark.parametrize("slots,lanes", [(3, 1), (4, 2)])
+def test_native_server_results_equal_results_alone(slots, lanes):
+    """fcg_server (continuous batching, grouped sigma builds; one lane, and two lanes of two
+    solves each): each request's energies equal its solve alone."""
     from fermicg_gb300.serving import NativeSolveServer
     p0 = workloads.build_problem(12, [3, 3, 3, 3], [(2, 1), (1, 2), (2, 1), (1, 2)], 36, 3, max_roots=1000)
     p1 = workloads.build_problem(16, [4, 4, 4, 4], [(2, 2)] * 4, 24, 4, max_roots=12, delta_elec=2)
@@ -55,7 +55,7 @@ def test_native_server_results_equal_results_alone():
         alone.append(srv.run([Request(0.0, r.rid, r.packed_ops, r.packed_terms, r.focks, r.cfgs, r.guess, r.tol,
                                       r.precision, r.max_iter, r.shape)])[0])
         srv.close()
-    srv = NativeSolveServer(slots=3)
+    srv = NativeSolveServer(slots=slots, lanes=lanes)
     mixed = srv.run(reqs)
     srv.close()
     assert [m.rid for m in mixed] == [r.rid for r in reqs]
@@ -70,7 +70,7 @@ def test_native_server_wait_times_out_and_a_failed_request_leaves_the_others():
     L = load_library()
     p0 = workloads.build_problem(12, [3, 3, 3, 3], [(2, 1), (1, 2), (2, 1), (1, 2)], 36, 3, max_roots=1000)
     h = ctypes.c_void_p()
-    assert L.fcg_server_create(0, 1, 1e10, ctypes.byref(h)) == 0
+    assert L.fcg_server_create(0, 1, 1, 1e10, ctypes.byref(h)) == 0
     gs, tickets, guesses = [], [], []
     for i in range(3):
         r = _request(i, p0, 1500, 1, 0, 0.0)  # requests 0 and 2 are the same solve
