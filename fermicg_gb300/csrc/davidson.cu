@@ -29,11 +29,13 @@
 // builds in float32 until the residual norms reach max(tol, 1e-5), then restarts from
 // the Ritz vectors with float64 sigma builds (the refinement) until tol.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -53,33 +55,94 @@ constexpr int kMaxB = 16;         // columns of the right-hand block of a Gram p
 constexpr int kMaxRowBlocks = 128;  // row blocks of a Gram product (partial sums per output)
 constexpr int kGramRows = 64;       // rows per row block while the block count allows
 
-// out[i + a*j] = sum_r A[r + lda*i] * B[r + ldb*j] for i < a, j < b <= BM.  The kernels of
-// this file are compiled for block widths BM = 1, 2, 4, 8, 16 and launched with the smallest
-// that fits: unrolled loops over unused columns would still issue their FP64 instructions.
-// Grid: x = row blocks, y = groups of 32 columns of A; a lane owns one column of A, each warp
-// a contiguous slice of the block's rows.  Each block writes its partial sums to
-// part[blk][i + a*j]; the last block of a column group to finish (counted in
-// counters[blockIdx.y], which it resets) adds the group's partials in row-block order, so
-// the result does not depend on the order in which blocks run.
+// One problem's share of a Davidson device operation.  Each kernel body below runs one
+// descriptor's block `blk` of `blocks`; a direct launch runs one descriptor (passed by value),
+// a grouped launch runs many (descriptors in device memory, ordered by `first`: CTA c works
+// for the descriptor whose [first, first + blocks) holds c), so that one launch serves every
+// problem of a lockstep round.
+struct GramDesc {  // out[i + a*j] = sum_r A[r + n*i] * B[r + n*j], i < a, j < b
+  const double* A;
+  const double* B;
+  double* part;
+  double* out;
+  unsigned* counters;
+  int64_t n, rows_per_block;
+  int a, b, row_blocks, first, blocks;
+};
+struct RitzDesc {  // Ritz vectors, residuals and corrections of R roots
+  const double* V;
+  const double* AV;
+  const double* Y;
+  const double* theta;
+  const double* hd;
+  double* X;
+  double* T;
+  double* rn_part;
+  double* rn_out;
+  unsigned* counter;
+  int64_t ld, n;
+  int nv, R, precond, first, blocks;
+};
+struct CombineDesc {  // T = V[:, nv : nv + kt] <- T M - V[:, :nv] P
+  double* V;
+  const double* M;
+  const double* P;
+  int64_t ld, n;
+  int nv, kt, mo, first, blocks;
+};
+struct UpdateDesc {  // C[:, j] = sum_i A[:, i] Y[i + a*j], j < b
+  const double* A;
+  const double* Y;
+  double* C;
+  int64_t lda, ldc, n;
+  int a, b, first, blocks;
+};
+constexpr int kMoveCols = 32;
+struct MoveDesc {  // dst[j][0 : n) = src[j][0 : n), j < cols
+  const double* src[kMoveCols];
+  double* dst[kMoveCols];
+  int64_t n;
+  int cols, first, blocks;
+};
+
+// index of the descriptor that CTA c works for (descriptors ordered by `first`)
+template <class D>
+__device__ __forceinline__ int find_desc(const D* ds, int nd, int c) {
+  int lo = 0, hi = nd - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (ds[mid].first <= c) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Gram product, block `blk` = row block + row_blocks * column group.  A lane owns one column
+// of A, each warp a contiguous slice of the block's rows.  Each block writes its partial sums
+// to part[row block][i + a*j]; the last block of a column group to finish (counted in
+// counters[group], which it resets) adds the group's partials in row-block order, so the
+// result does not depend on the order in which blocks run.  The kernels of this file are
+// compiled for block widths BM = 1, 2, 4, 8, 16 and launched with the smallest that fits:
+// unrolled loops over unused columns would still issue their FP64 instructions.
 template <int BM>
-__global__ void __launch_bounds__(kDavThreads) gram_kernel(const double* __restrict__ A, int64_t lda, int a,
-                                                           const double* __restrict__ B, int64_t ldb, int b, int64_t n,
-                                                           int64_t rows_per_block, double* __restrict__ part,
-                                                           double* __restrict__ out, unsigned* __restrict__ counters) {
+__device__ __forceinline__ void gram_body(const GramDesc& d, int blk) {
   __shared__ double red[kGramWarps][BM][32];
   __shared__ unsigned ticket;
+  const int rb = blk % d.row_blocks, group = blk / d.row_blocks;
+  const int a = d.a, b = d.b;
+  const int64_t n = d.n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int i = blockIdx.y * 32 + lane;
-  const int64_t r0 = int64_t(blockIdx.x) * rows_per_block;
-  const int64_t r1 = r0 + rows_per_block < n ? r0 + rows_per_block : n;
-  const int64_t slice = (rows_per_block + kGramWarps - 1) / kGramWarps;
+  const int i = group * 32 + lane;
+  const int64_t r0 = int64_t(rb) * d.rows_per_block;
+  const int64_t r1 = r0 + d.rows_per_block < n ? r0 + d.rows_per_block : n;
+  const int64_t slice = (d.rows_per_block + kGramWarps - 1) / kGramWarps;
   const int64_t s0 = r0 + warp * slice;
   const int64_t s1 = s0 + slice < r1 ? s0 + slice : r1;
   double acc[BM];
 #pragma unroll
   for (int j = 0; j < BM; ++j) acc[j] = 0.0;
   if (i < a) {
-    const double* Ai = A + lda * i;
+    const double* Ai = d.A + n * i;
     int64_t r = s0;
     for (; r + 8 <= s1; r += 8) {  // eight rows per step: independent loads in flight
       double x[8];
@@ -88,7 +151,7 @@ __global__ void __launch_bounds__(kDavThreads) gram_kernel(const double* __restr
 #pragma unroll
       for (int j = 0; j < BM; ++j)
         if (j < b) {
-          const double* Bj = B + ldb * j + r;
+          const double* Bj = d.B + n * j + r;
 #pragma unroll
           for (int u = 0; u < 8; ++u) acc[j] = fma(x[u], Bj[u], acc[j]);
         }
@@ -97,7 +160,7 @@ __global__ void __launch_bounds__(kDavThreads) gram_kernel(const double* __restr
       const double x = Ai[r];
 #pragma unroll
       for (int j = 0; j < BM; ++j)
-        if (j < b) acc[j] = fma(x, B[r + ldb * j], acc[j]);
+        if (j < b) acc[j] = fma(x, d.B[r + n * j], acc[j]);
     }
   }
 #pragma unroll
@@ -107,38 +170,26 @@ __global__ void __launch_bounds__(kDavThreads) gram_kernel(const double* __restr
   const int64_t P = int64_t(a) * b;
   for (int t = threadIdx.x; t < b * 32; t += blockDim.x) {
     const int j = t >> 5, l = t & 31;
-    const int col = blockIdx.y * 32 + l;
+    const int col = group * 32 + l;
     double s = 0.0;
     for (int w = 0; w < kGramWarps; ++w) s += red[w][j][l];
-    if (col < a) part[int64_t(blockIdx.x) * P + col + int64_t(a) * j] = s;
+    if (col < a) d.part[int64_t(rb) * P + col + int64_t(a) * j] = s;
   }
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) ticket = atomicAdd(counters + blockIdx.y, 1u);
+  if (threadIdx.x == 0) ticket = atomicAdd(d.counters + group, 1u);
   __syncthreads();
-  if (ticket != gridDim.x - 1) return;
+  if (ticket != unsigned(d.row_blocks) - 1u) return;
   for (int t = threadIdx.x; t < b * 32; t += blockDim.x) {
     const int j = t >> 5, l = t & 31;
-    const int col = blockIdx.y * 32 + l;
+    const int col = group * 32 + l;
     if (col >= a) continue;
     const int64_t p = col + int64_t(a) * j;
     double s = 0.0;
-    for (unsigned k = 0; k < gridDim.x; ++k) s += __ldcg(part + int64_t(k) * P + p);
-    out[p] = s;
+    for (int k = 0; k < d.row_blocks; ++k) s += __ldcg(d.part + int64_t(k) * P + p);
+    d.out[p] = s;
   }
-  if (threadIdx.x == 0) counters[blockIdx.y] = 0u;
-}
-
-// C[:, j] = sum_i A[:, i] * Y[i + a*j] for j < b (C and A must not overlap)
-__global__ void update_kernel(const double* __restrict__ A, int64_t lda, int a, const double* __restrict__ Y, int b,
-                              double* __restrict__ C, int64_t ldc, int64_t n) {
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  for (int j = 0; j < b; ++j) {
-    double s = 0.0;
-    for (int i = 0; i < a; ++i) s = fma(A[r + lda * i], Y[i + int64_t(a) * j], s);
-    C[r + ldc * j] = s;
-  }
+  if (threadIdx.x == 0) d.counters[group] = 0u;
 }
 
 // Ritz vectors and corrections for R roots: per row r,
@@ -148,23 +199,18 @@ __global__ void update_kernel(const double* __restrict__ A, int64_t lda, int a, 
 //   sums in rn_part, added in block order by the last block to finish).
 // Y (nv x R, column-major) and theta are staged in shared memory.
 template <int BM>
-__global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double* __restrict__ V,
-                                                                    const double* __restrict__ AV, int64_t ld, int nv,
-                                                                    const double* __restrict__ Y,
-                                                                    const double* __restrict__ theta,
-                                                                    const double* __restrict__ hd, int R, int64_t n,
-                                                                    double* __restrict__ X, double* __restrict__ T,
-                                                                    int precond, double* __restrict__ rn_part,
-                                                                    double* __restrict__ rn_out,
-                                                                    unsigned* __restrict__ counter) {
+__device__ __forceinline__ void ritz_body(const RitzDesc& d, int blk) {
   extern __shared__ double sm[];
-  double* sY = sm;              // nv * R
-  double* sth = sm + nv * R;    // R
   __shared__ double red[kDavThreads / 32][BM];
-  for (int t = threadIdx.x; t < nv * R; t += blockDim.x) sY[t] = Y[t];
-  for (int t = threadIdx.x; t < R; t += blockDim.x) sth[t] = theta[t];
+  __shared__ unsigned ticket;
+  const int nv = d.nv, R = d.R;
+  const int64_t n = d.n, ld = d.ld;
+  double* sY = sm;             // nv * R
+  double* sth = sm + nv * R;   // R
+  for (int t = threadIdx.x; t < nv * R; t += blockDim.x) sY[t] = d.Y[t];
+  for (int t = threadIdx.x; t < R; t += blockDim.x) sth[t] = d.theta[t];
   __syncthreads();
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  const int64_t r = int64_t(blk) * blockDim.x + threadIdx.x;
   double x[BM], hx[BM];
 #pragma unroll
   for (int j = 0; j < BM; ++j) x[j] = hx[j] = 0.0;
@@ -174,8 +220,8 @@ __global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         const bool in = i0 + u < nv;
-        v[u] = in ? V[r + ld * (i0 + u)] : 0.0;
-        av[u] = in ? AV[r + ld * (i0 + u)] : 0.0;
+        v[u] = in ? d.V[r + ld * (i0 + u)] : 0.0;
+        av[u] = in ? d.AV[r + ld * (i0 + u)] : 0.0;
       }
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
@@ -197,10 +243,10 @@ __global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double
     double res = 0.0;
     if (r < n) {
       res = hx[j] - sth[j] * x[j];
-      double d = precond ? sth[j] - hd[r] : 1.0;
-      if (fabs(d) < 1e-6) d = d < 0 ? -1e-6 : 1e-6;
-      X[r + n * j] = x[j];
-      T[r + ld * j] = res / d;
+      double den = d.precond ? sth[j] - d.hd[r] : 1.0;
+      if (fabs(den) < 1e-6) den = den < 0 ? -1e-6 : 1e-6;
+      d.X[r + n * j] = x[j];
+      d.T[r + ld * j] = res / den;
     }
     double s = res * res;
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
@@ -210,21 +256,20 @@ __global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double
   if (threadIdx.x < R) {
     double s = 0.0;
     for (int w = 0; w < int(blockDim.x >> 5); ++w) s += red[w][threadIdx.x];
-    rn_part[int64_t(blockIdx.x) * R + threadIdx.x] = s;
+    d.rn_part[int64_t(blk) * R + threadIdx.x] = s;
   }
   // the last block to finish adds the blocks' partial sums in block order
-  __shared__ unsigned ticket;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) ticket = atomicAdd(counter, 1u);
+  if (threadIdx.x == 0) ticket = atomicAdd(d.counter, 1u);
   __syncthreads();
-  if (ticket != gridDim.x - 1) return;
+  if (ticket != unsigned(d.blocks) - 1u) return;
   if (threadIdx.x < R) {
     double s = 0.0;
-    for (unsigned k = 0; k < gridDim.x; ++k) s += __ldcg(rn_part + int64_t(k) * R + threadIdx.x);
-    rn_out[threadIdx.x] = s;
+    for (int k = 0; k < d.blocks; ++k) s += __ldcg(d.rn_part + int64_t(k) * R + threadIdx.x);
+    d.rn_out[threadIdx.x] = s;
   }
-  if (threadIdx.x == 0) *counter = 0u;
+  if (threadIdx.x == 0) *d.counter = 0u;
 }
 
 // In place on the new block T = V[:, nv : nv + kt] (leading dimension ld):
@@ -232,19 +277,19 @@ __global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(const double
 // A thread owns a row: it reads the row's T entries before writing any (kt, mo <= BM).
 // M (kt x mo) and P (nv x mo) are staged in shared memory; P may be null (no projection).
 template <int BM>
-__global__ void __launch_bounds__(kDavThreads) combine_kernel(double* __restrict__ V, int64_t ld, int nv, int kt,
-                                                              const double* __restrict__ M,
-                                                              const double* __restrict__ P, int mo, int64_t n) {
+__device__ __forceinline__ void combine_body(const CombineDesc& d, int blk) {
   extern __shared__ double sm[];
+  const int nv = d.nv, kt = d.kt, mo = d.mo;
+  const int64_t ld = d.ld;
   double* sM = sm;            // kt * mo
   double* sP = sm + kt * mo;  // nv * mo
-  for (int t = threadIdx.x; t < kt * mo; t += blockDim.x) sM[t] = M[t];
-  if (P)
-    for (int t = threadIdx.x; t < nv * mo; t += blockDim.x) sP[t] = P[t];
+  for (int t = threadIdx.x; t < kt * mo; t += blockDim.x) sM[t] = d.M[t];
+  if (d.P)
+    for (int t = threadIdx.x; t < nv * mo; t += blockDim.x) sP[t] = d.P[t];
   __syncthreads();
-  const int64_t r = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
-  if (r >= n) return;
-  double* T = V + ld * nv;
+  const int64_t r = int64_t(blk) * blockDim.x + threadIdx.x;
+  if (r >= d.n) return;
+  double* T = d.V + ld * nv;
   double t_in[BM], out[BM];
 #pragma unroll
   for (int i = 0; i < BM; ++i) t_in[i] = i < kt ? T[r + ld * i] : 0.0;
@@ -258,11 +303,11 @@ __global__ void __launch_bounds__(kDavThreads) combine_kernel(double* __restrict
     }
     out[j] = s;
   }
-  if (P) {
+  if (d.P) {
     for (int i0 = 0; i0 < nv; i0 += 8) {  // eight columns' loads in flight before their use
       double v[8];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) v[u] = i0 + u < nv ? V[r + ld * (i0 + u)] : 0.0;
+      for (int u = 0; u < 8; ++u) v[u] = i0 + u < nv ? d.V[r + ld * (i0 + u)] : 0.0;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
         if (i0 + u >= nv) break;
@@ -278,16 +323,72 @@ __global__ void __launch_bounds__(kDavThreads) combine_kernel(double* __restrict
     if (j < mo) T[r + ld * j] = out[j];
 }
 
+// C[:, j] = sum_i A[:, i] * Y[i + a*j] for j < b (C and A must not overlap)
+__device__ __forceinline__ void update_body(const UpdateDesc& d, int blk) {
+  const int64_t r = int64_t(blk) * blockDim.x + threadIdx.x;
+  if (r >= d.n) return;
+  for (int j = 0; j < d.b; ++j) {
+    double s = 0.0;
+    for (int i = 0; i < d.a; ++i) s = fma(d.A[r + d.lda * i], d.Y[i + int64_t(d.a) * j], s);
+    d.C[r + d.ldc * j] = s;
+  }
+}
+
+// dst[j][r] = src[j][r]: a thread owns a row and reads all its sources before it writes a
+// destination, so a destination column may be another move's source
+__device__ __forceinline__ void move_body(const MoveDesc& d, int blk) {
+  const int64_t r = int64_t(blk) * blockDim.x + threadIdx.x;
+  if (r >= d.n) return;
+  double v[kMoveCols];
+#pragma unroll
+  for (int j = 0; j < kMoveCols; ++j)
+    if (j < d.cols) v[j] = d.src[j][r];
+#pragma unroll
+  for (int j = 0; j < kMoveCols; ++j)
+    if (j < d.cols) d.dst[j][r] = v[j];
+}
+
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) gram_kernel(GramDesc d) { gram_body<BM>(d, int(blockIdx.x)); }
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) ritz_residual_kernel(RitzDesc d) { ritz_body<BM>(d, int(blockIdx.x)); }
+template <int BM>
+__global__ void __launch_bounds__(kDavThreads) combine_kernel(CombineDesc d) { combine_body<BM>(d, int(blockIdx.x)); }
+__global__ void __launch_bounds__(kDavThreads) update_kernel(UpdateDesc d) { update_body(d, int(blockIdx.x)); }
+
+// grouped launches: one CTA per block of every descriptor
+#define FCG_GROUP_KERNEL(NAME, DESC, BODY)                                              \
+  template <int BM>                                                                     \
+  __global__ void __launch_bounds__(kDavThreads) NAME(const DESC* __restrict__ ds, int nd) { \
+    const int q = find_desc(ds, nd, int(blockIdx.x));                                   \
+    const DESC d = ds[q];                                                               \
+    BODY<BM>(d, int(blockIdx.x) - d.first);                                             \
+  }
+FCG_GROUP_KERNEL(gram_group_kernel, GramDesc, gram_body)
+FCG_GROUP_KERNEL(ritz_group_kernel, RitzDesc, ritz_body)
+FCG_GROUP_KERNEL(combine_group_kernel, CombineDesc, combine_body)
+#undef FCG_GROUP_KERNEL
+__global__ void __launch_bounds__(kDavThreads) update_group_kernel(const UpdateDesc* __restrict__ ds, int nd) {
+  const int q = find_desc(ds, nd, int(blockIdx.x));
+  const UpdateDesc d = ds[q];
+  update_body(d, int(blockIdx.x) - d.first);
+}
+__global__ void __launch_bounds__(kDavThreads) move_group_kernel(const MoveDesc* __restrict__ ds, int nd) {
+  const int q = find_desc(ds, nd, int(blockIdx.x));
+  const int first = ds[q].first;
+  move_body(ds[q], int(blockIdx.x) - first);
+}
+
 // the smallest compiled block width (1, 2, 4, 8, 16) that holds w columns
 inline int width_class(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : w <= 8 ? 8 : 16; }
 
-#define FCG_WIDTH_SWITCH(w, KERNEL, LAUNCH, ...)       \
-  switch (width_class(w)) {                            \
-    case 1: KERNEL<1><<<LAUNCH>>>(__VA_ARGS__); break; \
-    case 2: KERNEL<2><<<LAUNCH>>>(__VA_ARGS__); break; \
-    case 4: KERNEL<4><<<LAUNCH>>>(__VA_ARGS__); break; \
-    case 8: KERNEL<8><<<LAUNCH>>>(__VA_ARGS__); break; \
-    default: KERNEL<16><<<LAUNCH>>>(__VA_ARGS__); break; \
+#define FCG_WIDTH_SWITCH(w, KERNEL, GRID, BLOCK, SMEM, STREAM, ...)                \
+  switch (width_class(w)) {                                                        \
+    case 1: KERNEL<1><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 2: KERNEL<2><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 4: KERNEL<4><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    case 8: KERNEL<8><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;          \
+    default: KERNEL<16><<<GRID, BLOCK, SMEM, STREAM>>>(__VA_ARGS__); break;        \
   }
 
 }  // namespace
@@ -295,6 +396,38 @@ inline int width_class(int w) { return w <= 1 ? 1 : w <= 2 ? 2 : w <= 4 ? 4 : w 
 extern "C" int fcg_diagonal(fcg_ctx* ctx, int op_id, double* hd);
 
 namespace {
+
+// Device work of one problem recorded during a lockstep round, for the round's grouped launches.
+enum class OpKind : int { kGram, kRitz, kCombine, kUpdate, kMove };
+struct RecOp {
+  OpKind kind;
+  int width;    // block-width class of the kernel (0 for the width-free kernels)
+  size_t smem;  // dynamic shared memory bytes
+  union {
+    GramDesc g;
+    RitzDesc r;
+    CombineDesc c;
+    UpdateDesc u;
+    MoveDesc m;
+  };
+};
+constexpr int kMaxRoundOps = 16;  // device operations one problem records between two waits
+
+// Page-locked staging of a lockstep round with its device mirror: the problems' uploads and
+// the round's descriptors are reserved at [0, used) from any host thread, and one copy moves
+// them to the device before the round's launches.
+struct RoundArena {
+  PinnedBuf<unsigned char> h;
+  DevBuf<unsigned char> d;
+  std::atomic<size_t> used{0};
+  static constexpr size_t npos = ~size_t(0);
+  size_t cap() const { return std::min(h.n, d.n); }
+  size_t reserve(size_t bytes) {
+    bytes = (bytes + 15) & ~size_t(15);
+    const size_t off = used.fetch_add(bytes);
+    return off + bytes <= cap() ? off : npos;
+  }
+};
 
 struct DavidsonWork {
   fcg_ctx* ctx = nullptr;
@@ -308,11 +441,38 @@ struct DavidsonWork {
   int ngroups = 1;
   PinnedBuf<double> h_out, h_up;
   size_t up_used = 0, up_sent = 0;
+  size_t up_cap = 0, out_cap = 0;  // doubles staged between two waits; fetched values
+  double* hout = nullptr;          // the fetched values (h_out, or hout_vec in grouped mode)
+  std::vector<double> hout_vec;
+  // Grouped mode (arena set): device work is recorded in `ops` and launched with the other
+  // problems' work of the round; uploads go to the round's arena; the round copies
+  // d_out[0 : fetch_count) to hout, and fin_count doubles from fin_src to fin_dst.
+  RoundArena* arena = nullptr;
+  std::vector<RecOp> ops;
+  size_t fetch_count = 0;
+  const double* fin_src = nullptr;
+  double* fin_dst = nullptr;
+  size_t fin_count = 0;
 
-  // Stage `count` doubles in the pinned upload area and return where they will be on the
-  // device once flush() has queued the copy.  The area is reused only after the next fetch().
+  bool grouped() const { return arena != nullptr; }
+  int record(const RecOp& op) {
+    fcg_ctx* ctx = this->ctx;
+    FCG_REQUIRE(ops.size() < size_t(kMaxRoundOps), FCG_ELIMIT, "Davidson: too many device operations in a round");
+    ops.push_back(op);
+    return FCG_OK;
+  }
+
+  // Stage `count` doubles for the device and return where they will be once flush() (or the
+  // round's copy) has moved them.  The area is reused only after the next wait.
   int upload(const double* src, size_t count, const double** dptr) {
     fcg_ctx* ctx = this->ctx;
+    if (grouped()) {
+      const size_t off = arena->reserve(count * sizeof(double));
+      FCG_REQUIRE(off != RoundArena::npos, FCG_ELIMIT, "Davidson: round staging area exhausted");
+      if (count) std::memcpy(arena->h.p + off, src, count * sizeof(double));
+      *dptr = reinterpret_cast<const double*>(arena->d.p + off);
+      return FCG_OK;
+    }
     const size_t off = (up_used + 3) & ~size_t(3);
     FCG_REQUIRE(off + count <= h_up.n, FCG_ELIMIT, "Davidson: staging area exhausted");
     if (count) std::memcpy(h_up.p + off, src, count * sizeof(double));
@@ -323,6 +483,7 @@ struct DavidsonWork {
   // one host-to-device copy of everything staged since the last flush
   int flush() {
     fcg_ctx* ctx = this->ctx;
+    if (grouped()) return FCG_OK;
     if (up_used > up_sent)
       FCG_CUDA(cudaMemcpyAsync(d_up.p + up_sent, h_up.p + up_sent, (up_used - up_sent) * sizeof(double),
                                cudaMemcpyHostToDevice, ctx->stream));
@@ -333,18 +494,115 @@ struct DavidsonWork {
   int gram(const double* A, int a, const double* B, int b, double* out) {
     fcg_ctx* ctx = this->ctx;
     FCG_REQUIRE(a >= 1 && a <= kcap && b >= 1 && b <= R, FCG_ELIMIT, "Davidson: Gram block out of range");
-    const dim3 grid(unsigned(row_blocks), unsigned((a + 31) / 32));
-#define FCG_GRAM_LAUNCH grid, kDavThreads, 0, ctx->stream
-    FCG_WIDTH_SWITCH(b, gram_kernel, FCG_GRAM_LAUNCH, A, n, a, B, n, b, n, rows_per_block, part.p, out, counters.p)
-#undef FCG_GRAM_LAUNCH
+    RecOp op;
+    op.kind = OpKind::kGram;
+    op.width = width_class(b);
+    op.smem = 0;
+    GramDesc& d = op.g;
+    d = GramDesc{A, B, part.p, out, counters.p, n, rows_per_block, a, b, row_blocks, 0, row_blocks * ((a + 31) / 32)};
+    if (grouped()) return record(op);
+    FCG_WIDTH_SWITCH(b, gram_kernel, unsigned(d.blocks), kDavThreads, 0, ctx->stream, d)
     FCG_CUDA(cudaGetLastError());
     return FCG_OK;
   }
-  // queue h_out[0 : count) = d_out[0 : count); the values are there after the next wait for
+  // Ritz vectors X, corrections T = V[:, nv : nv + R] and squared residual norms d_out[0 : R)
+  int ritz(int nv, const double* dY, const double* dth, int precond) {
+    fcg_ctx* ctx = this->ctx;
+    RecOp op;
+    op.kind = OpKind::kRitz;
+    op.width = width_class(R);
+    op.smem = sizeof(double) * (size_t(nv) * R + R);
+    RitzDesc& d = op.r;
+    d = RitzDesc{V.p, AV.p, dY, dth, hd.p, X.p, V.p + n * nv, rn_part.p, d_out.p, counters.p + ngroups,
+                 n, n, nv, R, precond, 0, res_blocks};
+    if (grouped()) return record(op);
+    FCG_WIDTH_SWITCH(R, ritz_residual_kernel, unsigned(d.blocks), kDavThreads, op.smem, ctx->stream, d)
+    FCG_CUDA(cudaGetLastError());
+    return FCG_OK;
+  }
+  // C[:, :b] = A[:, :a] Y (Y on the device, a x b)
+  int update(const double* A, int a, const double* dY, int b, double* C) {
+    fcg_ctx* ctx = this->ctx;
+    RecOp op;
+    op.kind = OpKind::kUpdate;
+    op.width = 0;
+    op.smem = 0;
+    UpdateDesc& d = op.u;
+    d = UpdateDesc{A, dY, C, n, n, n, a, b, 0, int((n + kDavThreads - 1) / kDavThreads)};
+    if (grouped()) return record(op);
+    update_kernel<<<unsigned(d.blocks), kDavThreads, 0, ctx->stream>>>(d);
+    FCG_CUDA(cudaGetLastError());
+    return FCG_OK;
+  }
+  // columns dst[j] = src[j] (n doubles each), j < cols.  Direct mode copies the columns in
+  // order, grouped mode row by row with a row's sources read before its destinations are
+  // written; both agree when a destination is at most an earlier column's source.
+  int move(int cols, const double* const* src, double* const* dst) {
+    fcg_ctx* ctx = this->ctx;
+    FCG_REQUIRE(cols >= 0 && cols <= kMoveCols, FCG_ELIMIT, "Davidson: too many columns in one move");
+    if (cols == 0) return FCG_OK;
+    if (grouped()) {
+      RecOp op;
+      op.kind = OpKind::kMove;
+      op.width = 0;
+      op.smem = 0;
+      MoveDesc& d = op.m;
+      for (int j = 0; j < cols; ++j) {
+        d.src[j] = src[j];
+        d.dst[j] = dst[j];
+      }
+      d.n = n;
+      d.cols = cols;
+      d.first = 0;
+      d.blocks = int((n + kDavThreads - 1) / kDavThreads);
+      return record(op);
+    }
+    for (int j = 0; j < cols; ++j)
+      FCG_CUDA(cudaMemcpyAsync(dst[j], src[j], sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
+    return FCG_OK;
+  }
+  // the contiguous columns dst[:, :cols] = src[:, :cols] (leading dimension n, no overlap)
+  int copy_block(double* dst, const double* src, int cols) {
+    fcg_ctx* ctx = this->ctx;
+    if (!grouped()) {
+      FCG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * n * cols, cudaMemcpyDeviceToDevice, ctx->stream));
+      return FCG_OK;
+    }
+    const double* s[kMoveCols];
+    double* t[kMoveCols];
+    for (int c0 = 0; c0 < cols; c0 += kMoveCols) {
+      const int m = std::min(kMoveCols, cols - c0);
+      for (int j = 0; j < m; ++j) {
+        s[j] = src + n * (c0 + j);
+        t[j] = dst + n * (c0 + j);
+      }
+      const int rc = move(m, s, t);
+      if (rc) return rc;
+    }
+    return FCG_OK;
+  }
+  // queue hout[0 : count) = d_out[0 : count); the values are there after the next wait for
   // the stream, after which after_wait() frees the staging area
   int enqueue_fetch(size_t count) {
     fcg_ctx* ctx = this->ctx;
+    FCG_REQUIRE(count <= out_cap, FCG_ELIMIT, "Davidson: fetch larger than its buffer");
+    if (grouped()) {
+      fetch_count = count;
+      return FCG_OK;
+    }
     FCG_CUDA(cudaMemcpyAsync(h_out.p, d_out.p, count * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    return FCG_OK;
+  }
+  // queue dst[0 : count) = src[0 : count) to the host (the final vectors)
+  int fetch_final(double* dst, const double* src, size_t count) {
+    fcg_ctx* ctx = this->ctx;
+    if (grouped()) {
+      fin_dst = dst;
+      fin_src = src;
+      fin_count = count;
+      return FCG_OK;
+    }
+    FCG_CUDA(cudaMemcpyAsync(dst, src, sizeof(double) * count, cudaMemcpyDeviceToHost, ctx->stream));
     return FCG_OK;
   }
   void after_wait() { up_used = up_sent = 0; }
@@ -358,11 +616,14 @@ struct DavidsonWork {
     const bool proj = P && nv > 0;
     if (proj && (rc = upload(P->data(), size_t(nv) * mo, &dP))) return rc;
     if ((rc = flush())) return rc;
-    const size_t smem = sizeof(double) * (size_t(kt) * mo + (proj ? size_t(nv) * mo : 0));
-    const unsigned blocks = unsigned((n + kDavThreads - 1) / kDavThreads);
-#define FCG_COMBINE_LAUNCH blocks, kDavThreads, smem, ctx->stream
-    FCG_WIDTH_SWITCH(std::max(kt, mo), combine_kernel, FCG_COMBINE_LAUNCH, V.p, n, nv, kt, dM, dP, mo, n)
-#undef FCG_COMBINE_LAUNCH
+    RecOp op;
+    op.kind = OpKind::kCombine;
+    op.width = width_class(std::max(kt, mo));
+    op.smem = sizeof(double) * (size_t(kt) * mo + (proj ? size_t(nv) * mo : 0));
+    CombineDesc& d = op.c;
+    d = CombineDesc{V.p, dM, dP, n, n, nv, kt, mo, 0, int((n + kDavThreads - 1) / kDavThreads)};
+    if (grouped()) return record(op);
+    FCG_WIDTH_SWITCH(std::max(kt, mo), combine_kernel, unsigned(d.blocks), kDavThreads, op.smem, ctx->stream, d)
     FCG_CUDA(cudaGetLastError());
     return FCG_OK;
   }
@@ -435,7 +696,7 @@ int DavidsonWork::ortho_resume(bool* wait) {
   if (o_state == 1) {
     o_state = 0;
     const int k1 = o_k1, ld1 = nv + k1;
-    const double* G1 = h_out.p;
+    const double* G1 = hout;
     o_S2.assign(size_t(nv) * k1, 0.0);
     for (int q = 0; q < k1; ++q)
       for (int i = 0; i < nv; ++i) o_S2[i + size_t(nv) * q] = G1[i + size_t(ld1) * q];
@@ -457,7 +718,7 @@ int DavidsonWork::ortho_resume(bool* wait) {
   if (o_state == 2) {  // the second Cholesky QR (and projection)
     o_state = 0;
     const int good = o_good, ld3 = nv + good;
-    const double* G3 = h_out.p;
+    const double* G3 = hout;
     std::vector<double> S3(size_t(nv) * good), G3t(size_t(good) * good);
     for (int q = 0; q < good; ++q)
       for (int i = 0; i < nv; ++i) S3[i + size_t(nv) * q] = G3[i + size_t(ld3) * q];
@@ -568,8 +829,10 @@ struct DavidsonRun {
   int yprev_rows = 0;
   int sig_col = 0, sig_m = 0, sig_prec = 0;
 
+  // grouped: the solve runs in a lockstep round executor, which provides W.arena before the
+  // first step (no staging buffers of its own are allocated)
   int init(fcg_ctx* c, int R_, const double* v0_, int max_iter_, int max_ss_vecs, double tol_, double lindep,
-           int precision, int precond_, double* e, double* vecs, double* res, int* its) {
+           int precision, int precond_, double* e, double* vecs, double* res, int* its, bool grouped = false) {
     ctx = c;
     R = R_;
     v0 = v0_;
@@ -610,6 +873,16 @@ struct DavidsonRun {
       FCG_CUDA(cudaFuncSetAttribute(combine_kernel<4>, attr, sm));
       FCG_CUDA(cudaFuncSetAttribute(combine_kernel<8>, attr, sm));
       FCG_CUDA(cudaFuncSetAttribute(combine_kernel<16>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_group_kernel<1>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_group_kernel<2>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_group_kernel<4>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_group_kernel<8>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(ritz_group_kernel<16>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_group_kernel<1>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_group_kernel<2>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_group_kernel<4>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_group_kernel<8>, attr, sm));
+      FCG_CUDA(cudaFuncSetAttribute(combine_group_kernel<16>, attr, sm));
     }
     W.row_blocks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxRowBlocks, (n + kGramRows - 1) / kGramRows)));
     W.rows_per_block = (n + W.row_blocks - 1) / W.row_blocks;
@@ -624,18 +897,23 @@ struct DavidsonRun {
     W.ngroups = (kcap + 31) / 32;
     FCG_CUDA(W.counters.alloc(size_t(W.ngroups) + 1));
     FCG_CUDA(cudaMemsetAsync(W.counters.p, 0, sizeof(unsigned) * (W.ngroups + 1), ctx->stream));
-    const size_t out_cap = size_t(R) + size_t(kcap) * R + 16;
-    const size_t up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
-    FCG_CUDA(W.d_out.alloc(out_cap));
-    FCG_CUDA(W.h_out.alloc(out_cap));
-    FCG_CUDA(W.d_up.alloc(up_cap));
-    FCG_CUDA(W.h_up.alloc(up_cap));
+    W.out_cap = size_t(R) + size_t(kcap) * R + 16;
+    W.up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
+    FCG_CUDA(W.d_out.alloc(W.out_cap));
+    if (grouped) {
+      W.hout_vec.assign(W.out_cap, 0.0);
+      W.hout = W.hout_vec.data();
+    } else {
+      FCG_CUDA(W.h_out.alloc(W.out_cap));
+      FCG_CUDA(W.d_up.alloc(W.up_cap));
+      FCG_CUDA(W.h_up.alloc(W.up_cap));
+      W.hout = W.h_out.p;
+    }
     if (precond) {
       std::vector<double> hd(n);
-      int rc = fcg_diagonal(ctx, -1, hd.data());
+      int rc = fcg_diagonal(ctx, -1, hd.data());  // leaves the diagonal in ctx->d_hd as well
       if (rc) return rc;
-      FCG_CUDA(cudaMemcpyAsync(W.hd.p, hd.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-      FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // hd is a local vector
+      FCG_CUDA(cudaMemcpyAsync(W.hd.p, ctx->d_hd.p, sizeof(double) * n, cudaMemcpyDeviceToDevice, ctx->stream));
     }
     // a new direction must keep at least this fraction of its norm after projection
     drop = std::max(lindep, 1e-8);
@@ -677,7 +955,7 @@ int DavidsonRun::step(Act* act) {
         *act = Act::kWait;
         return FCG_OK;
       case kInitG0: {
-        std::vector<double> G0(W.h_out.p, W.h_out.p + size_t(R) * R);
+        std::vector<double> G0(W.hout, W.hout + size_t(R) * R);
         if ((rc = W.ortho_start(0, R, std::move(G0), drop, &wait))) return rc;
         st = wait ? kInitOrtho : kInitDone;
         if (wait) {
@@ -738,7 +1016,7 @@ int DavidsonRun::step(Act* act) {
       }
       case kRRWait: {  // the projected eigenproblem; Ritz vectors, residuals, corrections, [V T]^T T
         const int nb = nv - newlo;
-        const double* C = W.h_out.p;
+        const double* C = W.hout;
         for (int c = 0; c < nb; ++c) {
           const int col = newlo + c;
           for (int i = 0; i < nv; ++i) {
@@ -764,12 +1042,7 @@ int DavidsonRun::step(Act* act) {
         if ((rc = W.upload(Y.data(), size_t(nv) * R, &dY))) return rc;
         if ((rc = W.upload(th.data(), size_t(R), &dth))) return rc;
         if ((rc = W.flush())) return rc;
-        const size_t ritz_smem = sizeof(double) * (size_t(nv) * R + R);
-#define FCG_RITZ_LAUNCH unsigned(W.res_blocks), kDavThreads, ritz_smem, ctx->stream
-        FCG_WIDTH_SWITCH(R, ritz_residual_kernel, FCG_RITZ_LAUNCH, W.V.p, W.AV.p, n, nv, dY, dth, W.hd.p, R, n, W.X.p,
-                         W.V.p + n * nv, precond, W.rn_part.p, W.d_out.p, W.counters.p + W.ngroups)
-#undef FCG_RITZ_LAUNCH
-        FCG_CUDA(cudaGetLastError());
+        if ((rc = W.ritz(nv, dY, dth, precond))) return rc;
         if ((rc = W.gram(W.V.p, nv + R, W.V.p + n * nv, R, W.d_out.p + R))) return rc;
         if ((rc = W.enqueue_fetch(size_t(R) + size_t(nv + R) * R))) return rc;
         st = kResWait;
@@ -779,7 +1052,7 @@ int DavidsonRun::step(Act* act) {
       case kResWait: {
         double rmax = 0.0;
         for (int j = 0; j < R; ++j) {
-          rn[j] = std::sqrt(W.h_out.p[j]);
+          rn[j] = std::sqrt(W.hout[j]);
           rmax = std::max(rmax, rn[j]);
           if (!std::isfinite(rn[j]) || !std::isfinite(th[j])) {
             ctx->err = "Davidson: non-finite residual or Ritz value at iteration " + std::to_string(it);
@@ -809,7 +1082,7 @@ int DavidsonRun::step(Act* act) {
         if (to_fp64) {
           // refinement: restart from the Ritz vectors with float64 sigma builds
           prec = FCG_FP64;
-          FCG_CUDA(cudaMemcpyAsync(W.V.p, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToDevice, ctx->stream));
+          if ((rc = W.copy_block(W.V.p, W.X.p, R))) return rc;
           if ((rc = W.gram(W.V.p, R, W.V.p, R, W.d_out.p))) return rc;
           if ((rc = W.enqueue_fetch(size_t(R) * R))) return rc;
           st = kSwG0;
@@ -847,7 +1120,7 @@ int DavidsonRun::step(Act* act) {
         st = kIter;
         break;
       case kSwG0: {
-        std::vector<double> G0(W.h_out.p, W.h_out.p + size_t(R) * R);
+        std::vector<double> G0(W.hout, W.hout + size_t(R) * R);
         if ((rc = W.ortho_start(0, R, std::move(G0), drop, &wait))) return rc;
         st = wait ? kSwOrtho : kSwDone;
         if (wait) {
@@ -884,7 +1157,7 @@ int DavidsonRun::step(Act* act) {
           energies[j] = th[j];
           residuals[j] = rn[j];
         }
-        FCG_CUDA(cudaMemcpyAsync(vectors, W.X.p, sizeof(double) * n * R, cudaMemcpyDeviceToHost, ctx->stream));
+        if ((rc = W.fetch_final(vectors, W.X.p, size_t(n) * R))) return rc;
         *iters = std::min(it, max_iter);
         ctx->stats.davidson_sigma_calls = sigma_calls;
         st = kFinished;
@@ -909,7 +1182,7 @@ int DavidsonRun::new_directions(bool* wait) {
     if (rn[j] >= tol || prec == FCG_FP32) sel.push_back(j);
   const int nt = int(sel.size());
   const int ldg = nv + R;
-  const double* Gall = W.h_out.p + R;  // [V T]^T T, (nv + R) x R
+  const double* Gall = W.hout + R;  // [V T]^T T, (nv + R) x R
   std::vector<double> S(size_t(nv) * nt), Gtt(size_t(nt) * nt);
   for (int q = 0; q < nt; ++q) {
     for (int i = 0; i < nv; ++i) S[i + size_t(nv) * q] = Gall[i + size_t(ldg) * sel[q]];
@@ -946,13 +1219,10 @@ int DavidsonRun::new_directions(bool* wait) {
     const double* dQ = nullptr;
     if ((rc = W.upload(Q.data(), size_t(nv) * q, &dQ))) return rc;
     if ((rc = W.flush())) return rc;
-    const unsigned g = unsigned((n + 255) / 256);
-    update_kernel<<<g, 256, 0, ctx->stream>>>(W.V.p, n, nv, dQ, q, W.tmp.p, n, n);
-    FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaMemcpyAsync(W.V.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
-    update_kernel<<<g, 256, 0, ctx->stream>>>(W.AV.p, n, nv, dQ, q, W.tmp.p, n, n);
-    FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaMemcpyAsync(W.AV.p, W.tmp.p, sizeof(double) * n * q, cudaMemcpyDeviceToDevice, ctx->stream));
+    if ((rc = W.update(W.V.p, nv, dQ, q, W.tmp.p))) return rc;
+    if ((rc = W.copy_block(W.V.p, W.tmp.p, q))) return rc;
+    if ((rc = W.update(W.AV.p, nv, dQ, q, W.tmp.p))) return rc;
+    if ((rc = W.copy_block(W.AV.p, W.tmp.p, q))) return rc;
     std::vector<double> HQ(size_t(nv) * q, 0.0), Hn(size_t(q) * q, 0.0), Sn(size_t(q) * nt, 0.0),
         Yp(size_t(q) * R, 0.0);
     for (int c = 0; c < q; ++c)
@@ -994,11 +1264,18 @@ int DavidsonRun::new_directions(bool* wait) {
     yprev_rows = nv;
   }
   // the selected corrections move to V[:, nv : nv + nt] (never onto a later source column)
-  for (int q = 0; q < nt; ++q) {
-    const int src = nv_old + sel[q], dst = nv + q;
-    if (src != dst)
-      FCG_CUDA(cudaMemcpyAsync(W.V.p + n * dst, W.V.p + n * src, sizeof(double) * n, cudaMemcpyDeviceToDevice,
-                               ctx->stream));
+  {
+    const double* srcs[kMaxB];
+    double* dsts[kMaxB];
+    int moves = 0;
+    for (int q = 0; q < nt; ++q) {
+      const int src = nv_old + sel[q], dst = nv + q;
+      if (src == dst) continue;
+      srcs[moves] = W.V.p + n * src;
+      dsts[moves] = W.V.p + n * dst;
+      ++moves;
+    }
+    if ((rc = W.move(moves, srcs, dsts))) return rc;
   }
   std::vector<double> G0(size_t(nv + nt) * nt);
   for (int c = 0; c < nt; ++c) {
@@ -1015,79 +1292,384 @@ extern "C" int fcg_sigma_closed_grouped(int n, fcg_ctx* const* ctxs, const int* 
 
 namespace {
 
-// Drive the problems to completion on the leader's stream: every round runs each ready
-// problem until it needs the device; then either one wait for the stream serves all problems
-// that queued work, or -- when every unfinished problem asks for its sigma -- the sigma builds
-// run (one asynchronous launch for a single problem, one grouped launch per precision for
-// several), and the round repeats.
-int run_lockstep(std::vector<std::unique_ptr<DavidsonRun>>& runs, fcg_ctx* leader) {
-  fcg_ctx* ctx = leader;
-  enum { kReady, kWaiting, kSigma, kDone };
-  const int P = int(runs.size());
-  std::vector<int> state(P, kReady);
-  int active = P;
-  while (active > 0) {
-    for (int q = 0; q < P; ++q) {
-      if (state[q] != kReady) continue;
-      Act a = Act::kDone;
-      const int rc = runs[q]->step(&a);
-      if (rc) {
-        if (runs[q]->ctx != leader) leader->err = runs[q]->ctx->err + " (problem " + std::to_string(q) + ")";
-        return rc;
-      }
-      state[q] = a == Act::kWait ? kWaiting : a == Act::kSigma ? kSigma : kDone;
-      if (a == Act::kDone) --active;
-    }
-    bool waiting = false;
-    for (int q = 0; q < P; ++q) waiting = waiting || state[q] == kWaiting;
-    if (waiting) {
+// One problem alone on its context's stream: waits and asynchronous sigma builds as it asks.
+int run_solo(DavidsonRun& r) {
+  fcg_ctx* ctx = r.ctx;
+  for (;;) {
+    Act a = Act::kDone;
+    const int rc = r.step(&a);
+    if (rc) return rc;
+    if (a == Act::kDone) return FCG_OK;
+    if (a == Act::kWait) {
       FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-      for (int q = 0; q < P; ++q)
-        if (state[q] == kWaiting) {
-          runs[q]->W.after_wait();
-          state[q] = kReady;
+      r.W.after_wait();
+    } else {
+      const int64_t n = r.W.n;
+      const int rs = sigma_closed_device_async(ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col,
+                                               r.sig_prec);
+      if (rs) return rs;
+    }
+  }
+}
+
+// Host threads that run fn(i), i < count, together with the calling thread.
+class StepPool {
+ public:
+  explicit StepPool(int helpers) {
+    for (int i = 0; i < helpers; ++i) th_.emplace_back([this] { work(); });
+  }
+  ~StepPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      quit_ = true;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void run(int count, const std::function<void(int)>& fn) {
+    if (th_.empty() || count < 4) {
+      for (int i = 0; i < count; ++i) fn(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &fn;
+      count_ = count;
+      next_.store(0);
+      pending_ = int(th_.size());
+      ++gen_;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  void drain() {
+    for (int i = next_.fetch_add(1); i < count_; i = next_.fetch_add(1)) (*fn_)(i);
+  }
+  void work() {
+    int seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return quit_ || gen_ != seen; });
+        if (quit_) return;
+        seen = gen_;
+      }
+      drain();
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_.notify_all();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* fn_ = nullptr;
+  int count_ = 0, pending_ = 0, gen_ = 0;
+  std::atomic<int> next_{0};
+  bool quit_ = false;
+};
+
+// fetched values of one problem to the round's output area
+struct GatherDesc {
+  const double* src;
+  double* dst;
+  int64_t n;
+  int first, blocks;
+};
+__global__ void __launch_bounds__(kDavThreads) gather_group_kernel(const GatherDesc* __restrict__ ds, int nd) {
+  const int q = find_desc(ds, nd, int(blockIdx.x));
+  const GatherDesc d = ds[q];
+  const int64_t r = int64_t(int(blockIdx.x) - d.first) * blockDim.x + threadIdx.x;
+  if (r < d.n) d.dst[r] = d.src[r];
+}
+
+#define FCG_LS_CUDA(call)                                                  \
+  do {                                                                     \
+    cudaError_t e_ = (call);                                               \
+    if (e_ != cudaSuccess) {                                               \
+      err = std::string(#call) + ": " + cudaGetErrorString(e_);            \
+      return e_ == cudaErrorMemoryAllocation ? FCG_ENOMEM : FCG_ECUDA;     \
+    }                                                                      \
+  } while (0)
+
+// Independent Davidson solves advanced together on one stream.  A round steps every ready
+// problem until it needs the device (the host work of different problems on the step pool's
+// threads), then runs the device work all of them recorded: one copy of the round's uploads
+// and descriptors to the device; the operations level by level (each problem's i-th
+// operation in level i, one grouped launch per kernel and block width in a level, so every
+// problem's operations keep their order); the fetched values gathered into one area and
+// copied to the host at once; the sigma builds asked for, as one grouped launch per
+// precision; and one wait for the stream.  The problems' contexts must use this stream.
+class Lockstep {
+ public:
+  enum State { kReady, kWaiting, kSigma, kDone, kFailed };
+  struct Entry {
+    DavidsonRun* run;
+    int state;
+    int rc;
+  };
+  std::vector<Entry> entries;
+  std::string err;  // what made round() fail
+  int64_t rounds = 0, launches = 0;
+  double step_s = 0, issue_s = 0, wait_s = 0;  // host stepping, issuing, sigma builds and waits
+
+  Lockstep(cudaStream_t s, int helpers) : stream_(s), pool_(helpers) {}
+
+  // A problem joins between rounds (its init ran with grouped = true); nothing may be in
+  // flight on the stream from an earlier round, as the staging areas may move.
+  int add(DavidsonRun* r) {
+    need_in_ += in_bytes(*r);
+    need_out_ += out_doubles(*r);
+    if (need_in_ > arena_.cap()) {
+      const size_t cap = need_in_ + need_in_ / 2 + (size_t(64) << 10);
+      FCG_LS_CUDA(arena_.h.alloc(cap));
+      FCG_LS_CUDA(arena_.d.alloc(cap));
+    }
+    if (need_out_ > out_h_.n || need_out_ > out_d_.n) {
+      const size_t cap = need_out_ + need_out_ / 2 + 1024;
+      FCG_LS_CUDA(out_h_.alloc(cap));
+      FCG_LS_CUDA(out_d_.alloc(cap));
+    }
+    r->W.arena = &arena_;
+    entries.push_back({r, kReady, FCG_OK});
+    return FCG_OK;
+  }
+  void erase(size_t i) {
+    need_in_ -= in_bytes(*entries[i].run);
+    need_out_ -= out_doubles(*entries[i].run);
+    entries.erase(entries.begin() + i);
+  }
+  bool running() const {
+    for (const Entry& e : entries)
+      if (e.state == kReady) return true;
+    return false;
+  }
+  int round();
+
+ private:
+  enum LaunchKind { kLGram, kLRitz, kLCombine, kLUpdate, kLMove, kLGather };
+  struct Launch {
+    int kind, width;
+    size_t smem, off;
+    int nd, blocks;
+  };
+  static size_t in_bytes(const DavidsonRun& r) {
+    return r.W.up_cap * sizeof(double) + 16 * 16 + size_t(kMaxRoundOps) * (sizeof(MoveDesc) + 16) +
+           sizeof(GatherDesc) + 16;
+  }
+  static size_t out_doubles(const DavidsonRun& r) { return r.W.out_cap + 2; }
+  static int width_index(int w) { return w <= 0 ? 0 : w == 1 ? 1 : w == 2 ? 2 : w == 4 ? 3 : w == 8 ? 4 : 5; }
+
+  // descriptors of one launch into the arena, numbered by their first block
+  template <class D, class Get>
+  int put(int kind, int width, size_t smem, size_t count, Get get) {
+    const size_t off = arena_.reserve(count * sizeof(D));
+    if (off == RoundArena::npos) {
+      err = "Davidson rounds: staging area exhausted";
+      return FCG_ELIMIT;
+    }
+    D* h = reinterpret_cast<D*>(arena_.h.p + off);
+    int first = 0;
+    for (size_t k = 0; k < count; ++k) {
+      D d = get(k);
+      d.first = first;
+      first += d.blocks;
+      h[k] = d;
+    }
+    launches_.push_back({kind, width, smem, off, int(count), first});
+    return FCG_OK;
+  }
+  int launch(const Launch& L) {
+    const unsigned g = unsigned(L.blocks);
+    const unsigned char* p = arena_.d.p + L.off;
+    switch (L.kind) {
+      case kLGram:
+        FCG_WIDTH_SWITCH(L.width, gram_group_kernel, g, kDavThreads, 0, stream_,
+                         reinterpret_cast<const GramDesc*>(p), L.nd)
+        break;
+      case kLRitz:
+        FCG_WIDTH_SWITCH(L.width, ritz_group_kernel, g, kDavThreads, L.smem, stream_,
+                         reinterpret_cast<const RitzDesc*>(p), L.nd)
+        break;
+      case kLCombine:
+        FCG_WIDTH_SWITCH(L.width, combine_group_kernel, g, kDavThreads, L.smem, stream_,
+                         reinterpret_cast<const CombineDesc*>(p), L.nd)
+        break;
+      case kLUpdate:
+        update_group_kernel<<<g, kDavThreads, 0, stream_>>>(reinterpret_cast<const UpdateDesc*>(p), L.nd);
+        break;
+      case kLMove:
+        move_group_kernel<<<g, kDavThreads, 0, stream_>>>(reinterpret_cast<const MoveDesc*>(p), L.nd);
+        break;
+      default:
+        gather_group_kernel<<<g, kDavThreads, 0, stream_>>>(reinterpret_cast<const GatherDesc*>(p), L.nd);
+        break;
+    }
+    FCG_LS_CUDA(cudaGetLastError());
+    ++launches;
+    return FCG_OK;
+  }
+
+  cudaStream_t stream_;
+  StepPool pool_;
+  RoundArena arena_;
+  DevBuf<double> out_d_;
+  PinnedBuf<double> out_h_;
+  size_t need_in_ = 0, need_out_ = 0;
+  std::vector<Launch> launches_;
+};
+
+int Lockstep::round() {
+  std::vector<int> ready;
+  for (int i = 0; i < int(entries.size()); ++i)
+    if (entries[i].state == kReady) ready.push_back(i);
+  if (ready.empty()) return FCG_OK;
+  ++rounds;
+  using clock = std::chrono::steady_clock;
+  const auto t0 = clock::now();
+  arena_.used.store(0);
+  pool_.run(int(ready.size()), [&](int k) {
+    Entry& e = entries[ready[k]];
+    DavidsonWork& W = e.run->W;
+    W.ops.clear();
+    W.fetch_count = W.fin_count = 0;
+    Act a = Act::kDone;
+    const int rc = e.run->step(&a);
+    if (rc) {  // nothing of a failed step runs
+      e.state = kFailed;
+      e.rc = rc;
+      W.ops.clear();
+      W.fetch_count = W.fin_count = 0;
+      return;
+    }
+    e.state = a == Act::kWait ? kWaiting : a == Act::kSigma ? kSigma : kDone;
+  });
+  const auto t1 = clock::now();
+  step_s += std::chrono::duration<double>(t1 - t0).count();
+  // the recorded operations, level by level
+  launches_.clear();
+  size_t levels = 0;
+  for (int i : ready) levels = std::max(levels, entries[i].run->W.ops.size());
+  static constexpr int kWidths[6] = {0, 1, 2, 4, 8, 16};
+  std::vector<const RecOp*> bucket[5][6];
+  int rc;
+  for (size_t lev = 0; lev < levels; ++lev) {
+    for (auto& row : bucket)
+      for (auto& b : row) b.clear();
+    for (int i : ready) {
+      const std::vector<RecOp>& ops = entries[i].run->W.ops;
+      if (lev < ops.size()) bucket[int(ops[lev].kind)][width_index(ops[lev].width)].push_back(&ops[lev]);
+    }
+    for (int kd = 0; kd < 5; ++kd)
+      for (int wi = 0; wi < 6; ++wi) {
+        const std::vector<const RecOp*>& b = bucket[kd][wi];
+        if (b.empty()) continue;
+        size_t smem = 0;
+        for (const RecOp* op : b) smem = std::max(smem, op->smem);
+        const int w = kWidths[wi];
+        switch (OpKind(kd)) {
+          case OpKind::kGram:
+            rc = put<GramDesc>(kLGram, w, smem, b.size(), [&](size_t k) { return b[k]->g; });
+            break;
+          case OpKind::kRitz:
+            rc = put<RitzDesc>(kLRitz, w, smem, b.size(), [&](size_t k) { return b[k]->r; });
+            break;
+          case OpKind::kCombine:
+            rc = put<CombineDesc>(kLCombine, w, smem, b.size(), [&](size_t k) { return b[k]->c; });
+            break;
+          case OpKind::kUpdate:
+            rc = put<UpdateDesc>(kLUpdate, w, smem, b.size(), [&](size_t k) { return b[k]->u; });
+            break;
+          default:
+            rc = put<MoveDesc>(kLMove, w, smem, b.size(), [&](size_t k) { return b[k]->m; });
+            break;
         }
-      continue;
-    }
-    if (P == 1) {
-      if (state[0] == kSigma) {
-        DavidsonRun& r = *runs[0];
-        const int64_t n = r.W.n;
-        const int rc = sigma_closed_device_async(r.ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col,
-                                                 r.sig_prec);
         if (rc) return rc;
-        state[0] = kReady;
       }
-      continue;
+  }
+  // the fetched values of every problem into one area
+  std::vector<std::pair<int, size_t>> fetched;  // entry, offset in the output area
+  size_t out_used = 0;
+  for (int i : ready) {
+    const DavidsonWork& W = entries[i].run->W;
+    if (!W.fetch_count) continue;
+    fetched.push_back({i, out_used});
+    out_used += (W.fetch_count + 1) & ~size_t(1);
+  }
+  if (out_used > out_d_.n) {
+    err = "Davidson rounds: output area exhausted";
+    return FCG_ELIMIT;
+  }
+  if (!fetched.empty()) {
+    rc = put<GatherDesc>(kLGather, 0, 0, fetched.size(), [&](size_t k) {
+      const DavidsonWork& W = entries[fetched[k].first].run->W;
+      return GatherDesc{W.d_out.p, out_d_.p + fetched[k].second, int64_t(W.fetch_count), 0,
+                        int((W.fetch_count + kDavThreads - 1) / kDavThreads)};
+    });
+    if (rc) return rc;
+  }
+  const size_t staged = std::min(arena_.used.load(), arena_.cap());
+  if (staged) FCG_LS_CUDA(cudaMemcpyAsync(arena_.d.p, arena_.h.p, staged, cudaMemcpyHostToDevice, stream_));
+  for (const Launch& L : launches_)
+    if ((rc = launch(L))) return rc;
+  if (out_used)
+    FCG_LS_CUDA(cudaMemcpyAsync(out_h_.p, out_d_.p, out_used * sizeof(double), cudaMemcpyDeviceToHost, stream_));
+  for (int i : ready) {
+    const DavidsonWork& W = entries[i].run->W;
+    if (W.fin_count)
+      FCG_LS_CUDA(cudaMemcpyAsync(W.fin_dst, W.fin_src, W.fin_count * sizeof(double), cudaMemcpyDeviceToHost,
+                                  stream_));
+  }
+  const auto t2 = clock::now();
+  issue_s += std::chrono::duration<double>(t2 - t1).count();
+  // the sigma builds, one grouped launch per precision
+  for (int p : {FCG_FP32, FCG_FP64}) {
+    std::vector<fcg_ctx*> cs;
+    std::vector<int> Rs;
+    std::vector<const double*> dc;
+    std::vector<double*> ds;
+    for (int i : ready) {
+      const DavidsonRun& r = *entries[i].run;
+      if (entries[i].state != kSigma || r.sig_prec != p) continue;
+      const int64_t n = r.W.n;
+      cs.push_back(r.ctx);
+      Rs.push_back(r.sig_m);
+      dc.push_back(r.W.V.p + n * r.sig_col);
+      ds.push_back(r.W.AV.p + n * r.sig_col);
     }
-    for (int p : {FCG_FP32, FCG_FP64}) {
-      std::vector<fcg_ctx*> cs;
-      std::vector<int> Rs, who;
-      std::vector<const double*> dc;
-      std::vector<double*> ds;
-      for (int q = 0; q < P; ++q) {
-        DavidsonRun& r = *runs[q];
-        if (state[q] != kSigma || r.sig_prec != p) continue;
-        const int64_t n = r.W.n;
-        cs.push_back(r.ctx);
-        Rs.push_back(r.sig_m);
-        dc.push_back(r.W.V.p + n * r.sig_col);
-        ds.push_back(r.W.AV.p + n * r.sig_col);
-        who.push_back(q);
-      }
-      if (cs.empty()) continue;
-      const int rc = fcg_sigma_closed_grouped(int(cs.size()), cs.data(), Rs.data(), dc.data(), ds.data(), p);
-      if (rc) {
-        if (cs[0] != leader) leader->err = cs[0]->err;
-        return rc;
-      }
-      for (int q : who) {
-        runs[q]->W.after_wait();
-        state[q] = kReady;
-      }
+    if (cs.empty()) continue;
+    rc = cs.size() == 1 ? sigma_closed_device_async(cs[0], Rs[0], dc[0], ds[0], p)
+                        : fcg_sigma_closed_grouped(int(cs.size()), cs.data(), Rs.data(), dc.data(), ds.data(), p);
+    if (rc) {
+      err = cs[0]->err;
+      return rc;
+    }
+    launches += 3;
+  }
+  FCG_LS_CUDA(cudaStreamSynchronize(stream_));
+  wait_s += std::chrono::duration<double>(clock::now() - t2).count();
+  for (const auto& f : fetched) {
+    DavidsonWork& W = entries[f.first].run->W;
+    std::memcpy(W.hout, out_h_.p + f.second, W.fetch_count * sizeof(double));
+  }
+  for (int i : ready) {
+    Entry& e = entries[i];
+    if (e.state == kWaiting || e.state == kSigma) {
+      e.run->W.after_wait();
+      e.state = kReady;
     }
   }
   return FCG_OK;
+}
+
+// host threads that help a lockstep executor step its problems
+int step_helpers(int share) {
+  const int hw = int(std::max(1u, std::thread::hardware_concurrency()));
+  return std::max(0, std::min(15, hw / std::max(share, 1) - 1));
 }
 
 }  // namespace
@@ -1097,12 +1679,11 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
                             double* residuals, int* iters) {
   if (!ctx) return FCG_EINVAL;
   FCG_CUDA(cudaSetDevice(ctx->device));
-  std::vector<std::unique_ptr<DavidsonRun>> runs;
-  runs.emplace_back(new DavidsonRun());
-  const int rc = runs[0]->init(ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, precond, energies, vectors,
-                               residuals, iters);
+  DavidsonRun run;
+  const int rc = run.init(ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, precond, energies, vectors,
+                          residuals, iters);
   if (rc) return rc;
-  return run_lockstep(runs, ctx);
+  return run_solo(run);
 }
 
 extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* v0, int max_iter,
@@ -1119,36 +1700,62 @@ extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, c
     for (int q2 = 0; q2 < q; ++q2) FCG_REQUIRE(ctxs[q2] != ctxs[q], FCG_EINVAL, "a context appears twice in the group");
   }
   FCG_CUDA(cudaSetDevice(ctx->device));
+  if (n == 1)
+    return fcg_davidson(ctx, R[0], v0[0], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[0],
+                        vectors[0], residuals[0], &iters[0]);
   // every problem's work goes to the leader's stream while the group is solved
   std::vector<cudaStream_t> saved(n);
   for (int q = 0; q < n; ++q) {
     saved[q] = ctxs[q]->stream;
     ctxs[q]->stream = ctx->stream;
   }
-  std::vector<std::unique_ptr<DavidsonRun>> runs;
   int rc = FCG_OK;
-  for (int q = 0; q < n && rc == FCG_OK; ++q) {
-    runs.emplace_back(new DavidsonRun());
-    rc = runs[q]->init(ctxs[q], R[q], v0[q], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[q],
-                       vectors[q], residuals[q], &iters[q]);
-    if (rc && q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
+  {
+    std::vector<std::unique_ptr<DavidsonRun>> runs;
+    Lockstep L(ctx->stream, step_helpers(1));
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int q = 0; q < n && rc == FCG_OK; ++q) {
+      runs.emplace_back(new DavidsonRun());
+      rc = runs[q]->init(ctxs[q], R[q], v0[q], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[q],
+                         vectors[q], residuals[q], &iters[q], true);
+      if (rc && q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
+      if (rc == FCG_OK && (rc = L.add(runs[q].get()))) ctx->err = L.err;
+    }
+    const double setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    while (rc == FCG_OK && L.running()) {
+      if ((rc = L.round())) {
+        ctx->err = L.err;
+        break;
+      }
+      for (int q = 0; q < n; ++q)
+        if (L.entries[q].state == Lockstep::kFailed) {
+          rc = L.entries[q].rc;
+          if (q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
+          break;
+        }
+    }
+    cudaStreamSynchronize(ctx->stream);  // nothing of the group in flight when the runs go
+    ctx->stats.group_rounds = L.rounds;
+    ctx->stats.group_launches = L.launches;
+    ctx->stats.group_setup_seconds = setup_s;
+    ctx->stats.group_step_seconds = L.step_s;
+    ctx->stats.group_issue_seconds = L.issue_s;
+    ctx->stats.group_wait_seconds = L.wait_s;
   }
-  if (rc == FCG_OK) rc = run_lockstep(runs, ctx);
-  cudaStreamSynchronize(ctx->stream);  // nothing of the group in flight when the streams change back
   for (int q = 0; q < n; ++q) ctxs[q]->stream = saved[q];
   return rc;
 }
 
 // ---- serving: continuous batching of Davidson solves ---------------------------------------
 //
-// A server owns one stream and a scheduler thread.  Callers prepare a context per request
-// (fcg_set_ops, fcg_set_terms, fcg_state_set -- in their own threads) and submit it with a
-// guess; the scheduler admits requests while slots and the memory budget allow, and runs all
-// admitted solves in lockstep rounds as fcg_davidson_grouped does: every round advances each
-// solve to its next need of the device, then serves all of them with one wait for the stream
-// or one grouped sigma launch per precision.  Solves that finish leave after the round,
-// queued requests join at the next, so a request's work overlaps with whatever is in flight.
-// A solve's result is the same as fcg_davidson's on its own (the grouped sigma adds each
+// A server owns scheduler threads (lanes), each with a stream of its own.  Callers prepare a
+// context per request (fcg_set_ops, fcg_set_terms, fcg_state_set -- in their own threads) and
+// submit it with a guess; a lane admits requests while slots and the memory budget allow, and
+// runs its admitted solves in lockstep rounds as fcg_davidson_grouped does: every round
+// advances each solve to its next need of the device, then serves all of them with grouped
+// launches and one wait for the stream.  Solves that finish leave after the round, queued
+// requests join at the next, so a request's work overlaps with whatever is in flight.  A
+// solve's result is the same as fcg_davidson's on its own (the grouped sigma adds each
 // problem's sums in another order).
 
 struct fcg_server {
@@ -1188,8 +1795,6 @@ struct Slot {
   std::shared_ptr<fcg_server::Ticket> t;
   std::unique_ptr<DavidsonRun> run;
   cudaStream_t saved = nullptr;
-  int state = 0;  // 0 ready, 1 waiting, 2 sigma, 3 failed, 4 done
-  int rc = 0;
 };
 
 }  // namespace
@@ -1202,7 +1807,8 @@ void fcg_server::lane_loop(int lane) {
   cudaSetDevice(device);
   cudaStream_t stream = streams[lane];
   const int share = (max_active + lanes - 1) / lanes;
-  std::vector<Slot> active;
+  Lockstep L(stream, step_helpers(lanes));
+  std::vector<Slot> active;  // active[i] runs as L.entries[i]
   auto finish = [&](Slot& sl, int rc) {  // under the lock
     sl.t->ctx->stream = sl.saved;
     sl.t->rc = rc;
@@ -1229,9 +1835,10 @@ void fcg_server::lane_loop(int lane) {
         ++running;
         sl.run.reset(new DavidsonRun());
         lk.unlock();
-        const int rc = sl.run->init(t->ctx, t->R, t->v0.data(), t->max_iter, t->max_ss_vecs, t->tol, t->lindep,
-                                    t->precision, t->precond, t->energies.data(), t->vectors.data(),
-                                    t->residuals.data(), &t->iters);
+        int rc = sl.run->init(t->ctx, t->R, t->v0.data(), t->max_iter, t->max_ss_vecs, t->tol, t->lindep,
+                              t->precision, t->precond, t->energies.data(), t->vectors.data(),
+                              t->residuals.data(), &t->iters, true);
+        if (rc == FCG_OK && (rc = L.add(sl.run.get()))) t->ctx->err = L.err;
         lk.lock();
         if (rc) {
           cudaStreamSynchronize(stream);
@@ -1246,77 +1853,25 @@ void fcg_server::lane_loop(int lane) {
         continue;
       }
     }
-    // one round over the admitted solves
-    for (size_t q = 0; q < active.size(); ++q) {
-      Slot& sl = active[q];
-      while (sl.state == 0) {
-        Act a = Act::kDone;
-        const int rc = sl.run->step(&a);
-        if (rc) {
-          sl.rc = rc;
-          sl.state = 3;
-          break;
-        }
-        sl.state = a == Act::kWait ? 1 : a == Act::kSigma ? 2 : 4;
-      }
-    }
-    bool waiting = false;
-    for (auto& sl : active) waiting = waiting || sl.state == 1;
-    int rc_round = FCG_OK;
-    if (waiting) {
-      rc_round = cudaStreamSynchronize(stream) == cudaSuccess ? FCG_OK : FCG_ECUDA;
-      for (auto& sl : active)
-        if (sl.state == 1) {
-          sl.run->W.after_wait();
-          sl.state = 0;
-        }
-    } else {
-      for (int p : {FCG_FP32, FCG_FP64}) {
-        std::vector<fcg_ctx*> cs;
-        std::vector<int> Rs;
-        std::vector<const double*> dc;
-        std::vector<double*> ds;
-        std::vector<Slot*> who;
-        for (auto& sl : active) {
-          DavidsonRun& r = *sl.run;
-          if (sl.state != 2 || r.sig_prec != p) continue;
-          const int64_t n = r.W.n;
-          cs.push_back(r.ctx);
-          Rs.push_back(r.sig_m);
-          dc.push_back(r.W.V.p + n * r.sig_col);
-          ds.push_back(r.W.AV.p + n * r.sig_col);
-          who.push_back(&sl);
-        }
-        if (cs.empty()) continue;
-        const int rc = fcg_sigma_closed_grouped(int(cs.size()), cs.data(), Rs.data(), dc.data(), ds.data(), p);
-        for (Slot* sl : who) {
-          if (rc) {
-            sl->state = 3;
-            sl->rc = rc;
-            sl->t->ctx->err = cs[0]->err;
-          } else {
-            sl->run->W.after_wait();
-            sl->state = 0;
-          }
-        }
-      }
-    }
+    const int rc_round = L.round();
+    if (rc_round) cudaStreamSynchronize(stream);
     // retire finished and failed solves
     std::unique_lock<std::mutex> lk(mu);
-    std::vector<Slot> keep;
-    for (size_t q = 0; q < active.size(); ++q) {
-      Slot& sl = active[q];
-      if (sl.state == 4) {
+    for (size_t i = active.size(); i-- > 0;) {
+      const Lockstep::Entry& e = L.entries[i];
+      if (e.state != Lockstep::kDone && e.state != Lockstep::kFailed && rc_round == FCG_OK) continue;
+      Slot& sl = active[i];
+      if (e.state == Lockstep::kDone) {
         finish(sl, FCG_OK);
-      } else if (sl.state == 3 || rc_round != FCG_OK) {
-        cudaStreamSynchronize(stream);
-        if (sl.state != 3) sl.t->ctx->err = "serving: the shared stream failed";
-        finish(sl, sl.state == 3 ? sl.rc : rc_round);
+      } else if (e.state == Lockstep::kFailed) {
+        finish(sl, e.rc);
       } else {
-        keep.push_back(std::move(sl));
+        sl.t->ctx->err = "serving: the lane's stream failed: " + L.err;
+        finish(sl, rc_round);
       }
+      L.erase(i);
+      active.erase(active.begin() + i);
     }
-    active.swap(keep);
   }
 }
 

@@ -78,7 +78,10 @@ class Stats(ctypes.Structure):
                 ("bst_cache_elements", ctypes.c_int64), ("bst_flops_reference", ctypes.c_int64),
                 ("bst_flops_executed", ctypes.c_int64), ("bst_cache_seconds", ctypes.c_double),
                 ("bst_plan_seconds", ctypes.c_double), ("bst_fois_items", ctypes.c_int64),
-                ("bst_fois_seconds", ctypes.c_double)]
+                ("bst_fois_seconds", ctypes.c_double), ("group_rounds", ctypes.c_int64),
+                ("group_launches", ctypes.c_int64), ("group_setup_seconds", ctypes.c_double),
+                ("group_step_seconds", ctypes.c_double), ("group_issue_seconds", ctypes.c_double),
+                ("group_wait_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -72,6 +72,12 @@ typedef struct fcg_stats {
   double bst_plan_seconds;  /* of which host planning (triples, groups, cache layout) */
   int64_t bst_fois_items;   /* (term, ket block, target TuckerConfig) contributions of the last fcg_bst_fois */
   double bst_fois_seconds;  /* wall time of the last fcg_bst_fois */
+  int64_t group_rounds;     /* lockstep rounds of the last fcg_davidson_grouped (first context) */
+  int64_t group_launches;   /* kernels those rounds launched (grouped sigma: 3) */
+  double group_setup_seconds; /* its problems' set-up: buffers, diagonals, guesses */
+  double group_step_seconds;  /* host work of the rounds (problems stepped in parallel) */
+  double group_issue_seconds; /* descriptors, copies and launches of the rounds */
+  double group_wait_seconds;  /* sigma builds and waits for the stream */
 } fcg_stats;
 
 int fcg_version(void);
