@@ -48,6 +48,7 @@ def parse():
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the grouped launch of 256 uneven problems")
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
+    ap.add_argument("--instances", type=int, default=256, help="problems of the grouped-launch leg")
     ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
     ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
@@ -379,11 +380,23 @@ def batched_benchmark(steps, warmup, n_inst=256):
         t1 = time.perf_counter()
         seq = [g.davidson(gu, tol=tol, max_iter=200, precision=prec) for g, gu in zip(gs, guesses)]
         seq_s = time.perf_counter() - t1
+        # the same solves from 16 host threads, each problem on its own context's stream
+        from concurrent.futures import ThreadPoolExecutor
+        t1 = time.perf_counter()
+        with ThreadPoolExecutor(16) as ex:
+            list(ex.map(lambda a: a[0].davidson(a[1], tol=tol, max_iter=200, precision=prec), zip(gs, guesses)))
+        conc_s = time.perf_counter() - t1
+        st = gs[0].stats()
         solved[prec] = (res, seq)
         dmax = max(float(np.abs(r[0] - q[0]).max()) for r, q in zip(res, seq))
         out["solves_mixed" if prec == "fp32" else "solves_fp64"] = {
-            "grouped_s": grouped_s, "sequential_s": seq_s, "solves_per_s_grouped": n_inst / grouped_s,
-            "solves_per_s_sequential": n_inst / seq_s, "grouped_over_sequential": seq_s / grouped_s,
+            "grouped_s": grouped_s, "sequential_s": seq_s, "concurrent_16_threads_s": conc_s,
+            "solves_per_s_grouped": n_inst / grouped_s, "solves_per_s_sequential": n_inst / seq_s,
+            "solves_per_s_concurrent": n_inst / conc_s, "grouped_over_sequential": seq_s / grouped_s,
+            "grouped_over_concurrent": conc_s / grouped_s,
+            "grouped_phases_s": {k[6:]: st[k] for k in ("group_setup_seconds", "group_step_seconds",
+                                                         "group_issue_seconds", "group_wait_seconds")},
+            "grouped_rounds": st["group_rounds"], "grouped_launches": st["group_launches"],
             "max_energy_difference": dmax, "iterations_total": int(sum(r[3] for r in res)),
             "not_converged_grouped": int(sum(r[2].max() >= tol for r in res)),
             "not_converged_sequential": int(sum(q[2].max() >= tol for q in seq))}
@@ -589,7 +602,7 @@ def main():
         return
     if a.batched_only:
         if rank == 0:
-            print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup)}))
+            print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances)}))
         return
     if a.bst_only:
         peaks = {}
@@ -720,7 +733,7 @@ def main():
             out["open_sigma"] = {"error": str(ex)}
     if rank == 0 and a.batched:
         try:
-            out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup)
+            out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances)
         except Exception as ex:
             out["batched"] = {"error": str(ex)}
     if rank == 0 and a.bst:

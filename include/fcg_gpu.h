@@ -146,16 +146,20 @@ int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coef
  * Davidson(Hmap; v0, max_iter, max_ss_vecs, nroots=R, tol, lindep_thresh) + eigs with
  * Adiag = compute_diagonal): lowest R eigenpairs of H within the state's configurations.
  * v0, vectors: host column-major n_cfg x R; energies, residuals: R; tol is the residual
- * norm.  precision FCG_FP64, or FCG_FP32 = float32 sigma builds until the residuals
- * reach max(tol, 1e-5), then float64 sigma builds to tol.  precond: 1 = diagonal
+ * norm.  precision FCG_FP64, or FCG_FP32 = float32 sigma builds until the largest residual
+ * is below max(tol, 1e-5, 5e-7 * max|theta|) (the float32 sigma's residual floor) or has
+ * not fallen by 10% in 5 iterations while below 1e-3, then float64 sigma builds to tol.  precond: 1 = diagonal
  * preconditioner.  Subspace holds at most max_ss_vecs * R vectors. */
 int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol, double lindep,
                  int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
 /* The Davidson solves of n independent problems (one context each, state set) in lockstep:
- * every problem runs fcg_davidson's algorithm; their device work shares the first context's
- * stream and each wait for it, and the sigma builds of their new blocks run as one grouped
- * launch (fcg_sigma_closed_grouped) per precision.  The reference solves independent
+ * every problem runs fcg_davidson's algorithm on the first context's stream.  In each round
+ * every problem advances to its next need of the device (host work on a thread pool); then
+ * all their Gram products, Ritz/residual passes, orthonormalisation and restart updates run
+ * as one launch per kernel and block width and step, the fetched values come back in one
+ * copy, the sigma builds of their new blocks run as one grouped launch
+ * (fcg_sigma_closed_grouped) per precision, and the round ends with one wait.  The reference solves independent
  * problems one after another (tps_ci_davidson, src/tpsci_outer.jl:364-454, per problem).
  * Per problem q: R[q] roots, v0[q] / vectors[q] host column-major n_cfg_q x R[q],
  * energies[q], residuals[q], iters[q]; the settings are shared.  All contexts on one device
