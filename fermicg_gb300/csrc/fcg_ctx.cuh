@@ -120,6 +120,22 @@ struct fcg_ctx {
   DevBuf<unsigned char> d_group;    // entries of the last grouped closed sigma led by this context
   DevBuf<int32_t> d_group_cta;      // problem of every CTA of that launch
   DevBuf<int32_t> d_zero_terms;
+  // stored Hamiltonian blocks of the state (fcg_cache_hamiltonian): per work item and
+  // (bra, ket) pair, the sum over the item's terms of the matrix element
+  bool have_hcache = false;
+  int64_t hc_pairs = 0;
+  DevBuf<int64_t> d_hc_prefix;  // pairs before each work item
+  DevBuf<int64_t> d_hc_cta;     // first work item of each cached-sigma CTA
+  DevBuf<double> d_hc64;
+  DevBuf<float> d_hc32;
+  void drop_hcache() {
+    have_hcache = false;
+    hc_pairs = 0;
+    d_hc64.release();
+    d_hc32.release();
+    d_hc_prefix.release();
+    d_hc_cta.release();
+  }
   // vectors
   DevBuf<double> d_in64, d_out64;  // column-major staging for host calls
   DevBuf<double> d_c64, d_s64;     // row-major fp64

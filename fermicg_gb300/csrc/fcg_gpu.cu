@@ -109,6 +109,11 @@ struct SigmaParams {
   const int16_t* cfg;  // [n_cfg][N]
   int N;
   int R;
+  // stored Hamiltonian blocks (fcg_cache_hamiltonian): pairs before each work item, first
+  // work item of each cached-sigma CTA, pair count
+  const int64_t* hc_prefix;
+  const int64_t* hc_cta;
+  int64_t n_pairs;
 };
 
 // ---- vector loads ---------------------------------------------------------------------------
@@ -413,13 +418,147 @@ __global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB
   closed_sigma_cta<T, RR>(p, w, op, cin, sig, blockIdx.x);
 }
 
+
+// ---- stored Hamiltonian blocks -------------------------------------------------------------
+// Inside a work item the triples run term fastest, then ket, then bra, so the item's (bra,
+// ket) pairs are pair = bj * nk + kj.  The cache holds, at hc_prefix[w] + pair, the sum over
+// the item's terms of the dressed matrix element (signs included), added in term order in
+// float64.  A sigma from the cache reads one value per pair instead of recomputing every
+// term's contraction.
+constexpr int kCacheRun = 4;  // pairs per thread of the assembly
+constexpr int kHcRun = 16;    // pairs per thread of the cached sigma
+constexpr int64_t kCacheChunk = int64_t(kSigmaThreads) * kCacheRun;
+constexpr int64_t kHcChunk = int64_t(kSigmaThreads) * kHcRun;
+
+// first pair and pair count of the CTA's chunk; w_lo / w_hi its first and last work item
+__global__ void __launch_bounds__(kSigmaThreads) hcache_build_kernel(SigmaParams p, const int64_t* __restrict__ cta_lo,
+                                                                     const double* __restrict__ w,
+                                                                     const double* __restrict__ op,
+                                                                     double* __restrict__ hc) {
+  const int64_t s0 = int64_t(blockIdx.x) * kCacheChunk;
+  const int64_t e0 = (s0 + kCacheChunk < p.n_pairs) ? s0 + kCacheChunk : p.n_pairs;
+  const int64_t t0 = s0 + int64_t(threadIdx.x) * kCacheRun;
+  if (t0 >= e0) return;
+  const int64_t t1 = (t0 + kCacheRun < e0) ? t0 + kCacheRun : e0;
+  int64_t wi = find_item(p.hc_prefix, __ldg(cta_lo + blockIdx.x), __ldg(cta_lo + blockIdx.x + 1), t0);
+  const int64_t local = t0 - __ldg(p.hc_prefix + wi);
+  WorkItem it = p.items[wi];
+  int kj = int(local % it.nk);
+  int bj = int(local / it.nk);
+  const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
+  uint4 rb = __ldg(cfg + __ldg(p.perm + it.bra_off + bj));
+  uint4 rk = __ldg(cfg + __ldg(p.perm + it.ket_off + kj));
+  for (int64_t idx = t0; idx < t1; ++idx) {
+    double me = 0.0;
+    for (int t = 0; t < it.nt; ++t) me += dressed_element<double>(p.ts[it.ts_off + t], w, op, rb, rk);
+    hc[idx] = me;
+    if (idx + 1 == t1) break;
+    if (++kj == it.nk) {
+      kj = 0;
+      if (++bj == it.nb) {
+        bj = 0;
+        ++wi;
+        it = p.items[wi];
+      }
+      rb = __ldg(cfg + __ldg(p.perm + it.bra_off + bj));
+    }
+    rk = __ldg(cfg + __ldg(p.perm + it.ket_off + kj));
+  }
+}
+
+// sigma[bra] += hc[pair] * C[ket] over the CTA's chunk of pairs: each thread a run of kHcRun
+// consecutive pairs (read with 32-byte loads), contributions to one bra row summed in
+// registers and flushed with one atomic per root when the bra changes.
+template <typename T, int RR, int RMAX = kMaxR>
+__device__ __forceinline__ void cached_sigma_cta(const SigmaParams& p, const T* __restrict__ hc,
+                                                 const T* __restrict__ cin, T* __restrict__ sig, int64_t cta) {
+  constexpr int RV = RR > 0 ? RR : RMAX;
+  const int64_t s0 = cta * kHcChunk;
+  const int64_t e0 = (s0 + kHcChunk < p.n_pairs) ? s0 + kHcChunk : p.n_pairs;
+  __shared__ int64_t s_pre[kPrefixShared];
+  const int64_t w_lo = __ldg(p.hc_cta + cta), w_hi = __ldg(p.hc_cta + cta + 1);
+  const int span = int(w_hi - w_lo + 1 < kPrefixShared + 1 ? w_hi - w_lo + 1 : kPrefixShared + 1);
+  const bool staged = span <= kPrefixShared;
+  if (staged)
+    for (int i = threadIdx.x; i < span; i += kSigmaThreads) s_pre[i] = __ldg(p.hc_prefix + w_lo + i);
+  __syncthreads();
+  const int R = RR > 0 ? RR : p.R;
+  const int64_t t0 = s0 + int64_t(threadIdx.x) * kHcRun;
+  if (t0 >= e0) return;
+  const int n = int((t0 + kHcRun < e0) ? kHcRun : e0 - t0);
+  int64_t wi, local;
+  if (staged) {
+    const int q = find_item_shared(s_pre, 0, span - 1, t0);
+    wi = w_lo + q;
+    local = t0 - s_pre[q];
+  } else {
+    wi = find_item(p.hc_prefix, w_lo, w_hi, t0);
+    local = t0 - __ldg(p.hc_prefix + wi);
+  }
+  T mv[kHcRun];
+  if (n == kHcRun) {  // t0 is a multiple of kHcRun: the run starts on a 64-byte boundary
+    constexpr int C = Chunk<T>::n;
+#pragma unroll
+    for (int c = 0; c < kHcRun / C; ++c) {
+      Chunk<T> q;
+      q.load(hc + t0 + C * c);
+#pragma unroll
+      for (int u = 0; u < C; ++u) mv[C * c + u] = q.v[u];
+    }
+  } else {
+#pragma unroll
+    for (int i = 0; i < kHcRun; ++i) mv[i] = i < n ? __ldg(hc + t0 + i) : T(0);
+  }
+  WorkItem it = p.items[wi];
+  int kj = int(local % it.nk);
+  int bj = int(local / it.nk);
+  int b = __ldg(p.perm + it.bra_off + bj);
+  int k = __ldg(p.perm + it.ket_off + kj);
+  T acc[RV];
+#pragma unroll
+  for (int r = 0; r < RV; ++r) acc[r] = T(0);
+#pragma unroll
+  for (int i = 0; i < kHcRun; ++i) {
+    const T* ck = cin + int64_t(k) * R;
+#pragma unroll
+    for (int r = 0; r < RV; ++r)
+      if (r < R) acc[r] = fma(mv[i], __ldg(ck + r), acc[r]);
+    if (i + 1 == n) break;
+    if (++kj == it.nk) {
+      kj = 0;
+      if (++bj == it.nb) {
+        bj = 0;
+        ++wi;
+        it = p.items[wi];
+      }
+      const int nb_row = __ldg(p.perm + it.bra_off + bj);
+      if (nb_row != b) {
+        flush_row<T, RV>(sig, b, acc, R);
+#pragma unroll
+        for (int r = 0; r < RV; ++r) acc[r] = T(0);
+        b = nb_row;
+      }
+    }
+    k = __ldg(p.perm + it.ket_off + kj);
+  }
+  flush_row<T, RV>(sig, b, acc, R);
+}
+
+template <typename T, int RR>
+__global__ void __launch_bounds__(kSigmaThreads) cached_sigma_kernel(SigmaParams p, const T* __restrict__ hc,
+                                                                     const T* __restrict__ cin, T* __restrict__ sig) {
+  cached_sigma_cta<T, RR>(p, hc, cin, sig, blockIdx.x);
+}
+
 // Many independent problems in one launch: problem q owns CTAs [cta0, cta0 + its CTA count)
-// of the grid; cta_problem maps every CTA to its problem.
+// of the grid; cta_problem maps every CTA to its problem.  Problems with stored Hamiltonian
+// blocks (hc set) run in a second grid of cached-sigma CTAs, numbered from cta0 there.
 template <typename T>
 struct GroupEntry {
   SigmaParams p;
   const T* w;
   const T* op;
+  const T* hc;       // stored Hamiltonian blocks, or null
   T* cin;            // row-major [n_cfg][R] working copy of C
   T* sig;            // row-major [n_cfg][R] sigma
   const double* src; // caller's column-major C
@@ -434,6 +573,14 @@ __global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB
   const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
   const SigmaParams p = e.p;
   closed_sigma_cta<T, 0, RMAX>(p, e.w, e.op, e.cin, e.sig, int64_t(blockIdx.x) - e.cta0);
+}
+
+template <typename T, int RMAX>
+__global__ void __launch_bounds__(kSigmaThreads)
+    cached_sigma_grouped_kernel(const GroupEntry<T>* __restrict__ g, const int32_t* __restrict__ cta_problem) {
+  const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
+  const SigmaParams p = e.p;
+  cached_sigma_cta<T, 0, RMAX>(p, e.hc, e.cin, e.sig, int64_t(blockIdx.x) - e.cta0);
 }
 
 // problem blockIdx.y: C to the row-major working copy, sigma zeroed
@@ -603,6 +750,11 @@ static SigmaParams make_sigma_params(fcg_ctx* ctx, int R) {
   p.cfg = ctx->d_cfg.p;
   p.N = ctx->N;
   p.R = R;
+  if (ctx->have_hcache) {
+    p.hc_prefix = ctx->d_hc_prefix.p;
+    p.hc_cta = ctx->d_hc_cta.p;
+    p.n_pairs = ctx->hc_pairs;
+  }
   return p;
 }
 
@@ -733,6 +885,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   ctx->have_terms = false;
   ctx->have_state = false;
   ctx->have_bst = false;
+  ctx->drop_hcache();
   return FCG_OK;
 }
 
@@ -746,6 +899,7 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   ctx->have_terms = false;
   ctx->have_state = false;
   ctx->have_bst = false;
+  ctx->drop_hcache();
   ctx->n_terms = n_terms;
   ctx->trm.assign(term_table, term_table + int64_t(n_terms) * kTrmCols);
   ctx->n_trans = n_transfers;
@@ -856,6 +1010,7 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   pi.dress = &ctx->dress;
   pi.w_index = &ctx->w_index;
   ctx->have_state = false;
+  ctx->drop_hcache();
   std::string msg = build_plan(pi, n_cfg, fock, cfg, ctx->plan);
   FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   const Plan& P = ctx->plan;
@@ -916,6 +1071,25 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* 
   p.cta_lo = sizeof(T) == 4 ? ctx->d_cta32.p : ctx->d_cta64.p;
   if (zero_sig) FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
   int launches = 0;
+  if (ctx->have_hcache) {  // from the stored Hamiltonian blocks
+    const T* hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(ctx->d_hc32.p) : reinterpret_cast<const T*>(ctx->d_hc64.p);
+    const int64_t grid = (p.n_pairs + kHcChunk - 1) / kHcChunk;
+    FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (grid > 0) {
+      switch (R) {
+        case 1: cached_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+        case 2: cached_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+        case 4: cached_sigma_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+        default: cached_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+      }
+      FCG_CUDA(cudaGetLastError());
+      launches = 1;
+    }
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    ctx->stats.kernel_launches = launches;
+    return FCG_OK;
+  }
   if (p.n_triples > 0) {
     int64_t grid = (p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
     FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many triples for one launch");
@@ -963,7 +1137,7 @@ static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_s
   ctx->stats.kernel_launches += 2;
   if (!wait) return FCG_OK;  // untimed: no events were recorded
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (ctx->plan.n_triples > 0) {
+  if (ctx->plan.n_triples > 0 || ctx->have_hcache) {
     float ms = 0.f;
     FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->stats.last_kernel_ms = ms;
@@ -984,6 +1158,66 @@ int fcg_sigma_closed_device(fcg_ctx* ctx, int R, const double* d_c, double* d_si
   return sigma_device_impl(ctx, R, d_c, d_sigma, precision);
 }
 
+int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  const auto t0 = std::chrono::steady_clock::now();
+  ctx->drop_hcache();
+  ctx->stats.hcache_pairs = 0;
+  ctx->stats.hcache_bytes = 0;
+  ctx->stats.hcache_seconds = 0.0;
+  if (bytes) *bytes = 0;
+  if (!(max_bytes > 0)) return FCG_OK;  // 0: back to building every matrix element per sigma
+  const Plan& P = ctx->plan;
+  const int64_t n_items = int64_t(P.items.size());
+  std::vector<int64_t> pre(size_t(std::max<int64_t>(n_items, 1)), 0);
+  int64_t pairs = 0;
+  for (int64_t w = 0; w < n_items; ++w) {
+    pre[w] = pairs;
+    pairs += int64_t(P.items[w].nb) * P.items[w].nk;
+  }
+  const double need = double(pairs) * double(sizeof(double) + sizeof(float)) + double(n_items) * 8.0;
+  if (bytes) *bytes = int64_t(need);
+  FCG_REQUIRE(need <= max_bytes, FCG_ELIMIT,
+              "stored Hamiltonian blocks need " + std::to_string(int64_t(need)) + " bytes, over max_bytes");
+  auto cta_items = [&](int64_t chunk, std::vector<int64_t>& out) {
+    const int64_t n_cta = pairs > 0 ? (pairs + chunk - 1) / chunk : 0;
+    out.assign(size_t(n_cta) + 1, std::max<int64_t>(n_items - 1, 0));
+    for (int64_t c = 0; c < n_cta; ++c)
+      out[c] = int64_t(std::upper_bound(pre.begin(), pre.begin() + n_items, c * chunk) - pre.begin()) - 1;
+  };
+  std::vector<int64_t> lo_build, lo_sigma;
+  cta_items(kCacheChunk, lo_build);
+  cta_items(kHcChunk, lo_sigma);
+  FCG_REQUIRE(lo_build.size() < (size_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
+  FCG_CUDA(ctx->d_hc_prefix.upload(pre.data(), pre.size(), ctx->stream));
+  FCG_CUDA(ctx->d_hc_cta.upload(lo_sigma.data(), lo_sigma.size(), ctx->stream));
+  DevBuf<int64_t> d_lo;
+  FCG_CUDA(d_lo.upload(lo_build.data(), lo_build.size(), ctx->stream));
+  FCG_CUDA(ctx->d_hc64.alloc(size_t(std::max<int64_t>(pairs, 1))));
+  FCG_CUDA(ctx->d_hc32.alloc(size_t(std::max<int64_t>(pairs, 1))));
+  if (pairs > 0) {
+    SigmaParams p = make_sigma_params(ctx, 1);
+    p.hc_prefix = ctx->d_hc_prefix.p;
+    p.hc_cta = ctx->d_hc_cta.p;
+    p.n_pairs = pairs;
+    hcache_build_kernel<<<unsigned(lo_build.size() - 1), kSigmaThreads, 0, ctx->stream>>>(
+        p, d_lo.p, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
+    FCG_CUDA(cudaGetLastError());
+    to_float_kernel<<<unsigned(std::min<int64_t>((pairs + 255) / 256, 65535)), 256, 0, ctx->stream>>>(
+        ctx->d_hc64.p, ctx->d_hc32.p, pairs);
+    FCG_CUDA(cudaGetLastError());
+  }
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->hc_pairs = pairs;
+  ctx->have_hcache = true;
+  ctx->stats.hcache_pairs = pairs;
+  ctx->stats.hcache_bytes = int64_t(need);
+  ctx->stats.hcache_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return FCG_OK;
+}
+
 }  // extern "C"
 
 // One grouped launch (plus one pack and one unpack launch) over the closed sigmas of several
@@ -993,8 +1227,8 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
                         double* const* d_sigma) {
   fcg_ctx* ctx = ctxs[0];
   std::vector<GroupEntry<T>> entries(n);
-  std::vector<int32_t> cta_problem;
-  int64_t cta = 0, max_nr = 0;
+  std::vector<int32_t> cta_problem, cta_problem_hc;  // direct and stored-block grids
+  int64_t cta = 0, cta_hc = 0, max_nr = 0;
   for (int q = 0; q < n; ++q) {
     fcg_ctx* c = ctxs[q];
     const int64_t nr = c->n_cfg * R[q];
@@ -1018,17 +1252,31 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
     }
     e.src = d_c[q];
     e.dst = d_sigma[q];
-    e.cta0 = cta;
     e.n_cfg = c->n_cfg;
-    const int64_t n_cta = (e.p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
-    FCG_REQUIRE(cta + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
-    cta_problem.insert(cta_problem.end(), size_t(n_cta), int32_t(q));
-    cta += n_cta;
+    e.hc = nullptr;
+    if (c->have_hcache) {
+      e.hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(c->d_hc32.p) : reinterpret_cast<const T*>(c->d_hc64.p);
+      e.cta0 = cta_hc;
+      const int64_t n_cta = (e.p.n_pairs + kHcChunk - 1) / kHcChunk;
+      FCG_REQUIRE(cta_hc + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
+      cta_problem_hc.insert(cta_problem_hc.end(), size_t(n_cta), int32_t(q));
+      cta_hc += n_cta;
+    } else {
+      e.cta0 = cta;
+      const int64_t n_cta = (e.p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
+      FCG_REQUIRE(cta + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
+      cta_problem.insert(cta_problem.end(), size_t(n_cta), int32_t(q));
+      cta += n_cta;
+    }
     max_nr = std::max(max_nr, nr);
   }
   FCG_CUDA(ctx->d_group.upload(reinterpret_cast<const unsigned char*>(entries.data()),
                                entries.size() * sizeof(GroupEntry<T>), ctx->stream));
-  FCG_CUDA(ctx->d_group_cta.upload(cta_problem.data(), cta_problem.size(), ctx->stream));
+  {
+    std::vector<int32_t> both(cta_problem);
+    both.insert(both.end(), cta_problem_hc.begin(), cta_problem_hc.end());
+    FCG_CUDA(ctx->d_group_cta.upload(both.data(), both.size(), ctx->stream));
+  }
   const GroupEntry<T>* dg = reinterpret_cast<const GroupEntry<T>*>(ctx->d_group.p);
   const dim3 pgrid = dim3(unsigned(std::min<int64_t>((max_nr + 255) / 256, 1024)), unsigned(n));
   grouped_pack_kernel<T><<<pgrid, 256, 0, ctx->stream>>>(dg);
@@ -1043,6 +1291,16 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
       closed_sigma_grouped_kernel<T, kMaxR><<<unsigned(cta), kSigmaThreads, 0, ctx->stream>>>(dg, ctx->d_group_cta.p);
     FCG_CUDA(cudaGetLastError());
   }
+  if (cta_hc > 0) {
+    int rmax = 0;
+    for (int q = 0; q < n; ++q) rmax = std::max(rmax, R[q]);
+    const int32_t* tab = ctx->d_group_cta.p + cta;
+    if (rmax <= 4)
+      cached_sigma_grouped_kernel<T, 4><<<unsigned(cta_hc), kSigmaThreads, 0, ctx->stream>>>(dg, tab);
+    else
+      cached_sigma_grouped_kernel<T, kMaxR><<<unsigned(cta_hc), kSigmaThreads, 0, ctx->stream>>>(dg, tab);
+    FCG_CUDA(cudaGetLastError());
+  }
   FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
   grouped_unpack_kernel<T><<<pgrid, 256, 0, ctx->stream>>>(dg);
   FCG_CUDA(cudaGetLastError());
@@ -1050,7 +1308,7 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
   float ms = 0.f;
   FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->stats.last_kernel_ms = ms;
-  ctx->stats.kernel_launches = cta > 0 ? 3 : 2;
+  ctx->stats.kernel_launches = 2 + (cta > 0 ? 1 : 0) + (cta_hc > 0 ? 1 : 0);
   return FCG_OK;
 }
 
@@ -1244,7 +1502,7 @@ extern "C" int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, 
   FCG_CUDA(cudaGetLastError());
   ctx->stats.kernel_launches += 2;
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (ctx->plan.n_triples > 0) {
+  if (ctx->plan.n_triples > 0 || ctx->have_hcache) {
     float ms = 0.f;
     FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->stats.last_kernel_ms = ms;

@@ -38,6 +38,7 @@ SIGNATURES = {
     "fcg_state_set": (_I, [_P, _L, _P, _P]),
     "fcg_sigma_closed": (_I, [_P, _I, _P, _P, _I]),
     "fcg_sigma_closed_device": (_I, [_P, _I, _P, _P, _I]),
+    "fcg_cache_hamiltonian": (_I, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_int64)]),
     "fcg_diagonal": (_I, [_P, _I, _P]),
     "fcg_sigma_open": (_I, [_P, _I, _P, ctypes.c_double, _I, ctypes.POINTER(_L)]),
     "fcg_sigma_open_fetch": (_I, [_P, _P, _P, _P]),
@@ -81,7 +82,8 @@ class Stats(ctypes.Structure):
                 ("bst_fois_seconds", ctypes.c_double), ("group_rounds", ctypes.c_int64),
                 ("group_launches", ctypes.c_int64), ("group_setup_seconds", ctypes.c_double),
                 ("group_step_seconds", ctypes.c_double), ("group_issue_seconds", ctypes.c_double),
-                ("group_wait_seconds", ctypes.c_double)]
+                ("group_wait_seconds", ctypes.c_double), ("hcache_pairs", ctypes.c_int64),
+                ("hcache_bytes", ctypes.c_int64), ("hcache_seconds", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -190,6 +192,14 @@ class GpuSigma:
         """Device-pointer variant (column-major n_cfg x R float64 buffers on this GPU)."""
         self._check(self.L.fcg_sigma_closed_device(self.h, R, ctypes.c_void_p(d_c_ptr), ctypes.c_void_p(d_sigma_ptr),
                                                    PRECISION[precision]), "fcg_sigma_closed_device")
+
+    def cache_hamiltonian(self, max_bytes: float = 64e9) -> int:
+        """Store the state's Hamiltonian blocks on the device (fcg_cache_hamiltonian); later
+        closed sigmas, Davidson solves and grouped launches of this state read them.  Returns
+        the bytes they take; max_bytes <= 0 drops them."""
+        b = ctypes.c_int64(0)
+        self._check(self.L.fcg_cache_hamiltonian(self.h, float(max_bytes), ctypes.byref(b)), "fcg_cache_hamiltonian")
+        return int(b.value)
 
     def sigma_closed_noalloc(self, d_c_ptr: int, d_sigma_ptr: int, R: int, precision="fp64"):
         """Allocation-free device-pointer sigma (fixed 16 MiB scratch; n_cfg * R <= 2**20)."""

@@ -78,6 +78,9 @@ typedef struct fcg_stats {
   double group_step_seconds;  /* host work of the rounds (problems stepped in parallel) */
   double group_issue_seconds; /* descriptors, copies and launches of the rounds */
   double group_wait_seconds;  /* sigma builds and waits for the stream */
+  int64_t hcache_pairs;     /* (work item, bra, ket) pairs of the stored Hamiltonian blocks */
+  int64_t hcache_bytes;     /* device bytes they take (float64 and float32 copies, index) */
+  double hcache_seconds;    /* wall time of the last fcg_cache_hamiltonian */
 } fcg_stats;
 
 int fcg_version(void);
@@ -194,6 +197,21 @@ int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_ite
 int fcg_poll(fcg_server* s, int64_t ticket, int* state);
 int fcg_wait(fcg_server* s, int64_t ticket, int timeout_ms, double* energies, double* vectors, double* residuals,
              int* iters);
+
+/* Stored Hamiltonian blocks of the state: the TPSCI analogue of cache_hamiltonian
+ * (src/tucker_inner.jl:90-159, which stores dense operator blocks for the BST sigma).  For
+ * every work item of the closed sigma (a bra group, a ket group and the terms coupling them,
+ * the job structure of tps_ci_matvec, src/tpsci_outer.jl:462-527) the matrix element
+ * <bra|H|ket> of each of its (bra, ket) pairs, summed over the item's terms in float64, is
+ * computed once and kept on the device (float64 and float32 copies).  Every later closed
+ * sigma of this state -- fcg_sigma_closed*, fcg_davidson, fcg_davidson_grouped,
+ * fcg_sigma_closed_grouped, fcg_build_full_h, fcg_expectation -- then reads those values
+ * instead of contracting every (bra, ket, term) triple again.  Float64 results equal the
+ * direct build up to the order of the additions; float32 results are closer to float64
+ * than the direct float32 build (the term sums are rounded once).  The blocks take 12 bytes
+ * per pair: *bytes returns the need; FCG_ELIMIT (nothing stored) when it exceeds max_bytes.
+ * max_bytes <= 0 drops them.  fcg_set_ops, fcg_set_terms and fcg_state_set drop them too. */
+int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes);
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
 
