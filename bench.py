@@ -49,6 +49,8 @@ def parse():
                     help="skip the grouped launch of 256 uneven problems")
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
     ap.add_argument("--instances", type=int, default=256, help="problems of the grouped-launch leg")
+    ap.add_argument("--no-stored", dest="stored", action="store_false",
+                    help="skip the stored-Hamiltonian-block timings and solve variants")
     ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
     ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
@@ -124,7 +126,7 @@ SERVING_SHAPES = [  # (name, builder(seed), n_cfg, roots, share of the serving s
 ]
 
 
-def davidson_benchmark(reps=2):
+def davidson_benchmark(reps=2, stored=True):
     """One solve per serving shape, alone on the GPU (tol 1e-6, mixed and FP64): the host time
     of each stage of a request (fcg_set_ops, fcg_set_terms, fcg_state_set, fcg_davidson), the
     iteration count and the time per iteration."""
@@ -155,11 +157,26 @@ def davidson_benchmark(reps=2):
                     best = {"set_ops_ms": d[0], "set_terms_ms": d[1], "state_set_ms": d[2], "davidson_ms": d[3],
                             "iterations": it, "ms_per_iteration": d[3] / max(it, 1)}
             out[f"{name}/{'mixed' if prec == 'fp32' else 'fp64'}"] = best
+            if stored:  # the same solve after storing the Hamiltonian blocks (assembly timed)
+                bs = None
+                for _ in range(reps):
+                    g.state_set(f, c)
+                    t1 = time.perf_counter()
+                    g.cache_hamiltonian()
+                    t2 = time.perf_counter()
+                    e2, X2, res2, it2 = g.davidson(guess, tol=1e-6, max_iter=200, precision=prec)
+                    t3 = time.perf_counter()
+                    if bs is None or (t3 - t1) < (bs["cache_ms"] + bs["davidson_ms"]) * 1e-3:
+                        bs = {"cache_ms": (t2 - t1) * 1e3, "davidson_ms": (t3 - t2) * 1e3, "iterations": it2,
+                              "ms_per_iteration": (t3 - t2) * 1e3 / max(it2, 1),
+                              "max_energy_difference_vs_direct": float(np.abs(e2 - e).max())}
+                g.cache_hamiltonian(0)
+                out[f"{name}/{'mixed' if prec == 'fp32' else 'fp64'}/stored"] = bs
     g.close()
     return out
 
 
-def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4):
+def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4, stored=True):
     """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
     per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
     stream.  Returns p50/p99 latency and solves/s per precision."""
@@ -181,24 +198,35 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4):
     kinds = rng.choice(len(shapes), size=n_req, p=[sh[4] for sh in shapes])
     picks = [int(rng.integers(len(pools[k]))) for k in kinds]
     out = {}
-    for server in ("threads", "native"):
-        for prec in ("fp32", "fp64"):
-            reqs = []
-            for i in range(n_req):
-                po, pt, f, c, guess = pools[kinds[i]][picks[i]]
-                reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
-                                    shape=shapes[kinds[i]][0]))
-            srv = SolveServer(slots=slots) if server == "threads" else NativeSolveServer(slots=slots, lanes=lanes)
-            res = srv.run(reqs)
-            srv.close()
-            summ = latency_summary(res)
-            summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
-                                      for sh in shapes}
-            key = "mixed" if prec == "fp32" else "fp64"
-            if server == "threads":
-                out[key] = summ
-            else:
-                out.setdefault("native", {})[key] = summ
+    energies = {}
+    for cache in ((False, True) if stored else (False,)):
+        for server in ("threads", "native"):
+            for prec in ("fp32", "fp64"):
+                reqs = []
+                for i in range(n_req):
+                    po, pt, f, c, guess = pools[kinds[i]][picks[i]]
+                    reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
+                                        shape=shapes[kinds[i]][0], cache=cache))
+                srv = SolveServer(slots=slots) if server == "threads" else NativeSolveServer(slots=slots, lanes=lanes)
+                res = srv.run(reqs)
+                srv.close()
+                energies[(cache, server, prec)] = {r.rid: r.energies for r in res}
+                summ = latency_summary(res)
+                summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
+                                          for sh in shapes}
+                key = "mixed" if prec == "fp32" else "fp64"
+                dest = out.setdefault("stored_blocks", {}) if cache else out
+                if server == "threads":
+                    dest[key] = summ
+                else:
+                    dest.setdefault("native", {})[key] = summ
+    if stored:
+        # the same requests with and without stored blocks: largest energy difference
+        out["stored_blocks"]["max_energy_difference_vs_direct"] = max(
+            float(np.abs(energies[(True, sv, p)][i] - energies[(False, sv, p)][i]).max())
+            for sv in ("threads", "native") for p in ("fp32", "fp64") for i in range(n_req))
+        out["stored_blocks"]["note"] = ("each request also runs fcg_cache_hamiltonian after fcg_state_set; its "
+                                        "latency includes that assembly")
     out["servers"] = {"threads": "one context, stream and host thread per slot; solves overlap on the GPU",
                       "native": f"fcg_server: continuous batching in {lanes} lanes (a scheduler thread and a "
                                 "stream each); a lane's solves run in lockstep rounds, one grouped sigma launch "
@@ -314,7 +342,7 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
     return out
 
 
-def batched_benchmark(steps, warmup, n_inst=256):
+def batched_benchmark(steps, warmup, n_inst=256, stored=True):
     """Batched uneven instances: n_inst independent problems (orbitals in {8,12,16,20},
     clusters of 2-4 orbitals, half filling, M=8-16, 1-3 roots, seeds 3000+i), each problem's
     closed sigma in one grouped launch (fcg_sigma_closed_grouped) against the same sigmas
@@ -402,6 +430,26 @@ def batched_benchmark(steps, warmup, n_inst=256):
             "not_converged_sequential": int(sum(q[2].max() >= tol for q in seq))}
     out["solves_mixed"]["max_energy_difference_vs_fp64"] = max(
         float(np.abs(a[0] - b[0]).max()) for a, b in zip(solved["fp32"][0], solved["fp64"][1]))
+    if stored:
+        # the same grouped solves after storing every problem's Hamiltonian blocks (assembly timed)
+        t1 = time.perf_counter()
+        hc_bytes = sum(g.cache_hamiltonian() for g in gs)
+        hc_s = time.perf_counter() - t1
+        blk = {"assembly_s": hc_s, "bytes": hc_bytes}
+        for prec in ("fp32", "fp64"):
+            t1 = time.perf_counter()
+            res = davidson_grouped(gs, guesses, tol=tol, max_iter=200, precision=prec)
+            grouped_s = time.perf_counter() - t1
+            st = gs[0].stats()
+            blk["solves_mixed" if prec == "fp32" else "solves_fp64"] = {
+                "grouped_s": grouped_s, "solves_per_s_grouped": n_inst / grouped_s,
+                "solves_per_s_with_assembly": n_inst / (grouped_s + hc_s),
+                "grouped_phases_s": {k[6:]: st[k] for k in ("group_step_seconds", "group_issue_seconds",
+                                                             "group_wait_seconds")},
+                "not_converged": int(sum(r[2].max() >= tol for r in res)),
+                "max_energy_difference_vs_direct": max(float(np.abs(r[0] - q[0]).max())
+                                                       for r, q in zip(res, solved[prec][0]))}
+        out["stored_blocks"] = blk
     for g in gs:
         g.close()
     return out
@@ -590,11 +638,11 @@ def main():
         return
     if a.serving_only:
         if rank == 0:
-            print(json.dumps({"serving": serving_benchmark()}))
+            print(json.dumps({"serving": serving_benchmark(stored=a.stored)}))
         return
     if a.davidson_only:
         if rank == 0:
-            print(json.dumps({"davidson": davidson_benchmark()}))
+            print(json.dumps({"davidson": davidson_benchmark(stored=a.stored)}))
         return
     if a.fois_only:
         if rank == 0:
@@ -602,7 +650,7 @@ def main():
         return
     if a.batched_only:
         if rank == 0:
-            print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances)}))
+            print(json.dumps({"batched": batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances, a.stored)}))
         return
     if a.bst_only:
         peaks = {}
@@ -662,6 +710,35 @@ def main():
     g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp64")
     torch.cuda.synchronize()
     rel32 = float((sig32 - d_s).abs().max() / d_s.abs().max())
+    sig64 = d_s.clone()
+
+    # The same sigma from stored Hamiltonian blocks (fcg_cache_hamiltonian): the term-summed
+    # matrix element of every (work item, bra, ket) pair computed once, then each build reads
+    # one value per pair.  Reported beside the headline, which stays the direct build.
+    stored = None
+    if a.stored:
+        t1 = time.perf_counter()
+        hc_bytes = g.cache_hamiltonian()
+        hc_s = time.perf_counter() - t1
+        pairs = g.stats()["hcache_pairs"]
+        hms32, hk32 = timed("fp32", a.steps, a.warmup)
+        hms64, hk64 = timed("fp64", max(3, a.steps // 4), a.warmup)
+        g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp64")
+        torch.cuda.synchronize()
+        hrel64 = float((d_s - sig64).abs().max() / sig64.abs().max())
+        g.sigma_closed_device(d_c.data_ptr(), d_s.data_ptr(), R, "fp32")
+        torch.cuda.synchronize()
+        hrel32 = float((d_s - sig64).abs().max() / sig64.abs().max())
+        # algorithmic bytes of one float launch: the stored values, C and sigma, the work items
+        hb32 = pairs * 4 + 2 * n * R * 4 + stats["n_work_items"] * 24
+        stored = {"sigma_builds_per_s": 1e3 / hms32, "ms_per_step": hms32, "kernel_ms": hk32,
+                  "fp64": {"sigma_builds_per_s": 1e3 / hms64, "ms_per_step": hms64, "kernel_ms": hk64},
+                  "pairs": pairs, "bytes": hc_bytes, "assembly_s": hc_s,
+                  "assembly_over_direct_fp64_sigma": hc_s / (ms64 * 1e-3),
+                  "speedup_over_direct": {"fp32": ms32 / hms32, "fp64": ms64 / hms64},
+                  "rel_err_vs_direct_fp64": {"fp64": hrel64, "fp32": hrel32},
+                  "hbm_gbs_fp32": hb32 / (hk32 * 1e-3) / 1e9}
+        g.cache_hamiltonian(0)  # the rest of this leg times the direct build
 
     # end to end through the C ABI with pinned host buffers
     h_c = torch.from_numpy(np.asfortranarray(v).T.copy()).pin_memory()
@@ -721,9 +798,11 @@ def main():
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
         "clocks": clocks,
     }
+    if stored is not None:
+        out["stored_blocks"] = stored
     if rank == 0 and a.serving:
         try:
-            out["serving"] = serving_benchmark()
+            out["serving"] = serving_benchmark(stored=a.stored)
         except Exception as ex:
             out["serving"] = {"error": str(ex)}
     if rank == 0 and a.open:
@@ -733,7 +812,7 @@ def main():
             out["open_sigma"] = {"error": str(ex)}
     if rank == 0 and a.batched:
         try:
-            out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances)
+            out["batched"] = batched_benchmark(max(3, a.steps // 2), a.warmup, a.instances, a.stored)
         except Exception as ex:
             out["batched"] = {"error": str(ex)}
     if rank == 0 and a.bst:
@@ -743,7 +822,7 @@ def main():
             out["bst"] = {"error": str(ex)}
     if rank == 0 and a.davidson:
         try:
-            out["davidson"] = davidson_benchmark()
+            out["davidson"] = davidson_benchmark(stored=a.stored)
         except Exception as ex:
             out["davidson"] = {"error": str(ex)}
     if rank == 0 and a.fois:

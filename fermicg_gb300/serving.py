@@ -20,7 +20,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from .gpu import PRECISION, GpuSigma, _ptr
+from .gpu import PRECISION, FcgError, GpuSigma, _ptr
 
 
 @dataclass(order=True)
@@ -36,6 +36,7 @@ class Request:
     precision: str = field(compare=False, default="fp64")
     max_iter: int = field(compare=False, default=200)
     shape: str = field(compare=False, default="")
+    cache: bool = field(compare=False, default=False)  # store the Hamiltonian blocks (fcg_cache_hamiltonian)
 
 
 @dataclass
@@ -85,17 +86,29 @@ class SolveServer:
         if g is None:
             g = GpuSigma(self.device)
             self._ctx_pool[slot] = g
+        extra = 0
         try:
             g.set_ops(req.packed_ops)
             g.set_terms(req.packed_terms)
             g.state_set(req.focks, req.cfgs)
+            if req.cache:  # within the memory the admitted solves leave free, else the direct build
+                with self._lock:
+                    room = self.budget - self._in_use
+                try:
+                    extra = g.cache_hamiltonian(max(room, 0))
+                    with self._lock:
+                        self._in_use += extra
+                except FcgError:
+                    extra = 0
             e, X, res, it = g.davidson(req.guess, tol=req.tol, max_iter=req.max_iter, precision=req.precision)
             end = time.perf_counter()
             with self._lock:
                 self.results.append(Result(req.rid, req.shape, e, res, it, req.arrival, start, end))
         finally:
+            if extra:
+                g.cache_hamiltonian(0)
             with self._lock:
-                self._in_use -= fp
+                self._in_use -= fp + extra
                 self._active -= 1
                 self._free_slots.append(slot)
                 self._lock.notify_all()
@@ -161,7 +174,8 @@ class NativeSolveServer:
     leaving and new ones joining between rounds.  Latency runs from a request's arrival to its
     result, set-up included."""
 
-    def __init__(self, slots: int = 16, hbm_budget: float = 64e9, device: int = 0, lanes: int = 4):
+    def __init__(self, slots: int = 16, hbm_budget: float = 64e9, device: int = 0, lanes: int = 4,
+                 cache_budget: float = 8e9):
         import ctypes
         from .gpu import load_library
         self._ct = ctypes
@@ -172,6 +186,7 @@ class NativeSolveServer:
             raise RuntimeError(f"fcg_server_create failed ({rc})")
         self.h = h
         self.device = device
+        self.cache_budget = cache_budget  # largest stored Hamiltonian of one request (bytes)
         self._free = []
         self._lock = threading.Lock()
         self.results: list[Result] = []
@@ -193,6 +208,11 @@ class NativeSolveServer:
             g.set_ops(req.packed_ops)
             g.set_terms(req.packed_terms)
             g.state_set(req.focks, req.cfgs)
+            if req.cache:
+                try:
+                    g.cache_hamiltonian(self.cache_budget)
+                except FcgError:  # larger than a request may store: the direct build
+                    pass
             v = np.asfortranarray(req.guess, dtype=np.float64)
             n, R = v.shape
             ticket = ct.c_int64(0)
@@ -210,6 +230,8 @@ class NativeSolveServer:
             with self._lock:
                 self.results.append(Result(req.rid, req.shape, e, res, it.value, req.arrival, start, end))
         finally:
+            if req.cache:
+                g.cache_hamiltonian(0)  # a pooled context keeps no stored blocks between requests
             with self._lock:
                 self._free.append(g)
 

@@ -101,3 +101,26 @@ def test_native_server_wait_times_out_and_a_failed_request_leaves_the_others():
     assert L.fcg_server_destroy(h) == 0
     for g in gs:
         g.close()
+
+
+@pytest.mark.parametrize("native", [False, True])
+def test_stored_blocks_in_the_mix_give_the_same_energies(native):
+    """Requests that store their Hamiltonian blocks (fcg_cache_hamiltonian) before the solve
+    end with the energies of the same requests without them."""
+    from fermicg_gb300.serving import NativeSolveServer
+    p0 = workloads.build_problem(12, [3, 3, 3, 3], [(2, 1), (1, 2), (2, 1), (1, 2)], 36, 3, max_roots=1000)
+    p1 = workloads.build_problem(16, [4, 4, 4, 4], [(2, 2)] * 4, 24, 4, max_roots=12, delta_elec=2)
+    base = [_request(i, p0 if i % 2 == 0 else p1, 1500 if i % 2 == 0 else 3000, 1 + (i % 3), i, 0.002 * i,
+                     precision="fp64" if i % 4 < 2 else "fp32")
+            for i in range(6)]
+    out = {}
+    for cache in (False, True):
+        reqs = [Request(r.arrival, r.rid, r.packed_ops, r.packed_terms, r.focks, r.cfgs, r.guess, r.tol,
+                        r.precision, r.max_iter, r.shape, cache=cache) for r in base]
+        srv = NativeSolveServer(slots=3, lanes=1) if native else SolveServer(slots=3)
+        out[cache] = srv.run(reqs)
+        srv.close()
+    for a, b in zip(out[False], out[True]):
+        assert a.rid == b.rid
+        np.testing.assert_allclose(b.energies, a.energies, rtol=0, atol=1e-9)
+        assert b.residuals.max() < 1e-7
