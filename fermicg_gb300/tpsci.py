@@ -13,16 +13,19 @@ from __future__ import annotations
 import numpy as np
 
 from . import pack
-from .gpu import GpuSigma
+from .gpu import FcgError, GpuSigma
 from .state import (TPSCIstate, add_state, clip, copy_state, minus_state, overlap, project_out,
                     state_from_rows, times_matrix, zero_state)
 from .terms import extract_1body_operator
 
 
 class GpuTPSCI:
-    def __init__(self, ops, bases, ham, device: int = 0, precision: str = "fp64"):
+    def __init__(self, ops, bases, ham, device: int = 0, precision: str = "fp64", store_blocks: float = 16e9):
+        """store_blocks: largest stored Hamiltonian (bytes) a variational solve may keep on
+        the device (fcg_cache_hamiltonian); a larger one, or 0, solves with the direct build."""
         self.N = ham.n_clusters
         self.precision = precision
+        self.store_blocks = store_blocks
         self.H = GpuSigma(device)
         self.H.set_problem(ops, bases, ham)
         self.H0 = GpuSigma(device)
@@ -42,8 +45,14 @@ class GpuTPSCI:
     def solve(self, s: TPSCIstate, tol=1e-8, max_iter=200, max_ss_vecs=12, lindep=1e-12):
         """Lowest R eigenpairs of H within s's configurations (tps_ci_davidson)."""
         v = self._index(self.H, s)
+        if self.store_blocks > 0:  # every sigma of this solve reads the stored blocks
+            try:
+                self.H.cache_hamiltonian(self.store_blocks)
+            except FcgError:
+                pass
         e, X, res, it = self.H.davidson(v, max_iter=max_iter, max_ss_vecs=max_ss_vecs, tol=tol, lindep=lindep,
                                         precision=self.precision)
+        self.H.cache_hamiltonian(0)
         out = copy_state(s)
         out.set_vector(X)
         return e, out, res

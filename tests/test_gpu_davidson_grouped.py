@@ -58,3 +58,20 @@ def test_grouped_rejects_a_context_twice():
     with pytest.raises(Exception):
         davidson_grouped([g, g], [guess, guess])
     g.close()
+
+
+def test_a_failing_problem_is_named_and_the_contexts_stay_usable():
+    from fermicg_gb300.gpu import FcgError
+    probs = _problems(3)
+    gpus = [p[0] for p in probs]
+    guesses = [p[1].copy() for p in probs]
+    guesses[1][:] = np.nan  # no usable initial direction: the solve of problem 1 fails
+    with pytest.raises(FcgError, match="problem 1"):
+        davidson_grouped(gpus, guesses, tol=1e-7, max_iter=300)
+    for g, guess, ref in probs:  # every context still solves alone, on its own stream
+        e, X, r, it = g.davidson(guess, tol=1e-7, max_iter=300)
+        assert np.abs(e - ref).max() < 1e-9
+    res = davidson_grouped([gpus[0], gpus[2]], [probs[0][1], probs[2][1]], tol=1e-7, max_iter=300)
+    assert np.abs(res[1][0] - probs[2][2]).max() < 1e-9
+    for g in gpus:
+        g.close()
