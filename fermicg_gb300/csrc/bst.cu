@@ -15,10 +15,12 @@
 // bra core[kb] += sum_kk OP[kk, kb_active] X[kk_active, kb_spectators]  (the op2^T * ket2 GEMM
 // of contract_dense_H_with_state).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -477,202 +479,84 @@ void append_perm(const BstBlock& B, int N, int mask, std::vector<int32_t>& perm)
   }
 }
 
-// The triples of build_sigma! (every bra block against every ket block whose Fock sector
-// differs by a TransferConfig of H, every term of that transfer with at most nbody clusters
-// for which check_term holds on the TuckerConfigs: equal Fock sectors and equal ranges on
-// the spectators), grouped by (bra, ket, active clusters).
-std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>& blk, const int16_t* fock,
-                     BstPlan& P, const int32_t* given = nullptr, int64_t n_given = 0, int64_t split = 0) {
-  const int N = ctx->N;
-  const int nmax1 = ctx->nmax + 1;
+// The part of a BST plan that one range of bra blocks contributes, with offsets local to the
+// part (g_off of its dressed TDMs, op_off of its operators, t_off of its group terms, s_off
+// of its overlaps); plan_bst concatenates the parts in bra order and shifts the offsets.
+// Everything in a part is keyed by its own bra blocks, so parts are built independently.
+struct BstPart {
+  std::vector<int32_t> triples;
+  std::vector<BstGroup> groups;
+  std::vector<std::vector<BstGroupTerm>> gt;   // terms per group
+  std::vector<BstGroupTerm> gterms;            // the same, flattened by finish_part
+  std::vector<BstGamma> gammas;
+  std::vector<BstOverlapJob> overlaps;
+  std::unordered_map<uint64_t, int64_t> gamma_at;    // (bra, ket, c, op) -> g offset
+  std::unordered_map<uint64_t, int64_t> overlap_at;  // (bra, ket, c) -> S offset
+  int64_t g_total = 0, op_total = 0, s_total = 0, flops_ref = 0, flops_exec = 0;
+  std::string err;
+};
+
+// One (bra, ket, term) triple into its (bra, ket, active clusters) group, with the dressed
+// TDMs it needs; grp maps (ket, mask) to the bra block's groups.
+std::string add_triple(const fcg_ctx* ctx, const std::vector<BstBlock>& blk, BstPart& P, int64_t b, int32_t k, int t,
+                       const int32_t* r, int mask, const int* tdm, int sign,
+                       std::unordered_map<uint64_t, int32_t>& grp) {
   const int64_t nb = int64_t(blk.size());
-  std::vector<std::vector<int>> by_trans(ctx->n_trans);
-  for (int t = 0; t < ctx->n_terms; ++t) {
-    const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
-    if (r[0] <= nbody) by_trans[r[1]].push_back(t);
-  }
-  // ket lookup per active-cluster mask: hash of (fock, spectator ranges) -> blocks; the
-  // candidates of a hash are compared in full before use
-  auto mix = [](uint64_t h, uint64_t v) {
-    h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
-    return h;
-  };
-  auto hash_of = [&](int64_t b, const int16_t* f, int mask) {
-    uint64_t h = uint64_t(mask) * 0x100000001b3ULL;
-    for (int c = 0; c < N; ++c) {
-      h = mix(h, uint64_t(uint16_t(f[2 * c])) | (uint64_t(uint16_t(f[2 * c + 1])) << 16));
-      if (!((mask >> c) & 1)) h = mix(h, uint64_t(uint32_t(blk[b].start[c])) | (uint64_t(uint32_t(blk[b].len[c])) << 32));
-    }
-    return h;
-  };
-  // ket sides: 0 = blocks [0, split), 1 = blocks [split, nb), 2 = all blocks (no split)
-  auto in_side = [&](int64_t k, int side) { return side == 2 || ((k < split) == (side == 0)); };
-  std::unordered_map<int, std::unordered_map<uint64_t, std::vector<int32_t>>> lookup;
-  auto kets_of = [&](int mask, int side) -> std::unordered_map<uint64_t, std::vector<int32_t>>& {
-    const int key = mask * 4 + side;
-    auto it = lookup.find(key);
-    if (it != lookup.end()) return it->second;
-    auto& m = lookup[key];
-    for (int64_t k = 0; k < nb; ++k)
-      if (in_side(k, side)) m[hash_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
-    return m;
-  };
-  auto matches = [&](int64_t b, const int16_t* fk, int64_t k, int mask) {
-    const int16_t* f = fock + 2 * N * k;
-    for (int c = 0; c < N; ++c) {
-      if (f[2 * c] != fk[2 * c] || f[2 * c + 1] != fk[2 * c + 1]) return false;
-      if (!((mask >> c) & 1) && (blk[k].start[c] != blk[b].start[c] || blk[k].len[c] != blk[b].len[c])) return false;
-    }
-    return true;
-  };
-  // Fock sectors present (a transfer into any other sector has no ket)
-  std::unordered_map<uint64_t, int> sectors[3];
-  for (int64_t k = 0; k < nb; ++k)
-    for (int side = 0; side < 3; ++side)
-      if (in_side(k, side)) sectors[side][hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
-  std::unordered_map<uint64_t, int64_t> gamma_at;   // (bra, ket, c, op) -> g offset
-  std::unordered_map<uint64_t, int64_t> overlap_at; // (bra, ket, c) -> S offset
-  std::unordered_map<uint64_t, int64_t> perm_at;    // (block, active mask) -> index table offset
-  std::vector<std::vector<BstGroupTerm>> gt;        // terms per group
-  // one (bra, ket, term) triple into its (bra, ket, active clusters) group, with the
-  // dressed TDMs it needs; grp maps (ket, mask) to the bra block's groups
-  auto add_triple = [&](int64_t b, int32_t k, int t, const int32_t* r, int mask, const int* tdm, int sign,
-                        std::unordered_map<uint64_t, int32_t>& grp) -> std::string {
-    P.triples.insert(P.triples.end(), {int32_t(b), k, int32_t(t), int32_t(sign)});
-    const uint64_t gk = (uint64_t(uint32_t(k)) << 8) | uint64_t(mask);
-    auto gi = grp.find(gk);
-    int32_t g;
-    if (gi == grp.end()) {
-      g = int32_t(P.groups.size());
-      grp[gk] = g;
-      BstGroup G{};
-      G.bra = int32_t(b);
-      G.ket = k;
-      G.act_mask = mask;
-      P.groups.push_back(G);
-      gt.emplace_back();
-    } else {
-      g = gi->second;
-    }
-    BstGroupTerm T{};
-    T.nact = r[0];
-    T.sign = sign;
-    T.ints_off = r[0] == 1 ? -1 : ctx->terms[t].ints_off;
-    for (int o = 0; o < r[0]; ++o) {
-      const int c = r[2 + o];
-      const BlockInfo& BI = ctx->h_blocks[tdm[o]];
-      if (r[0] > 1 && BI.nidx != r[22 + o]) return "BST: TDM multi-index length differs from the term's ints";
-      const uint64_t key = ((uint64_t(b) * uint64_t(nb) + uint64_t(k)) * 8 + uint64_t(c)) * 32 + uint64_t(r[6 + o]);
-      auto ga = gamma_at.find(key);
-      if (ga == gamma_at.end()) {
-        BstGamma Q{};
-        Q.g_off = P.g_total;
-        Q.tdm_off = BI.off;
-        Q.bra = int32_t(b);
-        Q.ket = k;
-        Q.c = c;
-        Q.np = BI.nidx;
-        Q.tdm_mb = BI.mb;
-        if (blk[b].start[c] + blk[b].len[c] > BI.mb || blk[k].start[c] + blk[k].len[c] > BI.mk)
-          return "BST: a Tucker range exceeds the local basis of its Fock sector";
-        P.gammas.push_back(Q);
-        ga = gamma_at.emplace(key, P.g_total).first;
-        P.g_total += align_up(int64_t(BI.nidx) * blk[b].rank[c] * blk[k].rank[c]);
-      }
-      T.g_off[o] = ga->second;
-      T.np[o] = BI.nidx;
-    }
-    gt[g].push_back(T);
-    return std::string();
-  };
-  if (given) {
-    // the caller's triples {bra, ket, term}, taken in bra order (the groups of one bra block
-    // must be contiguous); each is checked as check_term would
-    std::vector<int64_t> order(static_cast<size_t>(n_given));
-    for (int64_t q = 0; q < n_given; ++q) order[size_t(q)] = q;
-    std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return given[3 * x] < given[3 * y]; });
-    std::unordered_map<uint64_t, int32_t> grp;
-    int64_t cur_bra = -1;
-    for (int64_t q : order) {
-      const int32_t* tq = given + 3 * q;
-      const int64_t b = tq[0];
-      const int32_t k = tq[1];
-      const int t = tq[2];
-      if (b < 0 || b >= nb || k < 0 || k >= nb || t < 0 || t >= ctx->n_terms) return "BST: a given triple is out of range";
-      if (b != cur_bra) {
-        grp.clear();
-        cur_bra = b;
-      }
-      const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
-      if (r[0] > nbody) return "BST: a given triple's term has more than nbody clusters";
-      const int16_t* fb = fock + 2 * N * b;
-      const int16_t* fkk = fock + 2 * N * k;
-      int mask = 0;
-      for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
-      for (int c = 0; c < N; ++c) {
-        for (int s2 = 0; s2 < 2; ++s2)
-          if (fb[2 * c + s2] - fkk[2 * c + s2] != ctx->trans[(int64_t(r[1]) * N + c) * 2 + s2])
-            return "BST: a given triple's Fock sectors do not differ by its term's transfer";
-        if (!((mask >> c) & 1) && (blk[b].start[c] != blk[k].start[c] || blk[b].len[c] != blk[k].len[c]))
-          return "BST: a given triple fails check_term on the spectator ranges";
-      }
-      int tdm[4];
-      for (int o = 0; o < r[0]; ++o) {
-        const int c = r[2 + o];
-        tdm[o] = ctx->h_blk_index[dense_block_index(nmax1, c, r[6 + o], fb[2 * c], fb[2 * c + 1], fkk[2 * c],
-                                                    fkk[2 * c + 1])];
-        if (tdm[o] < 0) return "BST: a given triple needs a TDM block that does not exist";
-      }
-      std::string msg = add_triple(b, k, t, r, mask, tdm, term_state_sign(r, fkk), grp);
-      if (!msg.empty()) return msg;
-    }
+  P.triples.insert(P.triples.end(), {int32_t(b), k, int32_t(t), int32_t(sign)});
+  const uint64_t gk = (uint64_t(uint32_t(k)) << 8) | uint64_t(mask);
+  auto gi = grp.find(gk);
+  int32_t g;
+  if (gi == grp.end()) {
+    g = int32_t(P.groups.size());
+    grp[gk] = g;
+    BstGroup G{};
+    G.bra = int32_t(b);
+    G.ket = k;
+    G.act_mask = mask;
+    P.groups.push_back(G);
+    P.gt.emplace_back();
   } else {
-  std::vector<int16_t> fk(2 * N);
-  for (int64_t b = 0; b < nb; ++b) {
-    const int16_t* fb = fock + 2 * N * b;
-    const int kside = split > 0 ? (b < split ? 1 : 0) : 2;  // the other state's blocks only
-    std::unordered_map<uint64_t, int32_t> grp;  // (ket, mask) -> group
-    for (int tr = 0; tr < ctx->n_trans; ++tr) {
-      if (by_trans[tr].empty()) continue;
-      bool ok = true;
-      for (int c = 0; c < N && ok; ++c)
-        for (int s = 0; s < 2; ++s) {
-          const int v = fb[2 * c + s] - ctx->trans[(int64_t(tr) * N + c) * 2 + s];
-          if (v < 0 || v > ctx->norb[c]) ok = false;
-          fk[2 * c + s] = int16_t(v);
-        }
-      if (!ok) continue;
-      if (!sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
-      for (int t : by_trans[tr]) {
-        const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
-        int mask = 0;
-        for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
-        // TDM blocks of the active clusters for this sector pair
-        int tdm[4];
-        bool have = true;
-        for (int o = 0; o < r[0] && have; ++o) {
-          const int c = r[2 + o];
-          tdm[o] = ctx->h_blk_index[dense_block_index(nmax1, c, r[6 + o], fb[2 * c], fb[2 * c + 1], fk[2 * c],
-                                                      fk[2 * c + 1])];
-          have = tdm[o] >= 0;
-        }
-        if (!have) continue;
-        auto& m = kets_of(mask, kside);
-        auto it = m.find(hash_of(b, fk.data(), mask));
-        if (it == m.end()) continue;
-        const int sign = term_state_sign(r, fk.data());
-        for (int32_t k : it->second) {
-          if (!matches(b, fk.data(), k, mask)) continue;
-          {
-            std::string msg = add_triple(b, k, t, r, mask, tdm, sign, grp);
-            if (!msg.empty()) return msg;
-          }
-        }
-      }
-    }
+    g = gi->second;
   }
-  }  // enumeration
-  // group operators, spectator overlaps, workspace sizes and flop counts
+  BstGroupTerm T{};
+  T.nact = r[0];
+  T.sign = sign;
+  T.ints_off = r[0] == 1 ? -1 : ctx->terms[t].ints_off;
+  for (int o = 0; o < r[0]; ++o) {
+    const int c = r[2 + o];
+    const BlockInfo& BI = ctx->h_blocks[tdm[o]];
+    if (r[0] > 1 && BI.nidx != r[22 + o]) return "BST: TDM multi-index length differs from the term's ints";
+    const uint64_t key = ((uint64_t(b) * uint64_t(nb) + uint64_t(k)) * 8 + uint64_t(c)) * 32 + uint64_t(r[6 + o]);
+    auto ga = P.gamma_at.find(key);
+    if (ga == P.gamma_at.end()) {
+      BstGamma Q{};
+      Q.g_off = P.g_total;
+      Q.tdm_off = BI.off;
+      Q.bra = int32_t(b);
+      Q.ket = k;
+      Q.c = c;
+      Q.np = BI.nidx;
+      Q.tdm_mb = BI.mb;
+      if (blk[b].start[c] + blk[b].len[c] > BI.mb || blk[k].start[c] + blk[k].len[c] > BI.mk)
+        return "BST: a Tucker range exceeds the local basis of its Fock sector";
+      P.gammas.push_back(Q);
+      ga = P.gamma_at.emplace(key, P.g_total).first;
+      P.g_total += align_up(int64_t(BI.nidx) * blk[b].rank[c] * blk[k].rank[c]);
+    }
+    T.g_off[o] = ga->second;
+    T.np[o] = BI.nidx;
+  }
+  P.gt[g].push_back(T);
+  return std::string();
+}
+
+// Group operators, spectator overlaps, workspace sizes and flop counts of a part (the
+// index-table offsets are left to the merge: tables are shared between parts).
+std::string finish_part(const std::vector<BstBlock>& blk, int N, BstPart& P) {
+  const int64_t nb = int64_t(blk.size());
+  size_t n_terms = 0;
+  for (const auto& v : P.gt) n_terms += v.size();
+  P.gterms.reserve(n_terms);
   for (size_t g = 0; g < P.groups.size(); ++g) {
     BstGroup& G = P.groups[g];
     const BstBlock& B = blk[G.bra];
@@ -692,8 +576,8 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     G.op_off = P.op_total;
     P.op_total += align_up(m * k);
     G.t_off = int32_t(P.gterms.size());
-    G.nt = int32_t(gt[g].size());
-    P.gterms.insert(P.gterms.end(), gt[g].begin(), gt[g].end());
+    G.nt = int32_t(P.gt[g].size());
+    P.gterms.insert(P.gterms.end(), P.gt[g].begin(), P.gt[g].end());
     // core strides and the index description of the rank > 1 clusters
     int64_t kst[kMaxClusters], bst[kMaxClusters];
     {
@@ -732,10 +616,10 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
       if ((G.act_mask >> c) & 1) continue;
       if (B.rank[c] == 1 && K.rank[c] == 1) continue;
       const uint64_t key = (uint64_t(G.bra) * uint64_t(nb) + uint64_t(G.ket)) * 8 + uint64_t(c);
-      auto it = overlap_at.find(key);
-      if (it == overlap_at.end()) {
+      auto it = P.overlap_at.find(key);
+      if (it == P.overlap_at.end()) {
         P.overlaps.push_back(BstOverlapJob{P.s_total, G.bra, G.ket, c, 0});
-        it = overlap_at.emplace(key, P.s_total).first;
+        it = P.overlap_at.emplace(key, P.s_total).first;
         P.s_total += align_up(int64_t(B.rank[c]) * K.rank[c]);
       }
       G.s_off[j++] = it->second;
@@ -746,19 +630,247 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     for (int j = G.nsp; j < kMaxClusters; ++j) G.s_off[j] = 0;
     if (ws > (int64_t(1) << 30)) return "BST: a core exceeds 2^30 elements";
     G.ws = int32_t(align_up(ws));
-    for (int side = 0; side < 2; ++side) {
-      const int32_t b = side == 0 ? G.ket : G.bra;
-      const uint64_t key = uint64_t(b) * 256 + uint64_t(G.act_mask);
-      auto it = perm_at.find(key);
-      if (it == perm_at.end()) {
-        it = perm_at.emplace(key, int64_t(P.perm.size())).first;
-        append_perm(blk[b], N, G.act_mask, P.perm);
-      }
-      (side == 0 ? G.kperm_off : G.bperm_off) = it->second;
-    }
     const int64_t f = 2 * m * k * n + tf;
     P.flops_exec += f;
     P.flops_ref += f * G.nt;
+  }
+  P.gt.clear();
+  P.gt.shrink_to_fit();
+  return "";
+}
+
+// The triples of build_sigma! (every bra block against every ket block whose Fock sector
+// differs by a TransferConfig of H, every term of that transfer with at most nbody clusters
+// for which check_term holds on the TuckerConfigs: equal Fock sectors and equal ranges on
+// the spectators), grouped by (bra, ket, active clusters).  Ranges of bra blocks are planned
+// on host threads and concatenated in bra order, so the plan does not depend on the thread
+// count.
+std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>& blk, const int16_t* fock,
+                     BstPlan& P, const int32_t* given = nullptr, int64_t n_given = 0, int64_t split = 0) {
+  const int N = ctx->N;
+  const int nmax1 = ctx->nmax + 1;
+  const int64_t nb = int64_t(blk.size());
+  std::vector<std::vector<int>> by_trans(ctx->n_trans);
+  for (int t = 0; t < ctx->n_terms; ++t) {
+    const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+    if (r[0] <= nbody) by_trans[r[1]].push_back(t);
+  }
+  // ket lookup per active-cluster mask: hash of (fock, spectator ranges) -> blocks; the
+  // candidates of a hash are compared in full before use
+  auto mix = [](uint64_t h, uint64_t v) {
+    h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+    return h;
+  };
+  auto hash_of = [&](int64_t b, const int16_t* f, int mask) {
+    uint64_t h = uint64_t(mask) * 0x100000001b3ULL;
+    for (int c = 0; c < N; ++c) {
+      h = mix(h, uint64_t(uint16_t(f[2 * c])) | (uint64_t(uint16_t(f[2 * c + 1])) << 16));
+      if (!((mask >> c) & 1)) h = mix(h, uint64_t(uint32_t(blk[b].start[c])) | (uint64_t(uint32_t(blk[b].len[c])) << 32));
+    }
+    return h;
+  };
+  // ket sides: 0 = blocks [0, split), 1 = blocks [split, nb), 2 = all blocks (no split)
+  auto in_side = [&](int64_t k, int side) { return side == 2 || ((k < split) == (side == 0)); };
+  auto matches = [&](int64_t b, const int16_t* fk, int64_t k, int mask) {
+    const int16_t* f = fock + 2 * N * k;
+    for (int c = 0; c < N; ++c) {
+      if (f[2 * c] != fk[2 * c] || f[2 * c + 1] != fk[2 * c + 1]) return false;
+      if (!((mask >> c) & 1) && (blk[k].start[c] != blk[b].start[c] || blk[k].len[c] != blk[b].len[c])) return false;
+    }
+    return true;
+  };
+  std::vector<BstPart> parts;
+  if (given) {
+    // the caller's triples {bra, ket, term}, taken in bra order (the groups of one bra block
+    // must be contiguous); each is checked as check_term would
+    parts.resize(1);
+    BstPart& part = parts[0];
+    std::vector<int64_t> order(static_cast<size_t>(n_given));
+    for (int64_t q = 0; q < n_given; ++q) order[size_t(q)] = q;
+    std::stable_sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return given[3 * x] < given[3 * y]; });
+    std::unordered_map<uint64_t, int32_t> grp;
+    int64_t cur_bra = -1;
+    for (int64_t q : order) {
+      const int32_t* tq = given + 3 * q;
+      const int64_t b = tq[0];
+      const int32_t k = tq[1];
+      const int t = tq[2];
+      if (b < 0 || b >= nb || k < 0 || k >= nb || t < 0 || t >= ctx->n_terms) return "BST: a given triple is out of range";
+      if (b != cur_bra) {
+        grp.clear();
+        cur_bra = b;
+      }
+      const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+      if (r[0] > nbody) return "BST: a given triple's term has more than nbody clusters";
+      const int16_t* fb = fock + 2 * N * b;
+      const int16_t* fkk = fock + 2 * N * k;
+      int mask = 0;
+      for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
+      for (int c = 0; c < N; ++c) {
+        for (int s2 = 0; s2 < 2; ++s2)
+          if (fb[2 * c + s2] - fkk[2 * c + s2] != ctx->trans[(int64_t(r[1]) * N + c) * 2 + s2])
+            return "BST: a given triple's Fock sectors do not differ by its term's transfer";
+        if (!((mask >> c) & 1) && (blk[b].start[c] != blk[k].start[c] || blk[b].len[c] != blk[k].len[c]))
+          return "BST: a given triple fails check_term on the spectator ranges";
+      }
+      int tdm[4];
+      for (int o = 0; o < r[0]; ++o) {
+        const int c = r[2 + o];
+        tdm[o] = ctx->h_blk_index[dense_block_index(nmax1, c, r[6 + o], fb[2 * c], fb[2 * c + 1], fkk[2 * c],
+                                                    fkk[2 * c + 1])];
+        if (tdm[o] < 0) return "BST: a given triple needs a TDM block that does not exist";
+      }
+      std::string msg = add_triple(ctx, blk, part, b, k, t, r, mask, tdm, term_state_sign(r, fkk), grp);
+      if (!msg.empty()) return msg;
+    }
+    std::string msg = finish_part(blk, N, part);
+    if (!msg.empty()) return msg;
+  } else {
+    // Fock sectors present (a transfer into any other sector has no ket), and the ket
+    // lookups of every active-cluster mask the terms use, built before the threads read them
+    std::unordered_map<uint64_t, int> sectors[3];
+    for (int64_t k = 0; k < nb; ++k)
+      for (int side = 0; side < 3; ++side)
+        if (in_side(k, side)) sectors[side][hash_of(k, fock + 2 * N * k, (1 << N) - 1)] = 1;
+    std::unordered_map<int, std::unordered_map<uint64_t, std::vector<int32_t>>> lookup;
+    {
+      std::vector<int> sides = split > 0 ? std::vector<int>{0, 1} : std::vector<int>{2};
+      for (int t = 0; t < ctx->n_terms; ++t) {
+        const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+        if (r[0] > nbody) continue;
+        int mask = 0;
+        for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
+        for (int side : sides) {
+          const int key = mask * 4 + side;
+          if (lookup.count(key)) continue;
+          auto& m = lookup[key];
+          for (int64_t k = 0; k < nb; ++k)
+            if (in_side(k, side)) m[hash_of(k, fock + 2 * N * k, mask)].push_back(int32_t(k));
+        }
+      }
+    }
+    constexpr int64_t kBrasPerPart = 16;
+    const int64_t n_parts = (nb + kBrasPerPart - 1) / kBrasPerPart;
+    parts.resize(size_t(n_parts));
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+      std::vector<int16_t> fk(2 * N);
+      for (int64_t q = next.fetch_add(1); q < n_parts; q = next.fetch_add(1)) {
+        BstPart& part = parts[size_t(q)];
+        const int64_t b1 = std::min(nb, (q + 1) * kBrasPerPart);
+        for (int64_t b = q * kBrasPerPart; b < b1 && part.err.empty(); ++b) {
+          const int16_t* fb = fock + 2 * N * b;
+          const int kside = split > 0 ? (b < split ? 1 : 0) : 2;  // the other state's blocks only
+          std::unordered_map<uint64_t, int32_t> grp;              // (ket, mask) -> group
+          for (int tr = 0; tr < ctx->n_trans && part.err.empty(); ++tr) {
+            if (by_trans[tr].empty()) continue;
+            bool ok = true;
+            for (int c = 0; c < N && ok; ++c)
+              for (int s = 0; s < 2; ++s) {
+                const int v = fb[2 * c + s] - ctx->trans[(int64_t(tr) * N + c) * 2 + s];
+                if (v < 0 || v > ctx->norb[c]) ok = false;
+                fk[2 * c + s] = int16_t(v);
+              }
+            if (!ok) continue;
+            if (!sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
+            for (int t : by_trans[tr]) {
+              const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+              int mask = 0;
+              for (int o = 0; o < r[0]; ++o) mask |= 1 << r[2 + o];
+              // TDM blocks of the active clusters for this sector pair
+              int tdm[4];
+              bool have = true;
+              for (int o = 0; o < r[0] && have; ++o) {
+                const int c = r[2 + o];
+                tdm[o] = ctx->h_blk_index[dense_block_index(nmax1, c, r[6 + o], fb[2 * c], fb[2 * c + 1], fk[2 * c],
+                                                            fk[2 * c + 1])];
+                have = tdm[o] >= 0;
+              }
+              if (!have) continue;
+              const auto& m = lookup.at(mask * 4 + kside);
+              auto it = m.find(hash_of(b, fk.data(), mask));
+              if (it == m.end()) continue;
+              const int sign = term_state_sign(r, fk.data());
+              for (int32_t k : it->second) {
+                if (!matches(b, fk.data(), k, mask)) continue;
+                std::string msg = add_triple(ctx, blk, part, b, k, t, r, mask, tdm, sign, grp);
+                if (!msg.empty()) {
+                  part.err = msg;
+                  break;
+                }
+              }
+              if (!part.err.empty()) break;
+            }
+          }
+        }
+        if (part.err.empty()) part.err = finish_part(blk, N, part);
+      }
+    };
+    const int n_threads = int(std::max<int64_t>(1, std::min<int64_t>(
+        {int64_t(std::max(1u, std::thread::hardware_concurrency())), int64_t(32), n_parts})));
+    std::vector<std::thread> pool;
+    for (int i = 1; i < n_threads; ++i) pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool) th.join();
+    for (const BstPart& part : parts)
+      if (!part.err.empty()) return part.err;
+  }
+  // concatenation in bra order; the index tables are shared: each (block, active mask) gets
+  // its table where it is first used, as a serial walk over the groups would place it
+  {
+    size_t n_groups = 0, n_gterms = 0, n_triples = 0, n_gammas = 0, n_ov = 0;
+    for (const BstPart& part : parts) {
+      n_groups += part.groups.size();
+      n_gterms += part.gterms.size();
+      n_triples += part.triples.size();
+      n_gammas += part.gammas.size();
+      n_ov += part.overlaps.size();
+    }
+    P.groups.reserve(n_groups);
+    P.gterms.reserve(n_gterms);
+    P.triples.reserve(n_triples);
+    P.gammas.reserve(n_gammas);
+    P.overlaps.reserve(n_ov);
+  }
+  std::unordered_map<uint64_t, int64_t> perm_at;  // (block, active mask) -> index table offset
+  for (BstPart& part : parts) {
+    const int64_t g0 = P.g_total, op0 = P.op_total, s0 = P.s_total, t0 = int64_t(P.gterms.size());
+    if (t0 + int64_t(part.gterms.size()) >= (int64_t(1) << 31)) return "BST: more than 2^31 group terms";
+    for (BstGamma Q : part.gammas) {
+      Q.g_off += g0;
+      P.gammas.push_back(Q);
+    }
+    for (BstGroupTerm T : part.gterms) {
+      for (int o = 0; o < T.nact; ++o) T.g_off[o] += g0;
+      P.gterms.push_back(T);
+    }
+    for (BstOverlapJob J : part.overlaps) {
+      J.s_off += s0;
+      P.overlaps.push_back(J);
+    }
+    P.triples.insert(P.triples.end(), part.triples.begin(), part.triples.end());
+    for (BstGroup G : part.groups) {
+      G.op_off += op0;
+      G.t_off += int32_t(t0);
+      for (int j = 0; j < G.nsp; ++j) G.s_off[j] += s0;
+      for (int side = 0; side < 2; ++side) {
+        const int32_t b = side == 0 ? G.ket : G.bra;
+        const uint64_t key = uint64_t(b) * 256 + uint64_t(G.act_mask);
+        auto it = perm_at.find(key);
+        if (it == perm_at.end()) {
+          it = perm_at.emplace(key, int64_t(P.perm.size())).first;
+          append_perm(blk[b], N, G.act_mask, P.perm);
+        }
+        (side == 0 ? G.kperm_off : G.bperm_off) = it->second;
+      }
+      P.groups.push_back(G);
+    }
+    P.g_total += part.g_total;
+    P.op_total += part.op_total;
+    P.s_total += part.s_total;
+    P.flops_exec += part.flops_exec;
+    P.flops_ref += part.flops_ref;
+    part = BstPart();  // free the part as it is consumed
   }
   return "";
 }
