@@ -230,7 +230,8 @@ class GpuSigma:
         return hd
 
     def sigma_open(self, coeffs, thresh, nbody=4):
-        """open_matvec_thread: (fock (m,N,2) int16, cfg (m,N) int16, coeff (m,R)) of the FOIS sigma."""
+        """open_matvec_thread: (fock (m,N,2) int16, cfg (m,N) int16, coeff (m,R)) of the FOIS sigma.
+        coeff is column-major as the library writes it (no second copy of m*R doubles)."""
         c = np.asfortranarray(coeffs, dtype=np.float64)
         n, R = c.shape
         if n != self.n_cfg:
@@ -243,7 +244,7 @@ class GpuSigma:
         oc = np.empty((m, self.N), dtype=np.int16)
         ov = np.empty((m, R), dtype=np.float64, order="F")
         self._check(self.L.fcg_sigma_open_fetch(self.h, _ptr(of), _ptr(oc), _ptr(ov)), "fcg_sigma_open_fetch")
-        return of, oc, np.ascontiguousarray(ov)
+        return of, oc, ov
 
     def davidson(self, v0, max_iter=100, max_ss_vecs=12, tol=1e-8, lindep=1e-12, precision="fp64",
                  precond=True):
