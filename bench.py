@@ -54,6 +54,8 @@ def parse():
     ap.add_argument("--no-open", dest="open", action="store_false", help="skip the open (FOIS) sigma leg")
     ap.add_argument("--open-only", action="store_true", help="run only the open (FOIS) sigma leg")
     ap.add_argument("--no-fois", dest="fois", action="store_false", help="skip the BST first-order space leg")
+    ap.add_argument("--no-tpsci", dest="tpsci", action="store_false", help="skip the tpsci_ci driver leg")
+    ap.add_argument("--tpsci-only", action="store_true", help="run only the tpsci_ci driver leg")
     ap.add_argument("--fois-only", action="store_true", help="run only the BST first-order space leg")
     ap.add_argument("--no-davidson", dest="davidson", action="store_false", help="skip the per-shape solve timings")
     ap.add_argument("--serving-only", action="store_true", help="run only the solve-stream leg (both servers)")
@@ -455,6 +457,50 @@ def batched_benchmark(steps, warmup, n_inst=256, stored=True):
     return out
 
 
+def tpsci_benchmark(cpu_seconds):
+    """tpsci_ci (src/tpsci.jl:39-363) on the 12-orbital / 4-cluster x 3 problem (full local FCI
+    bases, 6a/6b, one root, thresh_cipsi 1e-3, thresh_foi 1e-5, FP64) from the reference
+    configuration: the GPU driver to convergence with compute_pt2_energy on top, and the
+    first three macro-iterations on the GPU and in the oracle's restatement on the host
+    cores (equal work: the same spaces, the same energies)."""
+    from fermicg_gb300 import workloads
+    from fermicg_gb300.state import TPSCIstate
+    from fermicg_gb300.tpsci import GpuTPSCI
+    prob = workloads.config0_problem(0)
+    N = len(prob.clusters)
+
+    def start():
+        st = TPSCIstate(N, 1)
+        st[(tuple(map(tuple, prob.init_fspace)), (0,) * N)] = np.array([1.0])
+        return st
+
+    T = GpuTPSCI(prob.ops, prob.bases, prob.ham)
+    T.tpsci_ci(start(), thresh_cipsi=1e-3, thresh_foi=1e-5, max_iter=2)  # warm-up
+    t1 = time.perf_counter()
+    e0, v0 = T.tpsci_ci(start(), thresh_cipsi=1e-3, thresh_foi=1e-5)
+    t2 = time.perf_counter()
+    e2 = T.pt2_energy(v0, thresh_foi=1e-5)
+    t3 = time.perf_counter()
+    e3, v3 = T.tpsci_ci(start(), thresh_cipsi=1e-3, thresh_foi=1e-5, max_iter=3)
+    t4 = time.perf_counter()
+    T.close()
+    out = {"workload": "tpsci_ci 12o / 4 clusters x 3, full local FCI, 1 root, thresh_cipsi 1e-3, thresh_foi 1e-5",
+           "gpu_tpsci_ci_s": t2 - t1, "gpu_pt2_s": t3 - t2, "e0": float(e0[0]), "e0_plus_e2": float(e0[0] + e2[0]),
+           "configurations": len(v0), "first_3_iterations": {"gpu_s": t4 - t3, "configurations": len(v3),
+                                                             "e0": float(e3[0])}}
+    if cpu_seconds > 0:
+        from oracle.tpsci import OracleTPSCI
+        O = OracleTPSCI(prob.ops, prob.bases, prob.ham)
+        t5 = time.perf_counter()
+        eo, vo = O.tpsci_ci(start(), thresh_cipsi=1e-3, thresh_foi=1e-5, max_iter=3)
+        t6 = time.perf_counter()
+        f3 = out["first_3_iterations"]
+        f3.update({"oracle_s": t6 - t5, "oracle_configurations": len(vo), "oracle_e0": float(eo[0]),
+                   "gpu_over_oracle_speedup": (t6 - t5) / (t4 - t3), "cores": os.cpu_count(),
+                   "energy_difference": float(abs(eo[0] - e3[0]))})
+    return out
+
+
 def fois_benchmark(steps, warmup, cpu_seconds, thresh=1e-3):
     """build_compressed_1st_order_state of the CMF state of the 32-orbital / 8-cluster x 4 problem
     (local bases of 16 states per sector) at thresh 1e-3: wall time of fcg_bst_fois (planning,
@@ -644,6 +690,10 @@ def main():
         if rank == 0:
             print(json.dumps({"davidson": davidson_benchmark(stored=a.stored)}))
         return
+    if a.tpsci_only:
+        if rank == 0:
+            print(json.dumps({"tpsci": tpsci_benchmark(a.cpu_seconds)}))
+        return
     if a.fois_only:
         if rank == 0:
             print(json.dumps({"bst_fois": fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)}))
@@ -830,6 +880,11 @@ def main():
             out["bst_fois"] = fois_benchmark(max(3, a.steps // 4), a.warmup, a.cpu_seconds)
         except Exception as ex:
             out["bst_fois"] = {"error": str(ex)}
+    if rank == 0 and a.tpsci:
+        try:
+            out["tpsci"] = tpsci_benchmark(a.cpu_seconds)
+        except Exception as ex:
+            out["tpsci"] = {"error": str(ex)}
     if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1

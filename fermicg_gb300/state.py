@@ -197,3 +197,217 @@ def state_from_rows(n_clusters, R, focks, cfgs, coeffs) -> TPSCIstate:
         f = tuple((int(a), int(b)) for a, b in focks[i])
         out.data.setdefault(f, {})[tuple(int(x) for x in cfgs[i])] = np.array(coeffs[i], dtype=np.float64)
     return out
+
+
+# ---- array form of the same vector, for first-order spaces of millions of rows -------------
+
+class SectorRegistry:
+    """Fock sectors of one problem, numbered as first seen, with the mixed-radix key of a
+    configuration: key = sector id * prod(radix) + sum_c cfg_c * prod(radix[:c]), radix_c the
+    largest local dimension of cluster c over all its sectors."""
+
+    def __init__(self, n_clusters: int, radix):
+        self.N = n_clusters
+        self.radix = np.asarray(radix, dtype=np.int64)
+        self.stride = np.concatenate([[1], np.cumprod(self.radix)[:-1]]).astype(np.int64)
+        self.span = int(np.prod(self.radix))
+        self.ids = {}      # fock tuple -> id
+        self.focks = []    # id -> (N, 2) int16
+
+    def sector_ids(self, focks):
+        """ids of the (n, N, 2) int16 Fock rows (new sectors registered in first-row order)."""
+        focks = np.ascontiguousarray(focks, dtype=np.int16).reshape(-1, self.N * 2)
+        if len(focks) == 0:
+            return np.zeros(0, dtype=np.int64)
+        u, first, inv = np.unique(focks.view(np.dtype((np.void, focks.dtype.itemsize * focks.shape[1]))).ravel(),
+                                  return_index=True, return_inverse=True)
+        uid = np.empty(len(u), dtype=np.int64)
+        for j in np.argsort(first, kind="stable"):
+            f = focks[first[j]]
+            t = tuple((int(f[2 * c]), int(f[2 * c + 1])) for c in range(self.N))
+            if t not in self.ids:
+                if (len(self.focks) + 1) * self.span >= (1 << 62):
+                    raise OverflowError("configuration keys exceed 62 bits")
+                self.ids[t] = len(self.focks)
+                self.focks.append(np.asarray(t, dtype=np.int16))
+            uid[j] = self.ids[t]
+        return uid[inv.ravel()]
+
+    def keys(self, sec, cfgs):
+        return sec * self.span + (np.asarray(cfgs, dtype=np.int64) * self.stride).sum(axis=1)
+
+
+class FlatTPSCI:
+    """A TPSCIstate as arrays: sector id, configuration and R coefficients per row, in any
+    physical order, with the bookkeeping that gives TPSCIstate's row order -- sectors in
+    insertion order (a sector that loses its last row is deleted, and goes to the end when
+    it comes back), configurations in insertion order within their sector.  The operations
+    below are those of the TPSCIstate functions of the same names, vectorised."""
+
+    def __init__(self, reg: SectorRegistry, R: int):
+        self.reg, self.R = reg, R
+        self.sec = np.zeros(0, dtype=np.int64)
+        self.cfg = np.zeros((0, reg.N), dtype=np.int16)
+        self.coef = np.zeros((0, R))
+        self.ins = np.zeros(0, dtype=np.int64)   # insertion counter of each row
+        self.rank = {}                           # sector id -> insertion rank of the sector
+        self.next_ins = 0
+        self.next_rank = 0
+        self._key = None
+
+    # -- construction and views ----------------------------------------------------------
+    @staticmethod
+    def from_rows(reg, R, focks, cfgs, coeffs):
+        """Rows in the given order (distinct configurations), as appended to an empty state."""
+        s = FlatTPSCI(reg, R)
+        s._append(reg.sector_ids(focks), np.asarray(cfgs, dtype=np.int16).reshape(-1, reg.N),
+                  np.asarray(coeffs, dtype=np.float64).reshape(-1, R))
+        return s
+
+    @staticmethod
+    def from_state(reg, st: TPSCIstate):
+        f, c, v, _ = st.flat()
+        return FlatTPSCI.from_rows(reg, st.R, f, c, v)
+
+    def to_state(self) -> TPSCIstate:
+        f, c, v = self.rows()
+        return TPSCIstate.from_flat(self.reg.N, f, c, v) if len(f) else TPSCIstate(self.reg.N, self.R)
+
+    def __len__(self):
+        return len(self.sec)
+
+    def key(self):
+        if self._key is None:
+            self._key = self.reg.keys(self.sec, self.cfg)
+        return self._key
+
+    def order(self):
+        """physical rows in TPSCIstate row order"""
+        if len(self.sec) == 0:
+            return np.zeros(0, dtype=np.int64)
+        rank = np.zeros(len(self.reg.focks), dtype=np.int64)
+        for sid, r in self.rank.items():
+            rank[sid] = r
+        return np.lexsort((self.ins, rank[self.sec]))
+
+    def canonicalize(self):
+        """reorder the physical rows into TPSCIstate row order"""
+        o = self.order()
+        self.sec, self.cfg, self.coef, self.ins = self.sec[o], self.cfg[o], self.coef[o], self.ins[o]
+        self._key = None if self._key is None else self._key[o]
+
+    def rows(self):
+        """(focks (n, N, 2) int16, cfgs (n, N) int16, coeffs (n, R)) in row order"""
+        self.canonicalize()
+        focks = np.stack(self.reg.focks)[self.sec] if len(self.sec) else np.zeros((0, self.reg.N, 2), np.int16)
+        return focks, self.cfg.copy(), self.coef.copy()
+
+    def get_vector(self):
+        self.canonicalize()
+        return self.coef.copy()
+
+    def set_vector(self, v):
+        self.canonicalize()
+        v = np.asarray(v, dtype=np.float64).reshape(len(self), -1)
+        if v.shape[1] != self.R:
+            raise ValueError("root count mismatch")
+        self.coef = v.copy()
+
+    # -- bookkeeping -------------------------------------------------------------------------
+    def _append(self, sec, cfg, coef):
+        """new rows (configurations not present), in the given order"""
+        if len(sec) == 0:
+            return
+        u, first = np.unique(sec, return_index=True)
+        for sid in u[np.argsort(first, kind="stable")].tolist():  # sectors that (re)appear, in first-row order
+            if sid not in self.rank:
+                self.rank[sid] = self.next_rank
+                self.next_rank += 1
+        n = len(sec)
+        self.sec = np.concatenate([self.sec, sec])
+        self.cfg = np.concatenate([self.cfg, cfg])
+        self.coef = np.concatenate([self.coef, coef])
+        self.ins = np.concatenate([self.ins, self.next_ins + np.arange(n, dtype=np.int64)])
+        self.next_ins += n
+        self._key = None
+
+    def _keep(self, mask):
+        """keep the rows of mask; sectors left without rows are deleted"""
+        self.sec, self.cfg, self.coef, self.ins = self.sec[mask], self.cfg[mask], self.coef[mask], self.ins[mask]
+        self._key = None if self._key is None else self._key[mask]
+        live = set(np.unique(self.sec).tolist())
+        self.rank = {s: r for s, r in self.rank.items() if s in live}
+
+    def _find(self, keys):
+        """physical row of each key, -1 where absent"""
+        k = self.key()
+        if len(k) == 0:
+            return np.full(len(keys), -1, dtype=np.int64)
+        o = np.argsort(k, kind="stable")
+        ks = k[o]
+        p = np.searchsorted(ks, keys)
+        p = np.minimum(p, len(ks) - 1)
+        hit = ks[p] == keys
+        return np.where(hit, o[p], -1)
+
+    def copy(self):
+        """copy_state (empty sectors are not kept: a state never holds one)"""
+        s = FlatTPSCI(self.reg, self.R)
+        s.sec, s.cfg, s.coef, s.ins = self.sec.copy(), self.cfg.copy(), self.coef.copy(), self.ins.copy()
+        s.rank, s.next_ins, s.next_rank = dict(self.rank), self.next_ins, self.next_rank
+        s._key = None if self._key is None else self._key.copy()
+        return s
+
+    # -- TPSCIstate algebra ------------------------------------------------------------------
+    def zero(self):
+        """zero_state"""
+        self.coef = np.zeros_like(self.coef)
+
+    def scale(self, a: float):
+        self.coef = self.coef * a
+
+    def add(self, other: "FlatTPSCI"):
+        """add_state: self += other, new configurations appended in other's row order"""
+        if len(other) == 0:
+            return
+        o = other.order()
+        keys = other.key()[o]
+        pos = self._find(keys)
+        hit = pos >= 0
+        if hit.any():
+            np.add.at(self.coef, pos[hit], other.coef[o][hit])
+        new = o[~hit]
+        self._append(other.sec[new], other.cfg[new], other.coef[new])
+
+    def times_matrix(self, C) -> "FlatTPSCI":
+        out = self.copy()
+        if len(out):
+            out.coef = self.coef @ np.asarray(C)
+        return out
+
+    def minus(self, B: "FlatTPSCI") -> "FlatTPSCI":
+        """minus_state(self, B) = self - B, in B's row order then self's new rows"""
+        C = B.copy()
+        C.scale(-1.0)
+        C.add(self)
+        return C
+
+    def overlap(self, v2: "FlatTPSCI"):
+        """overlap(self, v2): R x R over the shared configurations"""
+        S = np.zeros((v2.R, v2.R))
+        if len(self) == 0 or len(v2) == 0:
+            return S
+        pos = self._find(v2.key())
+        hit = pos >= 0
+        return self.coef[pos[hit]].T @ v2.coef[hit]
+
+    def project_out(self, w: "FlatTPSCI"):
+        """project_out: drop w's configurations"""
+        if len(self) == 0 or len(w) == 0:
+            return
+        self._keep(w._find(self.key()) < 0)
+
+    def clip(self, thresh: float):
+        """clip: drop configurations with every |c| < thresh"""
+        if len(self):
+            self._keep(~np.all(np.abs(self.coef) < thresh, axis=1))
