@@ -125,7 +125,7 @@ struct fcg_ctx {
   bool have_hcache = false;
   int64_t hc_pairs = 0;
   DevBuf<int64_t> d_hc_prefix;  // pairs before each work item
-  DevBuf<int64_t> d_hc_cta;     // first work item of each cached-sigma CTA
+  DevBuf<int64_t> d_hc_cta32, d_hc_cta64;  // first work item of each cached-sigma CTA (float / double runs)
   DevBuf<double> d_hc64;
   DevBuf<float> d_hc32;
   void drop_hcache() {
@@ -134,7 +134,8 @@ struct fcg_ctx {
     d_hc64.release();
     d_hc32.release();
     d_hc_prefix.release();
-    d_hc_cta.release();
+    d_hc_cta32.release();
+    d_hc_cta64.release();
   }
   // vectors
   DevBuf<double> d_in64, d_out64;  // column-major staging for host calls

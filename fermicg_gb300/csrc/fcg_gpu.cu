@@ -426,9 +426,17 @@ __global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB
 // float64.  A sigma from the cache reads one value per pair instead of recomputing every
 // term's contraction.
 constexpr int kCacheRun = 4;  // pairs per thread of the assembly
-constexpr int kHcRun = 16;    // pairs per thread of the cached sigma
+// pairs per thread of the cached sigma (measured on the 1e5-configuration problem: 32 for
+// float builds, 16 for double builds)
+template <typename T>
+__host__ __device__ constexpr int hc_run() {
+  return sizeof(T) == 4 ? 32 : 16;
+}
 constexpr int64_t kCacheChunk = int64_t(kSigmaThreads) * kCacheRun;
-constexpr int64_t kHcChunk = int64_t(kSigmaThreads) * kHcRun;
+template <typename T>
+__host__ __device__ constexpr int64_t hc_chunk() {
+  return int64_t(kSigmaThreads) * hc_run<T>();
+}
 
 // first pair and pair count of the CTA's chunk; w_lo / w_hi its first and last work item
 __global__ void __launch_bounds__(kSigmaThreads) hcache_build_kernel(SigmaParams p, const int64_t* __restrict__ cta_lo,
@@ -466,13 +474,15 @@ __global__ void __launch_bounds__(kSigmaThreads) hcache_build_kernel(SigmaParams
   }
 }
 
-// sigma[bra] += hc[pair] * C[ket] over the CTA's chunk of pairs: each thread a run of kHcRun
+// sigma[bra] += hc[pair] * C[ket] over the CTA's chunk of pairs: each thread a run of hc_run<T>()
 // consecutive pairs (read with 32-byte loads), contributions to one bra row summed in
 // registers and flushed with one atomic per root when the bra changes.
 template <typename T, int RR, int RMAX = kMaxR>
 __device__ __forceinline__ void cached_sigma_cta(const SigmaParams& p, const T* __restrict__ hc,
                                                  const T* __restrict__ cin, T* __restrict__ sig, int64_t cta) {
   constexpr int RV = RR > 0 ? RR : RMAX;
+  constexpr int kHcRun = hc_run<T>();
+  constexpr int64_t kHcChunk = hc_chunk<T>();
   const int64_t s0 = cta * kHcChunk;
   const int64_t e0 = (s0 + kHcChunk < p.n_pairs) ? s0 + kHcChunk : p.n_pairs;
   __shared__ int64_t s_pre[kPrefixShared];
@@ -496,7 +506,7 @@ __device__ __forceinline__ void cached_sigma_cta(const SigmaParams& p, const T* 
     local = t0 - __ldg(p.hc_prefix + wi);
   }
   T mv[kHcRun];
-  if (n == kHcRun) {  // t0 is a multiple of kHcRun: the run starts on a 64-byte boundary
+  if (n == kHcRun) {  // t0 is a multiple of kHcRun: the run starts on a 64-byte boundary or more
     constexpr int C = Chunk<T>::n;
 #pragma unroll
     for (int c = 0; c < kHcRun / C; ++c) {
@@ -752,7 +762,7 @@ static SigmaParams make_sigma_params(fcg_ctx* ctx, int R) {
   p.R = R;
   if (ctx->have_hcache) {
     p.hc_prefix = ctx->d_hc_prefix.p;
-    p.hc_cta = ctx->d_hc_cta.p;
+    p.hc_cta = nullptr;  // per precision: set by the launch
     p.n_pairs = ctx->hc_pairs;
   }
   return p;
@@ -1073,7 +1083,8 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* 
   int launches = 0;
   if (ctx->have_hcache) {  // from the stored Hamiltonian blocks
     const T* hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(ctx->d_hc32.p) : reinterpret_cast<const T*>(ctx->d_hc64.p);
-    const int64_t grid = (p.n_pairs + kHcChunk - 1) / kHcChunk;
+    p.hc_cta = sizeof(T) == 4 ? ctx->d_hc_cta32.p : ctx->d_hc_cta64.p;
+    const int64_t grid = (p.n_pairs + hc_chunk<T>() - 1) / hc_chunk<T>();
     FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
     if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     if (grid > 0) {
@@ -1187,12 +1198,14 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
     for (int64_t c = 0; c < n_cta; ++c)
       out[c] = int64_t(std::upper_bound(pre.begin(), pre.begin() + n_items, c * chunk) - pre.begin()) - 1;
   };
-  std::vector<int64_t> lo_build, lo_sigma;
+  std::vector<int64_t> lo_build, lo_sigma32, lo_sigma64;
   cta_items(kCacheChunk, lo_build);
-  cta_items(kHcChunk, lo_sigma);
+  cta_items(hc_chunk<float>(), lo_sigma32);
+  cta_items(hc_chunk<double>(), lo_sigma64);
   FCG_REQUIRE(lo_build.size() < (size_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
   FCG_CUDA(ctx->d_hc_prefix.upload(pre.data(), pre.size(), ctx->stream));
-  FCG_CUDA(ctx->d_hc_cta.upload(lo_sigma.data(), lo_sigma.size(), ctx->stream));
+  FCG_CUDA(ctx->d_hc_cta32.upload(lo_sigma32.data(), lo_sigma32.size(), ctx->stream));
+  FCG_CUDA(ctx->d_hc_cta64.upload(lo_sigma64.data(), lo_sigma64.size(), ctx->stream));
   DevBuf<int64_t> d_lo;
   FCG_CUDA(d_lo.upload(lo_build.data(), lo_build.size(), ctx->stream));
   FCG_CUDA(ctx->d_hc64.alloc(size_t(std::max<int64_t>(pairs, 1))));
@@ -1200,7 +1213,7 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
   if (pairs > 0) {
     SigmaParams p = make_sigma_params(ctx, 1);
     p.hc_prefix = ctx->d_hc_prefix.p;
-    p.hc_cta = ctx->d_hc_cta.p;
+    p.hc_cta = nullptr;  // the assembly walks its own chunks (cta_lo)
     p.n_pairs = pairs;
     hcache_build_kernel<<<unsigned(lo_build.size() - 1), kSigmaThreads, 0, ctx->stream>>>(
         p, d_lo.p, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
@@ -1257,7 +1270,8 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
     if (c->have_hcache) {
       e.hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(c->d_hc32.p) : reinterpret_cast<const T*>(c->d_hc64.p);
       e.cta0 = cta_hc;
-      const int64_t n_cta = (e.p.n_pairs + kHcChunk - 1) / kHcChunk;
+      e.p.hc_cta = sizeof(T) == 4 ? c->d_hc_cta32.p : c->d_hc_cta64.p;
+      const int64_t n_cta = (e.p.n_pairs + hc_chunk<T>() - 1) / hc_chunk<T>();
       FCG_REQUIRE(cta_hc + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
       cta_problem_hc.insert(cta_problem_hc.end(), size_t(n_cta), int32_t(q));
       cta_hc += n_cta;
