@@ -436,10 +436,16 @@ struct DavidsonWork {
   int row_blocks = 1;             // Gram products: row blocks, rows per block
   int64_t rows_per_block = 1;
   int res_blocks = 1;             // residual kernel blocks
-  DevBuf<double> V, AV, X, tmp, hd, part, rn_part, d_out, d_up;
-  DevBuf<unsigned> counters;  // last-block tickets: [0, ngroups) Gram column groups, [ngroups] residual
+  // views of the context's grow-only buffers (fcg_ctx::dav_*), sized by init
+  template <class T>
+  struct Span {
+    T* p = nullptr;
+    size_t n = 0;
+  };
+  Span<double> V, AV, X, tmp, hd, part, rn_part, d_out, d_up;
+  Span<unsigned> counters;  // last-block tickets: [0, ngroups) Gram column groups, [ngroups] residual
   int ngroups = 1;
-  PinnedBuf<double> h_out, h_up;
+  Span<double> h_out, h_up;
   size_t up_used = 0, up_sent = 0;
   size_t up_cap = 0, out_cap = 0;  // doubles staged between two waits; fetched values
   double* hout = nullptr;          // the fetched values (h_out, or hout_vec in grouped mode)
@@ -887,26 +893,33 @@ struct DavidsonRun {
     W.row_blocks = int(std::max<int64_t>(1, std::min<int64_t>(kMaxRowBlocks, (n + kGramRows - 1) / kGramRows)));
     W.rows_per_block = (n + W.row_blocks - 1) / W.row_blocks;
     W.res_blocks = int((n + kDavThreads - 1) / kDavThreads);
-    FCG_CUDA(W.V.alloc(size_t(n) * kcap));
-    FCG_CUDA(W.AV.alloc(size_t(n) * kcap));
-    FCG_CUDA(W.X.alloc(size_t(n) * R));
-    FCG_CUDA(W.tmp.alloc(size_t(n) * std::min(kmax, 2 * R)));
-    FCG_CUDA(W.hd.alloc(n));
-    FCG_CUDA(W.part.alloc(size_t(W.row_blocks) * kcap * R));
-    FCG_CUDA(W.rn_part.alloc(size_t(W.res_blocks) * R));
+    // the context's buffers grow to this solve's sizes and stay for its later solves
+    auto take = [](auto& buf, auto& span, size_t count) {
+      const cudaError_t e = buf.alloc(count);
+      span.p = buf.p;
+      span.n = count;
+      return e;
+    };
+    FCG_CUDA(take(ctx->dav_V, W.V, size_t(n) * kcap));
+    FCG_CUDA(take(ctx->dav_AV, W.AV, size_t(n) * kcap));
+    FCG_CUDA(take(ctx->dav_X, W.X, size_t(n) * R));
+    FCG_CUDA(take(ctx->dav_tmp, W.tmp, size_t(n) * std::min(kmax, 2 * R)));
+    FCG_CUDA(take(ctx->dav_hd, W.hd, size_t(n)));
+    FCG_CUDA(take(ctx->dav_part, W.part, size_t(W.row_blocks) * kcap * R));
+    FCG_CUDA(take(ctx->dav_rn, W.rn_part, size_t(W.res_blocks) * R));
     W.ngroups = (kcap + 31) / 32;
-    FCG_CUDA(W.counters.alloc(size_t(W.ngroups) + 1));
+    FCG_CUDA(take(ctx->dav_counters, W.counters, size_t(W.ngroups) + 1));
     FCG_CUDA(cudaMemsetAsync(W.counters.p, 0, sizeof(unsigned) * (W.ngroups + 1), ctx->stream));
     W.out_cap = size_t(R) + size_t(kcap) * R + 16;
     W.up_cap = size_t(4) * (size_t(kcap) * 2 * R + size_t(R) * R + 64);
-    FCG_CUDA(W.d_out.alloc(W.out_cap));
+    FCG_CUDA(take(ctx->dav_out, W.d_out, W.out_cap));
     if (grouped) {
       W.hout_vec.assign(W.out_cap, 0.0);
       W.hout = W.hout_vec.data();
     } else {
-      FCG_CUDA(W.h_out.alloc(W.out_cap));
-      FCG_CUDA(W.d_up.alloc(W.up_cap));
-      FCG_CUDA(W.h_up.alloc(W.up_cap));
+      FCG_CUDA(take(ctx->dav_h_out, W.h_out, W.out_cap));
+      FCG_CUDA(take(ctx->dav_up, W.d_up, W.up_cap));
+      FCG_CUDA(take(ctx->dav_h_up, W.h_up, W.up_cap));
       W.hout = W.h_out.p;
     }
     if (precond) {

@@ -128,15 +128,22 @@ struct fcg_ctx {
   DevBuf<int64_t> d_hc_cta32, d_hc_cta64;  // first work item of each cached-sigma CTA (float / double runs)
   DevBuf<double> d_hc64;
   DevBuf<float> d_hc32;
-  void drop_hcache() {
+  // release = false keeps the buffers for the next state's blocks (grow-only; a cudaFree
+  // would wait for every stream of the device)
+  void drop_hcache(bool release = false) {
     have_hcache = false;
     hc_pairs = 0;
+    if (!release) return;
     d_hc64.release();
     d_hc32.release();
     d_hc_prefix.release();
     d_hc_cta32.release();
     d_hc_cta64.release();
   }
+  // Davidson working buffers of this context, grow-only and reused by its later solves
+  DevBuf<double> dav_V, dav_AV, dav_X, dav_tmp, dav_hd, dav_part, dav_rn, dav_out, dav_up;
+  DevBuf<unsigned> dav_counters;
+  PinnedBuf<double> dav_h_out, dav_h_up;
   // vectors
   DevBuf<double> d_in64, d_out64;  // column-major staging for host calls
   DevBuf<double> d_c64, d_s64;     // row-major fp64

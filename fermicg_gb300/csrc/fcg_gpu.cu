@@ -1174,7 +1174,7 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
   FCG_CUDA(cudaSetDevice(ctx->device));
   const auto t0 = std::chrono::steady_clock::now();
-  ctx->drop_hcache();
+  ctx->drop_hcache(!(max_bytes > 0));  // an explicit drop returns the memory
   ctx->stats.hcache_pairs = 0;
   ctx->stats.hcache_bytes = 0;
   ctx->stats.hcache_seconds = 0.0;

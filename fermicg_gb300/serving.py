@@ -105,8 +105,8 @@ class SolveServer:
             with self._lock:
                 self.results.append(Result(req.rid, req.shape, e, res, it, req.arrival, start, end))
         finally:
-            if extra:
-                g.cache_hamiltonian(0)
+            # the pooled context keeps the stored blocks' buffers for its next request (the next
+            # state invalidates them; freeing would wait for every stream of the device)
             with self._lock:
                 self._in_use -= fp + extra
                 self._active -= 1
@@ -230,9 +230,7 @@ class NativeSolveServer:
             with self._lock:
                 self.results.append(Result(req.rid, req.shape, e, res, it.value, req.arrival, start, end))
         finally:
-            if req.cache:
-                g.cache_hamiltonian(0)  # a pooled context keeps no stored blocks between requests
-            with self._lock:
+            with self._lock:  # the pooled context keeps its buffers for the next request
                 self._free.append(g)
 
     def run(self, requests: list[Request], t0: float | None = None):

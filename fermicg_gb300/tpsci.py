@@ -56,7 +56,6 @@ class GpuTPSCI:
                 pass
         e, X, res, it = self.H.davidson(v, max_iter=max_iter, max_ss_vecs=max_ss_vecs, tol=tol, lindep=lindep,
                                         precision=self.precision)
-        self.H.cache_hamiltonian(0)
         out = fs.copy()
         out.set_vector(X)
         return e, (out if isinstance(s, FlatTPSCI) else out.to_state()), res

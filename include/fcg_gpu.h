@@ -210,7 +210,10 @@ int fcg_wait(fcg_server* s, int64_t ticket, int timeout_ms, double* energies, do
  * direct build up to the order of the additions; float32 results are closer to float64
  * than the direct float32 build (the term sums are rounded once).  The blocks take 12 bytes
  * per pair: *bytes returns the need; FCG_ELIMIT (nothing stored) when it exceeds max_bytes.
- * max_bytes <= 0 drops them.  fcg_set_ops, fcg_set_terms and fcg_state_set drop them too. */
+ * max_bytes <= 0 drops them and frees their memory.  fcg_set_ops, fcg_set_terms and
+ * fcg_state_set drop them too but keep the memory for the context's next stored blocks.
+ * The Davidson working buffers of a context likewise stay allocated for its next solve
+ * (a freed buffer would make the call wait for every stream of the device). */
 int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes);
 
 int fcg_get_stats(const fcg_ctx* ctx, fcg_stats* out);
