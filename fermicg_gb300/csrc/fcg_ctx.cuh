@@ -140,6 +140,14 @@ struct fcg_ctx {
     d_hc_cta32.release();
     d_hc_cta64.release();
   }
+  // job lists of the set-up calls (fcg_set_ops, fcg_set_terms, fcg_cache_hamiltonian), grow-only
+  DevBuf<unsigned char> scratch_a, scratch_b;
+  template <class T>
+  static cudaError_t stage(DevBuf<unsigned char>& buf, const T* h, size_t count, cudaStream_t s, T** d) {
+    const cudaError_t e = buf.upload(reinterpret_cast<const unsigned char*>(h), count * sizeof(T), s);
+    *d = reinterpret_cast<T*>(buf.p);
+    return e;
+  }
   // Davidson working buffers of this context, grow-only and reused by its later solves
   DevBuf<double> dav_V, dav_AV, dav_X, dav_tmp, dav_hd, dav_part, dav_rn, dav_out, dav_up;
   DevBuf<unsigned> dav_counters;

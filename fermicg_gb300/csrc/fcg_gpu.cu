@@ -882,11 +882,11 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
       ctx->gmax_off[b] = tot;
       tot += int64_t(B.nidx) * B.mk;
     }
-    DevBuf<MaxJob> d_mj;
-    FCG_CUDA(d_mj.upload(mj.data(), mj.size(), ctx->stream));
+    MaxJob* d_mj = nullptr;
+    FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, mj.data(), mj.size(), ctx->stream, &d_mj));
     FCG_CUDA(ctx->d_gmax.alloc(std::max<int64_t>(tot, 1)));
     if (n_blocks > 0) {
-      colmax_kernel<<<unsigned(n_blocks), 128, 0, ctx->stream>>>(d_mj.p, ctx->d_op64.p, ctx->d_gmax.p);
+      colmax_kernel<<<unsigned(n_blocks), 128, 0, ctx->stream>>>(d_mj, ctx->d_op64.p, ctx->d_gmax.p);
       FCG_CUDA(cudaGetLastError());
     }
     FCG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -960,12 +960,12 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   FCG_CUDA(ctx->d_terms.upload(ctx->terms.data(), ctx->terms.size(), ctx->stream));
   FCG_CUDA(ctx->d_ints64.upload(ints, n_ints, ctx->stream));
   FCG_CUDA(ctx->d_ints32.upload(i32.data(), n_ints, ctx->stream));
-  DevBuf<DressJob> d_jobs;
-  FCG_CUDA(d_jobs.upload(jobs.data(), jobs.size(), ctx->stream));
+  DressJob* d_jobs = nullptr;
+  FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, jobs.data(), jobs.size(), ctx->stream, &d_jobs));
   FCG_CUDA(ctx->d_w64.alloc(std::max<int64_t>(w_total, 1)));
   FCG_CUDA(ctx->d_w32.alloc(std::max<int64_t>(w_total, 1)));
   if (!jobs.empty()) {
-    dress_kernel<<<unsigned(jobs.size()), 256, 0, ctx->stream>>>(d_jobs.p, ctx->d_op64.p, ctx->d_ints64.p,
+    dress_kernel<<<unsigned(jobs.size()), 256, 0, ctx->stream>>>(d_jobs, ctx->d_op64.p, ctx->d_ints64.p,
                                                                  ctx->d_w64.p);
     FCG_CUDA(cudaGetLastError());
     to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
@@ -988,14 +988,14 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
                                  [](const DressJob& J, int64_t v) { return J.w_off < v; });
       ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
     }
-    DevBuf<MaxJob> d_mj;
-    FCG_CUDA(d_mj.upload(mj.data(), mj.size(), ctx->stream));
+    MaxJob* d_mj = nullptr;
+    FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, mj.data(), mj.size(), ctx->stream, &d_mj));
     FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
     if (!jobs.empty()) {
-      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj.p, ctx->d_w64.p, ctx->d_wmax.p);
+      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj, ctx->d_w64.p, ctx->d_wmax.p);
       FCG_CUDA(cudaGetLastError());
     }
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // before d_mj / d_jobs are freed
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job lists are reused by the next call
   }
   ctx->have_terms = true;
   return FCG_OK;
@@ -1206,8 +1206,8 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
   FCG_CUDA(ctx->d_hc_prefix.upload(pre.data(), pre.size(), ctx->stream));
   FCG_CUDA(ctx->d_hc_cta32.upload(lo_sigma32.data(), lo_sigma32.size(), ctx->stream));
   FCG_CUDA(ctx->d_hc_cta64.upload(lo_sigma64.data(), lo_sigma64.size(), ctx->stream));
-  DevBuf<int64_t> d_lo;
-  FCG_CUDA(d_lo.upload(lo_build.data(), lo_build.size(), ctx->stream));
+  int64_t* d_lo = nullptr;
+  FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, lo_build.data(), lo_build.size(), ctx->stream, &d_lo));
   FCG_CUDA(ctx->d_hc64.alloc(size_t(std::max<int64_t>(pairs, 1))));
   FCG_CUDA(ctx->d_hc32.alloc(size_t(std::max<int64_t>(pairs, 1))));
   if (pairs > 0) {
@@ -1216,7 +1216,7 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
     p.hc_cta = nullptr;  // the assembly walks its own chunks (cta_lo)
     p.n_pairs = pairs;
     hcache_build_kernel<<<unsigned(lo_build.size() - 1), kSigmaThreads, 0, ctx->stream>>>(
-        p, d_lo.p, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
+        p, d_lo, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
     FCG_CUDA(cudaGetLastError());
     to_float_kernel<<<unsigned(std::min<int64_t>((pairs + 255) / 256, 65535)), 256, 0, ctx->stream>>>(
         ctx->d_hc64.p, ctx->d_hc32.p, pairs);
