@@ -443,8 +443,14 @@ def batched_benchmark(steps, warmup, n_inst=256, stored=True):
             res = davidson_grouped(gs, guesses, tol=tol, max_iter=200, precision=prec)
             grouped_s = time.perf_counter() - t1
             st = gs[0].stats()
+            from concurrent.futures import ThreadPoolExecutor
+            t1 = time.perf_counter()
+            with ThreadPoolExecutor(16) as ex:
+                list(ex.map(lambda a: a[0].davidson(a[1], tol=tol, max_iter=200, precision=prec), zip(gs, guesses)))
+            conc_s = time.perf_counter() - t1
             blk["solves_mixed" if prec == "fp32" else "solves_fp64"] = {
                 "grouped_s": grouped_s, "solves_per_s_grouped": n_inst / grouped_s,
+                "concurrent_16_threads_s": conc_s, "grouped_over_concurrent": conc_s / grouped_s,
                 "solves_per_s_with_assembly": n_inst / (grouped_s + hc_s),
                 "grouped_phases_s": {k[6:]: st[k] for k in ("group_step_seconds", "group_issue_seconds",
                                                              "group_wait_seconds")},

@@ -1716,46 +1716,95 @@ extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, c
   if (n == 1)
     return fcg_davidson(ctx, R[0], v0[0], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[0],
                         vectors[0], residuals[0], &iters[0]);
-  // every problem's work goes to the leader's stream while the group is solved
+  // Lanes: interleaved subsets of the problems, each solved in lockstep on its first
+  // problem's stream by a host thread of its own, so that one lane's host work overlaps the
+  // others' device work (one lane below 64 problems).
+  const int lanes = std::max(1, std::min(4, n / 32));
+  struct LaneOut {
+    int rc = FCG_OK;
+    int64_t bad = -1;  // failing problem, -1 for a failure of the lane's stream
+    std::string err;
+    int64_t rounds = 0, launches = 0;
+    double setup = 0, step = 0, issue = 0, wait = 0;
+  };
+  std::vector<LaneOut> out(static_cast<size_t>(lanes));
   std::vector<cudaStream_t> saved(n);
-  for (int q = 0; q < n; ++q) {
-    saved[q] = ctxs[q]->stream;
-    ctxs[q]->stream = ctx->stream;
-  }
-  int rc = FCG_OK;
-  {
-    std::vector<std::unique_ptr<DavidsonRun>> runs;
-    Lockstep L(ctx->stream, step_helpers(1));
-    const auto t0 = std::chrono::steady_clock::now();
-    for (int q = 0; q < n && rc == FCG_OK; ++q) {
-      runs.emplace_back(new DavidsonRun());
-      rc = runs[q]->init(ctxs[q], R[q], v0[q], max_iter, max_ss_vecs, tol, lindep, precision, precond, energies[q],
-                         vectors[q], residuals[q], &iters[q], true);
-      if (rc && q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
-      if (rc == FCG_OK && (rc = L.add(runs[q].get()))) ctx->err = L.err;
-    }
-    const double setup_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-    while (rc == FCG_OK && L.running()) {
-      if ((rc = L.round())) {
-        ctx->err = L.err;
-        break;
+  for (int q = 0; q < n; ++q) saved[q] = ctxs[q]->stream;
+  auto run_lane = [&](int l) {
+    LaneOut& o = out[size_t(l)];
+    cudaSetDevice(ctx->device);
+    std::vector<int> mem;
+    for (int q = l; q < n; q += lanes) mem.push_back(q);
+    const cudaStream_t stream = saved[mem[0]];
+    for (int q : mem) ctxs[q]->stream = stream;  // the lane's work on its first problem's stream
+    {
+      std::vector<std::unique_ptr<DavidsonRun>> runs;
+      Lockstep L(stream, step_helpers(lanes));
+      const auto t0 = std::chrono::steady_clock::now();
+      for (size_t i = 0; i < mem.size() && o.rc == FCG_OK; ++i) {
+        const int q = mem[i];
+        runs.emplace_back(new DavidsonRun());
+        o.rc = runs[i]->init(ctxs[q], R[q], v0[q], max_iter, max_ss_vecs, tol, lindep, precision, precond,
+                             energies[q], vectors[q], residuals[q], &iters[q], true);
+        if (o.rc) {
+          o.bad = q;
+          o.err = ctxs[q]->err;
+        } else if ((o.rc = L.add(runs[i].get()))) {
+          o.bad = q;
+          o.err = L.err;
+        }
       }
-      for (int q = 0; q < n; ++q)
-        if (L.entries[q].state == Lockstep::kFailed) {
-          rc = L.entries[q].rc;
-          if (q > 0) ctx->err = ctxs[q]->err + " (problem " + std::to_string(q) + ")";
+      o.setup = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+      while (o.rc == FCG_OK && L.running()) {
+        if ((o.rc = L.round())) {
+          o.bad = -1;
+          o.err = L.err;
           break;
         }
+        for (size_t i = 0; i < L.entries.size(); ++i)
+          if (L.entries[i].state == Lockstep::kFailed) {
+            o.rc = L.entries[i].rc;
+            o.bad = mem[i];
+            o.err = ctxs[mem[i]]->err;
+            break;
+          }
+      }
+      cudaStreamSynchronize(stream);  // nothing of the lane in flight when its runs go
+      o.rounds = L.rounds;
+      o.launches = L.launches;
+      o.step = L.step_s;
+      o.issue = L.issue_s;
+      o.wait = L.wait_s;
     }
-    cudaStreamSynchronize(ctx->stream);  // nothing of the group in flight when the runs go
-    ctx->stats.group_rounds = L.rounds;
-    ctx->stats.group_launches = L.launches;
-    ctx->stats.group_setup_seconds = setup_s;
-    ctx->stats.group_step_seconds = L.step_s;
-    ctx->stats.group_issue_seconds = L.issue_s;
-    ctx->stats.group_wait_seconds = L.wait_s;
+    for (int q : mem) ctxs[q]->stream = saved[q];
+  };
+  {
+    std::vector<std::thread> pool;
+    for (int l = 1; l < lanes; ++l) pool.emplace_back(run_lane, l);
+    run_lane(0);
+    for (auto& t : pool) t.join();
   }
-  for (int q = 0; q < n; ++q) ctxs[q]->stream = saved[q];
+  // the failure of the lowest problem (a stream failure first), named as one group would
+  int rc = FCG_OK;
+  int64_t first = n;
+  for (const LaneOut& o : out)
+    if (o.rc != FCG_OK && o.bad < first) {
+      rc = o.rc;
+      first = o.bad;
+      ctx->err = o.bad > 0 ? o.err + " (problem " + std::to_string(o.bad) + ")" : o.err;
+    }
+  ctx->stats.group_rounds = 0;
+  ctx->stats.group_launches = 0;
+  ctx->stats.group_setup_seconds = ctx->stats.group_step_seconds = 0.0;
+  ctx->stats.group_issue_seconds = ctx->stats.group_wait_seconds = 0.0;
+  for (const LaneOut& o : out) {  // lanes run side by side: the longest of each
+    ctx->stats.group_rounds = std::max(ctx->stats.group_rounds, o.rounds);
+    ctx->stats.group_launches += o.launches;
+    ctx->stats.group_setup_seconds = std::max(ctx->stats.group_setup_seconds, o.setup);
+    ctx->stats.group_step_seconds = std::max(ctx->stats.group_step_seconds, o.step);
+    ctx->stats.group_issue_seconds = std::max(ctx->stats.group_issue_seconds, o.issue);
+    ctx->stats.group_wait_seconds = std::max(ctx->stats.group_wait_seconds, o.wait);
+  }
   return rc;
 }
 

@@ -72,8 +72,8 @@ typedef struct fcg_stats {
   double bst_plan_seconds;  /* of which host planning (triples, groups, cache layout) */
   int64_t bst_fois_items;   /* (term, ket block, target TuckerConfig) contributions of the last fcg_bst_fois */
   double bst_fois_seconds;  /* wall time of the last fcg_bst_fois */
-  int64_t group_rounds;     /* lockstep rounds of the last fcg_davidson_grouped (first context) */
-  int64_t group_launches;   /* kernels those rounds launched (grouped sigma: 3) */
+  int64_t group_rounds;     /* lockstep rounds of the last fcg_davidson_grouped (first context; longest lane) */
+  int64_t group_launches;   /* kernels those rounds launched, all lanes (grouped sigma: 3) */
   double group_setup_seconds; /* its problems' set-up: buffers, diagonals, guesses */
   double group_step_seconds;  /* host work of the rounds (problems stepped in parallel) */
   double group_issue_seconds; /* descriptors, copies and launches of the rounds */
@@ -157,12 +157,15 @@ int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss
                  int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
 /* The Davidson solves of n independent problems (one context each, state set) in lockstep:
- * every problem runs fcg_davidson's algorithm on the first context's stream.  In each round
+ * every problem runs fcg_davidson's algorithm on its lane's stream (below).  In each round
  * every problem advances to its next need of the device (host work on a thread pool); then
  * all their Gram products, Ritz/residual passes, orthonormalisation and restart updates run
  * as one launch per kernel and block width and step, the fetched values come back in one
  * copy, the sigma builds of their new blocks run as one grouped launch
- * (fcg_sigma_closed_grouped) per precision, and the round ends with one wait.  The reference solves independent
+ * (fcg_sigma_closed_grouped) per precision, and the round ends with one wait.  From 64
+ * problems on, the problems are dealt round-robin to up to 4 lanes, each a lockstep group on
+ * its first problem's stream with a host thread of its own, so that lanes overlap one
+ * another's host and device work.  The reference solves independent
  * problems one after another (tps_ci_davidson, src/tpsci_outer.jl:364-454, per problem).
  * Per problem q: R[q] roots, v0[q] / vectors[q] host column-major n_cfg_q x R[q],
  * energies[q], residuals[q], iters[q]; the settings are shared.  All contexts on one device
