@@ -9,7 +9,7 @@ from helpers import small_full, config1_subspace, packed, rel_err
 
 pytestmark = pytest.mark.gpu
 
-FP64_TOL = 1e-10   # relative, FP64 sigma (spec parity bar)
+FP64_TOL = 1e-10   # relative, FP64 sigma (the parity bar for float64 builds)
 FP32_TOL = 2e-5    # relative, mixed (FP32 contraction + FP32 accumulation)
 
 
