@@ -73,3 +73,33 @@ def test_rows_of_new_sectors_keep_their_first_appearance_order():
     for r in rows:
         st[r] = np.ones(1)
     _same(s, st)
+
+
+def test_empty_states_and_round_trip():
+    reg = SectorRegistry(N, [5, 5, 5])
+    empty = FlatTPSCI(reg, R)
+    other = FlatTPSCI.from_state(reg, _random_state(np.random.default_rng(3), 30))
+    assert len(empty) == 0 and empty.get_vector().shape == (0, R)
+    np.testing.assert_array_equal(empty.overlap(other), np.zeros((R, R)))
+    np.testing.assert_array_equal(other.overlap(empty), np.zeros((R, R)))
+    e2 = empty.copy()
+    e2.project_out(other)
+    e2.clip(1.0)
+    assert len(e2) == 0 and len(empty.times_matrix(np.eye(R))) == 0
+    # adding into an empty state keeps the added state's row order
+    e2.add(other)
+    st = other.to_state()
+    _same(e2, st)
+    # TPSCIstate -> FlatTPSCI -> TPSCIstate keeps configurations, values and order
+    back = FlatTPSCI.from_state(reg, st).to_state()
+    f1, c1, v1, _ = back.flat()
+    f2, c2, v2, _ = st.flat()
+    assert np.array_equal(f1, f2) and np.array_equal(c1, c2) and np.array_equal(v1, v2)
+
+
+def test_keys_refuse_to_overflow():
+    import pytest
+    reg = SectorRegistry(2, [1 << 30, 1 << 30])  # 2^60 configurations per sector: 4 sectors fit in 2^62
+    focks = np.array([[[a, 0], [0, 0]] for a in range(6)], dtype=np.int16)
+    with pytest.raises(OverflowError):
+        reg.sector_ids(focks)
