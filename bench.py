@@ -870,6 +870,12 @@ def main():
         "clocks": clocks,
     }
     if stored is not None:
+        # the stored-block kernel's own roofline: algorithmic bytes (stored float32 values, C,
+        # sigma, work items) per launch over its CUDA-event time, of the measured HBM copy peak
+        stored["roofline"] = {"bound": "hbm", "achieved": stored["hbm_gbs_fp32"], "peak": hbm_peak, "unit": "GB/s",
+                              "frac": stored["hbm_gbs_fp32"] / hbm_peak,
+                              "note": "cached_sigma_kernel<float>; bound by the L1 data pipe (ket and C-row "
+                                      "gathers), not HBM"}
         out["stored_blocks"] = stored
     if rank == 0 and a.serving:
         try:
