@@ -75,3 +75,30 @@ def test_a_failing_problem_is_named_and_the_contexts_stay_usable():
     assert np.abs(res[1][0] - probs[2][2]).max() < 1e-9
     for g in gpus:
         g.close()
+
+
+def test_lanes_of_a_large_group_equal_solo_solves():
+    """64 problems: the group runs as two lanes (a stream and host thread each); every
+    problem's energies equal its solve alone, with and without stored blocks."""
+    gpus, guesses = [], []
+    for i in range(64):
+        prob, st = workloads.config3_instance(i, max_cluster=4, n_cfg_range=(150, 400))
+        f, c, v, _ = pack.pack_state(st)
+        g = GpuSigma(0)
+        g.set_ops(pack.pack_ops(prob.ops, prob.bases))
+        g.set_terms(pack.pack_terms(prob.ham))
+        g.state_set(f, c)
+        R = v.shape[1]
+        gpus.append(g)
+        guesses.append(workloads.davidson_guess(f.shape[0], R, seed=100 + i, lowest=np.argsort(g.diagonal())[:R]))
+    for stored in (False, True):
+        if stored:
+            for g in gpus:
+                g.cache_hamiltonian()
+        res = davidson_grouped(gpus, guesses, tol=1e-7, max_iter=300, precision="fp32")
+        assert gpus[0].stats()["group_launches"] > 0
+        for g, gu, (e, X, r, it) in zip(gpus, guesses, res):
+            e1, X1, r1, it1 = g.davidson(gu, tol=1e-7, max_iter=300, precision="fp32")
+            assert r.max() < 1e-7 and np.abs(e - e1).max() < 1e-9
+    for g in gpus:
+        g.close()
