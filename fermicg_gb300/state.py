@@ -219,8 +219,14 @@ class SectorRegistry:
         focks = np.ascontiguousarray(focks, dtype=np.int16).reshape(-1, self.N * 2)
         if len(focks) == 0:
             return np.zeros(0, dtype=np.int64)
-        u, first, inv = np.unique(focks.view(np.dtype((np.void, focks.dtype.itemsize * focks.shape[1]))).ravel(),
-                                  return_index=True, return_inverse=True)
+        if self.N <= 8 and focks.min() >= 0 and focks.max() <= 15:  # 4 bits per entry: one uint64 per row
+            packed = np.zeros(len(focks), dtype=np.uint64)
+            for j in range(2 * self.N):
+                packed |= focks[:, j].astype(np.uint64) << np.uint64(4 * j)
+            u, first, inv = np.unique(packed, return_index=True, return_inverse=True)
+        else:
+            u, first, inv = np.unique(focks.view(np.dtype((np.void, focks.dtype.itemsize * focks.shape[1]))).ravel(),
+                                      return_index=True, return_inverse=True)
         uid = np.empty(len(u), dtype=np.int64)
         for j in np.argsort(first, kind="stable"):
             f = focks[first[j]]
@@ -254,6 +260,7 @@ class FlatTPSCI:
         self.next_ins = 0
         self.next_rank = 0
         self._key = None
+        self._canon = True  # the physical rows are in TPSCIstate row order
 
     # -- construction and views ----------------------------------------------------------
     @staticmethod
@@ -288,13 +295,18 @@ class FlatTPSCI:
         rank = np.zeros(len(self.reg.focks), dtype=np.int64)
         for sid, r in self.rank.items():
             rank[sid] = r
+        if len(self.ins) == 0 or int(self.ins.max()) < (1 << 40):  # one sort key: rank, then insertion
+            return np.argsort((rank[self.sec] << 40) | self.ins, kind="stable")
         return np.lexsort((self.ins, rank[self.sec]))
 
     def canonicalize(self):
         """reorder the physical rows into TPSCIstate row order"""
+        if self._canon:
+            return
         o = self.order()
         self.sec, self.cfg, self.coef, self.ins = self.sec[o], self.cfg[o], self.coef[o], self.ins[o]
         self._key = None if self._key is None else self._key[o]
+        self._canon = True
 
     def rows(self):
         """(focks (n, N, 2) int16, cfgs (n, N) int16, coeffs (n, R)) in row order"""
@@ -324,6 +336,7 @@ class FlatTPSCI:
                 self.rank[sid] = self.next_rank
                 self.next_rank += 1
         n = len(sec)
+        self._canon = False  # new rows go to the end physically; row order is restored on demand
         self.sec = np.concatenate([self.sec, sec])
         self.cfg = np.concatenate([self.cfg, cfg])
         self.coef = np.concatenate([self.coef, coef])
@@ -356,6 +369,7 @@ class FlatTPSCI:
         s.sec, s.cfg, s.coef, s.ins = self.sec.copy(), self.cfg.copy(), self.coef.copy(), self.ins.copy()
         s.rank, s.next_ins, s.next_rank = dict(self.rank), self.next_ins, self.next_rank
         s._key = None if self._key is None else self._key.copy()
+        s._canon = self._canon
         return s
 
     # -- TPSCIstate algebra ------------------------------------------------------------------
@@ -374,8 +388,8 @@ class FlatTPSCI:
         keys = other.key()[o]
         pos = self._find(keys)
         hit = pos >= 0
-        if hit.any():
-            np.add.at(self.coef, pos[hit], other.coef[o][hit])
+        if hit.any():  # distinct rows (other's keys are distinct)
+            self.coef[pos[hit]] += other.coef[o][hit]
         new = o[~hit]
         self._append(other.sec[new], other.cfg[new], other.coef[new])
 
