@@ -65,6 +65,12 @@ def parse():
     return ap.parse_args()
 
 
+def bench_config(n_cfg, R, world):
+    """The workload description both arms print (identical dicts for the same workload)."""
+    return {"workload": WORKLOAD, "n_cfg": int(n_cfg), "roots": int(R), "parallelism": f"replicas{world}",
+            "l2": "flushed (256 MiB write) before every timed GPU step"}
+
+
 def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
 
@@ -94,7 +100,8 @@ def build_workload(n_cfg, R):
 def cpu_reference(po, pt, f, c, v, budget_s, threads):
     """Time the oracle's tps_ci_matvec restatement (all host threads): a 1/16 row sample
     first; the full build when it fits the budget, else a larger evenly spaced sample.
-    Returns (sigma builds/s for the full space, description of what was timed)."""
+    Returns (sigma builds/s for the full space, description of what was timed, the full
+    sigma (n_cfg, R) when the whole build ran, else None)."""
     import oracle
     O = oracle.Oracle(po, pt)
     n = f.shape[0]
@@ -112,11 +119,19 @@ def cpu_reference(po, pt, f, c, v, budget_s, threads):
     dt, done = run(16, 1.0 / 16)
     est_full = dt * n / done
     if est_full < budget_s:
-        dt, done = run(1, 1.0)
-        return 1.0 / dt, f"full build, all {n} bra rows, {dt:.2f} s"
+        sig, dt = cpu_full_build(O, f, c, v, threads)
+        return 1.0 / dt, f"full build, all {n} bra rows, {dt:.2f} s", sig
     frac = min(1.0, budget_s / est_full)
     dt, done = run(16, frac)
-    return done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full build"
+    return (done / (dt * n), f"{done} of {n} bra rows in 16 evenly spaced blocks, {dt:.1f} s, scaled to the full "
+            "build", None)
+
+
+def cpu_full_build(O, f, c, v, threads):
+    """One whole tps_ci_matvec of the oracle's restatement: (sigma, seconds)."""
+    t0 = time.perf_counter()
+    sig = O.sigma_closed(f, c, v, n_threads=threads)
+    return sig, time.perf_counter() - t0
 
 
 def _shape_12o(seed):
@@ -139,6 +154,32 @@ SERVING_SHAPES = [  # (name, builder(seed), n_cfg, roots, share of the serving s
     ("24o_6x4_M16", _shape_24o, 10000, 4, 0.3),
     ("32o_8x4_M8", _shape_32o, 5000, 2, 0.1),
 ]
+
+
+def headline_solve(g, n, R, tol=1e-6):
+    """The Davidson solve of the headline problem (tps_ci_davidson, src/tpsci_outer.jl:364-454):
+    R roots to a residual of tol, all-FP64 and mixed (float32 sigma builds, FP64 Gram-Schmidt,
+    Rayleigh-Ritz, residuals and final FP64 refinement).  Reports the energy error of the mixed
+    solve against the FP64 one per root."""
+    from fermicg_gb300 import workloads
+    guess = workloads.davidson_guess(n, R, seed=0, lowest=np.argsort(g.diagonal())[:R])
+    res = {}
+    for prec in ("fp64", "fp32"):
+        g.davidson(guess, tol=tol, max_iter=200, precision=prec)  # warm-up (buffers)
+        t1 = time.perf_counter()
+        e, X, rn, it = g.davidson(guess, tol=tol, max_iter=200, precision=prec)
+        res[prec] = (e, rn, it, time.perf_counter() - t1, g.stats()["davidson_sigma_calls"])
+    e64, e32 = res["fp64"][0], res["fp32"][0]
+    err = np.abs(e32 - e64)
+    return {"workload": f"{WORKLOAD}: Davidson, {R} roots, tol {tol:g}",
+            "energies_fp64": [float(x) for x in e64], "energies_mixed": [float(x) for x in e32],
+            "energy_error_per_root": [float(x) for x in err], "max_energy_error": float(err.max()),
+            "within_1uEh": bool(err.max() <= 1e-6),
+            "fp64": {"seconds": res["fp64"][3], "iterations": res["fp64"][2],
+                     "max_residual": float(np.max(res["fp64"][1]))},
+            "mixed": {"seconds": res["fp32"][3], "iterations": res["fp32"][2],
+                      "max_residual": float(np.max(res["fp32"][1]))},
+            "mixed_over_fp64_solve": res["fp64"][3] / res["fp32"][3]}
 
 
 def davidson_benchmark(reps=2, stored=True):
@@ -590,33 +631,75 @@ def open_benchmark(steps, warmup, cpu_seconds, n_cfg=10000, R=4, thresh=1e-4):
         kms.append(g.stats()["last_kernel_ms"])
     st_ = g.stats()
     wall = statistics.median(walls)
+    peaks = _peaks()
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    ach = st_["open_bytes"] / (st_["open_expand_ms"] * 1e-3) / 1e9
     out = {"workload": f"open_sigma_24o_6x4_M16_{n_cfg}cfg_R{R}_thresh{thresh:g}", "n_cfg": int(f.shape[0]),
            "roots": R, "thresh": thresh, "n_out": int(of.shape[0]), "jobs": st_["open_jobs"],
            "jobs_kept_by_screen": st_["open_jobs_kept"], "contractions": st_["open_contractions"],
            "value": 1.0 / wall, "unit": "open_sigma_builds/s", "wall_ms": 1e3 * wall,
-           "device_ms": statistics.median(kms),
-           "contractions_per_s": st_["open_contractions"] / wall}
-    g.close()
+           "device_ms": statistics.median(kms), "expand_kernel_ms": st_["open_expand_ms"],
+           "contractions_per_s": st_["open_contractions"] / wall,
+           "flops_reference": st_["open_flops_reference"],
+           "gflops_reference_count": st_["open_flops_reference"] / (st_["open_expand_ms"] * 1e-3) / 1e9,
+           "roofline": {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                        "bytes": st_["open_bytes"],
+                        "note": "compulsory bytes (TDM blocks touched, C, one key + row per output) over the "
+                                "expand_jobs_kernel time, of measured HBM copy peak; the kernel is bound by the "
+                                "exact FP64 evaluation of candidates, not HBM"}}
     if cpu_seconds > 0:
         import oracle
         O = oracle.Oracle(po, pt)
         threads = os.cpu_count() or 1
         n = f.shape[0]
         nblk = 8
-        for frac in (0.0025, 0.01):
-            rows = max(1, int(n * frac / nblk))
+        # ket rows of 8 evenly spaced blocks, regrouped so that the rows of a Fock sector are
+        # contiguous; the open sigma is a sum over ket rows, so the GPU run on these rows alone
+        # gives exactly their contributions
+        for per in (3, 12):
+            idx = np.concatenate([np.arange((b * n) // nblk, (b * n) // nblk + per) for b in range(nblk)])
+            idx = idx[np.lexsort(f[idx].reshape(len(idx), -1).T[::-1])]
             t1 = time.perf_counter()
-            for b in range(nblk):
-                s0 = (b * n) // nblk
-                O.sigma_open(f, c, v, thresh, rows=(s0, min(n, s0 + rows)), n_threads=threads)
+            ref = O.sigma_open(f[idx], c[idx], v[idx], thresh, n_threads=threads)
             dt = time.perf_counter() - t1
             if dt > cpu_seconds / 4:
                 break
-        done = nblk * rows
+        done = len(idx)
         out["cpu_baseline"] = {"value": done / (dt * n), "unit": "open_sigma_builds/s", "cores": threads,
                                "kind": "port", "sample": f"{done} of {n} ket rows in {nblk} evenly spaced blocks, "
                                f"{dt:.1f} s, scaled to the full build (oracle open_matvec_thread restatement)"}
+        g.state_set(f[idx], c[idx])
+        mine = g.sigma_open(v[idx], thresh)
+        ko, vo = _open_canon(*mine)
+        kr, vr = _open_canon(*ref)
+        same = ko.shape == kr.shape and bool(np.array_equal(ko, kr))
+        out["parity"] = {"sample": f"the same {done} ket rows, GPU against the oracle",
+                         "outputs": int(len(kr)), "key_sets_identical": same,
+                         "values_rel": (float(np.abs(vo - vr).max() / np.abs(vr).max()) if same else None),
+                         "tolerance": 1e-10}
+    g.close()
     return out
+
+
+def _open_canon(of, oc, ov):
+    """Rows of an open sigma as (sorted (Fock key, state key) pairs, values in that order)."""
+    fo = of.reshape(len(of), -1).astype(np.uint64)
+    co = oc.astype(np.uint64)
+    k1 = np.zeros(len(of), dtype=np.uint64)
+    for j in range(fo.shape[1]):
+        k1 = (k1 << np.uint64(4)) | fo[:, j]
+    k2 = np.zeros(len(of), dtype=np.uint64)
+    for j in range(co.shape[1]):
+        k2 = (k2 << np.uint64(8)) | co[:, j]
+    order = np.lexsort((k2, k1))
+    return np.stack([k1[order], k2[order]], axis=1), ov[order]
+
+
+def _peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
 
 
 def clocks_sampler():
@@ -671,21 +754,25 @@ def main():
     if a.impl == "reference":
         if rank != 0:
             return
+        import oracle
         prob, st, po, pt, f, c, v = build_workload(a.n_cfg, a.roots)
         threads = os.cpu_count() or 1
-        vals = []
-        for i in range(a.warmup + a.steps):
-            val, sample = cpu_reference(po, pt, f, c, v, a.cpu_seconds / max(a.steps, 1), threads)
+        O = oracle.Oracle(po, pt)
+        secs = []
+        for i in range(a.warmup + a.steps):  # every step is one whole build over all bra rows
+            _, dt = cpu_full_build(O, f, c, v, threads)
             if i >= a.warmup:
-                vals.append(val)
-        value = statistics.median(vals)
+                secs.append(dt)
+        ms = 1e3 * statistics.mean(secs)
+        value = 1e3 / ms
         print(json.dumps({
             "impl": "reference", "metric": METRIC, "value": value, "unit": "sigma_builds/s", "n_gpus": a.gpus,
-            "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "n_cfg": int(f.shape[0]), "roots": a.roots},
+            "config": bench_config(f.shape[0], a.roots, world),
             "cpu_baseline": {"value": value, "unit": "sigma_builds/s", "cores": threads, "kind": "port",
-                             "sample": sample + "; restatement of tps_ci_matvec (Julia not available)"},
+                             "sample": f"the whole build (all {f.shape[0]} bra rows) every step; C++ restatement "
+                                       "of tps_ci_matvec (the reference is Julia, which is not available)"},
             "e2e": {"value": value, "unit": "sigma_builds/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }))
         return
@@ -846,10 +933,9 @@ def main():
         "metric": METRIC, "value": value, "unit": "sigma_builds/s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": ms32, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 (mixed; fp64 line in fp64)", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n_cfg": n, "roots": R, "n_terms": prob.ham.n_terms(),
-                   "triples_per_sigma": stats["n_triples"], "work_items": stats["n_work_items"],
-                   "plan_seconds": stats["plan_seconds"], "l2": "flushed (256 MiB write) before every timed step",
-                   "parallelism": f"replicas{world}"},
+        "config": bench_config(n, R, world),
+        "workload_stats": {"n_terms": prob.ham.n_terms(), "triples_per_sigma": stats["n_triples"],
+                           "work_items": stats["n_work_items"], "plan_seconds": stats["plan_seconds"]},
         "fp64": {"value": world * 1e3 / ms64, "ms_per_step": ms64, "kernel_ms": k64,
                  "mixed_over_fp64": ms64 / ms32, "fp32_rel_err_vs_fp64": rel32},
         "flops_reference_per_sigma": stats["flops_reference"],
@@ -877,6 +963,11 @@ def main():
                               "note": "cached_sigma_kernel<float>; bound by the L1 data pipe (ket and C-row "
                                       "gathers), not HBM"}
         out["stored_blocks"] = stored
+    if rank == 0 and a.davidson:
+        try:
+            out["headline_solve"] = headline_solve(g, n, R)
+        except Exception as ex:
+            out["headline_solve"] = {"error": str(ex)}
     if rank == 0 and a.serving:
         try:
             out["serving"] = serving_benchmark(stored=a.stored)
@@ -915,9 +1006,21 @@ def main():
     if rank == 0 and a.cpu_seconds > 0:
         try:
             thr = os.cpu_count() or 1
-            cv, sample = cpu_reference(po, pt, f, c, v, a.cpu_seconds, thr)
+            cv, sample, ref = cpu_reference(po, pt, f, c, v, a.cpu_seconds, thr)
             out["cpu_baseline"] = {"value": cv, "unit": "sigma_builds/s", "cores": thr, "kind": "port",
                                    "sample": sample}
+            out["gpu_over_cpu"] = {"mixed": out["value"] / cv, "fp64": out["fp64"]["value"] / cv,
+                                   "e2e_mixed": out["e2e"]["value"] / cv}
+            if ref is not None:
+                # the headline sigma against the oracle's full build of the same C (every row)
+                s64 = sig64.double().cpu().numpy().T
+                s32 = sig32.double().cpu().numpy().T
+                scale = float(np.abs(ref).max())
+                out["parity"] = {"oracle": "oracle tps_ci_matvec restatement, full build, all rows",
+                                 "fp64_rel": float(np.abs(s64 - ref).max()) / scale,
+                                 "fp32_rel": float(np.abs(s32 - ref).max()) / scale,
+                                 "tolerance": {"fp64": 1e-10, "fp32": 2e-5}}
+                out["parity"]["ok"] = bool(out["parity"]["fp64_rel"] <= 1e-10 and out["parity"]["fp32_rel"] <= 2e-5)
         except Exception as ex:  # the baseline must not kill the GPU line
             out["cpu_baseline"] = {"value": None, "error": str(ex)}
     if rank == 0:

@@ -1791,7 +1791,7 @@ extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, c
     if (o.rc != FCG_OK && o.bad < first) {
       rc = o.rc;
       first = o.bad;
-      ctx->err = o.bad > 0 ? o.err + " (problem " + std::to_string(o.bad) + ")" : o.err;
+      ctx->err = o.bad >= 0 ? o.err + " (problem " + std::to_string(o.bad) + ")" : o.err;
     }
   ctx->stats.group_rounds = 0;
   ctx->stats.group_launches = 0;

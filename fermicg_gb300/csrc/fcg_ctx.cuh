@@ -79,6 +79,7 @@ struct fcg_ctx {
   cudaStream_t stream = nullptr;      // stream every call runs on
   cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around one kernel inside a timed sequence
   std::string err;
   // problem
   int N = 0;

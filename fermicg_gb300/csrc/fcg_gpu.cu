@@ -795,6 +795,8 @@ int fcg_ctx_create(int device, fcg_ctx** out) {
   ctx->stream = ctx->own_stream;
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev2);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev3);
   if (e != cudaSuccess) {
     delete ctx;
     return FCG_ECUDA;
@@ -809,6 +811,8 @@ int fcg_ctx_destroy(fcg_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->ev2) cudaEventDestroy(ctx->ev2);
+  if (ctx->ev3) cudaEventDestroy(ctx->ev3);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   delete ctx;
   return FCG_OK;

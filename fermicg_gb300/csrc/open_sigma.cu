@@ -24,6 +24,7 @@
 #include <cmath>
 #include <cstring>
 #include <unordered_map>
+#include <unordered_set>
 
 #include "fcg_ctx.cuh"
 
@@ -520,6 +521,8 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   std::vector<OpenTerm> ots;
   std::vector<OpenItem> items;
   std::vector<int16_t> fb(2 * N);
+  int64_t flops_ref = 0;
+  std::unordered_set<int32_t> tdm_used;  // TDM blocks the jobs read
   for (size_t sk = 0; sk < P.sec_start.size(); ++sk) {
     const int16_t* fk = &P.sec_fock[sk * 2 * N];
     for (int tr = 0; tr < ctx->n_trans; ++tr) {
@@ -586,6 +589,28 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
         }
         FCG_REQUIRE(cnt < (int64_t(1) << 31), FCG_ELIMIT, "bra tuples of one term exceed 2^31");
         o.out_count = int32_t(cnt);
+        // the reference's GEMM flops of this (ket, term) job (contract_matvec_thread,
+        // src/tpsci_matvec_thread.jl:279-818, no prescreen): bra dims M and orbital index
+        // lengths n in term order
+        {
+          const int nbd = r[0];
+          int64_t M[4] = {1, 1, 1, 1}, nn[4] = {1, 1, 1, 1};
+          for (int o2 = 0; o2 < nbd; ++o2) {
+            const int cq = r[2 + o2];
+            const int bl = ctx->h_blk_index[dense_block_index(nmax1, cq, r[6 + o2], fb[2 * cq], fb[2 * cq + 1],
+                                                              fk[2 * cq], fk[2 * cq + 1])];
+            M[o2] = ctx->h_blocks[bl].mb;
+            nn[o2] = r[22 + o2];
+            tdm_used.insert(bl);
+          }
+          int64_t f = 0;
+          if (nbd == 2) f = nn[0] * nn[1] * M[0] + nn[1] * M[0] * M[1];
+          if (nbd == 3) f = M[2] * (nn[0] * nn[1] * nn[2] + nn[0] * nn[1] * M[1] + nn[0] * M[0] * M[1]);
+          if (nbd == 4)
+            f = M[3] * (nn[0] * nn[1] * nn[2] * nn[3] +
+                        M[2] * (nn[0] * nn[1] * nn[2] + nn[0] * nn[1] * M[1] + nn[0] * M[0] * M[1]));
+          flops_ref += 2 * f * int64_t(P.sec_count[sk]);
+        }
         ots.push_back(o);
       }
       const int32_t nt = int32_t(ots.size()) - ot_off;
@@ -656,10 +681,12 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
       FCG_CUDA(cudaMemsetAsync(ctx->d_hkeys.p, 0xFF, cap * sizeof(unsigned long long), s));
       FCG_CUDA(cudaMemsetAsync(ctx->d_hvals.p, 0, cap * R * sizeof(double), s));
       FCG_CUDA(cudaMemsetAsync(ctx->d_counters.p + 2, 0, 3 * sizeof(unsigned long long), s));
+      FCG_CUDA(cudaEventRecord(ctx->ev2, s));
       expand_jobs_kernel<<<unsigned(grid), kExpThreads, smem, s>>>(p, ctx->d_ojobs.p, n_kept, ctx->d_w64.p,
                                                                    ctx->d_op64.p, ctx->d_hkeys.p, ctx->d_hvals.p,
                                                                    cap - 1, ctx->d_counters.p, smem_bytes);
       FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaEventRecord(ctx->ev3, s));
       FCG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(cnt), cudaMemcpyDeviceToHost, s));
       FCG_CUDA(cudaStreamSynchronize(s));
       launches += 2;
@@ -688,7 +715,17 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
     float ms = 0.f;
     FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
     ctx->stats.last_kernel_ms = ms;
+    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
+    ctx->stats.open_expand_ms = ms;
   }
+  // compulsory bytes: the TDM blocks the jobs touch, C, and one key + row per output
+  int64_t tdm_bytes = 0;
+  for (int32_t bl : tdm_used) {
+    const BlockInfo& B = ctx->h_blocks[bl];
+    tdm_bytes += int64_t(B.nidx) * B.mb * B.mk * 8;
+  }
+  ctx->stats.open_flops_reference = flops_ref;
+  ctx->stats.open_bytes = tdm_bytes + 8 * n * R + ctx->open_rows * (6 * int64_t(N) + 8 * int64_t(R));
   ctx->stats.kernel_launches = launches;
   ctx->stats.open_jobs = n_jobs;
   ctx->stats.open_jobs_kept = n_kept;

@@ -83,7 +83,9 @@ class Stats(ctypes.Structure):
                 ("group_launches", ctypes.c_int64), ("group_setup_seconds", ctypes.c_double),
                 ("group_step_seconds", ctypes.c_double), ("group_issue_seconds", ctypes.c_double),
                 ("group_wait_seconds", ctypes.c_double), ("hcache_pairs", ctypes.c_int64),
-                ("hcache_bytes", ctypes.c_int64), ("hcache_seconds", ctypes.c_double)]
+                ("hcache_bytes", ctypes.c_int64), ("hcache_seconds", ctypes.c_double),
+                ("open_expand_ms", ctypes.c_double), ("open_flops_reference", ctypes.c_int64),
+                ("open_bytes", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

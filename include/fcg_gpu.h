@@ -81,6 +81,9 @@ typedef struct fcg_stats {
   int64_t hcache_pairs;     /* (work item, bra, ket) pairs of the stored Hamiltonian blocks */
   int64_t hcache_bytes;     /* device bytes they take (float64 and float32 copies, index) */
   double hcache_seconds;    /* wall time of the last fcg_cache_hamiltonian */
+  double open_expand_ms;    /* device time of the expansion kernel of the last open sigma (CUDA events) */
+  int64_t open_flops_reference; /* the reference's GEMM flops of the last open sigma's jobs (no prescreen) */
+  int64_t open_bytes;       /* its compulsory bytes: TDM blocks touched, C, output rows */
 } fcg_stats;
 
 int fcg_version(void);
@@ -189,6 +192,9 @@ int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double
  * (0: just look) and never blocks longer; on success it copies the results (energies R,
  * vectors column-major n_cfg x R, residuals R, iterations; any may be null) and retires the
  * ticket; a failed solve returns its error code with the message in fcg_last_error(ctx).
+ * A finished ticket holds its result vectors on the host until it is waited for: a caller
+ * that polls or abandons requests retires each one with fcg_wait (null outputs drop the
+ * results), or the results stay until fcg_server_destroy.
  * fcg_server_destroy fails the queued requests, lets the running ones finish (each is
  * bounded by its max_iter) and must come after the last wait.  The reference has no
  * serving loop: each request is the tps_ci_davidson solve of fcg_davidson. */
@@ -304,11 +310,14 @@ int fcg_bst_fois_get(fcg_ctx* ctx, int16_t* fock, int64_t* blocks, int64_t* fact
  * loops driving several streams that cannot afford the device-wide synchronisation
  * cudaFree implies.  Same arguments and results as fcg_sigma_closed_device; the working
  * copies of C and sigma live in a fixed 16 MiB device array built into the library
- * (resident on every device that loads it, until exit), so n_cfg * R must not exceed
- * 1048576 (FCG_ELIMIT otherwise).  The state, operators and terms must already be set.
- * The first call on a device looks up the array's device address (cudaGetSymbolAddress)
- * and should come before any stream capture.  All calls on one device share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * (placed on a device when the library's device code is first used there, and held until
+ * exit), so n_cfg * R must not exceed 1048576 (FCG_ELIMIT otherwise).  The state,
+ * operators and terms must already be set.  The first call on a device looks up the
+ * array's device address (cudaGetSymbolAddress) and keeps it for the life of the process:
+ * that first call should come before any stream capture, and the device's primary context
+ * must not be reset (cudaDeviceReset) while the library is in use.  Like the other sigma
+ * calls it waits for its stream before returning.  All calls on one device share the
+ * array: calls that overlap on the GPU race and must be serialised by the caller. */
 int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
 
 #ifdef __cplusplus

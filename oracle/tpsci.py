@@ -183,10 +183,16 @@ class OracleTPSCI:
             norms = np.linalg.norm(vec_asci.get_vector(), axis=0)
             v_pt = np.zeros_like(sig_v)
             e2 = np.zeros(R)
-            for r in range(R):
-                denom = 1.0 / (efock[r] / (norms[r] * norms[r]) - hd)
-                v_pt[:, r] = denom * sig_v[:, r]
-                e2[r] = float(np.sum(sig_v[:, r] * v_pt[:, r]))
+            # A configuration whose Hcmf diagonal equals E0/|v|^2 exactly (degenerate local states,
+            # e.g. the spin-flipped partner of the reference) gets an infinite (sigma != 0) or NaN
+            # (sigma == 0) first-order coefficient, as 1.0 ./ (...) gives in the reference
+            # (src/tpsci.jl:323); clip! keeps such a row (no |c| < thresh holds), so it always enters
+            # the variational space, here as there.  Only the floating-point warning is silenced.
+            with np.errstate(divide="ignore", invalid="ignore"):
+                for r in range(R):
+                    denom = 1.0 / (efock[r] / (norms[r] * norms[r]) - hd)
+                    v_pt[:, r] = denom * sig_v[:, r]
+                    e2[r] = float(np.sum(sig_v[:, r] * v_pt[:, r]))
             vec_pt = _copy(sig)
             if len(vec_pt):
                 vec_pt.set_vector(v_pt)

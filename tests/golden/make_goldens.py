@@ -1,8 +1,8 @@
 """Generate the golden fixtures under tests/golden/ from the reference's own test data.
 
-Run in a checkout that has the reference at REFERENCE (default /root/reference):
+Run with the path of a FermiCG checkout as the one (required) argument:
 
-    python tests/golden/make_goldens.py
+    python tests/golden/make_goldens.py PATH_TO_FERMICG
 
 It reads the reference's JLD2 fixtures (test/_testdata_*.jld2) with the minimal
 HDF5 reader next to this script, and the known-answer values written in the
@@ -23,7 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, HERE)
 from jld2_reader import JLD2File  # noqa: E402
 
-REF = os.environ.get("REFERENCE", "/root/reference")
+REF = None  # the FermiCG checkout, set from the command line
 
 
 def _ints(f):
@@ -118,4 +118,7 @@ def main():
 
 
 if __name__ == "__main__":
+    if len(sys.argv) != 2 or not os.path.isdir(os.path.join(sys.argv[1], "test")):
+        sys.exit("usage: python tests/golden/make_goldens.py PATH_TO_FERMICG  (a checkout with test/*.jld2)")
+    REF = sys.argv[1]
     main()

@@ -73,6 +73,11 @@ def test_a_failing_problem_is_named_and_the_contexts_stay_usable():
         assert np.abs(e - ref).max() < 1e-9
     res = davidson_grouped([gpus[0], gpus[2]], [probs[0][1], probs[2][1]], tol=1e-7, max_iter=300)
     assert np.abs(res[1][0] - probs[2][2]).max() < 1e-9
+    # a failure of the first problem is named too
+    guesses = [p[1].copy() for p in probs]
+    guesses[0][:] = np.nan
+    with pytest.raises(FcgError, match=r"problem 0\)"):
+        davidson_grouped(gpus, guesses, tol=1e-7, max_iter=300)
     for g in gpus:
         g.close()
 

@@ -143,3 +143,20 @@ def test_closed_sigma_many_roots(R):
     assert rel_err(g.sigma_closed(x, "fp64"), ref) < FP64_TOL
     assert rel_err(g.sigma_closed(x, "fp32"), ref) < FP32_TOL
     np.testing.assert_allclose(g.diagonal(), O.diagonal_H(f, c), rtol=1e-12, atol=1e-12)
+
+
+def test_closed_sigma_config1_30k_matches_oracle():
+    """The headline problem's space at 3e4 configurations (about 5e7 triples): FP64 and FP32
+    sigma against the oracle's full tps_ci_matvec restatement, R = 4."""
+    prob, st = config1_subspace(30000, 4)
+    g, po, pt, f, c = _gpu_for(prob, st)
+    O = oracle.Oracle(po, pt)
+    x = st.get_vector()
+    ref = O.sigma_closed(f, c, x)
+    assert g.stats()["n_triples"] > 10_000_000
+    assert rel_err(g.sigma_closed(x, "fp64"), ref) < FP64_TOL
+    assert rel_err(g.sigma_closed(x, "fp32"), ref) < FP32_TOL
+    # the same through stored Hamiltonian blocks
+    g.cache_hamiltonian()
+    assert rel_err(g.sigma_closed(x, "fp64"), ref) < FP64_TOL
+    assert rel_err(g.sigma_closed(x, "fp32"), ref) < FP32_TOL

@@ -57,6 +57,29 @@ def test_noalloc_matches_device_entry_point_on_two_calls(precision, tol):
         assert rel_err(out, ref) < tol, (call, rel_err(out, ref))
 
 
+def test_noalloc_fp64_then_fp32_and_stored_blocks():
+    """An FP64 call, then an FP32 call on the same scratch (the float copies overlay the
+    double ones), then both again after the state's Hamiltonian blocks are stored (the
+    stored-block launch path): each against the regular device entry point."""
+    torch = pytest.importorskip("torch")
+    g, v = _ctx()
+    n, R = v.shape
+    d_c = _dev(torch, np.random.default_rng(5).standard_normal((n, R)))
+    for stored in (False, True):
+        if stored:
+            g.cache_hamiltonian()
+        for precision, tol in (("fp64", FP64_TOL), ("fp32", FP32_TOL)):
+            d_ref = torch.zeros_like(d_c)
+            d_out = torch.full_like(d_c, float("nan"))
+            g.sigma_closed_device(d_c.data_ptr(), d_ref.data_ptr(), R, precision)
+            g.sigma_closed_noalloc(d_c.data_ptr(), d_out.data_ptr(), R, precision)
+            torch.cuda.synchronize()
+            ref = d_ref.cpu().numpy().T
+            out = d_out.cpu().numpy().T
+            assert np.all(np.isfinite(out))
+            assert rel_err(out, ref) < tol, (stored, precision, rel_err(out, ref))
+
+
 def test_noalloc_rejects_sizes_beyond_its_scratch():
     torch = pytest.importorskip("torch")
     g, v = _ctx(n_cfg=600, R=4)
