@@ -114,8 +114,9 @@ struct fcg_ctx {
   DevBuf<int16_t> d_sec_fock;
   DevBuf<int32_t> d_row_sector;
   DevBuf<WorkItem> d_items;
-  DevBuf<int64_t> d_prefix;
-  DevBuf<int64_t> d_cta32, d_cta64;  // first work item of each closed-sigma CTA (float / double chunks)
+  DevBuf<LaneJob> d_jobs;           // closed-sigma lane jobs, 32 per warp task
+  DevBuf<int64_t> d_chunk_lo;       // first warp task of each warp chunk
+  DevBuf<int64_t> d_chunk_val;      // first stored value of each warp chunk
   DevBuf<int32_t> d_perm;
   DevBuf<TermSector> d_ts;
   DevBuf<unsigned char> d_group;    // entries of the last grouped closed sigma led by this context
@@ -125,8 +126,6 @@ struct fcg_ctx {
   // (bra, ket) pair, the sum over the item's terms of the matrix element
   bool have_hcache = false;
   int64_t hc_pairs = 0;
-  DevBuf<int64_t> d_hc_prefix;  // pairs before each work item
-  DevBuf<int64_t> d_hc_cta32, d_hc_cta64;  // first work item of each cached-sigma CTA (float / double runs)
   DevBuf<double> d_hc64;
   DevBuf<float> d_hc32;
   // release = false keeps the buffers for the next state's blocks (grow-only; a cudaFree
@@ -137,9 +136,6 @@ struct fcg_ctx {
     if (!release) return;
     d_hc64.release();
     d_hc32.release();
-    d_hc_prefix.release();
-    d_hc_cta32.release();
-    d_hc_cta64.release();
   }
   // job lists of the set-up calls (fcg_set_ops, fcg_set_terms, fcg_cache_hamiltonian), grow-only
   DevBuf<unsigned char> scratch_a, scratch_b;

@@ -98,24 +98,6 @@ __global__ void colmax_kernel(const MaxJob* __restrict__ jobs, const double* __r
 }
 
 // ---- closed sigma ------------------------------------------------------------------------
-struct SigmaParams {
-  const WorkItem* items;
-  const int64_t* prefix;
-  const int64_t* cta_lo;  // work item holding each CTA's first triple; [n_cta] = last item
-  int64_t n_items;
-  int64_t n_triples;
-  const int32_t* perm;
-  const TermSector* ts;
-  const int16_t* cfg;  // [n_cfg][N]
-  int N;
-  int R;
-  // stored Hamiltonian blocks (fcg_cache_hamiltonian): pairs before each work item, first
-  // work item of each cached-sigma CTA, pair count
-  const int64_t* hc_prefix;
-  const int64_t* hc_cta;
-  int64_t n_pairs;
-};
-
 // ---- vector loads ---------------------------------------------------------------------------
 // Vec4: 4 consecutive elements (16 bytes float, 32 bytes double); Chunk: 32 bytes (8 float
 // or 4 double) in one 256-bit load.  Callers guarantee the alignment: device TDM and W
@@ -272,300 +254,191 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
   return ts.sign < 0 ? -me : me;
 }
 
-#ifndef FCG_SIGMA_RUN32
-#define FCG_SIGMA_RUN32 16
-#endif
-#ifndef FCG_SIGMA_RUN64
-#define FCG_SIGMA_RUN64 16
-#endif
-#ifndef FCG_SIGMA_MINB32
-#define FCG_SIGMA_MINB32 4
-#endif
-#ifndef FCG_SIGMA_MINB64
-#define FCG_SIGMA_MINB64 3
-#endif
-constexpr int kSigmaThreads = 256;
-// consecutive triples per thread, and per CTA
-template <typename T>
-__host__ __device__ constexpr int sigma_run() {
-  return sizeof(T) == 4 ? FCG_SIGMA_RUN32 : FCG_SIGMA_RUN64;
-}
-template <typename T>
-__host__ __device__ constexpr int64_t sigma_chunk() {
-  return int64_t(kSigmaThreads) * sigma_run<T>();
-}
+constexpr int kSigmaThreads = 256;       // 8 warps per CTA
+constexpr int kWarpsPerCta = kSigmaThreads / 32;
 constexpr int kMaxR = 16;
+#ifndef FCG_LANE_MINB32
+#define FCG_LANE_MINB32 4
+#endif
+#ifndef FCG_LANE_MINB64
+#define FCG_LANE_MINB64 3
+#endif
 
-// largest w in [lo, hi] with prefix[w] <= x
-__device__ __forceinline__ int64_t find_item(const int64_t* prefix, int64_t lo, int64_t hi, int64_t x) {
-  while (lo < hi) {
-    int64_t mid = (lo + hi + 1) >> 1;
-    if (__ldg(prefix + mid) <= x)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
+struct LaneParams {
+  const LaneJob* jobs;       // 32 per warp task
+  const int64_t* chunk_lo;   // n_chunks + 1: first warp task of each warp chunk
+  const int64_t* chunk_val;  // n_chunks + 1: first stored value of each chunk
+  int64_t n_chunks;
+  const int32_t* perm;
+  const TermSector* ts;
+  const int16_t* cfg;  // [n_cfg][kCfgStride]
+  int R;
+};
 
-// the same over a shared-memory copy of prefix[base ..]
-__device__ __forceinline__ int find_item_shared(const int64_t* s_pre, int lo, int hi, int64_t x) {
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (s_pre[mid] <= x)
-      lo = mid;
-    else
-      hi = mid - 1;
-  }
-  return lo;
-}
-
-constexpr int kPrefixShared = 1024;  // prefix entries a CTA stages in shared memory
-
-template <typename T, int RV>
-__device__ __forceinline__ void flush_row(T* __restrict__ sig, int b, const T* acc, int R) {
+// R coefficients of one row of a row-major [n][R] array (RR > 0: R == RR, known at compile
+// time), with vector loads when exactly 2 or 4 roots; out[r] = 0 for r >= R
+template <typename T, int RR, int RV>
+__device__ __forceinline__ void load_row(const T* __restrict__ p, int R, T* out) {
+  if (RR == 4 && sizeof(T) == 4) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    out[0] = q.x, out[1] = q.y, out[2] = q.z, out[3] = q.w;
+  } else if (RR == 4) {
+    Vec4<double> q;
+    q.load(reinterpret_cast<const double*>(p));
 #pragma unroll
-  for (int r = 0; r < RV; ++r)
-    if (r < R) atomicAdd(sig + int64_t(b) * R + r, acc[r]);
-}
-
-// Each CTA owns a fixed chunk of the flattened triple space (exact load balance) and each
-// thread a run of sigma_run<T>() consecutive triples (term fastest, then ket, then bra inside a
-// work item), decoded incrementally; contributions to one bra row are summed in registers
-// and flushed with one atomic per root when the bra changes.
-// RR > 0: exactly RR roots; RR == 0: p.R roots, at most RMAX
-template <typename T, int RR, int RMAX = kMaxR>
-__device__ __forceinline__ void closed_sigma_cta(const SigmaParams& p, const T* __restrict__ w,
-                                                 const T* __restrict__ op, const T* __restrict__ cin,
-                                                 T* __restrict__ sig, int64_t cta) {
-  constexpr int RV = RR > 0 ? RR : RMAX;
-  constexpr int64_t kChunk = sigma_chunk<T>();
-  constexpr int kRun = sigma_run<T>();
-  const int64_t s0 = int64_t(cta) * kChunk;
-  const int64_t e0 = (s0 + kChunk < p.n_triples) ? s0 + kChunk : p.n_triples;
-  // the CTA's work items [w_lo, w_hi] come from the plan; their prefix goes to shared memory
-  __shared__ int64_t s_pre[kPrefixShared];
-  const int64_t w_lo = __ldg(p.cta_lo + cta), w_hi = __ldg(p.cta_lo + cta + 1);
-  const int span = int(w_hi - w_lo + 1 < kPrefixShared + 1 ? w_hi - w_lo + 1 : kPrefixShared + 1);
-  const bool staged = span <= kPrefixShared;
-  if (staged)
-    for (int i = threadIdx.x; i < span; i += kSigmaThreads) s_pre[i] = __ldg(p.prefix + w_lo + i);
-  __syncthreads();
-  const int R = RR > 0 ? RR : p.R;
-  const int64_t t0 = s0 + int64_t(threadIdx.x) * kRun;
-  if (t0 >= e0) return;
-  const int64_t t1 = (t0 + kRun < e0) ? t0 + kRun : e0;
-  const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
-  int64_t wi, local;
-  if (staged) {
-    const int q = find_item_shared(s_pre, 0, span - 1, t0);
-    wi = w_lo + q;
-    local = t0 - s_pre[q];
+    for (int r = 0; r < 4; ++r) out[r] = T(q.v[r]);
+  } else if (RR == 2 && sizeof(T) == 4) {
+    const float2 q = __ldg(reinterpret_cast<const float2*>(p));
+    out[0] = q.x, out[1] = q.y;
+  } else if (RR == 2) {
+    const double2 q = __ldg(reinterpret_cast<const double2*>(p));
+    out[0] = T(q.x), out[1] = T(q.y);
   } else {
-    wi = find_item(p.prefix, w_lo, w_hi, t0);
-    local = t0 - __ldg(p.prefix + wi);
-  }
-  WorkItem it = p.items[wi];
-  int ti = int(local % it.nt);
-  int64_t rest = local / it.nt;
-  int kj = int(rest % it.nk);
-  int bj = int(rest / it.nk);
-  int b = __ldg(p.perm + it.bra_off + bj);
-  int k = __ldg(p.perm + it.ket_off + kj);
-  uint4 rb = __ldg(cfg + b);
-  uint4 rk = __ldg(cfg + k);
-  T acc[RV];
 #pragma unroll
-  for (int r = 0; r < RV; ++r) acc[r] = T(0);
-  for (int64_t idx = t0; idx < t1; ++idx) {
-    const TermSector& ts = p.ts[it.ts_off + ti];  // fields read where used: fewer live registers
-    const T me = dressed_element<T>(ts, w, op, rb, rk);
-    const T* ck = cin + int64_t(k) * R;
+    for (int r = 0; r < RV; ++r) out[r] = r < R ? __ldg(p + r) : T(0);
+  }
+}
+
+// sig[row] += acc for R roots: one vector reduction for exactly four float roots, else
+// scalar atomics
+template <typename T, int RR, int RV>
+__device__ __forceinline__ void add_row(T* __restrict__ sig, int b, const T* acc, int R) {
+  T* dst = sig + int64_t(b) * R;
+  if (RR == 4 && sizeof(T) == 4) {
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(dst), "f"(float(acc[0])), "f"(float(acc[1])),
+                 "f"(float(acc[2])), "f"(float(acc[3]))
+                 : "memory");
+  } else {
 #pragma unroll
     for (int r = 0; r < RV; ++r)
-      if (r < R) acc[r] = fma(me, __ldg(ck + r), acc[r]);
-    if (idx + 1 == t1) break;
-    // advance to the next triple
-    if (++ti == it.nt) {
-      ti = 0;
-      if (++kj == it.nk) {
-        kj = 0;
-        if (++bj == it.nb) {  // next work item
-          bj = 0;
-          ++wi;
-          it = p.items[wi];
-        }
-        const int nb_row = __ldg(p.perm + it.bra_off + bj);
-        if (nb_row != b) {
-          flush_row<T, RV>(sig, b, acc, R);
-#pragma unroll
-          for (int r = 0; r < RV; ++r) acc[r] = T(0);
-          b = nb_row;
-          rb = __ldg(cfg + b);
-        }
-      }
-      k = __ldg(p.perm + it.ket_off + kj);
-      rk = __ldg(cfg + k);
-    }
+      if (r < R) atomicAdd(dst + r, acc[r]);
   }
-  flush_row<T, RV>(sig, b, acc, R);
+}
+
+// One warp chunk of the closed sigma: the chunk's warp tasks in order, lane i of a task
+// running lane job 32 * task + i.  For each of its kets the lane sums the work item's terms
+// (the lanes of a warp mostly share the term records: broadcast loads), multiplies by the
+// ket's coefficients and keeps the bra row in registers; the row goes to sigma once per job.
+// RR > 0: exactly RR roots; RR == 0: p.R roots, at most RMAX.
+template <typename T, int RR, int RMAX = kMaxR>
+__device__ __forceinline__ void closed_lane_warp(const LaneParams& p, const T* __restrict__ w,
+                                                 const T* __restrict__ op, const T* __restrict__ cin,
+                                                 T* __restrict__ sig, int64_t chunk) {
+  constexpr int RV = RR > 0 ? RR : RMAX;
+  const int R = RR > 0 ? RR : p.R;
+  const int lane = threadIdx.x & 31;
+  const int64_t t_lo = __ldg(p.chunk_lo + chunk), t_hi = __ldg(p.chunk_lo + chunk + 1);
+  const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
+  for (int64_t wt = t_lo; wt < t_hi; ++wt) {
+    const LaneJob j = p.jobs[wt * 32 + lane];
+    if (j.len == 0) continue;
+    const uint4 rb = __ldg(cfg + j.b);
+    const TermSector* tsl = p.ts + j.ts_off;
+    T acc[RV];
+#pragma unroll
+    for (int r = 0; r < RV; ++r) acc[r] = T(0);
+    for (int kk = 0; kk < int(j.len); ++kk) {
+      const int k = __ldg(p.perm + j.kp + kk);
+      const uint4 rk = __ldg(cfg + k);
+      T me = T(0);
+      for (int t = 0; t < int(j.nt); ++t) me += dressed_element<T>(tsl[t], w, op, rb, rk);
+      T c[RV];
+      load_row<T, RR, RV>(cin + int64_t(k) * R, R, c);
+#pragma unroll
+      for (int r = 0; r < RV; ++r) acc[r] = fma(me, c[r], acc[r]);
+    }
+    add_row<T, RR, RV>(sig, j.b, acc, R);
+  }
 }
 
 template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
-    closed_sigma_kernel(SigmaParams p, const T* __restrict__ w, const T* __restrict__ op,
-                        const T* __restrict__ cin, T* __restrict__ sig) {
-  closed_sigma_cta<T, RR>(p, w, op, cin, sig, blockIdx.x);
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_LANE_MINB32 : FCG_LANE_MINB64)
+    closed_sigma_lane_kernel(LaneParams p, const T* __restrict__ w, const T* __restrict__ op,
+                             const T* __restrict__ cin, T* __restrict__ sig) {
+  const int64_t chunk = int64_t(blockIdx.x) * kWarpsPerCta + (threadIdx.x >> 5);
+  if (chunk >= p.n_chunks) return;
+  closed_lane_warp<T, RR>(p, w, op, cin, sig, chunk);
 }
-
 
 // ---- stored Hamiltonian blocks -------------------------------------------------------------
-// Inside a work item the triples run term fastest, then ket, then bra, so the item's (bra,
-// ket) pairs are pair = bj * nk + kj.  The cache holds, at hc_prefix[w] + pair, the sum over
-// the item's terms of the dressed matrix element (signs included), added in term order in
-// float64.  A sigma from the cache reads one value per pair instead of recomputing every
-// term's contraction.
-constexpr int kCacheRun = 4;  // pairs per thread of the assembly
-// pairs per thread of the cached sigma (measured on the 1e5-configuration problem: 32 for
-// float builds, 16 for double builds)
-template <typename T>
-__host__ __device__ constexpr int hc_run() {
-  return sizeof(T) == 4 ? 32 : 16;
-}
-constexpr int64_t kCacheChunk = int64_t(kSigmaThreads) * kCacheRun;
-template <typename T>
-__host__ __device__ constexpr int64_t hc_chunk() {
-  return int64_t(kSigmaThreads) * hc_run<T>();
-}
+// For every warp task the blocks hold 32 values per ket step, one per lane: the sum over the
+// work item's terms of the dressed matrix element of the lane's (bra, ket) pair (added in term
+// order in float64; 0 past the lane's kets), at chunk_val[chunk] + 32 * (longest job of each
+// earlier task of the chunk, summed) + 32 * step + lane.  A sigma from the blocks reads each
+// step's 32 values with one coalesced load instead of recomputing every term's contraction.
+__device__ __forceinline__ int task_len(int len) { return __reduce_max_sync(0xffffffffu, unsigned(len)); }
 
-// first pair and pair count of the CTA's chunk; w_lo / w_hi its first and last work item
-__global__ void __launch_bounds__(kSigmaThreads) hcache_build_kernel(SigmaParams p, const int64_t* __restrict__ cta_lo,
-                                                                     const double* __restrict__ w,
-                                                                     const double* __restrict__ op,
-                                                                     double* __restrict__ hc) {
-  const int64_t s0 = int64_t(blockIdx.x) * kCacheChunk;
-  const int64_t e0 = (s0 + kCacheChunk < p.n_pairs) ? s0 + kCacheChunk : p.n_pairs;
-  const int64_t t0 = s0 + int64_t(threadIdx.x) * kCacheRun;
-  if (t0 >= e0) return;
-  const int64_t t1 = (t0 + kCacheRun < e0) ? t0 + kCacheRun : e0;
-  int64_t wi = find_item(p.hc_prefix, __ldg(cta_lo + blockIdx.x), __ldg(cta_lo + blockIdx.x + 1), t0);
-  const int64_t local = t0 - __ldg(p.hc_prefix + wi);
-  WorkItem it = p.items[wi];
-  int kj = int(local % it.nk);
-  int bj = int(local / it.nk);
+__global__ void __launch_bounds__(kSigmaThreads) hcache_lane_build_kernel(LaneParams p, const double* __restrict__ w,
+                                                                          const double* __restrict__ op,
+                                                                          double* __restrict__ hc) {
+  const int64_t chunk = int64_t(blockIdx.x) * kWarpsPerCta + (threadIdx.x >> 5);
+  if (chunk >= p.n_chunks) return;
+  const int lane = threadIdx.x & 31;
   const uint4* cfg = reinterpret_cast<const uint4*>(p.cfg);
-  uint4 rb = __ldg(cfg + __ldg(p.perm + it.bra_off + bj));
-  uint4 rk = __ldg(cfg + __ldg(p.perm + it.ket_off + kj));
-  for (int64_t idx = t0; idx < t1; ++idx) {
-    double me = 0.0;
-    for (int t = 0; t < it.nt; ++t) me += dressed_element<double>(p.ts[it.ts_off + t], w, op, rb, rk);
-    hc[idx] = me;
-    if (idx + 1 == t1) break;
-    if (++kj == it.nk) {
-      kj = 0;
-      if (++bj == it.nb) {
-        bj = 0;
-        ++wi;
-        it = p.items[wi];
+  int64_t val = __ldg(p.chunk_val + chunk);
+  const int64_t t_lo = __ldg(p.chunk_lo + chunk), t_hi = __ldg(p.chunk_lo + chunk + 1);
+  for (int64_t wt = t_lo; wt < t_hi; ++wt) {
+    const LaneJob j = p.jobs[wt * 32 + lane];
+    const int steps = task_len(j.len);
+    const uint4 rb = __ldg(cfg + j.b);
+    for (int s = 0; s < steps; ++s) {
+      double me = 0.0;
+      if (s < int(j.len)) {
+        const uint4 rk = __ldg(cfg + __ldg(p.perm + j.kp + s));
+        for (int t = 0; t < int(j.nt); ++t) me += dressed_element<double>(p.ts[j.ts_off + t], w, op, rb, rk);
       }
-      rb = __ldg(cfg + __ldg(p.perm + it.bra_off + bj));
+      hc[val + 32 * s + lane] = me;
     }
-    rk = __ldg(cfg + __ldg(p.perm + it.ket_off + kj));
+    val += 32 * int64_t(steps);
   }
 }
 
-// sigma[bra] += hc[pair] * C[ket] over the CTA's chunk of pairs: each thread a run of hc_run<T>()
-// consecutive pairs (read with 32-byte loads), contributions to one bra row summed in
-// registers and flushed with one atomic per root when the bra changes.
+// sigma from the stored blocks: the chunk's warp tasks as in closed_lane_warp, one stored value
+// per lane and ket in place of the term loop
 template <typename T, int RR, int RMAX = kMaxR>
-__device__ __forceinline__ void cached_sigma_cta(const SigmaParams& p, const T* __restrict__ hc,
-                                                 const T* __restrict__ cin, T* __restrict__ sig, int64_t cta) {
+__device__ __forceinline__ void cached_lane_warp(const LaneParams& p, const T* __restrict__ hc,
+                                                 const T* __restrict__ cin, T* __restrict__ sig, int64_t chunk) {
   constexpr int RV = RR > 0 ? RR : RMAX;
-  constexpr int kHcRun = hc_run<T>();
-  constexpr int64_t kHcChunk = hc_chunk<T>();
-  const int64_t s0 = cta * kHcChunk;
-  const int64_t e0 = (s0 + kHcChunk < p.n_pairs) ? s0 + kHcChunk : p.n_pairs;
-  __shared__ int64_t s_pre[kPrefixShared];
-  const int64_t w_lo = __ldg(p.hc_cta + cta), w_hi = __ldg(p.hc_cta + cta + 1);
-  const int span = int(w_hi - w_lo + 1 < kPrefixShared + 1 ? w_hi - w_lo + 1 : kPrefixShared + 1);
-  const bool staged = span <= kPrefixShared;
-  if (staged)
-    for (int i = threadIdx.x; i < span; i += kSigmaThreads) s_pre[i] = __ldg(p.hc_prefix + w_lo + i);
-  __syncthreads();
   const int R = RR > 0 ? RR : p.R;
-  const int64_t t0 = s0 + int64_t(threadIdx.x) * kHcRun;
-  if (t0 >= e0) return;
-  const int n = int((t0 + kHcRun < e0) ? kHcRun : e0 - t0);
-  int64_t wi, local;
-  if (staged) {
-    const int q = find_item_shared(s_pre, 0, span - 1, t0);
-    wi = w_lo + q;
-    local = t0 - s_pre[q];
-  } else {
-    wi = find_item(p.hc_prefix, w_lo, w_hi, t0);
-    local = t0 - __ldg(p.hc_prefix + wi);
-  }
-  T mv[kHcRun];
-  if (n == kHcRun) {  // t0 is a multiple of kHcRun: the run starts on a 64-byte boundary or more
-    constexpr int C = Chunk<T>::n;
+  const int lane = threadIdx.x & 31;
+  const int64_t t_lo = __ldg(p.chunk_lo + chunk), t_hi = __ldg(p.chunk_lo + chunk + 1);
+  int64_t val = __ldg(p.chunk_val + chunk);
+  for (int64_t wt = t_lo; wt < t_hi; ++wt) {
+    const LaneJob j = p.jobs[wt * 32 + lane];
+    const int steps = task_len(j.len);
+    if (j.len > 0) {
+      const T* hv = hc + val + lane;
+      T acc[RV];
 #pragma unroll
-    for (int c = 0; c < kHcRun / C; ++c) {
-      Chunk<T> q;
-      q.load(hc + t0 + C * c);
+      for (int r = 0; r < RV; ++r) acc[r] = T(0);
+      for (int s = 0; s < int(j.len); ++s) {
+        const T v = __ldg(hv + 32 * s);
+        T c[RV];
+        load_row<T, RR, RV>(cin + int64_t(__ldg(p.perm + j.kp + s)) * R, R, c);
 #pragma unroll
-      for (int u = 0; u < C; ++u) mv[C * c + u] = q.v[u];
-    }
-  } else {
-#pragma unroll
-    for (int i = 0; i < kHcRun; ++i) mv[i] = i < n ? __ldg(hc + t0 + i) : T(0);
-  }
-  WorkItem it = p.items[wi];
-  int kj = int(local % it.nk);
-  int bj = int(local / it.nk);
-  int b = __ldg(p.perm + it.bra_off + bj);
-  int k = __ldg(p.perm + it.ket_off + kj);
-  T acc[RV];
-#pragma unroll
-  for (int r = 0; r < RV; ++r) acc[r] = T(0);
-#pragma unroll
-  for (int i = 0; i < kHcRun; ++i) {
-    const T* ck = cin + int64_t(k) * R;
-#pragma unroll
-    for (int r = 0; r < RV; ++r)
-      if (r < R) acc[r] = fma(mv[i], __ldg(ck + r), acc[r]);
-    if (i + 1 == n) break;
-    if (++kj == it.nk) {
-      kj = 0;
-      if (++bj == it.nb) {
-        bj = 0;
-        ++wi;
-        it = p.items[wi];
+        for (int r = 0; r < RV; ++r) acc[r] = fma(v, c[r], acc[r]);
       }
-      const int nb_row = __ldg(p.perm + it.bra_off + bj);
-      if (nb_row != b) {
-        flush_row<T, RV>(sig, b, acc, R);
-#pragma unroll
-        for (int r = 0; r < RV; ++r) acc[r] = T(0);
-        b = nb_row;
-      }
+      add_row<T, RR, RV>(sig, j.b, acc, R);
     }
-    k = __ldg(p.perm + it.ket_off + kj);
+    val += 32 * int64_t(steps);
   }
-  flush_row<T, RV>(sig, b, acc, R);
 }
 
 template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads) cached_sigma_kernel(SigmaParams p, const T* __restrict__ hc,
-                                                                     const T* __restrict__ cin, T* __restrict__ sig) {
-  cached_sigma_cta<T, RR>(p, hc, cin, sig, blockIdx.x);
+__global__ void __launch_bounds__(kSigmaThreads) cached_sigma_lane_kernel(LaneParams p, const T* __restrict__ hc,
+                                                                          const T* __restrict__ cin,
+                                                                          T* __restrict__ sig) {
+  const int64_t chunk = int64_t(blockIdx.x) * kWarpsPerCta + (threadIdx.x >> 5);
+  if (chunk >= p.n_chunks) return;
+  cached_lane_warp<T, RR>(p, hc, cin, sig, chunk);
 }
 
-// Many independent problems in one launch: problem q owns CTAs [cta0, cta0 + its CTA count)
-// of the grid; cta_problem maps every CTA to its problem.  Problems with stored Hamiltonian
-// blocks (hc set) run in a second grid of cached-sigma CTAs, numbered from cta0 there.
+// Many independent problems in one launch: problem q owns CTAs [cta0, cta0 + ceil(its chunks
+// / 8)) of the grid; cta_problem maps every CTA to its problem.  Problems with stored
+// Hamiltonian blocks (hc set) run in a second grid, numbered from cta0 there.
 template <typename T>
 struct GroupEntry {
-  SigmaParams p;
+  LaneParams p;
   const T* w;
   const T* op;
   const T* hc;       // stored Hamiltonian blocks, or null
@@ -578,19 +451,23 @@ struct GroupEntry {
 };
 
 template <typename T, int RMAX>
-__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_SIGMA_MINB32 : FCG_SIGMA_MINB64)
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_LANE_MINB32 : FCG_LANE_MINB64)
     closed_sigma_grouped_kernel(const GroupEntry<T>* __restrict__ g, const int32_t* __restrict__ cta_problem) {
   const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
-  const SigmaParams p = e.p;
-  closed_sigma_cta<T, 0, RMAX>(p, e.w, e.op, e.cin, e.sig, int64_t(blockIdx.x) - e.cta0);
+  const LaneParams p = e.p;
+  const int64_t chunk = (int64_t(blockIdx.x) - e.cta0) * kWarpsPerCta + (threadIdx.x >> 5);
+  if (chunk >= p.n_chunks) return;
+  closed_lane_warp<T, 0, RMAX>(p, e.w, e.op, e.cin, e.sig, chunk);
 }
 
 template <typename T, int RMAX>
 __global__ void __launch_bounds__(kSigmaThreads)
     cached_sigma_grouped_kernel(const GroupEntry<T>* __restrict__ g, const int32_t* __restrict__ cta_problem) {
   const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
-  const SigmaParams p = e.p;
-  cached_sigma_cta<T, 0, RMAX>(p, e.hc, e.cin, e.sig, int64_t(blockIdx.x) - e.cta0);
+  const LaneParams p = e.p;
+  const int64_t chunk = (int64_t(blockIdx.x) - e.cta0) * kWarpsPerCta + (threadIdx.x >> 5);
+  if (chunk >= p.n_chunks) return;
+  cached_lane_warp<T, 0, RMAX>(p, e.hc, e.cin, e.sig, chunk);
 }
 
 // problem blockIdx.y: C to the row-major working copy, sigma zeroed
@@ -749,24 +626,21 @@ __global__ void diag_op_kernel(DiagParams p, const double* __restrict__ op, int 
 // ---------------------------------------------------------------------------------------
 // host side
 
-static SigmaParams make_sigma_params(fcg_ctx* ctx, int R) {
-  SigmaParams p{};
-  p.items = ctx->d_items.p;
-  p.prefix = ctx->d_prefix.p;
-  p.n_items = int64_t(ctx->plan.items.size());
-  p.n_triples = ctx->plan.n_triples;
+static LaneParams make_lane_params(fcg_ctx* ctx, int R) {
+  LaneParams p{};
+  p.jobs = ctx->d_jobs.p;
+  p.chunk_lo = ctx->d_chunk_lo.p;
+  p.chunk_val = ctx->d_chunk_val.p;
+  p.n_chunks = int64_t(ctx->plan.chunk_lo.size()) - 1;
   p.perm = ctx->d_perm.p;
   p.ts = ctx->d_ts.p;
   p.cfg = ctx->d_cfg.p;
-  p.N = ctx->N;
   p.R = R;
-  if (ctx->have_hcache) {
-    p.hc_prefix = ctx->d_hc_prefix.p;
-    p.hc_cta = nullptr;  // per precision: set by the launch
-    p.n_pairs = ctx->hc_pairs;
-  }
   return p;
 }
+
+// CTAs of a launch over n_chunks warp chunks
+static int64_t lane_ctas(int64_t n_chunks) { return (n_chunks + kWarpsPerCta - 1) / kWarpsPerCta; }
 
 static DiagParams make_diag_params(fcg_ctx* ctx) {
   DiagParams p{};
@@ -1041,24 +915,11 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
   FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
   FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));
-  FCG_CUDA(ctx->d_prefix.upload(P.prefix.data(), P.prefix.size(), ctx->stream));
-  {
-    // work item holding the first triple of every closed-sigma CTA, per precision's chunk
-    std::vector<int64_t> lo32, lo64;
-    const int64_t n_items = int64_t(P.items.size());
-    auto cta_items = [&](int64_t chunk, std::vector<int64_t>& out) {
-      const int64_t n_cta = P.n_triples > 0 ? (P.n_triples + chunk - 1) / chunk : 0;
-      out.assign(size_t(n_cta) + 1, std::max<int64_t>(n_items - 1, 0));
-      for (int64_t c = 0; c < n_cta; ++c) {
-        const int64_t x = c * chunk;
-        out[c] = int64_t(std::upper_bound(P.prefix.begin(), P.prefix.begin() + n_items, x) - P.prefix.begin()) - 1;
-      }
-    };
-    cta_items(sigma_chunk<float>(), lo32);
-    cta_items(sigma_chunk<double>(), lo64);
-    FCG_CUDA(ctx->d_cta32.upload(lo32.data(), lo32.size(), ctx->stream));
-    FCG_CUDA(ctx->d_cta64.upload(lo64.data(), lo64.size(), ctx->stream));
-  }
+  FCG_REQUIRE(lane_ctas(int64_t(P.chunk_lo.size()) - 1) < (int64_t(1) << 31), FCG_ELIMIT,
+              "too many warp chunks for one launch");
+  FCG_CUDA(ctx->d_jobs.upload(P.jobs.data(), P.jobs.size(), ctx->stream));
+  FCG_CUDA(ctx->d_chunk_lo.upload(P.chunk_lo.data(), P.chunk_lo.size(), ctx->stream));
+  FCG_CUDA(ctx->d_chunk_val.upload(P.chunk_val.data(), P.chunk_val.size(), ctx->stream));
   FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
@@ -1081,44 +942,32 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
 template <typename T>
 static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig, bool zero_sig = true,
                          bool timed = true) {
-  SigmaParams p = make_sigma_params(ctx, R);
-  p.cta_lo = sizeof(T) == 4 ? ctx->d_cta32.p : ctx->d_cta64.p;
+  const LaneParams p = make_lane_params(ctx, R);
   if (zero_sig) FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
+  const int64_t grid = lane_ctas(p.n_chunks);
   int launches = 0;
-  if (ctx->have_hcache) {  // from the stored Hamiltonian blocks
+  if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+  if (grid > 0 && ctx->have_hcache) {  // from the stored Hamiltonian blocks
     const T* hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(ctx->d_hc32.p) : reinterpret_cast<const T*>(ctx->d_hc64.p);
-    p.hc_cta = sizeof(T) == 4 ? ctx->d_hc_cta32.p : ctx->d_hc_cta64.p;
-    const int64_t grid = (p.n_pairs + hc_chunk<T>() - 1) / hc_chunk<T>();
-    FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
-    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    if (grid > 0) {
-      switch (R) {
-        case 1: cached_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
-        case 2: cached_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
-        case 4: cached_sigma_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
-        default: cached_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
-      }
-      FCG_CUDA(cudaGetLastError());
-      launches = 1;
-    }
-    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-    ctx->stats.kernel_launches = launches;
-    return FCG_OK;
-  }
-  if (p.n_triples > 0) {
-    int64_t grid = (p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
-    FCG_REQUIRE(grid < (int64_t(1) << 31), FCG_ELIMIT, "too many triples for one launch");
-    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     switch (R) {
-      case 1: closed_sigma_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      case 2: closed_sigma_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      case 4: closed_sigma_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      default: closed_sigma_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      case 1: cached_sigma_lane_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+      case 2: cached_sigma_lane_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+      case 4: cached_sigma_lane_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
+      default: cached_sigma_lane_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, hc, cin, sig); break;
     }
     FCG_CUDA(cudaGetLastError());
-    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    launches = 1;
+  } else if (grid > 0) {
+    switch (R) {
+      case 1: closed_sigma_lane_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      case 2: closed_sigma_lane_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      case 4: closed_sigma_lane_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+      default: closed_sigma_lane_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
+    }
+    FCG_CUDA(cudaGetLastError());
     launches = 1;
   }
+  if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
   ctx->stats.kernel_launches = launches;
   return FCG_OK;
 }
@@ -1152,11 +1001,9 @@ static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_s
   ctx->stats.kernel_launches += 2;
   if (!wait) return FCG_OK;  // untimed: no events were recorded
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (ctx->plan.n_triples > 0 || ctx->have_hcache) {
-    float ms = 0.f;
-    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->stats.last_kernel_ms = ms;
-  }
+  float ms = 0.f;
+  FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->stats.last_kernel_ms = ms;
   return FCG_OK;
 }
 
@@ -1185,42 +1032,18 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
   if (bytes) *bytes = 0;
   if (!(max_bytes > 0)) return FCG_OK;  // 0: back to building every matrix element per sigma
   const Plan& P = ctx->plan;
-  const int64_t n_items = int64_t(P.items.size());
-  std::vector<int64_t> pre(size_t(std::max<int64_t>(n_items, 1)), 0);
-  int64_t pairs = 0;
-  for (int64_t w = 0; w < n_items; ++w) {
-    pre[w] = pairs;
-    pairs += int64_t(P.items[w].nb) * P.items[w].nk;
-  }
-  const double need = double(pairs) * double(sizeof(double) + sizeof(float)) + double(n_items) * 8.0;
+  // one float64 and one float32 value per lane and task step (lanes without a pair hold 0)
+  const int64_t pairs = P.task_values;
+  const double need = double(pairs) * double(sizeof(double) + sizeof(float));
   if (bytes) *bytes = int64_t(need);
   FCG_REQUIRE(need <= max_bytes, FCG_ELIMIT,
               "stored Hamiltonian blocks need " + std::to_string(int64_t(need)) + " bytes, over max_bytes");
-  auto cta_items = [&](int64_t chunk, std::vector<int64_t>& out) {
-    const int64_t n_cta = pairs > 0 ? (pairs + chunk - 1) / chunk : 0;
-    out.assign(size_t(n_cta) + 1, std::max<int64_t>(n_items - 1, 0));
-    for (int64_t c = 0; c < n_cta; ++c)
-      out[c] = int64_t(std::upper_bound(pre.begin(), pre.begin() + n_items, c * chunk) - pre.begin()) - 1;
-  };
-  std::vector<int64_t> lo_build, lo_sigma32, lo_sigma64;
-  cta_items(kCacheChunk, lo_build);
-  cta_items(hc_chunk<float>(), lo_sigma32);
-  cta_items(hc_chunk<double>(), lo_sigma64);
-  FCG_REQUIRE(lo_build.size() < (size_t(1) << 31), FCG_ELIMIT, "too many stored pairs for one launch");
-  FCG_CUDA(ctx->d_hc_prefix.upload(pre.data(), pre.size(), ctx->stream));
-  FCG_CUDA(ctx->d_hc_cta32.upload(lo_sigma32.data(), lo_sigma32.size(), ctx->stream));
-  FCG_CUDA(ctx->d_hc_cta64.upload(lo_sigma64.data(), lo_sigma64.size(), ctx->stream));
-  int64_t* d_lo = nullptr;
-  FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, lo_build.data(), lo_build.size(), ctx->stream, &d_lo));
   FCG_CUDA(ctx->d_hc64.alloc(size_t(std::max<int64_t>(pairs, 1))));
   FCG_CUDA(ctx->d_hc32.alloc(size_t(std::max<int64_t>(pairs, 1))));
   if (pairs > 0) {
-    SigmaParams p = make_sigma_params(ctx, 1);
-    p.hc_prefix = ctx->d_hc_prefix.p;
-    p.hc_cta = nullptr;  // the assembly walks its own chunks (cta_lo)
-    p.n_pairs = pairs;
-    hcache_build_kernel<<<unsigned(lo_build.size() - 1), kSigmaThreads, 0, ctx->stream>>>(
-        p, d_lo, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
+    const LaneParams p = make_lane_params(ctx, 1);
+    hcache_lane_build_kernel<<<unsigned(lane_ctas(p.n_chunks)), kSigmaThreads, 0, ctx->stream>>>(
+        p, ctx->d_w64.p, ctx->d_op64.p, ctx->d_hc64.p);
     FCG_CUDA(cudaGetLastError());
     to_float_kernel<<<unsigned(std::min<int64_t>((pairs + 255) / 256, 65535)), 256, 0, ctx->stream>>>(
         ctx->d_hc64.p, ctx->d_hc32.p, pairs);
@@ -1250,8 +1073,7 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
     fcg_ctx* c = ctxs[q];
     const int64_t nr = c->n_cfg * R[q];
     GroupEntry<T>& e = entries[q];
-    e.p = make_sigma_params(c, R[q]);
-    e.p.cta_lo = sizeof(T) == 4 ? c->d_cta32.p : c->d_cta64.p;
+    e.p = make_lane_params(c, R[q]);
     if (sizeof(T) == 4) {
       FCG_CUDA(c->d_c32.alloc(size_t(nr)));
       FCG_CUDA(c->d_s32.alloc(size_t(nr)));
@@ -1271,17 +1093,15 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
     e.dst = d_sigma[q];
     e.n_cfg = c->n_cfg;
     e.hc = nullptr;
+    const int64_t n_cta = lane_ctas(e.p.n_chunks);
     if (c->have_hcache) {
       e.hc = sizeof(T) == 4 ? reinterpret_cast<const T*>(c->d_hc32.p) : reinterpret_cast<const T*>(c->d_hc64.p);
       e.cta0 = cta_hc;
-      e.p.hc_cta = sizeof(T) == 4 ? c->d_hc_cta32.p : c->d_hc_cta64.p;
-      const int64_t n_cta = (e.p.n_pairs + hc_chunk<T>() - 1) / hc_chunk<T>();
       FCG_REQUIRE(cta_hc + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
       cta_problem_hc.insert(cta_problem_hc.end(), size_t(n_cta), int32_t(q));
       cta_hc += n_cta;
     } else {
       e.cta0 = cta;
-      const int64_t n_cta = (e.p.n_triples + sigma_chunk<T>() - 1) / sigma_chunk<T>();
       FCG_REQUIRE(cta + n_cta < (int64_t(1) << 31), FCG_ELIMIT, "too many CTAs for one grouped launch");
       cta_problem.insert(cta_problem.end(), size_t(n_cta), int32_t(q));
       cta += n_cta;
@@ -1520,11 +1340,9 @@ extern "C" int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, 
   FCG_CUDA(cudaGetLastError());
   ctx->stats.kernel_launches += 2;
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  if (ctx->plan.n_triples > 0 || ctx->have_hcache) {
-    float ms = 0.f;
-    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-    ctx->stats.last_kernel_ms = ms;
-  }
+  float ms = 0.f;
+  FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->stats.last_kernel_ms = ms;
   return FCG_OK;
 }
 

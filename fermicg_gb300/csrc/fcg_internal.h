@@ -4,6 +4,12 @@
 #include <string>
 #include <vector>
 
+#ifdef __CUDACC__
+#define FCG_HD __host__ __device__
+#else
+#define FCG_HD
+#endif
+
 namespace fcg {
 
 constexpr int kMaxClusters = 8;
@@ -93,6 +99,21 @@ struct WorkItem {
   int32_t ts_off;   // offset of the term list in the TermSector pool
   int32_t nt;       // number of terms
 };
+
+// A closed-sigma lane job: one bra row of a work item against up to kLaneKets of the item's
+// kets.  Warps run 32 consecutive lane jobs, one per lane; a lane sums the item's terms for
+// each of its (bra, ket) pairs, multiplies by the ket's coefficients and adds its row to
+// sigma once.  The planner orders lane jobs so that the lanes of a warp have the same term
+// shape and about the same work.
+struct LaneJob {
+  int32_t b;       // bra row
+  int32_t kp;      // offset of the first ket in the permutation pool
+  int32_t ts_off;  // the item's term-sector records
+  uint16_t len;    // kets (0: an idle lane)
+  uint16_t nt;     // terms
+};
+static_assert(sizeof(LaneJob) == 16, "LaneJob layout");
+constexpr int kLaneKets = 32;
 
 // One W block to compute (fcg_set_terms): term t dressed with TDM block g of its dressed cluster.
 struct DressJob {
@@ -197,13 +218,19 @@ struct Plan {
   int64_t flops_ref = 0;        // sum over triples of 2*len(ints) (the reference's count)
   int64_t flops_dressed = 0;    // multiply-adds actually done per sigma (x2), excluding the R update
   std::vector<int32_t> zero_terms;
+  // lane jobs (32 per warp task, the last warp task padded with idle lanes) and the warp
+  // chunks: chunk c runs warp tasks [chunk_lo[c], chunk_lo[c+1]) (about kChunkCost of work);
+  // chunk_val[c] is the first stored value of the chunk (32 per ket step of each warp task)
+  std::vector<LaneJob> jobs;
+  std::vector<int64_t> chunk_lo;
+  std::vector<int64_t> chunk_val;
+  int64_t task_values = 0;      // 32 x the longest lane job of every warp task, summed
 };
 
-#ifdef __CUDACC__
-#define FCG_HD __host__ __device__
-#else
-#define FCG_HD
-#endif
+// work of one warp chunk of the closed sigma, in the planner's cost units (about one unit
+// per multiply-add or load of a lane's ket step)
+constexpr int64_t kChunkCost = int64_t(1) << 13;
+
 
 FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int fbb, int fka, int fkb) {
   return ((((int64_t(c) * kNumOps + op) * nmax1 + fba) * nmax1 + fbb) * nmax1 + fka) * nmax1 + fkb;

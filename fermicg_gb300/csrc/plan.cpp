@@ -8,8 +8,9 @@
 // local states on the untouched clusters), and for each (bra sector,
 // transfer, active set) the bra and ket key lists are merge-joined.  Each
 // matching key gives one work item = a dense block of (bra, ket, term)
-// triples that all pass check_term.  The kernel walks the flattened triple
-// space of all work items.
+// triples that all pass check_term.  Each bra row of a work item, with up to
+// 32 of its kets, becomes one lane job of the sigma kernel; lane jobs are
+// sorted so that a warp's 32 lanes do the same kind and amount of work.
 #include <algorithm>
 #include <cstring>
 #include <unordered_map>
@@ -39,6 +40,13 @@ struct Group {
   uint64_t key;
   int32_t start;  // relative to the (sector, set) permutation
   int32_t count;
+};
+
+// A lane job while planning: its term shape (nbody) and planner cost ride along for the sort.
+struct PJob {
+  LaneJob j;
+  int32_t cost;
+  int32_t nbody;
 };
 
 }  // namespace
@@ -212,6 +220,7 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
   // thread timing
   std::vector<std::vector<WorkItem>> tItems(n_sec);
   std::vector<std::vector<TermSector>> tTS(n_sec);
+  std::vector<std::vector<PJob>> tJobs(n_sec);
   std::vector<int64_t> tFlop(n_sec, 0), tFlopD(n_sec, 0);
 #pragma omp parallel
   {
@@ -256,6 +265,10 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
           }
           const int32_t ts_off = int32_t(tTS[sb].size());  // relative; rebased at concatenation
           tTS[sb].insert(tTS[sb].end(), tsl.begin(), tsl.end());
+          // one lane step (one ket): every term's multiply-adds, about 8 loads and index steps
+          // per term, and the coefficient update
+          const int64_t step_cost = flopd / 2 + 8 * int64_t(tsl.size()) + 4;
+          const int nbody_tl = TT(trm, tl.terms[0], 0);
           const auto& gb = groups[sb * n_sets + tl.s];
           const auto& gk = groups[sk * n_sets + tl.s];
           int64_t pb = fs_perm_off[sb * n_sets + tl.s], pk = fs_perm_off[sk * n_sets + tl.s];
@@ -274,6 +287,18 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
               w.ts_off = ts_off;
               w.nt = int32_t(tsl.size());
               tItems[sb].push_back(w);
+              for (int bj = 0; bj < w.nb; ++bj)
+                for (int k0 = 0; k0 < w.nk; k0 += kLaneKets) {
+                  PJob pj;
+                  pj.j.b = P.perm_pool[size_t(w.bra_off) + bj];
+                  pj.j.kp = w.ket_off + k0;
+                  pj.j.ts_off = w.ts_off;  // relative; rebased at concatenation
+                  pj.j.len = uint16_t(std::min(kLaneKets, w.nk - k0));
+                  pj.j.nt = uint16_t(w.nt);
+                  pj.cost = int32_t(std::min<int64_t>(step_cost * pj.j.len, int64_t(1) << 30));
+                  pj.nbody = nbody_tl;
+                  tJobs[sb].push_back(pj);
+                }
               tFlop[sb] += int64_t(w.nb) * w.nk * flop;
               tFlopD[sb] += int64_t(w.nb) * w.nk * flopd;
               ++a;
@@ -290,17 +315,72 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
     tots += tTS[sb].size();
   }
   if (tots >= (size_t(1) << 31)) return "term-sector pool exceeds 2^31 records";
+  if (tot >= (size_t(1) << 31)) return "work items exceed 2^31";
   P.items.reserve(tot);
   P.ts_pool.reserve(tots);
+  std::vector<int64_t> job_off(n_sec + 1, 0);
+  for (int64_t sb = 0; sb < n_sec; ++sb) job_off[sb + 1] = job_off[sb] + int64_t(tJobs[sb].size());
+  std::vector<PJob> pj(static_cast<size_t>(job_off[n_sec]));
   for (int64_t sb = 0; sb < n_sec; ++sb) {
     const int32_t base = int32_t(P.ts_pool.size());
     for (WorkItem w : tItems[sb]) {
       w.ts_off += base;
       P.items.push_back(w);
     }
+    PJob* dst = &pj[size_t(job_off[sb])];
+    for (const PJob& q : tJobs[sb]) {
+      *dst = q;
+      dst->j.ts_off += base;
+      ++dst;
+    }
     P.ts_pool.insert(P.ts_pool.end(), tTS[sb].begin(), tTS[sb].end());
     P.flops_ref += tFlop[sb];
     P.flops_dressed += tFlopD[sb];
+  }
+  // Lane jobs of windows of kSortWindow bra sectors sorted by term shape, then by decreasing
+  // cost (stable: the rows of one work item stay together and share their kets), so that the
+  // 32 lanes of a warp run the same code on about the same number of kets.
+  {
+    constexpr int64_t kSortWindow = 8;
+    const int64_t n_win = (n_sec + kSortWindow - 1) / kSortWindow;
+#pragma omp parallel for schedule(dynamic, 1)
+    for (int64_t wdx = 0; wdx < n_win; ++wdx) {
+      const int64_t a = job_off[wdx * kSortWindow], b = job_off[std::min(n_sec, (wdx + 1) * kSortWindow)];
+      std::stable_sort(pj.begin() + a, pj.begin() + b, [](const PJob& x, const PJob& y) {
+        return x.nbody != y.nbody ? x.nbody < y.nbody : x.cost > y.cost;
+      });
+    }
+  }
+  const int64_t n_jobs = int64_t(pj.size());
+  const int64_t n_wt = (n_jobs + 31) / 32;  // warp tasks
+  P.jobs.assign(size_t(n_wt) * 32, LaneJob{0, 0, 0, 0, 0});
+  for (int64_t i = 0; i < n_jobs; ++i) P.jobs[size_t(i)] = pj[size_t(i)].j;
+  // warp chunks: chunk c starts at the first warp task whose cost prefix reaches c * kChunkCost
+  // (a warp task costs its most expensive lane)
+  {
+    std::vector<int32_t> wt_cost(size_t(n_wt), 0);
+    std::vector<int32_t> wt_len(size_t(n_wt), 0);
+    for (int64_t i = 0; i < n_jobs; ++i) {
+      wt_cost[size_t(i / 32)] = std::max(wt_cost[size_t(i / 32)], pj[size_t(i)].cost);
+      wt_len[size_t(i / 32)] = std::max<int32_t>(wt_len[size_t(i / 32)], pj[size_t(i)].j.len);
+    }
+    int64_t total = 0;
+    for (int32_t c : wt_cost) total += c;
+    const int64_t n_chunks = (total + kChunkCost - 1) / kChunkCost;
+    P.chunk_lo.assign(size_t(n_chunks) + 1, n_wt);
+    P.chunk_val.assign(size_t(n_chunks) + 1, 0);
+    int64_t cum = 0, vals = 0, c = 0;
+    for (int64_t i = 0; i < n_wt; ++i) {
+      while (c < n_chunks && cum >= c * kChunkCost) {
+        P.chunk_lo[size_t(c)] = i;
+        P.chunk_val[size_t(c)] = vals;
+        ++c;
+      }
+      cum += wt_cost[size_t(i)];
+      vals += 32 * int64_t(wt_len[size_t(i)]);
+    }
+    for (; c <= n_chunks; ++c) P.chunk_val[size_t(c)] = vals;
+    P.task_values = vals;
   }
   P.prefix.assign(P.items.size() + 1, 0);
   for (size_t i = 0; i < P.items.size(); ++i)
