@@ -953,6 +953,8 @@ def main():
         "e2e": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": n * R * 8,
                 "d2h_bytes_per_step": n * R * 8},
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
+        "tuning": dict(g.tuning(), note="closed-sigma kernel candidate chosen by the library's tuner on the "
+                                        "first sigma of each precision (index into candidates)"),
         "clocks": clocks,
     }
     if stored is not None:

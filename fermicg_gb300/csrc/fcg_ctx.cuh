@@ -117,6 +117,14 @@ struct fcg_ctx {
   DevBuf<LaneJob> d_jobs;           // closed-sigma lane jobs, 32 per warp task
   DevBuf<int64_t> d_chunk_lo;       // first warp task of each warp chunk
   DevBuf<int64_t> d_chunk_val;      // first stored value of each warp chunk
+  // closed-sigma kernel tuning: candidate per precision (0 fp64, 1 fp32; -1 not yet tuned),
+  // forced candidate (-1: auto), the finer chunk table of candidates 2-3, candidate timings
+  int tuned[2] = {-1, -1};
+  int tune_mode = -1;
+  bool fine_built = false;
+  DevBuf<int64_t> d_chunk_lo_fine, d_chunk_val_fine;
+  int64_t n_chunks_fine = 0;
+  float tune_ms[2][4] = {};
   DevBuf<int32_t> d_perm;
   DevBuf<TermSector> d_ts;
   DevBuf<unsigned char> d_group;    // entries of the last grouped closed sigma led by this context

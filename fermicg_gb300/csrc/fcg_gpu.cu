@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <chrono>
+#include <map>
 #include <mutex>
 #include <cstdio>
 #include <cstring>
@@ -257,12 +258,7 @@ __device__ __forceinline__ T dressed_element(const TermSector& ts, const T* __re
 constexpr int kSigmaThreads = 256;       // 8 warps per CTA
 constexpr int kWarpsPerCta = kSigmaThreads / 32;
 constexpr int kMaxR = 16;
-#ifndef FCG_LANE_MINB32
-#define FCG_LANE_MINB32 4
-#endif
-#ifndef FCG_LANE_MINB64
-#define FCG_LANE_MINB64 3
-#endif
+constexpr int kTuneCandidates = 4;  // closed-sigma kernel candidates of the tuner
 
 struct LaneParams {
   const LaneJob* jobs;       // 32 per warp task
@@ -351,8 +347,9 @@ __device__ __forceinline__ void closed_lane_warp(const LaneParams& p, const T* _
   }
 }
 
-template <typename T, int RR>
-__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_LANE_MINB32 : FCG_LANE_MINB64)
+// MINB: resident CTAs per SM the register allocation is sized for (a tuning candidate)
+template <typename T, int RR, int MINB>
+__global__ void __launch_bounds__(kSigmaThreads, MINB)
     closed_sigma_lane_kernel(LaneParams p, const T* __restrict__ w, const T* __restrict__ op,
                              const T* __restrict__ cin, T* __restrict__ sig) {
   const int64_t chunk = int64_t(blockIdx.x) * kWarpsPerCta + (threadIdx.x >> 5);
@@ -451,7 +448,7 @@ struct GroupEntry {
 };
 
 template <typename T, int RMAX>
-__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? FCG_LANE_MINB32 : FCG_LANE_MINB64)
+__global__ void __launch_bounds__(kSigmaThreads, sizeof(T) == 4 ? 4 : 3)
     closed_sigma_grouped_kernel(const GroupEntry<T>* __restrict__ g, const int32_t* __restrict__ cta_problem) {
   const GroupEntry<T>& e = g[__ldg(cta_problem + blockIdx.x)];
   const LaneParams p = e.p;
@@ -933,15 +930,147 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   ctx->stats.flops_executed = P.flops_dressed;
   ctx->stats.dressed_elements = ctx->n_w;
   ctx->stats.plan_seconds = std::chrono::duration<double>(t1 - t0).count();
+  ctx->tuned[0] = ctx->tuned[1] = -1;  // a new shape: tune again (or find it in the shape cache)
+  ctx->fine_built = false;
   ctx->have_state = true;
+  return FCG_OK;
+}
+
+int fcg_set_tuning(fcg_ctx* ctx, int mode) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(mode >= -1 && mode < kTuneCandidates, FCG_EINVAL, "tuning mode must be -1 (auto) or a candidate 0..3");
+  ctx->tune_mode = mode;
+  return FCG_OK;
+}
+
+int fcg_tuning(const fcg_ctx* ctx, int* chosen, float* candidate_ms) {
+  if (!ctx || !chosen) return FCG_EINVAL;
+  for (int prec = 0; prec < 2; ++prec) {
+    chosen[prec] = ctx->tune_mode >= 0 ? ctx->tune_mode : ctx->tuned[prec];
+    if (candidate_ms)
+      for (int c = 0; c < kTuneCandidates; ++c) candidate_ms[prec * kTuneCandidates + c] = ctx->tune_ms[prec][c];
+  }
   return FCG_OK;
 }
 
 }  // extern "C"
 
+// ---- closed-sigma kernel tuning ---------------------------------------------------------
+// Candidates per precision: the lane kernel compiled for two occupancy targets (float 4 or 3
+// CTAs per SM, double 3 or 2) x two chunk granularities (about 4 or 16 waves of resident warps).
+// Candidate c: occupancy variant c & 1, chunk table c >> 1.
+template <typename T>
+constexpr int tune_minb(int variant) {
+  return sizeof(T) == 4 ? (variant ? 3 : 4) : (variant ? 2 : 3);
+}
+
+namespace {
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tune_cache;  // shape key -> candidate, for this process
+
+std::string tune_key(const fcg_ctx* ctx, int prec, int R) {
+  const Plan& P = ctx->plan;
+  return std::to_string(prec) + "/" + std::to_string(R) + "/" + std::to_string(ctx->N) + "/" +
+         std::to_string(ctx->n_cfg) + "/" + std::to_string(ctx->n_terms) + "/" + std::to_string(P.n_triples) + "/" +
+         std::to_string(P.jobs.size()) + "/" + std::to_string(ctx->device);
+}
+}  // namespace
+
+// the finer chunk table of the tuning candidates (built on first use)
+static int fine_chunks(fcg_ctx* ctx) {
+  if (ctx->fine_built) return FCG_OK;
+  std::vector<int64_t> lo, val;
+  make_chunks(ctx->plan, 4 * kTargetChunks, lo, val);
+  FCG_REQUIRE(lane_ctas(int64_t(lo.size()) - 1) < (int64_t(1) << 31), FCG_ELIMIT, "too many warp chunks for one launch");
+  FCG_CUDA(ctx->d_chunk_lo_fine.upload(lo.data(), lo.size(), ctx->stream));
+  FCG_CUDA(ctx->d_chunk_val_fine.upload(val.data(), val.size(), ctx->stream));
+  ctx->n_chunks_fine = int64_t(lo.size()) - 1;
+  ctx->fine_built = true;
+  return FCG_OK;
+}
+
+template <typename T, int MINB>
+static void launch_lane(const LaneParams& p, int64_t grid, int R, const T* w, const T* op, const T* cin, T* sig,
+                        cudaStream_t s) {
+  switch (R) {
+    case 1: closed_sigma_lane_kernel<T, 1, MINB><<<unsigned(grid), kSigmaThreads, 0, s>>>(p, w, op, cin, sig); break;
+    case 2: closed_sigma_lane_kernel<T, 2, MINB><<<unsigned(grid), kSigmaThreads, 0, s>>>(p, w, op, cin, sig); break;
+    case 4: closed_sigma_lane_kernel<T, 4, MINB><<<unsigned(grid), kSigmaThreads, 0, s>>>(p, w, op, cin, sig); break;
+    default: closed_sigma_lane_kernel<T, 0, MINB><<<unsigned(grid), kSigmaThreads, 0, s>>>(p, w, op, cin, sig); break;
+  }
+}
+
+// one direct closed sigma with candidate c
+template <typename T>
+static int launch_candidate(fcg_ctx* ctx, int c, int R, const T* w, const T* op, const T* cin, T* sig) {
+  LaneParams p = make_lane_params(ctx, R);
+  if (c >> 1) {
+    const int rc = fine_chunks(ctx);
+    if (rc) return rc;
+    p.chunk_lo = ctx->d_chunk_lo_fine.p;
+    p.chunk_val = ctx->d_chunk_val_fine.p;
+    p.n_chunks = ctx->n_chunks_fine;
+  }
+  const int64_t grid = lane_ctas(p.n_chunks);
+  if (grid == 0) return FCG_OK;
+  if (c & 1)
+    launch_lane<T, tune_minb<T>(1)>(p, grid, R, w, op, cin, sig, ctx->stream);
+  else
+    launch_lane<T, tune_minb<T>(0)>(p, grid, R, w, op, cin, sig, ctx->stream);
+  FCG_CUDA(cudaGetLastError());
+  return FCG_OK;
+}
+
+// Times every candidate once on this state (each run a complete sigma into sig), keeps the
+// fastest for the context and for later states of the same shape in this process.
+template <typename T>
+static int tune_closed(fcg_ctx* ctx, int prec, int R, const T* w, const T* op, const T* cin, T* sig) {
+  const auto t0 = std::chrono::steady_clock::now();
+  const std::string key = tune_key(ctx, prec, R);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      ctx->tuned[prec] = it->second;
+      ctx->stats.tune_cache_hits += 1;
+      return FCG_OK;
+    }
+  }
+  float best = 0.f;
+  int best_c = 0;
+  for (int c = 0; c < kTuneCandidates; ++c) {
+    FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
+    FCG_CUDA(cudaEventRecord(ctx->ev2, ctx->stream));
+    const int rc = launch_candidate<T>(ctx, c, R, w, op, cin, sig);
+    if (rc) return rc;
+    FCG_CUDA(cudaEventRecord(ctx->ev3, ctx->stream));
+    FCG_CUDA(cudaEventSynchronize(ctx->ev3));
+    float ms = 0.f;
+    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
+    ctx->tune_ms[prec][c] = ms;
+    if (c == 0 || ms < best) {
+      best = ms;
+      best_c = c;
+    }
+  }
+  ctx->tuned[prec] = best_c;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = best_c;
+  }
+  ctx->stats.tune_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  return FCG_OK;
+}
+
 template <typename T>
 static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig, bool zero_sig = true,
                          bool timed = true) {
+  const int prec = sizeof(T) == 4 ? 1 : 0;
+  if (!ctx->have_hcache && ctx->tune_mode < 0 && ctx->tuned[prec] < 0 && timed) {
+    const int rc = tune_closed<T>(ctx, prec, R, w, op, cin, sig);
+    if (rc) return rc;
+    zero_sig = true;  // the tuning runs left a sigma behind
+  }
   const LaneParams p = make_lane_params(ctx, R);
   if (zero_sig) FCG_CUDA(cudaMemsetAsync(sig, 0, sizeof(T) * size_t(ctx->n_cfg) * R, ctx->stream));
   const int64_t grid = lane_ctas(p.n_chunks);
@@ -958,13 +1087,9 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* 
     FCG_CUDA(cudaGetLastError());
     launches = 1;
   } else if (grid > 0) {
-    switch (R) {
-      case 1: closed_sigma_lane_kernel<T, 1><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      case 2: closed_sigma_lane_kernel<T, 2><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      case 4: closed_sigma_lane_kernel<T, 4><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-      default: closed_sigma_lane_kernel<T, 0><<<unsigned(grid), kSigmaThreads, 0, ctx->stream>>>(p, w, op, cin, sig); break;
-    }
-    FCG_CUDA(cudaGetLastError());
+    const int c = ctx->tune_mode >= 0 ? ctx->tune_mode : (ctx->tuned[prec] >= 0 ? ctx->tuned[prec] : 0);
+    const int rc = launch_candidate<T>(ctx, c, R, w, op, cin, sig);
+    if (rc) return rc;
     launches = 1;
   }
   if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));

@@ -225,11 +225,21 @@ struct Plan {
   std::vector<int64_t> chunk_lo;
   std::vector<int64_t> chunk_val;
   int64_t task_values = 0;      // 32 x the longest lane job of every warp task, summed
+  std::vector<int32_t> wt_cost;  // planner cost of every warp task (its most expensive lane)
+  std::vector<int32_t> wt_len;   // longest lane job of every warp task
 };
 
+// Warp chunks of about `target` chunks over the plan's warp tasks (chunk c runs warp tasks
+// [lo[c], lo[c+1]); val[c] is its first stored value).
+void make_chunks(const Plan& P, int64_t target, std::vector<int64_t>& lo, std::vector<int64_t>& val);
+
 // work of one warp chunk of the closed sigma, in the planner's cost units (about one unit
-// per multiply-add or load of a lane's ket step)
+// per multiply-add or load of a lane's ket step): the total cut into about kTargetChunks
+// chunks (four waves of 32 resident warps on each of 152 SMs), each within
+// [kMinChunkCost, kChunkCost]
 constexpr int64_t kChunkCost = int64_t(1) << 13;
+constexpr int64_t kMinChunkCost = 256;
+constexpr int64_t kTargetChunks = 4 * 152 * 32;
 
 
 FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int fbb, int fka, int fkb) {

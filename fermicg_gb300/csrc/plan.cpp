@@ -355,38 +355,44 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
   const int64_t n_wt = (n_jobs + 31) / 32;  // warp tasks
   P.jobs.assign(size_t(n_wt) * 32, LaneJob{0, 0, 0, 0, 0});
   for (int64_t i = 0; i < n_jobs; ++i) P.jobs[size_t(i)] = pj[size_t(i)].j;
-  // warp chunks: chunk c starts at the first warp task whose cost prefix reaches c * kChunkCost
-  // (a warp task costs its most expensive lane)
-  {
-    std::vector<int32_t> wt_cost(size_t(n_wt), 0);
-    std::vector<int32_t> wt_len(size_t(n_wt), 0);
-    for (int64_t i = 0; i < n_jobs; ++i) {
-      wt_cost[size_t(i / 32)] = std::max(wt_cost[size_t(i / 32)], pj[size_t(i)].cost);
-      wt_len[size_t(i / 32)] = std::max<int32_t>(wt_len[size_t(i / 32)], pj[size_t(i)].j.len);
-    }
-    int64_t total = 0;
-    for (int32_t c : wt_cost) total += c;
-    const int64_t n_chunks = (total + kChunkCost - 1) / kChunkCost;
-    P.chunk_lo.assign(size_t(n_chunks) + 1, n_wt);
-    P.chunk_val.assign(size_t(n_chunks) + 1, 0);
-    int64_t cum = 0, vals = 0, c = 0;
-    for (int64_t i = 0; i < n_wt; ++i) {
-      while (c < n_chunks && cum >= c * kChunkCost) {
-        P.chunk_lo[size_t(c)] = i;
-        P.chunk_val[size_t(c)] = vals;
-        ++c;
-      }
-      cum += wt_cost[size_t(i)];
-      vals += 32 * int64_t(wt_len[size_t(i)]);
-    }
-    for (; c <= n_chunks; ++c) P.chunk_val[size_t(c)] = vals;
-    P.task_values = vals;
+  P.wt_cost.assign(size_t(n_wt), 0);
+  P.wt_len.assign(size_t(n_wt), 0);
+  for (int64_t i = 0; i < n_jobs; ++i) {
+    P.wt_cost[size_t(i / 32)] = std::max(P.wt_cost[size_t(i / 32)], pj[size_t(i)].cost);
+    P.wt_len[size_t(i / 32)] = std::max<int32_t>(P.wt_len[size_t(i / 32)], pj[size_t(i)].j.len);
   }
+  P.task_values = 0;
+  for (int32_t l : P.wt_len) P.task_values += 32 * int64_t(l);
+  make_chunks(P, kTargetChunks, P.chunk_lo, P.chunk_val);
   P.prefix.assign(P.items.size() + 1, 0);
   for (size_t i = 0; i < P.items.size(); ++i)
     P.prefix[i + 1] = P.prefix[i] + int64_t(P.items[i].nb) * P.items[i].nk * P.items[i].nt;
   P.n_triples = P.prefix.back();
   return "";
+}
+
+void make_chunks(const Plan& P, int64_t target, std::vector<int64_t>& lo, std::vector<int64_t>& val) {
+  // chunk c starts at the first warp task whose cost prefix reaches c times the chunk cost;
+  // each chunk holds about 1 / target of the work, within [kMinChunkCost, kChunkCost]
+  const int64_t n_wt = int64_t(P.wt_cost.size());
+  int64_t total = 0;
+  for (int32_t c : P.wt_cost) total += c;
+  const int64_t chunk_cost =
+      std::max<int64_t>(kMinChunkCost, std::min<int64_t>(kChunkCost, total / std::max<int64_t>(target, 1)));
+  const int64_t n_chunks = (total + chunk_cost - 1) / chunk_cost;
+  lo.assign(size_t(n_chunks) + 1, n_wt);
+  val.assign(size_t(n_chunks) + 1, 0);
+  int64_t cum = 0, vals = 0, c = 0;
+  for (int64_t i = 0; i < n_wt; ++i) {
+    while (c < n_chunks && cum >= c * chunk_cost) {
+      lo[size_t(c)] = i;
+      val[size_t(c)] = vals;
+      ++c;
+    }
+    cum += P.wt_cost[size_t(i)];
+    vals += 32 * int64_t(P.wt_len[size_t(i)]);
+  }
+  for (; c <= n_chunks; ++c) val[size_t(c)] = vals;
 }
 
 std::string build_dress(int N, const std::vector<int>& norb, int nmax, const std::vector<int32_t>& trm, int n_terms,

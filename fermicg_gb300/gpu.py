@@ -19,6 +19,12 @@ from .local_fci import N_OPS
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_build", "libfcg_gpu.so")
 
+# closed-sigma kernel candidates of the library's tuner (index -> description)
+TUNE_CANDIDATES = ["4 (float) / 3 (double) CTAs per SM, ~4 waves of warp chunks",
+                   "3 (float) / 2 (double) CTAs per SM, ~4 waves of warp chunks",
+                   "4 (float) / 3 (double) CTAs per SM, ~16 waves of warp chunks",
+                   "3 (float) / 2 (double) CTAs per SM, ~16 waves of warp chunks"]
+
 FCG_FP64 = 0
 FCG_FP32 = 1
 PRECISION = {"fp64": FCG_FP64, "fp32": FCG_FP32, "mixed": FCG_FP32}
@@ -46,6 +52,8 @@ SIGNATURES = {
                           ctypes.POINTER(_I)]),
     "fcg_sigma_closed_noalloc": (_I, [_P, _I, _P, _P, _I]),
     "fcg_get_stats": (_I, [_P, _P]),
+    "fcg_set_tuning": (_I, [_P, _I]),
+    "fcg_tuning": (_I, [_P, _P, _P]),
     "fcg_bst_set": (_I, [_P, _I, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
     "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
     "fcg_bst_set_between": (_I, [_P, _I, _L, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
@@ -85,7 +93,8 @@ class Stats(ctypes.Structure):
                 ("group_wait_seconds", ctypes.c_double), ("hcache_pairs", ctypes.c_int64),
                 ("hcache_bytes", ctypes.c_int64), ("hcache_seconds", ctypes.c_double),
                 ("open_expand_ms", ctypes.c_double), ("open_flops_reference", ctypes.c_int64),
-                ("open_bytes", ctypes.c_int64)]
+                ("open_bytes", ctypes.c_int64), ("tune_seconds", ctypes.c_double),
+                ("tune_cache_hits", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -348,6 +357,19 @@ class GpuSigma:
         self._check(self.L.fcg_bst_fois_get(self.h, _ptr(of), _ptr(ob), _ptr(oo), _ptr(ofa), _ptr(oc)),
                     "fcg_bst_fois_get")
         return of, ob, oo, ofa[:nf.value], oc[:, :ct.value]
+
+    def set_tuning(self, mode: int = -1):
+        """Closed-sigma kernel candidate: -1 times the candidates on the first sigma of each
+        precision (default), 0..3 forces one."""
+        self._check(self.L.fcg_set_tuning(self.h, int(mode)), "fcg_set_tuning")
+
+    def tuning(self):
+        """{"fp64": candidate, "fp32": candidate (-1: not tuned yet), "candidate_ms": {...}}"""
+        ch = (ctypes.c_int * 2)()
+        ms = (ctypes.c_float * 8)()
+        self._check(self.L.fcg_tuning(self.h, ch, ms), "fcg_tuning")
+        return {"fp64": ch[0], "fp32": ch[1], "candidate_ms": {"fp64": list(ms[:4]), "fp32": list(ms[4:])},
+                "candidates": TUNE_CANDIDATES}
 
     def stats(self):
         s = Stats()

@@ -84,6 +84,8 @@ typedef struct fcg_stats {
   double open_expand_ms;    /* device time of the expansion kernel of the last open sigma (CUDA events) */
   int64_t open_flops_reference; /* the reference's GEMM flops of the last open sigma's jobs (no prescreen) */
   int64_t open_bytes;       /* its compulsory bytes: TDM blocks touched, C, output rows */
+  double tune_seconds;      /* host time spent timing closed-sigma kernel candidates */
+  int64_t tune_cache_hits;  /* tunings answered from the process's shape cache */
 } fcg_stats;
 
 int fcg_version(void);
@@ -303,6 +305,17 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
  * {rank, start, len}, factor_off [n][N], factors [n_factors], cores [R][core_total]. */
 int fcg_bst_fois_get(fcg_ctx* ctx, int16_t* fock, int64_t* blocks, int64_t* factor_off, double* factors,
                      double* cores);
+
+/* Closed-sigma kernel tuning (no counterpart in the reference: its matvec has no kernel
+ * variants).  The library has four candidates per precision (two occupancy targets x two
+ * chunk granularities of the lane kernel).  With mode -1 (the default) the first timed sigma
+ * of each precision on a state runs every candidate once, keeps the fastest for the context
+ * and remembers it for later states of the same shape (configurations, terms, triples) in
+ * this process; 0..3 forces a candidate.  fcg_state_set clears the choice.  fcg_tuning
+ * reports the candidate in use per precision (chosen[0] double, chosen[1] float; -1: not
+ * tuned yet) and, when candidate_ms is given (8 floats), the timings of the last tuning. */
+int fcg_set_tuning(fcg_ctx* ctx, int mode);
+int fcg_tuning(const fcg_ctx* ctx, int* chosen, float* candidate_ms);
 
 /* Allocation-free variant of fcg_sigma_closed_device (no counterpart in the reference).
  * For callers that cannot call cudaMalloc/cudaFree during a solve: applications whose
