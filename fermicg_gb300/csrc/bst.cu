@@ -25,6 +25,7 @@
 #include <vector>
 
 #include "fcg_ctx.cuh"
+#include "tcgen05.cuh"
 
 using namespace fcg;
 
@@ -245,13 +246,13 @@ __device__ __forceinline__ void prefetch_range(const void* p, int64_t bytes, int
 // every (bra active column kb, spectator index s, root) is one dot product of length k of
 // two contiguous vectors, OP[:, kb] and X[:, s], taken by a sub-warp of `lanes` threads
 // (power of two, <= 32) and added to out[r * out_stride + bra core index].
-template <typename T, int TEAM, bool ATOMIC>
-__device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ op, const T* __restrict__ S,
-                                const int32_t* __restrict__ perm, const T* __restrict__ cin, int64_t core_total,
-                                T* ws, int stride, T* out, int64_t out_stride) {
+// Steps 1-2 of a group (the GEMM operand X of every root), by a team; X of root r ends in
+// ws[(2 r + cur) * stride], cur = nsp & 1, which is returned.
+template <typename T, int TEAM>
+__device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__ S, const int32_t* __restrict__ perm,
+                                 const T* __restrict__ cin, int64_t core_total, T* ws, int stride) {
   const int tid = TEAM == 32 ? int(threadIdx.x & 31) : int(threadIdx.x);
-  const int k = G.k, m = G.m, na = G.na, nsp = G.nsp;
-  prefetch_range<TEAM, true>(op + G.op_off, int64_t(m) * k * int64_t(sizeof(T)), tid);
+  const int k = G.k, nsp = G.nsp;
   // 1. gather the ket cores in X order (the ket's actives-first index table)
   {
     const int n = G.kcore;
@@ -286,6 +287,17 @@ __device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ 
       inner *= rb;
     }
   }
+  return cur;
+}
+
+template <typename T, int TEAM, bool ATOMIC>
+__device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ op, const T* __restrict__ S,
+                                const int32_t* __restrict__ perm, const T* __restrict__ cin, int64_t core_total,
+                                T* ws, int stride, T* out, int64_t out_stride) {
+  const int tid = TEAM == 32 ? int(threadIdx.x & 31) : int(threadIdx.x);
+  const int k = G.k, m = G.m, nsp = G.nsp;
+  prefetch_range<TEAM, true>(op + G.op_off, int64_t(m) * k * int64_t(sizeof(T)), tid);
+  const int cur = bst_group_prepare<T, TEAM>(G, R, S, perm, cin, core_total, ws, stride);
   // 3. bra core[kb, s] += OP[:, kb] . X[:, s]; position col + m*s of the bra's actives-first
   // layout is bra core index bp[col + m*s]
   int ns = 1;
@@ -427,6 +439,162 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int
                                           core_total);
     __syncthreads();
   }
+}
+
+
+// ---- tensor-core path (float builds) -------------------------------------------------------
+// Groups whose product bra[m x ns] += OP^T[m x k] X[k x ns] (per root) is GEMM-shaped run on
+// the tcgen05 tensor cores: bst_tc_prep_kernel writes each group's operand X (steps 1-2 of
+// bst_group_apply) to a global workspace, then bst_tc_gemm_kernel computes 128 x N tiles of
+// D = A B^T with A[i][kk] = OP[kk + k i] and B[j][kk] = X_r[kk + k s] (j = s + ns r, the R
+// roots side by side), in three TF32 products per K step (hi*hi + hi*lo + lo*hi, each
+// operand split as x = hi + lo) accumulated in FP32 in tensor memory, and adds D into the bra
+// cores through the bra's actives-first index table.
+struct BstTcJob {
+  int32_t tc;  // position in the tensor-core group list
+  int32_t g;   // group
+  int32_t m0;  // first bra-active row of the tile
+  int32_t n0;  // first column (spectator index + ns * root) of the tile
+};
+
+constexpr int kTcThreads = 128;  // one warpgroup: thread i owns TMEM lane / tile row i
+constexpr int kTcM = 128;        // tile rows (MMA M)
+constexpr int kTcN = 256;        // tile columns at most (MMA N, a multiple of 16)
+constexpr int kTcK = 32;         // K elements staged per round: four 8-element MMA steps
+constexpr int kTcTmemCols = 256;
+constexpr int kTcSmem = 2 * kTcM * kTcK * 4 + 2 * kTcN * kTcK * 4 + 64;
+constexpr long long kTcWaitCycles = 4000000000LL;  // about 2 s at 2 GHz: a stuck MMA becomes an error
+// groups that go to the tensor cores: at least kTcMinM bra-active rows, kTcMinK ket-active
+// columns and kTcMinN spectator columns over all roots
+constexpr int kTcMinM = 64, kTcMinK = 16, kTcMinN = 32;
+
+__global__ void __launch_bounds__(kBstThreads) bst_tc_prep_kernel(const int32_t* __restrict__ list,
+                                                                  const int64_t* __restrict__ ws_off,
+                                                                  const BstGroup* __restrict__ groups, int R,
+                                                                  const float* __restrict__ S,
+                                                                  const int32_t* __restrict__ perm,
+                                                                  const float* __restrict__ cin, int64_t core_total,
+                                                                  float* __restrict__ ws_all) {
+  __shared__ __align__(16) BstGroup G;
+  load_group<kBstThreads>(groups + list[blockIdx.x], &G, threadIdx.x);
+  bst_group_prepare<float, kBstThreads>(G, R, S, perm, cin, core_total, ws_all + ws_off[blockIdx.x], G.ws);
+}
+
+__global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJob* __restrict__ jobs,
+                                                                   const BstGroup* __restrict__ groups, int R,
+                                                                   const float* __restrict__ op,
+                                                                   const float* __restrict__ ws_all,
+                                                                   const int64_t* __restrict__ ws_off,
+                                                                   const int32_t* __restrict__ perm,
+                                                                   float* __restrict__ cout, int64_t core_total,
+                                                                   unsigned* __restrict__ err) {
+  extern __shared__ __align__(1024) unsigned char tc_smem[];
+  unsigned char* a_hi = tc_smem;
+  unsigned char* a_lo = a_hi + kTcM * kTcK * 4;
+  unsigned char* b_hi = a_lo + kTcM * kTcK * 4;
+  unsigned char* b_lo = b_hi + kTcN * kTcK * 4;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(b_lo + kTcN * kTcK * 4);
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const BstTcJob J = jobs[blockIdx.x];
+  const BstGroup& G = groups[J.g];
+  const int m = G.m, k = G.k, ns = G.bcore / G.m, NT = ns * R;
+  const int rows = min(kTcM, m - J.m0), cols = min(kTcN, NT - J.n0);
+  const int nI = (cols + 15) & ~15;  // MMA N
+  const int stride = G.ws, cur = G.nsp & 1;
+  const float* A = op + G.op_off + int64_t(k) * J.m0;
+  const float* X = ws_all + ws_off[J.tc];
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), kTcTmemCols);
+  if (tid == 0) tc::mbar_init(tc::smem_u32(bar), 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t taddr = *tslot;
+  const uint32_t idesc = tc::idesc_tf32(kTcM, nI);
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int k0 = 0; k0 < k; k0 += kTcK) {
+    // A tile: thread tid loads row tid, 32 K elements (zero past m or k)
+    {
+      const bool rv = tid < rows;
+      const float* src = A + int64_t(k) * tid + k0;
+#pragma unroll 8
+      for (int q = 0; q < kTcK; ++q) {
+        const float x = (rv && k0 + q < k) ? __ldg(src + q) : 0.f;
+        float hi, lo;
+        tc::split_tf32(x, hi, lo);
+        const uint32_t o = (q >> 3) * (kTcM * 32) + tc::kmajor_off(tid, q & 7);
+        *reinterpret_cast<float*>(a_hi + o) = hi;
+        *reinterpret_cast<float*>(a_lo + o) = lo;
+      }
+    }
+    // B tile: rows (columns of D) tid, tid + 128; row j = s + ns r is X_r[:, s]
+    for (int jj = tid; jj < nI; jj += kTcThreads) {
+      const bool cv = jj < cols;
+      const int jp = J.n0 + (cv ? jj : 0);
+      const int r = jp / ns, sidx = jp - r * ns;
+      const float* src = X + int64_t(2 * r + cur) * stride + int64_t(k) * sidx + k0;
+#pragma unroll 8
+      for (int q = 0; q < kTcK; ++q) {
+        const float x = (cv && k0 + q < k) ? __ldg(src + q) : 0.f;
+        float hi, lo;
+        tc::split_tf32(x, hi, lo);
+        const uint32_t o = (q >> 3) * (kTcN * 32) + tc::kmajor_off(jj, q & 7);
+        *reinterpret_cast<float*>(b_hi + o) = hi;
+        *reinterpret_cast<float*>(b_lo + o) = lo;
+      }
+    }
+    tc::fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const int steps = min(kTcK / 8, (k - k0 + 7) / 8);
+      for (int st = 0; st < steps; ++st) {
+        const uint64_t ah = tc::smem_desc(tc::smem_u32(a_hi + st * kTcM * 32));
+        const uint64_t al = tc::smem_desc(tc::smem_u32(a_lo + st * kTcM * 32));
+        const uint64_t bh = tc::smem_desc(tc::smem_u32(b_hi + st * kTcN * 32));
+        const uint64_t bl = tc::smem_desc(tc::smem_u32(b_lo + st * kTcN * 32));
+        tc::mma_tf32(taddr, ah, bh, idesc, (k0 > 0 || st > 0) ? 1u : 0u);
+        tc::mma_tf32(taddr, ah, bl, idesc, 1u);
+        tc::mma_tf32(taddr, al, bh, idesc, 1u);
+      }
+      tc::mma_commit(tc::smem_u32(bar));
+    }
+    // every thread waits for the MMAs (they read the tiles the next round overwrites)
+    const bool done = tc::mbar_wait(tc::smem_u32(bar), phase, kTcWaitCycles);
+    phase ^= 1u;
+    if (__syncthreads_or(!done)) {
+      ok = false;
+      break;
+    }
+  }
+  tc::fence_after_sync();
+  if (ok) {
+    // epilogue: thread tid holds tile row tid; columns in runs of 16
+    const int i = J.m0 + tid;
+    const int32_t* bp = perm + G.bperm_off;
+    float* outb = cout + G.b_off;
+    for (int c0 = 0; c0 < nI; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(taddr + (uint32_t(32 * warp) << 16) + uint32_t(c0), v);
+      if (tid < rows) {
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+          const int col = c0 + q;
+          if (col < cols) {
+            const int jp = J.n0 + col;
+            const int r = jp / ns, sidx = jp - r * ns;
+            atomicAdd(outb + int64_t(r) * core_total + __ldg(bp + i + m * sidx), v[q]);
+          }
+        }
+      }
+    }
+  } else if (tid == 0) {
+    atomicExch(err, 1u);  // the host reports it; the context stays usable
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(taddr, kTcTmemCols);
 }
 
 // ---- host planning ---------------------------------------------------------------------------
@@ -937,6 +1105,12 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
   ctx->bst_ws_large = 0;
   ctx->bst_bra_slice = 0;
   ctx->bst_bra_acc = 0;
+  ctx->bst_tc.clear();
+  ctx->bst_tc_ws_off.clear();
+  ctx->bst_tc_jobs.clear();
+  ctx->bst_tc_ws_total = 0;
+  ctx->bst_tc_flops = 0;
+  ctx->bst_tc_mma_flops = 0;
   const size_t ng = ctx->bst_groups.size();
   size_t g = 0;
   while (g < ng) {
@@ -950,6 +1124,22 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
     for (size_t q = g; q < g1; ++q) {
       const BstGroup& G = ctx->bst_groups[q];
       const size_t need = sizeof(BstGroup) + size_t(2) * R * G.ws * elem;
+      const int64_t ns = G.bcore / std::max(G.m, 1);
+      if (elem == 4 && ctx->bst_tc_on && G.m >= kTcMinM && G.k >= kTcMinK && ns * R >= kTcMinN) {
+        // GEMM-shaped: tensor cores (its operand X in a global workspace of its own)
+        const int32_t tc = int32_t(ctx->bst_tc.size());
+        ctx->bst_tc.push_back(int32_t(q));
+        ctx->bst_tc_ws_off.push_back(ctx->bst_tc_ws_total);
+        ctx->bst_tc_ws_total += int64_t(2) * R * G.ws;
+        for (int m0 = 0; m0 < G.m; m0 += kTcM)
+          for (int64_t n0 = 0; n0 < ns * R; n0 += kTcN) {
+            ctx->bst_tc_jobs.insert(ctx->bst_tc_jobs.end(), {tc, int32_t(q), m0, int32_t(n0)});
+            const int64_t nI = (std::min<int64_t>(kTcN, ns * R - n0) + 15) / 16 * 16;
+            ctx->bst_tc_mma_flops += 3 * 2 * int64_t(kTcM) * nI * ((G.k + 7) / 8 * 8);
+          }
+        ctx->bst_tc_flops += 2 * int64_t(G.m) * G.k * ns * R;
+        continue;
+      }
       if (own && need <= size_t(warp_smem_bytes(elem))) {
         if (!open || work > kChunkWork) {
           if (open) ctx->bst_bra_ptr.push_back(int64_t(ctx->bst_bra_glist.size()));
@@ -985,6 +1175,9 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     FCG_CUDA(ctx->d_bst_bra_glist.upload(ctx->bst_bra_glist.data(), ctx->bst_bra_glist.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_small.upload(ctx->bst_small.data(), ctx->bst_small.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_large.upload(ctx->bst_large.data(), ctx->bst_large.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_tc.upload(ctx->bst_tc.data(), ctx->bst_tc.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_tc_ws_off.upload(ctx->bst_tc_ws_off.data(), ctx->bst_tc_ws_off.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_tc_jobs.upload(ctx->bst_tc_jobs.data(), ctx->bst_tc_jobs.size(), ctx->stream));
     ctx->bst_list_R = R;
     ctx->bst_list_elem = elem;
   }
@@ -1023,6 +1216,26 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
         ct, ws.p, int(stride));
     FCG_CUDA(cudaGetLastError());
     ++launches;
+  }
+  if constexpr (sizeof(T) == 4) {
+    if (!ctx->bst_tc.empty()) {
+      FCG_REQUIRE(ctx->bst_tc_jobs.size() / 4 < (size_t(1) << 31), FCG_ELIMIT, "too many tensor-core tiles");
+      FCG_CUDA(ctx->d_bst_tc_ws.alloc(size_t(ctx->bst_tc_ws_total)));
+      FCG_CUDA(ctx->d_bst_tc_err.alloc(1));
+      FCG_CUDA(cudaMemsetAsync(ctx->d_bst_tc_err.p, 0, sizeof(unsigned), ctx->stream));
+      bst_tc_prep_kernel<<<unsigned(ctx->bst_tc.size()), kBstThreads, 0, ctx->stream>>>(
+          ctx->d_bst_tc.p, ctx->d_bst_tc_ws_off.p, ctx->d_bst_groups.p, R, S, ctx->d_bst_perm.p, cin, ct,
+          ctx->d_bst_tc_ws.p);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaFuncSetAttribute(bst_tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+      FCG_CUDA(cudaEventRecord(ctx->ev2, ctx->stream));
+      bst_tc_gemm_kernel<<<unsigned(ctx->bst_tc_jobs.size() / 4), kTcThreads, kTcSmem, ctx->stream>>>(
+          reinterpret_cast<const BstTcJob*>(ctx->d_bst_tc_jobs.p), ctx->d_bst_groups.p, R, op, ctx->d_bst_tc_ws.p,
+          ctx->d_bst_tc_ws_off.p, ctx->d_bst_perm.p, cout, ct, ctx->d_bst_tc_err.p);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaEventRecord(ctx->ev3, ctx->stream));
+      launches += 2;
+    }
   }
   ctx->stats.kernel_launches = launches;
   return FCG_OK;
@@ -1192,6 +1405,25 @@ int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_s
   float ms = 0.f;
   FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->stats.last_kernel_ms = ms;
+  ctx->stats.bst_tc_groups = 0;
+  ctx->stats.bst_tc_ms = 0.0;
+  if (precision == FCG_FP32 && !ctx->bst_tc.empty()) {
+    unsigned err = 0;
+    FCG_CUDA(cudaMemcpy(&err, ctx->d_bst_tc_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    FCG_REQUIRE(err == 0, FCG_ECUDA, "BST tensor-core tile: the MMA completion wait timed out");
+    FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
+    ctx->stats.bst_tc_ms = ms;
+    ctx->stats.bst_tc_groups = int64_t(ctx->bst_tc.size());
+  }
+  ctx->stats.bst_tc_flops = precision == FCG_FP32 ? ctx->bst_tc_flops : 0;
+  ctx->stats.bst_tc_mma_flops = precision == FCG_FP32 ? ctx->bst_tc_mma_flops : 0;
+  return FCG_OK;
+}
+
+int fcg_bst_tensor_cores(fcg_ctx* ctx, int enable) {
+  if (!ctx) return FCG_EINVAL;
+  ctx->bst_tc_on = enable != 0;
+  ctx->bst_list_R = 0;  // the group lists are made again on the next sigma
   return FCG_OK;
 }
 

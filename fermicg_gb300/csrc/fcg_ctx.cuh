@@ -210,6 +210,17 @@ struct fcg_ctx {
   DevBuf<float> d_bst_op32, d_bst_s32;
   DevBuf<double> d_bst_in64, d_bst_out64, d_bst_ws64;
   DevBuf<float> d_bst_in32, d_bst_out32, d_bst_ws32;
+  // tensor-core groups of the float sigma: group ids, their X workspace offsets, the 128 x N
+  // tile jobs {tc index, group, m0, n0}, algorithmic and executed MMA flops per sigma
+  bool bst_tc_on = true;
+  std::vector<int32_t> bst_tc;
+  std::vector<int64_t> bst_tc_ws_off;
+  std::vector<int32_t> bst_tc_jobs;
+  int64_t bst_tc_ws_total = 0, bst_tc_flops = 0, bst_tc_mma_flops = 0;
+  DevBuf<int32_t> d_bst_tc, d_bst_tc_jobs;
+  DevBuf<int64_t> d_bst_tc_ws_off;
+  DevBuf<float> d_bst_tc_ws;
+  DevBuf<unsigned> d_bst_tc_err;
   // the last compressed first-order space (bst_fois.cu), in the fcg_bst_set layout
   struct {
     int R = 0;

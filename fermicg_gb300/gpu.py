@@ -53,6 +53,7 @@ SIGNATURES = {
     "fcg_sigma_closed_noalloc": (_I, [_P, _I, _P, _P, _I]),
     "fcg_get_stats": (_I, [_P, _P]),
     "fcg_set_tuning": (_I, [_P, _I]),
+    "fcg_bst_tensor_cores": (_I, [_P, _I]),
     "fcg_tuning": (_I, [_P, _P, _P]),
     "fcg_bst_set": (_I, [_P, _I, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
     "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
@@ -94,7 +95,8 @@ class Stats(ctypes.Structure):
                 ("hcache_bytes", ctypes.c_int64), ("hcache_seconds", ctypes.c_double),
                 ("open_expand_ms", ctypes.c_double), ("open_flops_reference", ctypes.c_int64),
                 ("open_bytes", ctypes.c_int64), ("tune_seconds", ctypes.c_double),
-                ("tune_cache_hits", ctypes.c_int64)]
+                ("tune_cache_hits", ctypes.c_int64), ("bst_tc_groups", ctypes.c_int64),
+                ("bst_tc_flops", ctypes.c_int64), ("bst_tc_mma_flops", ctypes.c_int64), ("bst_tc_ms", ctypes.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -357,6 +359,10 @@ class GpuSigma:
         self._check(self.L.fcg_bst_fois_get(self.h, _ptr(of), _ptr(ob), _ptr(oo), _ptr(ofa), _ptr(oc)),
                     "fcg_bst_fois_get")
         return of, ob, oo, ofa[:nf.value], oc[:, :ct.value]
+
+    def bst_tensor_cores(self, enable: bool = True):
+        """float BST sigma: GEMM-shaped groups on the tcgen05 tensor cores (default) or not."""
+        self._check(self.L.fcg_bst_tensor_cores(self.h, int(bool(enable))), "fcg_bst_tensor_cores")
 
     def set_tuning(self, mode: int = -1):
         """Closed-sigma kernel candidate: -1 times the candidates on the first sigma of each

@@ -86,6 +86,10 @@ typedef struct fcg_stats {
   int64_t open_bytes;       /* its compulsory bytes: TDM blocks touched, C, output rows */
   double tune_seconds;      /* host time spent timing closed-sigma kernel candidates */
   int64_t tune_cache_hits;  /* tunings answered from the process's shape cache */
+  int64_t bst_tc_groups;    /* groups of the last float BST sigma that ran on the tensor cores */
+  int64_t bst_tc_flops;     /* their algorithmic flops (2 m k n per root) */
+  int64_t bst_tc_mma_flops; /* flops the MMAs executed (3 TF32 products, tiles padded) */
+  double bst_tc_ms;         /* device time of the tensor-core GEMM kernel (CUDA events) */
 } fcg_stats;
 
 int fcg_version(void);
@@ -265,11 +269,20 @@ int fcg_bst_set(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, 
  * contract_dense_H_with_state src/tucker_contract_dense_H_with_state.jl:4-330):
  * sigma = H * cores over the blocks of the last fcg_bst_set (sigma is overwritten; the
  * reference adds into a zeroed sigma).  Host buffers [R][core_total].  precision:
- * FCG_FP64, or FCG_FP32 (float32 operators, cores and accumulation). */
+ * FCG_FP64, or FCG_FP32 (float32 operators, cores and accumulation).  In FCG_FP32 the
+ * groups whose op2^T * ket2 product is GEMM-shaped (at least 64 bra-active rows, 16
+ * ket-active columns and 32 spectator columns over all roots) run on the tcgen05 tensor
+ * cores: three TF32 products per operand pair (each operand split into a TF32 high part
+ * and a TF32 remainder) accumulated in FP32, about FP32 accuracy. */
 int fcg_bst_sigma(fcg_ctx* ctx, int R, const double* cores, double* sigma, int precision);
 
 /* Same on device buffers [R][core_total] float64 of the context's device. */
 int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision);
+
+/* FCG_FP32 BST sigma: GEMM-shaped groups on the tensor cores (enable = 1, the default) or
+ * every group on the CUDA cores (0).  No counterpart in the reference (its GEMMs are BLAS
+ * calls); fcg_stats reports the groups, flops and kernel time of the tensor-core part. */
+int fcg_bst_tensor_cores(fcg_ctx* ctx, int enable);
 
 /* fcg_bst_set for build_sigma! between two different BST states (src/tucker_inner.jl:165-245
  * with sigma_vector and ci_vector distinct): blocks [0, n_first) are one state, blocks
