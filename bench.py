@@ -44,7 +44,8 @@ def parse():
     ap.add_argument("--no-serving", dest="serving", action="store_false", help="skip the solve-latency stream")
     ap.add_argument("--no-bst", dest="bst", action="store_false", help="skip the block-sparse Tucker sigma leg")
     ap.add_argument("--bst-only", action="store_true", help="run only the block-sparse Tucker sigma leg")
-    ap.add_argument("--bst-sectors", type=int, default=0, help="first K Fock sectors of the BST vector (0 = all)")
+    ap.add_argument("--bst-sectors", type=int, default=5, help="first K Fock sectors of the BST vector (0 = all)")
+    ap.add_argument("--bst-maxq", type=int, default=4, help="most clusters in their excited range per Tucker block")
     ap.add_argument("--no-batched", dest="batched", action="store_false",
                     help="skip the grouped launch of 256 uneven problems")
     ap.add_argument("--batched-only", action="store_true", help="run only the grouped-launch leg")
@@ -295,22 +296,25 @@ def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4, stored=Tr
     return out
 
 
-def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
-    """build_sigma! with the operator cache on the 32-orbital / 8-cluster BST vector: the
-    reference sector and its 112 single-charge-transfer sectors, TuckerConfigs with at most
-    two clusters in their excited range, Tucker ranks 4-12, 2 roots.  FP64 and FP32 device
-    timings (L2 flushed before each step), the HBM roofline of reading the operator cache,
-    the host-buffer path, and a CPU sample of the oracle's build_sigma!."""
+def bst_benchmark(steps, warmup, cpu_seconds, peaks, n_sectors=5, max_q=4):
+    """build_sigma! with the operator cache on the config-2 BST vector: 32 orbitals, 8
+    clusters x 4, the reference Fock sector and its first single charge transfers, every
+    TuckerConfig with at most `max_q` clusters in their excited range, Tucker ranks 4-12
+    (cores up to 12^4), 2 roots.  FP64 and FP32 device timings (L2 flushed before each step;
+    the FP32 build runs its GEMM-shaped groups on the tcgen05 tensor cores, also timed with
+    them off), the HBM roofline of reading the operator cache, the tensor-pipe roofline of the
+    tensor-core kernel, the host-buffer path, and a CPU sample of the oracle's build_sigma!."""
     import torch
     from fermicg_gb300 import pack, workloads
     from fermicg_gb300.bst import PackedBST, synthetic_bst
     from fermicg_gb300.gpu import GpuSigma
+    hbm_peak = peaks.get("hbm_gbs", 6800.0)
     prob = workloads.config2_problem(0)
     secs = workloads.single_transfer_sectors(prob)
     if n_sectors > 0:
         secs = secs[:n_sectors]
     R = 2
-    vec = synthetic_bst(prob, secs, max_q=2, rank_range=(4, 12), R=R, seed=0)
+    vec = synthetic_bst(prob, secs, max_q=max_q, rank_range=(4, 12), R=R, seed=0)
     pb = PackedBST(vec, len(prob.clusters), R)
     g = GpuSigma(torch.cuda.current_device())
     g.set_ops(pack.pack_ops(prob.ops, prob.bases))
@@ -330,7 +334,7 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
         for _ in range(warmup):
             g.bst_sigma_device(x.data_ptr(), y.data_ptr(), R, prec)
         torch.cuda.synchronize()
-        ms, kern = [], []
+        ms, kern, tc = [], [], []
         for _ in range(steps):
             flush.zero_()
             e0 = torch.cuda.Event(enable_timing=True)
@@ -340,13 +344,20 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
             e1.record(stream)
             e1.synchronize()
             ms.append(e0.elapsed_time(e1))
-            kern.append(g.stats()["last_kernel_ms"])
-        return statistics.mean(ms), statistics.median(kern)
+            s_ = g.stats()
+            kern.append(s_["last_kernel_ms"])
+            tc.append(s_["bst_tc_ms"])
+        return statistics.mean(ms), statistics.median(kern), statistics.median(tc)
 
-    ms64, k64 = timed("fp64")
+    ms64, k64, _ = timed("fp64")
     y64 = y.clone()
-    ms32, k32 = timed("fp32")
+    ms32, k32, tc32 = timed("fp32")
     rel32 = float((y - y64).abs().max() / y64.abs().max())
+    s32 = g.stats()
+    g.bst_tensor_cores(False)
+    ms32c, k32c, _ = timed("fp32")
+    relc = float((y - y64).abs().max() / y64.abs().max())
+    g.bst_tensor_cores(True)
     walls = []
     for _ in range(max(3, steps // 2)):
         flush.zero_()
@@ -364,8 +375,14 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
         return {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                 "bytes_per_sigma": alg, "note": "operator cache + cores read/written per sigma, of measured HBM copy peak"}
 
+    # tensor-core kernel: executed MMA flops (three TF32 products per tile, tiles padded to
+    # 128 x 16k) over its CUDA-event time, against half the measured bf16 dense peak (TF32
+    # runs at half the bf16 rate)
+    tf32_peak = peaks.get("bf16_tflops", 1900.0) / 2
+    tc_ach = s32["bst_tc_mma_flops"] / (tc32 * 1e-3) / 1e12 if tc32 > 0 else 0.0
     out = {
-        "workload": "bst_sigma_32o_8x4_M16_113sectors_q2_ranks4-12_R2", "blocks": len(pb.keys),
+        "workload": f"bst_sigma_32o_8x4_M16_{len(secs)}sectors_q{max_q}_ranks4-12_R2",
+        "max_core": int(pb.blocks[:, 1].max()), "blocks": len(pb.keys),
         "core_total": pb.core_total, "roots": R, "triples": st["bst_triples"], "groups": st["bst_groups"],
         "cache_elements": cache, "cache_seconds": st["bst_cache_seconds"], "plan_seconds": st["bst_plan_seconds"],
         "set_wall_s": t_set,
@@ -373,7 +390,16 @@ def bst_benchmark(steps, warmup, cpu_seconds, hbm_peak, n_sectors=0):
         "fp64": {"value": 1e3 / ms64, "unit": "sigma_builds/s", "ms_per_step": ms64, "kernel_ms": k64,
                  "roofline": roof(k64, 8)},
         "fp32": {"value": 1e3 / ms32, "unit": "sigma_builds/s", "ms_per_step": ms32, "kernel_ms": k32,
-                 "roofline": roof(k32, 4), "rel_err_vs_fp64": rel32},
+                 "roofline": roof(k32, 4), "rel_err_vs_fp64": rel32,
+                 "tensor_cores": {"groups": s32["bst_tc_groups"], "of_groups": st["bst_groups"],
+                                  "algorithmic_flops": s32["bst_tc_flops"], "mma_flops": s32["bst_tc_mma_flops"],
+                                  "share_of_reference_flops": s32["bst_tc_flops"] / max(st["bst_flops_reference"] * R, 1),
+                                  "kernel_ms": tc32,
+                                  "roofline": {"bound": "tensor", "achieved": tc_ach, "peak": tf32_peak,
+                                               "unit": "TFLOP/s", "frac": tc_ach / tf32_peak,
+                                               "note": "bst_tc_gemm_kernel: executed 3xTF32 MMA flops / its time, "
+                                                       "of half the measured bf16 dense peak"}},
+                 "cuda_cores_only": {"ms_per_step": ms32c, "kernel_ms": k32c, "rel_err_vs_fp64": relc}},
         "e2e_fp32": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": host.nbytes,
                      "d2h_bytes_per_step": host.nbytes},
     }
@@ -815,8 +841,8 @@ def main():
         except Exception:
             pass
         if rank == 0:
-            print(json.dumps({"bst": bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds,
-                                                   peaks.get("hbm_gbs", 6800.0), a.bst_sectors)}))
+            print(json.dumps({"bst": bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, peaks,
+                                                   a.bst_sectors, a.bst_maxq)}))
         return
     if world > 1:
         import torch.distributed as dist
@@ -987,7 +1013,7 @@ def main():
             out["batched"] = {"error": str(ex)}
     if rank == 0 and a.bst:
         try:
-            out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, hbm_peak, a.bst_sectors)
+            out["bst"] = bst_benchmark(max(3, a.steps // 2), a.warmup, a.cpu_seconds, peaks, a.bst_sectors, a.bst_maxq)
         except Exception as ex:
             out["bst"] = {"error": str(ex)}
     if rank == 0 and a.davidson:

@@ -247,7 +247,7 @@ __device__ __forceinline__ void prefetch_range(const void* p, int64_t bytes, int
 // two contiguous vectors, OP[:, kb] and X[:, s], taken by a sub-warp of `lanes` threads
 // (power of two, <= 32) and added to out[r * out_stride + bra core index].
 // Steps 1-2 of a group (the GEMM operand X of every root), by a team; X of root r ends in
-// ws[(2 r + cur) * stride], cur = nsp & 1, which is returned.
+// ws[(2 r + cur) * stride], cur = ntr & 1 (one buffer swap per applied overlap), returned.
 template <typename T, int TEAM>
 __device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__ S, const int32_t* __restrict__ perm,
                                  const T* __restrict__ cin, int64_t core_total, T* ws, int stride) {
@@ -272,6 +272,10 @@ __device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__
       int outer = 1;
       for (int i = j + 1; i < nsp; ++i) outer *= G.s_kr[i];
       const int rb = G.s_br[j], rk = G.s_kr[j];
+      if (G.s_off[j] < 0) {  // the identity: X keeps this mode as it is
+        inner *= rb;
+        continue;
+      }
       const int n = inner * rb * outer;
       const T* Sj = S + G.s_off[j];
       for (int idx = tid; idx < R * n; idx += TEAM) {
@@ -501,7 +505,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJ
   const int m = G.m, k = G.k, ns = G.bcore / G.m, NT = ns * R;
   const int rows = min(kTcM, m - J.m0), cols = min(kTcN, NT - J.n0);
   const int nI = (cols + 15) & ~15;  // MMA N
-  const int stride = G.ws, cur = G.nsp & 1;
+  const int stride = G.ws, cur = G.ntr & 1;
   const float* A = op + G.op_off + int64_t(k) * J.m0;
   const float* X = ws_all + ws_off[J.tc];
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), kTcTmemCols);
@@ -784,9 +788,16 @@ std::string finish_part(const std::vector<BstBlock>& blk, int N, BstPart& P) {
       }
     }
     int64_t size = K.core_len, ws = size, tf = 0;
+    G.ntr = 0;
     for (int c = 0, j = 0; c < N; ++c) {
       if ((G.act_mask >> c) & 1) continue;
       if (B.rank[c] == 1 && K.rank[c] == 1) continue;
+      if (G.bra == G.ket && ((B.ortho >> c) & 1)) {
+        // U^T U of an orthonormal factor: the identity up to rounding, not applied
+        G.s_off[j++] = -1;
+        continue;
+      }
+      ++G.ntr;
       const uint64_t key = (uint64_t(G.bra) * uint64_t(nb) + uint64_t(G.ket)) * 8 + uint64_t(c);
       auto it = P.overlap_at.find(key);
       if (it == P.overlap_at.end()) {
@@ -1024,7 +1035,8 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     for (BstGroup G : part.groups) {
       G.op_off += op0;
       G.t_off += int32_t(t0);
-      for (int j = 0; j < G.nsp; ++j) G.s_off[j] += s0;
+      for (int j = 0; j < G.nsp; ++j)
+        if (G.s_off[j] >= 0) G.s_off[j] += s0;
       for (int side = 0; side < 2; ++side) {
         const int32_t b = side == 0 ? G.ket : G.bra;
         const uint64_t key = uint64_t(b) * 256 + uint64_t(G.act_mask);
@@ -1076,7 +1088,11 @@ std::string check_groups(const std::vector<BstGroup>& groups, const std::vector<
       bprod *= G.s_br[j];
       kmax += int64_t(G.s_kr[j] - 1) * G.s_ks[j];
       bmax += int64_t(G.s_br[j] - 1) * G.s_bs[j];
-      if (G.s_off[j] < 0 || G.s_off[j] + int64_t(G.s_br[j]) * G.s_kr[j] > s_total) return "BST check: overlap extent";
+      if (G.s_off[j] == -1) {
+        if (G.s_br[j] != G.s_kr[j] || G.bra != G.ket) return "BST check: identity overlap";
+      } else if (G.s_off[j] < 0 || G.s_off[j] + int64_t(G.s_br[j]) * G.s_kr[j] > s_total) {
+        return "BST check: overlap extent";
+      }
       size = size / G.s_kr[j] * G.s_br[j];
       ws_need = std::max(ws_need, size);
     }
@@ -1208,7 +1224,7 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     ++launches;
   }
   if (!ctx->bst_large.empty()) {
-    const int grid = int(std::min<size_t>(ctx->bst_large.size(), 2 * 152));
+    const int grid = int(std::min<size_t>(ctx->bst_large.size(), 4 * 152));
     const int64_t stride = ctx->bst_ws_large;
     FCG_CUDA(ws.alloc(size_t(grid) * 2 * R * stride));
     bst_sigma_global_kernel<T><<<unsigned(grid), kBstThreads, 0, ctx->stream>>>(
@@ -1276,6 +1292,19 @@ int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock,
       B.len[c] = int32_t(r[2 * N + c]);
       B.factor_off[c] = factor_off[N * b + c];
       len *= r[c];
+      // orthonormal columns (U^T U = 1 to 1e-13): a block's overlap with itself is the identity
+      {
+        const double* U = factors + factor_off[N * b + c];
+        const int64_t L = r[2 * N + c], rk = r[c];
+        double dev = 0.0;
+        for (int64_t x = 0; x < rk; ++x)
+          for (int64_t y = 0; y <= x; ++y) {
+            double d = 0.0;
+            for (int64_t i = 0; i < L; ++i) d += U[i + L * x] * U[i + L * y];
+            dev = std::max(dev, std::fabs(d - (x == y ? 1.0 : 0.0)));
+          }
+        if (dev < 1e-13) B.ortho |= 1 << c;
+      }
     }
     FCG_REQUIRE(len < (int64_t(1) << 30), FCG_ELIMIT, "BST: a core exceeds 2^30 elements");
     B.core_off = off;

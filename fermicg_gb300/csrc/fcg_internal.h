@@ -139,7 +139,7 @@ struct BstBlock {
   int32_t start[kMaxClusters];         // first local state of the range (0-based)
   int32_t len[kMaxClusters];           // range length
   int32_t core_len;
-  int32_t pad;
+  int32_t ortho;                       // bit c: the factor of cluster c has orthonormal columns
 };
 
 // Dressed TDM of one active cluster between a bra and a ket block:
@@ -170,7 +170,8 @@ struct BstGroupTerm {
 struct BstGroup {
   int64_t op_off;
   int64_t k_off, b_off;          // ket / bra core offsets
-  int64_t s_off[kMaxClusters];   // overlap U_bra^T U_ket (rank_bra x rank_ket) of spectator mode j
+  int64_t s_off[kMaxClusters];   // overlap U_bra^T U_ket (rank_bra x rank_ket) of spectator mode j; -1:
+                                 // the identity (bra and ket share an orthonormal factor), not applied
   int32_t bra, ket;
   int32_t m, k;                  // products of the active bra / ket ranks
   int32_t act_mask;
@@ -182,7 +183,8 @@ struct BstGroup {
   int32_t a_ks[4], a_bs[4];      // their strides in the ket / bra core
   int32_t s_kr[kMaxClusters], s_br[kMaxClusters];
   int32_t s_ks[kMaxClusters], s_bs[kMaxClusters];
-  int32_t pad[2];
+  int32_t ntr;                   // spectator modes with an overlap to apply (the others: U^T U = 1)
+  int32_t pad;
   // index tables (core offset of every position of the actives-first layout) of the ket and
   // the bra block for this group's active clusters
   int64_t kperm_off, bperm_off;
