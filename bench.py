@@ -426,7 +426,7 @@ def bst_benchmark(steps, warmup, cpu_seconds, peaks, n_sectors=5, max_q=4):
 
 def batched_benchmark(steps, warmup, n_inst=256, stored=True):
     """Batched uneven instances: n_inst independent problems (orbitals in {8,12,16,20},
-    clusters of 2-4 orbitals, half filling, M=8-16, 1-3 roots, seeds 3000+i), each problem's
+    clusters of 2-5 orbitals, half filling, M=8-16, 1-3 roots, seeds 3000+i), each problem's
     closed sigma in one grouped launch (fcg_sigma_closed_grouped) against the same sigmas
     launched one context after another.  Returns problem-sigmas/s for both, mixed and FP64."""
     import torch
@@ -434,20 +434,23 @@ def batched_benchmark(steps, warmup, n_inst=256, stored=True):
     from fermicg_gb300.gpu import GpuSigma, sigma_closed_grouped
     t0 = time.perf_counter()
     items = []
-    for i in range(n_inst):
-        prob, st = workloads.config3_instance(i, max_cluster=4)
-        f, c, v, _ = pack.pack_state(st)
+    built = workloads.config3_batch(n_inst, max_cluster=5)  # local bases in worker processes
+    t_inputs = time.perf_counter() - t0
+    for po, pt, f, c, v in built:
         g = GpuSigma(torch.cuda.current_device())
-        g.set_problem(prob.ops, prob.bases, prob.ham)
+        g.set_ops(po)
+        g.set_terms(pt)
         g.state_set(f, c)
         dc = torch.from_numpy(np.asfortranarray(v).T.copy()).cuda()
         items.append((g, dc, torch.empty_like(dc), v.shape[1], f.shape[0]))
     t_build = time.perf_counter() - t0
     gs = [it[0] for it in items]
     cps, sps, rs = [it[1].data_ptr() for it in items], [it[2].data_ptr() for it in items], [it[3] for it in items]
-    out = {"workload": f"{n_inst}_uneven_tpsci_problems_8-20o_clusters2-4_M8-16_R1-3",
+    out = {"workload": f"{n_inst}_uneven_tpsci_problems_8-20o_clusters2-5_M8-16_R1-3",
            "instances": n_inst, "total_configs": int(sum(it[4] for it in items)),
-           "total_triples": int(sum(it[0].stats()["n_triples"] for it in items)), "setup_s": t_build}
+           "instances_with_5_orbital_clusters": int(sum(int(5 in set(b[0].cluster_norb.tolist())) for b in built)),
+           "total_triples": int(sum(it[0].stats()["n_triples"] for it in items)), "setup_s": t_build,
+           "inputs_s": t_inputs}
     for prec in ("fp32", "fp64"):
         for _ in range(warmup):
             sigma_closed_grouped(gs, cps, sps, rs, prec)

@@ -153,3 +153,32 @@ def plan_triples(pb: PackedBST, ham, ops=None, nbody=4):
                     for k in g.get(tuple(tb[c] if c not in act else None for c in range(N)), []):
                         out.append((b, k, term_index[id(t)], 1 if t.nbody == 1 else sgn))
     return np.array(out, dtype=np.int32).reshape(-1, 4)
+
+
+def hcmf_diagonal(pb: PackedBST, vec, ops, op="Hcmf"):
+    """Preconditioner diagonal of a BST solve (one value per core element, the layout of one
+    root of PackedBST.cores_of): sum over clusters of the diagonal of U_c^T Hcmf_c U_c for the
+    block's factor U_c of the cluster's range.  The reference's ci_solve (precond=true,
+    src/tucker_outer.jl:90-95) first rotates every block's factors so that the local Hcmf is
+    diagonal and sums its eigenvalues; without the rotation this is the diagonal of the same
+    operator in the unrotated Tucker basis."""
+    N = pb.N
+    out = np.zeros(pb.core_total)
+    for i, key in enumerate(pb.keys):
+        fs, tcfg = key
+        o, n = int(pb.blocks[i, 0]), int(pb.blocks[i, 1])
+        facs = vec[key]["factors"]
+        d = np.zeros(n)
+        shape = [f.shape[1] for f in facs]
+        stride = 1
+        for c in range(N):
+            blocks = ops[c].data.get(op) or ops[c].data["H"]
+            Hc = np.asarray(blocks[(fs[c], fs[c])])
+            a, b = tcfg[c]
+            U = facs[c]
+            dc = np.einsum("ik,ij,jk->k", U, Hc[a:b, a:b], U)
+            idx = (np.arange(n) // stride) % shape[c]
+            d += dc[idx]
+            stride *= shape[c]
+        out[o:o + n] = d
+    return out

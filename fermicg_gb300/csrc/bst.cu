@@ -1194,6 +1194,8 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     FCG_CUDA(ctx->d_bst_tc.upload(ctx->bst_tc.data(), ctx->bst_tc.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_tc_ws_off.upload(ctx->bst_tc_ws_off.data(), ctx->bst_tc_ws_off.size(), ctx->stream));
     FCG_CUDA(ctx->d_bst_tc_jobs.upload(ctx->bst_tc_jobs.data(), ctx->bst_tc_jobs.size(), ctx->stream));
+    FCG_CUDA(ctx->d_bst_tc_err.alloc(1));  // set by a tensor-core tile whose MMA wait timed out
+    FCG_CUDA(cudaMemsetAsync(ctx->d_bst_tc_err.p, 0, sizeof(unsigned), ctx->stream));
     ctx->bst_list_R = R;
     ctx->bst_list_elem = elem;
   }
@@ -1237,8 +1239,6 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     if (!ctx->bst_tc.empty()) {
       FCG_REQUIRE(ctx->bst_tc_jobs.size() / 4 < (size_t(1) << 31), FCG_ELIMIT, "too many tensor-core tiles");
       FCG_CUDA(ctx->d_bst_tc_ws.alloc(size_t(ctx->bst_tc_ws_total)));
-      FCG_CUDA(ctx->d_bst_tc_err.alloc(1));
-      FCG_CUDA(cudaMemsetAsync(ctx->d_bst_tc_err.p, 0, sizeof(unsigned), ctx->stream));
       bst_tc_prep_kernel<<<unsigned(ctx->bst_tc.size()), kBstThreads, 0, ctx->stream>>>(
           ctx->d_bst_tc.p, ctx->d_bst_tc_ws_off.p, ctx->d_bst_groups.p, R, S, ctx->d_bst_perm.p, cin, ct,
           ctx->d_bst_tc_ws.p);
@@ -1258,6 +1258,52 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
 }
 
 }  // namespace
+
+int bst_sigma_device_async(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision, bool timed) {
+  FCG_REQUIRE(ctx->have_bst, FCG_ESTATE, "fcg_bst_set must come first");
+  FCG_REQUIRE(R >= 1 && R <= 64, FCG_ELIMIT, "R must be in [1, 64]");
+  FCG_REQUIRE(d_cores && d_sigma, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
+  int64_t max_core = 0;
+  for (const BstBlock& B : ctx->bst_blocks) max_core = std::max<int64_t>(max_core, B.core_len);
+  FCG_REQUIRE(max_core * R < (int64_t(1) << 31), FCG_ELIMIT, "R times the largest core must stay below 2^31");
+  const int64_t n = ctx->bst_core_total * R;
+  ctx->stats.last_kernel_ms = 0.0;
+  int rc;
+  if (precision == FCG_FP64) {
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    rc = bst_launch<double>(ctx, R, ctx->d_bst_op64.p, ctx->d_bst_s64.p, d_cores, d_sigma, ctx->d_bst_ws64);
+    if (rc) return rc;
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+  } else {
+    FCG_CUDA(ctx->d_bst_in32.alloc(size_t(n)));
+    FCG_CUDA(ctx->d_bst_out32.alloc(size_t(n)));
+    bst_convert_kernel<<<512, 256, 0, ctx->stream>>>(d_cores, ctx->d_bst_in32.p, n);
+    FCG_CUDA(cudaGetLastError());
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    rc = bst_launch<float>(ctx, R, ctx->d_bst_op32.p, ctx->d_bst_s32.p, ctx->d_bst_in32.p, ctx->d_bst_out32.p,
+                           ctx->d_bst_ws32);
+    if (rc) return rc;
+    if (timed) FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    bst_widen_kernel<<<512, 256, 0, ctx->stream>>>(ctx->d_bst_out32.p, d_sigma, n);
+    FCG_CUDA(cudaGetLastError());
+    ctx->stats.kernel_launches += 2;
+  }
+  return FCG_OK;
+}
+
+int bst_tc_check(fcg_ctx* ctx) {
+  if (ctx->bst_tc.empty()) return FCG_OK;
+  unsigned err = 0;
+  FCG_CUDA(cudaMemcpyAsync(&err, ctx->d_bst_tc_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (err) {
+    FCG_CUDA(cudaMemsetAsync(ctx->d_bst_tc_err.p, 0, sizeof(unsigned), ctx->stream));
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  FCG_REQUIRE(err == 0, FCG_ECUDA, "BST tensor-core tile: the MMA completion wait timed out");
+  return FCG_OK;
+}
 
 int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock, const int64_t* blocks,
                  const int64_t* factor_off, int64_t n_factors, const double* factors, const int32_t* triples,
@@ -1400,36 +1446,9 @@ int fcg_bst_set_between(fcg_ctx* ctx, int nbody, int64_t n_first, int64_t n_bloc
 
 int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision) {
   if (!ctx) return FCG_EINVAL;
-  FCG_REQUIRE(ctx->have_bst, FCG_ESTATE, "fcg_bst_set must come first");
-  FCG_REQUIRE(R >= 1 && R <= 64, FCG_ELIMIT, "R must be in [1, 64]");
-  FCG_REQUIRE(d_cores && d_sigma, FCG_EINVAL, "null pointer");
-  FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
-  int64_t max_core = 0;
-  for (const BstBlock& B : ctx->bst_blocks) max_core = std::max<int64_t>(max_core, B.core_len);
-  FCG_REQUIRE(max_core * R < (int64_t(1) << 31), FCG_ELIMIT, "R times the largest core must stay below 2^31");
   FCG_CUDA(cudaSetDevice(ctx->device));
-  const int64_t n = ctx->bst_core_total * R;
-  ctx->stats.last_kernel_ms = 0.0;
-  int rc;
-  if (precision == FCG_FP64) {
-    FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    rc = bst_launch<double>(ctx, R, ctx->d_bst_op64.p, ctx->d_bst_s64.p, d_cores, d_sigma, ctx->d_bst_ws64);
-    if (rc) return rc;
-    FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-  } else {
-    FCG_CUDA(ctx->d_bst_in32.alloc(size_t(n)));
-    FCG_CUDA(ctx->d_bst_out32.alloc(size_t(n)));
-    bst_convert_kernel<<<512, 256, 0, ctx->stream>>>(d_cores, ctx->d_bst_in32.p, n);
-    FCG_CUDA(cudaGetLastError());
-    FCG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    rc = bst_launch<float>(ctx, R, ctx->d_bst_op32.p, ctx->d_bst_s32.p, ctx->d_bst_in32.p, ctx->d_bst_out32.p,
-                           ctx->d_bst_ws32);
-    if (rc) return rc;
-    FCG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
-    bst_widen_kernel<<<512, 256, 0, ctx->stream>>>(ctx->d_bst_out32.p, d_sigma, n);
-    FCG_CUDA(cudaGetLastError());
-    ctx->stats.kernel_launches += 2;
-  }
+  int rc = bst_sigma_device_async(ctx, R, d_cores, d_sigma, precision, true);
+  if (rc) return rc;
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   float ms = 0.f;
   FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
@@ -1437,9 +1456,7 @@ int fcg_bst_sigma_device(fcg_ctx* ctx, int R, const double* d_cores, double* d_s
   ctx->stats.bst_tc_groups = 0;
   ctx->stats.bst_tc_ms = 0.0;
   if (precision == FCG_FP32 && !ctx->bst_tc.empty()) {
-    unsigned err = 0;
-    FCG_CUDA(cudaMemcpy(&err, ctx->d_bst_tc_err.p, sizeof(unsigned), cudaMemcpyDeviceToHost));
-    FCG_REQUIRE(err == 0, FCG_ECUDA, "BST tensor-core tile: the MMA completion wait timed out");
+    if ((rc = bst_tc_check(ctx))) return rc;
     FCG_CUDA(cudaEventElapsedTime(&ms, ctx->ev2, ctx->ev3));
     ctx->stats.bst_tc_ms = ms;
     ctx->stats.bst_tc_groups = int64_t(ctx->bst_tc.size());

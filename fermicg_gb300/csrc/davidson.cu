@@ -816,6 +816,7 @@ enum class Act { kWait, kSigma, kDone };
 struct DavidsonRun {
   DavidsonWork W;
   fcg_ctx* ctx = nullptr;
+  bool bst = false;  // the operator is the BST sigma of the context's fcg_bst_set structure
   int R = 0, max_iter = 0, precond = 0, prec = 0;
   double tol = 0, drop = 0, switch_tol = 0;
   // float32 phase: best largest residual so far and the iterations since it last fell by 10%
@@ -837,9 +838,14 @@ struct DavidsonRun {
 
   // grouped: the solve runs in a lockstep round executor, which provides W.arena before the
   // first step (no staging buffers of its own are allocated)
+  // bst_op: solve with the BST sigma (ci_solve, src/tucker_outer.jl:68-215) over the cores of
+  // the last fcg_bst_set, preconditioned by bst_hd (core_total values) when given
   int init(fcg_ctx* c, int R_, const double* v0_, int max_iter_, int max_ss_vecs, double tol_, double lindep,
-           int precision, int precond_, double* e, double* vecs, double* res, int* its, bool grouped = false) {
+           int precision, int precond_, double* e, double* vecs, double* res, int* its, bool grouped = false,
+           bool bst_op = false, const double* bst_hd = nullptr) {
     ctx = c;
+    bst = bst_op;
+    if (bst) precond_ = bst_hd != nullptr;
     R = R_;
     v0 = v0_;
     max_iter = max_iter_;
@@ -850,12 +856,15 @@ struct DavidsonRun {
     vectors = vecs;
     residuals = res;
     iters = its;
-    FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+    if (bst)
+      FCG_REQUIRE(ctx->have_bst, FCG_ESTATE, "fcg_bst_set must come first");
+    else
+      FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+    const int64_t n = bst ? ctx->bst_core_total : ctx->n_cfg;
     FCG_REQUIRE(v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
-    FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= ctx->n_cfg, FCG_ELIMIT, "R must be in [1, min(16, n_cfg)]");
+    FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= n, FCG_ELIMIT, "R must be in [1, min(16, vector length)]");
     FCG_REQUIRE(max_ss_vecs >= 2 && max_iter >= 1 && tol > 0, FCG_EINVAL, "bad Davidson settings");
     FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
-    const int64_t n = ctx->n_cfg;
     W.ctx = ctx;
     W.n = n;
     W.R = R;
@@ -922,7 +931,10 @@ struct DavidsonRun {
       FCG_CUDA(take(ctx->dav_h_up, W.h_up, W.up_cap));
       W.hout = W.h_out.p;
     }
-    if (precond) {
+    if (precond && bst) {
+      FCG_CUDA(cudaMemcpyAsync(W.hd.p, bst_hd, sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+      FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // bst_hd belongs to the caller
+    } else if (precond) {
       std::vector<double> hd(n);
       int rc = fcg_diagonal(ctx, -1, hd.data());  // leaves the diagonal in ctx->d_hd as well
       if (rc) return rc;
@@ -1318,8 +1330,10 @@ int run_solo(DavidsonRun& r) {
       r.W.after_wait();
     } else {
       const int64_t n = r.W.n;
-      const int rs = sigma_closed_device_async(ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col,
-                                               r.sig_prec);
+      const int rs = r.bst ? bst_sigma_device_async(ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col,
+                                                    r.sig_prec, false)
+                           : sigma_closed_device_async(ctx, r.sig_m, r.W.V.p + n * r.sig_col,
+                                                       r.W.AV.p + n * r.sig_col, r.sig_prec);
       if (rs) return rs;
     }
   }
@@ -1649,6 +1663,15 @@ int Lockstep::round() {
       const DavidsonRun& r = *entries[i].run;
       if (entries[i].state != kSigma || r.sig_prec != p) continue;
       const int64_t n = r.W.n;
+      if (r.bst) {  // BST sigma: a launch sequence of its own on the lane's stream
+        if ((rc = bst_sigma_device_async(r.ctx, r.sig_m, r.W.V.p + n * r.sig_col, r.W.AV.p + n * r.sig_col, p,
+                                         false))) {
+          err = r.ctx->err;
+          return rc;
+        }
+        launches += 3;
+        continue;
+      }
       cs.push_back(r.ctx);
       Rs.push_back(r.sig_m);
       dc.push_back(r.W.V.p + n * r.sig_col);
@@ -1697,6 +1720,20 @@ extern "C" int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter,
                           residuals, iters);
   if (rc) return rc;
   return run_solo(run);
+}
+
+extern "C" int fcg_bst_davidson(fcg_ctx* ctx, int R, const double* v0, const double* hdiag, int max_iter,
+                                int max_ss_vecs, double tol, double lindep, int precision, double* energies,
+                                double* vectors, double* residuals, int* iters) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  DavidsonRun run;
+  int rc = run.init(ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, 0, energies, vectors, residuals, iters,
+                    false, true, hdiag);
+  if (rc) return rc;
+  rc = run_solo(run);
+  if (rc) return rc;
+  return precision == FCG_FP32 ? bst_tc_check(ctx) : FCG_OK;
 }
 
 extern "C" int fcg_davidson_grouped(int n, fcg_ctx* const* ctxs, const int* R, const double* const* v0, int max_iter,
@@ -1835,6 +1872,8 @@ struct fcg_server {
     fcg_ctx* ctx = nullptr;
     int R = 0, max_iter = 0, max_ss_vecs = 0, precision = 0, precond = 0;
     double tol = 0, lindep = 0;
+    bool bst = false;            // a BST solve (fcg_submit_bst)
+    std::vector<double> bst_hd;  // its preconditioner diagonal, or empty
     std::vector<double> v0, energies, vectors, residuals;
     int iters = 0;
     int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
@@ -1899,7 +1938,8 @@ void fcg_server::lane_loop(int lane) {
         lk.unlock();
         int rc = sl.run->init(t->ctx, t->R, t->v0.data(), t->max_iter, t->max_ss_vecs, t->tol, t->lindep,
                               t->precision, t->precond, t->energies.data(), t->vectors.data(),
-                              t->residuals.data(), &t->iters, true);
+                              t->residuals.data(), &t->iters, true, t->bst,
+                              t->bst_hd.empty() ? nullptr : t->bst_hd.data());
         if (rc == FCG_OK && (rc = L.add(sl.run.get()))) t->ctx->err = L.err;
         lk.lock();
         if (rc) {
@@ -1924,7 +1964,9 @@ void fcg_server::lane_loop(int lane) {
       if (e.state != Lockstep::kDone && e.state != Lockstep::kFailed && rc_round == FCG_OK) continue;
       Slot& sl = active[i];
       if (e.state == Lockstep::kDone) {
-        finish(sl, FCG_OK);
+        // a float BST solve: its tensor-core tiles must all have completed
+        const int rc_tc = sl.t->bst && sl.t->precision == FCG_FP32 ? bst_tc_check(sl.t->ctx) : FCG_OK;
+        finish(sl, rc_tc);
       } else if (e.state == Lockstep::kFailed) {
         finish(sl, e.rc);
       } else {
@@ -1982,13 +2024,16 @@ int fcg_server_destroy(fcg_server* s) {
   return FCG_OK;
 }
 
-int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
-               double lindep, int precision, int precond, int64_t* ticket) {
+static int submit_impl(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs,
+                       double tol, double lindep, int precision, int precond, int64_t* ticket, bool bst,
+                       const double* bst_hd) {
   if (!s || !ctx || !v0 || !ticket || R < 1 || R > kMaxB) return FCG_EINVAL;
-  if (!ctx->have_state || ctx->n_cfg < R) return FCG_ESTATE;
+  if (bst ? (!ctx->have_bst || ctx->bst_core_total < R) : (!ctx->have_state || ctx->n_cfg < R)) return FCG_ESTATE;
   if (ctx->device != s->device) return FCG_EINVAL;
   auto t = std::make_shared<fcg_server::Ticket>();
-  const int64_t n = ctx->n_cfg;
+  const int64_t n = bst ? ctx->bst_core_total : ctx->n_cfg;
+  t->bst = bst;
+  if (bst && bst_hd) t->bst_hd.assign(bst_hd, bst_hd + n);
   t->ctx = ctx;
   t->R = R;
   t->max_iter = max_iter;
@@ -2014,6 +2059,16 @@ int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_ite
   *ticket = t->id;
   s->cv_work.notify_all();
   return FCG_OK;
+}
+
+int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
+               double lindep, int precision, int precond, int64_t* ticket) {
+  return submit_impl(s, ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, precond, ticket, false, nullptr);
+}
+
+int fcg_submit_bst(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, const double* hdiag, int max_iter,
+                   int max_ss_vecs, double tol, double lindep, int precision, int64_t* ticket) {
+  return submit_impl(s, ctx, R, v0, max_iter, max_ss_vecs, tol, lindep, precision, 0, ticket, true, hdiag);
 }
 
 int fcg_poll(fcg_server* s, int64_t ticket, int* state) {

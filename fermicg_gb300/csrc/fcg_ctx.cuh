@@ -237,6 +237,12 @@ struct fcg_ctx {
 // (fcg_gpu.cu)
 int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
 
+// BST sigma on device vectors [R][core_total] queued on ctx->stream without the host wait
+// (timed: CUDA events around the kernels), and the check of the tensor-core error flag (one
+// host wait) (bst.cu)
+int bst_sigma_device_async(fcg_ctx* ctx, int R, const double* d_cores, double* d_sigma, int precision, bool timed);
+int bst_tc_check(fcg_ctx* ctx);
+
 // fcg_bst_set with an optional caller-given triple list {bra, ket, term} (n_triples of them)
 // in place of the check_term enumeration, or (split > 0) with only the triples that couple a
 // block of [0, split) with a block of [split, n_blocks) (bst.cu)

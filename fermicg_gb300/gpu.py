@@ -54,6 +54,9 @@ SIGNATURES = {
     "fcg_get_stats": (_I, [_P, _P]),
     "fcg_set_tuning": (_I, [_P, _I]),
     "fcg_bst_tensor_cores": (_I, [_P, _I]),
+    "fcg_bst_davidson": (_I, [_P, _I, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P, _P, _P,
+                              ctypes.POINTER(_I)]),
+    "fcg_submit_bst": (_I, [_P, _P, _I, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, ctypes.POINTER(_L)]),
     "fcg_tuning": (_I, [_P, _P, _P]),
     "fcg_bst_set": (_I, [_P, _I, _L, _P, _P, _P, _L, _P, ctypes.POINTER(_L)]),
     "fcg_bst_sigma": (_I, [_P, _I, _P, _P, _I]),
@@ -324,6 +327,26 @@ class GpuSigma:
         out = np.zeros_like(c)
         self._check(self.L.fcg_bst_sigma(self.h, R, _ptr(c), _ptr(out), PRECISION[precision]), "fcg_bst_sigma")
         return out
+
+    def bst_davidson(self, v0, hdiag=None, max_iter=200, max_ss_vecs=12, tol=1e-6, lindep=1e-12,
+                     precision="fp64"):
+        """The BST ci_solve Davidson on the device over the cores of the last bst_set: v0
+        (core_total, R); hdiag (core_total,) preconditioner diagonal or None.  Returns
+        (energies, vectors (core_total, R), residuals, iterations)."""
+        v = np.asfortranarray(v0, dtype=np.float64)
+        n, R = v.shape
+        if n != self.bst_core_total:
+            raise ValueError("guess rows do not match the BST structure")
+        hd = None if hdiag is None else np.ascontiguousarray(hdiag, dtype=np.float64)
+        if hd is not None and hd.shape != (n,):
+            raise ValueError("hdiag must have core_total entries")
+        e, res = np.zeros(R), np.zeros(R)
+        out = np.zeros((n, R), order="F")
+        it = ctypes.c_int(0)
+        self._check(self.L.fcg_bst_davidson(self.h, R, _ptr(v), _ptr(hd) if hd is not None else None, int(max_iter),
+                                            int(max_ss_vecs), float(tol), float(lindep), PRECISION[precision],
+                                            _ptr(e), _ptr(out), _ptr(res), ctypes.byref(it)), "fcg_bst_davidson")
+        return e, np.ascontiguousarray(out), res, it.value
 
     def bst_sigma_device(self, d_cores_ptr: int, d_sigma_ptr: int, R: int, precision="fp64"):
         self._check(self.L.fcg_bst_sigma_device(self.h, R, ctypes.c_void_p(d_cores_ptr), ctypes.c_void_p(d_sigma_ptr),

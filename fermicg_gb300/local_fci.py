@@ -160,9 +160,12 @@ class LocalSpace:
         if dim == 0:
             return np.zeros((0, 0))
         E = self.one_body_E(na, nb)
+        n = E.shape[0]
         H = np.einsum("pq,pqij->ij", ints.h1, E)
-        EE = np.einsum("prij,qsjk->prqsik", E, E, optimize=True)
-        H += 0.5 * np.einsum("prqs,prqsik->ik", ints.h2, EE, optimize=True)
+        # 1/2 sum_pr E_pr W_pr with W_pr = sum_qs (pr|qs) E_qs: n^2 products of dim x dim
+        # matrices instead of the n^4 of E_pr E_qs
+        W = (ints.h2.reshape(n * n, n * n) @ E.reshape(n * n, dim * dim)).reshape(n * n, dim, dim)
+        H += 0.5 * np.matmul(E.reshape(n * n, dim, dim), W).sum(axis=0)
         H -= 0.5 * np.einsum("prrs,psik->ik", ints.h2, E, optimize=True)
         H += ints.h0 * np.eye(dim)
         return 0.5 * (H + H.T)

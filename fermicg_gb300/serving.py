@@ -37,6 +37,10 @@ class Request:
     max_iter: int = field(compare=False, default=200)
     shape: str = field(compare=False, default="")
     cache: bool = field(compare=False, default=False)  # store the Hamiltonian blocks (fcg_cache_hamiltonian)
+    # a BST solve (ci_solve, src/tucker_outer.jl:68-215) instead of a TPSCI one: the packed
+    # Tucker blocks (focks / cfgs unused; guess (core_total, R)) and the preconditioner diagonal
+    bst: object = field(compare=False, default=None)
+    bst_hd: np.ndarray = field(compare=False, default=None)
 
 
 @dataclass
@@ -58,14 +62,18 @@ class Result:
 def footprint_bytes(req: Request) -> int:
     """HBM a solve holds while admitted: operators (float64 + float32 copies), dressed
     operators (estimated as 8x the TDM blob, both precisions), the state index, and the
-    Davidson subspace (2 x 12R vectors) plus sigma working copies."""
-    n = req.focks.shape[0]
+    Davidson subspace (2 x 12R vectors) plus sigma working copies.  A BST solve holds its
+    operator cache instead of the dressed operators and index, estimated from its cores
+    (64 cached elements per core element, both precisions)."""
+    n = req.guess.shape[0]
     R = req.guess.shape[1]
     ops = req.packed_ops.data.size * 12
-    dressed = req.packed_ops.data.size * 8 * 12
     ints = req.packed_terms.ints.size * 12
-    index = n * (16 + 8 * 60)
     dav = n * 8 * (2 * (12 * R + R) + 6 * R)
+    if req.bst is not None:
+        return int(ops + ints + n * 64 * 12 + dav)
+    dressed = req.packed_ops.data.size * 8 * 12
+    index = n * (16 + 8 * 60)
     return int(ops + dressed + ints + index + dav)
 
 
@@ -90,6 +98,14 @@ class SolveServer:
         try:
             g.set_ops(req.packed_ops)
             g.set_terms(req.packed_terms)
+            if req.bst is not None:
+                g.bst_set(req.bst)
+                e, X, res, it = g.bst_davidson(req.guess, req.bst_hd, tol=req.tol, max_iter=req.max_iter,
+                                               precision=req.precision)
+                end = time.perf_counter()
+                with self._lock:
+                    self.results.append(Result(req.rid, req.shape, e, res, it, req.arrival, start, end))
+                return
             g.state_set(req.focks, req.cfgs)
             if req.cache:  # within the memory the admitted solves leave free, else the direct build
                 with self._lock:
@@ -207,17 +223,24 @@ class NativeSolveServer:
         try:
             g.set_ops(req.packed_ops)
             g.set_terms(req.packed_terms)
-            g.state_set(req.focks, req.cfgs)
-            if req.cache:
-                try:
-                    g.cache_hamiltonian(self.cache_budget)
-                except FcgError:  # larger than a request may store: the direct build
-                    pass
             v = np.asfortranarray(req.guess, dtype=np.float64)
             n, R = v.shape
             ticket = ct.c_int64(0)
-            g._check(self.L.fcg_submit(self.h, g.h, R, _ptr(v), int(req.max_iter), 12, float(req.tol), 1e-12,
-                                       PRECISION[req.precision], 1, ct.byref(ticket)), "fcg_submit")
+            if req.bst is not None:
+                g.bst_set(req.bst)
+                hd = None if req.bst_hd is None else np.ascontiguousarray(req.bst_hd, dtype=np.float64)
+                g._check(self.L.fcg_submit_bst(self.h, g.h, R, _ptr(v), _ptr(hd) if hd is not None else None,
+                                               int(req.max_iter), 12, float(req.tol), 1e-12, PRECISION[req.precision],
+                                               ct.byref(ticket)), "fcg_submit_bst")
+            else:
+                g.state_set(req.focks, req.cfgs)
+                if req.cache:
+                    try:
+                        g.cache_hamiltonian(self.cache_budget)
+                    except FcgError:  # larger than a request may store: the direct build
+                        pass
+                g._check(self.L.fcg_submit(self.h, g.h, R, _ptr(v), int(req.max_iter), 12, float(req.tol), 1e-12,
+                                           PRECISION[req.precision], 1, ct.byref(ticket)), "fcg_submit")
             e, res = np.zeros(R), np.zeros(R)
             X = np.zeros((n, R), order="F")
             it = ct.c_int(0)

@@ -277,6 +277,40 @@ def config3_instance(i, base_seed=3000, max_cluster=5, n_cfg_range=(1000, 4000))
     return prob, st
 
 
+def config3_packed(i, base_seed=3000, max_cluster=5, n_cfg_range=(1000, 4000)):
+    """config3_instance i in the form the C ABI takes: (PackedOps, PackedTerms, fock, cfg,
+    coefficients).  Small enough to return from a worker process."""
+    from . import pack
+    prob, st = config3_instance(i, base_seed, max_cluster, n_cfg_range)
+    f, c, v, _ = pack.pack_state(st)
+    return pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, v
+
+
+def config3_batch(n_inst, max_cluster=5, workers=None):
+    """The first n_inst config-3 instances (config3_packed), built in parallel in worker
+    processes started with spawn (safe after CUDA is initialised in the caller)."""
+    import multiprocessing as mp
+    import os
+    from concurrent.futures import ProcessPoolExecutor
+    workers = workers or min(16, os.cpu_count() or 1)
+    if workers <= 1 or n_inst < 8:
+        return [config3_packed(i, max_cluster=max_cluster) for i in range(n_inst)]
+    # one BLAS thread per worker (the workers start with this environment)
+    keys = ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS")
+    saved = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ[k] = "1"
+    try:
+        with ProcessPoolExecutor(workers, mp_context=mp.get_context("spawn")) as ex:
+            return list(ex.map(config3_packed, range(n_inst), [3000] * n_inst, [max_cluster] * n_inst, chunksize=2))
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
 def davidson_guess(n, R, seed=0, lowest=None, spread=0.05):
     """Starting block for R roots of an n-configuration problem: unit vectors on the
     configurations `lowest` (default the first R, the lowest in an energy-ordered space; pass

@@ -165,6 +165,18 @@ int fcg_sigma_open_fetch(fcg_ctx* ctx, int16_t* fock, int16_t* cfg, double* coef
 int fcg_davidson(fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol, double lindep,
                  int precision, int precond, double* energies, double* vectors, double* residuals, int* iters);
 
+/* The Davidson solve of the BST ci_solve (src/tucker_outer.jl:68-215, BlockDavidson with the
+ * build_sigma! matvec of :101-112) on the device: R lowest eigenpairs of H over the cores of
+ * the last fcg_bst_set (vector length core_total, [R][core_total] for v0 and vectors, like
+ * fcg_bst_sigma).  hdiag (core_total values, or NULL) is the preconditioner diagonal (the
+ * reference's precond option passes its Hcmf diagonal); NULL runs unpreconditioned (the
+ * reference's precond = false).  Settings, precision and results as fcg_davidson; FCG_FP32
+ * builds every sigma but the final refinements in float32, its GEMM-shaped groups on the
+ * tensor cores. */
+int fcg_bst_davidson(fcg_ctx* ctx, int R, const double* v0, const double* hdiag, int max_iter, int max_ss_vecs,
+                     double tol, double lindep, int precision, double* energies, double* vectors,
+                     double* residuals, int* iters);
+
 /* The Davidson solves of n independent problems (one context each, state set) in lockstep:
  * every problem runs fcg_davidson's algorithm on its lane's stream (below).  In each round
  * every problem advances to its next need of the device (host work on a thread pool); then
@@ -209,6 +221,10 @@ int fcg_server_create(int device, int max_active, int lanes, double memory_budge
 int fcg_server_destroy(fcg_server* s);
 int fcg_submit(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, int max_iter, int max_ss_vecs, double tol,
                double lindep, int precision, int precond, int64_t* ticket);
+/* A BST solve (fcg_bst_davidson's arguments) as a request: the context's fcg_bst_set
+ * structure is the problem; the results come back through fcg_wait (vectors core_total x R). */
+int fcg_submit_bst(fcg_server* s, fcg_ctx* ctx, int R, const double* v0, const double* hdiag, int max_iter,
+                   int max_ss_vecs, double tol, double lindep, int precision, int64_t* ticket);
 int fcg_poll(fcg_server* s, int64_t ticket, int* state);
 int fcg_wait(fcg_server* s, int64_t ticket, int timeout_ms, double* energies, double* vectors, double* residuals,
              int* iters);
