@@ -150,11 +150,42 @@ def _shape_32o(seed):
     return workloads.build_problem(32, [4] * 8, [(2, 2)] * 8, 96, seed, max_roots=8, delta_elec=2)
 
 
-SERVING_SHAPES = [  # (name, builder(seed), n_cfg, roots, share of the serving stream)
+def _shape_32o_bst(seed):
+    """A config-2-shaped request: the 32-orbital / 8-cluster x 4 problem (local bases of 16
+    states per sector), BST blocks of the reference sector with at most two excited clusters,
+    Tucker ranks 4-12."""
+    from fermicg_gb300 import workloads
+    return workloads.build_problem(32, [4] * 8, [(2, 2)] * 8, 96, seed, max_roots=16, delta_elec=2)
+
+
+SERVING_SHAPES = [  # (name, builder(seed), n_cfg (TPSCI) or None (BST), roots, share of the serving stream)
     ("12o_4x3_full", _shape_12o, 2000, 1, 0.6),
     ("24o_6x4_M16", _shape_24o, 10000, 4, 0.3),
-    ("32o_8x4_M8", _shape_32o, 5000, 2, 0.1),
+    ("32o_8x4_bst_q2", _shape_32o_bst, None, 2, 0.1),
 ]
+
+# the per-shape Davidson timings also cover the earlier TPSCI request of the 32-orbital shape
+DAVIDSON_SHAPES = [
+    ("12o_4x3_full", _shape_12o, 2000, 1),
+    ("24o_6x4_M16", _shape_24o, 10000, 4),
+    ("32o_8x4_M8", lambda seed: _shape_32o(seed), 5000, 2),
+]
+
+
+def _bst_request_parts(prob, R, seed):
+    """(PackedOps, PackedTerms, PackedBST, guess (core_total, R), preconditioner diagonal) of a
+    BST solve of the reference sector of `prob` (at most two excited clusters, ranks 4-12)."""
+    from fermicg_gb300 import pack
+    from fermicg_gb300.bst import PackedBST, hcmf_diagonal, synthetic_bst
+    ref = tuple(tuple(f) for f in prob.init_fspace)
+    vec = synthetic_bst(prob, [ref], max_q=2, rank_range=(4, 12), R=R, seed=seed)
+    pb = PackedBST(vec, len(prob.clusters), R)
+    hd = hcmf_diagonal(pb, vec, prob.ops)
+    rng = np.random.default_rng(seed)
+    guess = 0.05 * rng.standard_normal((pb.core_total, R)) / np.sqrt(pb.core_total)
+    for r, k in enumerate(np.argsort(hd)[:R]):
+        guess[k, r] += 1.0
+    return pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), pb, guess, hd
 
 
 def headline_solve(g, n, R, tol=1e-6):
@@ -191,7 +222,7 @@ def davidson_benchmark(reps=2, stored=True):
     from fermicg_gb300.gpu import GpuSigma
     g = GpuSigma(0)
     out = {}
-    for name, build, n_cfg, R, _ in SERVING_SHAPES:
+    for name, build, n_cfg, R in DAVIDSON_SHAPES:
         prob = build(1001)
         st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=0)
         f, c, v, _ = pack.pack_state(st)
@@ -233,66 +264,78 @@ def davidson_benchmark(reps=2, stored=True):
     return out
 
 
-def serving_benchmark(n_req=60, rate=200.0, seed=7, slots=16, lanes=4, stored=True):
-    """Poisson stream of Davidson solves (60/30/10 % from three problem shapes, fresh seeds
-    per problem), served by the continuous-batching loop; mixed and FP64 runs of the same
-    stream.  Returns p50/p99 latency and solves/s per precision."""
+def serving_benchmark(n_req=600, rate=200.0, steady_rate=40.0, seed=7, slots=16, lanes=4):
+    """Poisson streams of Davidson solves drawn 60/30/10 % from three problem shapes (12- and
+    24-orbital TPSCI requests with stored Hamiltonian blocks, 32-orbital BST requests), tol
+    1e-6, mixed and FP64: n_req requests at the stated arrival rate (above the GPU's capacity:
+    the queue grows, and latency with it) and at a rate below capacity (steady state), served
+    by the thread-per-slot server and the library's continuous-batching server.  Returns p50 /
+    p99 latency and solves/s per run, and the largest energy difference of a request between
+    runs."""
     from fermicg_gb300 import pack, workloads
     from fermicg_gb300.serving import NativeSolveServer, Request, SolveServer, latency_summary
     shapes = SERVING_SHAPES
     pools = []
     for k, (name, build, n_cfg, R, share) in enumerate(shapes):
         pool = []
-        for j in range(2 if k < 2 else 1):
+        for j in range(4 if n_cfg is not None else 2):
             prob = build(1000 * (k + 1) + j)
+            if n_cfg is None:
+                pool.append(("bst",) + _bst_request_parts(prob, R, seed=j))
+                continue
             st = workloads.energy_ordered_space(prob, n_cfg, R=R, seed=j)
             f, c, v, _ = pack.pack_state(st)
             guess = workloads.davidson_guess(f.shape[0], R, seed=j)
-            pool.append((pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, guess))
+            pool.append(("tpsci", pack.pack_ops(prob.ops, prob.bases), pack.pack_terms(prob.ham), f, c, guess))
         pools.append(pool)
     rng = np.random.default_rng(seed)
-    arrivals = np.cumsum(rng.exponential(1.0 / rate, n_req))
+    gaps = rng.exponential(1.0, n_req)
     kinds = rng.choice(len(shapes), size=n_req, p=[sh[4] for sh in shapes])
     picks = [int(rng.integers(len(pools[k]))) for k in kinds]
-    out = {}
+
+    def requests(prec, lam):
+        arrivals = np.cumsum(gaps / lam)
+        out = []
+        for i in range(n_req):
+            item = pools[kinds[i]][picks[i]]
+            if item[0] == "bst":
+                _, po, pt, pb, guess, hd = item
+                out.append(Request(float(arrivals[i]), i, po, pt, None, None, guess, tol=1e-6, precision=prec,
+                                   shape=shapes[kinds[i]][0], bst=pb, bst_hd=hd))
+            else:
+                _, po, pt, f, c, guess = item
+                out.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
+                                   shape=shapes[kinds[i]][0], cache=True))
+        return out
+
+    out = {"requests": n_req, "slots": slots, "mix": {sh[0]: sh[4] for sh in shapes},
+           "arrival_rate_per_s": rate, "steady_rate_per_s": steady_rate,
+           "servers": {"threads": "one context, stream and host thread per slot; solves overlap on the GPU",
+                       "native": f"fcg_server: continuous batching in {lanes} lanes (a scheduler thread and a "
+                                 "stream each); a lane's solves run in lockstep rounds, one grouped sigma launch "
+                                 "per precision per round"},
+           "note": "TPSCI requests store their Hamiltonian blocks after fcg_state_set (assembly inside the "
+                   "request's latency); BST requests plan and cache their operators in fcg_bst_set"}
     energies = {}
-    for cache in ((False, True) if stored else (False,)):
-        for server in ("threads", "native"):
-            for prec in ("fp32", "fp64"):
-                reqs = []
-                for i in range(n_req):
-                    po, pt, f, c, guess = pools[kinds[i]][picks[i]]
-                    reqs.append(Request(float(arrivals[i]), i, po, pt, f, c, guess, tol=1e-6, precision=prec,
-                                        shape=shapes[kinds[i]][0], cache=cache))
-                srv = SolveServer(slots=slots) if server == "threads" else NativeSolveServer(slots=slots, lanes=lanes)
-                res = srv.run(reqs)
-                srv.close()
-                energies[(cache, server, prec)] = {r.rid: r.energies for r in res}
-                summ = latency_summary(res)
-                summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
-                                          for sh in shapes}
-                key = "mixed" if prec == "fp32" else "fp64"
-                dest = out.setdefault("stored_blocks", {}) if cache else out
-                if server == "threads":
-                    dest[key] = summ
-                else:
-                    dest.setdefault("native", {})[key] = summ
-    if stored:
-        # the same requests with and without stored blocks: largest energy difference
-        out["stored_blocks"]["max_energy_difference_vs_direct"] = max(
-            float(np.abs(energies[(True, sv, p)][i] - energies[(False, sv, p)][i]).max())
-            for sv in ("threads", "native") for p in ("fp32", "fp64") for i in range(n_req))
-        out["stored_blocks"]["note"] = ("each request also runs fcg_cache_hamiltonian after fcg_state_set; its "
-                                        "latency includes that assembly")
-    out["servers"] = {"threads": "one context, stream and host thread per slot; solves overlap on the GPU",
-                      "native": f"fcg_server: continuous batching in {lanes} lanes (a scheduler thread and a "
-                                "stream each); a lane's solves run in lockstep rounds, one grouped sigma launch "
-                                "per precision per round"}
-    # same stream, same results: energies of mixed vs fp64 per request
-    out["requests"] = n_req
-    out["slots"] = slots
-    out["arrival_rate_per_s"] = rate
-    out["mix"] = {sh[0]: sh[4] for sh in shapes}
+    runs = [("native", rate), ("threads", rate), ("native", steady_rate), ("threads", steady_rate)]
+    for server, lam in runs:
+        for prec in ("fp32", "fp64"):
+            srv = SolveServer(slots=slots) if server == "threads" else NativeSolveServer(slots=slots, lanes=lanes)
+            res = srv.run(requests(prec, lam))
+            srv.close()
+            energies[(server, lam, prec)] = {r.rid: r.energies for r in res}
+            summ = latency_summary(res)
+            summ["by_shape_p50_s"] = {sh[0]: float(np.median([r.latency for r in res if r.shape == sh[0]] or [0]))
+                                      for sh in shapes}
+            summ["not_converged"] = int(sum(float(np.max(r.residuals)) >= 1e-6 for r in res))
+            key = f"{server}_{'steady' if lam == steady_rate else 'stated_rate'}"
+            out.setdefault(key, {})["mixed" if prec == "fp32" else "fp64"] = summ
+    keys = list(energies)
+    out["max_energy_difference_between_runs"] = max(
+        float(np.abs(energies[k][i] - energies[keys[0]][i]).max()) for k in keys for i in range(n_req))
+    out["max_energy_difference_mixed_vs_fp64"] = max(
+        float(np.abs(energies[(s_, l_, "fp32")][i] - energies[(s_, l_, "fp64")][i]).max())
+        for (s_, l_, p_) in keys if p_ == "fp32" for i in range(n_req))
     return out
 
 
@@ -819,7 +862,7 @@ def main():
         return
     if a.serving_only:
         if rank == 0:
-            print(json.dumps({"serving": serving_benchmark(stored=a.stored)}))
+            print(json.dumps({"serving": serving_benchmark()}))
         return
     if a.davidson_only:
         if rank == 0:
@@ -1001,7 +1044,7 @@ def main():
             out["headline_solve"] = {"error": str(ex)}
     if rank == 0 and a.serving:
         try:
-            out["serving"] = serving_benchmark(stored=a.stored)
+            out["serving"] = serving_benchmark()
         except Exception as ex:
             out["serving"] = {"error": str(ex)}
     if rank == 0 and a.open:

@@ -105,6 +105,8 @@ struct fcg_ctx {
   DevBuf<float> d_ints32;
   DevBuf<double> d_w64;
   DevBuf<float> d_w32;
+  std::vector<DressJob> dress_jobs;  // W blocks to build (fcg_set_terms), built by the first fcg_state_set
+  bool dressed = false;
   int n_trans = 0;
   std::vector<int16_t> trans;
   // state + plan

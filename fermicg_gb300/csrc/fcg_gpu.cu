@@ -774,6 +774,57 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   return FCG_OK;
 }
 
+}  // extern "C"
+
+// The dressed operators W of every term (and their column maxima for the open-sigma
+// screen) on the device, from the job list of fcg_set_terms; once per term set.
+static int ensure_dressed(fcg_ctx* ctx) {
+  if (ctx->dressed) return FCG_OK;
+  const std::vector<DressJob>& jobs = ctx->dress_jobs;
+  const int64_t w_total = ctx->n_w;
+  DressJob* d_jobs = nullptr;
+  FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, jobs.data(), jobs.size(), ctx->stream, &d_jobs));
+  FCG_CUDA(ctx->d_w64.alloc(std::max<int64_t>(w_total, 1)));
+  FCG_CUDA(ctx->d_w32.alloc(std::max<int64_t>(w_total, 1)));
+  if (!jobs.empty()) {
+    dress_kernel<<<unsigned(jobs.size()), 256, 0, ctx->stream>>>(d_jobs, ctx->d_op64.p, ctx->d_ints64.p,
+                                                                 ctx->d_w64.p);
+    FCG_CUDA(cudaGetLastError());
+    to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
+    FCG_CUDA(cudaGetLastError());
+  }
+  {
+    // Wmax[rest, k] per W block, indexed like w_index
+    std::vector<MaxJob> mj(jobs.size());
+    ctx->wmax_index.assign(ctx->w_index.size(), -1);
+    int64_t tot = 0;
+    for (size_t j = 0; j < jobs.size(); ++j) {
+      const DressJob& J = jobs[j];
+      mj[j] = MaxJob{J.w_off, tot, J.rest_len, J.mb, J.mk, 0};
+      tot += int64_t(J.rest_len) * J.mk;
+    }
+    for (size_t i = 0; i < ctx->w_index.size(); ++i) {
+      if (ctx->w_index[i] < 0) continue;
+      // jobs are in w_off order; find the job of this W block
+      auto it = std::lower_bound(jobs.begin(), jobs.end(), ctx->w_index[i],
+                                 [](const DressJob& J, int64_t v) { return J.w_off < v; });
+      ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
+    }
+    MaxJob* d_mj = nullptr;
+    FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, mj.data(), mj.size(), ctx->stream, &d_mj));
+    FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
+    if (!jobs.empty()) {
+      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj, ctx->d_w64.p, ctx->d_wmax.p);
+      FCG_CUDA(cudaGetLastError());
+    }
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job lists are reused by the next call
+  }
+  ctx->dressed = true;
+  return FCG_OK;
+}
+
+extern "C" {
+
 int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t n_ints, const double* ints,
                   int n_transfers, const int16_t* transfers) {
   if (!ctx) return FCG_EINVAL;
@@ -835,43 +886,11 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   FCG_CUDA(ctx->d_terms.upload(ctx->terms.data(), ctx->terms.size(), ctx->stream));
   FCG_CUDA(ctx->d_ints64.upload(ints, n_ints, ctx->stream));
   FCG_CUDA(ctx->d_ints32.upload(i32.data(), n_ints, ctx->stream));
-  DressJob* d_jobs = nullptr;
-  FCG_CUDA(fcg_ctx::stage(ctx->scratch_a, jobs.data(), jobs.size(), ctx->stream, &d_jobs));
-  FCG_CUDA(ctx->d_w64.alloc(std::max<int64_t>(w_total, 1)));
-  FCG_CUDA(ctx->d_w32.alloc(std::max<int64_t>(w_total, 1)));
-  if (!jobs.empty()) {
-    dress_kernel<<<unsigned(jobs.size()), 256, 0, ctx->stream>>>(d_jobs, ctx->d_op64.p, ctx->d_ints64.p,
-                                                                 ctx->d_w64.p);
-    FCG_CUDA(cudaGetLastError());
-    to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
-    FCG_CUDA(cudaGetLastError());
-  }
-  {
-    // Wmax[rest, k] per W block, indexed like w_index
-    std::vector<MaxJob> mj(jobs.size());
-    ctx->wmax_index.assign(ctx->w_index.size(), -1);
-    int64_t tot = 0;
-    for (size_t j = 0; j < jobs.size(); ++j) {
-      const DressJob& J = jobs[j];
-      mj[j] = MaxJob{J.w_off, tot, J.rest_len, J.mb, J.mk, 0};
-      tot += int64_t(J.rest_len) * J.mk;
-    }
-    for (size_t i = 0; i < ctx->w_index.size(); ++i) {
-      if (ctx->w_index[i] < 0) continue;
-      // jobs are in w_off order; find the job of this W block
-      auto it = std::lower_bound(jobs.begin(), jobs.end(), ctx->w_index[i],
-                                 [](const DressJob& J, int64_t v) { return J.w_off < v; });
-      ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
-    }
-    MaxJob* d_mj = nullptr;
-    FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, mj.data(), mj.size(), ctx->stream, &d_mj));
-    FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
-    if (!jobs.empty()) {
-      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj, ctx->d_w64.p, ctx->d_wmax.p);
-      FCG_CUDA(cudaGetLastError());
-    }
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job lists are reused by the next call
-  }
+  // the dressed operators themselves are built on the device by the first fcg_state_set
+  // (only the closed and open sigmas use them; a BST-only context never needs them)
+  ctx->dress_jobs.swap(jobs);
+  ctx->dressed = false;
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_terms = true;
   return FCG_OK;
 }
@@ -881,6 +900,10 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_REQUIRE(ctx->have_ops && ctx->have_terms, FCG_ESTATE, "upload ops and terms first");
   FCG_REQUIRE(n_cfg > 0 && fock && cfg, FCG_EINVAL, "empty state");
   FCG_CUDA(cudaSetDevice(ctx->device));
+  {
+    const int rc = ensure_dressed(ctx);
+    if (rc) return rc;
+  }
   auto t0 = std::chrono::steady_clock::now();
   ProblemInfo pi;
   pi.N = ctx->N;

@@ -183,7 +183,8 @@ class NativeSolveServer:
     """The library's continuous-batching server (fcg_server_create / fcg_submit / fcg_wait).
 
     Each request is set up in a host thread of its own (a pooled context: fcg_set_ops,
-    fcg_set_terms, fcg_state_set) and submitted when ready; the library's `lanes` scheduler
+    fcg_set_terms, fcg_state_set; at most 2 x slots requests hold a context at one time, the
+    others wait in arrival order) and submitted when ready; the library's `lanes` scheduler
     threads (a stream each) admit requests while fewer than `slots` run and the memory budget
     allows, and each advances its admitted solves together: one wait for its stream, or one
     grouped sigma launch per precision, per round for all of them, with finished solves
@@ -206,6 +207,9 @@ class NativeSolveServer:
         self._free = []
         self._lock = threading.Lock()
         self.results: list[Result] = []
+        # requests prepared or in the library at one time: each holds a context with its problem
+        # on the device, so the rest wait on the host (in arrival order) until one ends
+        self._prepared = threading.Semaphore(2 * int(slots))
 
     def _context(self):
         with self._lock:
@@ -218,6 +222,7 @@ class NativeSolveServer:
         wait = req.arrival - time.perf_counter()
         if wait > 0:
             time.sleep(wait)
+        self._prepared.acquire()
         start = time.perf_counter()
         g = self._context()
         try:
@@ -255,6 +260,7 @@ class NativeSolveServer:
         finally:
             with self._lock:  # the pooled context keeps its buffers for the next request
                 self._free.append(g)
+            self._prepared.release()
 
     def run(self, requests: list[Request], t0: float | None = None):
         """Serve `requests` (arrival times relative to t0 = now); returns the results by id."""
