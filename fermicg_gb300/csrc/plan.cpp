@@ -316,50 +316,80 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
   }
   if (tots >= (size_t(1) << 31)) return "term-sector pool exceeds 2^31 records";
   if (tot >= (size_t(1) << 31)) return "work items exceed 2^31";
-  P.items.reserve(tot);
-  P.ts_pool.reserve(tots);
-  std::vector<int64_t> job_off(n_sec + 1, 0);
-  for (int64_t sb = 0; sb < n_sec; ++sb) job_off[sb + 1] = job_off[sb] + int64_t(tJobs[sb].size());
-  std::vector<PJob> pj(static_cast<size_t>(job_off[n_sec]));
+  // concatenation in sector order, each sector's part copied by one thread
+  std::vector<int64_t> item_off(n_sec + 1, 0), tsp_off(n_sec + 1, 0), job_off(n_sec + 1, 0);
   for (int64_t sb = 0; sb < n_sec; ++sb) {
-    const int32_t base = int32_t(P.ts_pool.size());
-    for (WorkItem w : tItems[sb]) {
-      w.ts_off += base;
-      P.items.push_back(w);
-    }
-    PJob* dst = &pj[size_t(job_off[sb])];
-    for (const PJob& q : tJobs[sb]) {
-      *dst = q;
-      dst->j.ts_off += base;
-      ++dst;
-    }
-    P.ts_pool.insert(P.ts_pool.end(), tTS[sb].begin(), tTS[sb].end());
+    item_off[sb + 1] = item_off[sb] + int64_t(tItems[sb].size());
+    tsp_off[sb + 1] = tsp_off[sb] + int64_t(tTS[sb].size());
+    job_off[sb + 1] = job_off[sb] + int64_t(tJobs[sb].size());
     P.flops_ref += tFlop[sb];
     P.flops_dressed += tFlopD[sb];
   }
+  P.items.resize(tot);
+  P.ts_pool.resize(tots);
+#pragma omp parallel for schedule(dynamic, 8)
+  for (int64_t sb = 0; sb < n_sec; ++sb) {
+    const int32_t base = int32_t(tsp_off[sb]);
+    WorkItem* di = P.items.data() + item_off[sb];
+    for (const WorkItem& w : tItems[sb]) {
+      *di = w;
+      di->ts_off += base;
+      ++di;
+    }
+    std::copy(tTS[sb].begin(), tTS[sb].end(), P.ts_pool.begin() + tsp_off[sb]);
+    for (PJob& q : tJobs[sb]) q.j.ts_off += base;
+    std::vector<WorkItem>().swap(tItems[sb]);
+    std::vector<TermSector>().swap(tTS[sb]);
+  }
   // Lane jobs of windows of kSortWindow bra sectors sorted by term shape, then by decreasing
-  // cost (stable: the rows of one work item stay together and share their kets), so that the
-  // 32 lanes of a warp run the same code on about the same number of kets.
+  // cost (ties in planning order: the rows of one work item stay together and share their kets), so that the
+  // 32 lanes of a warp run the same code on about the same number of kets.  The last warp task
+  // is padded with idle lanes (len 0).
+  const int64_t n_jobs = job_off[n_sec];
+  const int64_t n_wt = (n_jobs + 31) / 32;  // warp tasks
+  P.jobs.resize(size_t(n_wt) * 32);
+  for (int64_t i = n_jobs; i < n_wt * 32; ++i) P.jobs[size_t(i)] = LaneJob{0, 0, 0, 0, 0};
+  std::vector<int32_t> job_cost(static_cast<size_t>(n_jobs));
   {
     constexpr int64_t kSortWindow = 8;
     const int64_t n_win = (n_sec + kSortWindow - 1) / kSortWindow;
-#pragma omp parallel for schedule(dynamic, 1)
-    for (int64_t wdx = 0; wdx < n_win; ++wdx) {
-      const int64_t a = job_off[wdx * kSortWindow], b = job_off[std::min(n_sec, (wdx + 1) * kSortWindow)];
-      std::stable_sort(pj.begin() + a, pj.begin() + b, [](const PJob& x, const PJob& y) {
-        return x.nbody != y.nbody ? x.nbody < y.nbody : x.cost > y.cost;
-      });
+#pragma omp parallel
+    {
+      std::vector<uint64_t> keys;  // (nbody, decreasing cost, position in the window): one sort key
+      std::vector<const PJob*> src;
+#pragma omp for schedule(dynamic, 1)
+      for (int64_t wdx = 0; wdx < n_win; ++wdx) {
+        const int64_t s0 = wdx * kSortWindow, s1 = std::min(n_sec, (wdx + 1) * kSortWindow);
+        keys.clear();
+        src.clear();
+        for (int64_t sb = s0; sb < s1; ++sb)
+          for (const PJob& q : tJobs[sb]) {
+            const uint64_t c = uint64_t(std::min<int32_t>(q.cost, (1 << 26) - 1));
+            keys.push_back((uint64_t(q.nbody) << 58) | (((uint64_t(1) << 26) - 1 - c) << 32) | uint64_t(src.size()));
+            src.push_back(&q);
+          }
+        std::sort(keys.begin(), keys.end());
+        const int64_t o = job_off[s0];
+        for (size_t i = 0; i < keys.size(); ++i) {
+          const PJob& q = *src[size_t(keys[i] & 0xFFFFFFFFu)];
+          P.jobs[size_t(o) + i] = q.j;
+          job_cost[size_t(o) + i] = q.cost;
+        }
+        for (int64_t sb = s0; sb < s1; ++sb) std::vector<PJob>().swap(tJobs[sb]);
+      }
     }
   }
-  const int64_t n_jobs = int64_t(pj.size());
-  const int64_t n_wt = (n_jobs + 31) / 32;  // warp tasks
-  P.jobs.assign(size_t(n_wt) * 32, LaneJob{0, 0, 0, 0, 0});
-  for (int64_t i = 0; i < n_jobs; ++i) P.jobs[size_t(i)] = pj[size_t(i)].j;
   P.wt_cost.assign(size_t(n_wt), 0);
   P.wt_len.assign(size_t(n_wt), 0);
-  for (int64_t i = 0; i < n_jobs; ++i) {
-    P.wt_cost[size_t(i / 32)] = std::max(P.wt_cost[size_t(i / 32)], pj[size_t(i)].cost);
-    P.wt_len[size_t(i / 32)] = std::max<int32_t>(P.wt_len[size_t(i / 32)], pj[size_t(i)].j.len);
+#pragma omp parallel for schedule(static)
+  for (int64_t w = 0; w < n_wt; ++w) {
+    int32_t c = 0, l = 0;
+    for (int64_t i = w * 32; i < std::min(n_jobs, w * 32 + 32); ++i) {
+      c = std::max(c, job_cost[size_t(i)]);
+      l = std::max<int32_t>(l, P.jobs[size_t(i)].len);
+    }
+    P.wt_cost[size_t(w)] = c;
+    P.wt_len[size_t(w)] = l;
   }
   P.task_values = 0;
   for (int32_t l : P.wt_len) P.task_values += 32 * int64_t(l);
