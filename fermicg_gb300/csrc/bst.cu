@@ -464,9 +464,9 @@ struct BstTcJob {
 constexpr int kTcThreads = 128;  // one warpgroup: thread i owns TMEM lane / tile row i
 constexpr int kTcM = 128;        // tile rows (MMA M)
 constexpr int kTcN = 256;        // tile columns at most (MMA N, a multiple of 16)
-constexpr int kTcK = 32;         // K elements staged per round: four 8-element MMA steps
+constexpr int kTcK = 16;         // K elements staged per round: two 8-element MMA steps
 constexpr int kTcTmemCols = 256;
-constexpr int kTcSmem = 2 * kTcM * kTcK * 4 + 2 * kTcN * kTcK * 4 + 64;
+constexpr int kTcSmem = 2 * (2 * kTcM * kTcK * 4 + 2 * kTcN * kTcK * 4) + 64;  // two stages
 constexpr long long kTcWaitCycles = 4000000000LL;  // about 2 s at 2 GHz: a stuck MMA becomes an error
 // groups that go to the tensor cores: at least kTcMinM bra-active rows, kTcMinK ket-active
 // columns and kTcMinN spectator columns over all roots
@@ -484,7 +484,11 @@ __global__ void __launch_bounds__(kBstThreads) bst_tc_prep_kernel(const int32_t*
   bst_group_prepare<float, kBstThreads>(G, R, S, perm, cin, core_total, ws_all + ws_off[blockIdx.x], G.ws);
 }
 
-__global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJob* __restrict__ jobs,
+// Two shared-memory stages: while the tensor cores multiply the tiles of one K step (16 K
+// elements), the four warps stage the next step into the other stage, split into TF32 high
+// and low parts (48 KB per stage: two CTAs per SM).  An mbarrier per stage,
+// armed by tcgen05.commit, tells when a stage's MMAs are done and it may be overwritten.
+__global__ void __launch_bounds__(kTcThreads, 2) bst_tc_gemm_kernel(const BstTcJob* __restrict__ jobs,
                                                                    const BstGroup* __restrict__ groups, int R,
                                                                    const float* __restrict__ op,
                                                                    const float* __restrict__ ws_all,
@@ -493,13 +497,12 @@ __global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJ
                                                                    float* __restrict__ cout, int64_t core_total,
                                                                    unsigned* __restrict__ err) {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
-  unsigned char* a_hi = tc_smem;
-  unsigned char* a_lo = a_hi + kTcM * kTcK * 4;
-  unsigned char* b_hi = a_lo + kTcM * kTcK * 4;
-  unsigned char* b_lo = b_hi + kTcN * kTcK * 4;
-  uint64_t* bar = reinterpret_cast<uint64_t*>(b_lo + kTcN * kTcK * 4);
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 1);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  constexpr int kAB = kTcM * kTcK * 4;  // bytes of one A operand copy (hi or lo) of a stage
+  constexpr int kBB = kTcN * kTcK * 4;  // bytes of one B operand copy
+  constexpr int kStage = 2 * kAB + 2 * kBB;
+  uint64_t* bar = reinterpret_cast<uint64_t*>(tc_smem + 2 * kStage);  // one per stage
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(bar + 2);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const BstTcJob J = jobs[blockIdx.x];
   const BstGroup& G = groups[J.g];
   const int m = G.m, k = G.k, ns = G.bcore / G.m, NT = ns * R;
@@ -509,41 +512,66 @@ __global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJ
   const float* A = op + G.op_off + int64_t(k) * J.m0;
   const float* X = ws_all + ws_off[J.tc];
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(tslot), kTcTmemCols);
-  if (tid == 0) tc::mbar_init(tc::smem_u32(bar), 1);
+  if (tid == 0) {
+    tc::mbar_init(tc::smem_u32(bar), 1);
+    tc::mbar_init(tc::smem_u32(bar + 1), 1);
+  }
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t taddr = *tslot;
   const uint32_t idesc = tc::idesc_tf32(kTcM, nI);
-  uint32_t phase = 0;
+  uint32_t phase[2] = {0u, 0u};
   bool ok = true;
-  for (int k0 = 0; k0 < k; k0 += kTcK) {
-    // A tile: thread tid loads row tid, 32 K elements (zero past m or k)
-    {
-      const bool rv = tid < rows;
-      const float* src = A + int64_t(k) * tid + k0;
-#pragma unroll 8
-      for (int q = 0; q < kTcK; ++q) {
-        const float x = (rv && k0 + q < k) ? __ldg(src + q) : 0.f;
+  const int ntile = (k + kTcK - 1) / kTcK;
+  for (int t = 0; t < ntile; ++t) {
+    const int st = t & 1, k0 = t * kTcK;
+    unsigned char* a_hi = tc_smem + st * kStage;
+    unsigned char* a_lo = a_hi + kAB;
+    unsigned char* b_hi = a_lo + kAB;
+    unsigned char* b_lo = b_hi + kBB;
+    if (t >= 2) {  // the MMAs of step t - 2 read this stage
+      const bool done = tc::mbar_wait(tc::smem_u32(bar + st), phase[st], kTcWaitCycles);
+      phase[st] ^= 1u;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
+    }
+    // a warp instruction moves 8 rows x 4 K elements: lane = (row within the group of 8, element
+    // within the group of 4), so that its shared-memory stores hit 32 different banks
+    const int rl = lane >> 2, ql = lane & 3;
+    // A: row groups warp, warp + 4, ...
+    for (int rg = warp; rg < kTcM / 8; rg += 4) {
+      const int r = 8 * rg + rl;
+      const float* src = A + int64_t(k) * r + k0;
+#pragma unroll
+      for (int q4 = 0; q4 < kTcK / 4; ++q4) {
+        const int q = 4 * q4 + ql;
+        const float x = (r < rows && k0 + q < k) ? __ldg(src + q) : 0.f;
         float hi, lo;
         tc::split_tf32(x, hi, lo);
-        const uint32_t o = (q >> 3) * (kTcM * 32) + tc::kmajor_off(tid, q & 7);
+        const uint32_t o = uint32_t(q >> 3) * (kTcM * 32) + tc::kmajor_off(r, q & 7);
         *reinterpret_cast<float*>(a_hi + o) = hi;
         *reinterpret_cast<float*>(a_lo + o) = lo;
       }
     }
-    // B tile: rows (columns of D) tid, tid + 128; row j = s + ns r is X_r[:, s]
-    for (int jj = tid; jj < nI; jj += kTcThreads) {
-      const bool cv = jj < cols;
-      const int jp = J.n0 + (cv ? jj : 0);
-      const int r = jp / ns, sidx = jp - r * ns;
-      const float* src = X + int64_t(2 * r + cur) * stride + int64_t(k) * sidx + k0;
-#pragma unroll 8
-      for (int q = 0; q < kTcK; ++q) {
-        const float x = (cv && k0 + q < k) ? __ldg(src + q) : 0.f;
+    // B: rows j = s + ns r (X_r[:, s]) of the tile's columns, in groups of 8
+    for (int jg = warp; jg < nI / 8; jg += 4) {
+      const int jj = 8 * jg + rl;
+      const float* src = nullptr;
+      if (jj < cols) {
+        const int jp = J.n0 + jj;
+        const int r = jp / ns, sidx = jp - r * ns;
+        src = X + int64_t(2 * r + cur) * stride + int64_t(k) * sidx + k0;
+      }
+#pragma unroll
+      for (int q4 = 0; q4 < kTcK / 4; ++q4) {
+        const int q = 4 * q4 + ql;
+        const float x = (src && k0 + q < k) ? __ldg(src + q) : 0.f;
         float hi, lo;
         tc::split_tf32(x, hi, lo);
-        const uint32_t o = (q >> 3) * (kTcN * 32) + tc::kmajor_off(jj, q & 7);
+        const uint32_t o = uint32_t(q >> 3) * (kTcN * 32) + tc::kmajor_off(jj, q & 7);
         *reinterpret_cast<float*>(b_hi + o) = hi;
         *reinterpret_cast<float*>(b_lo + o) = lo;
       }
@@ -553,23 +581,28 @@ __global__ void __launch_bounds__(kTcThreads, 1) bst_tc_gemm_kernel(const BstTcJ
     if (tid == 0) {
       tc::fence_after_sync();
       const int steps = min(kTcK / 8, (k - k0 + 7) / 8);
-      for (int st = 0; st < steps; ++st) {
-        const uint64_t ah = tc::smem_desc(tc::smem_u32(a_hi + st * kTcM * 32));
-        const uint64_t al = tc::smem_desc(tc::smem_u32(a_lo + st * kTcM * 32));
-        const uint64_t bh = tc::smem_desc(tc::smem_u32(b_hi + st * kTcN * 32));
-        const uint64_t bl = tc::smem_desc(tc::smem_u32(b_lo + st * kTcN * 32));
-        tc::mma_tf32(taddr, ah, bh, idesc, (k0 > 0 || st > 0) ? 1u : 0u);
+      for (int q = 0; q < steps; ++q) {
+        const uint64_t ah = tc::smem_desc(tc::smem_u32(a_hi + q * kTcM * 32));
+        const uint64_t al = tc::smem_desc(tc::smem_u32(a_lo + q * kTcM * 32));
+        const uint64_t bh = tc::smem_desc(tc::smem_u32(b_hi + q * kTcN * 32));
+        const uint64_t bl = tc::smem_desc(tc::smem_u32(b_lo + q * kTcN * 32));
+        tc::mma_tf32(taddr, ah, bh, idesc, (t > 0 || q > 0) ? 1u : 0u);
         tc::mma_tf32(taddr, ah, bl, idesc, 1u);
         tc::mma_tf32(taddr, al, bh, idesc, 1u);
       }
-      tc::mma_commit(tc::smem_u32(bar));
+      tc::mma_commit(tc::smem_u32(bar + st));
     }
-    // every thread waits for the MMAs (they read the tiles the next round overwrites)
-    const bool done = tc::mbar_wait(tc::smem_u32(bar), phase, kTcWaitCycles);
-    phase ^= 1u;
-    if (__syncthreads_or(!done)) {
-      ok = false;
-      break;
+  }
+  // the last one or two steps are still in flight
+  if (ok) {
+    for (int t = max(0, ntile - 2); t < ntile; ++t) {
+      const int st = t & 1;
+      const bool done = tc::mbar_wait(tc::smem_u32(bar + st), phase[st], kTcWaitCycles);
+      phase[st] ^= 1u;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
     }
   }
   tc::fence_after_sync();
