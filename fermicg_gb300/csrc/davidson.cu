@@ -856,10 +856,13 @@ struct DavidsonRun {
     vectors = vecs;
     residuals = res;
     iters = its;
-    if (bst)
+    if (bst) {
       FCG_REQUIRE(ctx->have_bst, FCG_ESTATE, "fcg_bst_set must come first");
-    else
+    } else {
       FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+      const int rc = ensure_plan(ctx);
+      if (rc) return rc;
+    }
     const int64_t n = bst ? ctx->bst_core_total : ctx->n_cfg;
     FCG_REQUIRE(v0 && energies && vectors && residuals && iters, FCG_EINVAL, "null pointer");
     FCG_REQUIRE(R >= 1 && R <= kMaxB && R <= n, FCG_ELIMIT, "R must be in [1, min(16, vector length)]");

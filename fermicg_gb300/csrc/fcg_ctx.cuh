@@ -86,6 +86,8 @@ struct fcg_ctx {
   std::vector<int> norb;
   int nmax = 0;
   bool have_ops = false, have_terms = false, have_state = false;
+  bool have_plan = false;             // the closed-sigma plan of the state (built on first use)
+  std::vector<int16_t> h_fock, h_cfg;  // the state's rows, for that plan
   std::vector<int64_t> opb;
   std::vector<BlockInfo> h_blocks;
   std::vector<int32_t> h_blk_index;
@@ -238,6 +240,11 @@ struct fcg_ctx {
 // host wait of fcg_sigma_closed_device; for drivers that keep working on the same stream
 // (fcg_gpu.cu)
 int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision);
+
+// The dressed operators of the term set, and the closed-sigma plan of the state, built on
+// first use (fcg_gpu.cu)
+int ensure_dressed(fcg_ctx* ctx);
+int ensure_plan(fcg_ctx* ctx);
 
 // BST sigma on device vectors [R][core_total] queued on ctx->stream without the host wait
 // (timed: CUDA events around the kernels), and the check of the tensor-core error flag (one

@@ -778,7 +778,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
 
 // The dressed operators W of every term (and their column maxima for the open-sigma
 // screen) on the device, from the job list of fcg_set_terms; once per term set.
-static int ensure_dressed(fcg_ctx* ctx) {
+int ensure_dressed(fcg_ctx* ctx) {
   if (ctx->dressed) return FCG_OK;
   const std::vector<DressJob>& jobs = ctx->dress_jobs;
   const int64_t w_total = ctx->n_w;
@@ -895,16 +895,9 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   return FCG_OK;
 }
 
-int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
-  if (!ctx) return FCG_EINVAL;
-  FCG_REQUIRE(ctx->have_ops && ctx->have_terms, FCG_ESTATE, "upload ops and terms first");
-  FCG_REQUIRE(n_cfg > 0 && fock && cfg, FCG_EINVAL, "empty state");
-  FCG_CUDA(cudaSetDevice(ctx->device));
-  {
-    const int rc = ensure_dressed(ctx);
-    if (rc) return rc;
-  }
-  auto t0 = std::chrono::steady_clock::now();
+}  // extern "C"
+
+static ProblemInfo problem_info(fcg_ctx* ctx) {
   ProblemInfo pi;
   pi.N = ctx->N;
   pi.norb = ctx->norb;
@@ -917,15 +910,29 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   pi.blocks = &ctx->h_blocks;
   pi.dress = &ctx->dress;
   pi.w_index = &ctx->w_index;
+  return pi;
+}
+
+// The rows of a state and its Fock sectors (checked), on the device; the closed-sigma plan
+// comes later (ensure_plan).
+static int state_rows_impl(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
+  FCG_REQUIRE(ctx->have_ops && ctx->have_terms, FCG_ESTATE, "upload ops and terms first");
+  FCG_REQUIRE(n_cfg > 0 && fock && cfg, FCG_EINVAL, "empty state");
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  const auto t0 = std::chrono::steady_clock::now();
   ctx->have_state = false;
+  ctx->have_plan = false;
   ctx->drop_hcache();
-  std::string msg = build_plan(pi, n_cfg, fock, cfg, ctx->plan);
+  const ProblemInfo pi = problem_info(ctx);
+  std::string msg = build_sectors(pi, n_cfg, fock, cfg, ctx->plan);
   FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   const Plan& P = ctx->plan;
   std::vector<int32_t> row_sector(n_cfg);
   for (size_t sct = 0; sct < P.sec_start.size(); ++sct)
     for (int64_t i = 0; i < P.sec_count[sct]; ++i) row_sector[P.sec_start[sct] + i] = int32_t(sct);
   ctx->n_cfg = n_cfg;
+  ctx->h_fock.assign(fock, fock + n_cfg * 2 * ctx->N);
+  ctx->h_cfg.assign(cfg, cfg + n_cfg * ctx->N);
   {
     std::vector<int16_t> cfg8(size_t(n_cfg) * kCfgStride, 0);
     for (int64_t i = 0; i < n_cfg; ++i)
@@ -934,6 +941,33 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   }
   FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
   FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
+  FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  ctx->stats.n_cfg = n_cfg;
+  ctx->stats.n_work_items = ctx->stats.n_triples = 0;  // until the plan is built
+  ctx->stats.flops_reference = ctx->stats.flops_executed = 0;
+  ctx->stats.n_sectors = int64_t(P.sec_start.size());
+  ctx->stats.plan_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx->tuned[0] = ctx->tuned[1] = -1;  // a new shape: tune again (or find it in the shape cache)
+  ctx->fine_built = false;
+  ctx->have_state = true;
+  return FCG_OK;
+}
+
+// The closed-sigma plan of the state (work items, lane jobs, warp chunks) and the dressed
+// operators, built on first use.
+int ensure_plan(fcg_ctx* ctx) {
+  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  if (ctx->have_plan) return FCG_OK;
+  {
+    const int rc = ensure_dressed(ctx);
+    if (rc) return rc;
+  }
+  const auto t0 = std::chrono::steady_clock::now();
+  const ProblemInfo pi = problem_info(ctx);
+  std::string msg = build_join(pi, ctx->h_fock.data(), ctx->h_cfg.data(), ctx->plan);
+  FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+  const Plan& P = ctx->plan;
   FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));
   FCG_REQUIRE(lane_ctas(int64_t(P.chunk_lo.size()) - 1) < (int64_t(1) << 31), FCG_ELIMIT,
               "too many warp chunks for one launch");
@@ -942,21 +976,28 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
   FCG_CUDA(ctx->d_chunk_val.upload(P.chunk_val.data(), P.chunk_val.size(), ctx->stream));
   FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
   FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
-  FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  auto t1 = std::chrono::steady_clock::now();
-  ctx->stats.n_cfg = n_cfg;
-  ctx->stats.n_sectors = int64_t(P.sec_start.size());
   ctx->stats.n_work_items = int64_t(P.items.size());
   ctx->stats.n_triples = P.n_triples;
   ctx->stats.flops_reference = P.flops_ref;
   ctx->stats.flops_executed = P.flops_dressed;
   ctx->stats.dressed_elements = ctx->n_w;
-  ctx->stats.plan_seconds = std::chrono::duration<double>(t1 - t0).count();
-  ctx->tuned[0] = ctx->tuned[1] = -1;  // a new shape: tune again (or find it in the shape cache)
-  ctx->fine_built = false;
-  ctx->have_state = true;
+  ctx->stats.plan_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx->have_plan = true;
   return FCG_OK;
+}
+
+extern "C" {
+
+int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
+  if (!ctx) return FCG_EINVAL;
+  const int rc = state_rows_impl(ctx, n_cfg, fock, cfg);
+  return rc ? rc : ensure_plan(ctx);
+}
+
+int fcg_state_rows(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
+  if (!ctx) return FCG_EINVAL;
+  return state_rows_impl(ctx, n_cfg, fock, cfg);
 }
 
 int fcg_set_tuning(fcg_ctx* ctx, int mode) {
@@ -1089,6 +1130,7 @@ template <typename T>
 static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* cin, T* sig, bool zero_sig = true,
                          bool timed = true) {
   const int prec = sizeof(T) == 4 ? 1 : 0;
+  FCG_REQUIRE(ctx->have_plan, FCG_ESTATE, "the closed-sigma plan is missing (fcg_state_set builds it)");
   if (!ctx->have_hcache && ctx->tune_mode < 0 && ctx->tuned[prec] < 0 && timed) {
     const int rc = tune_closed<T>(ctx, prec, R, w, op, cin, sig);
     if (rc) return rc;
@@ -1123,6 +1165,10 @@ static int launch_closed(fcg_ctx* ctx, int R, const T* w, const T* op, const T* 
 static int sigma_device_impl(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision,
                              bool wait = true) {
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  {
+    const int rc = ensure_plan(ctx);
+    if (rc) return rc;
+  }
   FCG_REQUIRE(R >= 1 && R <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
   FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
   const int64_t n = ctx->n_cfg;
@@ -1172,6 +1218,10 @@ int fcg_cache_hamiltonian(fcg_ctx* ctx, double max_bytes, int64_t* bytes) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
   FCG_CUDA(cudaSetDevice(ctx->device));
+  if (max_bytes > 0) {
+    const int rc = ensure_plan(ctx);
+    if (rc) return rc;
+  }
   const auto t0 = std::chrono::steady_clock::now();
   ctx->drop_hcache(!(max_bytes > 0));  // an explicit drop returns the memory
   ctx->stats.hcache_pairs = 0;
@@ -1219,6 +1269,13 @@ static int grouped_impl(int n, fcg_ctx* const* ctxs, const int* R, const double*
   int64_t cta = 0, cta_hc = 0, max_nr = 0;
   for (int q = 0; q < n; ++q) {
     fcg_ctx* c = ctxs[q];
+    if (!c->have_plan) {
+      const int rc = ensure_plan(c);
+      if (rc) {
+        ctx->err = c->err;
+        return rc;
+      }
+    }
     const int64_t nr = c->n_cfg * R[q];
     GroupEntry<T>& e = entries[q];
     e.p = make_lane_params(c, R[q]);
@@ -1458,7 +1515,8 @@ int noalloc_scratch(fcg_ctx* ctx, double** out) {
 extern "C" int fcg_sigma_closed_noalloc(fcg_ctx* ctx, int R, const double* d_c, double* d_sigma, int precision) {
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(d_c && d_sigma, FCG_EINVAL, "null pointer");
-  FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
+  FCG_REQUIRE(ctx->have_state && ctx->have_plan, FCG_ESTATE,
+              "fcg_state_set must come first (a state set by fcg_state_rows has no closed-sigma plan yet)");
   FCG_REQUIRE(R >= 1 && R <= kMaxR, FCG_ELIMIT, "R must be in [1, 16]");
   FCG_REQUIRE(precision == FCG_FP64 || precision == FCG_FP32, FCG_EINVAL, "unknown precision");
   FCG_REQUIRE(ctx->n_cfg * R <= kNoAllocMaxElems, FCG_ELIMIT,

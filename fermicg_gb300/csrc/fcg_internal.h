@@ -248,6 +248,11 @@ FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int f
   return ((((int64_t(c) * kNumOps + op) * nmax1 + fba) * nmax1 + fbb) * nmax1 + fka) * nmax1 + fkb;
 }
 
+// The plan of one state in two parts: build_sectors checks the rows and finds the Fock sectors
+// (enough for the diagonal and the open sigma); build_join adds the closed-sigma work items,
+// lane jobs and warp chunks.  build_plan does both.
+std::string build_sectors(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& plan);
+std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t* cfg, Plan& plan);
 std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& plan);
 
 // The term-sector record of term t between bra sector fb and ket sector fk (N x 2 each);

@@ -495,6 +495,10 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   FCG_REQUIRE(R >= 1 && R <= 16, FCG_ELIMIT, "R must be in [1, 16]");
   FCG_REQUIRE(thresh >= 0.0, FCG_EINVAL, "thresh must be >= 0");
   FCG_CUDA(cudaSetDevice(ctx->device));
+  {
+    const int rc = ensure_dressed(ctx);
+    if (rc) return rc;
+  }
   *n_out = 0;
   const int N = ctx->N;
   const int nmax1 = ctx->nmax + 1;

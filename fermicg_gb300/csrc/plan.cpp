@@ -91,7 +91,7 @@ bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int
   return true;
 }
 
-std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
+std::string build_sectors(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
   const int N = pi.N;
   const std::vector<int32_t>& trm = *pi.trm;
   const int n_terms = pi.n_terms;
@@ -131,7 +131,31 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
       if (bl < 0) return "a row uses a Fock sector with no local basis";
       if (cfg[i * N + c] >= (*pi.blocks)[bl].mb) return "local state index beyond the sector's basis";
     }
+  // 1-body terms of the zero transfer (compute_diagonal, src/tpsci_outer.jl:694-715)
+  for (int tr = 0; tr < n_trans; ++tr) {
+    bool zero = true;
+    for (int i = 0; i < 2 * N; ++i) zero &= trans[size_t(tr) * 2 * N + i] == 0;
+    if (zero)
+      for (int t = 0; t < n_terms; ++t)
+        if (TT(trm, t, 1) == tr) P.zero_terms.push_back(t);
+  }
+  return "";
+}
+
+std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t* cfg, Plan& P) {
+  (void)fock;
+  const int N = pi.N;
+  const std::vector<int32_t>& trm = *pi.trm;
+  const int n_terms = pi.n_terms;
+  const std::vector<int16_t>& trans = *pi.trans;
+  const int n_trans = pi.n_trans;
   const int64_t n_sec = int64_t(P.sec_start.size());
+  std::unordered_map<uint64_t, int32_t> sec_of;
+  for (int64_t sct = 0; sct < n_sec; ++sct) {
+    uint64_t k;
+    fock_key(&P.sec_fock[size_t(sct) * 2 * N], N, &k);
+    sec_of[k] = int32_t(sct);
+  }
 
   // ---- active sets and term lists per (transfer, set) ----------------------
   std::vector<uint32_t> masks;
@@ -166,13 +190,6 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
         if (by[tr][s].empty()) continue;
         tls[tr].push_back(TL{s, by[tr][s]});
       }
-    for (int tr = 0; tr < n_trans; ++tr) {
-      bool zero = true;
-      for (int i = 0; i < 2 * N; ++i) zero &= trans[size_t(tr) * 2 * N + i] == 0;
-      if (zero)
-        for (int t = 0; t < n_terms; ++t)
-          if (TT(trm, t, 1) == tr) P.zero_terms.push_back(t);
-    }
   }
   const int n_sets = int(masks.size());
 
@@ -399,6 +416,11 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
     P.prefix[i + 1] = P.prefix[i] + int64_t(P.items[i].nb) * P.items[i].nk * P.items[i].nt;
   P.n_triples = P.prefix.back();
   return "";
+}
+
+std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
+  std::string m = build_sectors(pi, n_cfg, fock, cfg, P);
+  return m.empty() ? build_join(pi, fock, cfg, P) : m;
 }
 
 void make_chunks(const Plan& P, int64_t target, std::vector<int64_t>& lo, std::vector<int64_t>& val) {

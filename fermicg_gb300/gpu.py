@@ -42,6 +42,7 @@ SIGNATURES = {
     "fcg_set_ops": (_I, [_P, _I, _P, _L, _P, _L, _P]),
     "fcg_set_terms": (_I, [_P, _I, _P, _L, _P, _I, _P]),
     "fcg_state_set": (_I, [_P, _L, _P, _P]),
+    "fcg_state_rows": (_I, [_P, _L, _P, _P]),
     "fcg_sigma_closed": (_I, [_P, _I, _P, _P, _I]),
     "fcg_sigma_closed_device": (_I, [_P, _I, _P, _P, _I]),
     "fcg_cache_hamiltonian": (_I, [_P, ctypes.c_double, ctypes.POINTER(ctypes.c_int64)]),
@@ -186,10 +187,14 @@ class GpuSigma:
         self.set_ops(pack.pack_ops(ops, bases))
         self.set_terms(pack.pack_terms(ham))
 
-    def state_set(self, focks, cfgs):
+    def state_set(self, focks, cfgs, plan: bool = True):
+        """The state's rows (TPSCIstate order) and, with plan (default), its closed-sigma plan;
+        plan=False sets only the rows and sectors (fcg_state_rows: diagonals, open sigma),
+        and the first closed sigma builds the plan."""
         f = np.ascontiguousarray(focks, dtype=np.int16)
         c = np.ascontiguousarray(cfgs, dtype=np.int16)
-        self._check(self.L.fcg_state_set(self.h, f.shape[0], _ptr(f), _ptr(c)), "fcg_state_set")
+        fn = self.L.fcg_state_set if plan else self.L.fcg_state_rows
+        self._check(fn(self.h, f.shape[0], _ptr(f), _ptr(c)), "fcg_state_set" if plan else "fcg_state_rows")
         self.n_cfg = f.shape[0]
 
     # --- sigma --------------------------------------------------------------

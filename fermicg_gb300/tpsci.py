@@ -40,9 +40,9 @@ class GpuTPSCI:
     def _flat(self, s) -> FlatTPSCI:
         return s if isinstance(s, FlatTPSCI) else FlatTPSCI.from_state(self.reg, s)
 
-    def _index(self, ctx, s: FlatTPSCI):
+    def _index(self, ctx, s: FlatTPSCI, plan: bool = True):
         f, c, v = s.rows()
-        ctx.state_set(np.ascontiguousarray(f), np.ascontiguousarray(c))
+        ctx.state_set(np.ascontiguousarray(f), np.ascontiguousarray(c), plan=plan)
         return v
 
     def solve(self, s, tol=1e-8, max_iter=200, max_ss_vecs=12, lindep=1e-12):
@@ -68,7 +68,7 @@ class GpuTPSCI:
 
     def open_sigma(self, s, thresh: float, nbody: int = 4):
         fs = self._flat(s)
-        v = self._index(self.H, fs)
+        v = self._index(self.H, fs, plan=False)  # the open sigma needs the rows and sectors only
         of, oc, ov = self.H.sigma_open(v, thresh, nbody)
         out = FlatTPSCI.from_rows(self.reg, fs.R, of, oc, ov)
         return out if isinstance(s, FlatTPSCI) else out.to_state()
@@ -77,7 +77,7 @@ class GpuTPSCI:
         fs = self._flat(s)
         if len(fs) == 0:
             return np.zeros(0)
-        self._index(self.H, fs)
+        self._index(self.H, fs, plan=False)  # compute_diagonal needs the rows and sectors only
         return self.H.diagonal("Hcmf")
 
     # ---- drivers -------------------------------------------------------------------------

@@ -118,6 +118,12 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
  * builds the device index used by every sigma call on this state. */
 int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg);
 
+/* The rows of a TPSCIstate and its Fock sectors only (no closed-sigma plan yet): enough for
+ * fcg_diagonal and fcg_sigma_open, as compute_diagonal (src/tpsci_outer.jl:694-787) and
+ * open_matvec_thread need.  A later closed sigma, cache or Davidson call on the state builds
+ * the plan first; fcg_sigma_closed_noalloc needs fcg_state_set (it allocates nothing). */
+int fcg_state_rows(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg);
+
 /* tps_ci_matvec (src/tpsci_outer.jl:462-527): sigma = H c within the state's
  * configurations.  Host buffers, column-major n_cfg x R; copies in and out
  * inside the call.  precision: FCG_FP64 or FCG_FP32. */

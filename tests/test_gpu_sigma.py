@@ -160,3 +160,27 @@ def test_closed_sigma_config1_30k_matches_oracle():
     g.cache_hamiltonian()
     assert rel_err(g.sigma_closed(x, "fp64"), ref) < FP64_TOL
     assert rel_err(g.sigma_closed(x, "fp32"), ref) < FP32_TOL
+
+
+def test_state_rows_then_diagonal_open_sigma_and_a_planned_sigma():
+    """fcg_state_rows sets rows and sectors only: the diagonal and the open sigma work on it,
+    and the first closed sigma builds the plan (same result as after fcg_state_set); the
+    allocation-free sigma refuses a state without a plan."""
+    import torch
+    from fermicg_gb300.gpu import FcgError
+    prob, st = config1_subspace(3000, 4)
+    g = GpuSigma(0)
+    po, pt = packed(prob)
+    g.set_ops(po)
+    g.set_terms(pt)
+    f, c, v, _ = pack.pack_state(st)
+    O = oracle.Oracle(po, pt)
+    g.state_set(f, c, plan=False)
+    assert g.stats()["n_triples"] == 0
+    np.testing.assert_allclose(g.diagonal(), O.diagonal_H(f, c), rtol=1e-12, atol=1e-12)
+    d_c = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(v).T)).cuda()
+    with pytest.raises(FcgError, match="plan"):
+        g.sigma_closed_noalloc(d_c.data_ptr(), d_c.data_ptr(), 4, "fp64")
+    _assert_open_equal(g.sigma_open(v[:, :2], 1e-3), O.sigma_open(f, c, v[:, :2], 1e-3))
+    assert rel_err(g.sigma_closed(v, "fp64"), O.sigma_closed(f, c, v)) < FP64_TOL
+    assert g.stats()["n_triples"] > 0
