@@ -1017,11 +1017,11 @@ def main():
                      "frac": achieved / hbm_peak,
                      # dram__bytes_read.sum + dram__bytes_write.sum of one float launch on this
                      # exact workload, from the ncu capture summarised in
-                     # profiles/closed_sigma_kernel_v4_24o6c.md
-                     "traffic": (190.4e6 + 3.2e6) if (n == 100000 and R == 4) else None,
-                     "note": "compulsory bytes per launch / closed_sigma_kernel time (fp32), of measured HBM "
-                             "copy peak; the kernel is bound by the L1 data pipe (80.6 % of peak wavefronts) "
-                             "and the double build by the FP64 pipe (87 %), not by HBM"},
+                     # profiles/closed_sigma_lane_kernel_24o6c.md
+                     "traffic": (334.6e6 + 1.5e6) if (n == 100000 and R == 4) else None,
+                     "note": "compulsory bytes per launch / closed_sigma_lane_kernel time (fp32), of measured HBM "
+                             "copy peak; the float kernel is bound by the L1 data pipe (87 % of peak) and the "
+                             "double kernel by the FP64 pipe, not by HBM"},
         "e2e": {"value": 1e3 / e2e_ms, "unit": "sigma_builds/s", "h2d_bytes_per_step": n * R * 8,
                 "d2h_bytes_per_step": n * R * 8},
         "gpu_launches": int(g.stats()["kernel_launches"]) * a.steps,
