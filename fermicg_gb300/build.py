@@ -10,7 +10,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libfcg_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["fcg_gpu.cu", "open_sigma.cu", "davidson.cu", "bst.cu", "bst_fois.cu", "plan.cpp"]
+SOURCES = ["fcg_gpu.cu", "open_sigma.cu", "davidson.cu", "bst.cu", "bst_fois.cu", "dplan.cu", "plan.cpp"]
 
 
 def _nvcc():
@@ -24,7 +24,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     deps = srcs + [os.path.join(CSRC, "fcg_internal.h"), os.path.join(CSRC, "fcg_ctx.cuh"),
                    os.path.join(CSRC, "small_dense.h"), os.path.join(CSRC, "tucker_small.cuh"),
-                   os.path.join(CSRC, "tcgen05.cuh"),
+                   os.path.join(CSRC, "tcgen05.cuh"), os.path.join(CSRC, "dprim.cuh"),
                    os.path.join(os.path.dirname(HERE), "include", "fcg_gpu.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in deps):
         return LIB

@@ -117,10 +117,33 @@ struct fcg_ctx {
   DevBuf<int16_t> d_cfg;
   DevBuf<int16_t> d_sec_fock;
   DevBuf<int32_t> d_row_sector;
-  DevBuf<WorkItem> d_items;
   DevBuf<LaneJob> d_jobs;           // closed-sigma lane jobs, 32 per warp task
   DevBuf<int64_t> d_chunk_lo;       // first warp task of each warp chunk
   DevBuf<int64_t> d_chunk_val;      // first stored value of each warp chunk
+  // sizes of the plan on the device (either planner): warp chunks of the chunk table, lane
+  // jobs (with the idle lanes of the last warp task), warp tasks, their summed cost, work
+  // items, term-sector records, permutation-pool entries
+  int64_t n_chunks = 0, plan_jobs = 0, plan_wt = 0, plan_total_cost = 0, plan_items = 0, plan_ts = 0,
+          plan_perm = 0;
+  bool plan_on_device = true;           // the join runs on the device (dplan.cu), else plan.cpp
+  DevBuf<int64_t> d_wt_cum, d_wt_vals;  // exclusive prefix of warp-task cost / stored values (device planner)
+  // device planner: the term set's tables on the device (uploaded at the first plan after
+  // fcg_set_ops / fcg_set_terms), the state's sector offsets, counters, grow-only arenas
+  struct {
+    bool ready = false;
+    TermLists lists;
+    int n_sets = 0, n_tl = 0, spec_bits = 0;
+    DevBuf<int32_t> d_trm;
+    DevBuf<TermDress> d_dress;
+    DevBuf<int64_t> d_w_index;
+    DevBuf<int16_t> d_trans;
+    DevBuf<int32_t> d_first_of_tr, d_tl_tr, d_tl_set, d_tl_off, d_tl_terms, d_tl_nbody;
+    DevBuf<uint8_t> d_spec_off;
+    DevBuf<int64_t> d_sec_start, d_sec_count;
+    DevBuf<unsigned long long> d_cnt;
+    PinnedBuf<unsigned long long> h_cnt;
+    DevBuf<unsigned char> arena[4];
+  } dj;
   // closed-sigma kernel tuning: candidate per precision (0 fp64, 1 fp32; -1 not yet tuned),
   // forced candidate (-1: auto), the finer chunk table of candidates 2-3, candidate timings
   int tuned[2] = {-1, -1};
@@ -245,6 +268,13 @@ int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_
 // first use (fcg_gpu.cu)
 int ensure_dressed(fcg_ctx* ctx);
 int ensure_plan(fcg_ctx* ctx);
+ProblemInfo problem_info(fcg_ctx* ctx);
+
+// The closed-sigma join of the state on the device (dplan.cu): fills d_perm, d_ts, d_jobs,
+// d_chunk_lo / d_chunk_val, d_wt_cum / d_wt_vals and the plan sizes; and a chunk table of
+// about `target` warp chunks over its warp tasks.
+int build_join_device(fcg_ctx* ctx);
+int device_chunks(fcg_ctx* ctx, int64_t target, DevBuf<int64_t>& lo, DevBuf<int64_t>& val, int64_t* n_chunks);
 
 // BST sigma on device vectors [R][core_total] queued on ctx->stream without the host wait
 // (timed: CUDA events around the kernels), and the check of the tensor-core error flag (one

@@ -628,7 +628,7 @@ static LaneParams make_lane_params(fcg_ctx* ctx, int R) {
   p.jobs = ctx->d_jobs.p;
   p.chunk_lo = ctx->d_chunk_lo.p;
   p.chunk_val = ctx->d_chunk_val.p;
-  p.n_chunks = int64_t(ctx->plan.chunk_lo.size()) - 1;
+  p.n_chunks = ctx->n_chunks;
   p.perm = ctx->d_perm.p;
   p.ts = ctx->d_ts.p;
   p.cfg = ctx->d_cfg.p;
@@ -768,6 +768,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   }
   ctx->have_ops = true;
   ctx->have_terms = false;
+  ctx->dj.ready = false;
   ctx->have_state = false;
   ctx->have_bst = false;
   ctx->drop_hcache();
@@ -890,6 +891,7 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
   // (only the closed and open sigmas use them; a BST-only context never needs them)
   ctx->dress_jobs.swap(jobs);
   ctx->dressed = false;
+  ctx->dj.ready = false;
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_terms = true;
   return FCG_OK;
@@ -897,7 +899,7 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
 
 }  // extern "C"
 
-static ProblemInfo problem_info(fcg_ctx* ctx) {
+ProblemInfo problem_info(fcg_ctx* ctx) {
   ProblemInfo pi;
   pi.N = ctx->N;
   pi.norb = ctx->norb;
@@ -964,25 +966,40 @@ int ensure_plan(fcg_ctx* ctx) {
     if (rc) return rc;
   }
   const auto t0 = std::chrono::steady_clock::now();
-  const ProblemInfo pi = problem_info(ctx);
-  std::string msg = build_join(pi, ctx->h_fock.data(), ctx->h_cfg.data(), ctx->plan);
-  FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+  if (ctx->plan_on_device) {
+    const int rc = build_join_device(ctx);
+    if (rc) return rc;
+  } else {
+    const ProblemInfo pi = problem_info(ctx);
+    std::string msg = build_join(pi, ctx->h_fock.data(), ctx->h_cfg.data(), ctx->plan);
+    FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+    const Plan& P = ctx->plan;
+    FCG_CUDA(ctx->d_jobs.upload(P.jobs.data(), P.jobs.size(), ctx->stream));
+    FCG_CUDA(ctx->d_chunk_lo.upload(P.chunk_lo.data(), P.chunk_lo.size(), ctx->stream));
+    FCG_CUDA(ctx->d_chunk_val.upload(P.chunk_val.data(), P.chunk_val.size(), ctx->stream));
+    FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
+    FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    ctx->n_chunks = int64_t(P.chunk_lo.size()) - 1;
+    ctx->plan_jobs = int64_t(P.jobs.size());
+    ctx->plan_wt = int64_t(P.wt_cost.size());
+    ctx->plan_total_cost = 0;
+    for (int32_t c : P.wt_cost) ctx->plan_total_cost += c;
+    ctx->plan_items = int64_t(P.items.size());
+    ctx->plan_ts = int64_t(P.ts_pool.size());
+    ctx->plan_perm = int64_t(P.perm_pool.size());
+  }
+  FCG_REQUIRE(lane_ctas(ctx->n_chunks) < (int64_t(1) << 31), FCG_ELIMIT, "too many warp chunks for one launch");
   const Plan& P = ctx->plan;
-  FCG_CUDA(ctx->d_items.upload(P.items.data(), P.items.size(), ctx->stream));
-  FCG_REQUIRE(lane_ctas(int64_t(P.chunk_lo.size()) - 1) < (int64_t(1) << 31), FCG_ELIMIT,
-              "too many warp chunks for one launch");
-  FCG_CUDA(ctx->d_jobs.upload(P.jobs.data(), P.jobs.size(), ctx->stream));
-  FCG_CUDA(ctx->d_chunk_lo.upload(P.chunk_lo.data(), P.chunk_lo.size(), ctx->stream));
-  FCG_CUDA(ctx->d_chunk_val.upload(P.chunk_val.data(), P.chunk_val.size(), ctx->stream));
-  FCG_CUDA(ctx->d_perm.upload(P.perm_pool.data(), P.perm_pool.size(), ctx->stream));
-  FCG_CUDA(ctx->d_ts.upload(P.ts_pool.data(), P.ts_pool.size(), ctx->stream));
-  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
-  ctx->stats.n_work_items = int64_t(P.items.size());
+  ctx->stats.n_work_items = ctx->plan_items;
   ctx->stats.n_triples = P.n_triples;
   ctx->stats.flops_reference = P.flops_ref;
   ctx->stats.flops_executed = P.flops_dressed;
   ctx->stats.dressed_elements = ctx->n_w;
-  ctx->stats.plan_seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  ctx->stats.join_seconds = dt;
+  ctx->stats.join_on_device = ctx->plan_on_device ? 1 : 0;
+  ctx->stats.plan_seconds += dt;
   ctx->have_plan = true;
   return FCG_OK;
 }
@@ -998,6 +1015,51 @@ int fcg_state_set(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_
 int fcg_state_rows(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
   if (!ctx) return FCG_EINVAL;
   return state_rows_impl(ctx, n_cfg, fock, cfg);
+}
+
+int fcg_set_planner(fcg_ctx* ctx, int on_device) {
+  if (!ctx) return FCG_EINVAL;
+  FCG_REQUIRE(on_device == 0 || on_device == 1, FCG_EINVAL, "on_device must be 0 or 1");
+  if (ctx->plan_on_device != (on_device == 1)) {
+    ctx->plan_on_device = on_device == 1;
+    ctx->have_plan = false;
+    ctx->drop_hcache();
+    ctx->fine_built = false;
+  }
+  return FCG_OK;
+}
+
+int fcg_plan_sizes(fcg_ctx* ctx, int64_t* sizes) {
+  if (!ctx || !sizes) return FCG_EINVAL;
+  const int rc = ensure_plan(ctx);
+  if (rc) return rc;
+  sizes[0] = ctx->plan_perm;
+  sizes[1] = ctx->plan_ts;
+  sizes[2] = ctx->plan_jobs;
+  sizes[3] = ctx->n_chunks + 1;
+  sizes[4] = ctx->plan_items;
+  return FCG_OK;
+}
+
+int fcg_plan_copy(fcg_ctx* ctx, int which, void* dst, int64_t bytes) {
+  if (!ctx || !dst) return FCG_EINVAL;
+  const int rc = ensure_plan(ctx);
+  if (rc) return rc;
+  FCG_CUDA(cudaSetDevice(ctx->device));
+  const void* src = nullptr;
+  int64_t need = 0;
+  switch (which) {
+    case 0: src = ctx->d_perm.p; need = ctx->plan_perm * int64_t(sizeof(int32_t)); break;
+    case 1: src = ctx->d_ts.p; need = ctx->plan_ts * int64_t(sizeof(TermSector)); break;
+    case 2: src = ctx->d_jobs.p; need = ctx->plan_jobs * int64_t(sizeof(LaneJob)); break;
+    case 3: src = ctx->d_chunk_lo.p; need = (ctx->n_chunks + 1) * int64_t(sizeof(int64_t)); break;
+    case 4: src = ctx->d_chunk_val.p; need = (ctx->n_chunks + 1) * int64_t(sizeof(int64_t)); break;
+    default: FCG_REQUIRE(false, FCG_EINVAL, "which must be 0..4");
+  }
+  FCG_REQUIRE(bytes == need, FCG_EINVAL, "bytes must be " + std::to_string(need));
+  if (need > 0) FCG_CUDA(cudaMemcpyAsync(dst, src, size_t(need), cudaMemcpyDeviceToHost, ctx->stream));
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  return FCG_OK;
 }
 
 int fcg_set_tuning(fcg_ctx* ctx, int mode) {
@@ -1036,13 +1098,22 @@ std::string tune_key(const fcg_ctx* ctx, int prec, int R) {
   const Plan& P = ctx->plan;
   return std::to_string(prec) + "/" + std::to_string(R) + "/" + std::to_string(ctx->N) + "/" +
          std::to_string(ctx->n_cfg) + "/" + std::to_string(ctx->n_terms) + "/" + std::to_string(P.n_triples) + "/" +
-         std::to_string(P.jobs.size()) + "/" + std::to_string(ctx->device);
+         std::to_string(ctx->plan_jobs) + "/" + std::to_string(ctx->device);
 }
 }  // namespace
 
 // the finer chunk table of the tuning candidates (built on first use)
 static int fine_chunks(fcg_ctx* ctx) {
   if (ctx->fine_built) return FCG_OK;
+  if (ctx->plan_on_device) {
+    int64_t nc = 0;
+    const int rc = device_chunks(ctx, 4 * kTargetChunks, ctx->d_chunk_lo_fine, ctx->d_chunk_val_fine, &nc);
+    if (rc) return rc;
+    FCG_REQUIRE(lane_ctas(nc) < (int64_t(1) << 31), FCG_ELIMIT, "too many warp chunks for one launch");
+    ctx->n_chunks_fine = nc;
+    ctx->fine_built = true;
+    return FCG_OK;
+  }
   std::vector<int64_t> lo, val;
   make_chunks(ctx->plan, 4 * kTargetChunks, lo, val);
   FCG_REQUIRE(lane_ctas(int64_t(lo.size()) - 1) < (int64_t(1) << 31), FCG_ELIMIT, "too many warp chunks for one launch");

@@ -248,6 +248,75 @@ FCG_HD inline int64_t dense_block_index(int nmax1, int c, int op, int fba, int f
   return ((((int64_t(c) * kNumOps + op) * nmax1 + fba) * nmax1 + fbb) * nmax1 + fka) * nmax1 + fkb;
 }
 
+// The term tables a term-sector record is made from, as plain arrays (host vectors or their
+// device copies): term rows (kTrmCols each), dressing, W offsets [term][fb_a][fb_b] of the
+// dressed cluster, the dense TDM block index and the blocks.
+struct TermTables {
+  const int32_t* trm;
+  const TermDress* dress;
+  const int64_t* w_index;
+  const int32_t* blk;
+  const BlockInfo* blocks;
+  int nmax1;
+};
+
+// The term-sector record of term t between bra sector fb and ket sector fk (N x 2 each) and
+// its multiply-add count per (bra, ket) pair (fma); false when a TDM block the term needs does
+// not exist there.  The host and the device planner both make their records here.
+FCG_HD inline bool term_sector_of(const TermTables& tt, int t, const int16_t* fb, const int16_t* fk,
+                                  TermSector& ts, int64_t* fma) {
+  const int32_t* r = tt.trm + int64_t(t) * kTrmCols;
+  const TermDress& d = tt.dress[t];
+  const int nmax1 = tt.nmax1;
+  const int nbody = r[0];
+  ts = TermSector{};
+  const int pos = d.pos < 0 ? 0 : d.pos;
+  const int cw = r[2 + pos], opw = r[6 + pos];
+  const int bw = tt.blk[dense_block_index(nmax1, cw, opw, fb[2 * cw], fb[2 * cw + 1], fk[2 * cw], fk[2 * cw + 1])];
+  const int64_t woff = tt.w_index[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
+  if (bw < 0 || woff < 0) return false;
+  ts.w_off = woff;
+  ts.w_mb = tt.blocks[bw].mb;
+  ts.cw = int8_t(cw);
+  ts.rest_len = int16_t(nbody == 1 ? 1 : d.rest_len);
+  ts.nrem = int8_t(nbody == 1 ? 0 : d.nrem);
+  for (int q = 0; q < ts.nrem; ++q) {
+    const int o = d.rem_pos[q];
+    const int c = r[2 + o], op = r[6 + o];
+    const int bl = tt.blk[dense_block_index(nmax1, c, op, fb[2 * c], fb[2 * c + 1], fk[2 * c], fk[2 * c + 1])];
+    if (bl < 0) return false;
+    ts.g_off[q] = tt.blocks[bl].off;
+    ts.g_mb[q] = tt.blocks[bl].mb;
+    ts.g_dim[q] = int16_t(tt.blocks[bl].nidx);
+    ts.cr[q] = int8_t(c);
+  }
+  // compute_terms_state_sign (type_ClusteredTerm.jl:181-196) on the ket sector
+  int sgn = 0;
+  for (int o = 0; o < nbody; ++o)
+    if (r[18 + o]) {
+      int ne = 0;
+      for (int ci = 0; ci < r[2 + o]; ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
+      sgn ^= ne & 1;
+    }
+  ts.sign = int8_t(nbody == 1 ? 1 : (sgn ? -1 : 1));
+  int64_t f = 0;
+  if (ts.nrem == 1) f = ts.rest_len;
+  if (ts.nrem == 2) f = ts.rest_len + ts.g_dim[1];
+  if (ts.nrem == 3) f = ts.rest_len + int64_t(ts.g_dim[1]) * ts.g_dim[2] + ts.g_dim[2];
+  *fma = f;
+  return true;
+}
+
+// the reference's flop count of one (bra, ket) pair of term t: 2 x len(ints) for terms of two
+// or more bodies
+FCG_HD inline int64_t term_ref_flops(const int32_t* trm, int t) {
+  const int32_t* r = trm + int64_t(t) * kTrmCols;
+  if (r[0] <= 1) return 0;
+  int64_t len = 1;
+  for (int o = 0; o < 4; ++o) len *= r[22 + o];
+  return 2 * len;
+}
+
 // The plan of one state in two parts: build_sectors checks the rows and finds the Fock sectors
 // (enough for the diagonal and the open sigma); build_join adds the closed-sigma work items,
 // lane jobs and warp chunks.  build_plan does both.
@@ -258,6 +327,19 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
 // The term-sector record of term t between bra sector fb and ket sector fk (N x 2 each);
 // false when a TDM block the term needs does not exist there.
 bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int16_t* fk, TermSector& ts);
+TermTables term_tables(const ProblemInfo& pi);
+
+// Active-cluster sets of the terms and the term lists of every (transfer, set), in the order
+// the closed-sigma join visits them: transfers ascending, then sets in order of first
+// appearance among the terms, each list's terms ascending.
+struct TermLists {
+  std::vector<uint32_t> masks;       // active clusters of each set (bit c: cluster c)
+  std::vector<int32_t> tr, set;      // transfer and set of every list
+  std::vector<int32_t> off;          // list j holds terms[off[j], off[j+1])
+  std::vector<int32_t> terms;
+  std::vector<int32_t> first_of_tr;  // lists of transfer tr: [first_of_tr[tr], first_of_tr[tr+1])
+};
+std::string term_lists(const ProblemInfo& pi, TermLists& lists);
 
 // Dressing plan of every term (which cluster is dressed, the W block of each of its
 // TDM blocks); fills dress, w_index ([term][fb_a][fb_b] -> W offset or -1), jobs, w_total.

@@ -51,44 +51,53 @@ struct PJob {
 
 }  // namespace
 
+TermTables term_tables(const ProblemInfo& pi) {
+  return TermTables{pi.trm->data(), pi.dress->data(), pi.w_index->data(), pi.blk_index->data(), pi.blocks->data(),
+                    pi.nmax + 1};
+}
+
 bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int16_t* fk, TermSector& ts) {
+  int64_t fma;
+  return term_sector_of(term_tables(pi), t, fb, fk, ts, &fma);
+}
+
+std::string term_lists(const ProblemInfo& pi, TermLists& L) {
   const std::vector<int32_t>& trm = *pi.trm;
-  const TermDress& d = (*pi.dress)[t];
-  const std::vector<int32_t>& blk = *pi.blk_index;
-  const std::vector<BlockInfo>& blocks = *pi.blocks;
-  const int nmax1 = pi.nmax + 1;
-  const int nbody = TT(trm, t, 0);
-  ts = TermSector{};
-  const int pos = d.pos < 0 ? 0 : d.pos;
-  const int cw = TT(trm, t, 2 + pos), opw = TT(trm, t, 6 + pos);
-  const int bw = blk[dense_block_index(nmax1, cw, opw, fb[2 * cw], fb[2 * cw + 1], fk[2 * cw], fk[2 * cw + 1])];
-  const int64_t woff = (*pi.w_index)[(int64_t(t) * nmax1 + fb[2 * cw]) * nmax1 + fb[2 * cw + 1]];
-  if (bw < 0 || woff < 0) return false;
-  ts.w_off = woff;
-  ts.w_mb = blocks[bw].mb;
-  ts.cw = int8_t(cw);
-  ts.rest_len = int16_t(nbody == 1 ? 1 : d.rest_len);
-  ts.nrem = int8_t(nbody == 1 ? 0 : d.nrem);
-  for (int r = 0; r < ts.nrem; ++r) {
-    const int o = d.rem_pos[r];
-    const int c = TT(trm, t, 2 + o), op = TT(trm, t, 6 + o);
-    const int bl = blk[dense_block_index(nmax1, c, op, fb[2 * c], fb[2 * c + 1], fk[2 * c], fk[2 * c + 1])];
-    if (bl < 0) return false;
-    ts.g_off[r] = blocks[bl].off;
-    ts.g_mb[r] = blocks[bl].mb;
-    ts.g_dim[r] = int16_t(blocks[bl].nidx);
-    ts.cr[r] = int8_t(c);
-  }
-  // compute_terms_state_sign (type_ClusteredTerm.jl:181-196) on the ket sector
-  int sgn = 0;
-  for (int o = 0; o < nbody; ++o)
-    if (TT(trm, t, 18 + o)) {
-      int ne = 0;
-      for (int ci = 0; ci < TT(trm, t, 2 + o); ++ci) ne += fk[2 * ci] + fk[2 * ci + 1];
-      sgn ^= ne & 1;
+  L = TermLists();
+  std::unordered_map<uint32_t, int> mask_id;
+  std::vector<std::vector<std::vector<int32_t>>> by(pi.n_trans);
+  for (int t = 0; t < pi.n_terms; ++t) {
+    const int nb = TT(trm, t, 0);
+    uint32_t m = 0;
+    for (int o = 0; o < nb; ++o) m |= 1u << TT(trm, t, 2 + o);
+    auto it = mask_id.find(m);
+    int s;
+    if (it == mask_id.end()) {
+      s = int(L.masks.size());
+      mask_id[m] = s;
+      L.masks.push_back(m);
+    } else {
+      s = it->second;
     }
-  ts.sign = int8_t(nbody == 1 ? 1 : (sgn ? -1 : 1));
-  return true;
+    const int tr = TT(trm, t, 1);
+    if (tr < 0 || tr >= pi.n_trans) return "term transfer id out of range";
+    if (int(by[tr].size()) <= s) by[tr].resize(s + 1);
+    by[tr][s].push_back(t);
+  }
+  L.first_of_tr.assign(size_t(pi.n_trans) + 1, 0);
+  L.off.push_back(0);
+  for (int tr = 0; tr < pi.n_trans; ++tr) {
+    L.first_of_tr[tr] = int32_t(L.tr.size());
+    for (int s = 0; s < int(by[tr].size()); ++s) {
+      if (by[tr][s].empty()) continue;
+      L.tr.push_back(tr);
+      L.set.push_back(s);
+      L.terms.insert(L.terms.end(), by[tr][s].begin(), by[tr][s].end());
+      L.off.push_back(int32_t(L.terms.size()));
+    }
+  }
+  L.first_of_tr[pi.n_trans] = int32_t(L.tr.size());
+  return "";
 }
 
 std::string build_sectors(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
@@ -157,40 +166,12 @@ std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t
     sec_of[k] = int32_t(sct);
   }
 
-  // ---- active sets and term lists per (transfer, set) ----------------------
-  std::vector<uint32_t> masks;
-  std::unordered_map<uint32_t, int> mask_id;
-  struct TL {
-    int s;
-    std::vector<int32_t> terms;
-  };
-  std::vector<std::vector<TL>> tls(n_trans);
+  TermLists L;
   {
-    std::vector<std::vector<std::vector<int32_t>>> by(n_trans);
-    for (int t = 0; t < n_terms; ++t) {
-      int nb = TT(trm, t, 0);
-      uint32_t m = 0;
-      for (int o = 0; o < nb; ++o) m |= 1u << TT(trm, t, 2 + o);
-      auto it = mask_id.find(m);
-      int s;
-      if (it == mask_id.end()) {
-        s = int(masks.size());
-        mask_id[m] = s;
-        masks.push_back(m);
-      } else {
-        s = it->second;
-      }
-      int tr = TT(trm, t, 1);
-      if (tr < 0 || tr >= n_trans) return "term transfer id out of range";
-      if (int(by[tr].size()) <= s) by[tr].resize(s + 1);
-      by[tr][s].push_back(t);
-    }
-    for (int tr = 0; tr < n_trans; ++tr)
-      for (int s = 0; s < int(by[tr].size()); ++s) {
-        if (by[tr][s].empty()) continue;
-        tls[tr].push_back(TL{s, by[tr][s]});
-      }
+    const std::string m = term_lists(pi, L);
+    if (!m.empty()) return m;
   }
+  const std::vector<uint32_t>& masks = L.masks;
   const int n_sets = int(masks.size());
 
   // ---- groups of every (sector, set) -----------------------------------------
@@ -239,6 +220,7 @@ std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t
   std::vector<std::vector<TermSector>> tTS(n_sec);
   std::vector<std::vector<PJob>> tJobs(n_sec);
   std::vector<int64_t> tFlop(n_sec, 0), tFlopD(n_sec, 0);
+  const TermTables tt = term_tables(pi);
 #pragma omp parallel
   {
     std::vector<int16_t> fk(2 * N);
@@ -248,29 +230,24 @@ std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t
     for (int64_t sb = 0; sb < n_sec; ++sb) {
       const int16_t* fb = &P.sec_fock[sb * 2 * N];
       for (int tr = 0; tr < n_trans; ++tr) {
-        if (tls[tr].empty()) continue;
+        if (L.first_of_tr[tr] == L.first_of_tr[tr + 1]) continue;
         for (int i = 0; i < 2 * N; ++i) fk[i] = int16_t(fb[i] - trans[size_t(tr) * 2 * N + i]);
         uint64_t key;
         if (!fock_key(fk.data(), N, &key)) continue;
         auto it = sec_of.find(key);
         if (it == sec_of.end()) continue;
         int64_t sk = it->second;
-        for (const TL& tl : tls[tr]) {
+        for (int j = L.first_of_tr[tr]; j < L.first_of_tr[tr + 1]; ++j) {
           // term-sector records of this (bra sector, ket sector, term list)
           tsl.clear();
           tflop.clear();
           tflopd.clear();
-          for (int t : tl.terms) {
+          for (int q = L.off[j]; q < L.off[j + 1]; ++q) {
+            const int t = L.terms[q];
             TermSector ts;
-            if (!make_term_sector(pi, t, fb, fk.data(), ts)) continue;  // a missing TDM block contributes nothing
-            const int nbody = TT(trm, t, 0);
-            int64_t len = 1;
-            for (int o = 0; o < 4; ++o) len *= TT(trm, t, 22 + o);
-            tflop.push_back(nbody > 1 ? 2 * len : 0);
-            int64_t fma = 0;
-            if (ts.nrem == 1) fma = ts.rest_len;
-            if (ts.nrem == 2) fma = ts.rest_len + ts.g_dim[1];
-            if (ts.nrem == 3) fma = ts.rest_len + int64_t(ts.g_dim[1]) * ts.g_dim[2] + ts.g_dim[2];
+            int64_t fma;
+            if (!term_sector_of(tt, t, fb, fk.data(), ts, &fma)) continue;  // a missing TDM block contributes nothing
+            tflop.push_back(term_ref_flops(trm.data(), t));
             tflopd.push_back(2 * fma);
             tsl.push_back(ts);
           }
@@ -285,10 +262,11 @@ std::string build_join(const ProblemInfo& pi, const int16_t* fock, const int16_t
           // one lane step (one ket): every term's multiply-adds, about 8 loads and index steps
           // per term, and the coefficient update
           const int64_t step_cost = flopd / 2 + 8 * int64_t(tsl.size()) + 4;
-          const int nbody_tl = TT(trm, tl.terms[0], 0);
-          const auto& gb = groups[sb * n_sets + tl.s];
-          const auto& gk = groups[sk * n_sets + tl.s];
-          int64_t pb = fs_perm_off[sb * n_sets + tl.s], pk = fs_perm_off[sk * n_sets + tl.s];
+          const int nbody_tl = TT(trm, L.terms[L.off[j]], 0);
+          const int set = L.set[j];
+          const auto& gb = groups[sb * n_sets + set];
+          const auto& gk = groups[sk * n_sets + set];
+          int64_t pb = fs_perm_off[sb * n_sets + set], pk = fs_perm_off[sk * n_sets + set];
           size_t a = 0, b = 0;
           while (a < gb.size() && b < gk.size()) {
             if (gb[a].key < gk[b].key) {

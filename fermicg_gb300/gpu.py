@@ -54,6 +54,9 @@ SIGNATURES = {
     "fcg_sigma_closed_noalloc": (_I, [_P, _I, _P, _P, _I]),
     "fcg_get_stats": (_I, [_P, _P]),
     "fcg_set_tuning": (_I, [_P, _I]),
+    "fcg_set_planner": (_I, [_P, _I]),
+    "fcg_plan_sizes": (_I, [_P, _P]),
+    "fcg_plan_copy": (_I, [_P, _I, _P, _L]),
     "fcg_bst_tensor_cores": (_I, [_P, _I]),
     "fcg_bst_davidson": (_I, [_P, _I, _P, _P, _I, _I, ctypes.c_double, ctypes.c_double, _I, _P, _P, _P,
                               ctypes.POINTER(_I)]),
@@ -100,7 +103,8 @@ class Stats(ctypes.Structure):
                 ("open_expand_ms", ctypes.c_double), ("open_flops_reference", ctypes.c_int64),
                 ("open_bytes", ctypes.c_int64), ("tune_seconds", ctypes.c_double),
                 ("tune_cache_hits", ctypes.c_int64), ("bst_tc_groups", ctypes.c_int64),
-                ("bst_tc_flops", ctypes.c_int64), ("bst_tc_mma_flops", ctypes.c_int64), ("bst_tc_ms", ctypes.c_double)]
+                ("bst_tc_flops", ctypes.c_int64), ("bst_tc_mma_flops", ctypes.c_int64), ("bst_tc_ms", ctypes.c_double),
+                ("join_seconds", ctypes.c_double), ("join_on_device", ctypes.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -391,6 +395,27 @@ class GpuSigma:
     def bst_tensor_cores(self, enable: bool = True):
         """float BST sigma: GEMM-shaped groups on the tcgen05 tensor cores (default) or not."""
         self._check(self.L.fcg_bst_tensor_cores(self.h, int(bool(enable))), "fcg_bst_tensor_cores")
+
+    def set_planner(self, on_device: bool = True):
+        """Closed-sigma join on the device (default) or on the host (its reference); the
+        state's plan is rebuilt on its next use.  Both give bit-identical plans."""
+        self._check(self.L.fcg_set_planner(self.h, int(bool(on_device))), "fcg_set_planner")
+
+    def plan_arrays(self):
+        """The state's closed-sigma plan as numpy arrays: permutation pool (int32), term-sector
+        records (72-byte rows, uint8), lane jobs (16-byte rows, uint8), warp-chunk first warp
+        tasks and first stored values (int64); and the work-item count."""
+        sz = np.zeros(5, dtype=np.int64)
+        self._check(self.L.fcg_plan_sizes(self.h, _ptr(sz)), "fcg_plan_sizes")
+        out = {}
+        for which, name, dt, width in ((0, "perm", np.int32, 1), (1, "ts", np.uint8, 72), (2, "jobs", np.uint8, 16),
+                                       (3, "chunk_lo", np.int64, 1), (4, "chunk_val", np.int64, 1)):
+            n = int(sz[which if which < 4 else 3])
+            a = np.zeros((n, width) if width > 1 else n, dtype=dt)
+            self._check(self.L.fcg_plan_copy(self.h, which, _ptr(a), a.nbytes), "fcg_plan_copy")
+            out[name] = a
+        out["items"] = int(sz[4])
+        return out
 
     def set_tuning(self, mode: int = -1):
         """Closed-sigma kernel candidate: -1 times the candidates on the first sigma of each

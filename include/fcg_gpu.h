@@ -90,6 +90,8 @@ typedef struct fcg_stats {
   int64_t bst_tc_flops;     /* their algorithmic flops (2 m k n per root) */
   int64_t bst_tc_mma_flops; /* flops the MMAs executed (3 TF32 products, tiles padded) */
   double bst_tc_ms;         /* device time of the tensor-core GEMM kernel (CUDA events) */
+  double join_seconds;      /* wall time of the last closed-sigma join (part of plan_seconds) */
+  int64_t join_on_device;   /* 1: that join ran on the device (the default), 0: on the host */
 } fcg_stats;
 
 int fcg_version(void);
@@ -350,6 +352,21 @@ int fcg_bst_fois_get(fcg_ctx* ctx, int16_t* fock, int64_t* blocks, int64_t* fact
  * reports the candidate in use per precision (chosen[0] double, chosen[1] float; -1: not
  * tuned yet) and, when candidate_ms is given (8 floats), the timings of the last tuning. */
 int fcg_set_tuning(fcg_ctx* ctx, int mode);
+
+/* Where the closed-sigma join of the next plan runs (no counterpart in the reference: its
+ * check_term filter runs per (bra, ket, term) in tps_ci_matvec, src/tpsci_outer.jl:462-527).
+ * on_device = 1 (the default): spectator-key radix sorts, a sector hash table and the joins
+ * in device kernels; 0: the host planner (C++/OpenMP), kept as its reference.  Both give
+ * bit-identical plans.  The state's plan is rebuilt on its next use. */
+int fcg_set_planner(fcg_ctx* ctx, int on_device);
+
+/* The state's closed-sigma plan, for tests and inspection (builds it when needed).
+ * fcg_plan_sizes: sizes[0] permutation-pool entries (int32), [1] term-sector records
+ * (72 bytes), [2] lane jobs (16 bytes, idle lanes included), [3] warp-chunk table entries
+ * (int64, chunks + 1), [4] work items.  fcg_plan_copy copies array `which` (0..3 as above;
+ * 4: the chunk table's first stored values, int64) to host memory of `bytes` bytes. */
+int fcg_plan_sizes(fcg_ctx* ctx, int64_t* sizes);
+int fcg_plan_copy(fcg_ctx* ctx, int which, void* dst, int64_t bytes);
 int fcg_tuning(const fcg_ctx* ctx, int* chosen, float* candidate_ms);
 
 /* Allocation-free variant of fcg_sigma_closed_device (no counterpart in the reference).
