@@ -14,7 +14,7 @@
 //  2. sector table: an open-addressed hash table of the sectors' Fock keys gives the ket
 //     sector of every (bra sector, transfer);
 //  3. term-sector records of every (bra sector, term list) pair whose ket sector exists, one
-//     warp per pair, compacted in order;
+//     thread per pair, compacted in order;
 //  4. join: every bra group of a pair looks its key up among the ket sector's groups (binary
 //     search); each match is a work item;
 //  5. lane jobs: each bra row of an item with up to 32 of its kets, then a stable radix sort
@@ -148,6 +148,90 @@ __global__ void group_count_kernel(int64_t n_el, const int32_t* __restrict__ n_g
   g_cnt[g] = int32_t(end - g_start[g]);
 }
 
+// ---- rows of a state ------------------------------------------------------------------
+// Checks of the rows, with the host planner's messages (build_sectors in plan.cpp) and its
+// order: the first error by (check group, row, cluster), where group 0 is the sector scan
+// (an entry outside [0, 15] at a sector's first row, a sector that comes back), group 1 the
+// range of the local states, group 2 the per-cluster checks of each row.
+enum RowError : int {
+  kErrFockRange = 1,
+  kErrSplitSector = 2,
+  kErrStateRange = 3,
+  kErrClusterSize = 4,
+  kErrNoBasis = 5,
+  kErrBeyondBasis = 6
+};
+
+__device__ __forceinline__ unsigned long long row_error(int group, int64_t row, int c, int code) {
+  return (static_cast<unsigned long long>(group) << 60) | (static_cast<unsigned long long>(row) << 8) |
+         (static_cast<unsigned long long>(c) << 4) | static_cast<unsigned long long>(code);
+}
+
+// per row: sector start flag (and a zero past the end for the scan), the checks, the
+// device copy of its local states (padded to kCfgStride)
+__global__ void rows_kernel(int64_t n, int N, const int16_t* __restrict__ fock, const int16_t* __restrict__ cfg,
+                            const int32_t* __restrict__ norb, const int32_t* __restrict__ blk,
+                            const BlockInfo* __restrict__ blocks, int nmax1, int16_t* __restrict__ cfg8,
+                            int32_t* __restrict__ flag, unsigned long long* __restrict__ err) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == n) {
+    flag[n] = 0;
+    return;
+  }
+  const int16_t* f = fock + i * 2 * N;
+  const int16_t* r = cfg + i * N;
+  bool start = i == 0;
+  for (int k = 0; k < 2 * N && !start; ++k) start = f[k] != f[k - 2 * N];
+  flag[i] = start ? 1 : 0;
+  unsigned long long e = ~0ull;
+  if (start)
+    for (int k = 0; k < 2 * N; ++k)
+      if (f[k] < 0 || f[k] > 15) {
+        e = row_error(0, i, 0, kErrFockRange);
+        break;
+      }
+  for (int c = 0; c < N; ++c)
+    if (r[c] < 0 || r[c] > 255) {
+      e = min(e, row_error(1, i, c, kErrStateRange));
+      break;
+    }
+  for (int c = 0; c < N; ++c) {
+    const int fa = f[2 * c], fb = f[2 * c + 1];
+    if (fa > norb[c] || fb > norb[c]) {
+      e = min(e, row_error(2, i, c, kErrClusterSize));
+      break;
+    }
+    if (fa < 0 || fb < 0) continue;  // reported at the sector's first row (group 0)
+    const int bl = blk[dense_block_index(nmax1, c, kOpH, fa, fb, fa, fb)];
+    if (bl < 0) {
+      e = min(e, row_error(2, i, c, kErrNoBasis));
+      break;
+    }
+    if (r[c] >= blocks[bl].mb) {
+      e = min(e, row_error(2, i, c, kErrBeyondBasis));
+      break;
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kCfgStride; ++c) cfg8[i * kCfgStride + c] = c < N ? r[c] : int16_t(0);
+  if (e != ~0ull) atomicMin(err, e);
+}
+
+// sector of every row; first row and Fock entries of every sector
+__global__ void sectors_kernel(int64_t n, int N, const int16_t* __restrict__ fock, const int32_t* __restrict__ excl,
+                               int32_t* __restrict__ row_sector, int64_t* __restrict__ sec_start,
+                               int16_t* __restrict__ sec_fock) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int32_t s1 = excl[i + 1];
+  row_sector[i] = s1 - 1;
+  if (s1 == excl[i]) return;
+  const int32_t sct = excl[i];
+  sec_start[sct] = i;
+  for (int k = 0; k < 2 * N; ++k) sec_fock[int64_t(sct) * 2 * N + k] = fock[i * 2 * N + k];
+}
+
 // ---- 2. sector table ------------------------------------------------------------------------
 __device__ __forceinline__ bool dev_fock_key(const int16_t* f, int N, uint64_t* key) {
   uint64_t k = 0;
@@ -170,6 +254,28 @@ __global__ void sector_insert_kernel(int64_t n_sec, int N, const int16_t* __rest
   for (uint64_t probe = 0; probe <= mask; ++probe) {
     if (atomicCAS(reinterpret_cast<int*>(tvals + h), -1, int(s)) == -1) {
       tkeys[h] = key;
+      return;
+    }
+    h = (h + 1) & mask;
+  }
+}
+
+// a sector whose Fock key an earlier sector already has: its rows are not contiguous
+__global__ void sector_verify_kernel(int64_t n_sec, int N, const int16_t* __restrict__ sec_fock,
+                                     const int64_t* __restrict__ sec_start, const uint64_t* __restrict__ tkeys,
+                                     const int32_t* __restrict__ tvals, uint64_t mask,
+                                     unsigned long long* __restrict__ err) {
+  const int64_t s = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (s >= n_sec) return;
+  uint64_t key;
+  if (!dev_fock_key(sec_fock + s * 2 * N, N, &key)) return;  // an entry out of range: reported already
+  uint64_t h = sector_hash(key) & mask;
+  // every slot of this key lies on its probe sequence before the first free slot
+  for (uint64_t probe = 0; probe <= mask; ++probe) {
+    const int32_t v = tvals[h];
+    if (v < 0) return;
+    if (tkeys[h] == key && v < s) {
+      atomicMin(err, row_error(0, sec_start[s], 0, kErrSplitSector));
       return;
     }
     h = (h + 1) & mask;
@@ -233,14 +339,14 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-// one warp per pair: records that exist, their flop counts, and the bra groups to join
+// one thread per pair (a term list holds a few terms, and most pairs have no ket sector):
+// the records that exist, their flop counts, and the bra groups to join
 __global__ void pair_count_kernel(PairParams p, int64_t* __restrict__ pt_nt, int64_t* __restrict__ pt_ng,
                                   int64_t* __restrict__ pt_flop, int64_t* __restrict__ pt_flopd) {
-  const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (w > p.n_pt) return;
   if (w == p.n_pt) {  // zeros past the end for the scans
-    if (lane == 0) pt_nt[w] = pt_ng[w] = 0;
+    pt_nt[w] = pt_ng[w] = 0;
     return;
   }
   const int64_t sb = w / p.n_tl;
@@ -250,7 +356,7 @@ __global__ void pair_count_kernel(PairParams p, int64_t* __restrict__ pt_nt, int
   if (sk >= 0) {
     const int16_t* fb = p.sec_fock + sb * 2 * p.N;
     const int16_t* fk = p.sec_fock + int64_t(sk) * 2 * p.N;
-    for (int q = p.tl_off[j] + lane; q < p.tl_off[j + 1]; q += 32) {
+    for (int q = p.tl_off[j]; q < p.tl_off[j + 1]; ++q) {
       const int t = p.tl_terms[q];
       TermSector ts;
       int64_t fma;
@@ -260,40 +366,29 @@ __global__ void pair_count_kernel(PairParams p, int64_t* __restrict__ pt_nt, int
         flopd += 2 * fma;
       }
     }
-    nt = warp_sum(nt);
-    flop = warp_sum(flop);
-    flopd = warp_sum(flopd);
   }
-  if (lane == 0) {
-    const int64_t seg = sb * p.n_sets + p.tl_set[j];
-    pt_nt[w] = nt;
-    pt_flop[w] = flop;
-    pt_flopd[w] = flopd;
-    pt_ng[w] = nt > 0 ? p.seg_g[seg + 1] - p.seg_g[seg] : 0;
-  }
+  const int64_t seg = sb * p.n_sets + p.tl_set[j];
+  pt_nt[w] = nt;
+  pt_flop[w] = flop;
+  pt_flopd[w] = flopd;
+  pt_ng[w] = nt > 0 ? p.seg_g[seg + 1] - p.seg_g[seg] : 0;
 }
 
-// one warp per pair: its records, in term order, at its scanned offset
+// one thread per pair: its records, in term order, at its scanned offset
 __global__ void pair_records_kernel(PairParams p, const int64_t* __restrict__ ts_off, TermSector* __restrict__ pool) {
-  const int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const int64_t w = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (w >= p.n_pt) return;
-  int64_t base = ts_off[w];
-  if (ts_off[w + 1] == base) return;
+  int64_t o = ts_off[w];
+  if (ts_off[w + 1] == o) return;
   const int64_t sb = w / p.n_tl;
   const int j = int(w - sb * p.n_tl);
   const int32_t sk = p.sk_of[sb * p.n_trans + p.tl_tr[j]];
   const int16_t* fb = p.sec_fock + sb * 2 * p.N;
   const int16_t* fk = p.sec_fock + int64_t(sk) * 2 * p.N;
-  const unsigned lt = (1u << lane) - 1u;
-  for (int q0 = p.tl_off[j]; q0 < p.tl_off[j + 1]; q0 += 32) {
-    const int q = q0 + lane;
+  for (int q = p.tl_off[j]; q < p.tl_off[j + 1]; ++q) {
     TermSector ts;
     int64_t fma;
-    const bool ok = q < p.tl_off[j + 1] && term_sector_of(p.tt, p.tl_terms[q], fb, fk, ts, &fma);
-    const unsigned bal = __ballot_sync(0xffffffffu, ok);
-    if (ok) pool[base + __popc(bal & lt)] = ts;
-    base += __popc(bal);
+    if (term_sector_of(p.tt, p.tl_terms[q], fb, fk, ts, &fma)) pool[o++] = ts;
   }
 }
 
@@ -578,6 +673,102 @@ static int read_counters(fcg_ctx* ctx, int n) {
   return FCG_OK;
 }
 
+__global__ void rows_collect_kernel(const int32_t* __restrict__ n_sec_at, unsigned long long* __restrict__ counters) {
+  counters[1] = (unsigned long long)*n_sec_at;
+}
+
+// the sector table of the state's sectors (Fock key -> sector), sized for n_sec sectors
+static int build_sector_table(fcg_ctx* ctx, int64_t n_sec) {
+  auto& D = ctx->dj;
+  int64_t cap = 64;
+  while (cap < 2 * n_sec) cap <<= 1;
+  FCG_CUDA(D.d_tkeys.alloc(size_t(cap)));
+  FCG_CUDA(D.d_tvals.alloc(size_t(cap)));
+  FCG_CUDA(cudaMemsetAsync(D.d_tvals.p, 0xFF, sizeof(int32_t) * cap, ctx->stream));
+  sector_insert_kernel<<<grid_for(n_sec), kThreads, 0, ctx->stream>>>(n_sec, ctx->N, ctx->d_sec_fock.p, D.d_tkeys.p,
+                                                                      D.d_tvals.p, uint64_t(cap - 1));
+  FCG_CUDA(cudaGetLastError());
+  D.table_cap = cap;
+  D.table_ready = true;
+  return FCG_OK;
+}
+
+int state_rows_device(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg) {
+  auto& D = ctx->dj;
+  Plan& P = ctx->plan;
+  const int N = ctx->N;
+  P = Plan();
+  P.N = N;
+  P.n_cfg = n_cfg;
+  D.table_ready = false;
+  FCG_REQUIRE(N <= kMaxClusters, FCG_EINVAL, "more than 8 clusters");
+  FCG_REQUIRE(n_cfg < (int64_t(1) << 31), FCG_EINVAL, "too many configurations");
+  cudaStream_t s = ctx->stream;
+  FCG_CUDA(D.d_cnt.alloc(8));
+  FCG_CUDA(D.h_cnt.alloc(8));
+  FCG_CUDA(D.d_fock_in.upload(fock, size_t(n_cfg) * 2 * N, s));
+  FCG_CUDA(D.d_cfg_in.upload(cfg, size_t(n_cfg) * N, s));
+  FCG_CUDA(ctx->d_cfg.alloc(size_t(n_cfg) * kCfgStride));
+  FCG_CUDA(ctx->d_row_sector.alloc(size_t(n_cfg)));
+  FCG_CUDA(ctx->d_sec_fock.alloc(size_t(n_cfg) * 2 * N));
+  int32_t *flag, *tmp;
+  int64_t* sec_start;
+  FCG_CUDA(carve(D.arena_rows, [&](Bump& b) {
+    flag = b.take<int32_t>(n_cfg + 1);
+    tmp = b.take<int32_t>(dprim::scan_scratch(n_cfg + 1));
+    sec_start = b.take<int64_t>(n_cfg);
+  }));
+  FCG_CUDA(cudaMemsetAsync(D.d_cnt.p, 0xFF, sizeof(unsigned long long), s));  // no error yet
+  rows_kernel<<<grid_for(n_cfg + 1), kThreads, 0, s>>>(n_cfg, N, D.d_fock_in.p, D.d_cfg_in.p, ctx->d_norb.p,
+                                                       ctx->d_blk_index.p, ctx->d_blocks.p, ctx->nmax + 1,
+                                                       ctx->d_cfg.p, flag, D.d_cnt.p);
+  FCG_CUDA(cudaGetLastError());
+  FCG_CUDA(dprim::exclusive_scan<int32_t>(flag, n_cfg + 1, tmp, s));
+  sectors_kernel<<<grid_for(n_cfg), kThreads, 0, s>>>(n_cfg, N, D.d_fock_in.p, flag, ctx->d_row_sector.p, sec_start,
+                                                      ctx->d_sec_fock.p);
+  FCG_CUDA(cudaGetLastError());
+  rows_collect_kernel<<<1, 1, 0, s>>>(flag + n_cfg, D.d_cnt.p);
+  FCG_CUDA(cudaGetLastError());
+  {
+    const int rc = read_counters(ctx, 2);
+    if (rc) return rc;
+  }
+  const int64_t n_sec = int64_t(D.h_cnt.p[1]);
+  {
+    const int rc = build_sector_table(ctx, n_sec);
+    if (rc) return rc;
+  }
+  sector_verify_kernel<<<grid_for(n_sec), kThreads, 0, s>>>(n_sec, N, ctx->d_sec_fock.p, sec_start, D.d_tkeys.p,
+                                                            D.d_tvals.p, uint64_t(D.table_cap - 1), D.d_cnt.p);
+  FCG_CUDA(cudaGetLastError());
+  P.sec_start.resize(size_t(n_sec));
+  P.sec_fock.resize(size_t(n_sec) * 2 * N);
+  FCG_CUDA(cudaMemcpyAsync(P.sec_start.data(), sec_start, sizeof(int64_t) * n_sec, cudaMemcpyDeviceToHost, s));
+  FCG_CUDA(cudaMemcpyAsync(P.sec_fock.data(), ctx->d_sec_fock.p, sizeof(int16_t) * n_sec * 2 * N,
+                           cudaMemcpyDeviceToHost, s));
+  {
+    const int rc = read_counters(ctx, 1);
+    if (rc) return rc;
+  }
+  const unsigned long long err = D.h_cnt.p[0];
+  if (err != ~0ull) {
+    D.table_ready = false;
+    static const char* const kMsg[] = {"",
+                                       "Fock sector entry outside [0, 15]",
+                                       "rows of a Fock sector are not contiguous",
+                                       "local state index outside [0, 255]",
+                                       "Fock sector exceeds cluster size",
+                                       "a row uses a Fock sector with no local basis",
+                                       "local state index beyond the sector's basis"};
+    const int code = int(err & 15);
+    FCG_REQUIRE(false, FCG_EINVAL, code >= 1 && code <= 6 ? kMsg[code] : "bad rows");
+  }
+  P.sec_count.resize(size_t(n_sec));
+  for (int64_t i = 0; i < n_sec; ++i) P.sec_count[i] = (i + 1 < n_sec ? P.sec_start[i + 1] : n_cfg) - P.sec_start[i];
+  P.zero_terms = zero_transfer_terms(problem_info(ctx));
+  return FCG_OK;
+}
+
 int device_chunks(fcg_ctx* ctx, int64_t target, DevBuf<int64_t>& lo, DevBuf<int64_t>& val, int64_t* n_chunks) {
   const int64_t total = ctx->plan_total_cost, n_wt = ctx->plan_wt;
   const int64_t chunk_cost =
@@ -666,15 +857,15 @@ int build_join_device(fcg_ctx* ctx) {
   group_count_kernel<<<grid_for(n_el), kThreads, 0, s>>>(n_el, flag + n_el, g_start, g_cnt, seg_g, n_seg);
   FCG_CUDA(cudaGetLastError());
 
-  // ---- 2. sector table and ket sectors --------------------------------------------------
-  int64_t cap = 64;
-  while (cap < 2 * n_sec) cap <<= 1;
-  uint64_t* tkeys;
-  int32_t *tvals, *sk_of;
+  // ---- 2. sector table (the state's rows built it, unless the host checked them) and ket
+  // sectors --------------------------------------------------------------------------------
+  if (!D.table_ready) {
+    const int rc = build_sector_table(ctx, n_sec);
+    if (rc) return rc;
+  }
+  int32_t* sk_of;
   int64_t *pt_nt, *pt_ng, *pt_flop, *pt_flopd, *pt_tmp;
   FCG_CUDA(carve(D.arena[1], [&](Bump& b) {
-    tkeys = b.take<uint64_t>(cap);
-    tvals = b.take<int32_t>(cap);
     sk_of = b.take<int32_t>(n_sec * n_trans);
     pt_nt = b.take<int64_t>(n_pt + 1);
     pt_ng = b.take<int64_t>(n_pt + 1);
@@ -682,13 +873,9 @@ int build_join_device(fcg_ctx* ctx) {
     pt_flopd = b.take<int64_t>(n_pt);
     pt_tmp = b.take<int64_t>(dprim::scan_scratch(n_pt + 1));
   }));
-  FCG_CUDA(cudaMemsetAsync(tvals, 0xFF, sizeof(int32_t) * cap, s));
-  sector_insert_kernel<<<grid_for(n_sec), kThreads, 0, s>>>(n_sec, N, ctx->d_sec_fock.p, tkeys, tvals,
-                                                            uint64_t(cap - 1));
-  FCG_CUDA(cudaGetLastError());
   ket_sector_kernel<<<grid_for(n_sec * n_trans), kThreads, 0, s>>>(n_sec, n_trans, N, ctx->d_sec_fock.p,
-                                                                   D.d_trans.p, D.d_first_of_tr.p, tkeys, tvals,
-                                                                   uint64_t(cap - 1), sk_of);
+                                                                   D.d_trans.p, D.d_first_of_tr.p, D.d_tkeys.p,
+                                                                   D.d_tvals.p, uint64_t(D.table_cap - 1), sk_of);
   FCG_CUDA(cudaGetLastError());
 
   // ---- 3. term-sector records ------------------------------------------------------------
@@ -706,7 +893,7 @@ int build_join_device(fcg_ctx* ctx) {
   pp.n_trans = n_trans;
   pp.n_sets = n_sets;
   pp.N = N;
-  pair_count_kernel<<<grid_for((n_pt + 1) * 32), kThreads, 0, s>>>(pp, pt_nt, pt_ng, pt_flop, pt_flopd);
+  pair_count_kernel<<<grid_for(n_pt + 1), kThreads, 0, s>>>(pp, pt_nt, pt_ng, pt_flop, pt_flopd);
   FCG_CUDA(cudaGetLastError());
   FCG_CUDA(dprim::exclusive_scan<int64_t>(pt_nt, n_pt + 1, pt_tmp, s));
   FCG_CUDA(dprim::exclusive_scan<int64_t>(pt_ng, n_pt + 1, pt_tmp, s));
@@ -721,7 +908,7 @@ int build_join_device(fcg_ctx* ctx) {
   FCG_REQUIRE(E < (int64_t(1) << 31), FCG_ELIMIT, "join exceeds 2^31 bra groups");
   FCG_CUDA(ctx->d_ts.alloc(size_t(n_ts)));
   if (n_ts > 0) {
-    pair_records_kernel<<<grid_for(n_pt * 32), kThreads, 0, s>>>(pp, pt_nt, ctx->d_ts.p);
+    pair_records_kernel<<<grid_for(n_pt), kThreads, 0, s>>>(pp, pt_nt, ctx->d_ts.p);
     FCG_CUDA(cudaGetLastError());
   }
 

@@ -95,6 +95,7 @@ struct fcg_ctx {
   DevBuf<float> d_op32;
   DevBuf<BlockInfo> d_blocks;
   DevBuf<int32_t> d_blk_index;
+  DevBuf<int32_t> d_norb;
   int n_terms = 0;
   std::vector<int32_t> trm;
   std::vector<TermInfo> terms;
@@ -142,7 +143,14 @@ struct fcg_ctx {
     DevBuf<int64_t> d_sec_start, d_sec_count;
     DevBuf<unsigned long long> d_cnt;
     PinnedBuf<unsigned long long> h_cnt;
-    DevBuf<unsigned char> arena[4];
+    DevBuf<unsigned char> arena[4], arena_rows;
+    // the state's rows as given (kept for the host planner) and its sector table: open
+    // addressing, Fock key -> sector (slots: key, sector or -1), built with the rows
+    DevBuf<int16_t> d_fock_in, d_cfg_in;
+    DevBuf<uint64_t> d_tkeys;
+    DevBuf<int32_t> d_tvals;
+    int64_t table_cap = 0;
+    bool table_ready = false;
   } dj;
   // closed-sigma kernel tuning: candidate per precision (0 fp64, 1 fp32; -1 not yet tuned),
   // forced candidate (-1: auto), the finer chunk table of candidates 2-3, candidate timings
@@ -274,6 +282,10 @@ ProblemInfo problem_info(fcg_ctx* ctx);
 // d_chunk_lo / d_chunk_val, d_wt_cum / d_wt_vals and the plan sizes; and a chunk table of
 // about `target` warp chunks over its warp tasks.
 int build_join_device(fcg_ctx* ctx);
+
+// The rows of a state checked, their sectors found and the sector table built on the device
+// (dplan.cu); same results and messages as build_sectors.
+int state_rows_device(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, const int16_t* cfg);
 int device_chunks(fcg_ctx* ctx, int64_t target, DevBuf<int64_t>& lo, DevBuf<int64_t>& val, int64_t* n_chunks);
 
 // BST sigma on device vectors [R][core_total] queued on ctx->stream without the host wait

@@ -747,6 +747,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   FCG_CUDA(ctx->d_op32.upload(d32.data(), d32.size(), ctx->stream));
   FCG_CUDA(ctx->d_blocks.upload(ctx->h_blocks.data(), ctx->h_blocks.size(), ctx->stream));
   FCG_CUDA(ctx->d_blk_index.upload(ctx->h_blk_index.data(), ctx->h_blk_index.size(), ctx->stream));
+  FCG_CUDA(ctx->d_norb.upload(ctx->norb.data(), ctx->norb.size(), ctx->stream));
   {
     std::vector<MaxJob> mj(n_blocks);
     ctx->gmax_off.assign(n_blocks, 0);
@@ -925,24 +926,31 @@ static int state_rows_impl(fcg_ctx* ctx, int64_t n_cfg, const int16_t* fock, con
   ctx->have_state = false;
   ctx->have_plan = false;
   ctx->drop_hcache();
-  const ProblemInfo pi = problem_info(ctx);
-  std::string msg = build_sectors(pi, n_cfg, fock, cfg, ctx->plan);
-  FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
-  const Plan& P = ctx->plan;
-  std::vector<int32_t> row_sector(n_cfg);
-  for (size_t sct = 0; sct < P.sec_start.size(); ++sct)
-    for (int64_t i = 0; i < P.sec_count[sct]; ++i) row_sector[P.sec_start[sct] + i] = int32_t(sct);
-  ctx->n_cfg = n_cfg;
-  ctx->h_fock.assign(fock, fock + n_cfg * 2 * ctx->N);
-  ctx->h_cfg.assign(cfg, cfg + n_cfg * ctx->N);
-  {
+  if (ctx->plan_on_device) {
+    const int rc = state_rows_device(ctx, n_cfg, fock, cfg);
+    if (rc) return rc;
+    ctx->h_fock.clear();  // the host planner fetches the rows from the device when it runs
+    ctx->h_cfg.clear();
+  } else {
+    const ProblemInfo pi = problem_info(ctx);
+    std::string msg = build_sectors(pi, n_cfg, fock, cfg, ctx->plan);
+    FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
+    const Plan& P = ctx->plan;
+    std::vector<int32_t> row_sector(n_cfg);
+    for (size_t sct = 0; sct < P.sec_start.size(); ++sct)
+      for (int64_t i = 0; i < P.sec_count[sct]; ++i) row_sector[P.sec_start[sct] + i] = int32_t(sct);
+    ctx->h_fock.assign(fock, fock + n_cfg * 2 * ctx->N);
+    ctx->h_cfg.assign(cfg, cfg + n_cfg * ctx->N);
     std::vector<int16_t> cfg8(size_t(n_cfg) * kCfgStride, 0);
     for (int64_t i = 0; i < n_cfg; ++i)
       for (int c = 0; c < ctx->N; ++c) cfg8[i * kCfgStride + c] = cfg[i * ctx->N + c];
     FCG_CUDA(ctx->d_cfg.upload(cfg8.data(), cfg8.size(), ctx->stream));
+    FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
+    FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
+    ctx->dj.table_ready = false;
   }
-  FCG_CUDA(ctx->d_sec_fock.upload(P.sec_fock.data(), P.sec_fock.size(), ctx->stream));
-  FCG_CUDA(ctx->d_row_sector.upload(row_sector.data(), row_sector.size(), ctx->stream));
+  const Plan& P = ctx->plan;
+  ctx->n_cfg = n_cfg;
   FCG_CUDA(ctx->d_zero_terms.upload(P.zero_terms.data(), P.zero_terms.size(), ctx->stream));
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->stats.n_cfg = n_cfg;
@@ -970,6 +978,15 @@ int ensure_plan(fcg_ctx* ctx) {
     const int rc = build_join_device(ctx);
     if (rc) return rc;
   } else {
+    if (ctx->h_fock.empty()) {  // rows checked on the device: fetch them
+      ctx->h_fock.resize(size_t(ctx->n_cfg) * 2 * ctx->N);
+      ctx->h_cfg.resize(size_t(ctx->n_cfg) * ctx->N);
+      FCG_CUDA(cudaMemcpyAsync(ctx->h_fock.data(), ctx->dj.d_fock_in.p, sizeof(int16_t) * ctx->h_fock.size(),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+      FCG_CUDA(cudaMemcpyAsync(ctx->h_cfg.data(), ctx->dj.d_cfg_in.p, sizeof(int16_t) * ctx->h_cfg.size(),
+                               cudaMemcpyDeviceToHost, ctx->stream));
+      FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
     const ProblemInfo pi = problem_info(ctx);
     std::string msg = build_join(pi, ctx->h_fock.data(), ctx->h_cfg.data(), ctx->plan);
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);

@@ -329,6 +329,9 @@ std::string build_plan(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock
 bool make_term_sector(const ProblemInfo& pi, int t, const int16_t* fb, const int16_t* fk, TermSector& ts);
 TermTables term_tables(const ProblemInfo& pi);
 
+// the terms of the zero transfer (the diagonal's terms), in term order
+std::vector<int32_t> zero_transfer_terms(const ProblemInfo& pi);
+
 // Active-cluster sets of the terms and the term lists of every (transfer, set), in the order
 // the closed-sigma join visits them: transfers ascending, then sets in order of first
 // appearance among the terms, each list's terms ascending.

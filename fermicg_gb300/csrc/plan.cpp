@@ -100,6 +100,19 @@ std::string term_lists(const ProblemInfo& pi, TermLists& L) {
   return "";
 }
 
+std::vector<int32_t> zero_transfer_terms(const ProblemInfo& pi) {
+  // 1-body terms of the zero transfer (compute_diagonal, src/tpsci_outer.jl:694-715)
+  std::vector<int32_t> out;
+  for (int tr = 0; tr < pi.n_trans; ++tr) {
+    bool zero = true;
+    for (int i = 0; i < 2 * pi.N; ++i) zero &= (*pi.trans)[size_t(tr) * 2 * pi.N + i] == 0;
+    if (zero)
+      for (int t = 0; t < pi.n_terms; ++t)
+        if (TT(*pi.trm, t, 1) == tr) out.push_back(t);
+  }
+  return out;
+}
+
 std::string build_sectors(const ProblemInfo& pi, int64_t n_cfg, const int16_t* fock, const int16_t* cfg, Plan& P) {
   const int N = pi.N;
   const std::vector<int32_t>& trm = *pi.trm;
@@ -140,14 +153,7 @@ std::string build_sectors(const ProblemInfo& pi, int64_t n_cfg, const int16_t* f
       if (bl < 0) return "a row uses a Fock sector with no local basis";
       if (cfg[i * N + c] >= (*pi.blocks)[bl].mb) return "local state index beyond the sector's basis";
     }
-  // 1-body terms of the zero transfer (compute_diagonal, src/tpsci_outer.jl:694-715)
-  for (int tr = 0; tr < n_trans; ++tr) {
-    bool zero = true;
-    for (int i = 0; i < 2 * N; ++i) zero &= trans[size_t(tr) * 2 * N + i] == 0;
-    if (zero)
-      for (int t = 0; t < n_terms; ++t)
-        if (TT(trm, t, 1) == tr) P.zero_terms.push_back(t);
-  }
+  P.zero_terms = zero_transfer_terms(pi);
   return "";
 }
 

@@ -105,3 +105,54 @@ def test_planners_agree_on_one_row_and_one_sector():
     first = np.all(f == f[0], axis=(1, 2))
     n0 = int(np.argmin(first)) if not first.all() else len(f)
     _both(po, pt, f[:n0].copy(), c[:n0].copy())
+
+
+def _corrupt(f, c, kind):
+    """A copy of the rows with one (or two) planted errors."""
+    f = f.copy()
+    c = c.copy()
+    n0 = int(np.argmin(np.all(f == f[0], axis=(1, 2))))  # first row of the second sector
+    if kind == "split_sector":       # the first sector comes back after the second
+        f[n0 + 1] = f[0]
+        c[n0 + 1] = c[0]
+    elif kind == "fock_range":
+        f[n0:n0 + 1, 2, 0] = 16
+    elif kind == "fock_negative":
+        f[n0:n0 + 1, 1, 1] = -1
+    elif kind == "state_range":
+        c[7, 3] = 300
+    elif kind == "cluster_size":
+        f[n0, 4, 0] = 5              # 4-orbital clusters
+    elif kind == "no_basis":
+        f[n0, 0] = (4, 4)            # a sector outside the local bases
+    elif kind == "beyond_basis":
+        c[11, 2] = 200
+    elif kind == "split_before_range":   # both; the earlier row wins
+        f[n0 + 1] = f[0]
+        c[n0 + 1] = c[0]
+        f[len(f) - 1, 2, 0] = 16
+    elif kind == "range_before_size":    # state range (checked first) beats an earlier size error
+        f[n0, 4, 0] = 5
+        c[len(c) - 1, 0] = -2
+    return f, c
+
+
+@pytest.mark.parametrize("kind", ["split_sector", "fock_range", "fock_negative", "state_range", "cluster_size",
+                                  "no_basis", "beyond_basis", "split_before_range", "range_before_size"])
+def test_bad_rows_same_message_both_planners(kind):
+    prob, st = config1_subspace(3000, 4)
+    po, pt, f, c, v = _state(prob, st)
+    fb, cb = _corrupt(f, c, kind)
+    msgs = []
+    for dev in (False, True):
+        g = GpuSigma(0)
+        g.set_ops(po)
+        g.set_terms(pt)
+        g.set_planner(dev)
+        with pytest.raises(Exception) as ei:
+            g.state_set(fb, cb)
+        msgs.append(str(ei.value))
+        g.state_set(f, c)  # the context stays usable
+        assert g.stats()["n_cfg"] == len(f)
+    assert msgs[0] == msgs[1], msgs
+    assert "Fock" in msgs[0] or "local state" in msgs[0]
