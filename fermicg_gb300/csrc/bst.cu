@@ -248,6 +248,9 @@ __device__ __forceinline__ void prefetch_range(const void* p, int64_t bytes, int
 // (power of two, <= 32) and added to out[r * out_stride + bra core index].
 // Steps 1-2 of a group (the GEMM operand X of every root), by a team; X of root r ends in
 // ws[(2 r + cur) * stride], cur = ntr & 1 (one buffer swap per applied overlap), returned.
+// ket ranks up to which a spectator mode product keeps a thread's input fibre in registers
+constexpr int kModeRegs = 16;
+
 template <typename T, int TEAM>
 __device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__ S, const int32_t* __restrict__ perm,
                                  const T* __restrict__ cin, int64_t core_total, T* ws, int stride) {
@@ -276,15 +279,38 @@ __device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__
         inner *= rb;
         continue;
       }
-      const int n = inner * rb * outer;
       const T* Sj = S + G.s_off[j];
-      for (int idx = tid; idx < R * n; idx += TEAM) {
-        const int r = idx / n, e = idx - r * n;
-        const int a = e % inner, q = (e / inner) % rb, o = e / (inner * rb);
-        const T* src = ws + int64_t(2 * r + cur) * stride + a + inner * rk * o;
-        T acc = T(0);
-        for (int l = 0; l < rk; ++l) acc = fma(Sj[q + rb * l], src[inner * l], acc);
-        ws[int64_t(2 * r + (cur ^ 1)) * stride + e] = acc;
+      if (sizeof(T) == 4 && rk <= kModeRegs) {
+        // one thread per (root, a, o): the rk inputs of its fibre in registers, all rb outputs
+        // (float builds: the unrolled, predicated multiply-adds cost the FP64 pipe more than
+        // the saved loads)
+        const int n = inner * outer;
+        for (int idx = tid; idx < R * n; idx += TEAM) {
+          const int r = idx / n, e = idx - r * n;
+          const int a = e % inner, o = e / inner;
+          const T* src = ws + int64_t(2 * r + cur) * stride + a + int64_t(inner) * rk * o;
+          T* dst = ws + int64_t(2 * r + (cur ^ 1)) * stride + a + int64_t(inner) * rb * o;
+          T v[kModeRegs];
+#pragma unroll
+          for (int l = 0; l < kModeRegs; ++l) v[l] = l < rk ? src[int64_t(inner) * l] : T(0);
+          for (int q = 0; q < rb; ++q) {
+            T acc = T(0);
+#pragma unroll
+            for (int l = 0; l < kModeRegs; ++l)
+              if (l < rk) acc = fma(__ldg(Sj + q + rb * l), v[l], acc);
+            dst[int64_t(inner) * q] = acc;
+          }
+        }
+      } else {
+        const int n = inner * rb * outer;
+        for (int idx = tid; idx < R * n; idx += TEAM) {
+          const int r = idx / n, e = idx - r * n;
+          const int a = e % inner, q = (e / inner) % rb, o = e / (inner * rb);
+          const T* src = ws + int64_t(2 * r + cur) * stride + a + inner * rk * o;
+          T acc = T(0);
+          for (int l = 0; l < rk; ++l) acc = fma(Sj[q + rb * l], src[inner * l], acc);
+          ws[int64_t(2 * r + (cur ^ 1)) * stride + e] = acc;
+        }
       }
       team_sync<TEAM>();
       cur ^= 1;
@@ -292,6 +318,89 @@ __device__ int bst_group_prepare(const BstGroup& G, int R, const T* __restrict__
     }
   }
   return cur;
+}
+
+// 4 consecutive elements at a 16-byte aligned generic address (global or shared memory)
+template <typename T>
+__device__ __forceinline__ void load4(const T* p, T* v) {
+  if constexpr (sizeof(T) == 4) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x, v[1] = q.y, v[2] = q.z, v[3] = q.w;
+  } else {
+    const double2 a = *reinterpret_cast<const double2*>(p);
+    const double2 b = *reinterpret_cast<const double2*>(p + 2);
+    v[0] = a.x, v[1] = a.y, v[2] = b.x, v[3] = b.y;
+  }
+}
+
+// Step 3 of a group in register tiles: each thread takes TM bra-active columns x TN
+// spectator indices of one root, D[col, s] = OP[:, col] . X[:, s], so that one column load
+// feeds TN (or TM) multiply-adds; columns of length k % 4 == 0 are read 4 elements at a time
+// (operator and workspace columns then start on 16-byte boundaries).  Edge tiles repeat the
+// last column and drop the extra results.
+template <typename T, int TEAM, bool ATOMIC, int TM, int TN>
+__device__ __forceinline__ void bst_tile_gemm(const T* __restrict__ opg, int k, int m, int ns, int R, const T* ws,
+                                              int stride, int cur, const int32_t* __restrict__ bp, T* out,
+                                              int64_t out_stride, int tid) {
+  const int tm = (m + TM - 1) / TM, tn = (ns + TN - 1) / TN, tiles = tm * tn;
+  const bool vec = (k & 3) == 0;
+  for (int it = tid; it < tiles * R; it += TEAM) {
+    const int r = it / tiles, t = it - r * tiles;
+    const int c0 = (t % tm) * TM, s0 = (t / tm) * TN;
+    const T* X = ws + int64_t(2 * r + cur) * stride;
+    const T* a[TM];
+    const T* b[TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i) a[i] = opg + int64_t(k) * min(c0 + i, m - 1);
+#pragma unroll
+    for (int j = 0; j < TN; ++j) b[j] = X + int64_t(k) * min(s0 + j, ns - 1);
+    T acc[TM][TN];
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) acc[i][j] = T(0);
+    if (vec) {
+      for (int kk = 0; kk < k; kk += 4) {
+        T av[TM][4], bv[TN][4];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) load4(a[i] + kk, av[i]);
+#pragma unroll
+        for (int j = 0; j < TN; ++j) load4(b[j] + kk, bv[j]);
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int i = 0; i < TM; ++i)
+#pragma unroll
+            for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i][q], bv[j][q], acc[i][j]);
+      }
+    } else {
+      for (int kk = 0; kk < k; ++kk) {
+        T av[TM], bv[TN];
+#pragma unroll
+        for (int i = 0; i < TM; ++i) av[i] = a[i][kk];
+#pragma unroll
+        for (int j = 0; j < TN; ++j) bv[j] = b[j][kk];
+#pragma unroll
+        for (int i = 0; i < TM; ++i)
+#pragma unroll
+          for (int j = 0; j < TN; ++j) acc[i][j] = fma(av[i], bv[j], acc[i][j]);
+      }
+    }
+    T* outr = out + int64_t(r) * out_stride;
+#pragma unroll
+    for (int i = 0; i < TM; ++i)
+#pragma unroll
+      for (int j = 0; j < TN; ++j) {
+        const int col = c0 + i, sp = s0 + j;
+        if (col < m && sp < ns) {
+          T* dst = outr + __ldg(bp + col + m * sp);
+          if (ATOMIC)
+            atomicAdd(dst, acc[i][j]);
+          else
+            *dst += acc[i][j];
+        }
+      }
+  }
 }
 
 template <typename T, int TEAM, bool ATOMIC>
@@ -309,6 +418,14 @@ __device__ void bst_group_apply(const BstGroup& G, int R, const T* __restrict__ 
   const int mn = m * ns;
   const T* opg = op + G.op_off;
   const int32_t* bp = perm + G.bperm_off;
+  if (mn * R >= 16 * TEAM) {
+    bst_tile_gemm<T, TEAM, ATOMIC, 4, 4>(opg, k, m, ns, R, ws, stride, cur, bp, out, out_stride, tid);
+    return;
+  }
+  if (mn * R >= 4 * TEAM) {
+    bst_tile_gemm<T, TEAM, ATOMIC, 2, 2>(opg, k, m, ns, R, ws, stride, cur, bp, out, out_stride, tid);
+    return;
+  }
   if (k < 32) {
     // short columns: one thread per (kb, s) and root; items of one group never share an output
     for (int r = 0; r < R; ++r) {
