@@ -101,6 +101,17 @@ __global__ void __launch_bounds__(kBstThreads) bst_gamma_kernel(const BstGamma* 
 }
 
 // One CTA per group: the group operator, scaled by the product of the rank-1 spectator overlaps.
+// Groups of two or more active clusters are built factored on the first active cluster: for
+// each index tuple q' of the other clusters (their bra and ket ranks),
+//   u[p0] = sum_{p1..} ints[p0, p1, ..] prod_{a>0} g_a[p_a, q'_a]
+// once per term, then every element of the first cluster's (bra, ket) ranks is
+// sum_p0 g_0[p0, kb0, kk0] u[p0] -- len(p1..) + rank^2 len(p0) multiply-adds per tuple in
+// place of rank^2 len(p0..) (the successive contractions of build_dense_H_term,
+// src/tucker_build_dense_H_term.jl:5-175).  A work item is one tuple and kOpChunk of the first
+// cluster's elements; u lives in shared memory, one column per thread.
+constexpr int kOpMaxD0 = 64;  // longest orbital multi-index of the first active cluster built factored
+constexpr int kOpChunk = 16;  // operator elements per work item of the factored build
+
 __global__ void __launch_bounds__(kOpThreads) bst_op_kernel(const BstGroup* __restrict__ groups,
                                                              const BstGroupTerm* __restrict__ gterms,
                                                              const BstBlock* __restrict__ blocks, int N,
@@ -109,6 +120,7 @@ __global__ void __launch_bounds__(kOpThreads) bst_op_kernel(const BstGroup* __re
                                                              const double* __restrict__ factors,
                                                              double* __restrict__ opc) {
   __shared__ double scal;
+  __shared__ double u_all[kOpMaxD0 * kOpThreads];
   const BstGroup& Gp = groups[blockIdx.x];
   const BstBlock& B = blocks[Gp.bra];
   const BstBlock& K = blocks[Gp.ket];
@@ -129,6 +141,81 @@ __global__ void __launch_bounds__(kOpThreads) bst_op_kernel(const BstGroup* __re
   int act[4], na = 0;
   for (int c = 0; c < N; ++c)
     if ((Gp.act_mask >> c) & 1) act[na++] = c;
+  bool factored = na >= 2;
+  for (int t = 0; t < Gp.nt && factored; ++t) {
+    const BstGroupTerm& T = gterms[Gp.t_off + t];
+    factored = T.ints_off >= 0 && T.nact == na && T.np[0] <= kOpMaxD0;
+  }
+  if (factored) {
+    const int rb0 = B.rank[act[0]], rk0 = K.rank[act[0]];
+    const int q0n = rb0 * rk0;
+    const int krest = Gp.k / rk0, brest = Gp.m / rb0;
+    const int nch = (q0n + kOpChunk - 1) / kOpChunk;
+    const int64_t items = int64_t(krest) * brest * nch;
+    double* u = u_all + threadIdx.x;  // u[p] at u[p * kOpThreads]
+    for (int64_t item = threadIdx.x; item < items; item += blockDim.x) {
+      const int64_t tq = item / nch;
+      const int ch = int(item - tq * nch);
+      const int kk_rest = int(tq % krest), kb_rest = int(tq / krest);
+      int ik[4] = {0, 0, 0, 0}, ib[4] = {0, 0, 0, 0};
+      {
+        int x = kk_rest, y = kb_rest;
+        for (int a = 1; a < na; ++a) {
+          ik[a] = x % K.rank[act[a]];
+          x /= K.rank[act[a]];
+          ib[a] = y % B.rank[act[a]];
+          y /= B.rank[act[a]];
+        }
+      }
+      const int o0 = ch * kOpChunk;
+      double acc[kOpChunk];
+#pragma unroll
+      for (int o = 0; o < kOpChunk; ++o) acc[o] = 0.0;
+      for (int t = 0; t < Gp.nt; ++t) {
+        const BstGroupTerm T = gterms[Gp.t_off + t];
+        const double* v = ints + T.ints_off;
+        const int d0 = T.np[0], d1 = T.np[1];
+        const int d2 = T.nact > 2 ? T.np[2] : 1, d3 = T.nact > 3 ? T.np[3] : 1;
+        const double* ga[4];
+        for (int a = 1; a < T.nact; ++a)
+          ga[a] = g + T.g_off[a] + int64_t(T.np[a]) * (ib[a] + int64_t(B.rank[act[a]]) * ik[a]);
+        for (int p = 0; p < d0; ++p) u[p * kOpThreads] = 0.0;
+        for (int l = 0; l < d3; ++l) {
+          const double x3 = T.nact > 3 ? ga[3][l] : 1.0;
+          for (int r = 0; r < d2; ++r) {
+            const double x2 = (T.nact > 2 ? ga[2][r] : 1.0) * x3;
+            for (int j = 0; j < d1; ++j) {
+              const double x1 = ga[1][j] * x2;
+              const double* vj = v + int64_t(d0) * (j + int64_t(d1) * (r + int64_t(d2) * l));
+              for (int p = 0; p < d0; ++p) u[p * kOpThreads] = fma(vj[p], x1, u[p * kOpThreads]);
+            }
+          }
+        }
+        const double sg = double(T.sign);
+        const double* g0 = g + T.g_off[0];
+#pragma unroll
+        for (int o = 0; o < kOpChunk; ++o) {
+          const int q = o0 + o;
+          if (q < q0n) {
+            const double* g0q = g0 + int64_t(d0) * q;  // (ib0 + rb0 * ik0) = q
+            double sacc = 0.0;
+            for (int p = 0; p < d0; ++p) sacc = fma(g0q[p], u[p * kOpThreads], sacc);
+            acc[o] = fma(sg, sacc, acc[o]);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 0; o < kOpChunk; ++o) {
+        const int q = o0 + o;
+        if (q < q0n) {
+          const int ib0 = q % rb0, ik0 = q / rb0;
+          const int64_t kk = ik0 + int64_t(rk0) * kk_rest, kb = ib0 + int64_t(rb0) * kb_rest;
+          opc[Gp.op_off + kk + int64_t(Gp.k) * kb] = scal * acc[o];
+        }
+      }
+    }
+    return;
+  }
   const int64_t n = int64_t(Gp.m) * Gp.k;
   for (int64_t e = threadIdx.x; e < n; e += blockDim.x) {
     int64_t kk = e % Gp.k, kb = e / Gp.k;
