@@ -292,6 +292,44 @@ __global__ void bst_widen_kernel(const float* __restrict__ a, double* __restrict
     b[i] = double(a[i]);
 }
 
+// One actives-first index table: block `block`'s positions for the active clusters `mask`,
+// at perm[off, off + core_len).
+struct BstPermTable {
+  int64_t off;
+  int32_t block, mask;
+};
+
+// One CTA per index table: perm[off + x] = core offset of position x of the block's
+// actives-first layout for the active clusters `mask`, x = (mixed radix over the active
+// clusters) + (their rank product) * (mixed radix over the other clusters), both in increasing
+// cluster order; the core is column-major over the clusters (cluster 0 fastest).
+__global__ void bst_perm_kernel(const BstPermTable* __restrict__ tables, const BstBlock* __restrict__ blocks, int N,
+                                int32_t* __restrict__ perm) {
+  const BstPermTable T = tables[blockIdx.x];
+  const BstBlock& B = blocks[T.block];
+  int rank[kMaxClusters];
+  int ka_len = 1;
+  for (int c = 0; c < N; ++c) {
+    rank[c] = B.rank[c];
+    if ((T.mask >> c) & 1) ka_len *= rank[c];
+  }
+  for (int e = threadIdx.x; e < B.core_len; e += blockDim.x) {
+    int rem = e, ka = 0, kam = 1, sp = 0, spm = 1;
+    for (int c = 0; c < N; ++c) {
+      const int v = rem % rank[c];
+      rem /= rank[c];
+      if ((T.mask >> c) & 1) {
+        ka += v * kam;
+        kam *= rank[c];
+      } else {
+        sp += v * spm;
+        spm *= rank[c];
+      }
+    }
+    perm[T.off + ka + int64_t(ka_len) * sp] = e;
+  }
+}
+
 // ---- sigma ---------------------------------------------------------------------------------
 
 template <int TEAM>
@@ -861,36 +899,11 @@ struct BstPlan {
   std::vector<BstGroup> groups;
   std::vector<BstOverlapJob> overlaps;
   std::vector<int32_t> triples;
-  std::vector<int32_t> perm;  // actives-first index tables
+  std::vector<BstPermTable> tables;  // actives-first index tables, filled on the device
+  int64_t perm_total = 0;
   int64_t g_total = 0, op_total = 0, s_total = 0;
   int64_t flops_ref = 0, flops_exec = 0;
 };
-
-// perm[x] = core offset of position x of block B's actives-first layout for the active
-// clusters `mask`: x = (mixed radix over the active clusters) + (their rank product) *
-// (mixed radix over the other clusters), both in increasing cluster order.
-void append_perm(const BstBlock& B, int N, int mask, std::vector<int32_t>& perm) {
-  const size_t base = perm.size();
-  perm.resize(base + size_t(B.core_len));
-  int ka_len = 1;
-  for (int c = 0; c < N; ++c)
-    if ((mask >> c) & 1) ka_len *= B.rank[c];
-  for (int e = 0; e < B.core_len; ++e) {
-    int rem = e, ka = 0, kam = 1, sp = 0, spm = 1;
-    for (int c = 0; c < N; ++c) {
-      const int v = rem % B.rank[c];
-      rem /= B.rank[c];
-      if ((mask >> c) & 1) {
-        ka += v * kam;
-        kam *= B.rank[c];
-      } else {
-        sp += v * spm;
-        spm *= B.rank[c];
-      }
-    }
-    perm[base + size_t(ka) + size_t(ka_len) * size_t(sp)] = e;
-  }
-}
 
 // The part of a BST plan that one range of bra blocks contributes, with offsets local to the
 // part (g_off of its dressed TDMs, op_off of its operators, t_off of its group terms, s_off
@@ -1279,8 +1292,9 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
         const uint64_t key = uint64_t(b) * 256 + uint64_t(G.act_mask);
         auto it = perm_at.find(key);
         if (it == perm_at.end()) {
-          it = perm_at.emplace(key, int64_t(P.perm.size())).first;
-          append_perm(blk[b], N, G.act_mask, P.perm);
+          it = perm_at.emplace(key, P.perm_total).first;
+          P.tables.push_back(BstPermTable{P.perm_total, b, G.act_mask});
+          P.perm_total += blk[b].core_len;
         }
         (side == 0 ? G.kperm_off : G.bperm_off) = it->second;
       }
@@ -1602,14 +1616,23 @@ int bst_set_impl(fcg_ctx* ctx, int nbody, int64_t n_blocks, const int16_t* fock,
   const double plan_s = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   FCG_REQUIRE(P.groups.size() < (size_t(1) << 31), FCG_ELIMIT, "BST: too many groups");
   {
-    std::string msg = check_groups(P.groups, blk, off, P.op_total, P.s_total, int64_t(P.perm.size()));
+    std::string msg = check_groups(P.groups, blk, off, P.op_total, P.s_total, P.perm_total);
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
   // device structures and the operator cache
   FCG_CUDA(ctx->d_bst_factors.upload(factors, size_t(n_factors), ctx->stream));
-  FCG_CUDA(ctx->d_bst_perm.upload(P.perm.data(), P.perm.size(), ctx->stream));
+  FCG_CUDA(ctx->d_bst_perm.alloc(size_t(std::max<int64_t>(P.perm_total, 1))));
   FCG_CUDA(ctx->d_bst_blocks.upload(blk.data(), blk.size(), ctx->stream));
   FCG_CUDA(ctx->d_bst_groups.upload(P.groups.data(), P.groups.size(), ctx->stream));
+  FCG_REQUIRE(P.tables.size() < (size_t(1) << 31), FCG_ELIMIT, "BST: too many index tables");
+  if (!P.tables.empty()) {
+    DevBuf<BstPermTable> d_tab;
+    FCG_CUDA(d_tab.upload(P.tables.data(), P.tables.size(), ctx->stream));
+    bst_perm_kernel<<<unsigned(P.tables.size()), 256, 0, ctx->stream>>>(d_tab.p, ctx->d_bst_blocks.p, N,
+                                                                      ctx->d_bst_perm.p);
+    FCG_CUDA(cudaGetLastError());
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // before d_tab goes
+  }
   DevBuf<BstGamma> d_gam;
   DevBuf<BstGroupTerm> d_gt;
   DevBuf<BstOverlapJob> d_ov;
