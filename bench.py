@@ -418,6 +418,19 @@ def bst_benchmark(steps, warmup, cpu_seconds, peaks, n_sectors=5, max_q=4):
         return {"bound": "hbm", "achieved": ach, "peak": hbm_peak, "unit": "GB/s", "frac": ach / hbm_peak,
                 "bytes_per_sigma": alg, "note": "operator cache + cores read/written per sigma, of measured HBM copy peak"}
 
+    # the sigma executes about 100 flops per byte of operator cache: its bound is arithmetic.
+    # Executed flops (spectator mode products + group contractions, all roots) over the kernel
+    # time, against the nominal CUDA-core peaks of GB300 (152 SMs at 2.07 GHz: 128 FP32 FMA or
+    # the FP64 rate per cycle); no measured figure exists for these pipes
+    flops_exec = st["bst_flops_executed"] * R
+    nominal = {"fp32": 152 * 128 * 2 * 2.07e9 / 1e12, "fp64": 1.25}
+
+    def flop_roof(kms, prec):
+        ach = flops_exec / (kms * 1e-3) / 1e12
+        return {"bound": f"{prec} cuda cores", "achieved": ach, "peak": nominal[prec], "unit": "TFLOP/s",
+                "frac": ach / nominal[prec], "flops_per_sigma": flops_exec,
+                "note": f"executed flops / kernel time, of the nominal {prec} CUDA-core peak (no measured peak)"}
+
     # tensor-core kernel: executed MMA flops (three TF32 products per tile, tiles padded to
     # 128 x 16k) over its CUDA-event time, against half the measured bf16 dense peak (TF32
     # runs at half the bf16 rate)
@@ -430,10 +443,11 @@ def bst_benchmark(steps, warmup, cpu_seconds, peaks, n_sectors=5, max_q=4):
         "cache_elements": cache, "cache_seconds": st["bst_cache_seconds"], "plan_seconds": st["bst_plan_seconds"],
         "set_wall_s": t_set,
         "flops_reference_per_sigma": st["bst_flops_reference"] * R,
+        "flops_executed_per_sigma": flops_exec,
         "fp64": {"value": 1e3 / ms64, "unit": "sigma_builds/s", "ms_per_step": ms64, "kernel_ms": k64,
-                 "roofline": roof(k64, 8)},
+                 "roofline": roof(k64, 8), "flop_roofline": flop_roof(k64, "fp64")},
         "fp32": {"value": 1e3 / ms32, "unit": "sigma_builds/s", "ms_per_step": ms32, "kernel_ms": k32,
-                 "roofline": roof(k32, 4), "rel_err_vs_fp64": rel32,
+                 "roofline": roof(k32, 4), "flop_roofline": flop_roof(k32, "fp32"), "rel_err_vs_fp64": rel32,
                  "tensor_cores": {"groups": s32["bst_tc_groups"], "of_groups": st["bst_groups"],
                                   "algorithmic_flops": s32["bst_tc_flops"], "mma_flops": s32["bst_tc_mma_flops"],
                                   "share_of_reference_flops": s32["bst_tc_flops"] / max(st["bst_flops_reference"] * R, 1),
@@ -898,7 +912,13 @@ def main():
     g = GpuSigma(local)
     g.set_ops(po)
     g.set_terms(pt)
-    g.state_set(f, c)
+    # the state's rows, sectors and closed-sigma plan (device join); the first call also
+    # uploads the term tables and grows the planner's buffers
+    t_set = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        g.state_set(f, c)
+        t_set.append(time.perf_counter() - t0)
     stream = torch.cuda.current_stream()
     g.set_stream(stream.cuda_stream)
     stats = g.stats()
@@ -1007,7 +1027,10 @@ def main():
         "vs_baseline": None, "dtype": "f32 (mixed; fp64 line in fp64)", "data": "synthetic",
         "config": bench_config(n, R, world),
         "workload_stats": {"n_terms": prob.ham.n_terms(), "triples_per_sigma": stats["n_triples"],
-                           "work_items": stats["n_work_items"], "plan_seconds": stats["plan_seconds"]},
+                           "work_items": stats["n_work_items"], "plan_seconds": stats["plan_seconds"],
+                           "join_seconds": stats["join_seconds"], "join_on_device": bool(stats["join_on_device"]),
+                           "state_set_ms": {"first": 1e3 * t_set[0], "warm": 1e3 * min(t_set[1:])},
+                           "plan_over_fp64_sigma": 1e3 * stats["plan_seconds"] / k64},
         "fp64": {"value": world * 1e3 / ms64, "ms_per_step": ms64, "kernel_ms": k64,
                  "mixed_over_fp64": ms64 / ms32, "fp32_rel_err_vs_fp64": rel32},
         "flops_reference_per_sigma": stats["flops_reference"],
