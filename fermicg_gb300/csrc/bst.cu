@@ -35,13 +35,18 @@ constexpr int kBstThreads = 256;
 constexpr int kOpThreads = 64;            // threads per group of the operator-cache build
 constexpr int kGammaSmem = 6144;          // doubles of the per-p staging tile of the gamma kernel
 constexpr int kSigmaSmemBytes = 96 * 1024;  // shared-memory workspace of a CTA-per-group sigma launch
+// CTA-per-group launches by workspace size: a launch reserves its largest group's shared
+// memory for every CTA, so groups are bucketed by the bytes they need (more resident CTAs for
+// the small ones)
+constexpr int kSmemBuckets = 4;
+constexpr int kSmemBucket[kSmemBuckets] = {12 * 1024, 24 * 1024, 48 * 1024, kSigmaSmemBytes};
 // shared memory of one warp of bst_sigma_bra_kernel (description + workspace); larger groups
 // run one CTA per group.  Measured on the 32-orbital / 8-cluster vector: float builds are
 // fastest with 8 KB, double builds with 2 KB (more resident warps; 11 % faster than 8 KB).
 constexpr int warp_smem_bytes(size_t elem) { return elem == 4 ? 8 * 1024 : 2 * 1024; }
 constexpr int kWarpSmemMax = 8 * 1024;
 constexpr int kAccBytes = 32 * 1024;        // shared-memory bra-core accumulator of bst_sigma_bra_kernel
-constexpr int64_t kChunkWork = int64_t(1) << 18;  // multiply-adds per bst_sigma_bra_kernel CTA, about
+constexpr int64_t kChunkWork = int64_t(1) << 16;  // multiply-adds per bst_sigma_bra_kernel CTA, about
 
 // ---- operator cache ----------------------------------------------------------------------
 
@@ -666,8 +671,8 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_smem_kernel(const int32
                                         core_total);
 }
 
-// Large groups: a grid of CTAs, each with its own global-memory workspace slice, walking
-// the list with a stride of the grid size.
+// Large groups: resident CTAs, each with its own global-memory workspace slice, taking the
+// next group of the list (longest first) from a counter until it runs out.
 template <typename T>
 __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int32_t* __restrict__ list, int n_list,
                                                                        const BstGroup* __restrict__ groups, int R,
@@ -676,10 +681,16 @@ __global__ void __launch_bounds__(kBstThreads) bst_sigma_global_kernel(const int
                                                                        const int32_t* __restrict__ perm,
                                                                        const T* __restrict__ cin,
                                                                        T* __restrict__ cout, int64_t core_total,
-                                                                       T* __restrict__ ws_all, int stride) {
+                                                                       T* __restrict__ ws_all, int stride,
+                                                                       unsigned* __restrict__ next) {
   __shared__ __align__(16) BstGroup G;
+  __shared__ int s_i;
   T* ws = ws_all + int64_t(blockIdx.x) * 2 * R * stride;
-  for (int i = blockIdx.x; i < n_list; i += gridDim.x) {
+  for (;;) {
+    if (threadIdx.x == 0) s_i = int(atomicAdd(next, 1u));
+    __syncthreads();
+    const int i = s_i;
+    if (i >= n_list) return;
     load_group<kBstThreads>(groups + list[i], &G, threadIdx.x);
     bst_group_apply<T, kBstThreads, true>(G, R, op, S, perm, cin, core_total, ws, stride, cout + G.b_off,
                                           core_total);
@@ -1363,6 +1374,11 @@ std::string check_groups(const std::vector<BstGroup>& groups, const std::vector<
 // R cores fit kAccBytes go to bst_sigma_bra_kernel, cut per bra block into chunks of about
 // kChunkWork multiply-adds; the others run one CTA per group from shared memory, or from
 // global memory.
+// multiply-adds and element moves of one group's sigma step, about
+int64_t group_work(const BstGroup& G, int R) {
+  return int64_t(R) * (int64_t(G.m) * G.k * (G.bcore / std::max(G.m, 1)) + 2 * G.kcore + 64);
+}
+
 void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
   ctx->bst_bra_ids.clear();
   ctx->bst_bra_ptr.assign(1, 0);
@@ -1379,6 +1395,7 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
   ctx->bst_tc_flops = 0;
   ctx->bst_tc_mma_flops = 0;
   const size_t ng = ctx->bst_groups.size();
+  std::vector<int32_t> bucket[kSmemBuckets];
   size_t g = 0;
   while (g < ng) {
     const int32_t b = ctx->bst_groups[g].bra;
@@ -1416,9 +1433,11 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
         }
         ctx->bst_bra_glist.push_back(int32_t(q));
         ctx->bst_bra_slice = std::max(ctx->bst_bra_slice, int((need + 15) / 16 * 16));
-        work += int64_t(R) * (int64_t(G.m) * G.k * (G.bcore / std::max(G.m, 1)) + 2 * G.kcore + 64);
+        work += group_work(G, R);
       } else if (need <= size_t(kSigmaSmemBytes)) {
-        ctx->bst_small.push_back(int32_t(q));
+        int i = 0;
+        while (need > size_t(kSmemBucket[i])) ++i;
+        bucket[i].push_back(int32_t(q));
       } else {
         ctx->bst_large.push_back(int32_t(q));
         ctx->bst_ws_large = std::max(ctx->bst_ws_large, G.ws);
@@ -1429,6 +1448,15 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
       ctx->bst_bra_acc = std::max(ctx->bst_bra_acc, int((acc + 15) / 16 * 16));
     }
     g = g1;
+  }
+  // longest first: the global-workspace CTAs take the list in order
+  std::stable_sort(ctx->bst_large.begin(), ctx->bst_large.end(), [&](int32_t x, int32_t y) {
+    return group_work(ctx->bst_groups[x], R) > group_work(ctx->bst_groups[y], R);
+  });
+  ctx->bst_small_ptr.assign(1, 0);
+  for (int i = 0; i < kSmemBuckets; ++i) {
+    ctx->bst_small.insert(ctx->bst_small.end(), bucket[i].begin(), bucket[i].end());
+    ctx->bst_small_ptr.push_back(int64_t(ctx->bst_small.size()));
   }
 }
 
@@ -1466,23 +1494,33 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     ++launches;
   }
   if (!ctx->bst_small.empty()) {
-    int ws_max = 0;
-    for (int32_t g : ctx->bst_small) ws_max = std::max(ws_max, ctx->bst_groups[g].ws);
-    const size_t smem = sizeof(BstGroup) + size_t(2) * R * ws_max * elem;
     FCG_CUDA(cudaFuncSetAttribute(bst_sigma_smem_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   int(kSigmaSmemBytes)));
-    bst_sigma_smem_kernel<T><<<unsigned(ctx->bst_small.size()), kBstThreads, smem, ctx->stream>>>(
-        ctx->d_bst_small.p, ctx->d_bst_groups.p, R, op, S, ctx->d_bst_perm.p, cin, cout, ct);
-    FCG_CUDA(cudaGetLastError());
-    ++launches;
+    for (int i = 0; i < kSmemBuckets; ++i) {
+      const int64_t a = ctx->bst_small_ptr[i], b = ctx->bst_small_ptr[i + 1];
+      if (a == b) continue;
+      int ws_max = 0;
+      for (int64_t q = a; q < b; ++q) ws_max = std::max(ws_max, ctx->bst_groups[ctx->bst_small[q]].ws);
+      const size_t smem = sizeof(BstGroup) + size_t(2) * R * ws_max * elem;
+      bst_sigma_smem_kernel<T><<<unsigned(b - a), kBstThreads, smem, ctx->stream>>>(
+          ctx->d_bst_small.p + a, ctx->d_bst_groups.p, R, op, S, ctx->d_bst_perm.p, cin, cout, ct);
+      FCG_CUDA(cudaGetLastError());
+      ++launches;
+    }
   }
   if (!ctx->bst_large.empty()) {
-    const int grid = int(std::min<size_t>(ctx->bst_large.size(), 4 * 152));
+    // as many CTAs as can be resident (each walks the list with the grid's stride)
+    int per_sm = 1, n_sm = 152;
+    FCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, bst_sigma_global_kernel<T>, kBstThreads, 0));
+    FCG_CUDA(cudaDeviceGetAttribute(&n_sm, cudaDevAttrMultiProcessorCount, ctx->device));
+    const int grid = int(std::min<size_t>(ctx->bst_large.size(), size_t(std::max(per_sm, 1)) * n_sm));
     const int64_t stride = ctx->bst_ws_large;
     FCG_CUDA(ws.alloc(size_t(grid) * 2 * R * stride));
+    FCG_CUDA(ctx->d_bst_next.alloc(1));
+    FCG_CUDA(cudaMemsetAsync(ctx->d_bst_next.p, 0, sizeof(unsigned), ctx->stream));
     bst_sigma_global_kernel<T><<<unsigned(grid), kBstThreads, 0, ctx->stream>>>(
         ctx->d_bst_large.p, int(ctx->bst_large.size()), ctx->d_bst_groups.p, R, op, S, ctx->d_bst_perm.p, cin, cout,
-        ct, ws.p, int(stride));
+        ct, ws.p, int(stride), ctx->d_bst_next.p);
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }

@@ -229,6 +229,7 @@ struct fcg_ctx {
   std::vector<BstGroup> bst_groups;
   std::vector<int32_t> bst_triples;     // [n][4] = {bra, ket, term, sign}
   std::vector<int32_t> bst_small, bst_large;  // groups run one CTA per group from shared / global memory
+  std::vector<int64_t> bst_small_ptr;         // bst_small in buckets of workspace size: [ptr[i], ptr[i+1])
   int32_t bst_ws_large = 0;
   std::vector<int32_t> bst_bra_ids, bst_bra_glist;  // bra block of each chunk, and the chunks' groups
   std::vector<int64_t> bst_bra_ptr;                 // chunk c holds bst_bra_glist[ptr[c], ptr[c+1])
@@ -238,6 +239,7 @@ struct fcg_ctx {
   DevBuf<BstBlock> d_bst_blocks;
   DevBuf<BstGroup> d_bst_groups;
   DevBuf<int32_t> d_bst_small, d_bst_large, d_bst_bra_ids, d_bst_bra_glist;
+  DevBuf<unsigned> d_bst_next;  // work counter of the global-workspace sigma launch
   DevBuf<int64_t> d_bst_bra_ptr;
   DevBuf<double> d_bst_factors;
   DevBuf<int32_t> d_bst_perm;      // actives-first index tables per (block, active clusters)
