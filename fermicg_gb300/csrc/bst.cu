@@ -1396,6 +1396,7 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
   ctx->bst_tc_mma_flops = 0;
   const size_t ng = ctx->bst_groups.size();
   std::vector<int32_t> bucket[kSmemBuckets];
+  std::vector<int64_t> chunk_work;  // per chunk of bst_sigma_bra_kernel
   size_t g = 0;
   while (g < ng) {
     const int32_t b = ctx->bst_groups[g].bra;
@@ -1428,12 +1429,14 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
         if (!open || work > kChunkWork) {
           if (open) ctx->bst_bra_ptr.push_back(int64_t(ctx->bst_bra_glist.size()));
           ctx->bst_bra_ids.push_back(b);
+          chunk_work.push_back(0);
           open = true;
           work = 0;
         }
         ctx->bst_bra_glist.push_back(int32_t(q));
         ctx->bst_bra_slice = std::max(ctx->bst_bra_slice, int((need + 15) / 16 * 16));
         work += group_work(G, R);
+        chunk_work.back() += group_work(G, R);
       } else if (need <= size_t(kSigmaSmemBytes)) {
         int i = 0;
         while (need > size_t(kSmemBucket[i])) ++i;
@@ -1449,12 +1452,36 @@ void bst_lists(fcg_ctx* ctx, int R, size_t elem) {
     }
     g = g1;
   }
+  // chunks of the warp kernel longest first (CTAs start in launch order)
+  {
+    const size_t nc = ctx->bst_bra_ids.size();
+    std::vector<size_t> order(nc);
+    for (size_t i = 0; i < nc; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return chunk_work[x] > chunk_work[y]; });
+    std::vector<int32_t> ids(nc), gl;
+    std::vector<int64_t> ptr(1, 0);
+    gl.reserve(ctx->bst_bra_glist.size());
+    for (size_t i = 0; i < nc; ++i) {
+      const size_t c = order[i];
+      ids[i] = ctx->bst_bra_ids[c];
+      gl.insert(gl.end(), ctx->bst_bra_glist.begin() + ctx->bst_bra_ptr[c],
+                ctx->bst_bra_glist.begin() + ctx->bst_bra_ptr[c + 1]);
+      ptr.push_back(int64_t(gl.size()));
+    }
+    ctx->bst_bra_ids.swap(ids);
+    ctx->bst_bra_glist.swap(gl);
+    ctx->bst_bra_ptr.swap(ptr);
+  }
   // longest first: the global-workspace CTAs take the list in order
   std::stable_sort(ctx->bst_large.begin(), ctx->bst_large.end(), [&](int32_t x, int32_t y) {
     return group_work(ctx->bst_groups[x], R) > group_work(ctx->bst_groups[y], R);
   });
   ctx->bst_small_ptr.assign(1, 0);
   for (int i = 0; i < kSmemBuckets; ++i) {
+    // CTAs start in launch order: longest first keeps the tail short
+    std::stable_sort(bucket[i].begin(), bucket[i].end(), [&](int32_t x, int32_t y) {
+      return group_work(ctx->bst_groups[x], R) > group_work(ctx->bst_groups[y], R);
+    });
     ctx->bst_small.insert(ctx->bst_small.end(), bucket[i].begin(), bucket[i].end());
     ctx->bst_small_ptr.push_back(int64_t(ctx->bst_small.size()));
   }
