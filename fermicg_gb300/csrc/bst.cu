@@ -1508,6 +1508,37 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
   const int64_t ct = ctx->bst_core_total;
   FCG_CUDA(cudaMemsetAsync(cout, 0, elem * size_t(ct) * R, ctx->stream));
   int launches = 1;
+  // tensor-core groups (float builds) on the second stream, overlapping the CUDA-core
+  // launches below: every kernel adds into the bra cores atomically
+  bool forked = false;
+  if constexpr (sizeof(T) == 4) {
+    if (!ctx->bst_tc.empty()) {
+      FCG_REQUIRE(ctx->bst_tc_jobs.size() / 4 < (size_t(1) << 31), FCG_ELIMIT, "too many tensor-core tiles");
+      if (!ctx->aux_stream) {
+        FCG_CUDA(cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking));
+        FCG_CUDA(cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        FCG_CUDA(cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+      }
+      cudaStream_t aux = ctx->aux_stream;
+      FCG_CUDA(ctx->d_bst_tc_ws.alloc(size_t(ctx->bst_tc_ws_total)));
+      FCG_CUDA(cudaEventRecord(ctx->ev_fork, ctx->stream));
+      FCG_CUDA(cudaStreamWaitEvent(aux, ctx->ev_fork, 0));
+      forked = true;
+      bst_tc_prep_kernel<<<unsigned(ctx->bst_tc.size()), kBstThreads, 0, aux>>>(
+          ctx->d_bst_tc.p, ctx->d_bst_tc_ws_off.p, ctx->d_bst_groups.p, R, S, ctx->d_bst_perm.p, cin, ct,
+          ctx->d_bst_tc_ws.p);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaFuncSetAttribute(bst_tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
+      FCG_CUDA(cudaEventRecord(ctx->ev2, aux));
+      bst_tc_gemm_kernel<<<unsigned(ctx->bst_tc_jobs.size() / 4), kTcThreads, kTcSmem, aux>>>(
+          reinterpret_cast<const BstTcJob*>(ctx->d_bst_tc_jobs.p), ctx->d_bst_groups.p, R, op, ctx->d_bst_tc_ws.p,
+          ctx->d_bst_tc_ws_off.p, ctx->d_bst_perm.p, cout, ct, ctx->d_bst_tc_err.p);
+      FCG_CUDA(cudaGetLastError());
+      FCG_CUDA(cudaEventRecord(ctx->ev3, aux));
+      FCG_CUDA(cudaEventRecord(ctx->ev_join, aux));
+      launches += 2;
+    }
+  }
   if (!ctx->bst_bra_ids.empty()) {
     constexpr int kWarps = kBstThreads / 32;
     const int priv = size_t(kWarps) * ctx->bst_bra_acc <= size_t(kAccBytes) ? 1 : 0;
@@ -1551,24 +1582,7 @@ int bst_launch(fcg_ctx* ctx, int R, const T* op, const T* S, const T* cin, T* co
     FCG_CUDA(cudaGetLastError());
     ++launches;
   }
-  if constexpr (sizeof(T) == 4) {
-    if (!ctx->bst_tc.empty()) {
-      FCG_REQUIRE(ctx->bst_tc_jobs.size() / 4 < (size_t(1) << 31), FCG_ELIMIT, "too many tensor-core tiles");
-      FCG_CUDA(ctx->d_bst_tc_ws.alloc(size_t(ctx->bst_tc_ws_total)));
-      bst_tc_prep_kernel<<<unsigned(ctx->bst_tc.size()), kBstThreads, 0, ctx->stream>>>(
-          ctx->d_bst_tc.p, ctx->d_bst_tc_ws_off.p, ctx->d_bst_groups.p, R, S, ctx->d_bst_perm.p, cin, ct,
-          ctx->d_bst_tc_ws.p);
-      FCG_CUDA(cudaGetLastError());
-      FCG_CUDA(cudaFuncSetAttribute(bst_tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, kTcSmem));
-      FCG_CUDA(cudaEventRecord(ctx->ev2, ctx->stream));
-      bst_tc_gemm_kernel<<<unsigned(ctx->bst_tc_jobs.size() / 4), kTcThreads, kTcSmem, ctx->stream>>>(
-          reinterpret_cast<const BstTcJob*>(ctx->d_bst_tc_jobs.p), ctx->d_bst_groups.p, R, op, ctx->d_bst_tc_ws.p,
-          ctx->d_bst_tc_ws_off.p, ctx->d_bst_perm.p, cout, ct, ctx->d_bst_tc_err.p);
-      FCG_CUDA(cudaGetLastError());
-      FCG_CUDA(cudaEventRecord(ctx->ev3, ctx->stream));
-      launches += 2;
-    }
-  }
+  if (forked) FCG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
   ctx->stats.kernel_launches = launches;
   return FCG_OK;
 }

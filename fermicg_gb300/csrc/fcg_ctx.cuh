@@ -80,6 +80,10 @@ struct fcg_ctx {
   cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ev2 = nullptr, ev3 = nullptr;  // around one kernel inside a timed sequence
+  // a second stream for work that overlaps the context stream's (created on first use),
+  // and the events that fork it from and join it back to that stream
+  cudaStream_t aux_stream = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   std::string err;
   // problem
   int N = 0;
