@@ -41,9 +41,10 @@ constexpr int kSigmaSmemBytes = 96 * 1024;  // shared-memory workspace of a CTA-
 constexpr int kSmemBuckets = 4;
 constexpr int kSmemBucket[kSmemBuckets] = {12 * 1024, 24 * 1024, 48 * 1024, kSigmaSmemBytes};
 // shared memory of one warp of bst_sigma_bra_kernel (description + workspace); larger groups
-// run one CTA per group.  Measured on the 32-orbital / 8-cluster vector: float builds are
-// fastest with 8 KB, double builds with 2 KB (more resident warps; 11 % faster than 8 KB).
-constexpr int warp_smem_bytes(size_t elem) { return elem == 4 ? 8 * 1024 : 2 * 1024; }
+// run one CTA per group.  Measured on the 32-orbital / 8-cluster vector with cores up to 12^4:
+// float builds are fastest with 4 KB (9 % faster than 8 KB once the CTA-per-group launches
+// were bucketed by workspace size), double builds with 2 KB.
+constexpr int warp_smem_bytes(size_t elem) { return elem == 4 ? 4 * 1024 : 2 * 1024; }
 constexpr int kWarpSmemMax = 8 * 1024;
 constexpr int kAccBytes = 32 * 1024;        // shared-memory bra-core accumulator of bst_sigma_bra_kernel
 constexpr int64_t kChunkWork = int64_t(1) << 16;  // multiply-adds per bst_sigma_bra_kernel CTA, about
