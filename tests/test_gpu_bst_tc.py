@@ -71,3 +71,32 @@ def test_tensor_core_sigma_at_config2_core_sizes():
     hy = g.bst_sigma(y, "fp32")
     assert rel_err(g.bst_sigma(x - 0.5 * y, "fp32"), out - 0.5 * hy) < 1e-5
     g.close()
+
+
+def test_config2_sigma_sampled_blocks_match_the_oracle():
+    """The FP64 and FP32 sigma on the config-2-sized vector (every launch path: warp chunks,
+    the CTA-per-group workspace buckets, the global-workspace groups taken largest first, the
+    tensor-core groups on the second stream) against the oracle's build_sigma! for a sample of
+    bra blocks: the largest cores and an even spread of the rest."""
+    prob = workloads.config2_problem(0)
+    secs = workloads.single_transfer_sectors(prob)
+    R = 2
+    vec = synthetic_bst(prob, secs[:1], max_q=4, rank_range=(4, 12), R=R, seed=0)
+    pb = PackedBST(vec, 8, R)
+    g = _gpu(prob)
+    g.bst_set(pb)
+    x = pb.cores_of(vec)
+    out64 = g.bst_sigma(x, "fp64")
+    out32 = g.bst_sigma(x, "fp32")
+    sizes = pb.blocks[:, 1]
+    pick = set(np.argsort(-sizes)[:3].tolist()) | set(range(0, len(pb.keys), max(1, len(pb.keys) // 5)))
+    sample = [pb.keys[i] for i in sorted(pick)]
+    want = obst.build_sigma({k: obst.zero_like({k: vec[k]}, R)[k] for k in sample}, vec, prob.ops, prob.ham, 8, R)
+    for k in sample:
+        i = pb.index[k]
+        o, n = int(pb.blocks[i, 0]), int(pb.blocks[i, 1])
+        ref = np.stack([np.asarray(want[k]["core"][r]).reshape(-1, order="F") for r in range(R)])
+        scale = max(float(np.abs(ref).max()), 1e-300)
+        assert float(np.abs(out64[:, o:o + n] - ref).max()) / scale < 1e-10
+        assert float(np.abs(out32[:, o:o + n] - ref).max()) / scale < FP32_TOL
+    g.close()
