@@ -156,3 +156,24 @@ def test_bad_rows_same_message_both_planners(kind):
         assert g.stats()["n_cfg"] == len(f)
     assert msgs[0] == msgs[1], msgs
     assert "Fock" in msgs[0] or "local state" in msgs[0]
+
+
+def test_planners_agree_on_an_empty_join():
+    """Only terms that change the Fock sector, on the rows of one sector: no ket sector exists
+    for any (bra sector, transfer), so the plan has no records, work items or lane jobs, and
+    sigma is zero."""
+    prob, st = config1_subspace(3000, 4)
+    ham = ClusteredOperator(prob.ham.n_clusters)
+    for tr, terms in prob.ham:
+        if any(int(x) != 0 for pair in tr for x in pair):
+            ham.trans[tr] = list(terms)
+    po = pack.pack_ops(prob.ops, prob.bases)
+    pt = pack.pack_terms(ham)
+    f, c, v, _ = pack.pack_state(st)
+    n0 = int(np.argmin(np.all(f == f[0], axis=(1, 2))))
+    g, host = _both(po, pt, f[:n0].copy(), c[:n0].copy())
+    assert host["items"] == 0 and len(host["jobs"]) == 0 and len(host["ts"]) == 0
+    assert g.stats()["n_triples"] == 0
+    x = v[:n0, :2].copy()
+    for prec in ("fp64", "fp32"):
+        assert np.abs(g.sigma_closed(x, prec)).max() == 0.0
