@@ -260,6 +260,7 @@ class FlatTPSCI:
         self.next_ins = 0
         self.next_rank = 0
         self._key = None
+        self._ks = None     # (argsort of the keys, the sorted keys), while the keys stay as they are
         self._canon = True  # the physical rows are in TPSCIstate row order
 
     # -- construction and views ----------------------------------------------------------
@@ -292,6 +293,8 @@ class FlatTPSCI:
         """physical rows in TPSCIstate row order"""
         if len(self.sec) == 0:
             return np.zeros(0, dtype=np.int64)
+        if self._canon:  # already in row order
+            return np.arange(len(self.sec), dtype=np.int64)
         rank = np.zeros(len(self.reg.focks), dtype=np.int64)
         for sid, r in self.rank.items():
             rank[sid] = r
@@ -306,6 +309,7 @@ class FlatTPSCI:
         o = self.order()
         self.sec, self.cfg, self.coef, self.ins = self.sec[o], self.cfg[o], self.coef[o], self.ins[o]
         self._key = None if self._key is None else self._key[o]
+        self._ks = None
         self._canon = True
 
     def rows(self):
@@ -343,11 +347,13 @@ class FlatTPSCI:
         self.ins = np.concatenate([self.ins, self.next_ins + np.arange(n, dtype=np.int64)])
         self.next_ins += n
         self._key = None
+        self._ks = None
 
     def _keep(self, mask):
         """keep the rows of mask; sectors left without rows are deleted"""
         self.sec, self.cfg, self.coef, self.ins = self.sec[mask], self.cfg[mask], self.coef[mask], self.ins[mask]
         self._key = None if self._key is None else self._key[mask]
+        self._ks = None
         live = set(np.unique(self.sec).tolist())
         self.rank = {s: r for s, r in self.rank.items() if s in live}
 
@@ -356,8 +362,10 @@ class FlatTPSCI:
         k = self.key()
         if len(k) == 0:
             return np.full(len(keys), -1, dtype=np.int64)
-        o = np.argsort(k, kind="stable")
-        ks = k[o]
+        if self._ks is None:
+            o = np.argsort(k, kind="stable")
+            self._ks = (o, k[o])
+        o, ks = self._ks
         p = np.searchsorted(ks, keys)
         p = np.minimum(p, len(ks) - 1)
         hit = ks[p] == keys
@@ -369,6 +377,7 @@ class FlatTPSCI:
         s.sec, s.cfg, s.coef, s.ins = self.sec.copy(), self.cfg.copy(), self.coef.copy(), self.ins.copy()
         s.rank, s.next_ins, s.next_rank = dict(self.rank), self.next_ins, self.next_rank
         s._key = None if self._key is None else self._key.copy()
+        s._ks = None if self._ks is None else (self._ks[0].copy(), self._ks[1].copy())
         s._canon = self._canon
         return s
 
