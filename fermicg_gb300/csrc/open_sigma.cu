@@ -149,6 +149,7 @@ __device__ __forceinline__ void table_add(unsigned long long* keys, double* vals
 }
 
 constexpr int kExpThreads = 256;
+constexpr int kOpenMaxR = 16;  // roots of one open sigma at most (checked on the host)
 constexpr int kExpSmemBytes = 96 * 1024;  // shared-memory budget of one expand CTA
 // The float pre-filter keeps a contribution for the exact double evaluation unless
 // |x32| + kFilterMargin * s32 <= thresh / max|c|, where s32 = sum of |products| of the same
@@ -228,7 +229,7 @@ __device__ __forceinline__ void expand_emit(const OpenParams& p, double x, doubl
                                             double* vals, unsigned long long cap_mask,
                                             unsigned long long* counters) {
   if (!(fabs(x) > tc)) return;
-  double add[16];
+  double add[kOpenMaxR];
   for (int r = 0; r < p.R; ++r) add[r] = x * crow[r];
   table_add(keys, vals, cap_mask, keybase | (unsigned long long)idx, add, p.R, counters + 2);
 }
@@ -238,7 +239,7 @@ __device__ __forceinline__ void expand_emit(const OpenParams& p, double x, doubl
 // d2 <= 16 with the run-time length `d2`.
 template <int D2>
 __device__ __forceinline__ void unit4(const OpenParams& p, const float* T1, const float* T1a, int P, int pr, int d1,
-                                      const float* g1, const float* G2f, int mb3, float tcf, double tc, double sg,
+                                      const float* g1, const float* G2f, int mb3, float tcf, double tc,
                                       int d0, const double* wc, const double* g0d, const double* g1d,
                                       const double* G2d, const double* crow, unsigned long long keybase,
                                       int64_t idx3, int64_t sa3, unsigned long long* keys, double* vals,
@@ -264,7 +265,7 @@ __device__ __forceinline__ void unit4(const OpenParams& p, const float* T1, cons
         s32 = fmaf(ua[l], fabsf(g2[l]), s32);
       }
     if (fabsf(x32) + kFilterMargin * s32 > tcf) {
-      const double x = sg * exact_x(3, d0, d1, d2, wc, g0d, g1d, G2d + d2 * b3);
+      const double x = exact_x(3, d0, d1, d2, wc, g0d, g1d, G2d + d2 * b3);
       expand_emit(p, x, tc, crow, keybase, idx3 + b3 * sa3, keys, vals, cap_mask, counters);
     }
   }
@@ -285,6 +286,7 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
   extern __shared__ __align__(16) double xs[];
   float* xf = reinterpret_cast<float*>(xs);
   __shared__ unsigned long long s_job;
+  __shared__ double s_cs[kOpenMaxR];
   for (;;) {
     if (threadIdx.x == 0) s_job = atomicAdd(counters + 4, 1ull);
     __syncthreads();
@@ -294,8 +296,8 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
     const OpenTerm& o = p.ot[job.y];
     const TermSector& ts = o.ts;
     const int16_t* ck = p.cfg + int64_t(job.x) * kCfgStride;
-    const double* crow = p.c + int64_t(job.x) * p.R;
-    const double tc = p.thresh / row_maxabs(crow, p.R);
+    const double* c_ket = p.c + int64_t(job.x) * p.R;
+    const double tc = p.thresh / row_maxabs(c_ket, p.R);
     const float tcf = float(tc * (1.0 - 1e-6));
     const int nrem = ts.nrem, rest = ts.rest_len;
     const int d0 = nrem >= 1 ? ts.g_dim[0] : 1, d1 = nrem >= 2 ? ts.g_dim[1] : 1, d2 = nrem >= 3 ? ts.g_dim[2] : 1;
@@ -312,6 +314,11 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
     }
     const unsigned long long keybase = (unsigned long long)(o.bsec) << kKeyIdxBits;
     const double sg = ts.sign < 0 ? -1.0 : 1.0;
+    // the ket's coefficients times the term's sign (exact): a kept value x contributes
+    // x * (sg * c) = (sg * x) * c to every root
+    if (threadIdx.x < p.R) s_cs[threadIdx.x] = sg * c_ket[threadIdx.x];
+    __syncthreads();
+    const double* crow = s_cs;
     const double* wblk = w + ts.w_off + int64_t(rest) * ts.w_mb * ck[ts.cw];  // [rest][mb0] for the ket state
     const double* gblk[3] = {nullptr, nullptr, nullptr};
     for (int r = 0; r < nrem; ++r) gblk[r] = op + ts.g_off[r] + int64_t(ts.g_dim[r]) * ts.g_mb[r] * ck[ts.cr[r]];
@@ -349,7 +356,7 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
             s32 = fmaf(fabsf(wc[i]), fabsf(g0[i]), s32);
           }
           if (fabsf(x32) + kFilterMargin * s32 > tcf) {
-            const double x = sg * exact_x(1, d0, 1, 1, W + rest * b0, xs + t.g64[0] + d0 * b1, nullptr, nullptr);
+            const double x = exact_x(1, d0, 1, 1, W + rest * b0, xs + t.g64[0] + d0 * b1, nullptr, nullptr);
             expand_emit(p, x, tc, crow, keybase, base + b0 * sa[0] + b1 * sa[1], keys, vals, cap_mask, counters);
           }
         }
@@ -388,26 +395,26 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
               s32 = fmaf(T1a[pr + P * j], fabsf(g1[j]), s32);
             }
             if (fabsf(x32) + kFilterMargin * s32 > tcf) {
-              const double x = sg * exact_x(2, d0, d1, 1, wc, g0d, g1d, nullptr);
+              const double x = exact_x(2, d0, d1, 1, wc, g0d, g1d, nullptr);
               expand_emit(p, x, tc, crow, keybase, idx3, keys, vals, cap_mask, counters);
             }
           } else {
             switch (d2) {
-              case 1: unit4<1>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 1: unit4<1>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 2: unit4<2>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 2: unit4<2>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 3: unit4<3>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 3: unit4<3>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 4: unit4<4>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 4: unit4<4>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 5: unit4<5>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 5: unit4<5>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 6: unit4<6>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 6: unit4<6>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              case 8: unit4<8>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              case 8: unit4<8>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters); break;
-              default: unit4<16>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, sg, d0, wc, g0d, g1d,
+              default: unit4<16>(p, T1, T1a, P, pr, d1, g1, xf + t.g32[2], mb[3], tcf, tc, d0, wc, g0d, g1d,
                                  xs + t.g64[2], crow, keybase, idx3, sa[3], keys, vals, cap_mask, counters, d2); break;
             }
           }
@@ -427,7 +434,7 @@ __global__ void __launch_bounds__(kExpThreads) expand_jobs_kernel(
                                   nrem >= 1 ? gblk[0] + int64_t(d0) * b[1] : nullptr,
                                   nrem >= 2 ? gblk[1] + int64_t(d1) * b[2] : nullptr,
                                   nrem >= 3 ? gblk[2] + int64_t(d2) * b[3] : nullptr);
-        const double x = nrem == 0 ? xr : sg * xr;
+        const double x = xr;
         int64_t idx = base;
         for (int a = 0; a < o.n_act; ++a) idx += b[a] * sa[a];
         expand_emit(p, x, tc, crow, keybase, idx, keys, vals, cap_mask, counters);
@@ -492,7 +499,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(ctx->have_state, FCG_ESTATE, "fcg_state_set must come first");
   FCG_REQUIRE(c && n_out, FCG_EINVAL, "null pointer");
-  FCG_REQUIRE(R >= 1 && R <= 16, FCG_ELIMIT, "R must be in [1, 16]");
+  FCG_REQUIRE(R >= 1 && R <= kOpenMaxR, FCG_ELIMIT, "R must be in [1, 16]");
   FCG_REQUIRE(thresh >= 0.0, FCG_EINVAL, "thresh must be >= 0");
   FCG_CUDA(cudaSetDevice(ctx->device));
   {
