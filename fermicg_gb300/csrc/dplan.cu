@@ -23,8 +23,6 @@
 //     warp chunks.
 // Four host waits read the sizes the next buffers need.
 #include <algorithm>
-#include <chrono>
-#include <cstring>
 
 #include "dprim.cuh"
 #include "fcg_ctx.cuh"
@@ -486,6 +484,11 @@ __global__ void items_kernel(PairParams p, int64_t E, const int64_t* __restrict_
   }
 }
 
+// the state's sector count, for the host
+__global__ void rows_collect_kernel(const int32_t* __restrict__ n_sec_at, unsigned long long* __restrict__ counters) {
+  counters[1] = (unsigned long long)*n_sec_at;
+}
+
 // the sizes the next phase needs, in one place for one copy
 __global__ void collect_kernel(const int32_t* __restrict__ n_items_at, const int64_t* __restrict__ n_jobs_at,
                                unsigned long long* __restrict__ counters) {
@@ -671,10 +674,6 @@ static int read_counters(fcg_ctx* ctx, int n) {
                            ctx->stream));
   FCG_CUDA(cudaStreamSynchronize(ctx->stream));
   return FCG_OK;
-}
-
-__global__ void rows_collect_kernel(const int32_t* __restrict__ n_sec_at, unsigned long long* __restrict__ counters) {
-  counters[1] = (unsigned long long)*n_sec_at;
 }
 
 // the sector table of the state's sectors (Fock key -> sector), sized for n_sec sectors
