@@ -517,6 +517,10 @@ int fcg_bst_fois(fcg_ctx* ctx, int R, int nbody, double thresh, int compress_twi
   FCG_REQUIRE(N <= kTuckMaxModes, FCG_ELIMIT, "at most 8 clusters");
   FCG_CUDA(cudaSetDevice(ctx->device));
   const auto t0 = std::chrono::steady_clock::now();
+  {
+    const int rc = term_norms(ctx);
+    if (rc) return rc;
+  }
   const int nmax1 = ctx->nmax + 1;
   // the state's blocks: validation, core offsets, and their grouping by Fock sector
   std::vector<int64_t> coff(n_blocks), clen(n_blocks);

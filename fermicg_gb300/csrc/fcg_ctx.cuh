@@ -97,13 +97,15 @@ struct fcg_ctx {
   std::vector<int32_t> h_blk_index;
   DevBuf<double> d_op64;
   DevBuf<float> d_op32;
+  DevBuf<double> d_op_raw;  // the caller's TDM blob as given (fcg_set_ops), placed into d_op64 / d_op32
   DevBuf<BlockInfo> d_blocks;
   DevBuf<int32_t> d_blk_index;
   DevBuf<int32_t> d_norb;
   int n_terms = 0;
   std::vector<int32_t> trm;
   std::vector<TermInfo> terms;
-  std::vector<double> term_ints_norm;  // Frobenius norm of each term's integrals (0 for 1-body terms)
+  std::vector<double> term_ints_norm;  // Frobenius norm of each term's integrals (0 for 1-body terms; term_norms)
+  int64_t n_ints = 0;
   std::vector<TermDress> dress;
   std::vector<int64_t> w_index;
   int64_t n_w = 0;
@@ -283,6 +285,7 @@ int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_
 int ensure_dressed(fcg_ctx* ctx);
 int ensure_plan(fcg_ctx* ctx);
 ProblemInfo problem_info(fcg_ctx* ctx);
+int term_norms(fcg_ctx* ctx);
 
 // The closed-sigma join of the state on the device (dplan.cu): fills d_perm, d_ts, d_jobs,
 // d_chunk_lo / d_chunk_val, d_wt_cum / d_wt_vals and the plan sizes; and a chunk table of

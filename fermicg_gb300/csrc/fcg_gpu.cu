@@ -78,6 +78,21 @@ __global__ void to_float_kernel(const double* __restrict__ a, float* __restrict_
   for (; i < n; i += int64_t(gridDim.x) * blockDim.x) b[i] = float(a[i]);
 }
 
+// One TDM block of the caller's blob placed at its aligned offset, with its float copy.
+struct PlaceJob {
+  int64_t src, dst, n;
+};
+
+__global__ void place_blocks_kernel(const PlaceJob* __restrict__ jobs, const double* __restrict__ raw,
+                                    double* __restrict__ op64, float* __restrict__ op32) {
+  const PlaceJob J = jobs[blockIdx.x];
+  for (int64_t i = threadIdx.x; i < J.n; i += blockDim.x) {
+    const double v = raw[J.src + i];
+    op64[J.dst + i] = v;
+    op32[J.dst + i] = float(v);
+  }
+}
+
 // Column maxima over the bra index, used by the open-sigma screen:
 // out[i + len*k] = max_b |in[i + len*(b + mb*k)]| for every block of a list.
 struct MaxJob {
@@ -707,6 +722,7 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
   if (!ctx) return FCG_EINVAL;
   FCG_REQUIRE(n_clusters > 0 && n_clusters <= kMaxClusters, FCG_ELIMIT, "n_clusters must be in [1, 8]");
   FCG_REQUIRE(cluster_norb && block_table && (data || n_data == 0) && n_blocks >= 0, FCG_EINVAL, "null pointer");
+  FCG_REQUIRE(n_blocks < (int64_t(1) << 31), FCG_ELIMIT, "at most 2^31 - 1 TDM blocks");
   FCG_CUDA(cudaSetDevice(ctx->device));
   ctx->N = n_clusters;
   ctx->norb.assign(cluster_norb, cluster_norb + n_clusters);
@@ -740,14 +756,28 @@ int fcg_set_ops(fcg_ctx* ctx, int n_clusters, const int32_t* cluster_norb, int64
     ctx->h_blocks[b] = BlockInfo{cursor, int32_t(r[6]), int32_t(r[7]), int32_t(r[8]), 0};
     cursor += r[6] * r[7] * r[8];
   }
-  std::vector<double> d64(size_t(std::max<int64_t>(cursor, 1)), 0.0);
-  for (int64_t b = 0; b < n_blocks; ++b) {
-    const int64_t* r = &ctx->opb[b * kOpbCols];
-    std::memcpy(&d64[ctx->h_blocks[b].off], data + r[9], sizeof(double) * r[6] * r[7] * r[8]);
+  // the caller's blob goes up once; a kernel places every block at its aligned offset and
+  // writes the float copy (the gaps between blocks are zero)
+  {
+    const size_t total = size_t(std::max<int64_t>(cursor, 1));
+    FCG_CUDA(ctx->d_op64.alloc(total));
+    FCG_CUDA(ctx->d_op32.alloc(total));
+    FCG_CUDA(cudaMemsetAsync(ctx->d_op64.p, 0, sizeof(double) * total, ctx->stream));
+    FCG_CUDA(cudaMemsetAsync(ctx->d_op32.p, 0, sizeof(float) * total, ctx->stream));
+    if (n_blocks > 0) {
+      std::vector<PlaceJob> pj(n_blocks);
+      for (int64_t b = 0; b < n_blocks; ++b) {
+        const int64_t* r = &ctx->opb[b * kOpbCols];
+        pj[b] = PlaceJob{r[9], ctx->h_blocks[b].off, r[6] * r[7] * r[8]};
+      }
+      FCG_CUDA(ctx->d_op_raw.upload(data, size_t(n_data), ctx->stream));
+      PlaceJob* d_pj = nullptr;
+      FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, pj.data(), pj.size(), ctx->stream, &d_pj));
+      place_blocks_kernel<<<unsigned(n_blocks), 256, 0, ctx->stream>>>(d_pj, ctx->d_op_raw.p, ctx->d_op64.p,
+                                                                        ctx->d_op32.p);
+      FCG_CUDA(cudaGetLastError());
+    }
   }
-  std::vector<float> d32(d64.begin(), d64.end());
-  FCG_CUDA(ctx->d_op64.upload(d64.data(), d64.size(), ctx->stream));
-  FCG_CUDA(ctx->d_op32.upload(d32.data(), d32.size(), ctx->stream));
   FCG_CUDA(ctx->d_blocks.upload(ctx->h_blocks.data(), ctx->h_blocks.size(), ctx->stream));
   FCG_CUDA(ctx->d_blk_index.upload(ctx->h_blk_index.data(), ctx->h_blk_index.size(), ctx->stream));
   FCG_CUDA(ctx->d_norb.upload(ctx->norb.data(), ctx->norb.size(), ctx->stream));
@@ -869,16 +899,8 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
     tm.ints_off = int64_t(uint32_t(r[26])) | (int64_t(r[27]) << 32);
     if (r[0] > 1) FCG_REQUIRE(tm.ints_off >= 0 && tm.ints_off + len <= n_ints, FCG_EINVAL, "term ints out of range");
   }
-  ctx->term_ints_norm.assign(size_t(n_terms), 0.0);
-  for (int t = 0; t < n_terms; ++t) {
-    const int32_t* r = term_table + int64_t(t) * kTrmCols;
-    if (r[0] < 2) continue;
-    int64_t len = 1;
-    for (int o = 0; o < r[0]; ++o) len *= r[22 + o];
-    double s2 = 0.0;
-    for (int64_t i = 0; i < len; ++i) s2 += ints[ctx->terms[t].ints_off + i] * ints[ctx->terms[t].ints_off + i];
-    ctx->term_ints_norm[size_t(t)] = std::sqrt(s2);
-  }
+  ctx->n_ints = n_ints;
+  ctx->term_ints_norm.clear();  // computed when first needed (term_norms)
   std::vector<DressJob> jobs;
   int64_t w_total = 0;
   {
@@ -887,10 +909,14 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
     FCG_REQUIRE(msg.empty(), FCG_EINVAL, msg);
   }
   ctx->n_w = w_total;
-  std::vector<float> i32(ints, ints + n_ints);
   FCG_CUDA(ctx->d_terms.upload(ctx->terms.data(), ctx->terms.size(), ctx->stream));
   FCG_CUDA(ctx->d_ints64.upload(ints, n_ints, ctx->stream));
-  FCG_CUDA(ctx->d_ints32.upload(i32.data(), n_ints, ctx->stream));
+  FCG_CUDA(ctx->d_ints32.alloc(size_t(std::max<int64_t>(n_ints, 1))));
+  if (n_ints > 0) {
+    to_float_kernel<<<unsigned(std::min<int64_t>((n_ints + 255) / 256, 65535)), 256, 0, ctx->stream>>>(
+        ctx->d_ints64.p, ctx->d_ints32.p, n_ints);
+    FCG_CUDA(cudaGetLastError());
+  }
   // the dressed operators themselves are built on the device by the first fcg_state_set
   // (only the closed and open sigmas use them; a BST-only context never needs them)
   ctx->dress_jobs.swap(jobs);
@@ -902,6 +928,31 @@ int fcg_set_terms(fcg_ctx* ctx, int n_terms, const int32_t* term_table, int64_t 
 }
 
 }  // extern "C"
+
+// Frobenius norm of every term's integrals (0 for 1-body terms), from the device copy of the
+// integrals, on first use after fcg_set_terms.
+int term_norms(fcg_ctx* ctx) {
+  if (int64_t(ctx->term_ints_norm.size()) == ctx->n_terms) return FCG_OK;
+  std::vector<double> ints(size_t(std::max<int64_t>(ctx->n_ints, 1)));
+  if (ctx->n_ints > 0) {
+    FCG_CUDA(cudaMemcpyAsync(ints.data(), ctx->d_ints64.p, sizeof(double) * size_t(ctx->n_ints),
+                             cudaMemcpyDeviceToHost, ctx->stream));
+    FCG_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  std::vector<double> norm(size_t(ctx->n_terms), 0.0);
+  for (int t = 0; t < ctx->n_terms; ++t) {
+    const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
+    if (r[0] < 2) continue;
+    int64_t len = 1;
+    for (int o = 0; o < r[0]; ++o) len *= r[22 + o];
+    double s2 = 0.0;
+    const double* v = ints.data() + ctx->terms[t].ints_off;
+    for (int64_t i = 0; i < len; ++i) s2 += v[i] * v[i];
+    norm[size_t(t)] = std::sqrt(s2);
+  }
+  ctx->term_ints_norm.swap(norm);
+  return FCG_OK;
+}
 
 ProblemInfo problem_info(fcg_ctx* ctx) {
   ProblemInfo pi;
