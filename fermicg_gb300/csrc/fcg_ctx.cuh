@@ -116,6 +116,7 @@ struct fcg_ctx {
   DevBuf<float> d_w32;
   std::vector<DressJob> dress_jobs;  // W blocks to build (fcg_set_terms), built by the first fcg_state_set
   bool dressed = false;
+  bool wmax_built = false;  // column maxima of the dressed operators (open-sigma screen)
   int n_trans = 0;
   std::vector<int16_t> trans;
   // state + plan
@@ -283,6 +284,7 @@ int sigma_closed_device_async(fcg_ctx* ctx, int R, const double* d_c, double* d_
 // The dressed operators of the term set, and the closed-sigma plan of the state, built on
 // first use (fcg_gpu.cu)
 int ensure_dressed(fcg_ctx* ctx);
+int ensure_wmax(fcg_ctx* ctx);  // the open sigma's column maxima of the dressed operators
 int ensure_plan(fcg_ctx* ctx);
 ProblemInfo problem_info(fcg_ctx* ctx);
 int term_norms(fcg_ctx* ctx);

@@ -828,33 +828,45 @@ int ensure_dressed(fcg_ctx* ctx) {
     to_float_kernel<<<1024, 256, 0, ctx->stream>>>(ctx->d_w64.p, ctx->d_w32.p, w_total);
     FCG_CUDA(cudaGetLastError());
   }
-  {
-    // Wmax[rest, k] per W block, indexed like w_index
-    std::vector<MaxJob> mj(jobs.size());
-    ctx->wmax_index.assign(ctx->w_index.size(), -1);
-    int64_t tot = 0;
-    for (size_t j = 0; j < jobs.size(); ++j) {
-      const DressJob& J = jobs[j];
-      mj[j] = MaxJob{J.w_off, tot, J.rest_len, J.mb, J.mk, 0};
-      tot += int64_t(J.rest_len) * J.mk;
-    }
-    for (size_t i = 0; i < ctx->w_index.size(); ++i) {
-      if (ctx->w_index[i] < 0) continue;
-      // jobs are in w_off order; find the job of this W block
-      auto it = std::lower_bound(jobs.begin(), jobs.end(), ctx->w_index[i],
-                                 [](const DressJob& J, int64_t v) { return J.w_off < v; });
-      ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
-    }
-    MaxJob* d_mj = nullptr;
-    FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, mj.data(), mj.size(), ctx->stream, &d_mj));
-    FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
-    if (!jobs.empty()) {
-      colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj, ctx->d_w64.p, ctx->d_wmax.p);
-      FCG_CUDA(cudaGetLastError());
-    }
-    FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job lists are reused by the next call
-  }
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job list's staging buffer is reused by the next call
+  ctx->wmax_built = false;
   ctx->dressed = true;
+  return FCG_OK;
+}
+
+// Column maxima of the dressed operators for the open sigma's screen: Wmax[rest, k] per W
+// block, indexed like w_index; built on the first open sigma after the dressing.
+int ensure_wmax(fcg_ctx* ctx) {
+  {
+    const int rc = ensure_dressed(ctx);
+    if (rc) return rc;
+  }
+  if (ctx->wmax_built) return FCG_OK;
+  const std::vector<DressJob>& jobs = ctx->dress_jobs;
+  std::vector<MaxJob> mj(jobs.size());
+  ctx->wmax_index.assign(ctx->w_index.size(), -1);
+  int64_t tot = 0;
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    const DressJob& J = jobs[j];
+    mj[j] = MaxJob{J.w_off, tot, J.rest_len, J.mb, J.mk, 0};
+    tot += int64_t(J.rest_len) * J.mk;
+  }
+  for (size_t i = 0; i < ctx->w_index.size(); ++i) {
+    if (ctx->w_index[i] < 0) continue;
+    // jobs are in w_off order; find the job of this W block
+    auto it = std::lower_bound(jobs.begin(), jobs.end(), ctx->w_index[i],
+                               [](const DressJob& J, int64_t v) { return J.w_off < v; });
+    ctx->wmax_index[i] = mj[it - jobs.begin()].out_off;
+  }
+  MaxJob* d_mj = nullptr;
+  FCG_CUDA(fcg_ctx::stage(ctx->scratch_b, mj.data(), mj.size(), ctx->stream, &d_mj));
+  FCG_CUDA(ctx->d_wmax.alloc(std::max<int64_t>(tot, 1)));
+  if (!jobs.empty()) {
+    colmax_kernel<<<unsigned(jobs.size()), 128, 0, ctx->stream>>>(d_mj, ctx->d_w64.p, ctx->d_wmax.p);
+    FCG_CUDA(cudaGetLastError());
+  }
+  FCG_CUDA(cudaStreamSynchronize(ctx->stream));  // the job list's staging buffer is reused by the next call
+  ctx->wmax_built = true;
   return FCG_OK;
 }
 

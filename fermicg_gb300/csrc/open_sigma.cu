@@ -503,7 +503,7 @@ int fcg_sigma_open(fcg_ctx* ctx, int R, const double* c, double thresh, int nbod
   FCG_REQUIRE(thresh >= 0.0, FCG_EINVAL, "thresh must be >= 0");
   FCG_CUDA(cudaSetDevice(ctx->device));
   {
-    const int rc = ensure_dressed(ctx);
+    const int rc = ensure_wmax(ctx);
     if (rc) return rc;
   }
   *n_out = 0;

@@ -12,6 +12,7 @@
 // 32 of its kets, becomes one lane job of the sigma kernel; lane jobs are
 // sorted so that a warp's 32 lanes do the same kind and amount of work.
 #include <algorithm>
+#include <array>
 #include <cstring>
 #include <unordered_map>
 
@@ -65,7 +66,8 @@ std::string term_lists(const ProblemInfo& pi, TermLists& L) {
   const std::vector<int32_t>& trm = *pi.trm;
   L = TermLists();
   std::unordered_map<uint32_t, int> mask_id;
-  std::vector<std::vector<std::vector<int32_t>>> by(pi.n_trans);
+  // (transfer, set, term) of every term; sets numbered in order of first appearance
+  std::vector<std::array<int32_t, 3>> key(size_t(pi.n_terms));
   for (int t = 0; t < pi.n_terms; ++t) {
     const int nb = TT(trm, t, 0);
     uint32_t m = 0;
@@ -81,18 +83,21 @@ std::string term_lists(const ProblemInfo& pi, TermLists& L) {
     }
     const int tr = TT(trm, t, 1);
     if (tr < 0 || tr >= pi.n_trans) return "term transfer id out of range";
-    if (int(by[tr].size()) <= s) by[tr].resize(s + 1);
-    by[tr][s].push_back(t);
+    key[size_t(t)] = {tr, s, t};
   }
+  std::stable_sort(key.begin(), key.end(), [](const std::array<int32_t, 3>& x, const std::array<int32_t, 3>& y) {
+    return x[0] != y[0] ? x[0] < y[0] : x[1] < y[1];
+  });
   L.first_of_tr.assign(size_t(pi.n_trans) + 1, 0);
   L.off.push_back(0);
+  size_t q = 0;
   for (int tr = 0; tr < pi.n_trans; ++tr) {
     L.first_of_tr[tr] = int32_t(L.tr.size());
-    for (int s = 0; s < int(by[tr].size()); ++s) {
-      if (by[tr][s].empty()) continue;
+    while (q < key.size() && key[q][0] == tr) {
+      const int s = key[q][1];
       L.tr.push_back(tr);
       L.set.push_back(s);
-      L.terms.insert(L.terms.end(), by[tr][s].begin(), by[tr][s].end());
+      for (; q < key.size() && key[q][0] == tr && key[q][1] == s; ++q) L.terms.push_back(key[q][2]);
       L.off.push_back(int32_t(L.terms.size()));
     }
   }
