@@ -7,8 +7,8 @@
 // Radix sort: one pass per 8-bit digit, lowest digit first.  Per pass, every tile of 2048
 // elements counts its digits (hist), the counts are laid out digit-major over tiles and
 // scanned, and the tile scatters its elements to (digit offset of the tile + rank among the
-// tile's elements of that digit).  The rank keeps the input order (rounds of 256 consecutive
-// elements; within a round, warps in order and lanes in order through __match_any_sync), so
+// tile's elements of that digit).  The rank keeps the input order (steps of 256 consecutive
+// elements; within a step, warps in order and lanes in order through __match_any_sync), so
 // every pass is stable and the passes together sort by the whole key, ties in input order.
 // A pass can take its digit from the key or from a per-element value computed from the
 // 32-bit value (the planner's segment of a row), which sorts by a second key without
@@ -96,8 +96,8 @@ cudaError_t exclusive_scan(T* a, int64_t n, T* scratch, cudaStream_t s) {
 
 // ---- radix sort ---------------------------------------------------------------------------
 constexpr int kSortThreads = 256;
-constexpr int kSortRounds = 8;
-constexpr int kSortTile = kSortThreads * kSortRounds;  // elements per tile
+constexpr int kSortSteps = 8;
+constexpr int kSortTile = kSortThreads * kSortSteps;  // elements per tile
 constexpr int kRadix = 256;
 
 // The digit of one pass: bits [shift, shift + 8) of the key (seg_n == 0), or of the segment
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_hist_kernel(const uint64_t
   __syncthreads();
   const int64_t base = int64_t(blockIdx.x) * kSortTile;
 #pragma unroll
-  for (int r = 0; r < kSortRounds; ++r) {
+  for (int r = 0; r < kSortSteps; ++r) {
     const int64_t i = base + r * kSortThreads + tid;
     if (i < n) atomicAdd(&h[dg(keys[i], vals[i])], 1);
   }
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
   __syncthreads();
   const unsigned lt = (1u << lane) - 1u;
   const int64_t base = int64_t(blockIdx.x) * kSortTile;
-  for (int r = 0; r < kSortRounds; ++r) {
+  for (int r = 0; r < kSortSteps; ++r) {
     const int64_t i = base + r * kSortThreads + tid;
     const bool valid = i < n;
     uint64_t k = 0;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kSortThreads) radix_scatter_kernel(
     const int rank = __popc(peers & lt);
     if (valid && rank == 0) s_cnt[warp][d] = __popc(peers);
     __syncthreads();
-    {  // thread tid: the offsets of digit tid for every warp of this round
+    {  // thread tid: the offsets of digit tid for every warp of this step
       int acc = s_run[tid];
 #pragma unroll
       for (int w = 0; w < kWarps; ++w) {
