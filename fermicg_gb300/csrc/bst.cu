@@ -1194,6 +1194,48 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
         }
       }
     }
+    // the transfers with terms whose ket sector exists, once per distinct bra sector (and ket
+    // side): blocks of one Fock sector share them
+    std::unordered_map<uint64_t, int32_t> bra_sec;      // (fock, side) hash -> list
+    std::vector<std::vector<int32_t>> sec_trans;         // list -> transfers
+    std::vector<int64_t> sec_first;                      // list -> its first block
+    std::vector<int> sec_side;                           // list -> ket side
+    std::vector<int32_t> blk_list(size_t(nb), -1);
+    {
+      std::vector<int16_t> fk(2 * N);
+      for (int64_t b = 0; b < nb; ++b) {
+        const int16_t* fb = fock + 2 * N * b;
+        const int kside = split > 0 ? (b < split ? 1 : 0) : 2;
+        const uint64_t key = mix(hash_of(0, fb, (1 << N) - 1), uint64_t(kside));
+        auto it = bra_sec.find(key);
+        if (it != bra_sec.end()) {
+          // equal hashes of different sectors would share a list: check the sector itself
+          const int16_t* f0 = fock + 2 * N * sec_first[size_t(it->second)];
+          if (std::equal(fb, fb + 2 * N, f0) && sec_side[size_t(it->second)] == kside) {
+            blk_list[size_t(b)] = it->second;
+            continue;
+          }
+        }
+        const int32_t id = int32_t(sec_trans.size());
+        if (it == bra_sec.end()) bra_sec.emplace(key, id);
+        sec_first.push_back(b);
+        sec_side.push_back(kside);
+        std::vector<int32_t> trs;
+        for (int tr = 0; tr < ctx->n_trans; ++tr) {
+          if (by_trans[tr].empty()) continue;
+          bool ok = true;
+          for (int c = 0; c < N && ok; ++c)
+            for (int q = 0; q < 2; ++q) {
+              const int v = fb[2 * c + q] - ctx->trans[(int64_t(tr) * N + c) * 2 + q];
+              if (v < 0 || v > ctx->norb[c]) ok = false;
+              fk[2 * c + q] = int16_t(v);
+            }
+          if (ok && sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) trs.push_back(tr);
+        }
+        sec_trans.push_back(std::move(trs));
+        blk_list[size_t(b)] = id;
+      }
+    }
     constexpr int64_t kBrasPerPart = 16;
     const int64_t n_parts = (nb + kBrasPerPart - 1) / kBrasPerPart;
     parts.resize(size_t(n_parts));
@@ -1207,17 +1249,11 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
           const int16_t* fb = fock + 2 * N * b;
           const int kside = split > 0 ? (b < split ? 1 : 0) : 2;  // the other state's blocks only
           std::unordered_map<uint64_t, int32_t> grp;              // (ket, mask) -> group
-          for (int tr = 0; tr < ctx->n_trans && part.err.empty(); ++tr) {
-            if (by_trans[tr].empty()) continue;
-            bool ok = true;
-            for (int c = 0; c < N && ok; ++c)
-              for (int s = 0; s < 2; ++s) {
-                const int v = fb[2 * c + s] - ctx->trans[(int64_t(tr) * N + c) * 2 + s];
-                if (v < 0 || v > ctx->norb[c]) ok = false;
-                fk[2 * c + s] = int16_t(v);
-              }
-            if (!ok) continue;
-            if (!sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) continue;
+          for (const int32_t tr : sec_trans[size_t(blk_list[size_t(b)])]) {
+            if (!part.err.empty()) break;
+            for (int c = 0; c < N; ++c)
+              for (int s = 0; s < 2; ++s)
+                fk[2 * c + s] = int16_t(fb[2 * c + s] - ctx->trans[(int64_t(tr) * N + c) * 2 + s]);
             for (int t : by_trans[tr]) {
               const int32_t* r = &ctx->trm[int64_t(t) * kTrmCols];
               int mask = 0;
