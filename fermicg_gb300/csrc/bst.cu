@@ -1201,40 +1201,52 @@ std::string plan_bst(const fcg_ctx* ctx, int nbody, const std::vector<BstBlock>&
     std::vector<int64_t> sec_first;                      // list -> its first block
     std::vector<int> sec_side;                           // list -> ket side
     std::vector<int32_t> blk_list(size_t(nb), -1);
-    {
-      std::vector<int16_t> fk(2 * N);
-      for (int64_t b = 0; b < nb; ++b) {
-        const int16_t* fb = fock + 2 * N * b;
-        const int kside = split > 0 ? (b < split ? 1 : 0) : 2;
-        const uint64_t key = mix(hash_of(0, fb, (1 << N) - 1), uint64_t(kside));
-        auto it = bra_sec.find(key);
-        if (it != bra_sec.end()) {
-          // equal hashes of different sectors would share a list: check the sector itself
-          const int16_t* f0 = fock + 2 * N * sec_first[size_t(it->second)];
-          if (std::equal(fb, fb + 2 * N, f0) && sec_side[size_t(it->second)] == kside) {
-            blk_list[size_t(b)] = it->second;
-            continue;
+    for (int64_t b = 0; b < nb; ++b) {  // the list of every block (hash lookups only)
+      const int16_t* fb = fock + 2 * N * b;
+      const int kside = split > 0 ? (b < split ? 1 : 0) : 2;
+      const uint64_t key = mix(hash_of(0, fb, (1 << N) - 1), uint64_t(kside));
+      auto it = bra_sec.find(key);
+      if (it != bra_sec.end()) {
+        // equal hashes of different sectors would share a list: check the sector itself
+        const int16_t* f0 = fock + 2 * N * sec_first[size_t(it->second)];
+        if (std::equal(fb, fb + 2 * N, f0) && sec_side[size_t(it->second)] == kside) {
+          blk_list[size_t(b)] = it->second;
+          continue;
+        }
+      }
+      const int32_t id = int32_t(sec_first.size());
+      if (it == bra_sec.end()) bra_sec.emplace(key, id);
+      sec_first.push_back(b);
+      sec_side.push_back(kside);
+      blk_list[size_t(b)] = id;
+    }
+    sec_trans.resize(sec_first.size());
+    {  // the lists themselves on host threads
+      std::atomic<size_t> next_list{0};
+      auto list_worker = [&]() {
+        std::vector<int16_t> fk(2 * N);
+        for (size_t id = next_list.fetch_add(1); id < sec_first.size(); id = next_list.fetch_add(1)) {
+          const int16_t* fb = fock + 2 * N * sec_first[id];
+          std::vector<int32_t>& trs = sec_trans[id];
+          for (int tr = 0; tr < ctx->n_trans; ++tr) {
+            if (by_trans[tr].empty()) continue;
+            bool ok = true;
+            for (int c = 0; c < N && ok; ++c)
+              for (int q = 0; q < 2; ++q) {
+                const int v = fb[2 * c + q] - ctx->trans[(int64_t(tr) * N + c) * 2 + q];
+                if (v < 0 || v > ctx->norb[c]) ok = false;
+                fk[2 * c + q] = int16_t(v);
+              }
+            if (ok && sectors[sec_side[id]].count(hash_of(0, fk.data(), (1 << N) - 1))) trs.push_back(tr);
           }
         }
-        const int32_t id = int32_t(sec_trans.size());
-        if (it == bra_sec.end()) bra_sec.emplace(key, id);
-        sec_first.push_back(b);
-        sec_side.push_back(kside);
-        std::vector<int32_t> trs;
-        for (int tr = 0; tr < ctx->n_trans; ++tr) {
-          if (by_trans[tr].empty()) continue;
-          bool ok = true;
-          for (int c = 0; c < N && ok; ++c)
-            for (int q = 0; q < 2; ++q) {
-              const int v = fb[2 * c + q] - ctx->trans[(int64_t(tr) * N + c) * 2 + q];
-              if (v < 0 || v > ctx->norb[c]) ok = false;
-              fk[2 * c + q] = int16_t(v);
-            }
-          if (ok && sectors[kside].count(hash_of(0, fk.data(), (1 << N) - 1))) trs.push_back(tr);
-        }
-        sec_trans.push_back(std::move(trs));
-        blk_list[size_t(b)] = id;
-      }
+      };
+      const int n_list_threads = int(std::max<size_t>(1, std::min<size_t>(
+          {size_t(std::max(1u, std::thread::hardware_concurrency())), size_t(32), sec_first.size()})));
+      std::vector<std::thread> lpool;
+      for (int i = 1; i < n_list_threads; ++i) lpool.emplace_back(list_worker);
+      list_worker();
+      for (auto& th : lpool) th.join();
     }
     constexpr int64_t kBrasPerPart = 16;
     const int64_t n_parts = (nb + kBrasPerPart - 1) / kBrasPerPart;
