@@ -334,11 +334,16 @@ class FlatTPSCI:
         """new rows (configurations not present), in the given order"""
         if len(sec) == 0:
             return
-        u, first = np.unique(sec, return_index=True)
-        for sid in u[np.argsort(first, kind="stable")].tolist():  # sectors that (re)appear, in first-row order
-            if sid not in self.rank:
-                self.rank[sid] = self.next_rank
-                self.next_rank += 1
+        # sectors that (re)appear get ranks in first-row order; sector ids are small, so the
+        # present ones come from a count, and the first rows are only sought for new ones
+        present = np.flatnonzero(np.bincount(sec))
+        new = [sid for sid in present.tolist() if sid not in self.rank]
+        if new:
+            u, first = np.unique(sec, return_index=True)
+            for sid in u[np.argsort(first, kind="stable")].tolist():
+                if sid not in self.rank:
+                    self.rank[sid] = self.next_rank
+                    self.next_rank += 1
         n = len(sec)
         self._canon = False  # new rows go to the end physically; row order is restored on demand
         self.sec = np.concatenate([self.sec, sec])
@@ -354,7 +359,7 @@ class FlatTPSCI:
         self.sec, self.cfg, self.coef, self.ins = self.sec[mask], self.cfg[mask], self.coef[mask], self.ins[mask]
         self._key = None if self._key is None else self._key[mask]
         self._ks = None
-        live = set(np.unique(self.sec).tolist())
+        live = set(np.flatnonzero(np.bincount(self.sec)).tolist()) if len(self.sec) else set()
         self.rank = {s: r for s, r in self.rank.items() if s in live}
 
     def _find(self, keys):
